@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark: Metropolis MC trial moves/s of the bulk-salt Ewald system.
+
+Workload (one step): R independent replica chains of the 20,000-ion bulk
+salt system (0.1 M, LJ + Coulomb, real-space erfc cutoff 12 A, alpha 0.3/A,
+ncutoff 8 -> 1152 k-vectors, 45^3 cells, atomic translation moves), each
+advanced by M trial moves in one persistent chain-kernel launch.
+
+  value   device-timed moves/s with all state resident in HBM, proposals
+          from the on-device counter RNG (fau_run_batch).
+  e2e     the same moves through the drop-in C ABI (fau_run_proposals_batch):
+          proposals drawn on the host in the reference's mt19937 order, copied
+          host->device from pinned memory, accept flags + dU copied back, all
+          inside the timed region.
+  --impl reference
+          the CPU oracle (the reference algorithm restated: all-pairs
+          Nonbonded, O(K) Ewald per state, two-state sync) on all host
+          threads, one chain per thread, bounded sample per step.
+
+Multi-GPU: replicas only (one process per GPU, each with its own R replicas,
+no collective on the data path); timing is max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# algorithmic work per unit (flops; add/mul/compare = 1, FMA = 2)
+FLOPS_PER_K_UPDATE = 26.0    # per k-vector per moved atom: 2 phases (12), dQ (8), dU_rec share (6)
+FLOPS_PER_PAIR = 38.0        # per pair interaction (LJ + Ewald real space)
+BYTES_PER_PAIR_CANDIDATE = 16.0
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"fau_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist_init(n_gpus):
+    rank, local, world = _env_rank()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return dist, rank, local, world
+    return None, 0, 0, 1
+
+
+def _max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _sum_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _profile_traffic():
+    """DRAM bytes per move of the chain kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "chain_kernel_bulk_ewald.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["dram_bytes_per_move"]), d.get("source", str(p.name))
+        except (ValueError, KeyError):
+            pass
+    return None, None
+
+
+def cpu_baseline(spec, seconds_per_thread: float = 1.0, threads: int | None = None) -> dict:
+    """The oracle (reference algorithm restated in C++) on the host cores:
+    one chain per thread, a bounded number of moves per chain."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import ctypes as C
+
+    import oracle_lib as O
+    from faunus_gb300.system import move_descs
+
+    threads = threads or os.cpu_count() or 1
+    d, keep = spec.to_desc()
+    arr, keep2 = move_descs(spec, spec.extra["moves"])
+    L = O.lib()
+    mps, wall = C.c_double(), C.c_double()
+    # calibrate on one chain, then size the sample to ~seconds_per_thread per thread
+    rc = L.orc_bench_chains(C.byref(d), arr, 1, 1, 1, 20, C.byref(mps), C.byref(wall))
+    if rc != 0:
+        raise RuntimeError(f"oracle bench failed: {rc}")
+    per_move = wall.value / 20
+    m = max(20, int(seconds_per_thread / max(per_move, 1e-9)))
+    rc = L.orc_bench_chains(C.byref(d), arr, 1, threads, threads, m, C.byref(mps), C.byref(wall))
+    if rc != 0:
+        raise RuntimeError(f"oracle bench failed: {rc}")
+    return {"value": mps.value, "unit": "moves/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} chains x {m} moves of the 20,000-ion bulk Ewald system, one chain per thread "
+                      f"({wall.value:.1f} s wall)", "wall_s": wall.value, "moves_per_chain": m}
+
+
+def run_reference(args) -> None:
+    dist, rank, local, world = _dist_init(args.gpus)
+    if rank != 0:
+        _barrier(dist)
+        return
+    from faunus_gb300 import configs
+    spec = configs.bulk_ewald(n_salt=10000, seed=1)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(spec, seconds_per_thread=0.2, threads=threads)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(spec, seconds_per_thread=0.5, threads=threads))
+    wall = time.perf_counter() - t0
+    total_moves = sum(v["value"] * v["wall_s"] for v in vals)
+    tot_wall = sum(v["wall_s"] for v in vals)
+    value = total_moves / tot_wall
+    line = {
+        "impl": "reference", "metric": "MC trial moves/sec", "value": value, "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot_wall / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": "bulk-salt Ewald, 20,000 ions, one chain per host thread", "n_particles": 20000,
+                   "kvectors": 1152, "parallelism": f"{threads} host threads"},
+        "cpu_baseline": {"value": value, "unit": "moves/s", "cores": threads, "kind": "port",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    _barrier(dist)
+
+
+def run_ours(args) -> None:
+    dist, rank, local, world = _dist_init(args.gpus)
+    import faunus_gb300 as F
+    from faunus_gb300 import _capi as A
+    from faunus_gb300 import configs
+
+    ctx = F.Context(local)
+    base = configs.bulk_ewald(n_salt=10000, seed=1)
+    sms = _sm_count(local)
+    R = args.replicas or 2 * sms
+    M = args.moves
+    systems = [ctx.create(base) for _ in range(R)]
+    streams = np.arange(R, dtype=np.uint32) + 1_000_000 * rank
+    resident = ctx.hbm_used()
+
+    # ---- value: device RNG, resident state
+    def step(k):
+        return ctx.run_batch(systems, M, seed=args.seed, counter_base=k * M, streams=streams, dp=2.0,
+                             threads=args.threads)
+
+    for w in range(args.warmup):
+        step(w)
+    clocks = Clocks(local)
+    clocks.start()
+    _barrier(dist)
+    t0 = time.perf_counter()
+    stats = [step(args.warmup + k) for k in range(args.steps)]
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = sum(s["device_ms"] for s in stats)
+    dev_s = _max_over_ranks(dist, dev_ms * 1e-3)
+    moves = sum(s["moves"] for s in stats)
+    pairs = sum(s["pair_evals"] for s in stats)
+    kup = sum(s["k_updates"] for s in stats)
+    acc = sum(s["accepted"] for s in stats)
+    tot_moves = _sum_over_ranks(dist, moves)
+    value = tot_moves / dev_s
+
+    # ---- e2e: reference-stream proposals through the C ABI, host buffers
+    gens = [F.MoveGenerator(base, base.extra["moves"], 7 + i, 11 + i, default_seeds=False) for i in range(R)]
+    offsets = np.arange(R + 1, dtype=np.int64) * M
+    props_buf, acc_buf, du_buf = _pinned(R * M)
+
+    def fill():
+        def one(i):
+            props_buf[i * M:(i + 1) * M] = gens[i].generate(M)
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            list(ex.map(one, range(R)))
+
+    e2e_systems = systems
+    for _ in range(max(1, args.warmup // 2)):
+        fill()
+        ctx.run_proposals_batch(e2e_systems, props_buf, offsets, acc_buf, du_buf)
+    e2e_s = 0.0
+    e2e_moves = 0
+    for _ in range(args.steps):
+        fill()  # the step's inputs (drawn by the caller's Move code), outside the timed region
+        _barrier(dist)
+        t1 = time.perf_counter()
+        st = ctx.run_proposals_batch(e2e_systems, props_buf, offsets, acc_buf, du_buf)
+        e2e_s += time.perf_counter() - t1
+        e2e_moves += st["moves"]
+    e2e_s = _max_over_ranks(dist, e2e_s)
+    e2e_value = _sum_over_ranks(dist, e2e_moves) / e2e_s
+
+    # ---- roofline of the chain kernel (FP32 pipe)
+    peak = ctx.fp32_peak_tflops()
+    flops = FLOPS_PER_K_UPDATE * kup + FLOPS_PER_PAIR * pairs
+    achieved = flops / (dev_ms * 1e-3) / 1e12
+    bytes_per_move, src = _profile_traffic()
+    traffic = bytes_per_move * (moves / args.steps) if bytes_per_move else None
+
+    line = {
+        "metric": "MC trial moves/sec", "value": value, "unit": "moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic",
+        "config": {"workload": "bulk-salt Ewald (20,000 LJ+Coulomb ions, 0.1 M, erfc Rc 12 A, alpha 0.3, "
+                               "ncutoff 8, 45^3 cells, transrot dp 2 A) x R replica chains",
+                   "replicas_per_gpu": R, "moves_per_replica_per_step": M, "n_particles": base.n,
+                   "kvectors": systems[0].K, "cells": "x".join(map(str, systems[0].cell_grid())),
+                   "threads_per_chain": args.threads or 256,
+                   "l2": f"inputs larger than L2: {resident / 2**30:.1f} GiB resident per GPU",
+                   "parallelism": f"replicas (dp{world})", "rng": "Philox4x32-10 on device (value); "
+                   "reference mt19937 stream on host (e2e)"},
+        "pair_interactions_per_s": _sum_over_ranks(dist, pairs) / dev_s,
+        "k_updates_per_s": _sum_over_ranks(dist, kup) / dev_s,
+        "acceptance": acc / max(moves, 1),
+        "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": int(R * M * 72 + 8 * (R + 1)),
+                "d2h_bytes_per_step": int(R * M * 9)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": "measured FP32 FMA probe (fau_measure_fp32_peak) in this run",
+                     "work": f"{FLOPS_PER_K_UPDATE:g} flop per k-vector x moved atom + {FLOPS_PER_PAIR:g} per pair",
+                     "traffic_source": src},
+        "clocks": clk,
+        "gpu_launches": 3 * args.steps,
+        "wall_s": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(base)
+        line["cpu_baseline"].pop("wall_s", None)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for s in systems:
+        s.close()
+    ctx.close()
+    _barrier(dist)
+
+
+def _sm_count(dev: int) -> int:
+    try:
+        import torch
+        return torch.cuda.get_device_properties(dev).multi_processor_count
+    except Exception:
+        return 152
+
+
+def _pinned(n):
+    """Pinned host buffers for the e2e proposals and results."""
+    from faunus_gb300 import _capi as A
+    try:
+        import torch
+        p = torch.empty(n * A.PROPOSAL_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy()
+        a = torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
+        d = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        return p.view(A.PROPOSAL_DTYPE), a, d
+    except Exception:
+        return np.zeros(n, dtype=A.PROPOSAL_DTYPE), np.zeros(n, np.uint8), np.zeros(n)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--replicas", type=int, default=0, help="replica chains per GPU (0: 2 x SMs)")
+    ap.add_argument("--moves", type=int, default=2000, help="moves per replica per step")
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=12345)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,12 @@
+"""GB300-native Metropolis Monte Carlo energy hot path (Faunus drop-in).
+
+The compute path is ``libfau_gpu.so`` (hand-written sm_103a CUDA behind the
+C ABI of ``include/fau_gpu.h``); this package is its Python host API.
+"""
+from . import _capi
+from ._capi import FauError
+from .system import (Context, MoveGenerator, System, SystemSpec, bjerrum_length, footprint,
+                     kjmol_to_kt, move_descs)
+
+__all__ = ["Context", "System", "SystemSpec", "MoveGenerator", "FauError", "bjerrum_length",
+           "kjmol_to_kt", "footprint", "move_descs", "_capi"]

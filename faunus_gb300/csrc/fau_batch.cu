@@ -1,0 +1,403 @@
+// fau_batch.cu -- many independent systems (replicas, parallel-tempering
+// walkers, served jobs) advanced by one chain-kernel launch per block of
+// moves, with device-side parallel-tempering swaps between blocks; the whole
+// sequence is captured once into a CUDA graph and replayed.
+//
+// Parallel tempering follows the semantics of ParallelTempering
+// (src/move.cpp:844-970): odd/even partner pairs (OddEvenPartner::generate,
+// src/mpicontroller.cpp:69-83), acceptance on the sum of each walker's energy
+// change in its own kT.  Exchanging configurations between two temperatures is
+// done by exchanging the temperatures (the beta multiplier of each system).
+#include "fau_dev.cuh"
+#include "fau_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace fau;
+
+// opaque handle layouts shared with fau_capi.cu
+struct fau_ctx;
+extern "C" int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device);
+extern "C" int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n, int* n_groups,
+                                     int* molecular_only, double* t_ref);
+extern "C" int fau_internal_fail(int code, const char* msg);
+
+namespace {
+
+// per-system summary gathered after a run
+struct SysSummary {
+    unsigned long long moves, accepted, pair_evals, k_updates;
+    double energy, beta_scale;
+    int err, pad;
+};
+
+__global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DevSys& S = *sys[i];
+        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.energy, S.beta_scale, S.err, 0};
+    }
+}
+
+// One parallel-tempering exchange step over the temperature ladder.
+// slot_sys[s]: system holding temperature slot s; T[s]: slot temperatures;
+// Tref[i]: temperature system i's parameters were built for (its kT unit).
+// Energies are converted to absolute units (kT_ref * T_ref) and pairs
+// (s, s+1) with s = parity, parity + 2, ... are exchanged with probability
+// min(1, exp[(1/T_s - 1/T_{s+1}) (E_a - E_b)]).
+__global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const double* T, const double* Tref,
+                               uint64_t seed, unsigned long long round, unsigned long long* stats)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    const U4 r0 = philox({(uint32_t)round, (uint32_t)(round >> 32), 0xFFFFFFFFu, 7u}, k0, k1);
+    const int parity = r0.x & 1;
+    for (int s = parity; s + 1 < n; s += 2) {
+        const int a = slot_sys[s], b = slot_sys[s + 1];
+        const double Ea = sys[a]->energy * Tref[a];
+        const double Eb = sys[b]->energy * Tref[b];
+        const double x = (1.0 / T[s] - 1.0 / T[s + 1]) * (Ea - Eb);
+        const U4 r = philox({(uint32_t)round, (uint32_t)(round >> 32), (uint32_t)s, 8u}, k0, k1);
+        const double u = u01_53(r.x, r.y);
+        stats[0]++;
+        bool acc = false;
+        if (x >= 0.0) acc = true;
+        else if (isfinite(x)) acc = u < exp(x);
+        if (acc) {
+            stats[1]++;
+            slot_sys[s] = b;
+            slot_sys[s + 1] = a;
+            sys[a]->beta_scale = Tref[a] / T[s + 1];
+            sys[b]->beta_scale = Tref[b] / T[s];
+        }
+    }
+}
+
+// each parallel-tempering run starts with every system at its own temperature
+__global__ void reset_beta_kernel(DevSys* const* sys, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) sys[i]->beta_scale = 1.0;
+}
+
+} // namespace
+
+extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* P,
+                             fau_batch_stats* stats)
+{
+    if (!ctx || !systems || !P || n < 1) return fau_internal_fail(FAU_ERR_ARG, "invalid batch arguments");
+    cudaStream_t st;
+    int device;
+    fau_internal_ctx_stream(ctx, &st, &device);
+    if (cudaSetDevice(device) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "cudaSetDevice failed");
+    const bool pt = P->swap_interval_moves > 0 && P->n_swap_blocks > 0;
+    if (pt && !P->temperatures) return fau_internal_fail(FAU_ERR_ARG, "parallel tempering needs temperatures");
+    if (!(P->dp >= 0.0)) return fau_internal_fail(FAU_ERR_ARG, "dp must be >= 0");
+
+    std::vector<DevSys*> dsys(n);
+    std::vector<long long> nm(n);
+    std::vector<uint32_t> ids(n);
+    std::vector<uint8_t> mol(n);
+    std::vector<double> tref(n, 1.0);
+    int Kmax = 0;
+    for (int i = 0; i < n; i++) {
+        fau_ctx* c2;
+        int K, np, ng, mo;
+        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tref[i]);
+        if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
+        Kmax = std::max(Kmax, K);
+        nm[i] = P->moves_per_system ? P->moves_per_system[i] : P->moves;
+        if (nm[i] < 0) return fau_internal_fail(FAU_ERR_ARG, "negative move count");
+        ids[i] = P->streams ? P->streams[i] : (uint32_t)i;
+        mol[i] = (uint8_t)mo;
+        if (pt) tref[i] = P->temperatures[i];
+    }
+    if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
+
+    // device argument arrays (one allocation, freed at the end of the call)
+    const size_t off_sys = 0, off_nm = off_sys + sizeof(DevSys*) * n, off_ids = off_nm + 8 * n,
+                 off_mol = off_ids + 4 * n, off_slot = (off_mol + n + 15) & ~size_t(15), off_T = off_slot + 4 * n,
+                 off_Tref = off_T + 8 * n, off_sum = off_Tref + 8 * n,
+                 off_st = off_sum + sizeof(SysSummary) * n, off_ctr = off_st + 64, total = off_ctr + 8 * n;
+    unsigned char* dbuf = nullptr;
+    if (cudaMalloc(&dbuf, total) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
+    std::vector<int> slot(n);
+    for (int i = 0; i < n; i++) slot[i] = i;
+    int rc = FAU_OK;
+    auto cleanup = [&]() { cudaFree(dbuf); };
+#define BTRY(x)                                                                 \
+    do {                                                                        \
+        if ((x) != cudaSuccess) {                                               \
+            cleanup();                                                          \
+            return fau_internal_fail(FAU_ERR_CUDA, "batch: " #x " failed");      \
+        }                                                                       \
+    } while (0)
+    BTRY(cudaMemcpyAsync(dbuf + off_sys, dsys.data(), sizeof(DevSys*) * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_ids, ids.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_mol, mol.data(), n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_slot, slot.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemsetAsync(dbuf + off_st, 0, 64, st));
+    if (pt) {
+        BTRY(cudaMemcpyAsync(dbuf + off_T, P->temperatures, 8 * n, cudaMemcpyHostToDevice, st));
+        BTRY(cudaMemcpyAsync(dbuf + off_Tref, tref.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    }
+    DevSys* const* d_sys = reinterpret_cast<DevSys* const*>(dbuf + off_sys);
+    SysSummary* d_sum = reinterpret_cast<SysSummary*>(dbuf + off_sum);
+
+    if (pt) reset_beta_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n);
+    // baseline counters
+    std::vector<SysSummary> s0(n), s1(n);
+    gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
+    BTRY(cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st));
+
+    ChainArgs a{};
+    a.sys = d_sys;
+    a.sys_ids = reinterpret_cast<const uint32_t*>(dbuf + off_ids);
+    a.seed = P->seed;
+    a.dp = P->dp;
+    a.dprot = P->dprot;
+    a.molecular = reinterpret_cast<const uint8_t*>(dbuf + off_mol);
+    if (P->counters) {
+        BTRY(cudaMemcpyAsync(dbuf + off_ctr, P->counters, 8 * n, cudaMemcpyHostToDevice, st));
+        a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_ctr);
+    }
+    const int threads = P->threads > 0 ? P->threads : 256;
+    const int nblk = pt ? P->n_swap_blocks : 1;
+    if (pt) {
+        a.n_moves = nullptr;
+        a.moves = P->swap_interval_moves;
+    }
+    else {
+        BTRY(cudaMemcpyAsync(dbuf + off_nm, nm.data(), 8 * n, cudaMemcpyHostToDevice, st));
+        a.n_moves = reinterpret_cast<const long long*>(dbuf + off_nm);
+    }
+    // set the kernel's shared-memory attribute before the capture starts
+    BTRY(prepare_chain(Kmax, threads, true));
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BTRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int b = 0; b < nblk; b++) {
+        a.counter_base = P->counter_base + (unsigned long long)b * (pt ? (unsigned long long)P->swap_interval_moves : 0ull);
+        if (launch_chain(a, n, Kmax, threads, true, st) != cudaSuccess) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cleanup();
+            return fau_internal_fail(FAU_ERR_CUDA, "chain launch failed during capture");
+        }
+        if (pt)
+            pt_swap_kernel<<<1, 1, 0, st>>>(d_sys, n, reinterpret_cast<int*>(dbuf + off_slot),
+                                            reinterpret_cast<const double*>(dbuf + off_T),
+                                            reinterpret_cast<const double*>(dbuf + off_Tref), P->seed ^ 0x5DEECE66DULL,
+                                            P->counter_base / (P->swap_interval_moves ? P->swap_interval_moves : 1) + b,
+                                            reinterpret_cast<unsigned long long*>(dbuf + off_st));
+    }
+    BTRY(cudaStreamEndCapture(st, &graph));
+    BTRY(cudaGraphInstantiate(&exec, graph, 0));
+    BTRY(cudaEventRecord(e0, st));
+    BTRY(cudaGraphLaunch(exec, st));
+    BTRY(cudaEventRecord(e1, st));
+    gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
+    unsigned long long pst[8] = {0};
+    BTRY(cudaMemcpyAsync(s1.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st));
+    BTRY(cudaMemcpyAsync(pst, dbuf + off_st, 64, cudaMemcpyDeviceToHost, st));
+    const cudaError_t se = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (se != cudaSuccess) {
+        cleanup();
+        return fau_internal_fail(FAU_ERR_CUDA, cudaGetErrorString(se));
+    }
+    fau_batch_stats S{};
+    int derr = FAU_OK;
+    for (int i = 0; i < n; i++) {
+        S.moves += (int64_t)(s1[i].moves - s0[i].moves);
+        S.accepted += (int64_t)(s1[i].accepted - s0[i].accepted);
+        S.pair_evals += (int64_t)(s1[i].pair_evals - s0[i].pair_evals);
+        S.k_updates += (int64_t)(s1[i].k_updates - s0[i].k_updates);
+        if (s1[i].err != FAU_OK && derr == FAU_OK) derr = s1[i].err;
+    }
+    S.swaps_attempted = (int64_t)pst[0];
+    S.swaps_accepted = (int64_t)pst[1];
+    S.device_ms = ms;
+    if (stats) *stats = S;
+    cleanup();
+#undef BTRY
+    if (derr != FAU_OK) {
+        // clear the device error flags so the systems stay usable
+        for (int i = 0; i < n; i++) cudaMemsetAsync(&dsys[i]->err, 0, sizeof(int), st);
+        cudaStreamSynchronize(st);
+        return fau_internal_fail(derr, "a system in the batch reported a device error");
+    }
+    return rc;
+}
+
+extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_proposal* props,
+                                       const int64_t* offsets, uint8_t* acc_out, double* du_out,
+                                       fau_batch_stats* stats)
+{
+    if (!ctx || !systems || !props || !offsets || n < 1)
+        return fau_internal_fail(FAU_ERR_ARG, "invalid batch arguments");
+    cudaStream_t st;
+    int device;
+    fau_internal_ctx_stream(ctx, &st, &device);
+    if (cudaSetDevice(device) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "cudaSetDevice failed");
+    std::vector<DevSys*> dsys(n);
+    std::vector<long long> nm(n), off(n);
+    int Kmax = 0;
+    const long long total = offsets[n];
+    if (offsets[0] != 0 || total < 0) return fau_internal_fail(FAU_ERR_ARG, "offsets must start at 0");
+    for (int i = 0; i < n; i++) {
+        fau_ctx* c2;
+        int K, np, ng, mo;
+        double tr;
+        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tr);
+        if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
+        if (offsets[i + 1] < offsets[i]) return fau_internal_fail(FAU_ERR_ARG, "offsets not sorted");
+        nm[i] = offsets[i + 1] - offsets[i];
+        off[i] = offsets[i];
+        Kmax = std::max(Kmax, K);
+        for (long long m = offsets[i]; m < offsets[i + 1]; m++) {
+            const fau_proposal& p = props[m];
+            if (p.kind == FAU_MOVE_ATOMIC) {
+                if (p.index < 0 || p.index >= np) return fau_internal_fail(FAU_ERR_ARG, "particle out of range");
+            }
+            else if (p.kind == FAU_MOVE_MOLECULAR) {
+                if (p.index < 0 || p.index >= ng) return fau_internal_fail(FAU_ERR_ARG, "group out of range");
+            }
+            else if (p.kind != FAU_MOVE_NONE) {
+                return fau_internal_fail(FAU_ERR_ARG, "unknown proposal kind");
+            }
+        }
+    }
+    if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
+    const size_t o_sys = 0, o_nm = o_sys + 8 * n, o_off = o_nm + 8 * n, o_sum = o_off + 8 * n,
+                 o_props = (o_sum + sizeof(SysSummary) * n + 255) & ~size_t(255),
+                 o_acc = o_props + sizeof(fau_proposal) * total, o_du = (o_acc + total + 255) & ~size_t(255),
+                 bytes = o_du + 8 * total;
+    unsigned char* dbuf = nullptr;
+    if (cudaMalloc(&dbuf, bytes) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch staging allocation");
+    auto done = [&](int code, const char* msg) {
+        cudaFree(dbuf);
+        return code == FAU_OK ? FAU_OK : fau_internal_fail(code, msg);
+    };
+    DevSys* const* d_sys = reinterpret_cast<DevSys* const*>(dbuf + o_sys);
+    SysSummary* d_sum = reinterpret_cast<SysSummary*>(dbuf + o_sum);
+    std::vector<SysSummary> s0(n), s1(n);
+    if (cudaMemcpyAsync(dbuf + o_sys, dsys.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_nm, nm.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_off, off.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_props, props, sizeof(fau_proposal) * total, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+        return done(FAU_ERR_CUDA, "proposal upload failed");
+    gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
+    cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st);
+    ChainArgs a{};
+    a.sys = d_sys;
+    a.n_moves = reinterpret_cast<const long long*>(dbuf + o_nm);
+    a.prop_off = reinterpret_cast<const long long*>(dbuf + o_off);
+    a.props = reinterpret_cast<const fau_proposal*>(dbuf + o_props);
+    a.acc_out = acc_out ? reinterpret_cast<uint8_t*>(dbuf + o_acc) : nullptr;
+    a.du_out = du_out ? reinterpret_cast<double*>(dbuf + o_du) : nullptr;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    if (launch_chain(a, n, Kmax, 256, false, st) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return done(FAU_ERR_CUDA, "chain launch failed");
+    }
+    cudaEventRecord(e1, st);
+    gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
+    cudaMemcpyAsync(s1.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st);
+    if (acc_out) cudaMemcpyAsync(acc_out, dbuf + o_acc, total, cudaMemcpyDeviceToHost, st);
+    if (du_out) cudaMemcpyAsync(du_out, dbuf + o_du, 8 * total, cudaMemcpyDeviceToHost, st);
+    const cudaError_t se = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (se != cudaSuccess) return done(FAU_ERR_CUDA, cudaGetErrorString(se));
+    fau_batch_stats S{};
+    int derr = FAU_OK;
+    for (int i = 0; i < n; i++) {
+        S.moves += (int64_t)(s1[i].moves - s0[i].moves);
+        S.accepted += (int64_t)(s1[i].accepted - s0[i].accepted);
+        S.pair_evals += (int64_t)(s1[i].pair_evals - s0[i].pair_evals);
+        S.k_updates += (int64_t)(s1[i].k_updates - s0[i].k_updates);
+        if (s1[i].err != FAU_OK && derr == FAU_OK) derr = s1[i].err;
+    }
+    S.device_ms = ms;
+    if (stats) *stats = S;
+    if (derr != FAU_OK) {
+        for (int i = 0; i < n; i++) cudaMemsetAsync(&dsys[i]->err, 0, sizeof(int), st);
+        cudaStreamSynchronize(st);
+        return done(derr, "a system in the batch reported a device error");
+    }
+    return done(FAU_OK, nullptr);
+}
+
+// ---------------------------------------------------------------- FP32 peak probe
+namespace {
+__global__ void fma_probe_kernel(float* out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+    float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 12345.678f) out[0] = s; // keeps the chains live
+}
+} // namespace
+
+extern "C" int fau_measure_fp32_peak(fau_ctx* ctx, double* tflops)
+{
+    if (!ctx || !tflops) return fau_internal_fail(FAU_ERR_ARG, "null argument");
+    cudaStream_t st;
+    int device;
+    fau_internal_ctx_stream(ctx, &st, &device);
+    cudaSetDevice(device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "probe allocation");
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fma_probe_kernel<<<blocks, threads, 0, st>>>(d, 64, 0.999999f, 1e-7f); // warm up
+    double best = 0.0;
+    for (int r = 0; r < 5; r++) {
+        cudaEventRecord(e0, st);
+        fma_probe_kernel<<<blocks, threads, 0, st>>>(d, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+        best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    const cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, cudaGetErrorString(e));
+    *tflops = best;
+    return FAU_OK;
+}

@@ -1,0 +1,1186 @@
+// fau_capi.cu -- host runtime behind the C ABI (include/fau_gpu.h).
+//
+// Owns device memory per system, builds the device tables (internal
+// (type, charge) classes, pair matrices, Ewald k-vectors, cell list) and
+// drives the kernels of fau_kernels.cu on the context's stream.
+#include "fau_dev.cuh"
+#include "fau_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+using namespace fau;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                                        \
+    do {                                                                                                      \
+        cudaError_t e_ = (expr);                                                                              \
+        if (e_ != cudaSuccess) return fail(e_ == cudaErrorMemoryAllocation ? FAU_ERR_OOM : FAU_ERR_CUDA,      \
+                                           "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// ---------------------------------------------------------------- handles
+struct fau_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0, used = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // scratch for batched launches (grown on demand)
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    std::mutex mu;
+};
+
+struct fau_sys {
+    fau_ctx* ctx = nullptr;
+    DevSys h{};                 // host mirror of the device struct (pointers are device pointers)
+    DevSys* d = nullptr;        // device copy
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    int n = 0, n_groups = 0, K = 0;
+    bool cells = false, molecular_only = false;
+    std::vector<int> g_begin, g_flags, group_of;
+    int max_group = 0;
+    int precision = FAU_PREC_FP32C;
+    // staging for run_proposals
+    fau_proposal* d_props = nullptr;
+    uint8_t* d_acc = nullptr;
+    double* d_du = nullptr;
+    fau_trial_result* d_detail = nullptr;
+    size_t stage_cap = 0;
+    PlainMove* d_plain = nullptr;
+    double2* d_dq = nullptr;
+    double* d_res = nullptr;
+    int* d_flags = nullptr;
+    DevSys** d_self = nullptr; // device array holding `d` (chain kernel argument)
+};
+
+template <class T>
+static int dev_alloc(fau_sys* s, T** p, size_t count)
+{
+    const size_t b = std::max<size_t>(count, 1) * sizeof(T);
+    if (s->ctx->budget && s->ctx->used + b > s->ctx->budget)
+        return fail(FAU_ERR_OOM, "HBM budget exceeded (%zu + %zu > %zu bytes)", s->ctx->used, b, s->ctx->budget);
+    void* v = nullptr;
+    CUDA_TRY(cudaMalloc(&v, b));
+    s->allocs.push_back(v);
+    s->bytes += b;
+    s->ctx->used += b;
+    *p = static_cast<T*>(v);
+    return FAU_OK;
+}
+template <class T>
+static int upload(fau_sys* s, T** p, const T* src, size_t count)
+{
+    int rc = dev_alloc(s, p, count);
+    if (rc) return rc;
+    if (count) CUDA_TRY(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, s->ctx->stream));
+    return FAU_OK;
+}
+
+static void free_sys(fau_sys* s)
+{
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->ctx) s->ctx->used -= std::min(s->ctx->used, s->bytes);
+    s->allocs.clear();
+    s->bytes = 0;
+}
+
+// ---------------------------------------------------------------- setup helpers
+namespace {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr double kTwo32 = 4294967296.0;
+
+struct EwaldTable {
+    std::vector<int> kn;
+    std::vector<double> Ak;
+};
+
+// PolicyIonIon::updateBox (src/energy.cpp:133-186): nx in [0, nc], ny, nz in
+// [-nc, nc], skip k^2 < 0.1 (2 pi / L_max)^2, spherical cut n^2 <= nc^2,
+// A_k = f exp(-k^2 / 4 alpha^2) / k^2 with f = 2 for nx > 0 (kappa = 0).
+EwaldTable build_kvectors(const double L[3], double alpha, double ncut, bool spherical)
+{
+    EwaldTable t;
+    const int nc = (int)std::ceil(ncut);
+    const double Lmax = std::max(L[0], std::max(L[1], L[2]));
+    const double check_k2_zero = 0.1 * std::pow(2 * kPi / Lmax, 2);
+    if ((2 * nc + 1) * (2 * nc + 1) * (2 * nc + 1) - 1 == 0) return t;
+    const double nc2 = ncut * ncut;
+    for (int nx = 0; nx <= nc; nx++) {
+        const double dnx2 = double(nx * nx);
+        const double factor = nx > 0 ? 2.0 : 1.0;
+        for (int ny = -nc; ny <= nc; ny++) {
+            const double dny2 = double(ny * ny);
+            for (int nz = -nc; nz <= nc; nz++) {
+                const double kx = 2 * kPi * (double(nx) / L[0]);
+                const double ky = 2 * kPi * (double(ny) / L[1]);
+                const double kz = 2 * kPi * (double(nz) / L[2]);
+                const double k2 = (kx * kx + ky * ky) + kz * kz;
+                if (k2 < check_k2_zero) continue;
+                if (spherical && (dnx2 + dny2 + double(nz * nz)) / nc2 > 1) continue;
+                t.kn.push_back((nx + 128) | ((ny + 128) << 8) | ((nz + 128) << 16));
+                t.Ak.push_back(factor * std::exp(-k2 / (4 * alpha * alpha)) / k2);
+            }
+        }
+    }
+    return t;
+}
+
+int validate(const fau_sys_desc* d)
+{
+    if (!d) return fail(FAU_ERR_ARG, "null descriptor");
+    if (d->n_particles < 1 || d->n_particles > (1 << 24) - 1)
+        return fail(FAU_ERR_ARG, "n_particles %d outside [1, 2^24)", d->n_particles);
+    if (!d->pos || !d->charge || !d->type) return fail(FAU_ERR_ARG, "pos, charge and type are required");
+    if (d->n_groups < 1 || !d->group_begin) return fail(FAU_ERR_ARG, "at least one group is required");
+    if (d->group_begin[0] != 0 || d->group_begin[d->n_groups] != d->n_particles)
+        return fail(FAU_ERR_ARG, "group_begin must start at 0 and end at n_particles");
+    for (int g = 0; g < d->n_groups; g++)
+        if (d->group_begin[g + 1] < d->group_begin[g]) return fail(FAU_ERR_ARG, "group_begin not sorted");
+    for (int k = 0; k < 3; k++)
+        if (!(d->box[k] > 0.0)) return fail(FAU_ERR_ARG, "box lengths must be positive");
+    if (d->n_types < 1) return fail(FAU_ERR_ARG, "n_types must be >= 1");
+    for (int i = 0; i < d->n_particles; i++) {
+        if (d->type[i] < 0 || d->type[i] >= d->n_types) return fail(FAU_ERR_ARG, "particle %d: type out of range", i);
+        for (int k = 0; k < 3; k++) {
+            const double x = d->pos[3 * i + k];
+            if (!std::isfinite(x)) return fail(FAU_ERR_ARG, "particle %d: non-finite position", i);
+            if (std::fabs(x) > 0.5 * d->box[k]) return fail(FAU_ERR_ARG, "particle %d: position outside the box", i);
+        }
+        if (!std::isfinite(d->charge[i])) return fail(FAU_ERR_ARG, "particle %d: non-finite charge", i);
+    }
+    if ((d->pair_terms & (FAU_PAIR_LJ | FAU_PAIR_WCA)) && (!d->sigma2 || !d->eps4))
+        return fail(FAU_ERR_ARG, "LJ/WCA need sigma2 and eps4 tables");
+    if ((d->pair_terms & FAU_PAIR_HS) && !d->hs_sigma2) return fail(FAU_ERR_ARG, "HS needs hs_sigma2");
+    if (d->ewald.enabled) {
+        if (!(d->ewald.alpha > 0.0)) return fail(FAU_ERR_ARG, "ewald.alpha must be positive");
+        if (d->ewald.ncutoff > 127) return fail(FAU_ERR_ARG, "ewald.ncutoff above 127");
+    }
+    if (d->precision != FAU_PREC_FP32C && d->precision != FAU_PREC_FP64)
+        return fail(FAU_ERR_ARG, "unknown precision %d", d->precision);
+    return FAU_OK;
+}
+
+struct Layout {
+    std::vector<int> itype;          // per particle
+    std::vector<int> itype_type;     // per itype
+    std::vector<double> itype_q;     // per itype
+    bool cells = false;
+    int cdim[3] = {1, 1, 1};
+    double cell_len[3] = {0, 0, 0};
+    int off_min[3] = {0, 0, 0}, off_max[3] = {0, 0, 0};
+    int cap = 0;
+    int K = 0;
+    EwaldTable ew;
+};
+
+int plan_layout(const fau_sys_desc* d, Layout& lay)
+{
+    std::map<std::pair<int, double>, int> cls;
+    lay.itype.resize(d->n_particles);
+    for (int i = 0; i < d->n_particles; i++) {
+        auto key = std::make_pair(d->type[i], d->charge[i]);
+        auto it = cls.find(key);
+        if (it == cls.end()) {
+            if ((int)cls.size() == kMaxITypes)
+                return fail(FAU_ERR_ARG, "more than %d distinct (type, charge) classes", kMaxITypes);
+            it = cls.emplace(key, (int)cls.size()).first;
+            lay.itype_type.push_back(d->type[i]);
+            lay.itype_q.push_back(d->charge[i]);
+        }
+        lay.itype[i] = it->second;
+    }
+    bool all_atomic = true;
+    for (int g = 0; g < d->n_groups; g++)
+        if (!(d->group_flags ? (d->group_flags[g] & FAU_GROUP_ATOMIC) : 1)) all_atomic = false;
+    // cell grid (GridBase::updateCellGrid src/celllistimpl.h:223-236) with the pair cutoff as
+    // the minimal cell dimension; only for all-atomic systems with a finite cutoff.
+    if (d->pair_cutoff > 0.0 && all_atomic) {
+        int ncell = 1;
+        for (int k = 0; k < 3; k++) {
+            lay.cdim[k] = (int)std::floor(d->box[k] / std::min(d->box[k], d->pair_cutoff));
+            lay.cell_len[k] = d->box[k] / double(lay.cdim[k]);
+            // distance-1 neighbour offsets clamped by the periodic grid's wrap-around limits
+            // (GridOffsets3D src/celllistimpl.cpp:15-31, src/celllistimpl.h:409-415)
+            const double mid = (lay.cdim[k] - 1) * 0.5;
+            lay.off_min[k] = std::max(-1, -(int)std::floor(mid));
+            lay.off_max[k] = std::min(1, (int)std::ceil(mid));
+            ncell *= lay.cdim[k];
+        }
+        if (d->box[0] < 2 * d->pair_cutoff || d->box[1] < 2 * d->pair_cutoff || d->box[2] < 2 * d->pair_cutoff)
+            ncell = 0; // minimum image + cutoff already covers every pair: all-pairs is cheaper
+        lay.cells = ncell >= 27;
+    }
+    if (d->ewald.enabled) {
+        lay.ew = build_kvectors(d->box, d->ewald.alpha, d->ewald.ncutoff, d->ewald.spherical_sum != 0);
+        lay.K = (int)lay.ew.kn.size();
+    }
+    return FAU_OK;
+}
+
+// bin one position, reference formula (bit-exact with the oracle)
+int host_cell(const double* x, const double L[3], const int dims[3], const double cell[3])
+{
+    int c[3];
+    for (int k = 0; k < 3; k++) {
+        const double t = x[k] + 0.5 * L[k];
+        int v = (int)std::floor(t / cell[k]);
+        if (v < 0) v += dims[k] * (std::abs(v) / dims[k] + 1);
+        else if (v >= dims[k]) v -= dims[k] * (v / dims[k]);
+        c[k] = v;
+    }
+    return c[0] + dims[0] * (c[1] + dims[1] * c[2]);
+}
+
+size_t footprint_bytes(const fau_sys_desc* d, const Layout& lay, int cap)
+{
+    const size_t n = d->n_particles, g = d->n_groups, nt = lay.itype_q.size();
+    size_t b = n * (3 * 8 + 16 + 4) + nt * (4 + 8 + 8) + (g + 1) * 4 + g * (4 + 24 + 16) + n * 4 +
+               nt * nt * (16 + 32) + sizeof(DevSys);
+    if (lay.cells) {
+        const size_t nc = (size_t)lay.cdim[0] * lay.cdim[1] * lay.cdim[2];
+        b += nc * 4 + nc * (size_t)cap * 16 + n * 8;
+    }
+    b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16);
+    b += sizeof(PlainMove) + 64 + sizeof(void*);
+    return b;
+}
+
+} // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int fau_abi_version(void) { return FAU_ABI_VERSION; }
+
+const char* fau_strerror(int status)
+{
+    switch (status) {
+    case FAU_OK: return "ok";
+    case FAU_ERR_ARG: return "invalid argument";
+    case FAU_ERR_OOM: return "out of device memory or HBM budget";
+    case FAU_ERR_CUDA: return "CUDA error";
+    case FAU_ERR_TIMEOUT: return "device wait timed out";
+    case FAU_ERR_NAN: return "Metropolis error: energy cannot be NaN";
+    case FAU_ERR_CAPACITY: return "cell list capacity exceeded";
+    case FAU_ERR_STATE: return "invalid state";
+    case FAU_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+const char* fau_last_error(void) { return g_last_error.c_str(); }
+
+int fau_ctx_create(int device, size_t hbm_budget_bytes, fau_ctx** out)
+{
+    if (!out) return fail(FAU_ERR_ARG, "null output");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(FAU_ERR_NODEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count) return fail(FAU_ERR_ARG, "device %d out of range", device);
+    CUDA_TRY(cudaSetDevice(device));
+    fau_ctx* c = new fau_ctx;
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return fail(FAU_ERR_CUDA, "stream/event creation failed");
+    }
+    *out = c;
+    return FAU_OK;
+}
+
+int fau_ctx_destroy(fau_ctx* c)
+{
+    if (!c) return FAU_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FAU_OK;
+}
+
+int fau_ctx_hbm_used(const fau_ctx* c, size_t* used)
+{
+    if (!c || !used) return fail(FAU_ERR_ARG, "null argument");
+    *used = c->used;
+    return FAU_OK;
+}
+
+int fau_sys_footprint(const fau_sys_desc* d, size_t* bytes)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    Layout lay;
+    rc = plan_layout(d, lay);
+    if (rc) return rc;
+    int cap = d->cell_capacity > 0 ? d->cell_capacity : 0;
+    if (lay.cells && cap == 0) {
+        const double ncell = (double)lay.cdim[0] * lay.cdim[1] * lay.cdim[2];
+        cap = std::max(16, (int)std::ceil(4.0 * d->n_particles / ncell) + 16);
+    }
+    *bytes = footprint_bytes(d, lay, cap);
+    return FAU_OK;
+}
+
+static int refresh_energy(fau_sys* s);
+
+int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
+{
+    if (!ctx || !out) return fail(FAU_ERR_ARG, "null argument");
+    int rc = validate(d);
+    if (rc) return rc;
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    Layout lay;
+    rc = plan_layout(d, lay);
+    if (rc) return rc;
+
+    fau_sys* s = new fau_sys;
+    s->ctx = ctx;
+    s->n = d->n_particles;
+    s->n_groups = d->n_groups;
+    s->K = lay.K;
+    s->cells = lay.cells;
+    s->precision = d->precision;
+    DevSys& h = s->h;
+    std::memset(&h, 0, sizeof(h));
+    auto bail = [&](int code) {
+        cudaStreamSynchronize(ctx->stream);
+        free_sys(s);
+        delete s;
+        return code;
+    };
+
+    // geometry
+    for (int k = 0; k < 3; k++) {
+        h.L[k] = d->box[k];
+        h.half[k] = 0.5 * d->box[k];
+        h.inv[k] = 1.0 / d->box[k];
+        h.fx_scale[k] = kTwo32 / d->box[k];
+        h.fx_len[k] = (float)(d->box[k] / kTwo32);
+        h.fx_lend[k] = d->box[k] / kTwo32;
+    }
+    const int n = d->n_particles;
+    h.n = n;
+    h.n_groups = d->n_groups;
+
+    // particles
+    std::vector<double> x(n), y(n), z(n);
+    std::vector<uint4> rec(n);
+    for (int i = 0; i < n; i++) {
+        x[i] = d->pos[3 * i];
+        y[i] = d->pos[3 * i + 1];
+        z[i] = d->pos[3 * i + 2];
+        rec[i] = make_uint4(to_fixed(x[i], h.fx_scale[0]), to_fixed(y[i], h.fx_scale[1]), to_fixed(z[i], h.fx_scale[2]),
+                            ((uint32_t)lay.itype[i] << 24) | (uint32_t)i);
+    }
+    // groups
+    const int G = d->n_groups;
+    s->g_begin.assign(d->group_begin, d->group_begin + G + 1);
+    s->g_flags.resize(G);
+    std::vector<int> group_of(n);
+    std::vector<double> cm(3 * G, 0.0);
+    std::vector<uint4> cmrec(G);
+    std::vector<int> atomic_idx;
+    bool molecular_only = true;
+    for (int g = 0; g < G; g++) {
+        s->g_flags[g] = d->group_flags ? d->group_flags[g] : FAU_GROUP_ATOMIC;
+        const int b = d->group_begin[g], e = d->group_begin[g + 1];
+        s->max_group = std::max(s->max_group, e - b);
+        for (int i = b; i < e; i++) group_of[i] = g;
+        if (s->g_flags[g] & FAU_GROUP_ATOMIC) {
+            molecular_only = false;
+            for (int i = b; i < e; i++) atomic_idx.push_back(i);
+        }
+        if (d->group_mass_center) {
+            for (int k = 0; k < 3; k++) cm[3 * g + k] = d->group_mass_center[3 * g + k];
+        }
+        else if (!(s->g_flags[g] & FAU_GROUP_ATOMIC) && e > b) {
+            // Group::updateMassCenter (src/group.cpp:136-157): shift by the middle particle,
+            // weighted centre (src/geometry.h:505-526), boundary, shift back.
+            const int mid = b + (e - b) / 2;
+            const double sh[3] = {-d->pos[3 * mid], -d->pos[3 * mid + 1], -d->pos[3 * mid + 2]};
+            double c[3] = {0, 0, 0}, ws = 0;
+            for (int i = b; i < e; i++) {
+                double p[3];
+                for (int k = 0; k < 3; k++) {
+                    p[k] = d->pos[3 * i + k] + sh[k];
+                    if (std::fabs(p[k]) > h.half[k]) {
+                        const double t = p[k] * h.inv[k];
+                        p[k] -= h.L[k] * (int)(t > 0.0 ? t + 0.5 : t - 0.5);
+                    }
+                }
+                const double w = d->type_mass ? d->type_mass[d->type[i]] : 1.0;
+                for (int k = 0; k < 3; k++) c[k] += w * p[k];
+                ws += w;
+            }
+            if (std::fabs(ws) > 2.220446049250313e-16) {
+                for (int k = 0; k < 3; k++) {
+                    double v = c[k] / ws - sh[k];
+                    if (std::fabs(v) > h.half[k]) {
+                        const double t = v * h.inv[k];
+                        v -= h.L[k] * (int)(t > 0.0 ? t + 0.5 : t - 0.5);
+                    }
+                    cm[3 * g + k] = v;
+                }
+            }
+        }
+        cmrec[g] = make_uint4(to_fixed(cm[3 * g], h.fx_scale[0]), to_fixed(cm[3 * g + 1], h.fx_scale[1]),
+                              to_fixed(cm[3 * g + 2], h.fx_scale[2]), 0u);
+    }
+    s->molecular_only = molecular_only;
+    s->group_of = group_of;
+
+    // pair tables over internal classes
+    const int nt = (int)lay.itype_q.size();
+    const int T = d->n_types;
+    std::vector<PairF> pf(nt * nt);
+    std::vector<double> pd(4 * nt * nt);
+    for (int a = 0; a < nt; a++)
+        for (int b = 0; b < nt; b++) {
+            const int ta = lay.itype_type[a], tb = lay.itype_type[b];
+            const double s2 = d->sigma2 ? d->sigma2[ta * T + tb] : 0.0;
+            const double e4 = d->eps4 ? d->eps4[ta * T + tb] : 0.0;
+            const double hs = d->hs_sigma2 ? d->hs_sigma2[ta * T + tb] : 0.0;
+            const double qq = d->bjerrum_length * lay.itype_q[a] * lay.itype_q[b];
+            pf[a * nt + b] = {(float)s2, (float)e4, (float)hs, (float)qq};
+            pd[4 * (a * nt + b) + 0] = s2;
+            pd[4 * (a * nt + b) + 1] = e4;
+            pd[4 * (a * nt + b) + 2] = hs;
+            pd[4 * (a * nt + b) + 3] = qq;
+        }
+    std::vector<float> iq(nt);
+    std::vector<double> iqd(nt), iself(nt, 0.0);
+    const bool has_self = (d->pair_terms & FAU_PAIR_COULOMB) && d->coulomb_type == FAU_COUL_EWALD;
+    for (int a = 0; a < nt; a++) {
+        iq[a] = (float)lay.itype_q[a];
+        iqd[a] = lay.itype_q[a];
+        // NewCoulombGalore self energy for S = erfc(alpha r): -lB alpha / sqrt(pi) q^2
+        if (has_self) iself[a] = d->bjerrum_length * (-d->coulomb_alpha / std::sqrt(kPi) * iqd[a] * iqd[a]);
+    }
+    h.nt = nt;
+    h.terms = d->pair_terms;
+    h.coul_type = d->coulomb_type;
+    h.lB = (float)d->bjerrum_length;
+    h.lB_d = d->bjerrum_length;
+    h.rc_coul = (float)d->coulomb_cutoff;
+    h.rc_coul_d = d->coulomb_cutoff;
+    h.rc2_coul = (float)(d->coulomb_cutoff * d->coulomb_cutoff);
+    h.alpha = (float)d->coulomb_alpha;
+    h.alpha_d = d->coulomb_alpha;
+    h.rc2_pair = d->pair_cutoff > 0 ? (float)(d->pair_cutoff * d->pair_cutoff) : 0.f;
+    h.rc2_pair_d = d->pair_cutoff > 0 ? d->pair_cutoff * d->pair_cutoff : 0.0;
+    h.cut_g2g2 = d->cutoff_g2g > 0 ? d->cutoff_g2g * d->cutoff_g2g : -1.0;
+    h.cut_g2g2f = (float)h.cut_g2g2;
+    h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
+              ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0);
+    h.beta_scale = 1.0;
+
+#define UP(dst, vec) \
+    if ((rc = upload(s, &dst, vec.data(), vec.size()))) return bail(rc)
+    UP(h.x, x);
+    UP(h.y, y);
+    UP(h.z, z);
+    UP(h.rec, rec);
+    UP(h.group_of, group_of);
+    UP(h.itype_q, iq);
+    UP(h.itype_qd, iqd);
+    UP(h.itype_self, iself);
+    UP(h.g_begin, s->g_begin);
+    UP(h.g_flags, s->g_flags);
+    UP(h.g_cm, cm);
+    UP(h.g_cmrec, cmrec);
+    UP(h.atomic_idx, atomic_idx);
+    h.n_atomic = molecular_only ? 0 : (int)atomic_idx.size();
+    if (!molecular_only && (int)atomic_idx.size() == n) h.n_atomic = 0; // all atomic: index = particle
+    UP(h.pair, pf);
+    UP(h.pair_d, pd);
+
+    // cell list
+    if (lay.cells) {
+        const int ncell = lay.cdim[0] * lay.cdim[1] * lay.cdim[2];
+        std::vector<int> cnt(ncell, 0), cell_of(n), slot_of(n);
+        for (int i = 0; i < n; i++) {
+            const double p[3] = {x[i], y[i], z[i]};
+            cell_of[i] = host_cell(p, d->box, lay.cdim, lay.cell_len);
+            slot_of[i] = cnt[cell_of[i]]++;
+        }
+        int maxc = *std::max_element(cnt.begin(), cnt.end());
+        int cap = d->cell_capacity > 0 ? d->cell_capacity
+                                       : std::max(16, (int)std::ceil(4.0 * n / (double)ncell) + 16);
+        cap = std::max(cap, maxc + 8);
+        cap = (cap + 3) & ~3;
+        std::vector<uint4> crec((size_t)ncell * cap, make_uint4(0, 0, 0, 0xFFFFFFFFu));
+        for (int i = 0; i < n; i++) crec[(size_t)cell_of[i] * cap + slot_of[i]] = rec[i];
+        for (int k = 0; k < 3; k++) {
+            h.cdim[k] = lay.cdim[k];
+            h.cell_len[k] = lay.cell_len[k];
+            h.off_min[k] = lay.off_min[k];
+            h.off_max[k] = lay.off_max[k];
+        }
+        h.ncell = ncell;
+        h.cap = cap;
+        UP(h.cell_cnt, cnt);
+        UP(h.cell_rec, crec);
+        UP(h.cell_of, cell_of);
+        UP(h.slot_of, slot_of);
+    }
+
+    // Ewald
+    if (d->ewald.enabled) {
+        std::vector<float> akf(lay.K);
+        for (int k = 0; k < lay.K; k++) akf[k] = (float)lay.ew.Ak[k];
+        h.K = lay.K;
+        UP(h.kn, lay.ew.kn);
+        UP(h.Ak, akf);
+        UP(h.Akd, lay.ew.Ak);
+        if ((rc = dev_alloc(s, &h.Q, lay.K))) return bail(rc);
+        const double V = d->box[0] * d->box[1] * d->box[2];
+        h.rec_pref = 2 * kPi * d->bjerrum_length / V;
+        const double const_inf = d->ewald.epss < 1 ? 0.0 : 1.0;
+        h.surf_pref = const_inf * 2.0 * kPi / ((2.0 * d->ewald.epss + 1.0) * V) * d->bjerrum_length;
+        double M[3] = {0, 0, 0};
+        for (int i = 0; i < n; i++) {
+            M[0] += d->charge[i] * x[i];
+            M[1] += d->charge[i] * y[i];
+            M[2] += d->charge[i] * z[i];
+        }
+        for (int k = 0; k < 3; k++) h.M[k] = M[k];
+    }
+#undef UP
+    // staging
+    if ((rc = dev_alloc(s, &s->d_plain, 1))) return bail(rc);
+    if ((rc = dev_alloc(s, &s->d_res, 8))) return bail(rc);
+    if ((rc = dev_alloc(s, &s->d_flags, 4))) return bail(rc);
+    if (lay.K > 0 && (rc = dev_alloc(s, &s->d_dq, lay.K))) return bail(rc);
+    if ((rc = dev_alloc(s, &s->d, 1))) return bail(rc);
+    if ((rc = dev_alloc(s, &s->d_self, 1))) return bail(rc);
+    if (cudaMemcpyAsync(s->d, &h, sizeof(DevSys), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(s->d_self, &s->d, sizeof(DevSys*), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+        return bail(fail(FAU_ERR_CUDA, "upload of the system descriptor failed"));
+    // Q(k) full update (src/energy.cpp:191-206) in FP64 on the device
+    if (lay.K > 0) {
+        if (launch_q_rebuild(s->d, lay.K, h.Q, ctx->stream) != cudaSuccess)
+            return bail(fail(FAU_ERR_CUDA, "q rebuild launch failed"));
+    }
+    if ((rc = refresh_energy(s))) return bail(rc);
+    *out = s;
+    return FAU_OK;
+}
+
+int fau_sys_destroy(fau_sys* s)
+{
+    if (!s) return FAU_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_sys(s);
+    delete s;
+    return FAU_OK;
+}
+
+int fau_sys_num_kvectors(const fau_sys* s, int* k)
+{
+    if (!s || !k) return fail(FAU_ERR_ARG, "null argument");
+    *k = s->K;
+    return FAU_OK;
+}
+
+// copy the device struct's running fields back to the host mirror
+static int pull_state(fau_sys* s)
+{
+    DevSys tmp;
+    CUDA_TRY(cudaMemcpyAsync(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    s->h.energy = tmp.energy;
+    for (int k = 0; k < 3; k++) s->h.M[k] = tmp.M[k];
+    s->h.err = tmp.err;
+    s->h.moves = tmp.moves;
+    s->h.accepted = tmp.accepted;
+    s->h.pair_evals = tmp.pair_evals;
+    s->h.k_updates = tmp.k_updates;
+    s->h.sum_du = tmp.sum_du;
+    return FAU_OK;
+}
+
+static int compute_total(fau_sys* s, fau_energy_terms* t)
+{
+    cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(cudaMemsetAsync(s->d_res, 0, 8 * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, 4 * sizeof(int), st));
+    CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_res, s->d_flags, st));
+    double r[8];
+    int f[4];
+    DevSys tmp;
+    CUDA_TRY(cudaMemcpyAsync(r, s->d_res, sizeof(r), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(f, s->d_flags, sizeof(f), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const double inf = std::numeric_limits<double>::infinity();
+    double nb = r[0];
+    if (f[0] & 2) nb = std::numeric_limits<double>::quiet_NaN();
+    else if (f[0] & 1) nb = inf;
+    t->self = (tmp.flags & SYS_SELF) ? r[2] : 0.0;
+    t->nonbonded = nb;
+    t->ewald_rec = (tmp.flags & SYS_EWALD) ? tmp.rec_pref * r[1] : 0.0;
+    double m2 = (tmp.M[0] * tmp.M[0] + tmp.M[1] * tmp.M[1]) + tmp.M[2] * tmp.M[2];
+    t->ewald_surf = (tmp.flags & SYS_SURFACE) ? tmp.surf_pref * m2 : 0.0;
+    // Hamiltonian::energy: [self], nonbonded, [ewald]; early break on +inf or NaN
+    double list[3];
+    int nl = 0;
+    if (tmp.flags & SYS_SELF) list[nl++] = t->self;
+    list[nl++] = t->nonbonded;
+    if (tmp.flags & SYS_EWALD) list[nl++] = t->ewald_surf + t->ewald_rec;
+    double sum = 0.0;
+    for (int i = 0; i < nl; i++) {
+        sum += list[i];
+        if (list[i] >= inf || std::isnan(list[i])) break;
+    }
+    t->total = sum;
+    return FAU_OK;
+}
+
+static int refresh_energy(fau_sys* s)
+{
+    fau_energy_terms t;
+    int rc = compute_total(s, &t);
+    if (rc) return rc;
+    s->h.energy = t.total;
+    CUDA_TRY(cudaMemcpyAsync(&s->d->energy, &t.total, sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_energy_total(fau_sys* s, fau_energy_terms* out)
+{
+    if (!s || !out) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    return compute_total(s, out);
+}
+
+static int ensure_stage(fau_sys* s, size_t n)
+{
+    if (n <= s->stage_cap) return FAU_OK;
+    size_t cap = std::max<size_t>(n, 1024);
+    int rc;
+    if ((rc = dev_alloc(s, &s->d_props, cap))) return rc;
+    if ((rc = dev_alloc(s, &s->d_acc, cap))) return rc;
+    if ((rc = dev_alloc(s, &s->d_du, cap))) return rc;
+    if ((rc = dev_alloc(s, &s->d_detail, cap))) return rc;
+    s->stage_cap = cap;
+    return FAU_OK;
+}
+
+static int chain_threads(const fau_sys* s)
+{
+    if (s->K >= 512 || s->n >= 4096) return 256;
+    return s->K > 0 || s->n > 512 ? 256 : 128;
+}
+
+static int check_device_err(fau_sys* s)
+{
+    int rc = pull_state(s);
+    if (rc) return rc;
+    if (s->h.err != FAU_OK) {
+        const int e = s->h.err;
+        s->h.err = 0;
+        CUDA_TRY(cudaMemsetAsync(&s->d->err, 0, sizeof(int), s->ctx->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+        return fail(e, "device reported: %s", fau_strerror(e));
+    }
+    return FAU_OK;
+}
+
+// Rebuild the cell list from the resident FP64 positions with a new capacity
+// (after an overflow); reference binning formula, bit-exact with the oracle.
+static int rebuild_cells(fau_sys* s, int cap)
+{
+    if (!s->cells) return FAU_OK;
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    std::vector<double> x(n), y(n), z(n);
+    std::vector<uint4> rec(n);
+    CUDA_TRY(cudaMemcpyAsync(x.data(), s->h.x, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(y.data(), s->h.y, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(z.data(), s->h.z, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(rec.data(), s->h.rec, sizeof(uint4) * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const int ncell = s->h.ncell;
+    std::vector<int> cnt(ncell, 0), cell_of(n), slot_of(n);
+    for (int i = 0; i < n; i++) {
+        const double p[3] = {x[i], y[i], z[i]};
+        cell_of[i] = host_cell(p, s->h.L, s->h.cdim, s->h.cell_len);
+        slot_of[i] = cnt[cell_of[i]]++;
+    }
+    const int maxc = *std::max_element(cnt.begin(), cnt.end());
+    cap = std::max(cap, maxc + 8);
+    cap = (cap + 3) & ~3;
+    std::vector<uint4> crec((size_t)ncell * cap, make_uint4(0, 0, 0, 0xFFFFFFFFu));
+    for (int i = 0; i < n; i++) crec[(size_t)cell_of[i] * cap + slot_of[i]] = rec[i];
+    uint4* nrec = nullptr;
+    int rc = dev_alloc(s, &nrec, crec.size());
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(nrec, crec.data(), sizeof(uint4) * crec.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->h.cell_cnt, cnt.data(), 4 * ncell, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->h.cell_of, cell_of.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->h.slot_of, slot_of.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    s->h.cell_rec = nrec;
+    s->h.cap = cap;
+    CUDA_TRY(cudaMemcpyAsync(&s->d->cell_rec, &nrec, sizeof(nrec), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&s->d->cap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return FAU_OK;
+}
+
+static int run_chain(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_trial_result* detail,
+                     fau_run_stats* stats)
+{
+    if (n < 0) return fail(FAU_ERR_ARG, "negative move count");
+    if (n == 0) {
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return FAU_OK;
+    }
+    for (int m = 0; m < n; m++) {
+        if (p[m].kind == FAU_MOVE_ATOMIC) {
+            if (p[m].index < 0 || p[m].index >= s->n) return fail(FAU_ERR_ARG, "proposal %d: particle out of range", m);
+            if (!(s->g_flags[s->group_of[p[m].index]] & FAU_GROUP_ATOMIC))
+                return fail(FAU_ERR_ARG, "proposal %d: single-atom move inside a molecular group is not supported", m);
+        }
+        else if (p[m].kind == FAU_MOVE_MOLECULAR) {
+            if (p[m].index < 0 || p[m].index >= s->n_groups) return fail(FAU_ERR_ARG, "proposal %d: group out of range", m);
+            if (s->g_flags[p[m].index] & FAU_GROUP_ATOMIC)
+                return fail(FAU_ERR_ARG, "proposal %d: molecular move of an atomic group", m);
+            if (s->g_begin[p[m].index + 1] - s->g_begin[p[m].index] > kMaxGroupAtoms)
+                return fail(FAU_ERR_ARG, "proposal %d: group larger than %d atoms", m, kMaxGroupAtoms);
+        }
+        else if (p[m].kind != FAU_MOVE_NONE) {
+            return fail(FAU_ERR_ARG, "proposal %d: unknown kind %d", m, p[m].kind);
+        }
+    }
+    int rc = ensure_stage(s, (size_t)n);
+    if (rc) return rc;
+    cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync(s->d_props, p, sizeof(fau_proposal) * n, cudaMemcpyHostToDevice, st));
+    DevSys before;
+    CUDA_TRY(cudaMemcpyAsync(&before, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+    float total_ms = 0.f;
+    long long offset = 0;
+    for (int attempt = 0; attempt < 16 && offset < n; attempt++) {
+        ChainArgs a{};
+        a.sys = s->d_self;
+        a.moves = n - offset;
+        a.props = s->d_props + offset;
+        a.acc_out = acc ? s->d_acc + offset : nullptr;
+        a.du_out = du ? s->d_du + offset : nullptr;
+        a.detail = detail ? s->d_detail + offset : nullptr;
+        CUDA_TRY(cudaEventRecord(s->ctx->ev0, st));
+        CUDA_TRY(launch_chain(a, 1, s->K, chain_threads(s), false, st));
+        CUDA_TRY(cudaEventRecord(s->ctx->ev1, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->ctx->ev0, s->ctx->ev1);
+        total_ms += ms;
+        DevSys now;
+        CUDA_TRY(cudaMemcpy(&now, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost));
+        if (now.err == FAU_ERR_CAPACITY) {
+            // a cell overflowed on an accepted move: the move is committed except for its
+            // cell-list entry; rebuild the cell list with twice the capacity and resume
+            offset += now.consumed;
+            const int zero = 0;
+            CUDA_TRY(cudaMemcpy(&s->d->err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+            if ((rc = rebuild_cells(s, 2 * s->h.cap))) return rc;
+            continue;
+        }
+        offset = n;
+    }
+    if (acc) CUDA_TRY(cudaMemcpyAsync(acc, s->d_acc, n, cudaMemcpyDeviceToHost, st));
+    if (du) CUDA_TRY(cudaMemcpyAsync(du, s->d_du, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (detail) CUDA_TRY(cudaMemcpyAsync(detail, s->d_detail, sizeof(fau_trial_result) * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    rc = check_device_err(s);
+    if (stats) {
+        stats->moves = (int64_t)(s->h.moves - before.moves);
+        stats->accepted = (int64_t)(s->h.accepted - before.accepted);
+        stats->pair_evals = (int64_t)(s->h.pair_evals - before.pair_evals);
+        stats->k_updates = (int64_t)(s->h.k_updates - before.k_updates);
+        stats->energy_change = s->h.sum_du - before.sum_du;
+        stats->energy = s->h.energy;
+        stats->max_rel_err = 0.0;
+        stats->device_ms = total_ms;
+    }
+    return rc;
+}
+
+static int plain_trial(fau_sys* s, int kind, int index, const double dr[3], const double* quat, double u01,
+                       fau_trial_result* out);
+
+int fau_run_proposals(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats)
+{
+    if (!s || (!p && n > 0)) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    if (s->precision != FAU_PREC_FP64) return run_chain(s, p, n, acc, du, nullptr, stats);
+    // plain FP64 form: one move per call, host Metropolis
+    int rc = pull_state(s);
+    if (rc) return rc;
+    const DevSys before = s->h;
+    CUDA_TRY(cudaEventRecord(s->ctx->ev0, s->ctx->stream));
+    for (int m = 0; m < n; m++) {
+        fau_trial_result r{};
+        if (p[m].kind == FAU_MOVE_ATOMIC) rc = fau_trial_atomic(s, p[m].index, p[m].dr, p[m].u, &r);
+        else if (p[m].kind == FAU_MOVE_MOLECULAR) rc = fau_trial_group(s, p[m].index, p[m].dr, p[m].quat, p[m].u, &r);
+        if (rc) return rc;
+        if (acc) acc[m] = (uint8_t)r.accepted;
+        if (du) du[m] = r.du;
+    }
+    CUDA_TRY(cudaEventRecord(s->ctx->ev1, s->ctx->stream));
+    CUDA_TRY(cudaEventSynchronize(s->ctx->ev1));
+    if ((rc = pull_state(s))) return rc;
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->ctx->ev0, s->ctx->ev1);
+        stats->moves = (int64_t)(s->h.moves - before.moves);
+        stats->accepted = (int64_t)(s->h.accepted - before.accepted);
+        stats->pair_evals = 2 * (int64_t)(s->n - 1) * n;
+        stats->k_updates = (int64_t)s->K * n;
+        stats->energy_change = s->h.sum_du - before.sum_du;
+        stats->energy = s->h.energy;
+        stats->max_rel_err = 0.0;
+        stats->device_ms = ms;
+    }
+    return FAU_OK;
+}
+
+// plain FP64 form: host computes the trial positions exactly like the device
+static double hb(double a, double L, double half, double inv)
+{
+    if (std::fabs(a) > half) {
+        const double t = a * inv;
+        a -= L * (int)(t > 0.0 ? t + 0.5 : t - 0.5);
+    }
+    return a;
+}
+
+static int plain_trial(fau_sys* s, int kind, int index, const double dr[3], const double* quat, double u01,
+                       fau_trial_result* out)
+{
+    cudaStream_t st = s->ctx->stream;
+    PlainMove pm{};
+    pm.kind = kind;
+    const DevSys& h = s->h;
+    std::vector<double> xo;
+    std::vector<double> qs;
+    if (kind == FAU_MOVE_ATOMIC) {
+        pm.first = index;
+        pm.m = 1;
+        pm.group = -1;
+        double p[3];
+        CUDA_TRY(cudaMemcpyAsync(&p[0], h.x + index, 8, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&p[1], h.y + index, 8, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&p[2], h.z + index, 8, cudaMemcpyDeviceToHost, st));
+        uint4 r;
+        CUDA_TRY(cudaMemcpyAsync(&r, h.rec + index, sizeof(uint4), cudaMemcpyDeviceToHost, st));
+        double q;
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaMemcpy(&q, h.itype_qd + (r.w >> 24), 8, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 3; k++) {
+            pm.xn[0][k] = hb(p[k] + dr[k], h.L[k], h.half[k], h.inv[k]);
+            pm.dM[k] = q * (pm.xn[0][k] - p[k]);
+        }
+    }
+    else {
+        const int b = s->g_begin[index], e = s->g_begin[index + 1];
+        pm.first = b;
+        pm.m = e - b;
+        pm.group = index;
+        std::vector<double> X(pm.m), Y(pm.m), Z(pm.m);
+        std::vector<uint4> R(pm.m);
+        double cm[3];
+        CUDA_TRY(cudaMemcpyAsync(X.data(), h.x + b, 8 * pm.m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(Y.data(), h.y + b, 8 * pm.m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(Z.data(), h.z + b, 8 * pm.m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(R.data(), h.rec + b, sizeof(uint4) * pm.m, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(cm, h.g_cm + 3 * index, 24, cudaMemcpyDeviceToHost, st));
+        std::vector<double> iq(h.nt);
+        CUDA_TRY(cudaMemcpyAsync(iq.data(), h.itype_qd, 8 * h.nt, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        for (int k = 0; k < 3; k++) pm.cm_new[k] = hb(cm[k] + dr[k], h.L[k], h.half[k], h.inv[k]);
+        const bool rot = quat && !(quat[0] == 0.0 && quat[1] == 0.0 && quat[2] == 0.0 && quat[3] == 0.0);
+        for (int a = 0; a < pm.m; a++) {
+            const double o[3] = {X[a], Y[a], Z[a]};
+            double v[3];
+            for (int k = 0; k < 3; k++) v[k] = hb(o[k] + dr[k], h.L[k], h.half[k], h.inv[k]);
+            if (rot) {
+                for (int k = 0; k < 3; k++) v[k] = hb(v[k] - pm.cm_new[k], h.L[k], h.half[k], h.inv[k]);
+                const double ux = quat[1], uy = quat[2], uz = quat[3], w = quat[0];
+                double tx = uy * v[2] - uz * v[1], ty = uz * v[0] - ux * v[2], tz = ux * v[1] - uy * v[0];
+                tx = tx + tx;
+                ty = ty + ty;
+                tz = tz + tz;
+                const double cx = uy * tz - uz * ty, cy = uz * tx - ux * tz, cz = ux * ty - uy * tx;
+                v[0] = v[0] + w * tx + cx;
+                v[1] = v[1] + w * ty + cy;
+                v[2] = v[2] + w * tz + cz;
+                for (int k = 0; k < 3; k++) v[k] = hb(v[k] + pm.cm_new[k], h.L[k], h.half[k], h.inv[k]);
+            }
+            const double q = iq[R[a].w >> 24];
+            for (int k = 0; k < 3; k++) {
+                pm.xn[a][k] = v[k];
+                pm.dM[k] += q * (v[k] - o[k]);
+            }
+        }
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->d_plain, &pm, sizeof(pm), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(s->d_res, 0, 8 * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, 4 * sizeof(int), st));
+    CUDA_TRY(launch_plain_du(s->d, s->d_plain, s->n, s->K, s->d_dq, s->d_res, s->d_flags, st));
+    double r[8];
+    int f[4];
+    CUDA_TRY(cudaMemcpyAsync(r, s->d_res, sizeof(r), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(f, s->d_flags, sizeof(f), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const double du_nb = r[0];
+    const double du_rec = s->K ? h.rec_pref * r[1] : 0.0;
+    double du_surf = 0.0;
+    if (h.flags & SYS_SURFACE) {
+        double M[3];
+        DevSys tmp;
+        CUDA_TRY(cudaMemcpy(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 3; k++) M[k] = tmp.M[k];
+        double m2o = 0, m2n = 0;
+        for (int k = 0; k < 3; k++) {
+            m2o += M[k] * M[k];
+            m2n += (M[k] + pm.dM[k]) * (M[k] + pm.dM[k]);
+        }
+        du_surf = h.surf_pref * (m2n - m2o);
+    }
+    const double inf = std::numeric_limits<double>::infinity();
+    const bool ni = f[0] & 1, oi = f[0] & 2, nn = f[0] & 4, on = f[0] & 8;
+    double du;
+    if (on && !nn) du = -inf;
+    else if (nn) du = inf;
+    else if (ni) du = inf;
+    else if (oi) du = -inf;
+    else du = du_nb + (du_rec + du_surf);
+    if (std::isnan(du)) return fail(FAU_ERR_NAN, "Metropolis error: energy cannot be NaN");
+    const double x = du * h.beta_scale;
+    bool acc;
+    if (std::isinf(x) && x < 0) acc = true;
+    else if (-x > 709.782712893384) acc = true;
+    else acc = u01 <= std::exp(-x);
+    if (out) {
+        out->du = du;
+        out->du_nonbonded = du_nb;
+        out->du_ewald = du_rec + du_surf;
+        out->err_scale = r[2];
+        out->accepted = acc;
+        out->new_inf = ni;
+        out->old_inf = oi;
+        out->pad = 0;
+    }
+    if (acc) {
+        pm.du = du;
+        CUDA_TRY(cudaMemcpyAsync(s->d_plain, &pm, sizeof(pm), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_plain_commit(s->d, s->d_plain, s->K, s->d_dq, st));
+    }
+    else {
+        unsigned long long one = 1;
+        DevSys tmp;
+        CUDA_TRY(cudaMemcpyAsync(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        tmp.moves += one;
+        CUDA_TRY(cudaMemcpyAsync(&s->d->moves, &tmp.moves, sizeof(one), cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return check_device_err(s);
+}
+
+int fau_trial_atomic(fau_sys* s, int particle, const double dr[3], double u01, fau_trial_result* out)
+{
+    if (!s || !dr) return fail(FAU_ERR_ARG, "null argument");
+    if (particle < 0 || particle >= s->n) return fail(FAU_ERR_ARG, "particle out of range");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    if (!(s->g_flags[s->group_of[particle]] & FAU_GROUP_ATOMIC))
+        return fail(FAU_ERR_ARG, "single-atom move inside a molecular group is not supported");
+    // the system's precision decides the form: plain FP64 or the FP32C chain kernel
+    if (s->precision == FAU_PREC_FP64) return plain_trial(s, FAU_MOVE_ATOMIC, particle, dr, nullptr, u01, out);
+    fau_proposal p{};
+    p.kind = FAU_MOVE_ATOMIC;
+    p.index = particle;
+    for (int k = 0; k < 3; k++) p.dr[k] = dr[k];
+    p.u = u01;
+    fau_trial_result r{};
+    int rc = run_chain(s, &p, 1, nullptr, nullptr, &r, nullptr);
+    if (out) *out = r;
+    return rc;
+}
+
+int fau_trial_group(fau_sys* s, int group, const double dr[3], const double quat[4], double u01, fau_trial_result* out)
+{
+    if (!s || !dr) return fail(FAU_ERR_ARG, "null argument");
+    if (group < 0 || group >= s->n_groups) return fail(FAU_ERR_ARG, "group out of range");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    if (s->g_flags[group] & FAU_GROUP_ATOMIC) return fail(FAU_ERR_ARG, "molecular move of an atomic group");
+    if (s->g_begin[group + 1] - s->g_begin[group] > kMaxGroupAtoms)
+        return fail(FAU_ERR_ARG, "group larger than %d atoms", kMaxGroupAtoms);
+    if (s->precision == FAU_PREC_FP64) return plain_trial(s, FAU_MOVE_MOLECULAR, group, dr, quat, u01, out);
+    fau_proposal p{};
+    p.kind = FAU_MOVE_MOLECULAR;
+    p.index = group;
+    for (int k = 0; k < 3; k++) p.dr[k] = dr[k];
+    if (quat)
+        for (int k = 0; k < 4; k++) p.quat[k] = quat[k];
+    p.u = u01;
+    fau_trial_result r{};
+    int rc = run_chain(s, &p, 1, nullptr, nullptr, &r, nullptr);
+    if (out) *out = r;
+    return rc;
+}
+
+// internal accessors used by fau_batch.cu (not part of the public header)
+int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device)
+{
+    *st = c->stream;
+    *device = c->device;
+    return FAU_OK;
+}
+int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n, int* n_groups, int* molecular_only,
+                          double* t_ref)
+{
+    *ctx = s->ctx;
+    *d = s->d;
+    *K = s->K;
+    *n = s->n;
+    *n_groups = s->n_groups;
+    *molecular_only = s->molecular_only ? 1 : 0;
+    *t_ref = 1.0;
+    return FAU_OK;
+}
+int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int fau_get_positions(fau_sys* s, double* xyz)
+{
+    if (!s || !xyz) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    std::vector<double> x(s->n), y(s->n), z(s->n);
+    cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync(x.data(), s->h.x, 8 * s->n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(y.data(), s->h.y, 8 * s->n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(z.data(), s->h.z, 8 * s->n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < s->n; i++) {
+        xyz[3 * i] = x[i];
+        xyz[3 * i + 1] = y[i];
+        xyz[3 * i + 2] = z[i];
+    }
+    return FAU_OK;
+}
+
+int fau_get_mass_centers(fau_sys* s, double* xyz)
+{
+    if (!s || !xyz) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    CUDA_TRY(cudaMemcpyAsync(xyz, s->h.g_cm, 24 * s->n_groups, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_get_cells(fau_sys* s, int* cell_out)
+{
+    if (!s || !cell_out) return fail(FAU_ERR_ARG, "null argument");
+    if (!s->cells) {
+        for (int i = 0; i < s->n; i++) cell_out[i] = -1;
+        return FAU_OK;
+    }
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    CUDA_TRY(cudaMemcpyAsync(cell_out, s->h.cell_of, 4 * s->n, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_get_cell_grid(const fau_sys* s, int dims[3])
+{
+    if (!s || !dims) return fail(FAU_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; k++) dims[k] = s->cells ? s->h.cdim[k] : 0;
+    return FAU_OK;
+}
+
+int fau_get_running_energy(fau_sys* s, double* e)
+{
+    if (!s || !e) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    int rc = pull_state(s);
+    if (rc) return rc;
+    *e = s->h.energy;
+    return FAU_OK;
+}
+
+int fau_set_temperature_scale(fau_sys* s, double scale)
+{
+    if (!s || !(scale > 0.0) || !std::isfinite(scale)) return fail(FAU_ERR_ARG, "invalid scale");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    s->h.beta_scale = scale;
+    CUDA_TRY(cudaMemcpyAsync(&s->d->beta_scale, &scale, sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_get_q(fau_sys* s, double* q)
+{
+    if (!s || !q) return fail(FAU_ERR_ARG, "null argument");
+    if (s->K == 0) return FAU_OK;
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    CUDA_TRY(cudaMemcpyAsync(q, s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_q_rebuild(fau_sys* s, double* drift)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null argument");
+    if (s->K == 0) {
+        if (drift) *drift = 0.0;
+        return FAU_OK;
+    }
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    std::vector<double2> before(s->K), after(s->K);
+    CUDA_TRY(cudaMemcpyAsync(before.data(), s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(launch_q_rebuild(s->d, s->K, s->h.Q, st));
+    CUDA_TRY(cudaMemcpyAsync(after.data(), s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    double mx = 0.0;
+    for (int k = 0; k < s->K; k++)
+        mx = std::max(mx, std::max(std::fabs(before[k].x - after[k].x), std::fabs(before[k].y - after[k].y)));
+    if (drift) *drift = mx;
+    return FAU_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,292 @@
+// fau_dev.cuh -- device-side layout and arithmetic helpers of the GB300
+// Metropolis MC hot path.
+//
+// Layout in HBM, per system (one Faunus Space + Hamiltonian):
+//   x, y, z       FP64 master positions (SoA).  All move arithmetic that
+//                 decides where a particle ends up is FP64 and IEEE-exact
+//                 (__dadd_rn / __dmul_rn: never contracted), so the chain
+//                 is bit-identical to the FP64 oracle under the same RNG.
+//   rec           uint4 {ux, uy, uz, (itype << 24) | index}: fixed-point
+//                 copy with 2^32 units per box length.  Integer subtraction
+//                 of two records is the minimum-image separation (exact),
+//                 and n.u mod 2^32 is the exact reduced Ewald phase.
+//   cell_rec      the same records bucketed by cell (fixed capacity),
+//                 cell_cnt, cell_of, slot_of: incremental cell list.
+//   Q             Ewald structure factor, FP64 complex master copy.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fau_gpu.h"
+
+namespace fau {
+
+constexpr int kMaxITypes = 16;     // internal (type, charge) classes per system
+constexpr int kMaxGroupAtoms = 32; // atoms moved together in one molecular move
+constexpr int kFlushAccepts = 64;  // FP32 pending Q deltas flushed to FP64 every N accepts
+
+enum SysFlags : int {
+    SYS_CELLS = 1 << 0,   // single-atom moves use the cell list
+    SYS_EWALD = 1 << 1,
+    SYS_SURFACE = 1 << 2, // Ewald surface term active (epss >= 1)
+    SYS_SELF = 1 << 3,    // ParticleSelfEnergy present
+};
+
+// pair parameters for one (itype a, itype b) class pair, FP32
+struct PairF {
+    float s2, e4, hs2, qq; // sigma^2, 4 eps, hard-sphere sigma^2, lB qa qb
+};
+
+struct DevSys {
+    // geometry (cuboid)
+    double L[3], half[3], inv[3];
+    double fx_scale[3]; // 2^32 / L : FP64 -> fixed point
+    float fx_len[3];    // L / 2^32 : fixed point -> FP32 angstrom
+    double fx_lend[3];  // L / 2^32 in FP64
+    int n, n_groups, flags, pad0;
+
+    double* x;
+    double* y;
+    double* z;
+    uint4* rec;
+    int* group_of;
+    float* itype_q;     // charge per internal type (FP32)
+    double* itype_qd;   // FP64
+    double* itype_self; // self energy per internal type (kT)
+
+    // groups
+    int* g_begin;     // n_groups + 1
+    int* g_flags;
+    double* g_cm;     // n_groups * 3 FP64 mass centres
+    uint4* g_cmrec;   // fixed-point mass centres
+    int* atomic_idx;  // particles of atomic groups (for molecular moves)
+    int n_atomic;
+
+    // pair potential
+    int nt, terms, coul_type, pad1;
+    float lB, rc_coul, rc2_coul, alpha;
+    float rc2_pair;   // 0: no truncation
+    double rc2_pair_d, rc_coul_d, alpha_d, lB_d;
+    double cut_g2g2;  // group mass-centre cutoff^2 (FP64); < 0: none
+    float cut_g2g2f;
+    PairF* pair;      // nt*nt
+    double* pair_d;   // nt*nt*4 FP64 copies (s2, e4, hs2, qq)
+
+    // cell list
+    int cdim[3], ncell;
+    int off_min[3], off_max[3];
+    int cap, pad2;
+    double cell_len[3];
+    int* cell_cnt;
+    uint4* cell_rec;
+    int* cell_of;
+    int* slot_of;
+
+    // Ewald
+    int K, pad3;
+    int* kn;          // packed (nx+128) | (ny+128)<<8 | (nz+128)<<16
+    float* Ak;
+    double* Akd;
+    double2* Q;       // FP64 master
+    double rec_pref;  // 2 pi lB / V
+    double surf_pref; // const_inf 2 pi lB / ((2 epss + 1) V)
+    double M[3];      // sum q r (surface term)
+
+    // running state
+    double energy;     // running total energy (kT), FP64
+    double beta_scale; // multiplies dU in the Metropolis test (PT temperature ladder)
+    int err;           // fau_status raised on the device
+    int pad4;
+    unsigned long long moves, accepted, pair_evals, k_updates;
+    double sum_du;
+    long long consumed; // proposals performed by the last chain launch
+};
+
+// ---------------------------------------------------------------- fixed point
+__host__ __device__ inline uint32_t to_fixed(double x, double scale)
+{
+#ifdef __CUDA_ARCH__
+    const double t = __dmul_rn(x, scale);
+    return (uint32_t)(unsigned long long)__double2ll_rn(t);
+#else
+    const double t = x * scale;
+    return (uint32_t)(unsigned long long)llrint(t);
+#endif
+}
+
+// ---------------------------------------------------------------- compensated sums
+// float-float accumulator (Knuth TwoSum): ~48-bit significand, FP32 pipe only.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF& a, float b)
+{
+    const float s = __fadd_rn(a.hi, b);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, e);
+}
+__device__ __forceinline__ FF ff_sum(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    const float lo = __fsub_rn(e, __fsub_rn(hi, s));
+    return {hi, lo};
+}
+__device__ __forceinline__ double ff_value(FF a) { return (double)a.hi + (double)a.lo; }
+
+// ---------------------------------------------------------------- Philox4x32-10
+// Counter-based RNG of Salmon, Moraes, Dror & Shaw (SC'11), published constants.
+struct U4 {
+    uint32_t x, y, z, w;
+};
+__device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = {hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+__device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) // [0,1) with 53 bits
+{
+    const unsigned long long v = ((unsigned long long)(a >> 5) << 26) | (b >> 6);
+    return (double)v * (1.0 / 9007199254740992.0);
+}
+__device__ __forceinline__ float u01_24(uint32_t a) { return (float)(a >> 8) * (1.0f / 16777216.0f); }
+
+// ---------------------------------------------------------------- geometry, FP64 exact
+// Chameleon::boundary (reference src/geometry.h:407-427) with anint (:132-135).
+__device__ __forceinline__ double boundary1(double a, double L, double half, double inv)
+{
+    if (fabs(a) > half) {
+        const double t = __dmul_rn(a, inv);
+        const int n = (int)(t > 0.0 ? __dadd_rn(t, 0.5) : __dsub_rn(t, 0.5));
+        a = __dsub_rn(a, __dmul_rn(L, (double)n));
+    }
+    return a;
+}
+// Chameleon::sqdist (src/geometry.h:460-485), summed ((x^2 + y^2) + z^2)
+__device__ __forceinline__ double sqdist_d(const DevSys& S, const double* a, const double* b)
+{
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double v = fabs(__dsub_rn(a[k], b[k]));
+        d[k] = __dsub_rn(v, v > S.half[k] ? S.L[k] : 0.0);
+    }
+    return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+
+// squared minimum-image distance of two fixed-point records, FP32
+__device__ __forceinline__ float r2_fixed(const DevSys& S, uint4 a, uint4 b)
+{
+    const float dx = (float)(int32_t)(a.x - b.x) * S.fx_len[0];
+    const float dy = (float)(int32_t)(a.y - b.y) * S.fx_len[1];
+    const float dz = (float)(int32_t)(a.z - b.z) * S.fx_len[2];
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// ---------------------------------------------------------------- pair energy, FP32
+// Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
+// overflow set `inf` instead of adding +inf, so the compensated sums stay finite.
+__device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, float r2, bool& inf, bool& nan)
+{
+    if (S.rc2_pair > 0.f && r2 >= S.rc2_pair) return 0.f;
+    float u = 0.f;
+    const int terms = S.terms;
+    const float rinv = rsqrtf(r2);
+    if (terms & FAU_PAIR_COULOMB) {
+        if (S.coul_type == FAU_COUL_PLAIN) {
+            u += p.qq * rinv;
+        }
+        else if (r2 < S.rc2_coul) {
+            float s = 1.f;
+            if (S.coul_type == FAU_COUL_EWALD) s = erfcf(S.alpha * (r2 * rinv));
+            u += p.qq * s * rinv;
+        }
+    }
+    if (terms & FAU_PAIR_LJ) {
+        float x = p.s2 * (rinv * rinv);
+        x = x * x * x;
+        u += p.e4 * (x * x - x);
+    }
+    if (terms & FAU_PAIR_WCA) {
+        if (!(r2 > p.s2 * 1.2599210498948732f)) {
+            float x = p.s2 * (rinv * rinv);
+            x = x * x * x;
+            u += p.e4 * (x * x - x + 0.25f);
+        }
+    }
+    if ((terms & FAU_PAIR_HS) && r2 < p.hs2) inf = true;
+    if (!isfinite(u)) {
+        if (isnan(u) && !(p.s2 == p.s2)) nan = true; // missing coefficients (NaN sigma)
+        else inf = true;                              // FP32 overflow at r -> 0
+        u = 0.f;
+    }
+    return u;
+}
+
+// FP64 pair energy (plain form and total energy), same term order as the oracle
+__device__ __forceinline__ double pair_u64(const DevSys& S, int ta, int tb, double r2)
+{
+    if (S.rc2_pair_d > 0.0 && r2 >= S.rc2_pair_d) return 0.0;
+    const double* P = S.pair_d + 4 * (ta * S.nt + tb);
+    const double s2 = P[0], e4 = P[1], hs2 = P[2], qq = P[3];
+    double u = 0.0;
+    if (S.terms & FAU_PAIR_COULOMB) {
+        if (S.coul_type == FAU_COUL_PLAIN) {
+            u += qq / sqrt(r2);
+        }
+        else {
+            const double r = sqrt(r2) + 2.220446049250313e-16;
+            if (r < S.rc_coul_d) {
+                const double s = (S.coul_type == FAU_COUL_EWALD) ? erfc(S.alpha_d * r) : 1.0;
+                u += qq / r * s;
+            }
+        }
+    }
+    if (S.terms & FAU_PAIR_LJ) {
+        double x = s2 / r2;
+        x = x * x * x;
+        u += e4 * (x * x - x);
+    }
+    if (S.terms & FAU_PAIR_WCA) {
+        double w = 0.0;
+        if (!(r2 > s2 * 1.2599210498948732)) {
+            double x = s2 / r2;
+            x = x * x * x;
+            w = e4 * (x * x - x + 0.25);
+        }
+        u += w;
+    }
+    if ((S.terms & FAU_PAIR_HS) && r2 < hs2) u += __longlong_as_double(0x7ff0000000000000ULL);
+    return u;
+}
+
+__device__ __forceinline__ void kn_unpack(int v, int& nx, int& ny, int& nz)
+{
+    nx = (v & 0xff) - 128;
+    ny = ((v >> 8) & 0xff) - 128;
+    nz = ((v >> 16) & 0xff) - 128;
+}
+
+// e^{i k.r} from a fixed-point record: the phase n.u mod 2^32 is exact.
+__device__ __forceinline__ float2 eikr32(int nx, int ny, int nz, uint4 r)
+{
+    const uint32_t ph = (uint32_t)nx * r.x + (uint32_t)ny * r.y + (uint32_t)nz * r.z;
+    const float t = (float)(int32_t)ph * 4.656612873077393e-10f; // 2^-31
+    float s, c;
+    sincospif(t, &s, &c);
+    return make_float2(c, s);
+}
+
+} // namespace fau

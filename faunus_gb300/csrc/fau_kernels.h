@@ -1,0 +1,49 @@
+// fau_kernels.h -- launch interface between the host runtime and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/fau_gpu.h"
+
+namespace fau {
+
+struct DevSys;
+
+// Arguments of the persistent chain kernel; one CTA per entry of `sys`.
+struct ChainArgs {
+    DevSys* const* sys;          // device array of device DevSys pointers
+    const uint32_t* sys_ids;     // RNG stream id per CTA (NULL: blockIdx.x)
+    const long long* n_moves;    // moves per CTA (NULL: `moves`)
+    long long moves;
+    // host-fed proposal mode
+    const fau_proposal* props;   // device proposal stream
+    const long long* prop_off;   // first proposal per CTA (NULL: 0)
+    uint8_t* acc_out;            // optional per-move outputs (indexed like props)
+    double* du_out;
+    fau_trial_result* detail;
+    // device RNG mode
+    uint64_t seed;
+    unsigned long long counter_base;
+    const unsigned long long* counters; // per CTA first counter (NULL: counter_base)
+    double dp, dprot;
+    const uint8_t* molecular;    // per CTA: 1 -> moltransrot moves, 0 -> transrot
+};
+
+// One plain FP64 trial move (host-computed trial positions).
+struct PlainMove {
+    int kind, first, m, group;
+    double xn[32][3];
+    double cm_new[3];
+    double dM[3];
+    double du;
+};
+
+size_t chain_smem_bytes(int K);
+cudaError_t prepare_chain(int K, int threads, bool philox);
+cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int threads, bool philox, cudaStream_t st);
+cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
+cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
+cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
+                            int* flags, cudaStream_t st);
+cudaError_t launch_plain_commit(DevSys* dsys, const PlainMove* pm, int K, const double2* dq, cudaStream_t st);
+
+} // namespace fau

@@ -1,0 +1,366 @@
+"""Python host API over the C ABI: a Faunus ``Space`` + ``Hamiltonian``
+description (:class:`SystemSpec`), a GPU context, resident systems and the
+reference-stream move generator.
+
+Units follow the reference (src/units.h:10-45, :230-233): energies in kT,
+lengths in angstrom, epsilon input in kJ/mol converted with the same
+physical constants.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _capi as A
+
+# PhysicalConstants (reference src/units.h:10-45)
+ELEMENTARY_CHARGE = 1.602177e-19
+VACUUM_PERMITTIVITY = 8.85419e-12
+BOLTZMANN = 1.380658e-23
+AVOGADRO = 6.022137e23
+PI = float(np.pi)
+
+
+def bjerrum_length(epsr: float, temperature: float = 298.15) -> float:
+    """Bjerrum length in angstrom (pc::bjerrumLength, src/units.h:37-41)."""
+    kT = temperature * BOLTZMANN
+    return ELEMENTARY_CHARGE ** 2 / (4 * PI * VACUUM_PERMITTIVITY * epsr * 1e-10 * kT)
+
+
+def kjmol_to_kt(x: float, temperature: float = 298.15) -> float:
+    """operator""_kJmol (src/units.h:230-233): kJ/mol per particle in kT."""
+    return x / (temperature * BOLTZMANN) / AVOGADRO * 1e3
+
+
+@dataclass
+class SystemSpec:
+    """Space + Hamiltonian of one system, as numpy arrays (see fau_sys_desc)."""
+
+    box: np.ndarray                       # (3,)
+    pos: np.ndarray                       # (N, 3) inside [-L/2, L/2]
+    charge: np.ndarray                    # (N,)
+    type: np.ndarray                      # (N,) int
+    group_begin: np.ndarray               # (G+1,)
+    group_flags: np.ndarray               # (G,)
+    n_types: int
+    sigma2: Optional[np.ndarray] = None   # (T, T)
+    eps4: Optional[np.ndarray] = None     # (T, T) in kT
+    hs_sigma2: Optional[np.ndarray] = None
+    type_mass: Optional[np.ndarray] = None
+    group_molid: Optional[np.ndarray] = None
+    mass_center: Optional[np.ndarray] = None  # (G, 3)
+    pair_terms: int = 0
+    coulomb_type: int = A.FAU_COUL_PLAIN
+    bjerrum_length: float = 0.0
+    coulomb_cutoff: float = 0.0
+    coulomb_alpha: float = 0.0
+    pair_cutoff: float = 0.0
+    cutoff_g2g: float = 0.0
+    ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
+    precision: int = A.FAU_PREC_FP32C
+    cell_capacity: int = 0
+    temperature: float = 298.15
+    name: str = ""
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    @property
+    def n_groups(self) -> int:
+        return int(self.group_flags.shape[0])
+
+    def copy(self) -> "SystemSpec":
+        import copy
+        return copy.deepcopy(self)
+
+    def to_desc(self):
+        """Build a fau_sys_desc; returns (desc, keepalive) -- keep both alive."""
+        keep = []
+
+        def f64(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return A.as_dptr(a)
+
+        def i32(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.int32)
+            keep.append(a)
+            return A.as_iptr(a)
+
+        d = A.SysDesc()
+        d.n_particles = self.n
+        d.box = (C.c_double * 3)(*[float(x) for x in self.box])
+        d.pos = f64(self.pos.reshape(-1))
+        d.charge = f64(self.charge)
+        d.type = i32(self.type)
+        d.n_groups = self.n_groups
+        d.group_begin = i32(self.group_begin)
+        d.group_molid = i32(self.group_molid)
+        d.group_flags = i32(self.group_flags)
+        d.group_mass_center = f64(None if self.mass_center is None else self.mass_center.reshape(-1))
+        d.n_types = int(self.n_types)
+        d.type_mass = f64(self.type_mass)
+        d.sigma2 = f64(None if self.sigma2 is None else self.sigma2.reshape(-1))
+        d.eps4 = f64(None if self.eps4 is None else self.eps4.reshape(-1))
+        d.hs_sigma2 = f64(None if self.hs_sigma2 is None else self.hs_sigma2.reshape(-1))
+        d.pair_terms = int(self.pair_terms)
+        d.coulomb_type = int(self.coulomb_type)
+        d.bjerrum_length = float(self.bjerrum_length)
+        d.coulomb_cutoff = float(self.coulomb_cutoff)
+        d.coulomb_alpha = float(self.coulomb_alpha)
+        d.pair_cutoff = float(self.pair_cutoff)
+        d.cutoff_g2g = float(self.cutoff_g2g)
+        if self.ewald:
+            d.ewald.enabled = 1
+            d.ewald.alpha = float(self.ewald["alpha"])
+            d.ewald.ncutoff = float(self.ewald["ncutoff"])
+            d.ewald.spherical_sum = int(self.ewald.get("spherical_sum", 1))
+            d.ewald.epss = float(self.ewald.get("epss", 0.0))
+        d.precision = int(self.precision)
+        d.cell_capacity = int(self.cell_capacity)
+        return d, keep
+
+
+class Context:
+    """One GPU, one stream, an optional HBM budget (bytes, 0 = unlimited)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._lib = A.lib()
+        h = C.c_void_p()
+        A.check(self._lib.fau_ctx_create(device, hbm_budget, C.byref(h)), "fau_ctx_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.fau_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def hbm_used(self) -> int:
+        v = C.c_size_t()
+        A.check(self._lib.fau_ctx_hbm_used(self.handle, C.byref(v)), "fau_ctx_hbm_used")
+        return int(v.value)
+
+    def create(self, spec: SystemSpec) -> "System":
+        return System(self, spec)
+
+    def run_batch(self, systems: Sequence["System"], moves=None, *, moves_per_system=None, seed: int = 1,
+                  counter_base: int = 0, dp: float = 1.0, dprot: float = 0.0, swap_interval: int = 0,
+                  n_swap_blocks: int = 0, temperatures=None, threads: int = 0, streams=None,
+                  counters=None) -> dict:
+        n = len(systems)
+        arr = (C.c_void_p * n)(*[s.handle for s in systems])
+        p = A.BatchParams()
+        p.moves = int(moves or 0)
+        keep = []
+        if moves_per_system is not None:
+            m = np.ascontiguousarray(moves_per_system, dtype=np.int64)
+            keep.append(m)
+            p.moves_per_system = m.ctypes.data_as(C.POINTER(C.c_int64))
+        p.seed = int(seed)
+        p.counter_base = int(counter_base)
+        p.dp = float(dp)
+        p.dprot = float(dprot)
+        p.swap_interval_moves = int(swap_interval)
+        p.n_swap_blocks = int(n_swap_blocks)
+        if temperatures is not None:
+            t = np.ascontiguousarray(temperatures, dtype=np.float64)
+            keep.append(t)
+            p.temperatures = A.as_dptr(t)
+        p.threads = int(threads)
+        if streams is not None:
+            sv = np.ascontiguousarray(streams, dtype=np.uint32)
+            keep.append(sv)
+            p.streams = sv.ctypes.data_as(C.POINTER(C.c_uint32))
+        if counters is not None:
+            cv = np.ascontiguousarray(counters, dtype=np.uint64)
+            keep.append(cv)
+            p.counters = cv.ctypes.data_as(C.POINTER(C.c_uint64))
+        st = A.BatchStats()
+        A.check(self._lib.fau_run_batch(self.handle, arr, n, C.byref(p), C.byref(st)), "fau_run_batch")
+        return st.as_dict()
+
+
+    def run_proposals_batch(self, systems: Sequence["System"], props: np.ndarray, offsets: np.ndarray,
+                            acc_out: Optional[np.ndarray] = None, du_out: Optional[np.ndarray] = None) -> dict:
+        """Host-fed proposals for many systems in one launch; props/acc_out/du_out
+        may live in pinned host memory (any C-contiguous buffers work)."""
+        n = len(systems)
+        arr = (C.c_void_p * n)(*[s.handle for s in systems])
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        st = A.BatchStats()
+        A.check(self._lib.fau_run_proposals_batch(
+            self.handle, arr, n, props.ctypes.data, off.ctypes.data_as(C.POINTER(C.c_int64)),
+            acc_out.ctypes.data if acc_out is not None else None,
+            A.as_dptr(du_out) if du_out is not None else None, C.byref(st)), "fau_run_proposals_batch")
+        return st.as_dict()
+
+    def fp32_peak_tflops(self) -> float:
+        v = C.c_double()
+        A.check(self._lib.fau_measure_fp32_peak(self.handle, C.byref(v)), "fau_measure_fp32_peak")
+        return float(v.value)
+
+
+def footprint(spec: SystemSpec) -> int:
+    d, keep = spec.to_desc()
+    v = C.c_size_t()
+    A.check(A.lib().fau_sys_footprint(C.byref(d), C.byref(v)), "fau_sys_footprint")
+    return int(v.value)
+
+
+class System:
+    """A Space + Hamiltonian resident on the device."""
+
+    def __init__(self, ctx: Context, spec: SystemSpec):
+        self._lib = A.lib()
+        self.ctx = ctx
+        self.spec = spec
+        d, keep = spec.to_desc()
+        h = C.c_void_p()
+        A.check(self._lib.fau_sys_create(ctx.handle, C.byref(d), C.byref(h)), "fau_sys_create")
+        self.handle = h
+        k = C.c_int()
+        A.check(self._lib.fau_sys_num_kvectors(h, C.byref(k)), "fau_sys_num_kvectors")
+        self.K = int(k.value)
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.fau_sys_destroy(self.handle)
+            self.handle = None
+
+    def energy_total(self) -> dict:
+        t = A.EnergyTerms()
+        A.check(self._lib.fau_energy_total(self.handle, C.byref(t)), "fau_energy_total")
+        return t.as_dict()
+
+    def trial_atomic(self, particle: int, dr, u: float) -> dict:
+        r = A.TrialResult()
+        drv = (C.c_double * 3)(*map(float, dr))
+        A.check(self._lib.fau_trial_atomic(self.handle, int(particle), drv, float(u), C.byref(r)), "fau_trial_atomic")
+        return r.as_dict()
+
+    def trial_group(self, group: int, dr, quat, u: float) -> dict:
+        r = A.TrialResult()
+        drv = (C.c_double * 3)(*map(float, dr))
+        q = (C.c_double * 4)(*map(float, quat))
+        A.check(self._lib.fau_trial_group(self.handle, int(group), drv, q, float(u), C.byref(r)), "fau_trial_group")
+        return r.as_dict()
+
+    def run_proposals(self, props: np.ndarray, want_acc: bool = True, want_du: bool = True):
+        props = np.ascontiguousarray(props, dtype=A.PROPOSAL_DTYPE)
+        n = len(props)
+        acc = np.zeros(n, dtype=np.uint8) if want_acc else None
+        du = np.zeros(n, dtype=np.float64) if want_du else None
+        st = A.RunStats()
+        A.check(self._lib.fau_run_proposals(self.handle, props.ctypes.data, n,
+                                            acc.ctypes.data if acc is not None else None,
+                                            A.as_dptr(du) if du is not None else None, C.byref(st)),
+                "fau_run_proposals")
+        return acc, du, st.as_dict()
+
+    def positions(self) -> np.ndarray:
+        out = np.zeros((self.spec.n, 3), dtype=np.float64)
+        A.check(self._lib.fau_get_positions(self.handle, A.as_dptr(out)), "fau_get_positions")
+        return out
+
+    def mass_centers(self) -> np.ndarray:
+        out = np.zeros((self.spec.n_groups, 3), dtype=np.float64)
+        A.check(self._lib.fau_get_mass_centers(self.handle, A.as_dptr(out)), "fau_get_mass_centers")
+        return out
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros(self.spec.n, dtype=np.int32)
+        A.check(self._lib.fau_get_cells(self.handle, A.as_iptr(out)), "fau_get_cells")
+        return out
+
+    def cell_grid(self) -> tuple:
+        out = np.zeros(3, dtype=np.int32)
+        A.check(self._lib.fau_get_cell_grid(self.handle, A.as_iptr(out)), "fau_get_cell_grid")
+        return tuple(int(x) for x in out)
+
+    def running_energy(self) -> float:
+        v = C.c_double()
+        A.check(self._lib.fau_get_running_energy(self.handle, C.byref(v)), "fau_get_running_energy")
+        return float(v.value)
+
+    def set_temperature_scale(self, scale: float) -> None:
+        A.check(self._lib.fau_set_temperature_scale(self.handle, float(scale)), "fau_set_temperature_scale")
+
+    def q(self) -> np.ndarray:
+        out = np.zeros(2 * max(self.K, 1), dtype=np.float64)
+        A.check(self._lib.fau_get_q(self.handle, A.as_dptr(out)), "fau_get_q")
+        return out[: 2 * self.K].view(np.complex128)
+
+    def q_rebuild(self) -> float:
+        v = C.c_double()
+        A.check(self._lib.fau_q_rebuild(self.handle, C.byref(v)), "fau_q_rebuild")
+        return float(v.value)
+
+
+def move_descs(spec: SystemSpec, moves: Sequence[dict]):
+    """fau_move_desc array from dicts {kind, repeat, dp, dprot, dir, groups, type_dp, type_dprot}."""
+    keep = []
+    arr = (A.MoveDesc * len(moves))()
+    for i, m in enumerate(moves):
+        g = np.ascontiguousarray(m["groups"], dtype=np.int32)
+        keep.append(g)
+        arr[i].kind = int(m["kind"])
+        arr[i].repeat = float(m["repeat"])
+        arr[i].dp = float(m.get("dp", 0.0))
+        arr[i].dprot = float(m.get("dprot", 0.0))
+        arr[i].dir = (C.c_double * 3)(*m.get("dir", (1.0, 1.0, 1.0)))
+        arr[i].n_groups = len(g)
+        arr[i].groups = A.as_iptr(g)
+        for key in ("type_dp", "type_dprot"):
+            if m.get(key) is not None:
+                t = np.ascontiguousarray(m[key], dtype=np.float64)
+                keep.append(t)
+                setattr(arr[i], key, A.as_dptr(t))
+    return arr, keep
+
+
+class MoveGenerator:
+    """Proposals drawn in the reference's RNG order (fau_movegen_*)."""
+
+    def __init__(self, spec: SystemSpec, moves: Sequence[dict], slump_seed: int = 0, random_seed: int = 0,
+                 default_seeds: bool = True):
+        self._lib = A.lib()
+        d, self._keep = spec.to_desc()
+        arr, keep2 = move_descs(spec, moves)
+        self._keep2 = (arr, keep2)
+        h = C.c_void_p()
+        A.check(self._lib.fau_movegen_create(C.byref(d), arr, len(moves), slump_seed, random_seed,
+                                             1 if default_seeds else 0, C.byref(h)), "fau_movegen_create")
+        self.handle = h
+
+    def generate(self, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=A.PROPOSAL_DTYPE)
+        A.check(self._lib.fau_movegen_generate(self.handle, out.ctypes.data, n), "fau_movegen_generate")
+        return out
+
+    def state(self) -> str:
+        buf = C.create_string_buffer(1 << 16)
+        A.check(self._lib.fau_movegen_get_state(self.handle, buf, len(buf)), "fau_movegen_get_state")
+        return buf.value.decode()
+
+    def set_state(self, s: str) -> None:
+        A.check(self._lib.fau_movegen_set_state(self.handle, s.encode()), "fau_movegen_set_state")
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.fau_movegen_destroy(self.handle)
+            self.handle = None

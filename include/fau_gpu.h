@@ -1,0 +1,301 @@
+/*
+ * fau_gpu.h -- C ABI of the GB300 Metropolis Monte Carlo energy hot path.
+ *
+ * The library replaces, for one process on one GPU, the part of Faunus that
+ * runs once per trial move:
+ *
+ *   MetropolisMonteCarlo::performMove        src/montecarlo.cpp:139-187
+ *     Hamiltonian::updateState / energy       src/energy.cpp:1227-1252
+ *       Nonbonded<...>::energy                src/energy.h:1561-1577
+ *       Ewald::updateState / energy           src/energy.cpp:564-587
+ *     getEnergyChange                         src/montecarlo.cpp:193-209
+ *     metropolisCriterion                     src/montecarlo.cpp:17-34
+ *     State::sync (accept / reject)           src/montecarlo.cpp:250-254
+ *
+ * Conventions (no exceptions cross this boundary):
+ *   - every entry point returns an int status (FAU_OK == 0);
+ *     fau_strerror() names it and fau_last_error() gives the detail text
+ *     of the last failure on the calling thread;
+ *   - handles are opaque; all pointers in descriptors are HOST pointers to
+ *     caller-owned memory that is only read during the call;
+ *   - energies are in kT at the system temperature, lengths in angstrom;
+ *   - one host thread per context: calls on the same context are serialised
+ *     by the caller (the reference is single threaded per process).
+ */
+#ifndef FAU_GPU_H
+#define FAU_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FAU_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+enum fau_status {
+    FAU_OK = 0,
+    FAU_ERR_ARG = 1,       /* invalid argument or unsupported combination       */
+    FAU_ERR_OOM = 2,       /* device allocation or HBM budget exceeded          */
+    FAU_ERR_CUDA = 3,      /* CUDA runtime error (detail in fau_last_error)     */
+    FAU_ERR_TIMEOUT = 4,   /* a bounded device wait ran out                     */
+    FAU_ERR_NAN = 5,       /* NaN energy change: metropolisCriterion throws     */
+    FAU_ERR_CAPACITY = 6,  /* a device cell-list cell overflowed                */
+    FAU_ERR_STATE = 7,     /* call not valid in the handle's current state      */
+    FAU_ERR_NODEVICE = 8   /* no CUDA device / driver                           */
+};
+
+/* ---- pair potential composition ------------------------------------------
+ * A pair energy is the sum of the enabled terms, as the reference's
+ * CombinedPairPotential (src/potentials_base.h:226-286) and
+ * FunctorPotential compositions (src/potentials.h:728-755).               */
+enum fau_pair_term {
+    FAU_PAIR_COULOMB = 1 << 0, /* lB qi qj S(r) / r                             */
+    FAU_PAIR_LJ = 1 << 1,      /* 4 eps [(s/r)^12 - (s/r)^6]   potentials.h:42-49  */
+    FAU_PAIR_WCA = 1 << 2,     /* LJ + eps, zero beyond 2^(1/6) s   :151-160     */
+    FAU_PAIR_HS = 1 << 3       /* +inf when r < s                   :203-207     */
+};
+
+/* Coulomb short-range function S(q = r/Rc) (docs/_docs/energy.md:169-205). */
+enum fau_coulomb_type {
+    FAU_COUL_PLAIN = 0, /* S = 1, no cutoff  (Coulomb potentials.h:472-476)        */
+    FAU_COUL_CUT = 1,   /* S = 1 for r < Rc, 0 beyond (poisson C=1, D=-1)         */
+    FAU_COUL_EWALD = 2  /* S = erfc(alpha r) for r < Rc, 0 beyond (kappa = 0)      */
+};
+
+/* group flags: MoleculeData::atomic / rigid (src/molecule.h:222-279) */
+enum fau_group_flag {
+    FAU_GROUP_ATOMIC = 1 << 0,
+    FAU_GROUP_RIGID = 1 << 1
+};
+
+/* arithmetic of the dU evaluation */
+enum fau_precision {
+    FAU_PREC_FP32C = 0, /* FP32 pair/Ewald terms, compensated sums, FP64 totals */
+    FAU_PREC_FP64 = 1   /* plain FP64 evaluation (in-GPU comparison form)        */
+};
+
+/* Ewald reciprocal space, EwaldData (src/energy.cpp:28-59), PBC policy. */
+typedef struct fau_ewald_desc {
+    int enabled;       /* 1: add Ewald reciprocal + surface terms             */
+    double alpha;      /* damping parameter (1/angstrom)                      */
+    double ncutoff;    /* reciprocal cutoff in units of 2 pi / L               */
+    int spherical_sum; /* 1: keep only n^2 <= ncutoff^2                        */
+    double epss;       /* surface dielectric constant; < 1 means tinfoil      */
+} fau_ewald_desc;
+
+/* A Space + Hamiltonian pair as the reference builds it from its input. */
+typedef struct fau_sys_desc {
+    int n_particles;
+    double box[3];            /* cuboid side lengths                                */
+    const double* pos;        /* n*3 xyz, each inside [-L/2, L/2] (Particle::pos)   */
+    const double* charge;     /* n (Particle::charge)                                */
+    const int* type;          /* n atom type ids in [0, n_types) (Particle::id)      */
+
+    int n_groups;
+    const int* group_begin;   /* n_groups + 1 offsets into the particle arrays       */
+    const int* group_molid;   /* n_groups molecule ids                               */
+    const int* group_flags;   /* n_groups fau_group_flag bits                        */
+    const double* group_mass_center; /* n_groups*3 Group::mass_center; NULL: computed */
+
+    int n_types;
+    const double* type_mass;  /* n_types AtomData::mw (mass centres); NULL: all 1    */
+    const double* sigma2;     /* n_types^2 LJ/WCA sigma_ij^2                         */
+    const double* eps4;       /* n_types^2 LJ/WCA 4 eps_ij in kT                     */
+    const double* hs_sigma2;  /* n_types^2 hard-sphere sigma_ij^2                    */
+
+    int pair_terms;           /* fau_pair_term bits                                  */
+    int coulomb_type;         /* fau_coulomb_type                                    */
+    double bjerrum_length;    /* lB (angstrom)                                       */
+    double coulomb_cutoff;    /* Rc of FAU_COUL_CUT / FAU_COUL_EWALD                 */
+    double coulomb_alpha;     /* alpha of FAU_COUL_EWALD real space                  */
+    double pair_cutoff;       /* > 0: every pair term is zero beyond this distance
+                                 and the device uses cell lists for single-atom
+                                 moves; <= 0: all pairs, reference semantics        */
+    double cutoff_g2g;        /* GroupCutoff mass-centre cutoff; <= 0: none          */
+    fau_ewald_desc ewald;
+
+    int precision;            /* fau_precision                                       */
+    int cell_capacity;        /* slots per cell; 0: chosen from the initial state    */
+} fau_sys_desc;
+
+/* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */
+typedef struct fau_energy_terms {
+    double self;        /* ParticleSelfEnergy                                   */
+    double nonbonded;   /* Nonbonded pair sum                                   */
+    double ewald_rec;   /* Ewald reciprocal energy                              */
+    double ewald_surf;  /* Ewald surface energy                                 */
+    double total;       /* sum as Hamiltonian::energy: ((self+nb)+ewald)        */
+} fau_energy_terms;
+
+/* Result of one trial move. */
+typedef struct fau_trial_result {
+    double du;          /* getEnergyChange(new, old) including the inf/NaN policy */
+    double du_nonbonded;/* finite parts of the change, per term                   */
+    double du_ewald;    /* reciprocal + surface                                   */
+    double err_scale;   /* sum of |term| magnitudes the change was summed from    */
+    int accepted;       /* Metropolis outcome (committed on the device if 1)      */
+    int new_inf;        /* trial energy is +inf (hard-sphere overlap)             */
+    int old_inf;        /* accepted-state energy is +inf                          */
+    int pad;
+} fau_trial_result;
+
+/* One trial move proposal, produced on the host from the reference's RNG
+ * stream (AtomicTranslateRotate::_move src/move.cpp:267-293,
+ * TranslateRotate::_move src/move.cpp:1670-1689).                          */
+enum fau_move_kind {
+    FAU_MOVE_NONE = -1,      /* empty Change: only the Metropolis draw is consumed */
+    FAU_MOVE_ATOMIC = 0,     /* translate particle `index` by dr                    */
+    FAU_MOVE_MOLECULAR = 1   /* translate group `index` by dr, then rotate by quat  */
+};
+typedef struct fau_proposal {
+    int32_t kind;       /* fau_move_kind                                           */
+    int32_t index;      /* absolute particle index or group index                  */
+    double dr[3];       /* displacement (angstrom)                                 */
+    double quat[4];     /* rotation quaternion w,x,y,z (molecular only)            */
+    double u;           /* Metropolis uniform in [0,1)                             */
+} fau_proposal;
+
+typedef struct fau_run_stats {
+    int64_t moves;          /* moves performed                                    */
+    int64_t accepted;       /* moves accepted                                     */
+    int64_t pair_evals;     /* pair interactions evaluated (old + new)            */
+    int64_t k_updates;      /* Ewald k-vector x moved-atom phase updates          */
+    double energy_change;   /* sum of accepted dU (sum_of_energy_changes)         */
+    double energy;          /* running total energy after the run                 */
+    double max_rel_err;     /* unused by the device path (set to 0)               */
+    double device_ms;       /* device time of the run (CUDA events)               */
+} fau_run_stats;
+
+/* Parameters of a batched run over many independent systems (replicas,
+ * parallel-tempering walkers or served jobs).                               */
+typedef struct fau_batch_params {
+    int64_t moves;            /* moves per system in this launch (when moves_per_system is NULL) */
+    const int64_t* moves_per_system; /* optional per-system move counts                       */
+    uint64_t seed;            /* counter-based RNG key                                    */
+    uint64_t counter_base;    /* first move counter (continue a stream across launches)   */
+    double dp;                /* translational displacement (angstrom)                    */
+    double dprot;             /* rotational displacement (rad) for molecular systems      */
+    int swap_interval_moves;  /* > 0: parallel-tempering swap after each block of this many
+                                 moves per system (odd/even partners); 0: no swaps        */
+    int n_swap_blocks;        /* number of swap blocks when swap_interval_moves > 0       */
+    const double* temperatures; /* n temperatures (K) of the PT ladder, or NULL             */
+    int threads;              /* CTA size (0: autotuned)                                   */
+    const uint32_t* streams;  /* optional per-system RNG stream ids (default: batch index)  */
+    const uint64_t* counters; /* optional per-system first move counter (default:
+                                 counter_base); a system's moves depend only on its
+                                 (seed, stream, counter), not on the rest of the batch   */
+} fau_batch_params;
+
+typedef struct fau_batch_stats {
+    int64_t moves;
+    int64_t accepted;
+    int64_t pair_evals;
+    int64_t k_updates;
+    int64_t swaps_attempted;
+    int64_t swaps_accepted;
+    double device_ms;
+} fau_batch_stats;
+
+typedef struct fau_ctx fau_ctx;
+typedef struct fau_sys fau_sys;
+
+/* ---- library ------------------------------------------------------------- */
+int fau_abi_version(void);
+const char* fau_strerror(int status);
+const char* fau_last_error(void);   /* detail of the last failure on this thread */
+
+/* ---- context: one GPU, one stream, an HBM budget ------------------------- */
+int fau_ctx_create(int device, size_t hbm_budget_bytes, fau_ctx** out);
+int fau_ctx_destroy(fau_ctx* ctx);
+int fau_ctx_hbm_used(const fau_ctx* ctx, size_t* used_bytes);
+
+/* ---- systems ------------------------------------------------------------- */
+/* Device bytes a system would hold (admission by HBM footprint). */
+int fau_sys_footprint(const fau_sys_desc* desc, size_t* bytes);
+/* Upload a Space + Hamiltonian; builds k-vectors (PolicyIonIon::updateBox,
+ * src/energy.cpp:133-186), Q(k) (updateComplex, :191-206) and cell lists. */
+int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* desc, fau_sys** out);
+int fau_sys_destroy(fau_sys* sys);
+/* Number of Ewald k-vectors (0 without Ewald). */
+int fau_sys_num_kvectors(const fau_sys* sys, int* k);
+
+/* Full energy, Change::everything (Hamiltonian::energy src/energy.cpp:1227-1241),
+ * evaluated on the device in FP64 from the resident state. */
+int fau_energy_total(fau_sys* sys, fau_energy_terms* out);
+
+/* One trial move, host-fed proposal and uniform: dU (trial minus accepted),
+ * Metropolis on u01, commit on accept. Mirrors performMove for a single
+ * transrot (src/move.cpp:267-293) or moltransrot (:1670-1689) move. */
+int fau_trial_atomic(fau_sys* sys, int particle, const double dr[3], double u01,
+                     fau_trial_result* out);
+int fau_trial_group(fau_sys* sys, int group, const double dr[3], const double quat[4],
+                    double u01, fau_trial_result* out);
+
+/* Run a stream of host-generated proposals back to back in one persistent
+ * device kernel (one CTA per chain).  accepted_out (n bytes) and du_out
+ * (n doubles) are optional host buffers. */
+int fau_run_proposals(fau_sys* sys, const fau_proposal* proposals, int n,
+                      uint8_t* accepted_out, double* du_out, fau_run_stats* stats);
+
+/* Advance n independent systems with device-generated (Philox4x32-10)
+ * proposals in one launch per swap block; PT swaps between blocks. */
+int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* params,
+                  fau_batch_stats* stats);
+
+/* Host-fed proposals for n systems in one launch (one CTA per system):
+ * proposals[offsets[i] .. offsets[i+1]) belong to systems[i].  accepted_out
+ * and du_out (optional) are indexed like proposals. */
+int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_proposal* proposals,
+                            const int64_t* offsets, uint8_t* accepted_out, double* du_out,
+                            fau_batch_stats* stats);
+
+/* Measured FP32 FMA throughput of the device (roofline denominator). */
+int fau_measure_fp32_peak(fau_ctx* ctx, double* tflops_out);
+
+/* ---- state access -------------------------------------------------------- */
+int fau_get_positions(fau_sys* sys, double* xyz_out);          /* n*3 FP64 */
+int fau_get_mass_centers(fau_sys* sys, double* xyz_out);       /* n_groups*3 */
+int fau_get_cells(fau_sys* sys, int* cell_out);                /* n cell index or -1 */
+int fau_get_cell_grid(const fau_sys* sys, int dims_out[3]);
+int fau_get_running_energy(fau_sys* sys, double* energy_out);  /* FP64 running total */
+int fau_set_temperature_scale(fau_sys* sys, double scale);     /* beta multiplier (PT) */
+/* Rebuild Q(k) in FP64 from the resident positions; returns the largest
+ * |Q_cumulative - Q_rebuilt| before replacing (drift of the running Q). */
+int fau_q_rebuild(fau_sys* sys, double* max_abs_drift_out);
+int fau_get_q(fau_sys* sys, double* q_out);                    /* K complex as 2K doubles */
+
+/* ---- host move generator (reference RNG stream) ---------------------------
+ * std::mt19937 streams `slump` (Move::slump, src/move.cpp:21) and `random`
+ * (global, src/random.cpp:62) drawn in the reference order; see
+ * MoveCollection::sample (src/move.cpp:513-526),
+ * AtomicTranslateRotate::_move (:267-293) and TranslateRotate::_move
+ * (:1670-1689); randomUnitVector src/core.cpp:249-261. */
+typedef struct fau_movegen fau_movegen;
+typedef struct fau_move_desc {
+    int kind;            /* FAU_MOVE_ATOMIC (transrot) or FAU_MOVE_MOLECULAR (moltransrot) */
+    double repeat;       /* weight in the move collection (Move::repeat)                  */
+    double dp;           /* translational displacement                                    */
+    double dprot;        /* rotational displacement (rad)                                 */
+    double dir[3];       /* translation directions                                        */
+    int n_groups;        /* candidate groups (Space::findMolecules of the molecule)       */
+    const int* groups;   /* group indices                                                 */
+    const double* type_dp;    /* n_types AtomData::dp, NaN = unset (transrot); may be NULL */
+    const double* type_dprot; /* n_types AtomData::dprot, NaN = unset; may be NULL         */
+} fau_move_desc;
+int fau_movegen_create(const fau_sys_desc* space, const fau_move_desc* moves, int n_moves,
+                       uint32_t slump_seed, uint32_t random_seed, int default_seeds,
+                       fau_movegen** out);
+int fau_movegen_destroy(fau_movegen* gen);
+/* Fill n proposals (one performMove each). */
+int fau_movegen_generate(fau_movegen* gen, fau_proposal* out, int n);
+/* Serialise / restore both engines (std::mt19937 text form, as Random::to_json). */
+int fau_movegen_get_state(const fau_movegen* gen, char* buf, size_t buflen);
+int fau_movegen_set_state(fau_movegen* gen, const char* state);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FAU_GPU_H */
