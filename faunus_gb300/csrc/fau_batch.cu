@@ -118,10 +118,12 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
 
     // device argument arrays (one allocation, freed at the end of the call)
-    const size_t off_sys = 0, off_nm = off_sys + sizeof(DevSys*) * n, off_ids = off_nm + 8 * n,
-                 off_mol = off_ids + 4 * n, off_slot = (off_mol + n + 15) & ~size_t(15), off_T = off_slot + 4 * n,
-                 off_Tref = off_T + 8 * n, off_sum = off_Tref + 8 * n,
-                 off_st = off_sum + sizeof(SysSummary) * n, off_ctr = off_st + 64, total = off_ctr + 8 * n;
+    // every sub-buffer starts on a 16-byte boundary (8-byte fields inside)
+    auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+    const size_t off_sys = 0, off_nm = al(off_sys + sizeof(DevSys*) * n), off_ids = al(off_nm + 8 * n),
+                 off_mol = al(off_ids + 4 * n), off_slot = al(off_mol + n), off_T = al(off_slot + 4 * n),
+                 off_Tref = al(off_T + 8 * n), off_sum = al(off_Tref + 8 * n),
+                 off_st = al(off_sum + sizeof(SysSummary) * n), off_ctr = al(off_st + 64), total = al(off_ctr + 8 * n);
     unsigned char* dbuf = nullptr;
     if (cudaMalloc(&dbuf, total) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
     std::vector<int> slot(n);
@@ -281,10 +283,10 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         }
     }
     if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
-    const size_t o_sys = 0, o_nm = o_sys + 8 * n, o_off = o_nm + 8 * n, o_sum = o_off + 8 * n,
-                 o_props = (o_sum + sizeof(SysSummary) * n + 255) & ~size_t(255),
-                 o_acc = o_props + sizeof(fau_proposal) * total, o_du = (o_acc + total + 255) & ~size_t(255),
-                 bytes = o_du + 8 * total;
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_sys = 0, o_nm = al(o_sys + 8 * n), o_off = al(o_nm + 8 * n), o_sum = al(o_off + 8 * n),
+                 o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * total),
+                 o_du = al(o_acc + total), bytes = al(o_du + 8 * total);
     unsigned char* dbuf = nullptr;
     if (cudaMalloc(&dbuf, bytes) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch staging allocation");
     auto done = [&](int code, const char* msg) {

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <string>
@@ -72,6 +73,7 @@ struct fau_sys {
     PlainMove* d_plain = nullptr;
     double2* d_dq = nullptr;
     double* d_res = nullptr;
+    double* d_partials = nullptr; // kTotalPartials per-block partial sums of the total energy
     int* d_flags = nullptr;
     DevSys** d_self = nullptr; // device array holding `d` (chain kernel argument)
 };
@@ -580,6 +582,7 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     // staging
     if ((rc = dev_alloc(s, &s->d_plain, 1))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_res, 8))) return bail(rc);
+    if ((rc = dev_alloc(s, &s->d_partials, kTotalPartials))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_flags, 4))) return bail(rc);
     if (lay.K > 0 && (rc = dev_alloc(s, &s->d_dq, lay.K))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d, 1))) return bail(rc);
@@ -634,16 +637,23 @@ static int pull_state(fau_sys* s)
 static int compute_total(fau_sys* s, fau_energy_terms* t)
 {
     cudaStream_t st = s->ctx->stream;
-    CUDA_TRY(cudaMemsetAsync(s->d_res, 0, 8 * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_partials, 0, kTotalPartials * sizeof(double), st));
     CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, 4 * sizeof(int), st));
-    CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_res, s->d_flags, st));
-    double r[8];
+    CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_partials, s->d_flags, st));
+    std::vector<double> part(kTotalPartials);
     int f[4];
     DevSys tmp;
-    CUDA_TRY(cudaMemcpyAsync(r, s->d_res, sizeof(r), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(part.data(), s->d_partials, kTotalPartials * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(f, s->d_flags, sizeof(f), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    // sums in block order: deterministic for a given state
+    double r[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < kTotalPairBlocks; b++) r[0] += part[b];
+    for (int b = 0; b < kTotalMiscBlocks; b++) {
+        r[1] += part[kTotalPairBlocks + 2 * b];
+        r[2] += part[kTotalPairBlocks + 2 * b + 1];
+    }
     const double inf = std::numeric_limits<double>::infinity();
     double nb = r[0];
     if (f[0] & 2) nb = std::numeric_limits<double>::quiet_NaN();

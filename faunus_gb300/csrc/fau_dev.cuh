@@ -198,40 +198,74 @@ __device__ __forceinline__ float r2_fixed(const DevSys& S, uint4 a, uint4 b)
 // ---------------------------------------------------------------- pair energy, FP32
 // Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
 // overflow set `inf` instead of adding +inf, so the compensated sums stay finite.
-__device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, float r2, bool& inf, bool& nan)
+// The terms are discontinuous at the pair cutoff, the Coulomb cutoff and the
+// hard-sphere contact; when the FP32 distance is within 1e-5 (relative) of one of
+// them, the reference FP64 distance (sqdist of the FP64 positions xi and particle
+// j) decides which side the pair is on, so inclusion matches the FP64 oracle.
+// `mag` accumulates the sum of |term| over the enabled terms (the floating-point
+// error scale of this pair energy).
+__device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int pidx, float r2, const double* xi,
+                                          int j, bool& inf, bool& nan, float& mag)
 {
-    if (S.rc2_pair > 0.f && r2 >= S.rc2_pair) return 0.f;
-    float u = 0.f;
     const int terms = S.terms;
-    const float rinv = rsqrtf(r2);
+    const bool cut_coul = (terms & FAU_PAIR_COULOMB) && S.coul_type != FAU_COUL_PLAIN;
+    bool in_pair = !(S.rc2_pair > 0.f && r2 >= S.rc2_pair);
+    bool in_coul = r2 < S.rc2_coul;
+    bool overlap = (terms & FAU_PAIR_HS) && r2 < p.hs2;
+    const bool near = (S.rc2_pair > 0.f && fabsf(r2 - S.rc2_pair) <= 1e-5f * S.rc2_pair) ||
+                      (cut_coul && fabsf(r2 - S.rc2_coul) <= 1e-5f * S.rc2_coul) ||
+                      ((terms & FAU_PAIR_HS) && fabsf(r2 - p.hs2) <= 1e-5f * p.hs2);
+    if (near) {
+        const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+        const double r2d = sqdist_d(S, xi, xj);
+        in_pair = !(S.rc2_pair_d > 0.0 && r2d >= S.rc2_pair_d);
+        in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
+        overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
+    }
+    if (!in_pair) return 0.f;
+    float u = 0.f, m = 0.f;
     if (terms & FAU_PAIR_COULOMB) {
+        float c = 0.f;
         if (S.coul_type == FAU_COUL_PLAIN) {
-            u += p.qq * rinv;
+            c = p.qq * rsqrtf(r2);
         }
-        else if (r2 < S.rc2_coul) {
-            float s = 1.f;
-            if (S.coul_type == FAU_COUL_EWALD) s = erfcf(S.alpha * (r2 * rinv));
-            u += p.qq * s * rinv;
+        else if (in_coul) {
+            if (S.coul_type == FAU_COUL_EWALD) {
+                // erfc amplifies argument errors by ~2 (alpha r)^2: correctly rounded r and 1/r
+                const float r = __fsqrt_rn(r2);
+                c = p.qq * erfcf(S.alpha * r) * __frcp_rn(r);
+            }
+            else {
+                c = p.qq * rsqrtf(r2);
+            }
         }
+        u += c;
+        m += fabsf(c);
     }
-    if (terms & FAU_PAIR_LJ) {
-        float x = p.s2 * (rinv * rinv);
+    if (terms & (FAU_PAIR_LJ | FAU_PAIR_WCA)) {
+        // (s/r)^6 from the correctly rounded 1/r^2: x^6 - x^3 cancels near the LJ
+        // minimum, so the approximate rsqrt would cost ~10x the error
+        float x = p.s2 * __frcp_rn(r2);
         x = x * x * x;
-        u += p.e4 * (x * x - x);
-    }
-    if (terms & FAU_PAIR_WCA) {
-        if (!(r2 > p.s2 * 1.2599210498948732f)) {
-            float x = p.s2 * (rinv * rinv);
-            x = x * x * x;
-            u += p.e4 * (x * x - x + 0.25f);
+        if (terms & FAU_PAIR_LJ) {
+            const float l = p.e4 * (x * x - x);
+            u += l;
+            m += fabsf(l);
+        }
+        if ((terms & FAU_PAIR_WCA) && !(r2 > p.s2 * 1.2599210498948732f)) {
+            const float w = p.e4 * (x * x - x + 0.25f);
+            u += w;
+            m += fabsf(w);
         }
     }
-    if ((terms & FAU_PAIR_HS) && r2 < p.hs2) inf = true;
+    if (overlap) inf = true;
     if (!isfinite(u)) {
         if (isnan(u) && !(p.s2 == p.s2)) nan = true; // missing coefficients (NaN sigma)
         else inf = true;                              // FP32 overflow at r -> 0
         u = 0.f;
+        m = 0.f;
     }
+    mag += m;
     return u;
 }
 

@@ -24,9 +24,11 @@ struct MoveShared {
     double du_nb, du_ew, scale;
     int new_inf, old_inf, pad0, pad1;
     float q[kMaxGroupAtoms];
+    float3 g[kMaxGroupAtoms]; // minimum-image displacement / L per moved atom (FP32, from FP64)
     uint4 rec_old[kMaxGroupAtoms];
     uint4 rec_new[kMaxGroupAtoms];
     double xn[kMaxGroupAtoms][3];
+    double xo[kMaxGroupAtoms][3];
     double cm_new[3];
     double dM[3];
     uint4 cmrec_old, cmrec_new;
@@ -160,6 +162,22 @@ __device__ __forceinline__ Proposal load_proposal(const fau_proposal& f)
     return p;
 }
 
+// (xn - xo) / L per axis under minimum image (Chameleon::vdist src/geometry.h:429-458),
+// FP64 difference rounded once to FP32: the Ewald phase increment k.(xn - xo) / 2 pi
+// of every k-vector follows from it without cancellation.
+__device__ __forceinline__ float3 min_image_frac(const DevSys& S, const double* xn, const double* xo)
+{
+    float g[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double v = __dsub_rn(xn[d], xo[d]);
+        if (v > S.half[d]) v = __dsub_rn(v, S.L[d]);
+        else if (v < -S.half[d]) v = __dadd_rn(v, S.L[d]);
+        g[d] = (float)v * (float)S.inv[d];
+    }
+    return make_float3(g[0], g[1], g[2]);
+}
+
 // Warp 0 turns a proposal into trial positions (FP64, exact) and records.
 // AtomicTranslateRotate::translateParticle (src/move.cpp:225-240);
 // Group::translate (src/group.cpp:115-123) then Group::rotate about the new
@@ -194,8 +212,10 @@ __device__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p,
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 ms.xn[0][d] = xn[d];
+                ms.xo[0][d] = xo[d];
                 ms.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
             }
+            ms.g[0] = min_image_frac(S, xn, xo);
             if (S.flags & SYS_CELLS) {
                 ms.cell_old = S.cell_of[i];
                 ms.cell_new = cell_of_pos(S, xn, rn);
@@ -238,8 +258,10 @@ __device__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p,
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 ms.xn[lane][d] = v[d];
+                ms.xo[lane][d] = xo[d];
                 dM[d] = __dmul_rn(q, __dsub_rn(v[d], xo[d]));
             }
+            ms.g[lane] = min_image_frac(S, v, xo);
         }
         // sum dM over the group's atoms in atom order (lane 0 gathers)
 #pragma unroll
@@ -275,7 +297,7 @@ __device__ __forceinline__ bool metropolis(double du, double u)
 {
     if (isinf(du) && du < 0.0) return true;
     if (-du > 709.782712893384) return true;
-    if (du <= 0.0) return true; // exp(-du) >= 1 > u
+    if (du <= 0.0 && u < 1.0) return true; // exp(-du) >= 1 > u
     const float ef = __expf((float)(-du));
     if (ef > 1e-30f) {
         if (u < (double)ef * 0.9999) return true;
@@ -341,11 +363,9 @@ __device__ __forceinline__ void block_reduce(FF& a, FF& b, float& sc, int& flags
 
 enum : int { F_NEW_INF = 1, F_OLD_INF = 2, F_NEW_NAN = 4, F_OLD_NAN = 8 };
 
-__device__ __forceinline__ void add_pair(FF& acc, float& scale, int& flags, float un, float uo, bool ni, bool oi,
-                                         bool nn, bool on)
+__device__ __forceinline__ void add_pair(FF& acc, int& flags, float un, float uo, bool ni, bool oi, bool nn, bool on)
 {
     ff_add(acc, un - uo);
-    scale += fabsf(un) + fabsf(uo);
     flags |= (ni ? F_NEW_INF : 0) | (oi ? F_OLD_INF : 0) | (nn ? F_NEW_NAN : 0) | (on ? F_OLD_NAN : 0);
 }
 
@@ -420,12 +440,18 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             for (int k = tid; k < K; k += NT) {
                 int nx, ny, nz;
                 kn_unpack(kn[k], nx, ny, nz);
+                // d = sum_a q_a (e^{i phi_new} - e^{i phi_old}) = sum_a 2 q_a sin(D/2) i e^{i(phi_old + D/2)},
+                // D = k.(r_new - r_old): no cancellation for small moves
                 float2 d = make_float2(0.f, 0.f);
                 for (int a = 0; a < m; a++) {
-                    const float2 en = eikr32(nx, ny, nz, ms.rec_new[a]);
                     const float2 eo = eikr32(nx, ny, nz, ms.rec_old[a]);
-                    d.x = fmaf(ms.q[a], en.x - eo.x, d.x);
-                    d.y = fmaf(ms.q[a], en.y - eo.y, d.y);
+                    const float3 g = ms.g[a];
+                    const float t = fmaf((float)nx, g.x, fmaf((float)ny, g.y, (float)nz * g.z)); // D/2 in units of pi
+                    float sh, ch;
+                    sincospif(t, &sh, &ch);
+                    const float f = 2.f * ms.q[a] * sh;
+                    d.x = fmaf(f, fmaf(-eo.x, sh, -eo.y * ch), d.x);
+                    d.y = fmaf(f, fmaf(eo.x, ch, -eo.y * sh), d.y);
                 }
                 dlt[k] = d;
                 const float2 qf = Qf[k], pe = pend[k];
@@ -471,14 +497,17 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                         const int cnt = S.cell_cnt[cell];
                         const uint4* cr = S.cell_rec + (size_t)cell * S.cap;
                         const uint4 ri = state ? rn : ro;
+                        const double* xi = state ? ms.xn[0] : ms.xo[0];
                         for (int s = sub; s < cnt; s += G) {
                             const uint4 rj = cr[s];
-                            if ((int)(rj.w & 0xFFFFFFu) == i) continue;
-                            const PairF p = pt[ti * nt + (rj.w >> 24)];
+                            const int j = (int)(rj.w & 0xFFFFFFu);
+                            if (j == i) continue;
+                            const int pidx = ti * nt + (rj.w >> 24);
+                            const PairF p = pt[pidx];
                             bool inf = false, nan = false;
-                            const float u = pair_u32(S, p, r2_fixed(S, ri, rj), inf, nan);
-                            if (state) add_pair(accp, scale, flags, u, 0.f, inf, false, nan, false);
-                            else add_pair(accp, scale, flags, 0.f, u, false, inf, false, nan);
+                            const float u = pair_u32(S, p, pidx, r2_fixed(S, ri, rj), xi, j, inf, nan, scale);
+                            if (state) add_pair(accp, flags, u, 0.f, inf, false, nan, false);
+                            else add_pair(accp, flags, 0.f, u, false, inf, false, nan);
                             n_pairs++;
                         }
                     }
@@ -487,11 +516,12 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     for (int j = tid; j < S.n; j += NT) {
                         if (j == i) continue;
                         const uint4 rj = S.rec[j];
-                        const PairF p = pt[ti * nt + (rj.w >> 24)];
+                        const int pidx = ti * nt + (rj.w >> 24);
+                        const PairF p = pt[pidx];
                         bool ni = false, nn = false, oi = false, on = false;
-                        const float un = pair_u32(S, p, r2_fixed(S, rn, rj), ni, nn);
-                        const float uo = pair_u32(S, p, r2_fixed(S, ro, rj), oi, on);
-                        add_pair(accp, scale, flags, un, uo, ni, oi, nn, on);
+                        const float un = pair_u32(S, p, pidx, r2_fixed(S, rn, rj), ms.xn[0], j, ni, nn, scale);
+                        const float uo = pair_u32(S, p, pidx, r2_fixed(S, ro, rj), ms.xo[0], j, oi, on, scale);
+                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
                         n_pairs += 2;
                     }
                 }
@@ -510,11 +540,16 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                         const uint4 rb = S.rec[b];
                         const int tb = rb.w >> 24;
                         for (int a = 0; a < m; a++) {
-                            const PairF p = pt[(ms.rec_new[a].w >> 24) * nt + tb];
+                            const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                            const PairF p = pt[pidx];
                             bool ni = false, nn = false, oi = false, on = false;
-                            const float un = cut_n ? 0.f : pair_u32(S, p, r2_fixed(S, ms.rec_new[a], rb), ni, nn);
-                            const float uo = cut_o ? 0.f : pair_u32(S, p, r2_fixed(S, ms.rec_old[a], rb), oi, on);
-                            add_pair(accp, scale, flags, un, uo, ni, oi, nn, on);
+                            const float un = cut_n ? 0.f
+                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b,
+                                                              ni, nn, scale);
+                            const float uo = cut_o ? 0.f
+                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b,
+                                                              oi, on, scale);
+                            add_pair(accp, flags, un, uo, ni, oi, nn, on);
                             n_pairs += (cut_n ? 0 : 1) + (cut_o ? 0 : 1);
                         }
                     }
@@ -524,11 +559,14 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     const uint4 rb = S.rec[b];
                     const int tb = rb.w >> 24;
                     for (int a = 0; a < m; a++) {
-                        const PairF p = pt[(ms.rec_new[a].w >> 24) * nt + tb];
+                        const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                        const PairF p = pt[pidx];
                         bool ni = false, nn = false, oi = false, on = false;
-                        const float un = pair_u32(S, p, r2_fixed(S, ms.rec_new[a], rb), ni, nn);
-                        const float uo = pair_u32(S, p, r2_fixed(S, ms.rec_old[a], rb), oi, on);
-                        add_pair(accp, scale, flags, un, uo, ni, oi, nn, on);
+                        const float un =
+                            pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b, ni, nn, scale);
+                        const float uo =
+                            pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b, oi, on, scale);
+                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
                         n_pairs += 2;
                     }
                 }
@@ -764,10 +802,10 @@ __global__ void total_pair_kernel(const DevSys* Sp, double* out, int* flags)
     }
     const double s = block_sum_d(e, red);
     if (f) atomicOr(flags, f);
-    if (threadIdx.x == 0) atomicAdd(out, s);
+    if (threadIdx.x == 0) out[blockIdx.x] = s; // per-block partial: summed in block order on the host
 }
 
-// out[0] = sum_k A_k |Q_k|^2, out[1] = sum_i self(i)
+// out[2b] = sum_k A_k |Q_k|^2, out[2b+1] = sum_i self(i), per block b
 __global__ void total_misc_kernel(const DevSys* Sp, double* out)
 {
     const DevSys& S = *Sp;
@@ -784,29 +822,31 @@ __global__ void total_misc_kernel(const DevSys* Sp, double* out)
     const double te = block_sum_d(e, red);
     const double ts = block_sum_d(s, red);
     if (threadIdx.x == 0) {
-        atomicAdd(out, te);
-        atomicAdd(out + 1, ts);
+        out[2 * blockIdx.x] = te;
+        out[2 * blockIdx.x + 1] = ts;
     }
 }
 
 // ---------------------------------------------------------------- FP64 Q(k) rebuild
-// Q_k = sum_j q_j e^{i k.r_j}; the phase n.u mod 2^32 of the fixed-point record is
-// exact, so sincospi of it in FP64 is exact to rounding.  One CTA per k-block.
+// Q_k = sum_j q_j e^{i k.r_j} from the FP64 master positions with k = 2 pi n / L
+// and k.r = (kx x + ky y) + kz z, as PolicyIonIon::updateComplex
+// (src/energy.cpp:191-206).  One CTA per k.
 __global__ void q_rebuild_kernel(const DevSys* Sp, double2* out)
 {
     const DevSys& S = *Sp;
     __shared__ double rx[32], ry[32];
+    const double twopi = 6.283185307179586476925286766559;
     for (int k = blockIdx.x; k < S.K; k += gridDim.x) {
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
+        const double kx = twopi * ((double)nx / S.L[0]), ky = twopi * ((double)ny / S.L[1]),
+                     kz = twopi * ((double)nz / S.L[2]);
         double sx = 0.0, sy = 0.0;
         for (int j = threadIdx.x; j < S.n; j += blockDim.x) {
-            const uint4 r = S.rec[j];
-            const uint32_t ph = (uint32_t)nx * r.x + (uint32_t)ny * r.y + (uint32_t)nz * r.z;
-            const double t = (double)(int32_t)ph * 4.656612873077392578125e-10; // 2^-31, exact
+            const double ph = __dadd_rn(__dadd_rn(__dmul_rn(kx, S.x[j]), __dmul_rn(ky, S.y[j])), __dmul_rn(kz, S.z[j]));
             double s, c;
-            sincospi(t, &s, &c);
-            const double q = S.itype_qd[r.w >> 24];
+            sincos(ph, &s, &c);
+            const double q = S.itype_qd[S.rec[j].w >> 24];
             sx += q * c;
             sy += q * s;
         }
@@ -1021,14 +1061,17 @@ cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int threads, bo
     }
 }
 
+// Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then
+// 2 * kTotalMiscBlocks (reciprocal, self) pairs; unused blocks write nothing, so
+// the caller zeroes the buffer first.  Deterministic: no floating-point atomics.
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st)
 {
-    int blocks = n < 4096 ? (n > 0 ? n : 1) : 4096;
+    int blocks = n < kTotalPairBlocks ? (n > 0 ? n : 1) : kTotalPairBlocks;
     total_pair_kernel<<<blocks, 256, 0, st>>>(dsys, d_out, d_flags);
     int kb = (K + n + 255) / 256;
     if (kb < 1) kb = 1;
-    if (kb > 1024) kb = 1024;
-    total_misc_kernel<<<kb, 256, 0, st>>>(dsys, d_out + 1);
+    if (kb > kTotalMiscBlocks) kb = kTotalMiscBlocks;
+    total_misc_kernel<<<kb, 256, 0, st>>>(dsys, d_out + kTotalPairBlocks);
     return cudaGetLastError();
 }
 

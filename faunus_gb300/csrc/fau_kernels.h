@@ -37,6 +37,10 @@ struct PlainMove {
     double du;
 };
 
+constexpr int kTotalPairBlocks = 4096;
+constexpr int kTotalMiscBlocks = 1024;
+constexpr int kTotalPartials = kTotalPairBlocks + 2 * kTotalMiscBlocks;
+
 size_t chain_smem_bytes(int K);
 cudaError_t prepare_chain(int K, int threads, bool philox);
 cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int threads, bool philox, cudaStream_t st);

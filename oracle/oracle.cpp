@@ -137,6 +137,19 @@ struct PairParams {
             u += (r2 < hs2[ab]) ? infty : 0.0;
         return u;
     }
+    // sum of |term| over the enabled terms: the floating-point error scale of a pair energy
+    double magnitude(int ta, int tb, double qa, double qb, double r2) const
+    {
+        if (pair_cutoff2 > 0.0 && r2 >= pair_cutoff2) return 0.0;
+        const size_t ab = size_t(ta) * n_types + tb;
+        double m = 0.0;
+        if (terms & FAU_PAIR_COULOMB) m += std::fabs(coulomb(qa, qb, r2));
+        double x = sigma2[ab] / r2;
+        x = x * x * x;
+        if (terms & FAU_PAIR_LJ) m += std::fabs(eps4[ab] * (x * x - x));
+        if ((terms & FAU_PAIR_WCA) && !(r2 > sigma2[ab] * 1.2599210498948732)) m += std::fabs(eps4[ab] * (x * x - x + 0.25));
+        return std::isfinite(m) ? m : 0.0;
+    }
     // self energy per particle (NewCoulombGalore::setSelfEnergy src/potentials.cpp:1599-1604)
     bool has_self() const { return (terms & FAU_PAIR_COULOMB) && coul_type != FAU_COUL_PLAIN; }
     double self(double q) const
@@ -337,6 +350,7 @@ struct System {
         return box.sqdist(cm[g1], cm[g2]) >= cutoff_g2g2;
     }
     double u(int i, int j) const { return pair(type[i], type[j], q[i], q[j], box.sqdist(pos[i], pos[j])); }
+    double mag(int i, int j) const { return pair.magnitude(type[i], type[j], q[i], q[j], box.sqdist(pos[i], pos[j])); }
     double u_at(const Vec3& ri, int ti, double qi, int j) const
     {
         return pair(ti, type[j], qi, q[j], box.sqdist(ri, pos[j]));
@@ -488,6 +502,20 @@ struct TrialOut {
     int accepted = 0, new_inf = 0, old_inf = 0, nan = 0;
 };
 
+// magnitude of the terms the reciprocal-energy change is summed from:
+// (2 pi lB / V) sum_k A_k (|2 Re(conj(Q_old) d)| + |d|^2), d = Q_new - Q_old
+static double ewaldScale(const System& s, const std::vector<std::complex<double>>& Qold)
+{
+    if (!s.ewald.enabled) return 0.0;
+    double e = 0.0;
+    for (size_t k = 0; k < Qold.size(); k++) {
+        const std::complex<double> d = s.ewald.Q[k] - Qold[k];
+        const double cross = 2.0 * (Qold[k].real() * d.real() + Qold[k].imag() * d.imag());
+        e += s.ewald.Ak[k] * (std::fabs(cross) + std::norm(d));
+    }
+    return 2 * pi * e * s.ewald.lB / s.box.volume();
+}
+
 static TrialOut trialAtom(System& s, int i, const Vec3& dr, double u01)
 {
     TrialOut out;
@@ -501,10 +529,7 @@ static TrialOut trialAtom(System& s, int i, const Vec3& dr, double u01)
     auto addScale = [&]() {
         if (!s.want_scale) return;
         for (int j = 0; j < (int)s.pos.size(); j++)
-            if (j != i) {
-                double a = s.u(i, j);
-                if (std::isfinite(a)) scale += std::fabs(a);
-            }
+            if (j != i) scale += s.mag(i, j);
     };
     addScale();
     std::vector<std::complex<double>> Qacc = s.ewald.Q;
@@ -512,6 +537,7 @@ static TrialOut trialAtom(System& s, int i, const Vec3& dr, double u01)
     if (s.ewald.enabled) s.ewald.partialQ({np}, {old}, {s.q[i]}); // Ewald::updateState (trial)
     const Terms en = energyOf(s, CH_ATOM, i);
     addScale();
+    if (s.want_scale) scale += ewaldScale(s, Qacc);
     out.du = getEnergyChange(en.total, eo.total);
     out.du_nb = en.nb - eo.nb;
     out.du_ew = (en.rec + en.surf) - (eo.rec + eo.surf);
@@ -570,10 +596,7 @@ static TrialOut trialGroup(System& s, int g, const Vec3& dr, const Quat* q, doub
         for (size_t h = 0; h < s.groups.size(); h++) {
             if ((int)h == g || s.cut(g, (int)h)) continue;
             for (int i = G.begin; i < G.end; i++)
-                for (int j = s.groups[h].begin; j < s.groups[h].end; j++) {
-                    double a = s.u(i, j);
-                    if (std::isfinite(a)) scale += std::fabs(a);
-                }
+                for (int j = s.groups[h].begin; j < s.groups[h].end; j++) scale += s.mag(i, j);
         }
     };
     addScale();
@@ -586,6 +609,7 @@ static TrialOut trialGroup(System& s, int g, const Vec3& dr, const Quat* q, doub
     }
     const Terms en = energyOf(s, CH_GROUP, g);
     addScale();
+    if (s.want_scale) scale += ewaldScale(s, Qacc);
     out.du = getEnergyChange(en.total, eo.total);
     out.du_nb = en.nb - eo.nb;
     out.du_ew = (en.rec + en.surf) - (eo.rec + eo.surf);
