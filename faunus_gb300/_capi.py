@@ -145,6 +145,8 @@ def _declare(lib: C.CDLL) -> None:
         "fau_trial_atomic": ([P, C.c_int, dptr, C.c_double, C.POINTER(TrialResult)], C.c_int),
         "fau_trial_group": ([P, C.c_int, dptr, dptr, C.c_double, C.POINTER(TrialResult)], C.c_int),
         "fau_run_proposals": ([P, P, C.c_int, P, dptr, C.POINTER(RunStats)], C.c_int),
+        "fau_energy_change": ([P, C.POINTER(Proposal), C.POINTER(TrialResult)], C.c_int),
+        "fau_commit_pending": ([P, C.c_int], C.c_int),
         "fau_run_batch": ([P, C.POINTER(P), C.c_int, C.POINTER(BatchParams), C.POINTER(BatchStats)], C.c_int),
         "fau_run_proposals_batch": ([P, C.POINTER(P), C.c_int, P, C.POINTER(C.c_int64), P, dptr,
                                      C.POINTER(BatchStats)], C.c_int),

@@ -76,6 +76,7 @@ struct fau_sys {
     double* d_partials = nullptr; // kTotalPartials per-block partial sums of the total energy
     int* d_flags = nullptr;
     DevSys** d_self = nullptr; // device array holding `d` (chain kernel argument)
+    bool pending = false;      // a fau_energy_change trial waits for fau_commit_pending
 };
 
 template <class T>
@@ -904,6 +905,7 @@ static int plain_trial(fau_sys* s, int kind, int index, const double dr[3], cons
     cudaStream_t st = s->ctx->stream;
     PlainMove pm{};
     pm.kind = kind;
+    pm.count_move = 1;
     const DevSys& h = s->h;
     std::vector<double> xo;
     std::vector<double> qs;
@@ -1094,6 +1096,63 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
     return FAU_OK;
 }
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int fau_energy_change(fau_sys* s, const fau_proposal* p, fau_trial_result* out)
+{
+    if (!s || !p) return fail(FAU_ERR_ARG, "null argument");
+    if (s->pending) return fail(FAU_ERR_STATE, "a pending trial must be committed or rejected first");
+    if (p->kind != FAU_MOVE_ATOMIC && p->kind != FAU_MOVE_MOLECULAR)
+        return fail(FAU_ERR_ARG, "fau_energy_change needs an atomic or molecular proposal");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    if (p->kind == FAU_MOVE_ATOMIC) {
+        if (p->index < 0 || p->index >= s->n) return fail(FAU_ERR_ARG, "particle out of range");
+        if (!(s->g_flags[s->group_of[p->index]] & FAU_GROUP_ATOMIC))
+            return fail(FAU_ERR_ARG, "single-atom move inside a molecular group is not supported");
+    }
+    else {
+        if (p->index < 0 || p->index >= s->n_groups) return fail(FAU_ERR_ARG, "group out of range");
+        if (s->g_flags[p->index] & FAU_GROUP_ATOMIC) return fail(FAU_ERR_ARG, "molecular move of an atomic group");
+        if (s->g_begin[p->index + 1] - s->g_begin[p->index] > kMaxGroupAtoms)
+            return fail(FAU_ERR_ARG, "group larger than %d atoms", kMaxGroupAtoms);
+    }
+    int rc = ensure_stage(s, 1);
+    if (rc) return rc;
+    cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(cudaMemcpyAsync(s->d_props, p, sizeof(fau_proposal), cudaMemcpyHostToDevice, st));
+    ChainArgs a{};
+    a.sys = s->d_self;
+    a.moves = 1;
+    a.props = s->d_props;
+    a.detail = s->d_detail;
+    a.pending = s->d_plain;
+    a.pending_dq = s->K ? s->d_dq : nullptr;
+    CUDA_TRY(launch_chain(a, 1, s->K, chain_threads(s), false, st));
+    fau_trial_result r{};
+    CUDA_TRY(cudaMemcpyAsync(&r, s->d_detail, sizeof(r), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if ((rc = check_device_err(s))) return rc;
+    r.accepted = 0;
+    if (out) *out = r;
+    s->pending = true;
+    return FAU_OK;
+}
+
+int fau_commit_pending(fau_sys* s, int accept)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null argument");
+    if (!s->pending) return fail(FAU_ERR_STATE, "no pending trial");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    s->pending = false;
+    cudaStream_t st = s->ctx->stream;
+    if (accept) {
+        CUDA_TRY(launch_plain_commit(s->d, s->d_plain, s->K, s->d_dq, st));
+    }
+    // a rejected trial needs no device work: the accepted state was never modified
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const int rc = check_device_err(s);
+    if (rc == FAU_ERR_CAPACITY) return rebuild_cells(s, 2 * s->h.cap);
+    return rc;
+}
 
 int fau_get_positions(fau_sys* s, double* xyz)
 {

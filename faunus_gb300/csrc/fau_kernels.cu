@@ -595,7 +595,23 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 const double fin = du_nb + (du_rec + du_surf);
                 du = energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
                 const double x = du * S.beta_scale;
-                if (isnan(x)) {
+                if (A.pending) {
+                    // evaluate only: hand the trial to the caller's Metropolis
+                    PlainMove& P = *A.pending;
+                    P.kind = kind;
+                    P.first = ms.first;
+                    P.m = m;
+                    P.group = kind == FAU_MOVE_MOLECULAR ? ms.index : -1;
+                    P.count_move = 0;
+                    for (int a = 0; a < m; a++)
+                        for (int d = 0; d < 3; d++) P.xn[a][d] = ms.xn[a][d];
+                    for (int d = 0; d < 3; d++) {
+                        P.cm_new[d] = ms.cm_new[d];
+                        P.dM[d] = ms.dM[d];
+                    }
+                    P.du = du;
+                }
+                else if (isnan(x)) {
                     err = FAU_ERR_NAN;
                     ms.stop = FAU_ERR_NAN;
                 }
@@ -632,6 +648,9 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             err = ms.stop;
             break;
         }
+
+        if (A.pending_dq) // evaluate only: the trial's Q(k) change for a later commit
+            for (int k = tid; k < K; k += NT) A.pending_dq[k] = make_double2((double)dlt[k].x, (double)dlt[k].y);
 
         // ---- 4. commit on accept (State::sync trial -> accepted)
         if (ms.accept) {
@@ -1008,7 +1027,7 @@ __global__ void plain_commit_kernel(DevSys* Sp, const PlainMove* P, const double
         }
         for (int d = 0; d < 3; d++) S.M[d] += P->dM[d];
         S.energy += P->du;
-        S.moves += 1;
+        S.moves += P->count_move;
         S.accepted += 1;
         S.sum_du += P->du;
     }

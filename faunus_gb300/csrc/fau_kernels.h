@@ -26,11 +26,16 @@ struct ChainArgs {
     const unsigned long long* counters; // per CTA first counter (NULL: counter_base)
     double dp, dprot;
     const uint8_t* molecular;    // per CTA: 1 -> moltransrot moves, 0 -> transrot
+    // evaluate-only mode (one move, one CTA): no Metropolis, no commit; the trial is
+    // written to `pending` and its Q(k) change to `pending_dq` for a later commit
+    struct PlainMove* pending;
+    double2* pending_dq;
 };
 
-// One plain FP64 trial move (host-computed trial positions).
+// One trial move held for a later commit (plain FP64 form and evaluate-only mode).
 struct PlainMove {
     int kind, first, m, group;
+    int count_move, pad; // 1: the commit also counts the move (plain form); 0: already counted
     double xn[32][3];
     double cm_new[3];
     double dM[3];

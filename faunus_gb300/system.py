@@ -260,6 +260,21 @@ class System:
         A.check(self._lib.fau_trial_group(self.handle, int(group), drv, q, float(u), C.byref(r)), "fau_trial_group")
         return r.as_dict()
 
+    def energy_change(self, proposal) -> dict:
+        """Evaluate one trial (kept pending on the device); see commit()."""
+        p = A.Proposal()
+        p.kind = int(proposal["kind"])
+        p.index = int(proposal["index"])
+        p.dr = (C.c_double * 3)(*map(float, proposal["dr"]))
+        p.quat = (C.c_double * 4)(*map(float, proposal["quat"]))
+        p.u = float(proposal["u"])
+        r = A.TrialResult()
+        A.check(self._lib.fau_energy_change(self.handle, C.byref(p), C.byref(r)), "fau_energy_change")
+        return r.as_dict()
+
+    def commit(self, accept: bool) -> None:
+        A.check(self._lib.fau_commit_pending(self.handle, 1 if accept else 0), "fau_commit_pending")
+
     def run_proposals(self, props: np.ndarray, want_acc: bool = True, want_du: bool = True):
         props = np.ascontiguousarray(props, dtype=A.PROPOSAL_DTYPE)
         n = len(props)

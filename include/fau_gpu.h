@@ -234,6 +234,15 @@ int fau_trial_atomic(fau_sys* sys, int particle, const double dr[3], double u01,
 int fau_trial_group(fau_sys* sys, int group, const double dr[3], const double quat[4],
                     double u01, fau_trial_result* out);
 
+/* Two-phase form of one trial move for an EnergyTerm-level integration, where
+ * the caller's MetropolisMonteCarlo decides: fau_energy_change evaluates the
+ * trial (Hamiltonian::updateState + energy of both states, src/energy.cpp:
+ * 1227-1252) and keeps it pending on the device; fau_commit_pending(accept=1)
+ * is State::sync trial -> accepted, accept=0 is accepted -> trial (the device
+ * accepted state was never modified).  One pending move per system. */
+int fau_energy_change(fau_sys* sys, const fau_proposal* proposal, fau_trial_result* out);
+int fau_commit_pending(fau_sys* sys, int accept);
+
 /* Run a stream of host-generated proposals back to back in one persistent
  * device kernel (one CTA per chain).  accepted_out (n bytes) and du_out
  * (n doubles) are optional host buffers. */

@@ -329,3 +329,29 @@ def test_parallel_tempering_swaps(ctx):
         e_run = s.running_energy()
         e_tot = s.energy_total()["total"]
         assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot))
+
+
+# ---------------------------------------------------------------- two-phase (EnergyTerm-level) form
+def test_energy_change_then_commit_matches_oracle(ctx):
+    """The caller decides: evaluate, draw Metropolis on the host, commit or drop."""
+    for spec in (configs.bulk_ewald(n_salt=500), configs.spce_water(n_mol=256, L=18.6)):
+        g = ctx.create(spec)
+        o = O.OracleSystem(spec)
+        props = _props(spec, 300)
+        for p in props:
+            if p["kind"] == A.FAU_MOVE_NONE:
+                continue
+            r = g.energy_change(p)
+            ro = (o.trial_atomic(p["index"], p["dr"], p["u"]) if p["kind"] == A.FAU_MOVE_ATOMIC
+                  else o.trial_group(p["index"], p["dr"], p["quat"], p["u"]))
+            assert abs(r["du"] - ro["du"]) <= TOL_FP32C * max(abs(ro["du"]), ro["err_scale"])
+            accept = (not math.isnan(r["du"])) and (r["du"] == -math.inf or p["u"] <= math.exp(-min(r["du"], 700)))
+            assert bool(accept) == bool(ro["accepted"])
+            g.commit(accept)
+        assert np.array_equal(g.positions(), o.positions())
+        e_run = g.running_energy()
+        g.q_rebuild()
+        assert abs(e_run - g.energy_total()["total"]) <= 1e-6 * abs(e_run)
+        with pytest.raises(F.FauError) as e:
+            g.commit(True)
+        assert e.value.status == A.FAU_ERR_STATE
