@@ -174,9 +174,9 @@ def cpu_baseline(spec, seconds_per_thread: float = 1.0, threads: int | None = No
 
 
 def run_reference(args) -> None:
-    dist, rank, local, world = _dist_init(args.gpus)
+    # rank 0 alone runs the CPU reference; the other ranks exit without work
+    rank, _, _ = _env_rank()
     if rank != 0:
-        _barrier(dist)
         return
     from faunus_gb300 import configs
     spec = configs.bulk_ewald(n_salt=10000, seed=1)
@@ -204,7 +204,6 @@ def run_reference(args) -> None:
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
-    _barrier(dist)
 
 
 def run_ours(args) -> None:
@@ -218,7 +217,8 @@ def run_ours(args) -> None:
     sms = _sm_count(local)
     R = args.replicas or 2 * sms
     M = args.moves
-    systems = [ctx.create(base) for _ in range(R)]
+    first = ctx.create(base)
+    systems = [first] + [first.clone() for _ in range(R - 1)]
     streams = np.arange(R, dtype=np.uint32) + 1_000_000 * rank
     resident = ctx.hbm_used()
 
@@ -244,6 +244,14 @@ def run_ours(args) -> None:
     acc = sum(s["accepted"] for s in stats)
     tot_moves = _sum_over_ranks(dist, moves)
     value = tot_moves / dev_s
+
+    if args.value_only:
+        if rank == 0:
+            print(json.dumps({"metric": "MC trial moves/sec", "value": value, "unit": "moves/s",
+                              "ms_per_step": 1e3 * dev_s / args.steps, "replicas": R, "moves": M}), flush=True)
+        ctx.close()
+        _barrier(dist)
+        return
 
     # ---- e2e: reference-stream proposals through the C ABI, host buffers
     gens = [F.MoveGenerator(base, base.extra["moves"], 7 + i, 11 + i, default_seeds=False) for i in range(R)]
@@ -345,10 +353,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--replicas", type=int, default=0, help="replica chains per GPU (0: 2 x SMs)")
-    ap.add_argument("--moves", type=int, default=2000, help="moves per replica per step")
+    ap.add_argument("--moves", type=int, default=10000, help="moves per replica per step")
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -140,6 +140,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_sys_footprint": ([C.POINTER(SysDesc), C.POINTER(C.c_size_t)], C.c_int),
         "fau_sys_create": ([P, C.POINTER(SysDesc), C.POINTER(P)], C.c_int),
         "fau_sys_destroy": ([P], C.c_int),
+        "fau_sys_clone": ([P, C.POINTER(P)], C.c_int),
         "fau_sys_num_kvectors": ([P, iptr], C.c_int),
         "fau_energy_total": ([P, C.POINTER(EnergyTerms)], C.c_int),
         "fau_trial_atomic": ([P, C.c_int, dptr, C.c_double, C.POINTER(TrialResult)], C.c_int),

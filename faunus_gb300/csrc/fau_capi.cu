@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -58,6 +59,7 @@ struct fau_sys {
     DevSys h{};                 // host mirror of the device struct (pointers are device pointers)
     DevSys* d = nullptr;        // device copy
     std::vector<void*> allocs;
+    std::vector<size_t> alloc_bytes;
     size_t bytes = 0;
     int n = 0, n_groups = 0, K = 0;
     bool cells = false, molecular_only = false;
@@ -88,6 +90,7 @@ static int dev_alloc(fau_sys* s, T** p, size_t count)
     void* v = nullptr;
     CUDA_TRY(cudaMalloc(&v, b));
     s->allocs.push_back(v);
+    s->alloc_bytes.push_back(b);
     s->bytes += b;
     s->ctx->used += b;
     *p = static_cast<T*>(v);
@@ -107,6 +110,7 @@ static void free_sys(fau_sys* s)
     for (void* p : s->allocs) cudaFree(p);
     if (s->ctx) s->ctx->used -= std::min(s->ctx->used, s->bytes);
     s->allocs.clear();
+    s->alloc_bytes.clear();
     s->bytes = 0;
 }
 
@@ -597,6 +601,77 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
             return bail(fail(FAU_ERR_CUDA, "q rebuild launch failed"));
     }
     if ((rc = refresh_energy(s))) return bail(rc);
+    *out = s;
+    return FAU_OK;
+}
+
+// Deep copy of a resident system: every device array is copied device to device and
+// every device pointer of the copy is re-pointed into the copy's own arrays.  As the
+// reference builds its trial state as a second State from the same input
+// (src/montecarlo.cpp:101-111), this builds replicas and served jobs that share an
+// initial state without re-uploading or re-evaluating it.
+int fau_sys_clone(const fau_sys* src, fau_sys** out)
+{
+    if (!src || !out) return fail(FAU_ERR_ARG, "null argument");
+    if (src->pending) return fail(FAU_ERR_STATE, "clone of a system with a pending trial");
+    fau_ctx* ctx = src->ctx;
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    fau_sys* s = new fau_sys(*src);
+    s->allocs.clear();
+    s->alloc_bytes.clear();
+    s->bytes = 0;
+    auto bail = [&](int code) {
+        cudaStreamSynchronize(ctx->stream);
+        free_sys(s);
+        delete s;
+        return code;
+    };
+    std::vector<std::pair<char*, char*>> remap; // (src base, dst base) with sizes from src
+    for (size_t a = 0; a < src->allocs.size(); a++) {
+        char* dst = nullptr;
+        int rc = dev_alloc(s, &dst, src->alloc_bytes[a]);
+        if (rc) return bail(rc);
+        if (cudaMemcpyAsync(dst, src->allocs[a], src->alloc_bytes[a], cudaMemcpyDeviceToDevice, ctx->stream) !=
+            cudaSuccess)
+            return bail(fail(FAU_ERR_CUDA, "clone copy failed"));
+        remap.emplace_back(static_cast<char*>(src->allocs[a]), dst);
+    }
+    auto fix = [&](auto*& ptr) {
+        if (!ptr) return;
+        char* p = reinterpret_cast<char*>(ptr);
+        for (size_t a = 0; a < remap.size(); a++) {
+            char* b = remap[a].first;
+            if (p >= b && p < b + src->alloc_bytes[a]) {
+                ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(remap[a].second + (p - b));
+                return;
+            }
+        }
+    };
+    DevSys& h = s->h;
+    fix(h.x); fix(h.y); fix(h.z); fix(h.rec); fix(h.group_of); fix(h.itype_q); fix(h.itype_qd); fix(h.itype_self);
+    fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
+    fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
+    fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
+    fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);
+    // the copy's device struct: running fields from the source's device struct, pointers from h
+    DevSys cur;
+    if (cudaMemcpyAsync(&cur, src->d, sizeof(DevSys), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return bail(fail(FAU_ERR_CUDA, "clone state read failed"));
+    DevSys nd = h;
+    nd.energy = cur.energy;
+    nd.beta_scale = cur.beta_scale;
+    for (int k = 0; k < 3; k++) nd.M[k] = cur.M[k];
+    nd.cap = cur.cap;
+    nd.err = 0;
+    nd.moves = nd.accepted = nd.pair_evals = nd.k_updates = 0;
+    nd.sum_du = 0.0;
+    h = nd;
+    if (cudaMemcpyAsync(s->d, &nd, sizeof(DevSys), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(s->d_self, &s->d, sizeof(DevSys*), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return bail(fail(FAU_ERR_CUDA, "clone descriptor upload failed"));
     *out = s;
     return FAU_OK;
 }

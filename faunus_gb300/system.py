@@ -242,6 +242,14 @@ class System:
             self._lib.fau_sys_destroy(self.handle)
             self.handle = None
 
+    def clone(self) -> "System":
+        """Device-to-device deep copy (same context)."""
+        h = C.c_void_p()
+        A.check(self._lib.fau_sys_clone(self.handle, C.byref(h)), "fau_sys_clone")
+        other = System.__new__(System)
+        other._lib, other.ctx, other.spec, other.handle, other.K = self._lib, self.ctx, self.spec, h, self.K
+        return other
+
     def energy_total(self) -> dict:
         t = A.EnergyTerms()
         A.check(self._lib.fau_energy_total(self.handle, C.byref(t)), "fau_energy_total")

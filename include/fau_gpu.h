@@ -219,6 +219,10 @@ int fau_sys_footprint(const fau_sys_desc* desc, size_t* bytes);
  * src/energy.cpp:133-186), Q(k) (updateComplex, :191-206) and cell lists. */
 int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* desc, fau_sys** out);
 int fau_sys_destroy(fau_sys* sys);
+/* Deep device-to-device copy of a resident system in the same context (as the
+ * reference builds a second State from one input, src/montecarlo.cpp:101-111):
+ * replicas and jobs that share an initial state.  Counters start at zero. */
+int fau_sys_clone(const fau_sys* src, fau_sys** out);
 /* Number of Ewald k-vectors (0 without Ewald). */
 int fau_sys_num_kvectors(const fau_sys* sys, int* k);
 

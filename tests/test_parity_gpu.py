@@ -355,3 +355,16 @@ def test_energy_change_then_commit_matches_oracle(ctx):
         with pytest.raises(F.FauError) as e:
             g.commit(True)
         assert e.value.status == A.FAU_ERR_STATE
+
+
+def test_clone_is_an_independent_copy(ctx):
+    spec = configs.bulk_ewald(n_salt=500)
+    a = ctx.create(spec)
+    b = a.clone()
+    assert np.array_equal(a.positions(), b.positions())
+    assert a.running_energy() == b.running_energy()
+    ctx.run_batch([a], 500, seed=1, streams=[3], threads=256)
+    assert not np.array_equal(a.positions(), b.positions())
+    ctx.run_batch([b], 500, seed=1, streams=[3], threads=256)
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.q(), b.q()) and np.array_equal(a.cells(), b.cells())
