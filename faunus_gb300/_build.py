@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libfau_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fau_kernels.cu", "fau_capi.cu", "fau_batch.cu", "fau_movegen.cpp"]
+SOURCES = ["fau_kernels.cu", "fau_capi.cu", "fau_batch.cu", "fau_movegen.cpp", "fau_noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -117,6 +117,18 @@ class MoveDesc(C.Structure):
                 ("type_dp", dptr), ("type_dprot", dptr)]
 
 
+FAU_NOALLOC_MAX_PARTICLES = 65536
+
+
+class NonbondedArgs(C.Structure):
+    """fau_nonbonded_args: device pointers (as integers) for the allocation-free entry point."""
+    _fields_ = [("n_particles", C.c_int), ("box", C.c_double * 3), ("pos", C.c_void_p), ("charge", C.c_void_p),
+                ("type", C.c_void_p), ("n_types", C.c_int), ("sigma2", C.c_void_p), ("eps4", C.c_void_p),
+                ("hs_sigma2", C.c_void_p), ("pair_terms", C.c_int), ("coulomb_type", C.c_int),
+                ("bjerrum_length", C.c_double), ("coulomb_cutoff", C.c_double), ("coulomb_alpha", C.c_double),
+                ("pair_cutoff", C.c_double)]
+
+
 class FauError(RuntimeError):
     """A non-zero status returned by the C ABI."""
 
@@ -152,6 +164,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_run_proposals_batch": ([P, C.POINTER(P), C.c_int, P, C.POINTER(C.c_int64), P, dptr,
                                      C.POINTER(BatchStats)], C.c_int),
         "fau_measure_fp32_peak": ([P, dptr], C.c_int),
+        "fau_nonbonded_energy_noalloc": ([C.POINTER(NonbondedArgs), C.c_void_p, C.c_void_p], C.c_int),
         "fau_get_positions": ([P, dptr], C.c_int),
         "fau_get_mass_centers": ([P, dptr], C.c_int),
         "fau_get_cells": ([P, iptr], C.c_int),

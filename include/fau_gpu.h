@@ -268,6 +268,39 @@ int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const 
 /* Measured FP32 FMA throughput of the device (roofline denominator). */
 int fau_measure_fp32_peak(fau_ctx* ctx, double* tflops_out);
 
+/* ---- nonbonded energy without device allocation ---------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a host engine that owns all device memory through its own pool and does not
+ * let a plugin allocate (cudaMalloc/cudaFree synchronise the device and
+ * fragment the pool), or a latency-critical loop that must not stall on an
+ * allocation.  The caller passes DEVICE pointers for every input and for the
+ * output; nothing is allocated or freed, by this library or any library it
+ * calls.  E = sum_{i<j} u(r_ij) over all particles as one atomic group (the
+ * Nonbonded energy of Change::everything for a single atomic group), FP64,
+ * written to *energy_out (device) asynchronously on `stream` (a cudaStream_t;
+ * NULL = default stream).  type[i] must lie in [0, n_types).
+ * Scratch: one file-scope device array of FAU_NOALLOC_MAX_PARTICLES doubles
+ * (512 KiB) that every GPU loading this library holds until the process exits;
+ * larger n_particles is rejected with FAU_ERR_ARG.  The first call on a device
+ * looks up the array's device address; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+#define FAU_NOALLOC_MAX_PARTICLES 65536
+typedef struct fau_nonbonded_args {
+    int n_particles;
+    double box[3];
+    const double* pos;        /* device, n*3 xyz inside [-L/2, L/2]  */
+    const double* charge;     /* device, n                           */
+    const int* type;          /* device, n                           */
+    int n_types;
+    const double* sigma2;     /* device, n_types^2 (LJ/WCA)          */
+    const double* eps4;       /* device, n_types^2 in kT (LJ/WCA)    */
+    const double* hs_sigma2;  /* device, n_types^2 (HS) or NULL      */
+    int pair_terms;           /* fau_pair_term bits                  */
+    int coulomb_type;         /* fau_coulomb_type                    */
+    double bjerrum_length, coulomb_cutoff, coulomb_alpha, pair_cutoff;
+} fau_nonbonded_args;
+int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* args, double* energy_out, void* stream);
+
 /* ---- state access -------------------------------------------------------- */
 int fau_get_positions(fau_sys* sys, double* xyz_out);          /* n*3 FP64 */
 int fau_get_mass_centers(fau_sys* sys, double* xyz_out);       /* n_groups*3 */
