@@ -23,7 +23,7 @@ using namespace fau;
 struct fau_ctx;
 extern "C" int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device);
 extern "C" int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n, int* n_groups,
-                                     int* molecular_only, double* t_ref);
+                                     int* molecular_only, double* t_ref, int* knc);
 extern "C" int fau_internal_fail(int code, const char* msg);
 
 namespace {
@@ -102,20 +102,24 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     std::vector<uint32_t> ids(n);
     std::vector<uint8_t> mol(n);
     std::vector<double> tref(n, 1.0);
-    int Kmax = 0;
+    int Kmax = 0, ncmax = 0;
     for (int i = 0; i < n; i++) {
         fau_ctx* c2;
-        int K, np, ng, mo;
-        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tref[i]);
+        int K, np, ng, mo, knc;
+        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tref[i], &knc);
         if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
         Kmax = std::max(Kmax, K);
+        ncmax = std::max(ncmax, knc);
         nm[i] = P->moves_per_system ? P->moves_per_system[i] : P->moves;
         if (nm[i] < 0) return fau_internal_fail(FAU_ERR_ARG, "negative move count");
         ids[i] = P->streams ? P->streams[i] : (uint32_t)i;
         mol[i] = (uint8_t)mo;
         if (pt) tref[i] = P->temperatures[i];
     }
-    if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
+    const int threads = P->threads > 0 ? P->threads : 128;
+    if (threads != 128 && threads != 256) return fau_internal_fail(FAU_ERR_ARG, "threads must be 128 or 256");
+    if (Kmax > chain_max_k(threads) || chain_smem_bytes(Kmax, ncmax) + 16384 > 227 * 1024)
+        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
 
     // device argument arrays (one allocation, freed at the end of the call)
     // every sub-buffer starts on a 16-byte boundary (8-byte fields inside)
@@ -166,7 +170,6 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         BTRY(cudaMemcpyAsync(dbuf + off_ctr, P->counters, 8 * n, cudaMemcpyHostToDevice, st));
         a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_ctr);
     }
-    const int threads = P->threads > 0 ? P->threads : 256;
     const int nblk = pt ? P->n_swap_blocks : 1;
     if (pt) {
         a.n_moves = nullptr;
@@ -177,7 +180,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         a.n_moves = reinterpret_cast<const long long*>(dbuf + off_nm);
     }
     // set the kernel's shared-memory attribute before the capture starts
-    BTRY(prepare_chain(Kmax, threads, true));
+    BTRY(prepare_chain(Kmax, ncmax, threads, true));
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -187,7 +190,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     BTRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int b = 0; b < nblk; b++) {
         a.counter_base = P->counter_base + (unsigned long long)b * (pt ? (unsigned long long)P->swap_interval_moves : 0ull);
-        if (launch_chain(a, n, Kmax, threads, true, st) != cudaSuccess) {
+        if (launch_chain(a, n, Kmax, ncmax, threads, true, st) != cudaSuccess) {
             cudaStreamEndCapture(st, &graph);
             if (graph) cudaGraphDestroy(graph);
             cleanup();
@@ -256,14 +259,15 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     if (cudaSetDevice(device) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "cudaSetDevice failed");
     std::vector<DevSys*> dsys(n);
     std::vector<long long> nm(n), off(n);
-    int Kmax = 0;
+    int Kmax = 0, ncmax = 0;
     const long long total = offsets[n];
     if (offsets[0] != 0 || total < 0) return fau_internal_fail(FAU_ERR_ARG, "offsets must start at 0");
     for (int i = 0; i < n; i++) {
         fau_ctx* c2;
-        int K, np, ng, mo;
+        int K, np, ng, mo, knc;
         double tr;
-        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tr);
+        fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tr, &knc);
+        ncmax = std::max(ncmax, knc);
         if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
         if (offsets[i + 1] < offsets[i]) return fau_internal_fail(FAU_ERR_ARG, "offsets not sorted");
         nm[i] = offsets[i + 1] - offsets[i];
@@ -282,7 +286,8 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             }
         }
     }
-    if (chain_smem_bytes(Kmax) + 8192 > 227 * 1024) return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors");
+    if (Kmax > chain_max_k(128) || chain_smem_bytes(Kmax, ncmax) + 16384 > 227 * 1024)
+        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t o_sys = 0, o_nm = al(o_sys + 8 * n), o_off = al(o_nm + 8 * n), o_sum = al(o_off + 8 * n),
                  o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * total),
@@ -315,7 +320,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    if (launch_chain(a, n, Kmax, 256, false, st) != cudaSuccess) {
+    if (launch_chain(a, n, Kmax, ncmax, 128, false, st) != cudaSuccess) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return done(FAU_ERR_CUDA, "chain launch failed");

@@ -395,6 +395,7 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         h.fx_scale[k] = kTwo32 / d->box[k];
         h.fx_len[k] = (float)(d->box[k] / kTwo32);
         h.fx_lend[k] = d->box[k] / kTwo32;
+        h.inv_f[k] = (float)(1.0 / d->box[k]);
     }
     const int n = d->n_particles;
     h.n = n;
@@ -567,6 +568,15 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         std::vector<float> akf(lay.K);
         for (int k = 0; k < lay.K; k++) akf[k] = (float)lay.ew.Ak[k];
         h.K = lay.K;
+        int knc = 0;
+        for (int v : lay.ew.kn) {
+            const int a = std::abs((v & 0xff) - 128), b = std::abs(((v >> 8) & 0xff) - 128),
+                      c = std::abs(((v >> 16) & 0xff) - 128);
+            knc = std::max(knc, std::max(a, std::max(b, c)));
+        }
+        h.knc = knc;
+        if (lay.K > chain_max_k(128) || chain_smem_bytes(lay.K, knc) + 16384 > 227 * 1024)
+            return bail(fail(FAU_ERR_ARG, "%d k-vectors exceed the chain kernel's shared-memory budget", lay.K));
         UP(h.kn, lay.ew.kn);
         UP(h.Ak, akf);
         UP(h.Akd, lay.ew.Ak);
@@ -888,7 +898,7 @@ static int run_chain(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, dou
         a.du_out = du ? s->d_du + offset : nullptr;
         a.detail = detail ? s->d_detail + offset : nullptr;
         CUDA_TRY(cudaEventRecord(s->ctx->ev0, st));
-        CUDA_TRY(launch_chain(a, 1, s->K, chain_threads(s), false, st));
+        CUDA_TRY(launch_chain(a, 1, s->K, s->h.knc, chain_threads(s), false, st));
         CUDA_TRY(cudaEventRecord(s->ctx->ev1, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         float ms = 0.f;
@@ -1159,8 +1169,9 @@ int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device)
     return FAU_OK;
 }
 int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n, int* n_groups, int* molecular_only,
-                          double* t_ref)
+                          double* t_ref, int* knc)
 {
+    *knc = s->h.knc;
     *ctx = s->ctx;
     *d = s->d;
     *K = s->K;
@@ -1201,7 +1212,7 @@ int fau_energy_change(fau_sys* s, const fau_proposal* p, fau_trial_result* out)
     a.detail = s->d_detail;
     a.pending = s->d_plain;
     a.pending_dq = s->K ? s->d_dq : nullptr;
-    CUDA_TRY(launch_chain(a, 1, s->K, chain_threads(s), false, st));
+    CUDA_TRY(launch_chain(a, 1, s->K, s->h.knc, chain_threads(s), false, st));
     fau_trial_result r{};
     CUDA_TRY(cudaMemcpyAsync(&r, s->d_detail, sizeof(r), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));

@@ -1,0 +1,930 @@
+// fau_chain.cuh -- the persistent Metropolis chain kernel (one CTA per chain).
+//
+// One loop iteration is one MetropolisMonteCarlo::performMove
+// (reference src/montecarlo.cpp:139-187) for a transrot or moltransrot move:
+//
+//   [all warps]  apply the previous move's Q(k) change if it was accepted,
+//                then evaluate this move: Ewald dU over the CTA's k-vectors
+//                (two-per-axis phase tables, see below) and the pair dU over
+//                the cell-list neighbours (or all particles), accumulated in
+//                float-float per thread and per warp
+//   barrier
+//   [warp 0]     final sum, getEnergyChange + metropolisCriterion (FP64),
+//                commit positions / records / cell list / mass centre,
+//                prepare the next move (FP64 trial positions, phase tables)
+//   barrier
+//
+// Ewald phases: for a moved atom with fixed-point position u and
+// displacement g = (r_new - r_old) / L (minimum image), the CTA builds per
+// axis the tables e^{i n 2 pi u_d / 2^32} and e^{i n pi g_d} for n = -nc..nc
+// (sincospi of exactly reduced integer phases, 6 (2 nc + 1) entries).  Every
+// k-vector then needs five complex products:
+//     e_old = ex[nx] ey[ny] ez[nz],   h = e^{i D/2} = hx[nx] hy[ny] hz[nz],
+//     d     = q (e_new - e_old) = 2 q sin(D/2) i e_old h,
+// which keeps d accurate for small moves (no e_new - e_old cancellation).
+#pragma once
+#include "fau_dev.cuh"
+#include "fau_kernels.h"
+
+namespace fau {
+
+constexpr int kTableAtoms = 8; // moved atoms handled with phase tables (larger groups: direct sincospi)
+
+struct MoveShared {
+    int kind, index, m, first;
+    int accept, stop, prev_accept, pad;
+    long long consumed;
+    double u;
+    int cc_old[3], cc_new[3]; // cell coordinates of the moved atom (atomic moves with cells)
+    int cell_old, cell_new;
+    float q[kMaxGroupAtoms];
+    float3 g[kMaxGroupAtoms]; // minimum-image displacement / L per moved atom
+    uint4 rec_old[kMaxGroupAtoms];
+    uint4 rec_new[kMaxGroupAtoms];
+    double xn[kMaxGroupAtoms][3];
+    double xo[kMaxGroupAtoms][3];
+    double cm_new[3];
+    double dM[3];
+    uint4 cmrec_old, cmrec_new;
+};
+
+// cell coordinates of a position: fixed-point fast path; the FP64 reference formula
+// floor((x + L/2) / cell_len) (src/celllistimpl.h:139-143, src/sasa.cpp:466-468)
+// decides within 2^-18 of a cell boundary, so binning is bit-exact.
+__device__ __forceinline__ void cell_coords(const DevSys& S, const double* x, uint4 r, int* c)
+{
+    const uint32_t u[3] = {r.x, r.y, r.z};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const uint32_t s = u[d] + 0x80000000u;
+        const unsigned long long prod = (unsigned long long)s * (unsigned long long)S.cdim[d];
+        int v = (int)(prod >> 32);
+        const uint32_t frac = (uint32_t)prod;
+        if (frac < (1u << 14) || frac > 0xFFFFFFFFu - (1u << 14)) {
+            const double t = __dadd_rn(x[d], __dmul_rn(0.5, S.L[d]));
+            v = (int)floor(__ddiv_rn(t, S.cell_len[d]));
+        }
+        if (v < 0) v += S.cdim[d] * (abs(v) / S.cdim[d] + 1);
+        else if (v >= S.cdim[d]) v -= S.cdim[d] * (v / S.cdim[d]);
+        c[d] = v;
+    }
+}
+__device__ __forceinline__ int cell_index(const DevSys& S, const int* c)
+{
+    return c[0] + S.cdim[0] * (c[1] + S.cdim[1] * c[2]);
+}
+
+// GroupCutoff::cut (src/energy.h:761-768): sqdist(cm1, cm2) >= cutoff^2, FP32 on
+// fixed-point mass centres, FP64 inside a 1e-5 guard band.
+__device__ __forceinline__ bool group_cut(const DevSys& S, uint4 cmrec, const double* cm, int h)
+{
+    if (S.cut_g2g2 < 0.0) return false;
+    const float r2 = r2_fixed(S, cmrec, S.g_cmrec[h]);
+    if (r2 < S.cut_g2g2f * 0.99999f) return false;
+    if (r2 > S.cut_g2g2f * 1.00001f) return true;
+    const double o[3] = {S.g_cm[3 * h], S.g_cm[3 * h + 1], S.g_cm[3 * h + 2]};
+    return sqdist_d(S, cm, o) >= S.cut_g2g2;
+}
+
+// quaternion rotation v' = v + w t + u x t, t = 2 u x v (FP64, never contracted)
+__device__ __forceinline__ void quat_rotate(const double* q, double* v)
+{
+    const double ux = q[1], uy = q[2], uz = q[3], w = q[0];
+    double tx = __dsub_rn(__dmul_rn(uy, v[2]), __dmul_rn(uz, v[1]));
+    double ty = __dsub_rn(__dmul_rn(uz, v[0]), __dmul_rn(ux, v[2]));
+    double tz = __dsub_rn(__dmul_rn(ux, v[1]), __dmul_rn(uy, v[0]));
+    tx = __dadd_rn(tx, tx);
+    ty = __dadd_rn(ty, ty);
+    tz = __dadd_rn(tz, tz);
+    const double cx = __dsub_rn(__dmul_rn(uy, tz), __dmul_rn(uz, ty));
+    const double cy = __dsub_rn(__dmul_rn(uz, tx), __dmul_rn(ux, tz));
+    const double cz = __dsub_rn(__dmul_rn(ux, ty), __dmul_rn(uy, tx));
+    v[0] = __dadd_rn(__dadd_rn(v[0], __dmul_rn(w, tx)), cx);
+    v[1] = __dadd_rn(__dadd_rn(v[1], __dmul_rn(w, ty)), cy);
+    v[2] = __dadd_rn(__dadd_rn(v[2], __dmul_rn(w, tz)), cz);
+}
+
+struct Proposal {
+    int kind, index;
+    double dr[3];
+    double quat[4];
+    double u;
+    bool rotate;
+};
+
+// Device-RNG proposal (batched mode), a deliberate deviation from the reference's
+// mt19937 stream: uniform direction (Archimedes), |dr| = dp U(0,1), uniform
+// particle / group, 53-bit Metropolis uniform.
+static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigned long long ctr, uint32_t sys_id, uint64_t seed,
+                                           double dp, double dprot, bool molecular)
+{
+    Proposal p;
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    const U4 c1 = philox({(uint32_t)ctr, (uint32_t)(ctr >> 32), sys_id, 0u}, k0, k1);
+    const U4 c2 = philox({(uint32_t)ctr, (uint32_t)(ctr >> 32), sys_id, 1u}, k0, k1);
+    const float z = fmaf(2.f, u01_24(c1.y), -1.f);
+    float s, c;
+    sincospif(2.f * u01_24(c1.z), &s, &c);
+    const float rxy = sqrtf(fmaxf(0.f, 1.f - z * z));
+    const double len = dp * (double)u01_24(c1.w);
+    p.dr[0] = (double)(rxy * c) * len;
+    p.dr[1] = (double)(rxy * s) * len;
+    p.dr[2] = (double)z * len;
+    p.u = u01_53(c2.x, c2.y);
+    p.rotate = false;
+    p.quat[0] = 1.0;
+    p.quat[1] = p.quat[2] = p.quat[3] = 0.0;
+    if (!molecular) {
+        p.kind = FAU_MOVE_ATOMIC;
+        const uint32_t n = S.n_atomic > 0 ? (uint32_t)S.n_atomic : (uint32_t)S.n;
+        const uint32_t j = __umulhi(c1.x, n);
+        p.index = S.n_atomic > 0 ? S.atomic_idx[j] : (int)j;
+    }
+    else {
+        p.kind = FAU_MOVE_MOLECULAR;
+        p.index = (int)__umulhi(c1.x, (uint32_t)S.n_groups);
+        if (dprot > 0.0) {
+            const float az = fmaf(2.f, u01_24(c2.z), -1.f);
+            float as, ac;
+            sincospif(2.f * u01_24(c2.w), &as, &ac);
+            const float axy = sqrtf(fmaxf(0.f, 1.f - az * az));
+            const U4 c3 = philox({(uint32_t)ctr, (uint32_t)(ctr >> 32), sys_id, 2u}, k0, k1);
+            const double angle = dprot * ((double)u01_24(c3.x) - 0.5);
+            const double ha = 0.5 * angle;
+            const double sh = sin(ha);
+            p.quat[0] = cos(ha);
+            p.quat[1] = sh * (double)(axy * ac);
+            p.quat[2] = sh * (double)(axy * as);
+            p.quat[3] = sh * (double)az;
+            p.rotate = true;
+        }
+    }
+    return p;
+}
+
+__device__ __forceinline__ Proposal load_proposal(const fau_proposal& f)
+{
+    Proposal p;
+    p.kind = f.kind;
+    p.index = f.index;
+#pragma unroll
+    for (int d = 0; d < 3; d++) p.dr[d] = f.dr[d];
+#pragma unroll
+    for (int d = 0; d < 4; d++) p.quat[d] = f.quat[d];
+    p.u = f.u;
+    p.rotate = !(f.quat[0] == 0.0 && f.quat[1] == 0.0 && f.quat[2] == 0.0 && f.quat[3] == 0.0);
+    return p;
+}
+
+// (xn - xo) / L per axis under minimum image (Chameleon::vdist src/geometry.h:429-458)
+__device__ __forceinline__ float3 min_image_frac(const DevSys& S, const double* xn, const double* xo)
+{
+    float g[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double v = __dsub_rn(xn[d], xo[d]);
+        if (v > S.half[d]) v = __dsub_rn(v, S.L[d]);
+        else if (v < -S.half[d]) v = __dadd_rn(v, S.L[d]);
+        g[d] = (float)v * S.inv_f[d];
+    }
+    return make_float3(g[0], g[1], g[2]);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// e^{i pi P 2^-31} for an exact 32-bit phase P: sincospi of the top 24 bits
+// (exact in FP32) times the first-order rotation by the remaining 8 bits.
+__device__ __forceinline__ float2 phase_exact(uint32_t P)
+{
+    const uint32_t hi = P & 0xFFFFFF00u;
+    const float th = (float)(int32_t)hi * 4.656612873077393e-10f;          // 2^-31
+    const float dl = (float)(P & 0xFFu) * (3.14159265358979f * 4.656612873077393e-10f);
+    float s, c;
+    sincospif(th, &s, &c);
+    return make_float2(fmaf(-s, dl, c), fmaf(c, dl, s));
+}
+
+// Warp 0: proposal -> FP64 trial positions (AtomicTranslateRotate::translateParticle
+// src/move.cpp:225-240; Group::translate src/group.cpp:115-123 then Group::rotate
+// src/group.cpp:110-113, src/geometry.h:613-627), fixed-point records, cells, and
+// the phase tables of the moved atoms.
+static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p, int lane, float2* tab, int nc)
+{
+    const int TS = 2 * nc + 1;
+    if (lane == 0) {
+        ms.kind = p.kind;
+        ms.index = p.index;
+        ms.u = p.u;
+        ms.stop = 0;
+    }
+    int m = 0;
+    if (p.kind == FAU_MOVE_ATOMIC) {
+        m = 1;
+        if (lane == 0) {
+            const int i = p.index;
+            const double xo[3] = {S.x[i], S.y[i], S.z[i]};
+            double xn[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) xn[d] = boundary1(__dadd_rn(xo[d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
+            const uint4 ro = S.rec[i];
+            uint4 rn;
+            rn.x = to_fixed(xn[0], S.fx_scale[0]);
+            rn.y = to_fixed(xn[1], S.fx_scale[1]);
+            rn.z = to_fixed(xn[2], S.fx_scale[2]);
+            rn.w = ro.w;
+            ms.m = 1;
+            ms.first = i;
+            ms.rec_old[0] = ro;
+            ms.rec_new[0] = rn;
+            const double q = S.itype_qd[ro.w >> 24];
+            ms.q[0] = (float)q;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                ms.xn[0][d] = xn[d];
+                ms.xo[0][d] = xo[d];
+                ms.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
+            }
+            ms.g[0] = min_image_frac(S, xn, xo);
+            if (S.flags & SYS_CELLS) {
+                const int co = S.cell_of[i];
+                ms.cell_old = co;
+                ms.cc_old[0] = co % S.cdim[0];
+                ms.cc_old[1] = (co / S.cdim[0]) % S.cdim[1];
+                ms.cc_old[2] = co / (S.cdim[0] * S.cdim[1]);
+                int c[3];
+                cell_coords(S, xn, rn, c);
+                ms.cc_new[0] = c[0];
+                ms.cc_new[1] = c[1];
+                ms.cc_new[2] = c[2];
+                ms.cell_new = cell_index(S, c);
+            }
+        }
+    }
+    else if (p.kind == FAU_MOVE_MOLECULAR) {
+        const int g = p.index;
+        const int b = S.g_begin[g];
+        m = S.g_begin[g + 1] - b;
+        double cm[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            cm[d] = boundary1(__dadd_rn(S.g_cm[3 * g + d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
+        double dM[3] = {0, 0, 0};
+        if (lane < m && m <= kMaxGroupAtoms) {
+            const int i = b + lane;
+            const double xo[3] = {S.x[i], S.y[i], S.z[i]};
+            double v[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) v[d] = boundary1(__dadd_rn(xo[d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
+            if (p.rotate) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) v[d] = boundary1(__dsub_rn(v[d], cm[d]), S.L[d], S.half[d], S.inv[d]);
+                quat_rotate(p.quat, v);
+#pragma unroll
+                for (int d = 0; d < 3; d++) v[d] = boundary1(__dadd_rn(v[d], cm[d]), S.L[d], S.half[d], S.inv[d]);
+            }
+            const uint4 ro = S.rec[i];
+            uint4 rn;
+            rn.x = to_fixed(v[0], S.fx_scale[0]);
+            rn.y = to_fixed(v[1], S.fx_scale[1]);
+            rn.z = to_fixed(v[2], S.fx_scale[2]);
+            rn.w = ro.w;
+            ms.rec_old[lane] = ro;
+            ms.rec_new[lane] = rn;
+            const double q = S.itype_qd[ro.w >> 24];
+            ms.q[lane] = (float)q;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                ms.xn[lane][d] = v[d];
+                ms.xo[lane][d] = xo[d];
+                dM[d] = __dmul_rn(q, __dsub_rn(v[d], xo[d]));
+            }
+            ms.g[lane] = min_image_frac(S, v, xo);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; d++) { // sum over the group's atoms in atom order
+            double acc = 0.0;
+            for (int a = 0; a < m && a < 32; a++) acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, dM[d], a));
+            dM[d] = acc;
+        }
+        if (lane == 0) {
+            ms.m = m;
+            ms.first = b;
+            if (m > kMaxGroupAtoms) ms.stop = FAU_ERR_ARG;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                ms.cm_new[d] = cm[d];
+                ms.dM[d] = dM[d];
+            }
+            ms.cmrec_old = S.g_cmrec[g];
+            ms.cmrec_new = make_uint4(to_fixed(cm[0], S.fx_scale[0]), to_fixed(cm[1], S.fx_scale[1]),
+                                      to_fixed(cm[2], S.fx_scale[2]), 0u);
+        }
+    }
+    else if (lane == 0) {
+        ms.m = 0;
+        ms.first = -1;
+    }
+    __syncwarp();
+    // phase tables: per atom (a < min(m, kTableAtoms)), per axis d, n = 0..nc
+    if (tab && m <= kTableAtoms) {
+        const int per_atom = 6 * (nc + 1);
+        for (int e = lane; e < m * per_atom; e += 32) {
+            const int a = e / per_atom, r = e - a * per_atom;
+            const int kind = r / (nc + 1), n = r - kind * (nc + 1); // kind 0..2: old phase, 3..5: half delta
+            float2 v;
+            if (kind < 3) {
+                const uint4 ro = ms.rec_old[a];
+                const uint32_t u = kind == 0 ? ro.x : (kind == 1 ? ro.y : ro.z);
+                v = phase_exact((uint32_t)n * u);
+            }
+            else {
+                const float3 g = ms.g[a];
+                const float gd = kind == 3 ? g.x : (kind == 4 ? g.y : g.z);
+                float s, c;
+                sincospif((float)n * gd, &s, &c);
+                v = make_float2(c, s);
+            }
+            float2* t = tab + (a * 6 + kind) * TS;
+            t[nc + n] = v;
+            t[nc - n] = make_float2(v.x, -v.y);
+        }
+    }
+}
+
+// metropolisCriterion (src/montecarlo.cpp:17-34) for a non-NaN du: FP32 exp decides
+// unless u is within 1e-4 of the threshold; then the FP64 u <= exp(-du) decides.
+__device__ __forceinline__ bool metropolis(double du, double u)
+{
+    if (isinf(du) && du < 0.0) return true;
+    if (-du > 709.782712893384) return true;
+    if (du <= 0.0 && u < 1.0) return true; // exp(-du) >= 1 > u
+    const float ef = __expf((float)(-du));
+    if (ef > 1e-30f) {
+        if (u < (double)ef * 0.9999) return true;
+        if (u > (double)ef * 1.0001) return false;
+    }
+    else if (u > 1e-29) {
+        return false;
+    }
+    return u <= exp(-du);
+}
+
+// getEnergyChange (src/montecarlo.cpp:193-209) from per-state inf/NaN flags
+__device__ __forceinline__ double energy_change(double finite_du, bool new_inf, bool old_inf, bool new_nan,
+                                                bool old_nan)
+{
+    const double inf = __longlong_as_double(0x7ff0000000000000ULL);
+    if (old_nan && !new_nan) return -inf;
+    if (new_nan) return inf;
+    if (new_inf) return inf;
+    if (old_inf) return -inf;
+    return finite_du;
+}
+
+enum : int { F_NEW_INF = 1, F_OLD_INF = 2, F_NEW_NAN = 4, F_OLD_NAN = 8 };
+
+__device__ __forceinline__ void add_pair(FF& acc, int& flags, float un, float uo, bool ni, bool oi, bool nn, bool on)
+{
+    ff_add(acc, un - uo);
+    flags |= (ni ? F_NEW_INF : 0) | (oi ? F_OLD_INF : 0) | (nn ? F_NEW_NAN : 0) | (on ? F_OLD_NAN : 0);
+}
+
+__device__ __forceinline__ void warp_reduce(FF& a, FF& b, float& sc, int& flags, bool two)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        FF ta{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+        a = ff_sum(a, ta);
+        if (two) {
+            FF tb{__shfl_xor_sync(0xffffffffu, b.hi, o), __shfl_xor_sync(0xffffffffu, b.lo, o)};
+            b = ff_sum(b, tb);
+            sc += __shfl_xor_sync(0xffffffffu, sc, o);
+        }
+    }
+    flags = __reduce_or_sync(0xffffffffu, flags);
+}
+
+template <int NT, int KPT, bool PHILOX>
+__global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
+{
+    constexpr int NW = NT / 32;
+    DevSys& S = *A.sys[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int K = (S.flags & SYS_EWALD) ? S.K : 0;
+    const int nc = S.knc;
+    const int TS = 2 * nc + 1;
+    float2* Qb = reinterpret_cast<float2*>(smem_raw); // FP32 copy of the FP64 master Q
+    float2* pend = Qb + K;                            // accepted changes not yet flushed to FP64
+    int* kidx = reinterpret_cast<int*>(pend + K);     // table indices (nx+nc) | (ny+nc)<<8 | (nz+nc)<<16
+    float* Af = reinterpret_cast<float*>(kidx + K);   // (2 pi lB / V) A_k
+    float2* tab = reinterpret_cast<float2*>(Af + K);  // kTableAtoms * 6 * TS phase tables
+
+    __shared__ PairF pt[kMaxITypes * kMaxITypes];
+    __shared__ MoveShared ms;
+    __shared__ FF red_a[NW], red_b[NW];
+    __shared__ float red_s[NW];
+    __shared__ int red_f[NW];
+    __shared__ int nbo[27][3];
+
+    const float rec_pref_f = (float)S.rec_pref;
+    for (int k = tid; k < K; k += NT) {
+        const double2 q = S.Q[k];
+        Qb[k] = make_float2((float)q.x, (float)q.y);
+        pend[k] = make_float2(0.f, 0.f);
+        int nx, ny, nz;
+        kn_unpack(S.kn[k], nx, ny, nz);
+        kidx[k] = (nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16);
+        Af[k] = rec_pref_f * S.Ak[k];
+    }
+    for (int t = tid; t < S.nt * S.nt; t += NT) pt[t] = S.pair[t];
+    int nnb = 0, gshift = 0;
+    if (S.flags & SYS_CELLS) {
+        const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1,
+                  nbz = S.off_max[2] - S.off_min[2] + 1;
+        nnb = nbx * nby * nbz;
+        if (tid < nnb) {
+            nbo[tid][0] = tid % nbx + S.off_min[0];
+            nbo[tid][1] = (tid / nbx) % nby + S.off_min[1];
+            nbo[tid][2] = tid / (nbx * nby) + S.off_min[2];
+        }
+        while ((2 * nnb) << (gshift + 1) <= NT) gshift++; // G = 2^gshift lanes per (state, cell)
+    }
+
+    const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
+    const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
+    const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
+    const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+    const bool molecular_sys = A.molecular ? (A.molecular[blockIdx.x] != 0) : false;
+    const bool detail = A.detail != nullptr;
+    const int nt = S.nt;
+
+    unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
+    int since_flush = 0;
+    double energy = S.energy, sum_du = 0.0;
+    double M[3] = {S.M[0], S.M[1], S.M[2]};
+    float2 dl[KPT];
+#pragma unroll
+    for (int r = 0; r < KPT; r++) dl[r] = make_float2(0.f, 0.f);
+
+    if (tid == 0) {
+        ms.prev_accept = 0;
+        ms.consumed = 0;
+    }
+    __syncthreads();
+    if (warp == 0 && nmoves > 0) {
+        const Proposal p = PHILOX ? philox_proposal(S, ctr0, sys_id, A.seed, A.dp, A.dprot, molecular_sys)
+                                  : load_proposal(A.props[poff]);
+        prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
+    }
+    __syncthreads();
+
+    for (long long mv = 0; mv < nmoves; mv++) {
+        if (ms.stop) break;
+        // ---- the previous move's Q(k) change (State::sync trial -> accepted, deferred)
+        if (ms.prev_accept) {
+#pragma unroll
+            for (int r = 0; r < KPT; r++) {
+                const int k = tid + r * NT;
+                if (k < K) {
+                    float2 pe = pend[k];
+                    pe.x += dl[r].x;
+                    pe.y += dl[r].y;
+                    pend[k] = pe;
+                }
+            }
+            if (++since_flush == kFlushAccepts) { // FP32 pending -> FP64 master
+                since_flush = 0;
+                for (int k = tid; k < K; k += NT) {
+                    double2 q = S.Q[k];
+                    const float2 pe = pend[k];
+                    q.x += (double)pe.x;
+                    q.y += (double)pe.y;
+                    S.Q[k] = q;
+                    Qb[k] = make_float2((float)q.x, (float)q.y);
+                    pend[k] = make_float2(0.f, 0.f);
+                }
+            }
+        }
+        const int kind = ms.kind;
+        const int m = ms.m;
+
+        // ---- energy change of this move
+        FF accp{0.f, 0.f}, accr{0.f, 0.f};
+        float scale = 0.f;
+        int flags = 0;
+        if (kind != FAU_MOVE_NONE) {
+            if (K) {
+                const bool tables = m <= kTableAtoms;
+#pragma unroll
+                for (int r = 0; r < KPT; r++) {
+                    const int k = tid + r * NT;
+                    float2 d = make_float2(0.f, 0.f);
+                    if (k < K) {
+                        const int ki = kidx[k];
+                        const int ix = ki & 0xff, iy = (ki >> 8) & 0xff, iz = ki >> 16;
+                        for (int a = 0; a < m; a++) {
+                            float2 eo, h;
+                            if (tables) {
+                                const float2* t = tab + a * 6 * TS;
+                                eo = cmul(t[ix], cmul(t[TS + iy], t[2 * TS + iz]));
+                                h = cmul(t[3 * TS + ix], cmul(t[4 * TS + iy], t[5 * TS + iz]));
+                            }
+                            else { // large groups: direct phases
+                                const int nx = ix - nc, ny = iy - nc, nz = iz - nc;
+                                eo = eikr32(nx, ny, nz, ms.rec_old[a]);
+                                const float3 g = ms.g[a];
+                                float sh, ch;
+                                sincospif(fmaf((float)nx, g.x, fmaf((float)ny, g.y, (float)nz * g.z)), &sh, &ch);
+                                h = make_float2(ch, sh);
+                            }
+                            const float2 p = cmul(eo, h);
+                            const float f = 2.f * ms.q[a] * h.y;
+                            d.x = fmaf(-f, p.y, d.x);
+                            d.y = fmaf(f, p.x, d.y);
+                        }
+                        const float2 qb = Qb[k], pe = pend[k];
+                        const float qx = qb.x + pe.x, qy = qb.y + pe.y;
+                        const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
+                        const float dd = fmaf(d.x, d.x, d.y * d.y);
+                        const float af = Af[k];
+                        ff_add(accr, af * (cross + dd));
+                        if (detail) scale += af * (fabsf(cross) + dd);
+                    }
+                    dl[r] = d;
+                }
+                n_k += (unsigned long long)m * (unsigned long long)((K - tid + NT - 1) / NT > 0 ? (K - tid + NT - 1) / NT : 0);
+                if (A.pending_dq) {
+#pragma unroll
+                    for (int r = 0; r < KPT; r++) {
+                        const int k = tid + r * NT;
+                        if (k < K) A.pending_dq[k] = make_double2((double)dl[r].x, (double)dl[r].y);
+                    }
+                }
+            }
+
+            if (kind == FAU_MOVE_ATOMIC) {
+                const int i = ms.index;
+                const uint4 rn = ms.rec_new[0], ro = ms.rec_old[0];
+                const int ti = rn.w >> 24;
+                if (S.flags & SYS_CELLS) {
+                    const int G = 1 << gshift;
+                    const int items = (2 * nnb) << gshift;
+                    for (int it = tid; it < items; it += NT) {
+                        const int sc = it >> gshift, sub = it & (G - 1);
+                        const int state = sc >= nnb ? 1 : 0;
+                        const int c = sc - state * nnb;
+                        const int* cc = state ? ms.cc_new : ms.cc_old;
+                        int v[3];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            int w = cc[d] + nbo[c][d];
+                            if (w < 0) w += S.cdim[d];
+                            else if (w >= S.cdim[d]) w -= S.cdim[d];
+                            v[d] = w;
+                        }
+                        const int cell = v[0] + S.cdim[0] * (v[1] + S.cdim[1] * v[2]);
+                        const int cnt = S.cell_cnt[cell];
+                        const uint4* cr = S.cell_rec + (size_t)cell * S.cap;
+                        const uint4 ri = state ? rn : ro;
+                        const double* xi = state ? ms.xn[0] : ms.xo[0];
+                        for (int s = sub; s < cnt; s += G) {
+                            const uint4 rj = cr[s];
+                            const int j = (int)(rj.w & 0xFFFFFFu);
+                            if (j == i) continue;
+                            const int pidx = ti * nt + (rj.w >> 24);
+                            bool inf = false, nan = false;
+                            float mg = 0.f;
+                            const float u = pair_u32(S, pt[pidx], pidx, r2_fixed(S, ri, rj), xi, j, inf, nan, mg);
+                            if (state) add_pair(accp, flags, u, 0.f, inf, false, nan, false);
+                            else add_pair(accp, flags, 0.f, u, false, inf, false, nan);
+                            if (detail) scale += mg;
+                            n_pairs++;
+                        }
+                    }
+                }
+                else {
+                    for (int j = tid; j < S.n; j += NT) {
+                        if (j == i) continue;
+                        const uint4 rj = S.rec[j];
+                        const int pidx = ti * nt + (rj.w >> 24);
+                        const PairF p = pt[pidx];
+                        bool ni = false, nn = false, oi = false, on = false;
+                        float mg = 0.f;
+                        const float un = pair_u32(S, p, pidx, r2_fixed(S, rn, rj), ms.xn[0], j, ni, nn, mg);
+                        const float uo = pair_u32(S, p, pidx, r2_fixed(S, ro, rj), ms.xo[0], j, oi, on, mg);
+                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                        if (detail) scale += mg;
+                        n_pairs += 2;
+                    }
+                }
+            }
+            else if (kind == FAU_MOVE_MOLECULAR) { // group2all(group) with GroupCutoff
+                const int g = ms.index;
+                const uint4 cmo = ms.cmrec_old, cmn = ms.cmrec_new;
+                const double cmo_d[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
+                for (int h = tid; h < S.n_groups; h += NT) {
+                    if (h == g || (S.g_flags[h] & FAU_GROUP_ATOMIC)) continue;
+                    const bool cut_o = group_cut(S, cmo, cmo_d, h);
+                    const bool cut_n = group_cut(S, cmn, ms.cm_new, h);
+                    if (cut_o && cut_n) continue;
+                    const int hb = S.g_begin[h], he = S.g_begin[h + 1];
+                    for (int b = hb; b < he; b++) {
+                        const uint4 rb = S.rec[b];
+                        const int tb = rb.w >> 24;
+                        for (int a = 0; a < m; a++) {
+                            const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                            const PairF p = pt[pidx];
+                            bool ni = false, nn = false, oi = false, on = false;
+                            float mg = 0.f;
+                            const float un = cut_n ? 0.f
+                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b,
+                                                              ni, nn, mg);
+                            const float uo = cut_o ? 0.f
+                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b,
+                                                              oi, on, mg);
+                            add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                            if (detail) scale += mg;
+                            n_pairs += (cut_n ? 0 : 1) + (cut_o ? 0 : 1);
+                        }
+                    }
+                }
+                for (int t = tid; t < S.n_atomic; t += NT) { // atomic groups are never cut
+                    const int b = S.atomic_idx[t];
+                    const uint4 rb = S.rec[b];
+                    const int tb = rb.w >> 24;
+                    for (int a = 0; a < m; a++) {
+                        const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                        const PairF p = pt[pidx];
+                        bool ni = false, nn = false, oi = false, on = false;
+                        float mg = 0.f;
+                        const float un = pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b, ni, nn, mg);
+                        const float uo = pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b, oi, on, mg);
+                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                        if (detail) scale += mg;
+                        n_pairs += 2;
+                    }
+                }
+            }
+        }
+
+        // ---- reduce: per warp, then warp 0 (B1)
+        if (!detail) accp = ff_sum(accp, accr);
+        warp_reduce(accp, accr, scale, flags, detail);
+        if (lane == 0) {
+            red_a[warp] = accp;
+            red_b[warp] = accr;
+            red_s[warp] = scale;
+            red_f[warp] = flags;
+        }
+        __syncthreads();
+
+        if (warp == 0) {
+            accp = lane < NW ? red_a[lane] : FF{0.f, 0.f};
+            accr = lane < NW ? red_b[lane] : FF{0.f, 0.f};
+            scale = lane < NW ? red_s[lane] : 0.f;
+            flags = lane < NW ? red_f[lane] : 0;
+#pragma unroll
+            for (int o = NW / 2; o > 0; o >>= 1) {
+                FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
+                accp = ff_sum(accp, ta);
+                if (detail) {
+                    FF tb{__shfl_xor_sync(0xffffffffu, accr.hi, o), __shfl_xor_sync(0xffffffffu, accr.lo, o)};
+                    accr = ff_sum(accr, tb);
+                    scale += __shfl_xor_sync(0xffffffffu, scale, o);
+                }
+                flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+            }
+            int accept = 0, stop = 0;
+            double du = 0.0;
+            if (lane == 0) {
+                if (kind != FAU_MOVE_NONE) {
+                    const double du_nb = ff_value(accp); // without detail: pair + reciprocal together
+                    const double du_rec = detail ? ff_value(accr) : 0.0;
+                    double du_surf = 0.0;
+                    if (S.flags & SYS_SURFACE) {
+                        double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            const double mn = __dadd_rn(M[d], ms.dM[d]);
+                            m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
+                            m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
+                        }
+                        du_surf = S.surf_pref * (m2n - m2o);
+                    }
+                    const double fin = du_nb + (du_rec + du_surf);
+                    du = energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
+                    const double x = du * S.beta_scale;
+                    if (A.pending) { // evaluate only: the caller's Metropolis decides
+                        PlainMove& P = *A.pending;
+                        P.kind = kind;
+                        P.first = ms.first;
+                        P.m = m;
+                        P.group = kind == FAU_MOVE_MOLECULAR ? ms.index : -1;
+                        P.count_move = 0;
+                        for (int a = 0; a < m; a++)
+                            for (int d = 0; d < 3; d++) P.xn[a][d] = ms.xn[a][d];
+                        for (int d = 0; d < 3; d++) {
+                            P.cm_new[d] = ms.cm_new[d];
+                            P.dM[d] = ms.dM[d];
+                        }
+                        P.du = du;
+                    }
+                    else if (isnan(x)) {
+                        stop = FAU_ERR_NAN;
+                    }
+                    else {
+                        accept = metropolis(x, ms.u) ? 1 : 0;
+                    }
+                    if (detail) {
+                        fau_trial_result r;
+                        r.du = du;
+                        r.du_nonbonded = du_nb;
+                        r.du_ewald = du_rec + du_surf;
+                        r.err_scale = (double)scale;
+                        r.accepted = accept;
+                        r.new_inf = (flags & F_NEW_INF) ? 1 : 0;
+                        r.old_inf = (flags & F_OLD_INF) ? 1 : 0;
+                        r.pad = 0;
+                        A.detail[poff + mv] = r;
+                    }
+                    if (accept) {
+                        n_acc++;
+                        sum_du += du;
+                        energy += du;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
+                    }
+                    if (!stop) n_mv++;
+                }
+                if (A.acc_out) A.acc_out[poff + mv] = (uint8_t)accept;
+                if (A.du_out) A.du_out[poff + mv] = du;
+            }
+            accept = __shfl_sync(0xffffffffu, accept, 0);
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            if (stop) {
+                if (lane == 0) {
+                    ms.stop = stop;
+                    ms.prev_accept = 0;
+                    ms.consumed = mv;
+                }
+            }
+            else {
+                // ---- commit (State::sync trial -> accepted): positions, records, cells, mass centre
+                if (accept) {
+                    if (lane < m) {
+                        const int i = ms.first + lane;
+                        S.x[i] = ms.xn[lane][0];
+                        S.y[i] = ms.xn[lane][1];
+                        S.z[i] = ms.xn[lane][2];
+                        S.rec[i] = ms.rec_new[lane];
+                    }
+                    if (lane == 0) {
+                        if (kind == FAU_MOVE_MOLECULAR) {
+                            const int g = ms.index;
+#pragma unroll
+                            for (int d = 0; d < 3; d++) S.g_cm[3 * g + d] = ms.cm_new[d];
+                            S.g_cmrec[g] = ms.cmrec_new;
+                        }
+                        else if (S.flags & SYS_CELLS) {
+                            const int i = ms.index;
+                            const int co = ms.cell_old, cn = ms.cell_new;
+                            const int so = S.slot_of[i];
+                            if (co == cn) {
+                                S.cell_rec[(size_t)co * S.cap + so] = ms.rec_new[0];
+                            }
+                            else {
+                                const int last = S.cell_cnt[co] - 1;
+                                if (so != last) {
+                                    const uint4 mvd = S.cell_rec[(size_t)co * S.cap + last];
+                                    S.cell_rec[(size_t)co * S.cap + so] = mvd;
+                                    S.slot_of[mvd.w & 0xFFFFFFu] = so;
+                                }
+                                S.cell_cnt[co] = last;
+                                const int sn = S.cell_cnt[cn];
+                                if (sn >= S.cap) {
+                                    // keep the particle listed in its old cell: the host regrows the list
+                                    S.cell_rec[(size_t)co * S.cap + last] = ms.rec_new[0];
+                                    S.slot_of[i] = last;
+                                    S.cell_cnt[co] = last + 1;
+                                    stop = FAU_ERR_CAPACITY;
+                                }
+                                else {
+                                    S.cell_rec[(size_t)cn * S.cap + sn] = ms.rec_new[0];
+                                    S.cell_cnt[cn] = sn + 1;
+                                    S.cell_of[i] = cn;
+                                    S.slot_of[i] = sn;
+                                }
+                            }
+                        }
+                    }
+                    stop = __shfl_sync(0xffffffffu, stop, 0);
+                }
+                __syncwarp();
+                if (stop) {
+                    if (lane == 0) {
+                        ms.stop = stop;
+                        ms.prev_accept = accept;
+                        ms.consumed = mv + 1;
+                    }
+                }
+                else if (mv + 1 < nmoves) {
+                    // ---- prepare the next move
+                    const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed,
+                                                                A.dp, A.dprot, molecular_sys)
+                                              : load_proposal(A.props[poff + mv + 1]);
+                    prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
+                    if (lane == 0) {
+                        ms.prev_accept = accept;
+                        ms.consumed = mv + 1;
+                    }
+                }
+                else if (lane == 0) {
+                    ms.prev_accept = accept;
+                    ms.consumed = mv + 1;
+                }
+            }
+        }
+        __syncthreads(); // B2
+    }
+
+    // the last accepted move's Q(k) change, then everything pending into the FP64 master
+    if (ms.prev_accept) {
+#pragma unroll
+        for (int r = 0; r < KPT; r++) {
+            const int k = tid + r * NT;
+            if (k < K) {
+                float2 pe = pend[k];
+                pe.x += dl[r].x;
+                pe.y += dl[r].y;
+                pend[k] = pe;
+            }
+        }
+    }
+    for (int k = tid; k < K; k += NT) {
+        const float2 pe = pend[k];
+        if (pe.x != 0.f || pe.y != 0.f) {
+            double2 q = S.Q[k];
+            q.x += (double)pe.x;
+            q.y += (double)pe.y;
+            S.Q[k] = q;
+        }
+    }
+    __shared__ unsigned long long red_u[NW][2];
+    unsigned long long a = n_pairs, b = n_k;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        red_u[warp][0] = a;
+        red_u[warp][1] = b;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long pa = 0, kb = 0;
+        for (int w = 0; w < NW; w++) {
+            pa += red_u[w][0];
+            kb += red_u[w][1];
+        }
+        S.pair_evals += pa;
+        S.k_updates += kb;
+        S.moves += n_mv;
+        S.accepted += n_acc;
+        S.sum_du += sum_du;
+        S.energy = energy;
+#pragma unroll
+        for (int d = 0; d < 3; d++) S.M[d] = M[d];
+        if (ms.stop) S.err = ms.stop;
+        S.consumed = ms.stop ? ms.consumed : nmoves;
+    }
+}
+
+// dynamic shared memory of a chain kernel for K k-vectors and table size nc
+__host__ __device__ inline size_t chain_smem_bytes_v2(int K, int nc)
+{
+    return (size_t)K * (2 * sizeof(float2) + sizeof(int) + sizeof(float)) +
+           (size_t)kTableAtoms * 6 * (2 * nc + 1) * sizeof(float2);
+}
+
+template <int NT, int KPT, bool PH>
+cudaError_t launch_chain_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
+{
+    static size_t granted = 48 * 1024;
+    const size_t smem = chain_smem_bytes_v2(K, nc);
+    if (smem > granted) { // raised on demand, never inside a capture (callers prepare first)
+        cudaError_t e = cudaFuncSetAttribute(chain_kernel<NT, KPT, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        granted = smem;
+    }
+    if (prepare_only) return cudaSuccess;
+    chain_kernel<NT, KPT, PH><<<nblocks, NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace fau

@@ -43,6 +43,8 @@ struct DevSys {
     double fx_scale[3]; // 2^32 / L : FP64 -> fixed point
     float fx_len[3];    // L / 2^32 : fixed point -> FP32 angstrom
     double fx_lend[3];  // L / 2^32 in FP64
+    float inv_f[3];     // 1 / L in FP32
+    int knc;            // largest |n| component of the k-vectors (phase table half-width)
     int n, n_groups, flags, pad0;
 
     double* x;

@@ -46,9 +46,15 @@ constexpr int kTotalPairBlocks = 4096;
 constexpr int kTotalMiscBlocks = 1024;
 constexpr int kTotalPartials = kTotalPairBlocks + 2 * kTotalMiscBlocks;
 
-size_t chain_smem_bytes(int K);
-cudaError_t prepare_chain(int K, int threads, bool philox);
-cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int threads, bool philox, cudaStream_t st);
+size_t chain_smem_bytes(int K, int nc);
+int chain_max_k(int threads);
+cudaError_t prepare_chain(int K, int nc, int threads, bool philox);
+cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int threads, bool philox, cudaStream_t st);
+// per (CTA size, proposal source) dispatch over the instantiated k-per-thread variants
+cudaError_t chain_dispatch_128_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_128_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
