@@ -13,6 +13,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -182,6 +184,15 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     // set the kernel's shared-memory attribute before the capture starts
     BTRY(prepare_chain(Kmax, ncmax, threads, true));
 
+    // profiling: FAU_PHASE_TIMING=1 prints the chain kernel's per-phase cycles to stderr
+    unsigned long long* d_phase = nullptr;
+    const char* pt_env = std::getenv("FAU_PHASE_TIMING");
+    if (pt_env && pt_env[0] == '1') {
+        if (cudaMalloc(&d_phase, sizeof(unsigned long long) * kPhaseSlots * n) == cudaSuccess) {
+            cudaMemsetAsync(d_phase, 0, sizeof(unsigned long long) * kPhaseSlots * n, st);
+            a.phase_cycles = d_phase;
+        }
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -221,7 +232,22 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     cudaEventDestroy(e1);
     if (se != cudaSuccess) {
         cleanup();
+        if (d_phase) cudaFree(d_phase);
         return fau_internal_fail(FAU_ERR_CUDA, cudaGetErrorString(se));
+    }
+    if (d_phase) {
+        std::vector<unsigned long long> ph(kPhaseSlots * n);
+        cudaMemcpy(ph.data(), d_phase, sizeof(unsigned long long) * ph.size(), cudaMemcpyDeviceToHost);
+        cudaFree(d_phase);
+        double tot[kPhaseSlots] = {0};
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < kPhaseSlots; j++) tot[j] += (double)ph[i * kPhaseSlots + j];
+        const double mv = tot[11] > 0 ? tot[11] : 1.0;
+        static const char* names[kPhaseSlots] = {"deferred_q", "ewald", "pairs", "reduce+B1", "decision", "commit",
+                                                 "prepare", "B2(w0)", "compute(w1)", "B1(w1)", "B2(w1)", "moves"};
+        std::fprintf(stderr, "FAU_PHASE_TIMING cycles per move:");
+        for (int j = 0; j < kPhaseSlots - 1; j++) std::fprintf(stderr, " %s=%.0f", names[j], tot[j] / mv);
+        std::fprintf(stderr, " (moves %.0f)\n", tot[11]);
     }
     fau_batch_stats S{};
     int derr = FAU_OK;

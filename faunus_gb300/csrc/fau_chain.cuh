@@ -407,7 +407,7 @@ __device__ __forceinline__ void warp_reduce(FF& a, FF& b, float& sc, int& flags,
     flags = __reduce_or_sync(0xffffffffu, flags);
 }
 
-template <int NT, int KPT, bool PHILOX>
+template <int NT, bool PHILOX>
 __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 {
     constexpr int NW = NT / 32;
@@ -419,7 +419,8 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     const int TS = 2 * nc + 1;
     float2* Qb = reinterpret_cast<float2*>(smem_raw); // FP32 copy of the FP64 master Q
     float2* pend = Qb + K;                            // accepted changes not yet flushed to FP64
-    int* kidx = reinterpret_cast<int*>(pend + K);     // table indices (nx+nc) | (ny+nc)<<8 | (nz+nc)<<16
+    float2* dlt = pend + K;                           // this move's change of Q(k)
+    int* kidx = reinterpret_cast<int*>(dlt + K);      // table indices (nx+nc) | (ny+nc)<<8 | (nz+nc)<<16
     float* Af = reinterpret_cast<float*>(kidx + K);   // (2 pi lB / V) A_k
     float2* tab = reinterpret_cast<float2*>(Af + K);  // kTableAtoms * 6 * TS phase tables
 
@@ -435,6 +436,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         const double2 q = S.Q[k];
         Qb[k] = make_float2((float)q.x, (float)q.y);
         pend[k] = make_float2(0.f, 0.f);
+        dlt[k] = make_float2(0.f, 0.f);
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
         kidx[k] = (nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16);
@@ -466,10 +468,20 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     int since_flush = 0;
     double energy = S.energy, sum_du = 0.0;
     double M[3] = {S.M[0], S.M[1], S.M[2]};
-    float2 dl[KPT];
-#pragma unroll
-    for (int r = 0; r < KPT; r++) dl[r] = make_float2(0.f, 0.f);
 
+    // phase timers (profiling only; every phase still runs): slots
+    // 0 deferred Q commit, 1 Ewald, 2 pairs, 3 reduce + barrier 1, 4 decision, 5 commit,
+    // 6 prepare next, 7 barrier 2 (warp 0); 8 compute, 9 barrier 1, 10 barrier 2 (warp 1); 11 moves
+    const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
+    unsigned long long tacc[kPhaseSlots] = {0};
+    long long tprev = timing ? clock64() : 0;
+    auto tick = [&](int slot) {
+        if (timing) {
+            const long long t = clock64();
+            tacc[slot] += (unsigned long long)(t - tprev);
+            tprev = t;
+        }
+    };
     if (tid == 0) {
         ms.prev_accept = 0;
         ms.consumed = 0;
@@ -486,15 +498,12 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         if (ms.stop) break;
         // ---- the previous move's Q(k) change (State::sync trial -> accepted, deferred)
         if (ms.prev_accept) {
-#pragma unroll
-            for (int r = 0; r < KPT; r++) {
-                const int k = tid + r * NT;
-                if (k < K) {
-                    float2 pe = pend[k];
-                    pe.x += dl[r].x;
-                    pe.y += dl[r].y;
-                    pend[k] = pe;
-                }
+            for (int k = tid; k < K; k += NT) {
+                float2 pe = pend[k];
+                const float2 d = dlt[k];
+                pe.x += d.x;
+                pe.y += d.y;
+                pend[k] = pe;
             }
             if (++since_flush == kFlushAccepts) { // FP32 pending -> FP64 master
                 since_flush = 0;
@@ -511,6 +520,10 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         }
         const int kind = ms.kind;
         const int m = ms.m;
+        if (timing) {
+            tick(0);
+            if (tid == 0) tacc[11]++;
+        }
 
         // ---- energy change of this move
         FF accp{0.f, 0.f}, accr{0.f, 0.f};
@@ -518,14 +531,34 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         int flags = 0;
         if (kind != FAU_MOVE_NONE) {
             if (K) {
-                const bool tables = m <= kTableAtoms;
-#pragma unroll
-                for (int r = 0; r < KPT; r++) {
-                    const int k = tid + r * NT;
-                    float2 d = make_float2(0.f, 0.f);
-                    if (k < K) {
+                // one thread per k-vector (strided): d = sum_a q_a (e_new - e_old) from the phase tables
+                if (m == 1) {
+                    const float2* t = tab;
+                    const float f0 = 2.f * ms.q[0];
+                    for (int k = tid; k < K; k += NT) {
                         const int ki = kidx[k];
                         const int ix = ki & 0xff, iy = (ki >> 8) & 0xff, iz = ki >> 16;
+                        const float2 qb = Qb[k], pe = pend[k];
+                        const float af = Af[k];
+                        const float2 eo = cmul(t[ix], cmul(t[TS + iy], t[2 * TS + iz]));
+                        const float2 h = cmul(t[3 * TS + ix], cmul(t[4 * TS + iy], t[5 * TS + iz]));
+                        const float2 pp = cmul(eo, h);
+                        const float f = f0 * h.y;
+                        const float2 d = make_float2(-f * pp.y, f * pp.x);
+                        dlt[k] = d;
+                        const float qx = qb.x + pe.x, qy = qb.y + pe.y;
+                        const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
+                        const float dd = fmaf(d.x, d.x, d.y * d.y);
+                        ff_add(accr, af * (cross + dd));
+                        if (detail) scale += af * (fabsf(cross) + dd);
+                    }
+                }
+                else {
+                    const bool tables = m <= kTableAtoms;
+                    for (int k = tid; k < K; k += NT) {
+                        const int ki = kidx[k];
+                        const int ix = ki & 0xff, iy = (ki >> 8) & 0xff, iz = ki >> 16;
+                        float2 d = make_float2(0.f, 0.f);
                         for (int a = 0; a < m; a++) {
                             float2 eo, h;
                             if (tables) {
@@ -541,11 +574,12 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                                 sincospif(fmaf((float)nx, g.x, fmaf((float)ny, g.y, (float)nz * g.z)), &sh, &ch);
                                 h = make_float2(ch, sh);
                             }
-                            const float2 p = cmul(eo, h);
+                            const float2 pp = cmul(eo, h);
                             const float f = 2.f * ms.q[a] * h.y;
-                            d.x = fmaf(-f, p.y, d.x);
-                            d.y = fmaf(f, p.x, d.y);
+                            d.x = fmaf(-f, pp.y, d.x);
+                            d.y = fmaf(f, pp.x, d.y);
                         }
+                        dlt[k] = d;
                         const float2 qb = Qb[k], pe = pend[k];
                         const float qx = qb.x + pe.x, qy = qb.y + pe.y;
                         const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
@@ -554,17 +588,12 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                         ff_add(accr, af * (cross + dd));
                         if (detail) scale += af * (fabsf(cross) + dd);
                     }
-                    dl[r] = d;
                 }
                 n_k += (unsigned long long)m * (unsigned long long)((K - tid + NT - 1) / NT > 0 ? (K - tid + NT - 1) / NT : 0);
-                if (A.pending_dq) {
-#pragma unroll
-                    for (int r = 0; r < KPT; r++) {
-                        const int k = tid + r * NT;
-                        if (k < K) A.pending_dq[k] = make_double2((double)dl[r].x, (double)dl[r].y);
-                    }
-                }
+                if (A.pending_dq)
+                    for (int k = tid; k < K; k += NT) A.pending_dq[k] = make_double2((double)dlt[k].x, (double)dlt[k].y);
             }
+            tick(tid == 0 ? 1 : 8);
 
             if (kind == FAU_MOVE_ATOMIC) {
                 const int i = ms.index;
@@ -612,11 +641,16 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                         const uint4 rj = S.rec[j];
                         const int pidx = ti * nt + (rj.w >> 24);
                         const PairF p = pt[pidx];
-                        bool ni = false, nn = false, oi = false, on = false;
+                        float uu[2];
+                        bool fi[2], fn[2];
                         float mg = 0.f;
-                        const float un = pair_u32(S, p, pidx, r2_fixed(S, rn, rj), ms.xn[0], j, ni, nn, mg);
-                        const float uo = pair_u32(S, p, pidx, r2_fixed(S, ro, rj), ms.xo[0], j, oi, on, mg);
-                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                        for (int st = 0; st < 2; st++) { // st 0: trial (new), 1: accepted (old)
+                            fi[st] = false;
+                            fn[st] = false;
+                            uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ro : rn, rj), st ? ms.xo[0] : ms.xn[0], j,
+                                              fi[st], fn[st], mg);
+                        }
+                        add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
                         if (detail) scale += mg;
                         n_pairs += 2;
                     }
@@ -638,17 +672,17 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                         for (int a = 0; a < m; a++) {
                             const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
                             const PairF p = pt[pidx];
-                            bool ni = false, nn = false, oi = false, on = false;
+                            float uu[2] = {0.f, 0.f};
+                            bool fi[2] = {false, false}, fn[2] = {false, false};
                             float mg = 0.f;
-                            const float un = cut_n ? 0.f
-                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b,
-                                                              ni, nn, mg);
-                            const float uo = cut_o ? 0.f
-                                                   : pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b,
-                                                              oi, on, mg);
-                            add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                            for (int st = 0; st < 2; st++) {
+                                if (st ? cut_o : cut_n) continue;
+                                uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ms.rec_old[a] : ms.rec_new[a], rb),
+                                                  st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
+                                n_pairs++;
+                            }
+                            add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
                             if (detail) scale += mg;
-                            n_pairs += (cut_n ? 0 : 1) + (cut_o ? 0 : 1);
                         }
                     }
                 }
@@ -659,11 +693,16 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     for (int a = 0; a < m; a++) {
                         const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
                         const PairF p = pt[pidx];
-                        bool ni = false, nn = false, oi = false, on = false;
+                        float uu[2];
+                        bool fi[2], fn[2];
                         float mg = 0.f;
-                        const float un = pair_u32(S, p, pidx, r2_fixed(S, ms.rec_new[a], rb), ms.xn[a], b, ni, nn, mg);
-                        const float uo = pair_u32(S, p, pidx, r2_fixed(S, ms.rec_old[a], rb), ms.xo[a], b, oi, on, mg);
-                        add_pair(accp, flags, un, uo, ni, oi, nn, on);
+                        for (int st = 0; st < 2; st++) {
+                            fi[st] = false;
+                            fn[st] = false;
+                            uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ms.rec_old[a] : ms.rec_new[a], rb),
+                                              st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
+                        }
+                        add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
                         if (detail) scale += mg;
                         n_pairs += 2;
                     }
@@ -671,6 +710,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             }
         }
 
+        tick(tid == 0 ? 2 : 8);
         // ---- reduce: per warp, then warp 0 (B1)
         if (!detail) accp = ff_sum(accp, accr);
         warp_reduce(accp, accr, scale, flags, detail);
@@ -681,6 +721,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             red_f[warp] = flags;
         }
         __syncthreads();
+        tick(tid == 0 ? 3 : 9);
 
         if (warp == 0) {
             accp = lane < NW ? red_a[lane] : FF{0.f, 0.f};
@@ -765,6 +806,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             }
             accept = __shfl_sync(0xffffffffu, accept, 0);
             stop = __shfl_sync(0xffffffffu, stop, 0);
+            tick(4);
             if (stop) {
                 if (lane == 0) {
                     ms.stop = stop;
@@ -824,6 +866,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     stop = __shfl_sync(0xffffffffu, stop, 0);
                 }
                 __syncwarp();
+                tick(5);
                 if (stop) {
                     if (lane == 0) {
                         ms.stop = stop;
@@ -846,22 +889,24 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     ms.prev_accept = accept;
                     ms.consumed = mv + 1;
                 }
+                tick(6);
             }
         }
         __syncthreads(); // B2
+        tick(tid == 0 ? 7 : 10);
     }
+    if (timing)
+        for (int j = 0; j < kPhaseSlots; j++)
+            if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kPhaseSlots + j], tacc[j]);
 
     // the last accepted move's Q(k) change, then everything pending into the FP64 master
     if (ms.prev_accept) {
-#pragma unroll
-        for (int r = 0; r < KPT; r++) {
-            const int k = tid + r * NT;
-            if (k < K) {
-                float2 pe = pend[k];
-                pe.x += dl[r].x;
-                pe.y += dl[r].y;
-                pend[k] = pe;
-            }
+        for (int k = tid; k < K; k += NT) {
+            float2 pe = pend[k];
+            const float2 d = dlt[k];
+            pe.x += d.x;
+            pe.y += d.y;
+            pend[k] = pe;
         }
     }
     for (int k = tid; k < K; k += NT) {
@@ -907,23 +952,25 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 // dynamic shared memory of a chain kernel for K k-vectors and table size nc
 __host__ __device__ inline size_t chain_smem_bytes_v2(int K, int nc)
 {
-    return (size_t)K * (2 * sizeof(float2) + sizeof(int) + sizeof(float)) +
+    return (size_t)K * (3 * sizeof(float2) + sizeof(int) + sizeof(float)) +
            (size_t)kTableAtoms * 6 * (2 * nc + 1) * sizeof(float2);
 }
 
-template <int NT, int KPT, bool PH>
+template <int NT, bool PH>
 cudaError_t launch_chain_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
 {
-    static size_t granted = 48 * 1024;
+    // the dynamic allowance is raised on demand (the 48 KiB default also covers the static shared
+    // memory), never inside a stream capture: callers prepare first
+    static size_t granted = 0;
     const size_t smem = chain_smem_bytes_v2(K, nc);
-    if (smem > granted) { // raised on demand, never inside a capture (callers prepare first)
-        cudaError_t e = cudaFuncSetAttribute(chain_kernel<NT, KPT, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (smem > granted || granted == 0) {
+        cudaError_t e = cudaFuncSetAttribute(chain_kernel<NT, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         granted = smem;
     }
     if (prepare_only) return cudaSuccess;
-    chain_kernel<NT, KPT, PH><<<nblocks, NT, smem, st>>>(a);
+    chain_kernel<NT, PH><<<nblocks, NT, smem, st>>>(a);
     return cudaGetLastError();
 }
 

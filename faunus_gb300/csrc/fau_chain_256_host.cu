@@ -1,20 +1,11 @@
-// fau_chain_256_host.cu -- chain kernel instantiations: 256 threads per chain, host-fed proposals.
+// fau_chain_256_host.cu -- chain kernel instantiation: 256 threads per chain, host-fed proposals.
 #include "fau_chain.cuh"
 
 namespace fau {
 
-cudaError_t chain_dispatch_256_host(const ChainArgs& a, int nb, int K, int nc, int kpt, cudaStream_t st, bool prep)
+cudaError_t chain_dispatch_256_host(const ChainArgs& a, int nb, int K, int nc, cudaStream_t st, bool prep)
 {
-    switch (kpt) {
-    case 1: return launch_chain_inst<256, 1, false>(a, nb, K, nc, st, prep);
-    case 2: return launch_chain_inst<256, 2, false>(a, nb, K, nc, st, prep);
-    case 3: return launch_chain_inst<256, 3, false>(a, nb, K, nc, st, prep);
-    case 5: return launch_chain_inst<256, 5, false>(a, nb, K, nc, st, prep);
-    case 8: return launch_chain_inst<256, 8, false>(a, nb, K, nc, st, prep);
-    case 12: return launch_chain_inst<256, 12, false>(a, nb, K, nc, st, prep);
-    case 18: return launch_chain_inst<256, 18, false>(a, nb, K, nc, st, prep);
-    default: return cudaErrorInvalidValue;
-    }
+    return launch_chain_inst<256, false>(a, nb, K, nc, st, prep);
 }
 
 } // namespace fau

@@ -284,33 +284,16 @@ __global__ void plain_commit_kernel(DevSys* Sp, const PlainMove* P, const double
 // ---------------------------------------------------------------- launchers
 size_t chain_smem_bytes(int K, int nc) { return chain_smem_bytes_v2(K, nc); }
 
-// k-vectors per thread of the instantiated chain kernels (fau_chain_*.cu)
-static const int kKpt128[] = {1, 2, 4, 6, 9, 12, 18, 24, 36};
-static const int kKpt256[] = {1, 2, 3, 5, 8, 12, 18};
-
-static int pick_kpt(int K, int NT)
-{
-    const int need = (K + NT - 1) / NT;
-    const int* t = NT == 128 ? kKpt128 : kKpt256;
-    const int n = NT == 128 ? 9 : 7;
-    for (int i = 0; i < n; i++)
-        if (t[i] >= need) return t[i];
-    return -1;
-}
-
-int chain_max_k(int threads) { return threads == 128 ? 128 * 36 : 256 * 18; }
+int chain_max_k(int threads) { return 6400; }
 
 cudaError_t chain_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int threads, bool philox,
                               cudaStream_t st, bool prepare_only)
 {
-    const int NT = threads == 128 ? 128 : 256;
-    const int kpt = pick_kpt(K, NT);
-    if (kpt < 0) return cudaErrorInvalidValue;
-    if (NT == 128)
-        return philox ? chain_dispatch_128_ph(a, nblocks, K, nc, kpt, st, prepare_only)
-                      : chain_dispatch_128_host(a, nblocks, K, nc, kpt, st, prepare_only);
-    return philox ? chain_dispatch_256_ph(a, nblocks, K, nc, kpt, st, prepare_only)
-                  : chain_dispatch_256_host(a, nblocks, K, nc, kpt, st, prepare_only);
+    if (threads == 128)
+        return philox ? chain_dispatch_128_ph(a, nblocks, K, nc, st, prepare_only)
+                      : chain_dispatch_128_host(a, nblocks, K, nc, st, prepare_only);
+    return philox ? chain_dispatch_256_ph(a, nblocks, K, nc, st, prepare_only)
+                  : chain_dispatch_256_host(a, nblocks, K, nc, st, prepare_only);
 }
 
 cudaError_t prepare_chain(int K, int nc, int threads, bool philox)

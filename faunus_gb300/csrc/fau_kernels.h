@@ -30,7 +30,10 @@ struct ChainArgs {
     // written to `pending` and its Q(k) change to `pending_dq` for a later commit
     struct PlainMove* pending;
     double2* pending_dq;
+    // optional per-CTA phase timers (clock64 cycles, kPhaseSlots per CTA) for profiling
+    unsigned long long* phase_cycles;
 };
+constexpr int kPhaseSlots = 12;
 
 // One trial move held for a later commit (plain FP64 form and evaluate-only mode).
 struct PlainMove {
@@ -50,11 +53,11 @@ size_t chain_smem_bytes(int K, int nc);
 int chain_max_k(int threads);
 cudaError_t prepare_chain(int K, int nc, int threads, bool philox);
 cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int threads, bool philox, cudaStream_t st);
-// per (CTA size, proposal source) dispatch over the instantiated k-per-thread variants
-cudaError_t chain_dispatch_128_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
-cudaError_t chain_dispatch_128_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
-cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
-cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+// per (CTA size, proposal source) instantiations of the chain kernel
+cudaError_t chain_dispatch_128_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_128_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
