@@ -296,7 +296,8 @@ def run_ours(args) -> None:
                                "ncutoff 8, 45^3 cells, transrot dp 2 A) x R replica chains",
                    "replicas_per_gpu": R, "moves_per_replica_per_step": M, "n_particles": base.n,
                    "kvectors": systems[0].K, "cells": "x".join(map(str, systems[0].cell_grid())),
-                   "threads_per_chain": args.threads or 256,
+                   "threads_per_chain": args.threads or 160,
+                   "kernel": "pipelined chain kernel" if args.threads in (0, 160) else "chain kernel",
                    "l2": f"inputs larger than L2: {resident / 2**30:.1f} GiB resident per GPU",
                    "parallelism": f"replicas (dp{world})", "rng": "Philox4x32-10 on device (value); "
                    "reference mt19937 stream on host (e2e)"},
@@ -354,7 +355,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--replicas", type=int, default=0, help="replica chains per GPU (0: 2 x SMs)")
     ap.add_argument("--moves", type=int, default=10000, help="moves per replica per step")
-    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--threads", type=int, default=0,
+                    help="chain CTA size: 0 = pipelined kernel (1 producer + 4 compute warps), 128/256 = chain kernel")
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")

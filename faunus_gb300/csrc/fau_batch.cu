@@ -104,23 +104,51 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     std::vector<uint32_t> ids(n);
     std::vector<uint8_t> mol(n);
     std::vector<double> tref(n, 1.0);
-    int Kmax = 0, ncmax = 0;
     for (int i = 0; i < n; i++) {
         fau_ctx* c2;
         int K, np, ng, mo, knc;
         fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tref[i], &knc);
         if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
-        Kmax = std::max(Kmax, K);
-        ncmax = std::max(ncmax, knc);
         nm[i] = P->moves_per_system ? P->moves_per_system[i] : P->moves;
         if (nm[i] < 0) return fau_internal_fail(FAU_ERR_ARG, "negative move count");
         ids[i] = P->streams ? P->streams[i] : (uint32_t)i;
         mol[i] = (uint8_t)mo;
         if (pt) tref[i] = P->temperatures[i];
     }
-    const int threads = P->threads > 0 ? P->threads : 128;
-    if (threads != 128 && threads != 256) return fau_internal_fail(FAU_ERR_ARG, "threads must be 128 or 256");
-    if (Kmax > chain_max_k(threads) || chain_smem_bytes(Kmax, ncmax) + 16384 > 227 * 1024)
+    // kernel choice: threads 0 or 160 -> the pipelined kernel for every system whose device proposals
+    // are single-atom moves (the others run in the 128-thread chain kernel); 128 or 256 -> the chain
+    // kernel of that size for all systems
+    const int req = P->threads;
+    if (req != 0 && req != 128 && req != 160 && req != 256)
+        return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 128, 160 or 256");
+    const int threads = (req == 0 || req == 160) ? 128 : req;
+    const bool use_fast = req == 0 || req == 160;
+    std::vector<int> order;   // kernel order: pipelined-kernel systems first
+    order.reserve(n);
+    for (int i = 0; i < n; i++)
+        if (use_fast && !mol[i]) order.push_back(i);
+    const int nfast = (int)order.size();
+    for (int i = 0; i < n; i++)
+        if (!(use_fast && !mol[i])) order.push_back(i);
+    const int nexact = n - nfast;
+    int Kf = 0, ncf = 0, Ke = 0, nce = 0;
+    for (int r = 0; r < n; r++) {
+        int K, np, ng, mo, knc;
+        fau_ctx* c2;
+        DevSys* dd;
+        double tr;
+        fau_internal_sys_view(systems[order[r]], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+        if (r < nfast) {
+            Kf = std::max(Kf, K);
+            ncf = std::max(ncf, knc);
+        }
+        else {
+            Ke = std::max(Ke, K);
+            nce = std::max(nce, knc);
+        }
+    }
+    if ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
+        (nfast && fast_smem_bytes_total(Kf, ncf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
 
     // device argument arrays (one allocation, freed at the end of the call)
@@ -129,13 +157,28 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     const size_t off_sys = 0, off_nm = al(off_sys + sizeof(DevSys*) * n), off_ids = al(off_nm + 8 * n),
                  off_mol = al(off_ids + 4 * n), off_slot = al(off_mol + n), off_T = al(off_slot + 4 * n),
                  off_Tref = al(off_T + 8 * n), off_sum = al(off_Tref + 8 * n),
-                 off_st = al(off_sum + sizeof(SysSummary) * n), off_ctr = al(off_st + 64), total = al(off_ctr + 8 * n);
+                 off_st = al(off_sum + sizeof(SysSummary) * n), off_ctr = al(off_st + 64),
+                 off_ksys = al(off_ctr + 8 * n), off_knm = al(off_ksys + sizeof(DevSys*) * n),
+                 off_kids = al(off_knm + 8 * n), off_kmol = al(off_kids + 4 * n), off_kctr = al(off_kmol + n),
+                 total = al(off_kctr + 8 * n);
     unsigned char* dbuf = nullptr;
     if (cudaMalloc(&dbuf, total) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
     std::vector<int> slot(n);
     for (int i = 0; i < n; i++) slot[i] = i;
     int rc = FAU_OK;
-    auto cleanup = [&]() { cudaFree(dbuf); };
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    auto release2 = [&]() {
+        if (st2) cudaStreamDestroy(st2);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
+        st2 = nullptr;
+        fork_ev = join_ev = nullptr;
+    };
+    auto cleanup = [&]() {
+        release2();
+        cudaFree(dbuf);
+    };
 #define BTRY(x)                                                                 \
     do {                                                                        \
         if ((x) != cudaSuccess) {                                               \
@@ -161,28 +204,72 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
     BTRY(cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st));
 
+    // per-CTA arguments in kernel order
+    std::vector<DevSys*> ksys(n);
+    std::vector<long long> knm(n);
+    std::vector<uint32_t> kids(n);
+    std::vector<uint8_t> kmol(n);
+    std::vector<unsigned long long> kctr(n, 0);
+    for (int r = 0; r < n; r++) {
+        const int i = order[r];
+        ksys[r] = dsys[i];
+        knm[r] = nm[i];
+        kids[r] = ids[i];
+        kmol[r] = mol[i];
+        if (P->counters) kctr[r] = P->counters[i];
+    }
+    BTRY(cudaMemcpyAsync(dbuf + off_ksys, ksys.data(), sizeof(DevSys*) * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_knm, knm.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_kids, kids.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_kmol, kmol.data(), n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_kctr, kctr.data(), 8 * n, cudaMemcpyHostToDevice, st));
     ChainArgs a{};
-    a.sys = d_sys;
-    a.sys_ids = reinterpret_cast<const uint32_t*>(dbuf + off_ids);
+    a.sys = reinterpret_cast<DevSys* const*>(dbuf + off_ksys);
+    a.sys_ids = reinterpret_cast<const uint32_t*>(dbuf + off_kids);
     a.seed = P->seed;
     a.dp = P->dp;
     a.dprot = P->dprot;
-    a.molecular = reinterpret_cast<const uint8_t*>(dbuf + off_mol);
-    if (P->counters) {
-        BTRY(cudaMemcpyAsync(dbuf + off_ctr, P->counters, 8 * n, cudaMemcpyHostToDevice, st));
-        a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_ctr);
-    }
+    a.molecular = reinterpret_cast<const uint8_t*>(dbuf + off_kmol);
+    if (P->counters) a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_kctr);
     const int nblk = pt ? P->n_swap_blocks : 1;
     if (pt) {
         a.n_moves = nullptr;
         a.moves = P->swap_interval_moves;
     }
     else {
-        BTRY(cudaMemcpyAsync(dbuf + off_nm, nm.data(), 8 * n, cudaMemcpyHostToDevice, st));
-        a.n_moves = reinterpret_cast<const long long*>(dbuf + off_nm);
+        a.n_moves = reinterpret_cast<const long long*>(dbuf + off_knm);
     }
-    // set the kernel's shared-memory attribute before the capture starts
-    BTRY(prepare_chain(Kmax, ncmax, threads, true));
+    // the same arguments shifted to the chain-kernel systems
+    ChainArgs ae = a;
+    ae.sys = a.sys + nfast;
+    ae.sys_ids = a.sys_ids + nfast;
+    ae.molecular = a.molecular + nfast;
+    if (a.counters) ae.counters = a.counters + nfast;
+    if (a.n_moves) ae.n_moves = a.n_moves + nfast;
+    // set the kernels' shared-memory attributes before the capture starts
+    if (nexact) BTRY(prepare_chain(Ke, nce, threads, true));
+    if (nfast) BTRY(prepare_fast(Kf, ncf, 4, true));
+    if (nfast && nexact) {
+        BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+        BTRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        BTRY(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+    }
+    // one block of moves: the pipelined kernel on `st`, the chain kernel on a forked stream
+    auto launch_block = [&](unsigned long long cbase) -> cudaError_t {
+        a.counter_base = cbase;
+        ae.counter_base = cbase;
+        cudaError_t e = cudaSuccess;
+        if (nfast && nexact) {
+            if ((e = cudaEventRecord(fork_ev, st)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st2, fork_ev, 0)) != cudaSuccess) return e;
+            if ((e = launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, 4, true, st)) != cudaSuccess) return e;
+            return cudaStreamWaitEvent(st, join_ev, 0);
+        }
+        if (nfast) return launch_fast(a, nfast, Kf, ncf, 4, true, st);
+        return launch_chain(ae, nexact, Ke, nce, threads, true, st);
+    };
 
     // profiling: FAU_PHASE_TIMING=1 prints the chain kernel's per-phase cycles to stderr
     unsigned long long* d_phase = nullptr;
@@ -200,8 +287,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     cudaGraphExec_t exec = nullptr;
     BTRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int b = 0; b < nblk; b++) {
-        a.counter_base = P->counter_base + (unsigned long long)b * (pt ? (unsigned long long)P->swap_interval_moves : 0ull);
-        if (launch_chain(a, n, Kmax, ncmax, threads, true, st) != cudaSuccess) {
+        const unsigned long long cbase =
+            P->counter_base + (unsigned long long)b * (pt ? (unsigned long long)P->swap_interval_moves : 0ull);
+        if (launch_block(cbase) != cudaSuccess) {
             cudaStreamEndCapture(st, &graph);
             if (graph) cudaGraphDestroy(graph);
             cleanup();
@@ -230,6 +318,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     cudaGraphDestroy(graph);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    release2();
     if (se != cudaSuccess) {
         cleanup();
         if (d_phase) cudaFree(d_phase);
@@ -285,7 +374,8 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     if (cudaSetDevice(device) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "cudaSetDevice failed");
     std::vector<DevSys*> dsys(n);
     std::vector<long long> nm(n), off(n);
-    int Kmax = 0, ncmax = 0;
+    std::vector<int> Kv(n), ncv(n);
+    std::vector<uint8_t> has_mol(n, 0);
     const long long total = offsets[n];
     if (offsets[0] != 0 || total < 0) return fau_internal_fail(FAU_ERR_ARG, "offsets must start at 0");
     for (int i = 0; i < n; i++) {
@@ -293,12 +383,12 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         int K, np, ng, mo, knc;
         double tr;
         fau_internal_sys_view(systems[i], &c2, &dsys[i], &K, &np, &ng, &mo, &tr, &knc);
-        ncmax = std::max(ncmax, knc);
         if (c2 != ctx) return fau_internal_fail(FAU_ERR_ARG, "system from another context");
         if (offsets[i + 1] < offsets[i]) return fau_internal_fail(FAU_ERR_ARG, "offsets not sorted");
         nm[i] = offsets[i + 1] - offsets[i];
         off[i] = offsets[i];
-        Kmax = std::max(Kmax, K);
+        Kv[i] = K;
+        ncv[i] = knc;
         for (long long m = offsets[i]; m < offsets[i + 1]; m++) {
             const fau_proposal& p = props[m];
             if (p.kind == FAU_MOVE_ATOMIC) {
@@ -306,16 +396,41 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             }
             else if (p.kind == FAU_MOVE_MOLECULAR) {
                 if (p.index < 0 || p.index >= ng) return fau_internal_fail(FAU_ERR_ARG, "group out of range");
+                has_mol[i] = 1;
             }
             else if (p.kind != FAU_MOVE_NONE) {
                 return fau_internal_fail(FAU_ERR_ARG, "unknown proposal kind");
             }
         }
     }
-    if (Kmax > chain_max_k(128) || chain_smem_bytes(Kmax, ncmax) + 16384 > 227 * 1024)
+    // systems with only single-atom (or empty) proposals run in the pipelined kernel, the rest in the
+    // 128-thread chain kernel; kernel order puts the former first
+    std::vector<int> order;
+    order.reserve(n);
+    for (int i = 0; i < n; i++)
+        if (!has_mol[i]) order.push_back(i);
+    const int nfast = (int)order.size();
+    for (int i = 0; i < n; i++)
+        if (has_mol[i]) order.push_back(i);
+    const int nexact = n - nfast;
+    int Kf = 0, ncf = 0, Ke = 0, nce = 0;
+    for (int r = 0; r < n; r++) {
+        const int i = order[r];
+        if (r < nfast) {
+            Kf = std::max(Kf, Kv[i]);
+            ncf = std::max(ncf, ncv[i]);
+        }
+        else {
+            Ke = std::max(Ke, Kv[i]);
+            nce = std::max(nce, ncv[i]);
+        }
+    }
+    if ((nexact && (Ke > chain_max_k(128) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
+        (nfast && fast_smem_bytes_total(Kf, ncf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t o_sys = 0, o_nm = al(o_sys + 8 * n), o_off = al(o_nm + 8 * n), o_sum = al(o_off + 8 * n),
+    const size_t o_sys = 0, o_ksys = al(o_sys + 8 * n), o_nm = al(o_ksys + 8 * n), o_off = al(o_nm + 8 * n),
+                 o_sum = al(o_off + 8 * n),
                  o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * total),
                  o_du = al(o_acc + total), bytes = al(o_du + 8 * total);
     unsigned char* dbuf = nullptr;
@@ -327,16 +442,24 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     DevSys* const* d_sys = reinterpret_cast<DevSys* const*>(dbuf + o_sys);
     SysSummary* d_sum = reinterpret_cast<SysSummary*>(dbuf + o_sum);
     std::vector<SysSummary> s0(n), s1(n);
+    std::vector<DevSys*> ksys(n);
+    std::vector<long long> knm(n), koff(n);
+    for (int r = 0; r < n; r++) {
+        ksys[r] = dsys[order[r]];
+        knm[r] = nm[order[r]];
+        koff[r] = off[order[r]];
+    }
     if (cudaMemcpyAsync(dbuf + o_sys, dsys.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(dbuf + o_nm, nm.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(dbuf + o_off, off.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_ksys, ksys.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_nm, knm.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dbuf + o_off, koff.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(dbuf + o_props, props, sizeof(fau_proposal) * total, cudaMemcpyHostToDevice, st) !=
             cudaSuccess)
         return done(FAU_ERR_CUDA, "proposal upload failed");
     gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
     cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st);
     ChainArgs a{};
-    a.sys = d_sys;
+    a.sys = reinterpret_cast<DevSys* const*>(dbuf + o_ksys);
     a.n_moves = reinterpret_cast<const long long*>(dbuf + o_nm);
     a.prop_off = reinterpret_cast<const long long*>(dbuf + o_off);
     a.props = reinterpret_cast<const fau_proposal*>(dbuf + o_props);
@@ -345,8 +468,36 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    ChainArgs ae = a;
+    ae.sys = a.sys + nfast;
+    ae.n_moves = a.n_moves + nfast;
+    ae.prop_off = a.prop_off + nfast;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    bool ok = true;
+    if (nfast && nexact) {
+        ok = cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming) == cudaSuccess;
+    }
     cudaEventRecord(e0, st);
-    if (launch_chain(a, n, Kmax, ncmax, 128, false, st) != cudaSuccess) {
+    if (ok && nexact) {
+        if (nfast) {
+            ok = cudaEventRecord(fork_ev, st) == cudaSuccess && cudaStreamWaitEvent(st2, fork_ev, 0) == cudaSuccess &&
+                 launch_chain(ae, nexact, Ke, nce, 128, false, st2) == cudaSuccess &&
+                 cudaEventRecord(join_ev, st2) == cudaSuccess;
+        }
+        else {
+            ok = launch_chain(ae, nexact, Ke, nce, 128, false, st) == cudaSuccess;
+        }
+    }
+    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, 4, false, st) == cudaSuccess;
+    if (ok && nfast && nexact) ok = cudaStreamWaitEvent(st, join_ev, 0) == cudaSuccess;
+    if (!ok) {
+        cudaStreamSynchronize(st);
+        if (st2) cudaStreamDestroy(st2);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return done(FAU_ERR_CUDA, "chain launch failed");
@@ -361,6 +512,9 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st2) cudaStreamDestroy(st2);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
     if (se != cudaSuccess) return done(FAU_ERR_CUDA, cudaGetErrorString(se));
     fau_batch_stats S{};
     int derr = FAU_OK;

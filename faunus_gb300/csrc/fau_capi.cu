@@ -248,6 +248,18 @@ int plan_layout(const fau_sys_desc* d, Layout& lay)
     return FAU_OK;
 }
 
+// slots per cell: at least the requested count (else twice the mean occupancy
+// plus four), four more than the fullest cell, at least 8, rounded up to a
+// power of two so a slot index splits into (cell, slot) by shifts
+int cell_capacity(int requested, int maxc, double mean)
+{
+    int c = requested > 0 ? requested : (int)std::ceil(2.0 * mean) + 4;
+    c = std::max(std::max(c, maxc + 4), 8);
+    int p = 8;
+    while (p < c) p *= 2;
+    return p;
+}
+
 // bin one position, reference formula (bit-exact with the oracle)
 int host_cell(const double* x, const double L[3], const int dims[3], const double cell[3])
 {
@@ -350,10 +362,10 @@ int fau_sys_footprint(const fau_sys_desc* d, size_t* bytes)
     Layout lay;
     rc = plan_layout(d, lay);
     if (rc) return rc;
-    int cap = d->cell_capacity > 0 ? d->cell_capacity : 0;
-    if (lay.cells && cap == 0) {
+    int cap = 0;
+    if (lay.cells) {
         const double ncell = (double)lay.cdim[0] * lay.cdim[1] * lay.cdim[2];
-        cap = std::max(16, (int)std::ceil(4.0 * d->n_particles / ncell) + 16);
+        cap = cell_capacity(d->cell_capacity, 0, d->n_particles / ncell);
     }
     *bytes = footprint_bytes(d, lay, cap);
     return FAU_OK;
@@ -542,11 +554,8 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
             cell_of[i] = host_cell(p, d->box, lay.cdim, lay.cell_len);
             slot_of[i] = cnt[cell_of[i]]++;
         }
-        int maxc = *std::max_element(cnt.begin(), cnt.end());
-        int cap = d->cell_capacity > 0 ? d->cell_capacity
-                                       : std::max(16, (int)std::ceil(4.0 * n / (double)ncell) + 16);
-        cap = std::max(cap, maxc + 8);
-        cap = (cap + 3) & ~3;
+        const int maxc = *std::max_element(cnt.begin(), cnt.end());
+        const int cap = cell_capacity(d->cell_capacity, maxc, n / (double)ncell);
         std::vector<uint4> crec((size_t)ncell * cap, make_uint4(0, 0, 0, 0xFFFFFFFFu));
         for (int i = 0; i < n; i++) crec[(size_t)cell_of[i] * cap + slot_of[i]] = rec[i];
         for (int k = 0; k < 3; k++) {
@@ -837,8 +846,7 @@ static int rebuild_cells(fau_sys* s, int cap)
         slot_of[i] = cnt[cell_of[i]]++;
     }
     const int maxc = *std::max_element(cnt.begin(), cnt.end());
-    cap = std::max(cap, maxc + 8);
-    cap = (cap + 3) & ~3;
+    cap = cell_capacity(cap, maxc, n / (double)ncell);
     std::vector<uint4> crec((size_t)ncell * cap, make_uint4(0, 0, 0, 0xFFFFFFFFu));
     for (int i = 0; i < n; i++) crec[(size_t)cell_of[i] * cap + slot_of[i]] = rec[i];
     uint4* nrec = nullptr;

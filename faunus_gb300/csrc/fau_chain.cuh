@@ -845,6 +845,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                                     S.cell_rec[(size_t)co * S.cap + so] = mvd;
                                     S.slot_of[mvd.w & 0xFFFFFFu] = so;
                                 }
+                                S.cell_rec[(size_t)co * S.cap + last] = make_uint4(0u, 0u, 0u, kEmptySlot);
                                 S.cell_cnt[co] = last;
                                 const int sn = S.cell_cnt[cn];
                                 if (sn >= S.cap) {

@@ -10,8 +10,10 @@
 //                 copy with 2^32 units per box length.  Integer subtraction
 //                 of two records is the minimum-image separation (exact),
 //                 and n.u mod 2^32 is the exact reduced Ewald phase.
-//   cell_rec      the same records bucketed by cell (fixed capacity),
-//                 cell_cnt, cell_of, slot_of: incremental cell list.
+//   cell_rec      the same records bucketed by cell: `cap` slots per cell
+//                 (a power of two), the first cell_cnt[c] in use, the rest
+//                 holding .w = kEmptySlot; cell_of, slot_of: where each
+//                 particle is listed.  Updated incrementally on every accept.
 //   Q             Ewald structure factor, FP64 complex master copy.
 #pragma once
 #include <cstdint>
@@ -24,6 +26,7 @@ namespace fau {
 constexpr int kMaxITypes = 16;     // internal (type, charge) classes per system
 constexpr int kMaxGroupAtoms = 32; // atoms moved together in one molecular move
 constexpr int kFlushAccepts = 64;  // FP32 pending Q deltas flushed to FP64 every N accepts
+constexpr uint32_t kEmptySlot = 0xFFFFFFFFu; // .w of a cell-list slot at or beyond the cell's count
 
 enum SysFlags : int {
     SYS_CELLS = 1 << 0,   // single-atom moves use the cell list
@@ -204,10 +207,12 @@ __device__ __forceinline__ float r2_fixed(const DevSys& S, uint4 a, uint4 b)
 // hard-sphere contact; when the FP32 distance is within 1e-5 (relative) of one of
 // them, the reference FP64 distance (sqdist of the FP64 positions xi and particle
 // j) decides which side the pair is on, so inclusion matches the FP64 oracle.
-// `mag` accumulates the sum of |term| over the enabled terms (the floating-point
-// error scale of this pair energy).
+// `xj` (optional) replaces particle j's resident FP64 position when the caller
+// knows a newer one than memory holds.  `mag` accumulates the sum of |summand|
+// over the enabled terms, LJ's r^-12 and r^-6 parts counted separately (the
+// floating-point error scale of this pair energy).
 __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int pidx, float r2, const double* xi,
-                                          int j, bool& inf, bool& nan, float& mag)
+                                          int j, bool& inf, bool& nan, float& mag, const double* xj = nullptr)
 {
     const int terms = S.terms;
     const bool cut_coul = (terms & FAU_PAIR_COULOMB) && S.coul_type != FAU_COUL_PLAIN;
@@ -218,8 +223,8 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
                       (cut_coul && fabsf(r2 - S.rc2_coul) <= 1e-5f * S.rc2_coul) ||
                       ((terms & FAU_PAIR_HS) && fabsf(r2 - p.hs2) <= 1e-5f * p.hs2);
     if (near) {
-        const double xj[3] = {S.x[j], S.y[j], S.z[j]};
-        const double r2d = sqdist_d(S, xi, xj);
+        const double xr[3] = {xj ? xj[0] : S.x[j], xj ? xj[1] : S.y[j], xj ? xj[2] : S.z[j]};
+        const double r2d = sqdist_d(S, xi, xr);
         in_pair = !(S.rc2_pair_d > 0.0 && r2d >= S.rc2_pair_d);
         in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
         overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
@@ -249,15 +254,14 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
         // minimum, so the approximate rsqrt would cost ~10x the error
         float x = p.s2 * __frcp_rn(r2);
         x = x * x * x;
+        // error scale: the r^-12 and r^-6 parts separately (they cancel near r = sigma)
         if (terms & FAU_PAIR_LJ) {
-            const float l = p.e4 * (x * x - x);
-            u += l;
-            m += fabsf(l);
+            u += p.e4 * (x * x - x);
+            m += fabsf(p.e4) * (x * x + x);
         }
         if ((terms & FAU_PAIR_WCA) && !(r2 > p.s2 * 1.2599210498948732f)) {
-            const float w = p.e4 * (x * x - x + 0.25f);
-            u += w;
-            m += fabsf(w);
+            u += p.e4 * (x * x - x + 0.25f);
+            m += fabsf(p.e4) * (x * x + x + 0.25f);
         }
     }
     if (overlap) inf = true;

@@ -10,6 +10,7 @@
 //   plain_*           the plain FP64 single-move form: one move per call,
 //                     host-fed proposal and uniform (in-GPU comparison point).
 #include "fau_chain.cuh"
+#include "fau_fast.cuh"
 #include "fau_dev.cuh"
 #include "fau_kernels.h"
 
@@ -250,6 +251,7 @@ __global__ void plain_commit_kernel(DevSys* Sp, const PlainMove* P, const double
                         S.cell_rec[(size_t)co * S.cap + so] = mvd;
                         S.slot_of[mvd.w & 0xFFFFFFu] = so;
                     }
+                    S.cell_rec[(size_t)co * S.cap + last] = make_uint4(0u, 0u, 0u, kEmptySlot);
                     S.cell_cnt[co] = last;
                     const int sn = S.cell_cnt[cn];
                     if (sn >= S.cap) {
@@ -305,6 +307,31 @@ cudaError_t prepare_chain(int K, int nc, int threads, bool philox)
 cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int threads, bool philox, cudaStream_t st)
 {
     return chain_launch_impl(a, nblocks, K, nc, threads, philox, st, false);
+}
+
+size_t fast_smem_bytes_total(int K, int nc)
+{
+    // dynamic part + the kernel's static shared memory (move slots, proposal ring, partials)
+    return fast_smem_bytes(K, nc) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
+}
+
+static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox,
+                                    cudaStream_t st, bool prepare_only)
+{
+    if (warps != 4) return cudaErrorInvalidValue;
+    return philox ? fast_dispatch_4_ph(a, nblocks, K, nc, st, prepare_only)
+                  : fast_dispatch_4_host(a, nblocks, K, nc, st, prepare_only);
+}
+
+cudaError_t prepare_fast(int K, int nc, int warps, bool philox)
+{
+    ChainArgs a{};
+    return fast_launch_impl(a, 0, K, nc, warps, philox, nullptr, true);
+}
+
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox, cudaStream_t st)
+{
+    return fast_launch_impl(a, nblocks, K, nc, warps, philox, st, false);
 }
 
 // Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then

@@ -137,7 +137,9 @@ struct PairParams {
             u += (r2 < hs2[ab]) ? infty : 0.0;
         return u;
     }
-    // sum of |term| over the enabled terms: the floating-point error scale of a pair energy
+    // sum of |summand| over the enabled terms: the floating-point error scale of a pair
+    // energy.  The r^-12 and r^-6 parts of LJ / WCA count separately: they cancel near
+    // r = sigma, where the rounding error of any evaluation scales with their sum.
     double magnitude(int ta, int tb, double qa, double qb, double r2) const
     {
         if (pair_cutoff2 > 0.0 && r2 >= pair_cutoff2) return 0.0;
@@ -146,8 +148,9 @@ struct PairParams {
         if (terms & FAU_PAIR_COULOMB) m += std::fabs(coulomb(qa, qb, r2));
         double x = sigma2[ab] / r2;
         x = x * x * x;
-        if (terms & FAU_PAIR_LJ) m += std::fabs(eps4[ab] * (x * x - x));
-        if ((terms & FAU_PAIR_WCA) && !(r2 > sigma2[ab] * 1.2599210498948732)) m += std::fabs(eps4[ab] * (x * x - x + 0.25));
+        const double e = std::fabs(eps4[ab]);
+        if (terms & FAU_PAIR_LJ) m += e * (x * x + x);
+        if ((terms & FAU_PAIR_WCA) && !(r2 > sigma2[ab] * 1.2599210498948732)) m += e * (x * x + x + 0.25);
         return std::isfinite(m) ? m : 0.0;
     }
     // self energy per particle (NewCoulombGalore::setSelfEnergy src/potentials.cpp:1599-1604)

@@ -2,9 +2,9 @@
 
 Tolerance (FP32 pair and Ewald terms with compensated sums, FP64 totals):
     |dU_gpu - dU_oracle| <= 1e-6 * max(|dU|, S)
-where S is the sum of |term| magnitudes the change is summed from over both
-states: every pair potential term (Coulomb, LJ, WCA) of every pair counted
-separately, plus (2 pi lB / V) sum_k A_k (|2 Re(Q_k* d_k)| + |d_k|^2) for the
+where S is the sum of |summand| magnitudes the change is summed from over both
+states: every pair potential term of every pair counted separately (Coulomb,
+and the r^-12 and r^-6 parts of LJ and WCA, which cancel near r = sigma), plus (2 pi lB / V) sum_k A_k (|2 Re(Q_k* d_k)| + |d_k|^2) for the
 reciprocal change -- the floating-point error scale of the sum.  Accept sequences must be identical under the same proposal stream
 except at near ties, where u falls between exp(-dU_gpu) and exp(-dU_oracle);
 positions after an identical accept sequence are bit-identical (FP64 move

@@ -1,0 +1,164 @@
+"""GPU parity of the pipelined chain kernel (batched single-atom moves).
+
+fau_run_batch (threads 0 or 160) and fau_run_proposals_batch run every system
+whose proposals are single-atom translations in the pipelined kernel.  It must
+reproduce:
+  * the chain kernel (threads=128) under the same device proposals: the same
+    accept sequence and bit-identical FP64 positions (barring a near tie, where
+    u falls between the two FP32C energy changes' exponentials);
+  * the FP64 oracle under reference-stream host proposals, to the tolerance of
+    test_parity_gpu (1e-6 of max(|dU|, S));
+  * its own running energy against an FP64 recomputation of the total.
+Cases cover cell lists (union stencil box and the separate-stencil fallback of
+a 3x3x3 grid), frequent commit/stencil conflicts (small box), all-pairs with
+hard spheres, the Ewald surface term and batches mixing both kernels.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import faunus_gb300 as F
+from faunus_gb300 import _capi as A
+from faunus_gb300 import configs
+
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+CASES = {
+    "primitive_model": lambda: configs.primitive_model(n=200, seed=3),
+    "bulk_cells": lambda: configs.bulk_ewald(n_salt=1000, seed=4),
+    "bulk_surface": lambda: configs.bulk_ewald(n_salt=1000, epss=1.0, seed=5),
+    "bulk_small_box": lambda: configs.bulk_ewald(n_salt=100, seed=6),
+    "bulk_3x3x3_cells": lambda: configs.bulk_ewald(n_salt=50, L=40.0, seed=7),
+}
+
+
+def _energy_consistent(s):
+    e_run = s.running_energy()
+    s.q_rebuild()
+    e_tot = s.energy_total()["total"]
+    assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot)), (e_run, e_tot)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_pipelined_equals_chain_kernel(ctx, case):
+    spec = CASES[case]()
+    a, b = ctx.create(spec), ctx.create(spec)
+    if case == "bulk_3x3x3_cells":
+        assert a.cell_grid() == (3, 3, 3)
+    moves = 3000
+    sa = ctx.run_batch([a], moves, seed=21, streams=[5], dp=2.0, threads=0)
+    sb = ctx.run_batch([b], moves, seed=21, streams=[5], dp=2.0, threads=128)
+    assert sa["moves"] == sb["moves"] == moves
+    assert sa["accepted"] == sb["accepted"] and sa["accepted"] > 100
+    assert sa["pair_evals"] > 0
+    assert np.array_equal(a.positions(), b.positions())
+    ea, eb = a.running_energy(), b.running_energy()
+    assert abs(ea - eb) <= 1e-6 * max(1.0, abs(eb))
+    if a.cell_grid() != (0, 0, 0):
+        assert np.array_equal(a.cells(), b.cells())
+    if a.K:
+        assert np.abs(a.q() - b.q()).max() < 1e-4
+    _energy_consistent(a)
+
+
+def _oracle_compare(g_pos, acc_g, du_g, spec, props):
+    o = O.OracleSystem(spec)
+    det = o.run_detail(props)
+    acc_o, du_o, scale = det["accepted"].astype(np.uint8), det["du"], det["err_scale"]
+    mism = np.nonzero(acc_g != acc_o)[0]
+    first = int(mism[0]) if len(mism) else len(props)
+    sl = slice(0, first + 1 if first < len(props) else first)
+    fin = np.isfinite(du_o[sl])
+    assert np.array_equal(np.isfinite(du_g[sl]), fin)
+    err = np.abs(du_g[sl][fin] - du_o[sl][fin])
+    den = np.maximum(np.abs(du_o[sl][fin]), scale[sl][fin])
+    rel = err / np.where(den > 0, den, 1.0)
+    assert rel.max(initial=0.0) <= TOL, f"max rel err {rel.max():.3e}"
+    if len(mism):
+        m = first
+        lo, hi = sorted([math.exp(-min(du_g[m], 700)), math.exp(-min(du_o[m], 700))])
+        assert lo <= props["u"][m] <= hi
+        assert first > len(props) // 10
+    else:
+        assert np.array_equal(g_pos, o.positions())
+    return int(acc_g.sum())
+
+
+def test_pipelined_host_proposals_match_oracle(ctx):
+    specs = [CASES["primitive_model"](), CASES["bulk_cells"](), CASES["bulk_surface"](),
+             CASES["bulk_3x3x3_cells"]()]
+    systems = [ctx.create(s) for s in specs]
+    M = 3000
+    props = [F.MoveGenerator(s, s.extra["moves"], 31 + i, 37 + i, default_seeds=False).generate(M)
+             for i, s in enumerate(specs)]
+    allp = np.concatenate(props)
+    off = np.arange(len(specs) + 1, dtype=np.int64) * M
+    acc = np.zeros(len(allp), np.uint8)
+    du = np.zeros(len(allp))
+    st = ctx.run_proposals_batch(systems, allp, off, acc, du)
+    assert st["moves"] == len(allp)
+    for i, (s, spec) in enumerate(zip(systems, specs)):
+        sl = slice(i * M, (i + 1) * M)
+        n_acc = _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i])
+        assert n_acc > 100
+        _energy_consistent(s)
+
+
+def test_pipelined_empty_moves_and_reference_move_counts(ctx):
+    """FAU_MOVE_NONE proposals are skipped (not counted, never accepted)."""
+    spec = CASES["bulk_cells"]()
+    g = ctx.create(spec)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 3, 4, default_seeds=False).generate(500)
+    props["kind"][::3] = A.FAU_MOVE_NONE
+    acc = np.zeros(len(props), np.uint8)
+    du = np.zeros(len(props))
+    st = ctx.run_proposals_batch([g], props, np.array([0, len(props)], np.int64), acc, du)
+    none = props["kind"] == A.FAU_MOVE_NONE
+    assert st["moves"] == int((~none).sum())
+    assert not acc[none].any() and not du[none].any()
+    props_o = props.copy()
+    _oracle_compare(g.positions(), acc, du, spec, props_o)
+
+
+def test_pipelined_mixed_batch_with_molecular_systems(ctx):
+    """Water (molecular moves) runs in the chain kernel beside the pipelined systems,
+    on a forked stream inside the same graph."""
+    specs = [configs.primitive_model(n=200, seed=1), configs.bulk_ewald(n_salt=1000, seed=2),
+             configs.spce_water(n_mol=256, L=18.6, seed=3)]
+    systems = [ctx.create(s) for s in specs]
+    st = ctx.run_batch(systems, 3000, seed=7, dp=1.0, dprot=0.3, threads=0)
+    assert st["moves"] == 9000 and st["accepted"] > 0
+    for s in systems:
+        _energy_consistent(s)
+
+
+def test_pipelined_alone_equals_in_mix(ctx):
+    a1 = ctx.create(configs.bulk_ewald(n_salt=500, seed=4))
+    ctx.run_batch([a1], 2000, seed=3, streams=[42], counters=[0], threads=0)
+    others = [ctx.create(configs.primitive_model(n=200, seed=s)) for s in range(3)]
+    a2 = ctx.create(configs.bulk_ewald(n_salt=500, seed=4))
+    ctx.run_batch(others[:1] + [a2] + others[1:], 2000, seed=3, streams=[1, 42, 2, 3], counters=[0] * 4, threads=0)
+    assert np.array_equal(a1.positions(), a2.positions())
+    assert a1.running_energy() == a2.running_energy()
+    b1 = ctx.create(configs.bulk_ewald(n_salt=500, seed=8))
+    ctx.run_batch([b1], 1000, seed=5, streams=[9], counters=[0], threads=0)
+    ctx.run_batch([b1], 1000, seed=5, streams=[9], counters=[1000], threads=0)
+    b2 = ctx.create(configs.bulk_ewald(n_salt=500, seed=8))
+    ctx.run_batch([b2], 2000, seed=5, streams=[9], counters=[0], threads=0)
+    assert np.array_equal(b1.positions(), b2.positions())
+
+
+def test_pipelined_parallel_tempering(ctx):
+    specs, temps = configs.pt_replicas(n_rep=8, n_min=100, n_max=300)
+    systems = [ctx.create(s) for s in specs]
+    st = ctx.run_batch(systems, swap_interval=400, n_swap_blocks=6, temperatures=temps, seed=11, dp=2.0, threads=0)
+    assert st["swaps_attempted"] >= 6 * 3 and st["moves"] == 8 * 400 * 6
+    for s in systems:
+        e_run = s.running_energy()
+        e_tot = s.energy_total()["total"]
+        assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot))
