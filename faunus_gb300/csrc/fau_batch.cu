@@ -79,6 +79,18 @@ __global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const d
     }
 }
 
+// the pipelined kernel writes each move's energy change as a packed float-float pair
+// {hi, lo}; one CTA per system turns its range into FP64 values in place
+__global__ void unpack_du_kernel(double* du, const long long* off, const long long* nm)
+{
+    const long long o = off[blockIdx.x], n = nm[blockIdx.x];
+    float2* p = reinterpret_cast<float2*>(du);
+    for (long long m = threadIdx.x; m < n; m += blockDim.x) {
+        const float2 v = p[o + m];
+        du[o + m] = (double)v.x + (double)v.y;
+    }
+}
+
 // each parallel-tempering run starts with every system at its own temperature
 __global__ void reset_beta_kernel(DevSys* const* sys, int n)
 {
@@ -275,9 +287,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     unsigned long long* d_phase = nullptr;
     const char* pt_env = std::getenv("FAU_PHASE_TIMING");
     if (pt_env && pt_env[0] == '1') {
-        if (cudaMalloc(&d_phase, sizeof(unsigned long long) * kPhaseSlots * n) == cudaSuccess) {
-            cudaMemsetAsync(d_phase, 0, sizeof(unsigned long long) * kPhaseSlots * n, st);
+        if (cudaMalloc(&d_phase, sizeof(unsigned long long) * kFastPhaseSlots * n) == cudaSuccess) {
+            cudaMemsetAsync(d_phase, 0, sizeof(unsigned long long) * kFastPhaseSlots * n, st);
             a.phase_cycles = d_phase;
+            ae.phase_cycles = d_phase + (size_t)kFastPhaseSlots * nfast;
         }
     }
     cudaEvent_t e0, e1;
@@ -325,18 +338,31 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         return fau_internal_fail(FAU_ERR_CUDA, cudaGetErrorString(se));
     }
     if (d_phase) {
-        std::vector<unsigned long long> ph(kPhaseSlots * n);
+        std::vector<unsigned long long> ph((size_t)kFastPhaseSlots * n);
         cudaMemcpy(ph.data(), d_phase, sizeof(unsigned long long) * ph.size(), cudaMemcpyDeviceToHost);
         cudaFree(d_phase);
-        double tot[kPhaseSlots] = {0};
-        for (int i = 0; i < n; i++)
-            for (int j = 0; j < kPhaseSlots; j++) tot[j] += (double)ph[i * kPhaseSlots + j];
-        const double mv = tot[11] > 0 ? tot[11] : 1.0;
-        static const char* names[kPhaseSlots] = {"deferred_q", "ewald", "pairs", "reduce+B1", "decision", "commit",
-                                                 "prepare", "B2(w0)", "compute(w1)", "B1(w1)", "B2(w1)", "moves"};
-        std::fprintf(stderr, "FAU_PHASE_TIMING cycles per move:");
-        for (int j = 0; j < kPhaseSlots - 1; j++) std::fprintf(stderr, " %s=%.0f", names[j], tot[j] / mv);
-        std::fprintf(stderr, " (moves %.0f)\n", tot[11]);
+        static const char* names_e[kPhaseSlots] = {"deferred_q", "ewald", "pairs", "reduce+B1", "decision", "commit",
+                                                   "prepare", "B2(w0)", "compute(w1)", "B1(w1)", "B2(w1)", "moves"};
+        static const char* names_f[kFastPhaseSlots] = {
+            "P:commit_data", "P:prepare", "P:copies", "P:B1", "P:decision", "P:commit", "P:B2",
+            "C:preload", "C:ewald", "C:pairs", "C:sums", "C:B1", "C:decision", "C:q_update", "C:B2", "moves",
+            "prep:scalar_rest", "prep:tables", "prep:entries", "C:pairs_pre", "prep:fp64_add", "P:proposal",
+            "prep:to_fixed", "prep:cells"};
+        for (int part = 0; part < 2; part++) {
+            const int r0 = part == 0 ? 0 : nfast, r1 = part == 0 ? nfast : n;
+            if (r1 <= r0) continue;
+            const int ns = part == 0 ? kFastPhaseSlots : kPhaseSlots;
+            const int mslot = part == 0 ? 15 : kPhaseSlots - 1;
+            double tot[kFastPhaseSlots] = {0};
+            for (int r = r0; r < r1; r++)
+                for (int j = 0; j < ns; j++) tot[j] += (double)ph[(size_t)r * kFastPhaseSlots + j];
+            const double mv = tot[mslot] > 0 ? tot[mslot] : 1.0;
+            std::fprintf(stderr, "FAU_PHASE_TIMING %s cycles per move:", part == 0 ? "pipelined" : "chain");
+            for (int j = 0; j < ns; j++)
+                if (j != mslot && tot[j] > 0)
+                    std::fprintf(stderr, " %s=%.0f", part == 0 ? names_f[j] : names_e[j], tot[j] / mv);
+            std::fprintf(stderr, " (moves %.0f)\n", tot[mslot]);
+        }
     }
     fau_batch_stats S{};
     int derr = FAU_OK;
@@ -492,6 +518,10 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         }
     }
     if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, 4, false, st) == cudaSuccess;
+    if (ok && nfast && a.du_out) {
+        unpack_du_kernel<<<nfast, 256, 0, st>>>(a.du_out, a.prop_off, a.n_moves);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
     if (ok && nfast && nexact) ok = cudaStreamWaitEvent(st, join_ev, 0) == cudaSuccess;
     if (!ok) {
         cudaStreamSynchronize(st);

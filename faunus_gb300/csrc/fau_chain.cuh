@@ -109,14 +109,16 @@ struct Proposal {
     double dr[3];
     double quat[4];
     double u;
+    float uf; // u truncated to float (decides unless within 1e-4 of the threshold)
     bool rotate;
 };
 
 // Device-RNG proposal (batched mode), a deliberate deviation from the reference's
-// mt19937 stream: uniform direction (Archimedes), |dr| = dp U(0,1), uniform
-// particle / group, 53-bit Metropolis uniform.
+// mt19937 stream: uniform direction (Archimedes), |dr| = dp U(0,1) computed in FP32
+// and widened exactly, uniform particle / group, 53-bit Metropolis uniform.  The
+// doubles are assembled from bit patterns (no FP64 instruction on this path).
 static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigned long long ctr, uint32_t sys_id, uint64_t seed,
-                                           double dp, double dprot, bool molecular)
+                                           float dp, double dprot, bool molecular)
 {
     Proposal p;
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
@@ -126,11 +128,13 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
     float s, c;
     sincospif(2.f * u01_24(c1.z), &s, &c);
     const float rxy = sqrtf(fmaxf(0.f, 1.f - z * z));
-    const double len = dp * (double)u01_24(c1.w);
-    p.dr[0] = (double)(rxy * c) * len;
-    p.dr[1] = (double)(rxy * s) * len;
-    p.dr[2] = (double)z * len;
-    p.u = u01_53(c2.x, c2.y);
+    const float len = dp * u01_24(c1.w);
+    p.dr[0] = f2d_bits(rxy * c * len);
+    p.dr[1] = f2d_bits(rxy * s * len);
+    p.dr[2] = f2d_bits(z * len);
+    const unsigned long long v = ((unsigned long long)(c2.x >> 5) << 26) | (c2.y >> 6);
+    p.u = u53_bits(v);
+    p.uf = (float)(uint32_t)(v >> 29) * 5.9604644775390625e-8f; // top 24 bits, 2^-24
     p.rotate = false;
     p.quat[0] = 1.0;
     p.quat[1] = p.quat[2] = p.quat[3] = 0.0;
@@ -172,6 +176,7 @@ __device__ __forceinline__ Proposal load_proposal(const fau_proposal& f)
 #pragma unroll
     for (int d = 0; d < 4; d++) p.quat[d] = f.quat[d];
     p.u = f.u;
+    p.uf = d2f_trunc01(f.u);
     p.rotate = !(f.quat[0] == 0.0 && f.quat[1] == 0.0 && f.quat[2] == 0.0 && f.quat[3] == 0.0);
     return p;
 }
@@ -411,8 +416,15 @@ template <int NT, bool PHILOX>
 __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 {
     constexpr int NW = NT / 32;
-    DevSys& S = *A.sys[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // the system descriptor in shared memory: its fields sit on every move's dependent
+    // chain, and global copies fall out of L1 under the cell-list traffic
+    DevSys& G = *A.sys[blockIdx.x];
+    __shared__ __align__(16) DevSys Ssh;
+    for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += NT)
+        reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
+    __syncthreads();
+    const DevSys& S = Ssh;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int K = (S.flags & SYS_EWALD) ? S.K : 0;
     const int nc = S.knc;
@@ -488,7 +500,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
-        const Proposal p = PHILOX ? philox_proposal(S, ctr0, sys_id, A.seed, A.dp, A.dprot, molecular_sys)
+        const Proposal p = PHILOX ? philox_proposal(S, ctr0, sys_id, A.seed, (float)A.dp, A.dprot, molecular_sys)
                                   : load_proposal(A.props[poff]);
         prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
     }
@@ -878,7 +890,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 else if (mv + 1 < nmoves) {
                     // ---- prepare the next move
                     const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed,
-                                                                A.dp, A.dprot, molecular_sys)
+                                                                (float)A.dp, A.dprot, molecular_sys)
                                               : load_proposal(A.props[poff + mv + 1]);
                     prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
                     if (lane == 0) {
@@ -898,7 +910,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     }
     if (timing)
         for (int j = 0; j < kPhaseSlots; j++)
-            if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kPhaseSlots + j], tacc[j]);
+            if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + j], tacc[j]);
 
     // the last accepted move's Q(k) change, then everything pending into the FP64 master
     if (ms.prev_accept) {
@@ -937,16 +949,16 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
             pa += red_u[w][0];
             kb += red_u[w][1];
         }
-        S.pair_evals += pa;
-        S.k_updates += kb;
-        S.moves += n_mv;
-        S.accepted += n_acc;
-        S.sum_du += sum_du;
-        S.energy = energy;
+        G.pair_evals += pa;
+        G.k_updates += kb;
+        G.moves += n_mv;
+        G.accepted += n_acc;
+        G.sum_du += sum_du;
+        G.energy = energy;
 #pragma unroll
-        for (int d = 0; d < 3; d++) S.M[d] = M[d];
-        if (ms.stop) S.err = ms.stop;
-        S.consumed = ms.stop ? ms.consumed : nmoves;
+        for (int d = 0; d < 3; d++) G.M[d] = M[d];
+        if (ms.stop) G.err = ms.stop;
+        G.consumed = ms.stop ? ms.consumed : nmoves;
     }
 }
 

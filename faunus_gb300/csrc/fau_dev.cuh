@@ -168,6 +168,60 @@ __device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) // [0,1) with 5
 }
 __device__ __forceinline__ float u01_24(uint32_t a) { return (float)(a >> 8) * (1.0f / 16777216.0f); }
 
+// ---------------------------------------------------------------- exact conversions on the integer pipe
+// GB300's FP64 pipe issues about one warp instruction per 64 cycles, so the per-move
+// path builds doubles from their bit patterns where the value is exact anyway.
+
+// float -> double, exact (normal, subnormal, zero, inf, NaN)
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+    unsigned long long r = (unsigned long long)(b >> 31) << 63;
+    if (e == 0xFFu) {
+        r |= 0x7FF0000000000000ULL | ((unsigned long long)m << 29);
+    }
+    else if (e != 0u) {
+        r |= ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    }
+    else if (m != 0u) { // subnormal: m 2^-149 with the leading bit at position p
+        const int p = 31 - __clz((int)m);
+        r |= ((unsigned long long)(p - 149 + 1023) << 52) | (((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFULL);
+    }
+    return __longlong_as_double((long long)r);
+}
+
+// v 2^-53 for an integer 0 <= v < 2^53, exact
+__device__ __forceinline__ double u53_bits(unsigned long long v)
+{
+    if (v == 0ull) return 0.0;
+    const int p = 63 - __clzll((long long)v);
+    const unsigned long long r = ((unsigned long long)(p - 53 + 1023) << 52) | ((v << (52 - p)) & 0xFFFFFFFFFFFFFULL);
+    return __longlong_as_double((long long)r);
+}
+
+// a finite double truncated to float (relative error below 2^-23; magnitudes below
+// 2^-126 give a signed zero, above the float range an infinity)
+__device__ __forceinline__ float d2f_trunc(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+}
+
+// a double in [0, 1] truncated to float (relative error below 2^-23; values below 2^-126 give 0)
+__device__ __forceinline__ float d2f_trunc01(double u)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if ((long long)b <= 0 || e <= 0) return 0.f;
+    if (e >= 255) return __uint_as_float(0x7F800000u);
+    return __uint_as_float(((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+}
+
 // ---------------------------------------------------------------- geometry, FP64 exact
 // Chameleon::boundary (reference src/geometry.h:407-427) with anint (:132-135).
 __device__ __forceinline__ double boundary1(double a, double L, double half, double inv)

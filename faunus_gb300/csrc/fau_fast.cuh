@@ -34,6 +34,7 @@ namespace fau {
 
 constexpr int kFastEntries = 64; // cells listed per move: union box (<= 4x4x4) or two stencils (<= 54)
 constexpr int kFastRing = 64;    // host proposals staged in shared memory, refilled 32 at a time
+constexpr int kFastFlushAccepts = 256; // FP32 pending Q deltas flushed to the FP64 master every N accepts
 
 enum : int { FC_SELF = 1, FC_CELLS = 2 };
 constexpr int kFastUnsupported = -2; // proposal kind this kernel does not handle (FAU_MOVE_NONE is -1)
@@ -45,8 +46,8 @@ struct FastMove {
     int cc_o[3], cc_n[3];
     uint4 ro, rn;
     double xo[3], xn[3], dM[3];
-    double u;
-    float q, gx, gy, gz;
+    double u, du_surf; // du_surf: Ewald surface-term change, computed by the producer before the barrier
+    float uf, q;
     uint32_t ent[kFastEntries]; // cell | kEntNew (trial state reads it) | kEntOld (accepted state)
 };
 
@@ -56,7 +57,22 @@ struct Ahead {
     uint4 rec;
     double x[3];
     double dr[3], u;
-    int kind, i, cell, pad;
+    int kind, i, cell;
+    float uf;
+};
+
+// state only producer lane 0 uses, kept in shared memory so it costs no registers in
+// the compute warps (the kernel's register count is the maximum over all threads)
+struct ProdState {
+    double energy, sum_du; // FP64 folds of accepted energy changes
+    FF e_acc;              // accepted finite changes since the last fold
+    unsigned long long n_acc, n_mv;
+    double M[3];           // sum q r (surface term)
+    unsigned long long ctr0;
+    long long poff;
+    uint32_t sys_id;
+    float dp_f;
+    long long tprev[2];    // phase timers
 };
 
 // cell-list state read ahead of a commit (asynchronous copies as well)
@@ -83,15 +99,16 @@ __device__ __forceinline__ void cp_async_wait()
 
 template <bool PHILOX>
 __device__ __forceinline__ void fast_proposal(const DevSys& S, const ChainArgs& A, const fau_proposal* ring, long long s,
-                                              unsigned long long ctr0, uint32_t sys_id, Ahead& a)
+                                              unsigned long long ctr0, uint32_t sys_id, float dp_f, Ahead& a)
 {
     if (PHILOX) {
-        const Proposal p = philox_proposal(S, ctr0 + (unsigned long long)s, sys_id, A.seed, A.dp, A.dprot, false);
+        const Proposal p = philox_proposal(S, ctr0 + (unsigned long long)s, sys_id, A.seed, dp_f, 0.0, false);
         a.kind = p.kind;
         a.i = p.index;
 #pragma unroll
         for (int d = 0; d < 3; d++) a.dr[d] = p.dr[d];
         a.u = p.u;
+        a.uf = p.uf;
     }
     else {
         const fau_proposal& f = ring[s % kFastRing];
@@ -100,6 +117,7 @@ __device__ __forceinline__ void fast_proposal(const DevSys& S, const ChainArgs& 
 #pragma unroll
         for (int d = 0; d < 3; d++) a.dr[d] = f.dr[d];
         a.u = f.u;
+        a.uf = d2f_trunc01(f.u);
     }
 }
 
@@ -130,18 +148,31 @@ __device__ __forceinline__ void fast_commit_loads(const DevSys& S, const FastMov
 
 __device__ __forceinline__ int wrap_cell(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
-// Producer warp: trial position, record, cells, phase tables and cell entries of
-// the move staged in `m`; `prev` is the move evaluated just before it.
+// Producer warp: trial position, record, cells, phase tables and cell entries of the
+// move staged in `a`; `prev` is the move evaluated just before it.  Lane 0 computes
+// the position while lanes 1..31 build the phase tables (which need only the old
+// record and the displacement).  FP64 work per move: the IEEE add and fixed-point
+// rounding of AtomicTranslateRotate's new position (3 x add, multiply, convert).
 static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, const Ahead& a, const FastMove* prev,
-                                                 int lane, float2* T, int nc, const double* itq)
+                                                 int lane, float2* T, int nc, const float* itq, const double* itqd,
+                                                 unsigned long long* tsm)
 {
     const int TS = 2 * nc + 1;
+    long long t0 = (tsm && lane == 0) ? clock64() : 0;
+    auto sub = [&](int slot) { // profiling only (lane 0)
+        if (tsm && lane == 0) {
+            const long long now = clock64();
+            tsm[slot] += (unsigned long long)(now - t0);
+            t0 = now;
+        }
+    };
     const bool cells = (S.flags & SYS_CELLS) != 0;
+    const int kind = a.kind;
     if (lane == 0) {
-        const int kind = a.kind;
         m.kind = kind == kFastUnsupported ? FAU_MOVE_NONE : kind;
         m.i = a.i;
         m.u = a.u;
+        m.uf = a.uf;
         m.stop = kind == kFastUnsupported ? FAU_ERR_ARG : 0; // molecular proposal: not handled by this kernel
         m.cap_full = 0;
         m.nue = 0;
@@ -150,32 +181,44 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 xo[d] = a.x[d];
-                xn[d] = boundary1(__dadd_rn(xo[d], a.dr[d]), S.L[d], S.half[d], S.inv[d]);
+                xn[d] = __dadd_rn(xo[d], a.dr[d]);
+                // Chameleon::boundary only when |x| > L/2 (compared as bit patterns)
+                if ((__double_as_longlong(xn[d]) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(S.half[d]))
+                    xn[d] = boundary1(xn[d], S.L[d], S.half[d], S.inv[d]);
             }
             const uint4 ro = a.rec;
-            m.ro = ro;
-            m.cell_old = a.cell;
             const uint4 rn = make_uint4(to_fixed(xn[0], S.fx_scale[0]), to_fixed(xn[1], S.fx_scale[1]),
                                         to_fixed(xn[2], S.fx_scale[2]), ro.w);
-            const double q = itq[ro.w >> 24];
+            sub(20);
+            m.ro = ro;
             m.rn = rn;
-            m.q = (float)q;
+            m.q = itq[ro.w >> 24];
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 m.xo[d] = xo[d];
                 m.xn[d] = xn[d];
-                m.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
             }
-            const float3 g = min_image_frac(S, xn, xo);
-            m.gx = g.x;
-            m.gy = g.y;
-            m.gz = g.z;
+            if (S.flags & SYS_SURFACE) {
+                const double q = itqd[ro.w >> 24];
+#pragma unroll
+                for (int d = 0; d < 3; d++) m.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
+            }
+            sub(22);
             if (cells) {
                 const int co = a.cell;
-                m.cc_o[0] = co % S.cdim[0];
-                m.cc_o[1] = (co / S.cdim[0]) % S.cdim[1];
-                m.cc_o[2] = co / (S.cdim[0] * S.cdim[1]);
                 int c[3];
+                // the old cell's coordinates: the binning of the old position, checked against
+                // the cell the particle is listed in (divisions only if they ever differ)
+                cell_coords(S, xo, ro, c);
+                if (cell_index(S, c) != co) {
+                    c[0] = co % S.cdim[0];
+                    c[1] = (co / S.cdim[0]) % S.cdim[1];
+                    c[2] = co / (S.cdim[0] * S.cdim[1]);
+                }
+                m.cell_old = co;
+                m.cc_o[0] = c[0];
+                m.cc_o[1] = c[1];
+                m.cc_o[2] = c[2];
                 cell_coords(S, xn, rn, c);
                 m.cc_n[0] = c[0];
                 m.cc_n[1] = c[1];
@@ -185,26 +228,23 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
             else {
                 m.cell_old = m.cell_new = 0;
             }
+            sub(23);
         }
         else {
             m.i = -1;
             m.cell_old = m.cell_new = -1;
         }
     }
-    __syncwarp();
-    if (m.kind != FAU_MOVE_ATOMIC) {
-        if (lane == 0) m.conflict = 0;
-        __syncwarp();
-        return;
-    }
-    // phase tables: per axis, mid = e^{i n (phi + pi g)} and h = e^{i n pi g}, n = -nc..nc
-    if (T) {
-        const uint4 ro = m.ro;
-        const float gx = m.gx, gy = m.gy, gz = m.gz;
-        for (int e = lane; e < 3 * (nc + 1); e += 32) {
+    else if (T && kind == FAU_MOVE_ATOMIC) {
+        // phase tables: per axis, mid = e^{i n (phi + pi g)} and h = e^{i n pi g}, n = -nc..nc, where
+        // g = dr / L: the proposal's dr equals the minimum-image xn - xo up to the rounding of xo + dr
+        // (and whole box lengths, which leave every phase change unchanged); the records' difference
+        // would carry their 2^-32 L rounding, too coarse for small moves
+        const uint4 ro = a.rec;
+        for (int e = lane - 1; e < 3 * (nc + 1); e += 31) {
             const int ax = e / (nc + 1), n = e - ax * (nc + 1);
             const uint32_t u = ax == 0 ? ro.x : (ax == 1 ? ro.y : ro.z);
-            const float g = ax == 0 ? gx : (ax == 1 ? gy : gz);
+            const float g = d2f_trunc(a.dr[ax]) * S.inv_f[ax];
             float s, c;
             sincospif((float)n * g, &s, &c);
             const float2 h = make_float2(c, s);
@@ -216,16 +256,22 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
             row[TS + nc - n] = make_float2(h.x, -h.y);
         }
     }
+    __syncwarp();
+    sub(16);
+    if (m.kind != FAU_MOVE_ATOMIC) {
+        if (lane == 0) m.conflict = 0;
+        __syncwarp();
+        return;
+    }
     bool hit = false;
     if (cells) {
-        int cco[3], ccn[3], df[3], lo[3], w[3];
+        int cco[3], df[3], lo[3], w[3];
         bool uni = true;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             cco[d] = m.cc_o[d];
-            ccn[d] = m.cc_n[d];
             const int n = S.cdim[d];
-            int v = ccn[d] - cco[d];
+            int v = m.cc_n[d] - cco[d];
             if (2 * v > n) v -= n;
             else if (2 * v < -n) v += n;
             df[d] = v;
@@ -239,7 +285,9 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
         if (uni) { // one box holding both stencils; each cell flags the states whose stencil contains it
             nue = w[0] * w[1] * w[2];
             for (int e = lane; e < nue; e += 32) {
-                const int ex = e % w[0], ey = (e / w[0]) % w[1], ez = e / (w[0] * w[1]);
+                // box extents are 3 or 4: constant divisors
+                const int ex = w[0] == 3 ? e % 3 : (e & 3), e1 = w[0] == 3 ? e / 3 : (e >> 2);
+                const int ey = w[1] == 3 ? e1 % 3 : (e1 & 3), ez = w[1] == 3 ? e1 / 3 : (e1 >> 2);
                 const int o[3] = {lo[0] + ex, lo[1] + ey, lo[2] + ez};
                 bool in_o = true, in_n = true;
                 int c[3];
@@ -264,7 +312,7 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
                 const int o[3] = {r % nbx + S.off_min[0], (r / nbx) % nby + S.off_min[1], r / (nbx * nby) + S.off_min[2]};
                 int c[3];
 #pragma unroll
-                for (int d = 0; d < 3; d++) c[d] = wrap_cell((st ? ccn[d] : cco[d]) + o[d], S.cdim[d]);
+                for (int d = 0; d < 3; d++) c[d] = wrap_cell((st ? m.cc_n[d] : cco[d]) + o[d], S.cdim[d]);
                 const int cell = cell_index(S, c);
                 hit = hit || cell == pc_o || cell == pc_n;
                 m.ent[e] = (uint32_t)cell | (st ? kEntNew : kEntOld);
@@ -278,6 +326,7 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
         m.conflict = (self ? FC_SELF : 0) | (hit ? FC_CELLS : 0);
     }
     __syncwarp();
+    sub(18);
 }
 
 struct PairOut {
@@ -305,7 +354,7 @@ static __device__ __noinline__ PairOut fast_pair_state(const DevSys& S, PairF p,
 // getEnergyChange value (src/montecarlo.cpp:193-209).  Returns accept; sets
 // nan_stop for a NaN energy change.
 __device__ __forceinline__ bool fast_decide(FF s, int flags, double du_surf, bool surface, double beta, float beta_f,
-                                            double u, bool& nan_stop)
+                                            double u, float uf, bool& nan_stop)
 {
     nan_stop = false;
     if (flags == 0 && !surface) {
@@ -313,7 +362,6 @@ __device__ __forceinline__ bool fast_decide(FF s, int flags, double du_surf, boo
         if (xf <= 0.f) return true;
         const float ef = __expf(-xf);
         if (ef > 1e-30f) {
-            const float uf = (float)u;
             if (uf < ef * 0.9999f) return true;
             if (uf > ef * 1.0001f) return false;
         }
@@ -335,8 +383,15 @@ template <int NWC, bool PHILOX>
 __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs A)
 {
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
-    DevSys& S = *A.sys[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // the system descriptor in shared memory: its fields sit on every move's dependent
+    // chain, and global copies fall out of L1 under the cell-list traffic
+    DevSys& G = *A.sys[blockIdx.x];
+    __shared__ __align__(16) DevSys Ssh;
+    for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += NT)
+        reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
+    __syncthreads();
+    const DevSys& S = Ssh;
     const bool producer = warp == 0;
     const int ctid = tid - 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -355,9 +410,26 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
     __shared__ CommitPre cps[2];   // move s: cps[s & 1]
     __shared__ FF red_a[2][NWC];
     __shared__ int red_f[2][NWC];
-    __shared__ double itq[kMaxITypes];
+    __shared__ float itq[kMaxITypes];
+    __shared__ double itqd[kMaxITypes];
     __shared__ fau_proposal ring[PHILOX ? 1 : kFastRing];
     __shared__ unsigned long long red_u[NWC][2];
+    // phase timers (profiling only; every phase still runs), accumulated by thread 0 (producer) and
+    // thread 32 (first compute warp): 0 commit data, 1 prepare t+1, 2 copies of t+2, 3 barrier 1,
+    // 4 decision, 5 commit, 6 conflict barrier | 7 preload, 8 Ewald, 9 pairs, 10 warp sums,
+    // 11 barrier 1, 12 decision, 13 Q update, 14 conflict barrier | 15 moves | inside prepare:
+    // 16 scalar part, 17 phase tables, 18 cell entries | 19 pairs: preloaded part | 21 proposal
+    __shared__ unsigned long long tsm[kFastPhaseSlots];
+    __shared__ ProdState ps;
+    const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
+    if (tid < kFastPhaseSlots) tsm[tid] = 0;
+    auto tick = [&](int slot) {
+        if (timing) {
+            const long long now = clock64();
+            tsm[slot] += (unsigned long long)(now - ps.tprev[tid >> 5]);
+            ps.tprev[tid >> 5] = now;
+        }
+    };
 
     const float rec_pref_f = (float)S.rec_pref;
     for (int k = tid; k < K; k += NT) {
@@ -368,33 +440,43 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         kaf[k] = make_int2((nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16), __float_as_int(rec_pref_f * S.Ak[k]));
     }
     for (int t = tid; t < nt * nt; t += NT) pt[t] = S.pair[t];
-    if (tid < nt) itq[tid] = S.itype_qd[tid];
+    if (tid < nt) {
+        itq[tid] = S.itype_q[tid];
+        itqd[tid] = S.itype_qd[tid];
+    }
 
     const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
-    const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
-    const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
-    const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+    if (tid == 0) {
+        ps.poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
+        ps.sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
+        ps.ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+        ps.dp_f = (float)A.dp;
+        ps.energy = S.energy;
+        ps.sum_du = 0.0;
+        ps.e_acc = FF{0.f, 0.f};
+        ps.n_acc = ps.n_mv = 0;
+#pragma unroll
+        for (int d = 0; d < 3; d++) ps.M[d] = S.M[d];
+    }
+    __syncthreads();
     const bool cells = (S.flags & SYS_CELLS) != 0;
     const bool surface = (S.flags & SYS_SURFACE) != 0;
     const int cap = S.cap;
     const int cap_shift = cells ? __ffs(cap) - 1 : 0;
-    const double beta = S.beta_scale, surf_pref = S.surf_pref;
-    const float beta_f = (float)beta;
-    double M[3] = {S.M[0], S.M[1], S.M[2]};
+    const float beta_f = (float)S.beta_scale;
 
     // proposals [s0, s0 + 32) into their ring slots (host proposals)
     auto ring_fill = [&](long long s0) {
         const long long e = s0 + 32 < nmoves ? s0 + 32 : nmoves;
         if (e <= s0) return;
         const int words = (int)(e - s0) * (int)(sizeof(fau_proposal) / 8);
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(A.props + poff + s0);
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(A.props + ps.poff + s0);
         unsigned long long* dst = reinterpret_cast<unsigned long long*>(ring + (s0 % kFastRing));
         for (int w = lane; w < words; w += 32) dst[w] = src[w];
     };
 
-    unsigned long long n_acc = 0, n_mv = 0, n_pairs = 0, n_k = 0;
-    double energy = S.energy, sum_du = 0.0;
-    int since_flush = 0;
+    unsigned long long n_pairs = 0;
+    int since_flush = 0, q_pending = 0; // compute threads: accepts since the FP64 flush; dQ not yet folded in
 
     if (producer) {
         if (!PHILOX) {
@@ -403,16 +485,16 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             __syncwarp();
         }
         if (lane == 0 && nmoves > 0) {
-            fast_proposal<PHILOX>(S, A, ring, 0, ctr0, sys_id, ahs[0]);
+            fast_proposal<PHILOX>(S, A, ring, 0, ps.ctr0, ps.sys_id, ps.dp_f, ahs[0]);
             fast_load(S, ahs[0]);
             cp_async_commit();
             cp_async_wait<0>();
         }
         __syncwarp();
-        if (nmoves > 0) fast_prepare(S, mvb[0], ahs[0], nullptr, lane, K ? tabs : nullptr, nc, itq);
+        if (nmoves > 0) fast_prepare(S, mvb[0], ahs[0], nullptr, lane, K ? tabs : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
         if (lane == 0) {
             if (nmoves > 1) {
-                fast_proposal<PHILOX>(S, A, ring, 1, ctr0, sys_id, ahs[1]);
+                fast_proposal<PHILOX>(S, A, ring, 1, ps.ctr0, ps.sys_id, ps.dp_f, ahs[1]);
                 fast_load(S, ahs[1]);
             }
             fast_commit_loads(S, mvb[0], cps[0]);
@@ -422,17 +504,18 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
     __syncthreads();
 
     int prev_accept = 0, stop = 0;
-    long long consumed = nmoves;
-    for (long long t = 0; t < nmoves; t++) {
+    if (timing) ps.tprev[tid >> 5] = clock64();
+    long long t = 0;
+    for (; t < nmoves; t++) {
         const int b = (int)(t % 3);
         FastMove& m = mvb[b];
         if (m.stop) {
             stop = m.stop;
-            consumed = t;
             break;
         }
         const int kind = m.kind;
         const int rb = (int)(t & 1);
+        if (timing && tid == 0) tsm[15]++;
         if (producer) {
             CommitPre& cp = cps[t & 1];
             if (lane == 0) {
@@ -452,7 +535,18 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     }
                 }
                 cp_async_commit(); // group 1: the record that fills the old cell's hole
+                if (surface && kind == FAU_MOVE_ATOMIC) { // surface-term change of move t (Ewald::updateState)
+                    double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        const double mn = __dadd_rn(ps.M[d], m.dM[d]);
+                        m2o = __dadd_rn(m2o, __dmul_rn(ps.M[d], ps.M[d]));
+                        m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
+                    }
+                    m.du_surf = S.surf_pref * (m2n - m2o);
+                }
             }
+            tick(0);
             if (!PHILOX && (t & 31) == 0 && t >= 32) ring_fill(t + 32);
             if (t + 1 < nmoves) {
                 const FastMove& pm = mvb[(t + 2) % 3]; // move t-1
@@ -465,17 +559,20 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     an.cell = pm.cell_new;
                 }
                 __syncwarp();
-                fast_prepare(S, mvb[(t + 1) % 3], an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq);
+                fast_prepare(S, mvb[(t + 1) % 3], an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
+                tick(1);
                 if (lane == 0) {
                     if (t + 2 < nmoves) {
                         Ahead& a2 = ahs[t & 1];
-                        fast_proposal<PHILOX>(S, A, ring, t + 2, ctr0, sys_id, a2);
+                        fast_proposal<PHILOX>(S, A, ring, t + 2, ps.ctr0, ps.sys_id, ps.dp_f, a2);
+                        tick(21);
                         fast_load(S, a2);
                     }
                     fast_commit_loads(S, mvb[(t + 1) % 3], cps[(t + 1) & 1]);
                 }
             }
             if (lane == 0) cp_async_commit(); // group 2: Ahead of move t+2, commit counts of move t+1
+            tick(2);
         }
         else if (kind == FAU_MOVE_ATOMIC) {
             const int i = m.i;
@@ -508,13 +605,37 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             uint32_t e0 = 0, e1 = 0;
             if (ctid < n_items) load_item(ctid, r0, e0);
             if (ctid + NTC < n_items) load_item(ctid + NTC, r1, e1);
+            tick(7);
 
-            // ---- Ewald: one k-vector per thread and step, two independent accumulators
+            // ---- Ewald: one k-vector per thread and step, two independent accumulators.  The
+            // last accepted move's Q(k) change (State::sync trial -> accepted) is folded in here,
+            // in the same pass; every 256 accepts the FP32 pending sums go to the FP64 master.
             FF acc0{0.f, 0.f}, acc1{0.f, 0.f};
             if (K) {
+                if (q_pending && since_flush >= kFastFlushAccepts) {
+                    for (int k = ctid; k < K; k += NTC) {
+                        const float4 qq = kq[k];
+                        const float2 d = dlt[k];
+                        double2 q = S.Q[k];
+                        q.x += (double)(qq.z + d.x);
+                        q.y += (double)(qq.w + d.y);
+                        S.Q[k] = q;
+                        kq[k] = make_float4((float)q.x, (float)q.y, 0.f, 0.f);
+                    }
+                    q_pending = 0;
+                    since_flush = 0;
+                }
+                const bool pa = q_pending != 0;
                 const float2* Tb = tabs + b * 6 * TS;
                 const float f0 = 2.f * m.q;
                 auto ewald_k = [&](int k, FF& acc) {
+                    float4 qq = kq[k];
+                    if (pa) {
+                        const float2 dp = dlt[k];
+                        qq.z += dp.x;
+                        qq.w += dp.y;
+                        kq[k] = qq;
+                    }
                     const int2 ka = kaf[k];
                     const int ix = ka.x & 0xff, iy = (ka.x >> 8) & 0xff, iz = ka.x >> 16;
                     const float2 mid = cmul(cmul(Tb[ix], Tb[2 * TS + iy]), Tb[4 * TS + iz]);
@@ -523,7 +644,6 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     const float f = f0 * fmaf(hxy.x, hz.y, hxy.y * hz.x); // 2 q sin(D/2)
                     const float2 d = make_float2(-f * mid.y, f * mid.x);
                     dlt[k] = d;
-                    const float4 qq = kq[k];
                     const float qx = qq.x + qq.z, qy = qq.y + qq.w;
                     const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
                     const float dd = fmaf(d.x, d.x, d.y * d.y);
@@ -535,10 +655,11 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     ewald_k(k + NTC, acc1);
                 }
                 if (k < K) ewald_k(k, acc0);
-                n_k += (unsigned long long)((K - ctid + NTC - 1) / NTC);
+                q_pending = 0;
             }
             FF accp = ff_sum(acc0, acc1);
             int flags = 0;
+            tick(8);
 
             // ---- pairs
             for (int r = 0;; r++) {
@@ -555,6 +676,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     ent = e1;
                 }
                 else {
+                    if (r == 2) tick(19);
                     load_item(it, rj, ent);
                 }
                 if (rj.w == kEmptySlot) continue;
@@ -580,6 +702,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                 }
                 ff_add(accp, un - uo);
             }
+            tick(9);
             float sc_unused = 0.f;
             FF b_unused{0.f, 0.f};
             warp_reduce(accp, b_unused, sc_unused, flags, false);
@@ -587,8 +710,10 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                 red_a[rb][warp - 1] = accp;
                 red_f[rb][warp - 1] = flags;
             }
+            tick(10);
         }
         __syncthreads(); // B1
+        tick(tid == 0 ? 3 : 11);
 
         // ---- decision, identical in every thread
         int accept = 0;
@@ -602,62 +727,54 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                 s = ff_sum(s, red_a[rb][w]);
                 fl |= red_f[rb][w];
             }
-            if (surface) {
-                double m2o = 0.0, m2n = 0.0;
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    const double mn = __dadd_rn(M[d], m.dM[d]);
-                    m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
-                    m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
-                }
-                du_surf = surf_pref * (m2n - m2o);
-            }
-            accept = fast_decide(s, fl, du_surf, surface, beta, beta_f, m.u, nan_stop) ? 1 : 0;
+            if (surface) du_surf = m.du_surf;
+            accept = fast_decide(s, fl, du_surf, surface, S.beta_scale, beta_f, m.u, m.uf, nan_stop) ? 1 : 0;
         }
         if (nan_stop) {
             stop = FAU_ERR_NAN;
-            consumed = t;
             break;
         }
+        tick(tid == 0 ? 4 : 12);
         if (producer && lane == 0) {
-            double du = 0.0;
+            FF dff{0.f, 0.f}; // this move's energy change as float-float (written packed to du_out)
             if (kind == FAU_MOVE_ATOMIC) {
-                if (accept || A.du_out)
-                    du = energy_change(ff_value(s) + du_surf, fl & F_NEW_INF, fl & F_OLD_INF, fl & F_NEW_NAN,
-                                       fl & F_OLD_NAN);
-                n_mv++;
-                if (accept) {
-                    n_acc++;
-                    sum_du += du;
-                    energy += du;
+                ps.n_mv++;
+                if (fl == 0 && !surface) {
+                    dff = s;
+                    if (accept) {
+                        ps.n_acc++;
+                        ps.e_acc = ff_sum(ps.e_acc, s);
+                    }
+                }
+                else if (accept || A.du_out) {
+                    const double du = energy_change(ff_value(s) + du_surf, fl & F_NEW_INF, fl & F_OLD_INF,
+                                                    fl & F_NEW_NAN, fl & F_OLD_NAN);
+                    dff.hi = (float)du;
+                    dff.lo = isfinite(du) ? (float)(du - (double)dff.hi) : 0.f;
+                    if (accept) {
+                        ps.n_acc++;
+                        const double acc = ff_value(ps.e_acc);
+                        ps.energy += acc + du;
+                        ps.sum_du += acc + du;
+                        ps.e_acc = FF{0.f, 0.f};
+                    }
                 }
             }
-            if (A.acc_out) A.acc_out[poff + t] = (uint8_t)accept;
-            if (A.du_out) A.du_out[poff + t] = du;
+            const long long po = ps.poff + t;
+            if (A.acc_out) A.acc_out[po] = (uint8_t)accept;
+            if (A.du_out) // packed {hi, lo}; a kernel after the launch turns the range into doubles
+                reinterpret_cast<float2*>(A.du_out)[po] = make_float2(dff.hi, dff.lo);
+            if (accept && surface) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) ps.M[d] = __dadd_rn(ps.M[d], m.dM[d]);
+            }
         }
         if (accept) {
-            if (surface) {
-#pragma unroll
-                for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], m.dM[d]);
+            if (!producer && K) { // this thread's share of Q(k) += dQ(k), folded into the next Ewald pass
+                q_pending = 1;
+                since_flush++;
             }
-            if (!producer && K) { // this thread's share of Q(k) += dQ(k); FP32 pending -> FP64 master every N accepts
-                const bool flush = ++since_flush == kFlushAccepts;
-                if (flush) since_flush = 0;
-                for (int k = ctid; k < K; k += NTC) {
-                    float4 qq = kq[k];
-                    const float2 d = dlt[k];
-                    qq.z += d.x;
-                    qq.w += d.y;
-                    if (flush) {
-                        double2 q = S.Q[k];
-                        q.x += (double)qq.z;
-                        q.y += (double)qq.w;
-                        S.Q[k] = q;
-                        qq = make_float4((float)q.x, (float)q.y, 0.f, 0.f);
-                    }
-                    kq[k] = qq;
-                }
-            }
+            tick(tid == 0 ? 4 : 13);
             if (producer && lane == 0) { // commit (State::sync trial -> accepted): positions, record, cell list
                 cp_async_wait<1>();
                 const CommitPre& cp_cur = cps[t & 1];
@@ -670,7 +787,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                                   (m.cell_old == m.cell_new ||
                                    (cp_cur.cnt_o >= 1 && cp_cur.cnt_o <= cap && cp_cur.cnt_n >= 0));
                 if (cells && !sane) {
-                    S.err = FAU_ERR_STATE; // inconsistent cell list: leave it untouched
+                    G.err = FAU_ERR_STATE; // inconsistent cell list: leave it untouched
                 }
                 else if (cells) {
                     const int co = m.cell_old, cn = m.cell_new;
@@ -693,9 +810,9 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     }
                 }
             }
+            tick(tid == 0 ? 5 : 13);
             if (m.cap_full) {
                 stop = FAU_ERR_CAPACITY;
-                consumed = t + 1;
                 break;
             }
         }
@@ -707,13 +824,13 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                 Ahead& an = ahs[(t + 1) & 1];
                 if (lane == 0) {
                     cp_async_wait<0>();
-                    fast_proposal<PHILOX>(S, A, ring, t + 1, ctr0, sys_id, an);
+                    fast_proposal<PHILOX>(S, A, ring, t + 1, ps.ctr0, ps.sys_id, ps.dp_f, an);
                     fast_load(S, an);
                     cp_async_commit();
                     cp_async_wait<0>();
                 }
                 __syncwarp();
-                fast_prepare(S, nm, an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq);
+                fast_prepare(S, nm, an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
                 if (lane == 0) {
                     fast_commit_loads(S, nm, cps[(t + 1) & 1]);
                     cp_async_commit();
@@ -721,14 +838,23 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             }
             __syncthreads(); // B2
         }
+        tick(tid == 0 ? 6 : 14);
         prev_accept = accept;
     }
+    __syncthreads();
+    if (A.phase_cycles && tid < kFastPhaseSlots && tsm[tid])
+        atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + tid], tsm[tid]);
     if (producer && lane == 0) cp_async_wait<0>();
 
-    // everything pending into the FP64 master Q
+    // the last accepted move's change and everything pending into the FP64 master Q
     if (!producer) {
         for (int k = ctid; k < K; k += NTC) {
-            const float4 qq = kq[k];
+            float4 qq = kq[k];
+            if (q_pending) {
+                const float2 d = dlt[k];
+                qq.z += d.x;
+                qq.w += d.y;
+            }
             if (qq.z != 0.f || qq.w != 0.f) {
                 double2 q = S.Q[k];
                 q.x += (double)qq.z;
@@ -737,33 +863,25 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             }
         }
     }
-    unsigned long long pa = n_pairs, kb = n_k;
+    unsigned long long pa = n_pairs;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        pa += __shfl_xor_sync(0xffffffffu, pa, o);
-        kb += __shfl_xor_sync(0xffffffffu, kb, o);
-    }
-    if (!producer && lane == 0) {
-        red_u[warp - 1][0] = pa;
-        red_u[warp - 1][1] = kb;
-    }
+    for (int o = 16; o > 0; o >>= 1) pa += __shfl_xor_sync(0xffffffffu, pa, o);
+    if (!producer && lane == 0) red_u[warp - 1][0] = pa;
     __syncthreads();
     if (tid == 0) {
-        unsigned long long sp = 0, sk = 0;
-        for (int w = 0; w < NWC; w++) {
-            sp += red_u[w][0];
-            sk += red_u[w][1];
-        }
-        S.pair_evals += sp;
-        S.k_updates += sk;
-        S.moves += n_mv;
-        S.accepted += n_acc;
-        S.sum_du += sum_du;
-        S.energy = energy;
+        unsigned long long sp = 0;
+        for (int w = 0; w < NWC; w++) sp += red_u[w][0];
+        G.pair_evals += sp;
+        G.k_updates += ps.n_mv * (unsigned long long)K; // every k-vector once per single-atom move
+        const double acc = ff_value(ps.e_acc);
+        G.moves += ps.n_mv;
+        G.accepted += ps.n_acc;
+        G.sum_du += ps.sum_du + acc;
+        G.energy = ps.energy + acc;
 #pragma unroll
-        for (int d = 0; d < 3; d++) S.M[d] = M[d];
-        if (stop) S.err = stop;
-        S.consumed = consumed;
+        for (int d = 0; d < 3; d++) G.M[d] = ps.M[d];
+        if (stop) G.err = stop;
+        G.consumed = stop == FAU_ERR_CAPACITY ? t + 1 : t;
     }
 }
 

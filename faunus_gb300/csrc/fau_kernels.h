@@ -33,7 +33,8 @@ struct ChainArgs {
     // optional per-CTA phase timers (clock64 cycles, kPhaseSlots per CTA) for profiling
     unsigned long long* phase_cycles;
 };
-constexpr int kPhaseSlots = 12;
+constexpr int kPhaseSlots = 12;     // chain kernel
+constexpr int kFastPhaseSlots = 24; // pipelined kernel (the per-CTA stride of phase_cycles for both)
 
 // One trial move held for a later commit (plain FP64 form and evaluate-only mode).
 struct PlainMove {
