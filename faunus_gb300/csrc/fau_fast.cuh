@@ -44,6 +44,8 @@ struct FastMove {
     int kind, i, cell_old, cell_new;
     int nue, conflict, cap_full, stop; // conflict: FC_* against the previous move
     int cc_o[3], cc_n[3];
+    int uni, lo[3], w[3], df[3];       // cell entries: union box (uni) or the two stencils
+    float g[3];                        // displacement / L (phase tables)
     uint4 ro, rn;
     double xo[3], xn[3], dM[3];
     double u, du_surf; // du_surf: Ewald surface-term change, computed by the producer before the barrier
@@ -148,19 +150,16 @@ __device__ __forceinline__ void fast_commit_loads(const DevSys& S, const FastMov
 
 __device__ __forceinline__ int wrap_cell(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
-// Producer warp: trial position, record, cells, phase tables and cell entries of the
-// move staged in `a`; `prev` is the move evaluated just before it.  Lane 0 computes
-// the position while lanes 1..31 build the phase tables (which need only the old
-// record and the displacement).  FP64 work per move: the IEEE add and fixed-point
-// rounding of AtomicTranslateRotate's new position (3 x add, multiply, convert).
-static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, const Ahead& a, const FastMove* prev,
-                                                 int lane, float2* T, int nc, const float* itq, const double* itqd,
-                                                 unsigned long long* tsm)
+// Producer lane 0: trial position, record, charge, cells and the layout of the cell
+// entries of the move staged in `a`; `prev` is the move evaluated just before it.
+// FP64 work per move: the IEEE add and fixed-point rounding of AtomicTranslateRotate's
+// new position (3 x add, multiply, convert).
+static __device__ __noinline__ void fast_scalar(const DevSys& S, FastMove& m, const Ahead& a, const FastMove* prev,
+                                                const float* itq, const double* itqd, unsigned long long* tsm)
 {
-    const int TS = 2 * nc + 1;
-    long long t0 = (tsm && lane == 0) ? clock64() : 0;
-    auto sub = [&](int slot) { // profiling only (lane 0)
-        if (tsm && lane == 0) {
+    long long t0 = tsm ? clock64() : 0;
+    auto sub = [&](int slot) { // profiling only
+        if (tsm) {
             const long long now = clock64();
             tsm[slot] += (unsigned long long)(now - t0);
             t0 = now;
@@ -168,85 +167,108 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
     };
     const bool cells = (S.flags & SYS_CELLS) != 0;
     const int kind = a.kind;
-    if (lane == 0) {
-        m.kind = kind == kFastUnsupported ? FAU_MOVE_NONE : kind;
-        m.i = a.i;
-        m.u = a.u;
-        m.uf = a.uf;
-        m.stop = kind == kFastUnsupported ? FAU_ERR_ARG : 0; // molecular proposal: not handled by this kernel
-        m.cap_full = 0;
-        m.nue = 0;
-        if (kind == FAU_MOVE_ATOMIC) {
-            double xo[3], xn[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                xo[d] = a.x[d];
-                xn[d] = __dadd_rn(xo[d], a.dr[d]);
-                // Chameleon::boundary only when |x| > L/2 (compared as bit patterns)
-                if ((__double_as_longlong(xn[d]) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(S.half[d]))
-                    xn[d] = boundary1(xn[d], S.L[d], S.half[d], S.inv[d]);
-            }
-            const uint4 ro = a.rec;
-            const uint4 rn = make_uint4(to_fixed(xn[0], S.fx_scale[0]), to_fixed(xn[1], S.fx_scale[1]),
-                                        to_fixed(xn[2], S.fx_scale[2]), ro.w);
-            sub(20);
-            m.ro = ro;
-            m.rn = rn;
-            m.q = itq[ro.w >> 24];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                m.xo[d] = xo[d];
-                m.xn[d] = xn[d];
-            }
-            if (S.flags & SYS_SURFACE) {
-                const double q = itqd[ro.w >> 24];
-#pragma unroll
-                for (int d = 0; d < 3; d++) m.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
-            }
-            sub(22);
-            if (cells) {
-                const int co = a.cell;
-                int c[3];
-                // the old cell's coordinates: the binning of the old position, checked against
-                // the cell the particle is listed in (divisions only if they ever differ)
-                cell_coords(S, xo, ro, c);
-                if (cell_index(S, c) != co) {
-                    c[0] = co % S.cdim[0];
-                    c[1] = (co / S.cdim[0]) % S.cdim[1];
-                    c[2] = co / (S.cdim[0] * S.cdim[1]);
-                }
-                m.cell_old = co;
-                m.cc_o[0] = c[0];
-                m.cc_o[1] = c[1];
-                m.cc_o[2] = c[2];
-                cell_coords(S, xn, rn, c);
-                m.cc_n[0] = c[0];
-                m.cc_n[1] = c[1];
-                m.cc_n[2] = c[2];
-                m.cell_new = cell_index(S, c);
-            }
-            else {
-                m.cell_old = m.cell_new = 0;
-            }
-            sub(23);
-        }
-        else {
-            m.i = -1;
-            m.cell_old = m.cell_new = -1;
-        }
+    m.kind = kind == kFastUnsupported ? FAU_MOVE_NONE : kind;
+    m.i = a.i;
+    m.u = a.u;
+    m.uf = a.uf;
+    m.stop = kind == kFastUnsupported ? FAU_ERR_ARG : 0; // molecular proposal: not handled by this kernel
+    m.cap_full = 0;
+    m.nue = 0;
+    m.conflict = 0;
+    if (kind != FAU_MOVE_ATOMIC) {
+        m.i = -1;
+        m.cell_old = m.cell_new = -1;
+        return;
     }
-    else if (T && kind == FAU_MOVE_ATOMIC) {
-        // phase tables: per axis, mid = e^{i n (phi + pi g)} and h = e^{i n pi g}, n = -nc..nc, where
-        // g = dr / L: the proposal's dr equals the minimum-image xn - xo up to the rounding of xo + dr
-        // (and whole box lengths, which leave every phase change unchanged); the records' difference
-        // would carry their 2^-32 L rounding, too coarse for small moves
-        const uint4 ro = a.rec;
-        for (int e = lane - 1; e < 3 * (nc + 1); e += 31) {
+    double xo[3], xn[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        xo[d] = a.x[d];
+        xn[d] = __dadd_rn(xo[d], a.dr[d]);
+        // Chameleon::boundary only when |x| > L/2 (compared as bit patterns)
+        if ((__double_as_longlong(xn[d]) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(S.half[d]))
+            xn[d] = boundary1(xn[d], S.L[d], S.half[d], S.inv[d]);
+    }
+    const uint4 ro = a.rec;
+    const uint4 rn = make_uint4(to_fixed(xn[0], S.fx_scale[0]), to_fixed(xn[1], S.fx_scale[1]),
+                                to_fixed(xn[2], S.fx_scale[2]), ro.w);
+    sub(20);
+    m.ro = ro;
+    m.rn = rn;
+    m.q = itq[ro.w >> 24];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        m.xo[d] = xo[d];
+        m.xn[d] = xn[d];
+        // g = dr / L: the proposal's dr equals the minimum-image xn - xo up to the rounding of
+        // xo + dr (and whole box lengths, which leave every phase change unchanged); the records'
+        // difference would carry their 2^-32 L rounding, too coarse for small moves
+        m.g[d] = d2f_trunc(a.dr[d]) * S.inv_f[d];
+    }
+    if (S.flags & SYS_SURFACE) {
+        const double q = itqd[ro.w >> 24];
+#pragma unroll
+        for (int d = 0; d < 3; d++) m.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
+    }
+    if (prev && prev->kind == FAU_MOVE_ATOMIC && prev->i == m.i) m.conflict = FC_SELF;
+    sub(22);
+    if (cells) {
+        const int co = a.cell;
+        int c[3], cn[3];
+        // the old cell's coordinates: the binning of the old position, checked against the cell
+        // the particle is listed in (divisions only if they ever differ)
+        cell_coords(S, xo, ro, c);
+        if (cell_index(S, c) != co) {
+            c[0] = co % S.cdim[0];
+            c[1] = (co / S.cdim[0]) % S.cdim[1];
+            c[2] = co / (S.cdim[0] * S.cdim[1]);
+        }
+        cell_coords(S, xn, rn, cn);
+        m.cell_old = co;
+        m.cell_new = cell_index(S, cn);
+        bool uni = true;
+        int w = 1;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            m.cc_o[d] = c[d];
+            m.cc_n[d] = cn[d];
+            const int n = S.cdim[d];
+            int v = cn[d] - c[d];
+            if (2 * v > n) v -= n;
+            else if (2 * v < -n) v += n;
+            m.df[d] = v;
+            if (v < -1 || v > 1 || n < 3 + abs(v)) uni = false;
+            m.lo[d] = c[d] + min(v, 0) - 1;
+            m.w[d] = 3 + abs(v);
+            w *= 3 + abs(v);
+        }
+        m.uni = uni ? 1 : 0;
+        m.nue = uni ? w
+                    : 2 * (S.off_max[0] - S.off_min[0] + 1) * (S.off_max[1] - S.off_min[1] + 1) *
+                          (S.off_max[2] - S.off_min[2] + 1);
+    }
+    else {
+        m.cell_old = m.cell_new = 0;
+    }
+    sub(23);
+}
+
+// All threads of the CTA but the producer warp (busy committing): the phase tables
+// (threads 32, 33, ...) and the cell entries (threads NT-1, NT-2, ...) of the move whose
+// scalar part is in `m`.  Returns whether this thread's entries include a cell `prev`
+// (the move evaluated just before) rewrote.
+__device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, const FastMove& prev, int tid, int NT,
+                                              float2* T, int nc)
+{
+    if (m.kind != FAU_MOVE_ATOMIC) return false;
+    const int TS = 2 * nc + 1;
+    if (T && tid >= 32) { // per axis: mid = e^{i n (phi + pi g)} and h = e^{i n pi g}, n = -nc..nc
+        for (int e = tid - 32; e < 3 * (nc + 1); e += NT - 32) {
             const int ax = e / (nc + 1), n = e - ax * (nc + 1);
+            const uint4 ro = m.ro;
             const uint32_t u = ax == 0 ? ro.x : (ax == 1 ? ro.y : ro.z);
-            const float g = d2f_trunc(a.dr[ax]) * S.inv_f[ax];
             float s, c;
-            sincospif((float)n * g, &s, &c);
+            sincospif((float)n * m.g[ax], &s, &c);
             const float2 h = make_float2(c, s);
             const float2 mid = cmul(phase_exact((uint32_t)n * u), h);
             float2* row = T + 2 * ax * TS;
@@ -256,77 +278,44 @@ static __device__ __noinline__ void fast_prepare(const DevSys& S, FastMove& m, c
             row[TS + nc - n] = make_float2(h.x, -h.y);
         }
     }
-    __syncwarp();
-    sub(16);
-    if (m.kind != FAU_MOVE_ATOMIC) {
-        if (lane == 0) m.conflict = 0;
-        __syncwarp();
-        return;
-    }
     bool hit = false;
-    if (cells) {
-        int cco[3], df[3], lo[3], w[3];
-        bool uni = true;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            cco[d] = m.cc_o[d];
-            const int n = S.cdim[d];
-            int v = m.cc_n[d] - cco[d];
-            if (2 * v > n) v -= n;
-            else if (2 * v < -n) v += n;
-            df[d] = v;
-            if (v < -1 || v > 1 || n < 3 + abs(v)) uni = false;
-            lo[d] = cco[d] + min(v, 0) - 1;
-            w[d] = 3 + abs(v);
-        }
-        const int pc_o = prev && prev->kind == FAU_MOVE_ATOMIC ? prev->cell_old : -1;
-        const int pc_n = prev && prev->kind == FAU_MOVE_ATOMIC ? prev->cell_new : -1;
-        int nue;
-        if (uni) { // one box holding both stencils; each cell flags the states whose stencil contains it
-            nue = w[0] * w[1] * w[2];
-            for (int e = lane; e < nue; e += 32) {
+    if (S.flags & SYS_CELLS) {
+        const int nue = m.nue;
+        const int pc_o = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_old : -1;
+        const int pc_n = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_new : -1;
+        for (int e = NT - 1 - tid; tid >= 32 && e < nue; e += NT - 32) {
+            int c[3];
+            uint32_t mask;
+            if (m.uni) { // one box holding both stencils; each cell flags the states whose stencil contains it
+                const int w0 = m.w[0], w1 = m.w[1];
                 // box extents are 3 or 4: constant divisors
-                const int ex = w[0] == 3 ? e % 3 : (e & 3), e1 = w[0] == 3 ? e / 3 : (e >> 2);
-                const int ey = w[1] == 3 ? e1 % 3 : (e1 & 3), ez = w[1] == 3 ? e1 / 3 : (e1 >> 2);
-                const int o[3] = {lo[0] + ex, lo[1] + ey, lo[2] + ez};
+                const int ex = w0 == 3 ? e % 3 : (e & 3), e1 = w0 == 3 ? e / 3 : (e >> 2);
+                const int ey = w1 == 3 ? e1 % 3 : (e1 & 3), ez = w1 == 3 ? e1 / 3 : (e1 >> 2);
+                const int o[3] = {m.lo[0] + ex, m.lo[1] + ey, m.lo[2] + ez};
                 bool in_o = true, in_n = true;
-                int c[3];
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    in_o = in_o && abs(o[d] - cco[d]) <= 1;
-                    in_n = in_n && abs(o[d] - (cco[d] + df[d])) <= 1;
+                    in_o = in_o && abs(o[d] - m.cc_o[d]) <= 1;
+                    in_n = in_n && abs(o[d] - (m.cc_o[d] + m.df[d])) <= 1;
                     c[d] = wrap_cell(o[d], S.cdim[d]);
                 }
-                const int cell = cell_index(S, c);
-                hit = hit || cell == pc_o || cell == pc_n;
-                m.ent[e] = (uint32_t)cell | (in_n ? kEntNew : 0u) | (in_o ? kEntOld : 0u);
+                mask = (in_n ? kEntNew : 0u) | (in_o ? kEntOld : 0u);
             }
-        }
-        else { // the two neighbour stencils listed separately (GridOffsets3D src/celllistimpl.cpp:15-31)
-            const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1,
-                      nbz = S.off_max[2] - S.off_min[2] + 1;
-            const int nb = nbx * nby * nbz;
-            nue = 2 * nb;
-            for (int e = lane; e < nue; e += 32) {
+            else { // the two neighbour stencils listed separately (GridOffsets3D src/celllistimpl.cpp:15-31)
+                const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1;
+                const int nb = nue / 2;
                 const int st = e >= nb ? 1 : 0, r = e - st * nb;
                 const int o[3] = {r % nbx + S.off_min[0], (r / nbx) % nby + S.off_min[1], r / (nbx * nby) + S.off_min[2]};
-                int c[3];
 #pragma unroll
-                for (int d = 0; d < 3; d++) c[d] = wrap_cell((st ? m.cc_n[d] : cco[d]) + o[d], S.cdim[d]);
-                const int cell = cell_index(S, c);
-                hit = hit || cell == pc_o || cell == pc_n;
-                m.ent[e] = (uint32_t)cell | (st ? kEntNew : kEntOld);
+                for (int d = 0; d < 3; d++) c[d] = wrap_cell((st ? m.cc_n[d] : m.cc_o[d]) + o[d], S.cdim[d]);
+                mask = st ? kEntNew : kEntOld;
             }
+            const int cell = cell_index(S, c);
+            hit = hit || cell == pc_o || cell == pc_n;
+            m.ent[e] = (uint32_t)cell | mask;
         }
-        if (lane == 0) m.nue = nue;
     }
-    hit = __any_sync(0xffffffffu, hit);
-    if (lane == 0) {
-        const bool self = prev && prev->kind == FAU_MOVE_ATOMIC && prev->i == m.i;
-        m.conflict = (self ? FC_SELF : 0) | (hit ? FC_CELLS : 0);
-    }
-    __syncwarp();
-    sub(18);
+    return hit;
 }
 
 struct PairOut {
@@ -457,6 +446,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         ps.n_acc = ps.n_mv = 0;
 #pragma unroll
         for (int d = 0; d < 3; d++) ps.M[d] = S.M[d];
+        mvb[2].kind = FAU_MOVE_NONE; // "previous move" of move 0
     }
     __syncthreads();
     const bool cells = (S.flags & SYS_CELLS) != 0;
@@ -478,29 +468,27 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
     unsigned long long n_pairs = 0;
     int since_flush = 0, q_pending = 0; // compute threads: accepts since the FP64 flush; dQ not yet folded in
 
-    if (producer) {
-        if (!PHILOX) {
-            ring_fill(0);
-            ring_fill(32);
-            __syncwarp();
-        }
-        if (lane == 0 && nmoves > 0) {
-            fast_proposal<PHILOX>(S, A, ring, 0, ps.ctr0, ps.sys_id, ps.dp_f, ahs[0]);
-            fast_load(S, ahs[0]);
-            cp_async_commit();
-            cp_async_wait<0>();
-        }
+    // move 0: its scalar part, then tables and cell entries by every thread
+    if (producer && !PHILOX) {
+        ring_fill(0);
+        ring_fill(32);
         __syncwarp();
-        if (nmoves > 0) fast_prepare(S, mvb[0], ahs[0], nullptr, lane, K ? tabs : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
-        if (lane == 0) {
-            if (nmoves > 1) {
-                fast_proposal<PHILOX>(S, A, ring, 1, ps.ctr0, ps.sys_id, ps.dp_f, ahs[1]);
-                fast_load(S, ahs[1]);
-            }
-            fast_commit_loads(S, mvb[0], cps[0]);
-            cp_async_commit();
-        }
     }
+    if (producer && lane == 0 && nmoves > 0) {
+        fast_proposal<PHILOX>(S, A, ring, 0, ps.ctr0, ps.sys_id, ps.dp_f, ahs[0]);
+        fast_load(S, ahs[0]);
+        cp_async_commit();
+        cp_async_wait<0>();
+        fast_scalar(S, mvb[0], ahs[0], nullptr, itq, itqd, nullptr);
+        if (nmoves > 1) {
+            fast_proposal<PHILOX>(S, A, ring, 1, ps.ctr0, ps.sys_id, ps.dp_f, ahs[1]);
+            fast_load(S, ahs[1]);
+        }
+        fast_commit_loads(S, mvb[0], cps[0]);
+        cp_async_commit();
+    }
+    __syncthreads();
+    if (nmoves > 0) fast_parallel(S, mvb[0], mvb[2], tid, NT, K ? tabs : nullptr, nc);
     __syncthreads();
 
     int prev_accept = 0, stop = 0;
@@ -517,8 +505,12 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         const int rb = (int)(t & 1);
         if (timing && tid == 0) tsm[15]++;
         if (producer) {
-            CommitPre& cp = cps[t & 1];
+            if (!PHILOX && (t & 31) == 0 && t >= 32) {
+                ring_fill(t + 32); // proposals [t+32, t+64): first read at move t+30
+                __syncwarp();
+            }
             if (lane == 0) {
+                CommitPre& cp = cps[t & 1];
                 cp_async_wait<0>(); // Ahead of move t+1, commit counts of move t
                 if (kind == FAU_MOVE_ATOMIC && cells) {
                     // read before move t-1's commit: read again if that commit touched them
@@ -545,23 +537,19 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     }
                     m.du_surf = S.surf_pref * (m2n - m2o);
                 }
-            }
-            tick(0);
-            if (!PHILOX && (t & 31) == 0 && t >= 32) ring_fill(t + 32);
-            if (t + 1 < nmoves) {
-                const FastMove& pm = mvb[(t + 2) % 3]; // move t-1
-                Ahead& an = ahs[(t + 1) & 1];
-                if (lane == 0 && t >= 1 && prev_accept && pm.kind == FAU_MOVE_ATOMIC && an.kind == FAU_MOVE_ATOMIC &&
-                    an.i == pm.i) { // copied before move t-1's commit: take the committed state
+                tick(0);
+                if (t + 1 < nmoves) {
+                    const FastMove& pm = mvb[(t + 2) % 3]; // move t-1
+                    Ahead& an = ahs[(t + 1) & 1];
+                    if (t >= 1 && prev_accept && pm.kind == FAU_MOVE_ATOMIC && an.kind == FAU_MOVE_ATOMIC &&
+                        an.i == pm.i) { // copied before move t-1's commit: take the committed state
 #pragma unroll
-                    for (int d = 0; d < 3; d++) an.x[d] = pm.xn[d];
-                    an.rec = pm.rn;
-                    an.cell = pm.cell_new;
-                }
-                __syncwarp();
-                fast_prepare(S, mvb[(t + 1) % 3], an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
-                tick(1);
-                if (lane == 0) {
+                        for (int d = 0; d < 3; d++) an.x[d] = pm.xn[d];
+                        an.rec = pm.rn;
+                        an.cell = pm.cell_new;
+                    }
+                    fast_scalar(S, mvb[(t + 1) % 3], an, &m, itq, itqd, timing ? tsm : nullptr);
+                    tick(1);
                     if (t + 2 < nmoves) {
                         Ahead& a2 = ahs[t & 1];
                         fast_proposal<PHILOX>(S, A, ring, t + 2, ps.ctr0, ps.sys_id, ps.dp_f, a2);
@@ -570,26 +558,14 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     }
                     fast_commit_loads(S, mvb[(t + 1) % 3], cps[(t + 1) & 1]);
                 }
+                cp_async_commit(); // group 2: Ahead of move t+2, commit counts of move t+1
+                tick(2);
             }
-            if (lane == 0) cp_async_commit(); // group 2: Ahead of move t+2, commit counts of move t+1
-            tick(2);
         }
         else if (kind == FAU_MOVE_ATOMIC) {
             const int i = m.i;
             const uint4 ro = m.ro, rn = m.rn;
             const int ti = rn.w >> 24;
-            // all-pairs mode: the previous move's particle may not be in memory yet
-            int pi = -1;
-            uint4 prn = make_uint4(0, 0, 0, 0);
-            const double* pxn = nullptr;
-            if (!cells && prev_accept && t >= 1) {
-                const FastMove& pm = mvb[(t + 2) % 3];
-                if (pm.kind == FAU_MOVE_ATOMIC) {
-                    pi = pm.i;
-                    prn = pm.rn;
-                    pxn = pm.xn;
-                }
-            }
             const int n_items = cells ? (m.nue << cap_shift) : S.n;
             auto load_item = [&](int it, uint4& rj, uint32_t& ent) {
                 if (cells) {
@@ -606,7 +582,6 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             if (ctid < n_items) load_item(ctid, r0, e0);
             if (ctid + NTC < n_items) load_item(ctid + NTC, r1, e1);
             tick(7);
-
             // ---- Ewald: one k-vector per thread and step, two independent accumulators.  The
             // last accepted move's Q(k) change (State::sync trial -> accepted) is folded in here,
             // in the same pass; every 256 accepts the FP32 pending sums go to the FP64 master.
@@ -680,21 +655,15 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     load_item(it, rj, ent);
                 }
                 if (rj.w == kEmptySlot) continue;
-                int j = (int)(rj.w & 0xFFFFFFu);
-                if (!cells) j = it;
+                const int j = cells ? (int)(rj.w & 0xFFFFFFu) : it;
                 if (j == i) continue;
-                const double* xj = nullptr;
-                if (j == pi) {
-                    rj = prn;
-                    xj = pxn;
-                }
                 const int pidx = ti * nt + (int)(rj.w >> 24);
                 const PairF p = pt[pidx];
                 float un = 0.f, uo = 0.f;
                 for (int st = 0; st < 2; st++) {
                     if (!(ent & (st ? kEntOld : kEntNew))) continue;
                     const PairOut o = fast_pair_state(S, p, pidx, r2_fixed(S, st ? ro : rn, rj), st ? m.xo : m.xn, j,
-                                                      xj, st == 0);
+                                                      nullptr, st == 0);
                     if (st) uo = o.u;
                     else un = o.u;
                     flags |= o.flags;
@@ -712,7 +681,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
             }
             tick(10);
         }
-        __syncthreads(); // B1
+        __syncthreads(); // B0
         tick(tid == 0 ? 3 : 11);
 
         // ---- decision, identical in every thread
@@ -768,14 +737,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
 #pragma unroll
                 for (int d = 0; d < 3; d++) ps.M[d] = __dadd_rn(ps.M[d], m.dM[d]);
             }
-        }
-        if (accept) {
-            if (!producer && K) { // this thread's share of Q(k) += dQ(k), folded into the next Ewald pass
-                q_pending = 1;
-                since_flush++;
-            }
-            tick(tid == 0 ? 4 : 13);
-            if (producer && lane == 0) { // commit (State::sync trial -> accepted): positions, record, cell list
+            if (accept) { // commit (State::sync trial -> accepted): positions, record, cell list
                 cp_async_wait<1>();
                 const CommitPre& cp_cur = cps[t & 1];
                 const int i = m.i;
@@ -810,41 +772,49 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     }
                 }
             }
-            tick(tid == 0 ? 5 : 13);
+            tick(5);
+        }
+        if (accept) {
+            if (!producer && K) { // this thread's share of Q(k) += dQ(k), folded into the next Ewald pass
+                q_pending = 1;
+                since_flush++;
+            }
             if (m.cap_full) {
                 stop = FAU_ERR_CAPACITY;
                 break;
             }
         }
-        // ---- the next move reads what this commit rewrote: make it visible (and re-prepare a same-particle move)
-        const int nconf = (accept && t + 1 < nmoves) ? mvb[(t + 1) % 3].conflict : 0;
-        if (nconf) {
-            if (producer && (nconf & FC_SELF)) {
-                FastMove& nm = mvb[(t + 1) % 3];
-                Ahead& an = ahs[(t + 1) & 1];
-                if (lane == 0) {
+        // ---- the next move: re-prepared if it moves the particle just committed, then its
+        // phase tables and cell entries by every thread
+        bool hit = false;
+        if (t + 1 < nmoves) {
+            FastMove& nm = mvb[(t + 1) % 3];
+            if (accept && (nm.conflict & FC_SELF)) {
+                if (producer && lane == 0) {
+                    Ahead& an = ahs[(t + 1) & 1];
                     cp_async_wait<0>();
                     fast_proposal<PHILOX>(S, A, ring, t + 1, ps.ctr0, ps.sys_id, ps.dp_f, an);
                     fast_load(S, an);
                     cp_async_commit();
                     cp_async_wait<0>();
-                }
-                __syncwarp();
-                fast_prepare(S, nm, an, &m, lane, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc, itq, itqd, timing ? tsm : nullptr);
-                if (lane == 0) {
+                    fast_scalar(S, nm, an, &m, itq, itqd, nullptr);
                     fast_commit_loads(S, nm, cps[(t + 1) & 1]);
                     cp_async_commit();
                 }
+                __syncthreads();
             }
-            __syncthreads(); // B2
+            hit = fast_parallel(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc);
         }
+        tick(tid == 0 ? 6 : 13);
+        hit = __syncthreads_or(hit) != 0; // B1: commit, tables and entries visible
+        if (hit && producer && lane == 0) mvb[(t + 1) % 3].conflict |= FC_CELLS;
         tick(tid == 0 ? 6 : 14);
         prev_accept = accept;
     }
+    if (producer && lane == 0) cp_async_wait<0>();
     __syncthreads();
     if (A.phase_cycles && tid < kFastPhaseSlots && tsm[tid])
         atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + tid], tsm[tid]);
-    if (producer && lane == 0) cp_async_wait<0>();
 
     // the last accepted move's change and everything pending into the FP64 master Q
     if (!producer) {
