@@ -135,13 +135,22 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 128, 160 or 256");
     const int threads = (req == 0 || req == 160) ? 128 : req;
     const bool use_fast = req == 0 || req == 160;
+    std::vector<uint8_t> fast(n, 0);
+    for (int i = 0; i < n; i++) {
+        fau_ctx* c2;
+        int K, np, ng, mo, knc;
+        double tr;
+        DevSys* dd;
+        fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+        fast[i] = use_fast && !mol[i] && knc <= kFastMaxNc;
+    }
     std::vector<int> order;   // kernel order: pipelined-kernel systems first
     order.reserve(n);
     for (int i = 0; i < n; i++)
-        if (use_fast && !mol[i]) order.push_back(i);
+        if (fast[i]) order.push_back(i);
     const int nfast = (int)order.size();
     for (int i = 0; i < n; i++)
-        if (!(use_fast && !mol[i])) order.push_back(i);
+        if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
     int Kf = 0, ncf = 0, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {
@@ -434,10 +443,10 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     std::vector<int> order;
     order.reserve(n);
     for (int i = 0; i < n; i++)
-        if (!has_mol[i]) order.push_back(i);
+        if (!has_mol[i] && ncv[i] <= kFastMaxNc) order.push_back(i);
     const int nfast = (int)order.size();
     for (int i = 0; i < n; i++)
-        if (has_mol[i]) order.push_back(i);
+        if (!(!has_mol[i] && ncv[i] <= kFastMaxNc)) order.push_back(i);
     const int nexact = n - nfast;
     int Kf = 0, ncf = 0, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {

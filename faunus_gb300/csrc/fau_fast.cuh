@@ -258,24 +258,21 @@ static __device__ __noinline__ void fast_scalar(const DevSys& S, FastMove& m, co
 // scalar part is in `m`.  Returns whether this thread's entries include a cell `prev`
 // (the move evaluated just before) rewrote.
 __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, const FastMove& prev, int tid, int NT,
-                                              float2* T, int nc)
+                                              float4* T, int nc)
 {
     if (m.kind != FAU_MOVE_ATOMIC) return false;
     const int TS = 2 * nc + 1;
-    if (T && tid >= 32) { // per axis: mid = e^{i n (phi + pi g)} and h = e^{i n pi g}, n = -nc..nc
+    if (T && tid >= 32) { // per axis and n = -nc..nc: {mid, h}, mid = e^{i n (phi + pi g)}, h = e^{i n pi g}
         for (int e = tid - 32; e < 3 * (nc + 1); e += NT - 32) {
             const int ax = e / (nc + 1), n = e - ax * (nc + 1);
             const uint4 ro = m.ro;
             const uint32_t u = ax == 0 ? ro.x : (ax == 1 ? ro.y : ro.z);
             float s, c;
             sincospif((float)n * m.g[ax], &s, &c);
-            const float2 h = make_float2(c, s);
-            const float2 mid = cmul(phase_exact((uint32_t)n * u), h);
-            float2* row = T + 2 * ax * TS;
-            row[nc + n] = mid;
-            row[nc - n] = make_float2(mid.x, -mid.y);
-            row[TS + nc + n] = h;
-            row[TS + nc - n] = make_float2(h.x, -h.y);
+            const float2 mid = cmul(phase_exact((uint32_t)n * u), make_float2(c, s));
+            float4* row = T + ax * TS;
+            row[nc + n] = make_float4(mid.x, mid.y, c, s);
+            row[nc - n] = make_float4(mid.x, -mid.y, c, -s);
         }
     }
     bool hit = false;
@@ -390,9 +387,9 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
     const int nt = S.nt;
     float4* kq = reinterpret_cast<float4*>(smem_raw); // {Q.x, Q.y, pending.x, pending.y} (FP32 copy + accepted, unflushed)
     float2* dlt = reinterpret_cast<float2*>(kq + K);  // this move's change of Q(k)
-    int2* kaf = reinterpret_cast<int2*>(dlt + K);     // {(nx+nc) | (ny+nc)<<8 | (nz+nc)<<16, (2 pi lB / V) A_k}
-    float2* tabs = reinterpret_cast<float2*>(kaf + K); // 3 slots x 6 rows x TS phase tables
-    PairF* pt = reinterpret_cast<PairF*>(tabs + 3 * 6 * TS);
+    int2* kaf = reinterpret_cast<int2*>(dlt + K);     // {table entries of nx, ny, nz (8 bits each), (2 pi lB / V) A_k}
+    float4* tabs = reinterpret_cast<float4*>(kaf + K); // 3 slots x 3 axes x TS phase-table entries {mid, h}
+    PairF* pt = reinterpret_cast<PairF*>(tabs + 3 * 3 * TS);
 
     __shared__ FastMove mvb[3];
     __shared__ Ahead ahs[2];       // move s: ahs[s & 1]
@@ -426,7 +423,8 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         kq[k] = make_float4((float)q.x, (float)q.y, 0.f, 0.f);
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
-        kaf[k] = make_int2((nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16), __float_as_int(rec_pref_f * S.Ak[k]));
+        kaf[k] = make_int2((nx + nc) | ((TS + ny + nc) << 8) | ((2 * TS + nz + nc) << 16),
+                           __float_as_int(rec_pref_f * S.Ak[k]));
     }
     for (int t = tid; t < nt * nt; t += NT) pt[t] = S.pair[t];
     if (tid < nt) {
@@ -601,9 +599,10 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     since_flush = 0;
                 }
                 const bool pa = q_pending != 0;
-                const float2* Tb = tabs + b * 6 * TS;
+                const float4* Tb = tabs + b * 3 * TS;
                 const float f0 = 2.f * m.q;
-                auto ewald_k = [&](int k, FF& acc) {
+                // (2 pi lB / V) A_k (|Q + d|^2 - |Q|^2) for one k-vector; dQ(k) = d kept for the commit
+                auto ewald_k = [&](int k) {
                     float4 qq = kq[k];
                     if (pa) {
                         const float2 dp = dlt[k];
@@ -612,64 +611,80 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                         kq[k] = qq;
                     }
                     const int2 ka = kaf[k];
-                    const int ix = ka.x & 0xff, iy = (ka.x >> 8) & 0xff, iz = ka.x >> 16;
-                    const float2 mid = cmul(cmul(Tb[ix], Tb[2 * TS + iy]), Tb[4 * TS + iz]);
-                    const float2 hxy = cmul(Tb[TS + ix], Tb[3 * TS + iy]);
-                    const float2 hz = Tb[5 * TS + iz];
-                    const float f = f0 * fmaf(hxy.x, hz.y, hxy.y * hz.x); // 2 q sin(D/2)
+                    const float4 tx = Tb[ka.x & 0xff], ty = Tb[(ka.x >> 8) & 0xff], tz = Tb[ka.x >> 16];
+                    const float2 mid = cmul(cmul(make_float2(tx.x, tx.y), make_float2(ty.x, ty.y)), make_float2(tz.x, tz.y));
+                    const float2 hxy = cmul(make_float2(tx.z, tx.w), make_float2(ty.z, ty.w));
+                    const float f = f0 * fmaf(hxy.x, tz.w, hxy.y * tz.z); // 2 q sin(D/2)
                     const float2 d = make_float2(-f * mid.y, f * mid.x);
                     dlt[k] = d;
                     const float qx = qq.x + qq.z, qy = qq.y + qq.w;
                     const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
                     const float dd = fmaf(d.x, d.x, d.y * d.y);
-                    ff_add(acc, __int_as_float(ka.y) * (cross + dd));
+                    return __int_as_float(ka.y) * (cross + dd);
                 };
                 int k = ctid;
                 for (; k + NTC < K; k += 2 * NTC) {
-                    ewald_k(k, acc0);
-                    ewald_k(k + NTC, acc1);
+                    const float ta = ewald_k(k), tb = ewald_k(k + NTC);
+                    ff_add(acc0, ta + tb);
                 }
-                if (k < K) ewald_k(k, acc0);
+                if (k < K) ff_add(acc1, ewald_k(k));
                 q_pending = 0;
             }
             FF accp = ff_sum(acc0, acc1);
             int flags = 0;
             tick(8);
 
-            // ---- pairs
-            for (int r = 0;; r++) {
-                const int it = ctid + r * NTC;
-                if (it >= n_items) break;
-                uint4 rj;
-                uint32_t ent;
-                if (r == 0) {
-                    rj = r0;
-                    ent = e0;
-                }
-                else if (r == 1) {
-                    rj = r1;
-                    ent = e1;
+            // ---- pairs: items in rounds of two per lane; the occupied ones (non-empty slot, not the
+            // moved particle, in a stencil) are compacted across the warp and each lane evaluates
+            // one (pair, state) task, so a sparse neighbourhood costs one pass, not one per item
+            const unsigned FULL = 0xffffffffu;
+            const int wbase = (warp - 1) * 32;
+            for (int rr = 0; 2 * rr * NTC < n_items; rr++) {
+                const int ita = ctid + 2 * rr * NTC, itb = ita + NTC;
+                uint4 ra, rb2;
+                uint32_t ea = 0, eb = 0;
+                if (rr == 0) {
+                    ra = r0;
+                    ea = e0;
+                    rb2 = r1;
+                    eb = e1;
                 }
                 else {
-                    if (r == 2) tick(19);
-                    load_item(it, rj, ent);
+                    if (rr == 1) tick(19);
+                    ra = rb2 = make_uint4(0, 0, 0, kEmptySlot);
+                    if (ita < n_items) load_item(ita, ra, ea);
+                    if (itb < n_items) load_item(itb, rb2, eb);
                 }
-                if (rj.w == kEmptySlot) continue;
-                const int j = cells ? (int)(rj.w & 0xFFFFFFu) : it;
-                if (j == i) continue;
-                const int pidx = ti * nt + (int)(rj.w >> 24);
-                const PairF p = pt[pidx];
-                float un = 0.f, uo = 0.f;
-                for (int st = 0; st < 2; st++) {
-                    if (!(ent & (st ? kEntOld : kEntNew))) continue;
-                    const PairOut o = fast_pair_state(S, p, pidx, r2_fixed(S, st ? ro : rn, rj), st ? m.xo : m.xn, j,
-                                                      nullptr, st == 0);
-                    if (st) uo = o.u;
-                    else un = o.u;
-                    flags |= o.flags;
-                    n_pairs++;
+                auto occupied = [&](const uint4& r, uint32_t e, int it) {
+                    if (it >= n_items || r.w == kEmptySlot || !(e & (kEntNew | kEntOld))) return false;
+                    return (cells ? (int)(r.w & 0xFFFFFFu) : it) != i;
+                };
+                const unsigned ba = __ballot_sync(FULL, occupied(ra, ea, ita));
+                const unsigned bb = __ballot_sync(FULL, occupied(rb2, eb, itb));
+                const int na = __popc(ba), nv = na + __popc(bb);
+                for (int base = 0; base < 2 * nv; base += 32) {
+                    const int task = base + lane, q = task >> 1, st = task & 1;
+                    const bool second = q >= na;
+                    int src = 0;
+                    if (q < nv) src = (int)__fns(second ? bb : ba, 0, (second ? q - na : q) + 1);
+                    // the source lane's item (both of its items travel; this lane picks one)
+                    const uint4 xa = make_uint4(__shfl_sync(FULL, ra.x, src), __shfl_sync(FULL, ra.y, src),
+                                                __shfl_sync(FULL, ra.z, src), __shfl_sync(FULL, ra.w, src));
+                    const uint4 xb = make_uint4(__shfl_sync(FULL, rb2.x, src), __shfl_sync(FULL, rb2.y, src),
+                                                __shfl_sync(FULL, rb2.z, src), __shfl_sync(FULL, rb2.w, src));
+                    const uint32_t xea = __shfl_sync(FULL, ea, src), xeb = __shfl_sync(FULL, eb, src);
+                    const uint4 rj = second ? xb : xa;
+                    const uint32_t ent = second ? xeb : xea;
+                    if (q < nv && (ent & (st ? kEntOld : kEntNew))) {
+                        const int j = cells ? (int)(rj.w & 0xFFFFFFu) : wbase + src + (2 * rr + (second ? 1 : 0)) * NTC;
+                        const int pidx = ti * nt + (int)(rj.w >> 24);
+                        const PairOut o = fast_pair_state(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
+                                                          st ? m.xo : m.xn, j, nullptr, st == 0);
+                        ff_add(accp, st ? -o.u : o.u);
+                        flags |= o.flags;
+                        n_pairs++;
+                    }
                 }
-                ff_add(accp, un - uo);
             }
             tick(9);
             float sc_unused = 0.f;
@@ -803,7 +818,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                 }
                 __syncthreads();
             }
-            hit = fast_parallel(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 6 * TS : nullptr, nc);
+            hit = fast_parallel(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc);
         }
         tick(tid == 0 ? 6 : 13);
         hit = __syncthreads_or(hit) != 0; // B1: commit, tables and entries visible
@@ -858,7 +873,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
 // dynamic shared memory of the pipelined kernel for K k-vectors, table size nc
 __host__ __device__ inline size_t fast_smem_bytes(int K, int nc)
 {
-    return (size_t)K * (sizeof(float4) + sizeof(float2) + sizeof(int2)) + (size_t)3 * 6 * (2 * nc + 1) * sizeof(float2) +
+    return (size_t)K * (sizeof(float4) + sizeof(float2) + sizeof(int2)) + (size_t)3 * 3 * (2 * nc + 1) * sizeof(float4) +
            (size_t)kMaxITypes * kMaxITypes * sizeof(PairF);
 }
 

@@ -59,7 +59,9 @@ cudaError_t chain_dispatch_128_host(const ChainArgs&, int, int, int, cudaStream_
 cudaError_t chain_dispatch_128_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
-// pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps
+// pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps;
+// k-vector components up to kFastMaxNc (8-bit phase-table indices)
+constexpr int kFastMaxNc = 40;
 size_t fast_smem_bytes_total(int K, int nc);
 cudaError_t prepare_fast(int K, int nc, int warps, bool philox);
 cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox, cudaStream_t st);
