@@ -154,7 +154,7 @@ __device__ __forceinline__ int wrap_cell(int v, int n) { return v < 0 ? v + n : 
 // entries of the move staged in `a`; `prev` is the move evaluated just before it.
 // FP64 work per move: the IEEE add and fixed-point rounding of AtomicTranslateRotate's
 // new position (3 x add, multiply, convert).
-static __device__ __noinline__ void fast_scalar(const DevSys& S, FastMove& m, const Ahead& a, const FastMove* prev,
+static __device__ __forceinline__ void fast_scalar(const DevSys& S, FastMove& m, const Ahead& a, const FastMove* prev,
                                                 const float* itq, const double* itqd, unsigned long long* tsm)
 {
     long long t0 = tsm ? clock64() : 0;
@@ -615,12 +615,11 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
                     const float2 mid = cmul(cmul(make_float2(tx.x, tx.y), make_float2(ty.x, ty.y)), make_float2(tz.x, tz.y));
                     const float2 hxy = cmul(make_float2(tx.z, tx.w), make_float2(ty.z, ty.w));
                     const float f = f0 * fmaf(hxy.x, tz.w, hxy.y * tz.z); // 2 q sin(D/2)
-                    const float2 d = make_float2(-f * mid.y, f * mid.x);
-                    dlt[k] = d;
+                    dlt[k] = make_float2(-f * mid.y, f * mid.x);             // d = 2 q sin(D/2) i mid
                     const float qx = qq.x + qq.z, qy = qq.y + qq.w;
-                    const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
-                    const float dd = fmaf(d.x, d.x, d.y * d.y);
-                    return __int_as_float(ka.y) * (cross + dd);
+                    // 2 Re(Q* d) + |d|^2 = f (2 (Qy mid.x - Qx mid.y) + f)
+                    const float r = fmaf(qy, mid.x, -qx * mid.y);
+                    return __int_as_float(ka.y) * (f * fmaf(2.f, r, f));
                 };
                 int k = ctid;
                 for (; k + NTC < K; k += 2 * NTC) {
