@@ -38,7 +38,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 # algorithmic work per unit (flops; add/mul/compare = 1, FMA = 2)
-FLOPS_PER_K_UPDATE = 26.0    # per k-vector per moved atom: 2 phases (12), dQ (8), dU_rec share (6)
+FLOPS_PER_K_UPDATE = 37.0    # per k-vector per moved atom: midpoint phase (12), sin(D/2) (9), dQ (3),
+                             # pending fold (2), dU_rec term (7), accumulation (4)
 FLOPS_PER_PAIR = 38.0        # per pair interaction (LJ + Ewald real space)
 BYTES_PER_PAIR_CANDIDATE = 16.0
 
@@ -134,8 +135,8 @@ def _sum_over_ranks(dist, x: float) -> float:
 
 
 def _profile_traffic():
-    """DRAM bytes per move of the chain kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "chain_kernel_bulk_ewald.json"
+    """DRAM bytes per move of the pipelined chain kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "fast_chain_kernel_bulk_ewald.json"
     if p.exists():
         try:
             d = json.loads(p.read_text())
@@ -215,7 +216,7 @@ def run_ours(args) -> None:
     ctx = F.Context(local)
     base = configs.bulk_ewald(n_salt=10000, seed=1)
     sms = _sm_count(local)
-    R = args.replicas or 2 * sms
+    R = args.replicas or 4 * sms  # four chains per SM: the pipelined kernel's occupancy limit
     M = args.moves
     first = ctx.create(base)
     systems = [first] + [first.clone() for _ in range(R - 1)]

@@ -170,6 +170,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_get_cells": ([P, iptr], C.c_int),
         "fau_get_cell_grid": ([P, iptr], C.c_int),
         "fau_get_running_energy": ([P, dptr], C.c_int),
+        "fau_get_counters": ([P, C.POINTER(C.c_int64)], C.c_int),
         "fau_set_temperature_scale": ([P, C.c_double], C.c_int),
         "fau_q_rebuild": ([P, dptr], C.c_int),
         "fau_get_q": ([P, dptr], C.c_int),

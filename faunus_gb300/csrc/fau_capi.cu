@@ -1305,6 +1305,19 @@ int fau_get_running_energy(fau_sys* s, double* e)
     return FAU_OK;
 }
 
+int fau_get_counters(fau_sys* s, int64_t* out)
+{
+    if (!s || !out) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    int rc = pull_state(s);
+    if (rc) return rc;
+    out[0] = (int64_t)s->h.moves;
+    out[1] = (int64_t)s->h.accepted;
+    out[2] = (int64_t)s->h.pair_evals;
+    out[3] = (int64_t)s->h.k_updates;
+    return FAU_OK;
+}
+
 int fau_set_temperature_scale(fau_sys* s, double scale)
 {
     if (!s || !(scale > 0.0) || !std::isfinite(scale)) return fail(FAU_ERR_ARG, "invalid scale");

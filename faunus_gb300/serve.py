@@ -1,0 +1,234 @@
+"""Continuous-batching server for Metropolis MC jobs on one GPU.
+
+A job is one Faunus system (``SystemSpec``) and a number of single-atom or
+molecular translate/rotate moves.  The server
+
+  * admits queued jobs while a slot is free and the job's device footprint
+    (positions, records, cell list, Q(k), pair tables: ``fau_sys_footprint``)
+    fits in the HBM budget beside the jobs already resident; a job that can
+    never fit is rejected at once;
+  * keeps every admitted job's state resident on the device between launches;
+  * advances all resident jobs together, ``block_moves`` moves per round, in
+    one ``fau_run_batch`` call per (dp, dprot) group -- jobs join and leave
+    between rounds, so work that arrives while others run overlaps with them;
+  * retires a job when its moves are done and reports, per job, the queueing
+    and run time, and for the stream, p50/p99 latency (arrival -> result) and
+    the aggregate moves/s.
+
+Each job's moves come from the device counter RNG keyed by (server seed, job
+id, move counter), so a job's trajectory -- and its result -- is the same
+alone and in any mix of other jobs.
+
+The scheduler talks to a small backend interface (``GpuBackend`` drives the
+C ABI); tests of the scheduling logic substitute a host-only backend.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+from typing import Callable, Dict, List, Optional, Sequence
+
+import numpy as np
+
+from .system import Context, SystemSpec, footprint
+
+
+@dataclass
+class Job:
+    spec: SystemSpec
+    moves: int
+    id: int
+    dp: float = 2.0
+    dprot: float = 0.0
+    arrival_s: float = 0.0  # seconds after the stream starts
+
+
+@dataclass
+class JobResult:
+    id: int
+    status: str                  # "done" or "rejected: ..."
+    moves: int = 0
+    accepted: int = 0
+    energy: float = float("nan")  # running total energy at the end (kT)
+    positions: Optional[np.ndarray] = None
+    arrival_s: float = 0.0
+    admitted_s: float = float("nan")
+    finished_s: float = float("nan")
+
+    @property
+    def latency_s(self) -> float:
+        return self.finished_s - self.arrival_s
+
+
+@dataclass
+class _Active:
+    job: Job
+    handle: object
+    bytes: int
+    done: int = 0
+    admitted_s: float = 0.0
+
+
+class GpuBackend:
+    """The device through the C ABI: one resident system per job."""
+
+    def __init__(self, ctx: Context, threads: int = 0):
+        self.ctx = ctx
+        self.threads = threads
+
+    def footprint(self, spec: SystemSpec) -> int:
+        return footprint(spec)
+
+    def create(self, spec: SystemSpec):
+        return self.ctx.create(spec)
+
+    def run(self, handles, moves: Sequence[int], *, seed: int, streams: Sequence[int], counters: Sequence[int],
+            dp: float, dprot: float) -> None:
+        """Advance each system by its move count in one launch (CUDA graph)."""
+        self.ctx.run_batch(handles, moves_per_system=np.asarray(moves, dtype=np.int64), seed=seed,
+                           streams=np.asarray(streams, dtype=np.uint32),
+                           counters=np.asarray(counters, dtype=np.uint64), dp=dp, dprot=dprot,
+                           threads=self.threads)
+
+    def result(self, handle, with_positions: bool) -> dict:
+        c = handle.counters()
+        return {"energy": handle.running_energy(), "accepted": c["accepted"], "moves": c["moves"],
+                "positions": handle.positions() if with_positions else None}
+
+    def close(self, handle) -> None:
+        handle.close()
+
+
+class Server:
+    def __init__(self, backend, hbm_budget: int, max_slots: int = 608, block_moves: int = 2000, seed: int = 1,
+                 keep_positions: bool = False, clock: Callable[[], float] = time.perf_counter):
+        if hbm_budget <= 0:
+            raise ValueError("hbm_budget must be positive")
+        self.backend = backend
+        self.budget = int(hbm_budget)
+        self.max_slots = int(max_slots)
+        self.block = int(block_moves)
+        self.seed = int(seed)
+        self.keep_positions = keep_positions
+        self.clock = clock
+        self.queue: List[Job] = []
+        self.active: Dict[int, _Active] = {}
+        self.results: Dict[int, JobResult] = {}
+        self.moves_done = 0
+        self.rounds = 0
+        self.resident = 0  # footprint of the admitted jobs (the budget covers only these)
+        self.t0 = None
+
+    # ---------------------------------------------------------------- time
+    def now(self) -> float:
+        if self.t0 is None:
+            self.t0 = self.clock()
+        return self.clock() - self.t0
+
+    # ---------------------------------------------------------------- jobs
+    def submit(self, job: Job) -> None:
+        if job.id in self.active or job.id in self.results or any(q.id == job.id for q in self.queue):
+            raise ValueError(f"job id {job.id} already used")
+        if job.moves < 0:
+            raise ValueError("negative move count")
+        self.queue.append(job)
+
+    def _admit(self) -> None:
+        now = self.now()
+        keep = []
+        for job in self.queue:
+            if job.arrival_s > now:
+                keep.append(job)
+                continue
+            need = self.backend.footprint(job.spec)
+            if need > self.budget:
+                self.results[job.id] = JobResult(job.id, f"rejected: footprint {need} B exceeds the HBM budget "
+                                                         f"{self.budget} B", arrival_s=job.arrival_s,
+                                                 finished_s=now)
+                continue
+            if len(self.active) >= self.max_slots or self.resident + need > self.budget:
+                keep.append(job)  # waits for a slot / memory to free up
+                continue
+            self.active[job.id] = _Active(job, self.backend.create(job.spec), need, admitted_s=now)
+            self.resident += need
+        self.queue = keep
+
+    def _retire(self) -> None:
+        now = self.now()
+        for jid in [j for j, a in self.active.items() if a.done >= a.job.moves]:
+            a = self.active.pop(jid)
+            r = self.backend.result(a.handle, self.keep_positions)
+            self.backend.close(a.handle)
+            self.resident -= a.bytes
+            self.results[jid] = JobResult(jid, "done", moves=r["moves"], accepted=r["accepted"], energy=r["energy"],
+                                          positions=r["positions"], arrival_s=a.job.arrival_s,
+                                          admitted_s=a.admitted_s, finished_s=now)
+
+    def step(self) -> int:
+        """Admit, run one round of moves over every resident job, retire; returns moves run."""
+        self._admit()
+        self._retire()  # zero-move jobs
+        if not self.active:
+            return 0
+        groups: Dict[tuple, List[_Active]] = {}
+        for a in self.active.values():
+            groups.setdefault((a.job.dp, a.job.dprot), []).append(a)
+        total = 0
+        for (dp, dprot), members in groups.items():
+            moves = [min(self.block, a.job.moves - a.done) for a in members]
+            self.backend.run([a.handle for a in members], moves, seed=self.seed,
+                             streams=[a.job.id for a in members], counters=[a.done for a in members],
+                             dp=dp, dprot=dprot)
+            for a, m in zip(members, moves):
+                a.done += m
+                total += m
+        self.moves_done += total
+        self.rounds += 1
+        self._retire()
+        return total
+
+    def idle(self) -> bool:
+        return not self.active and not self.queue
+
+    def run(self, jobs: Sequence[Job] = (), fast_forward: bool = True) -> dict:
+        """Serve a stream until every job has a result.  With fast_forward, idle gaps
+        before the next arrival are skipped (the clock jumps) instead of slept."""
+        for j in jobs:
+            self.submit(j)
+        self.now()
+        while not self.idle():
+            ran = self.step()
+            if ran == 0 and not self.active and self.queue:
+                wait = min(j.arrival_s for j in self.queue) - self.now()
+                if wait > 0:
+                    if fast_forward:
+                        self.t0 -= wait
+                    else:
+                        time.sleep(wait)
+        return self.report()
+
+    def report(self) -> dict:
+        done = [r for r in self.results.values() if r.status == "done"]
+        lat = np.array([r.latency_s for r in done]) if done else np.zeros(0)
+        wall = self.now()
+        return {
+            "jobs_done": len(done),
+            "jobs_rejected": sum(1 for r in self.results.values() if r.status != "done"),
+            "moves": int(self.moves_done),
+            "rounds": self.rounds,
+            "wall_s": wall,
+            "moves_per_s": self.moves_done / wall if wall > 0 else 0.0,
+            "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+        }
+
+
+def jobs_from_stream(stream: Sequence[dict]) -> List[Job]:
+    """Jobs from configs.served_jobs() records, with the shape's displacement parameters."""
+    out = []
+    for rec in stream:
+        spec = rec["spec"]
+        mv = spec.extra["moves"][0]
+        out.append(Job(spec=spec, moves=int(rec["moves"]), id=int(rec["id"]), dp=float(mv.get("dp", 2.0)),
+                       dprot=float(mv.get("dprot", 0.0)), arrival_s=float(rec["arrival_s"])))
+    return out

@@ -320,6 +320,15 @@ class System:
         A.check(self._lib.fau_get_running_energy(self.handle, C.byref(v)), "fau_get_running_energy")
         return float(v.value)
 
+    def counters(self) -> dict:
+        """Moves, accepted moves, pair evaluations and k-vector updates since creation."""
+        v = (C.c_int64 * 4)()
+        A.check(self._lib.fau_get_counters(self.handle, v), "fau_get_counters")
+        return {"moves": int(v[0]), "accepted": int(v[1]), "pair_evals": int(v[2]), "k_updates": int(v[3])}
+
+    def accepted_moves(self) -> int:
+        return self.counters()["accepted"]
+
     def set_temperature_scale(self, scale: float) -> None:
         A.check(self._lib.fau_set_temperature_scale(self.handle, float(scale)), "fau_set_temperature_scale")
 

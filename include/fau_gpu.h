@@ -307,6 +307,10 @@ int fau_get_mass_centers(fau_sys* sys, double* xyz_out);       /* n_groups*3 */
 int fau_get_cells(fau_sys* sys, int* cell_out);                /* n cell index or -1 */
 int fau_get_cell_grid(const fau_sys* sys, int dims_out[3]);
 int fau_get_running_energy(fau_sys* sys, double* energy_out);  /* FP64 running total */
+/* Move counters since the system was created: {moves, accepted, pair
+ * evaluations, k-vector updates} (Move::number_of_attempted_moves and
+ * number_of_accepted_moves, src/move.h:50-59, summed over moves). */
+int fau_get_counters(fau_sys* sys, int64_t counters_out[4]);
 int fau_set_temperature_scale(fau_sys* sys, double scale);     /* beta multiplier (PT) */
 /* Rebuild Q(k) in FP64 from the resident positions; returns the largest
  * |Q_cumulative - Q_rebuilt| before replacing (drift of the running Q). */

@@ -1,0 +1,140 @@
+"""Scheduling logic of the continuous-batching server (host only).
+
+A fake backend stands in for the device: each "system" advances a
+deterministic counter, and a fake clock advances a fixed time per launched
+move, so admission, slot limits, memory limits, rejection, continuous
+joining and latency accounting are checked exactly.
+"""
+import numpy as np
+import pytest
+
+from faunus_gb300.serve import Job, Server
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+
+class FakeSystem:
+    def __init__(self, spec):
+        self.spec = spec
+        self.moves = 0
+        self.state = 0
+        self.closed = False
+
+
+class FakeBackend:
+    """Footprint = spec["bytes"]; a run advances each system's state by a hash of
+    (seed, stream, counter) per move, independent of the other systems."""
+
+    def __init__(self, clock, seconds_per_move=1e-6):
+        self.clock = clock
+        self.spm = seconds_per_move
+        self.live = []
+        self.launches = []
+
+    def footprint(self, spec):
+        return spec["bytes"]
+
+    def create(self, spec):
+        s = FakeSystem(spec)
+        self.live.append(s)
+        return s
+
+    def run(self, handles, moves, *, seed, streams, counters, dp, dprot):
+        self.launches.append(sorted(streams))
+        for h, m, st, c in zip(handles, moves, streams, counters):
+            for k in range(c, c + m):
+                h.state = (h.state * 6364136223846793005 + (seed ^ (st << 20) ^ k)) & (2**64 - 1)
+            h.moves += m
+        self.clock.t += self.spm * max(moves)  # the launch lasts as long as its longest chain
+
+    def result(self, h, with_positions):
+        return {"energy": float(h.state % 1000003), "accepted": h.moves // 2, "moves": h.moves,
+                "positions": None}
+
+    def close(self, h):
+        h.closed = True
+        self.live.remove(h)
+
+
+def _server(budget=100, slots=4, block=1000, **kw):
+    clock = FakeClock()
+    be = FakeBackend(clock)
+    return Server(be, hbm_budget=budget, max_slots=slots, block_moves=block, clock=clock, **kw), be, clock
+
+
+def test_every_job_finishes_with_its_moves():
+    srv, be, _ = _server()
+    jobs = [Job(spec={"bytes": 10}, moves=m, id=i) for i, m in enumerate([500, 2500, 1000, 0, 7000])]
+    rep = srv.run(jobs)
+    assert rep["jobs_done"] == 5 and rep["jobs_rejected"] == 0
+    assert [srv.results[i].moves for i in range(5)] == [500, 2500, 1000, 0, 7000]
+    assert rep["moves"] == 11000 and not be.live
+
+
+def test_oversize_job_is_rejected_and_others_run():
+    srv, be, _ = _server(budget=100)
+    rep = srv.run([Job(spec={"bytes": 101}, moves=10, id=0), Job(spec={"bytes": 50}, moves=10, id=1)])
+    assert srv.results[0].status.startswith("rejected")
+    assert srv.results[1].status == "done"
+    assert rep["jobs_rejected"] == 1
+
+
+def test_admission_waits_for_memory_and_slots():
+    srv, be, _ = _server(budget=100, slots=2, block=1000)
+    jobs = [Job(spec={"bytes": 60}, moves=3000, id=0), Job(spec={"bytes": 60}, moves=1000, id=1),
+            Job(spec={"bytes": 30}, moves=1000, id=2), Job(spec={"bytes": 10}, moves=1000, id=3)]
+    srv.run(jobs)
+    # job 1 cannot share memory with job 0; jobs 2 and 3 fill the second slot one after the other
+    for launch in be.launches:
+        assert len(launch) <= 2
+        assert sum(jobs[i].spec["bytes"] for i in launch) <= 100
+    assert be.launches[0] == [0, 2]
+    assert all(r.status == "done" for r in srv.results.values())
+
+
+def test_continuous_batching_jobs_join_between_rounds():
+    srv, be, clock = _server(budget=1000, slots=8, block=1000)
+    # one second per launched move would be too slow: 1 ms per 1000-move round
+    be.spm = 1e-6
+    jobs = [Job(spec={"bytes": 1}, moves=10000, id=0, arrival_s=0.0),
+            Job(spec={"bytes": 1}, moves=2000, id=1, arrival_s=0.0025)]
+    srv.run(jobs)
+    # job 1 arrived while job 0 was running and was launched together with it
+    joint = [l for l in be.launches if l == [0, 1]]
+    assert len(joint) == 2
+    r0, r1 = srv.results[0], srv.results[1]
+    assert r1.admitted_s >= 0.0025 and r1.finished_s < r0.finished_s
+    assert r1.latency_s == pytest.approx(r1.finished_s - 0.0025)
+
+
+def test_result_is_the_same_alone_and_in_the_mix():
+    a, _, _ = _server(block=700)
+    a.run([Job(spec={"bytes": 1}, moves=5000, id=42)])
+    b, _, _ = _server(block=700, slots=8)
+    b.run([Job(spec={"bytes": 1}, moves=m, id=i) for i, m in [(1, 900), (2, 12000), (42, 5000), (3, 10)]])
+    assert a.results[42].energy == b.results[42].energy
+
+
+def test_report_percentiles_and_idle_gaps_are_skipped():
+    srv, be, clock = _server(budget=100, slots=4, block=1000)
+    jobs = [Job(spec={"bytes": 1}, moves=1000 * (i + 1), id=i, arrival_s=10.0 * i) for i in range(10)]
+    rep = srv.run(jobs, fast_forward=True)
+    lat = np.array([srv.results[i].latency_s for i in range(10)])
+    assert rep["p50_latency_s"] == pytest.approx(np.percentile(lat, 50))
+    assert rep["p99_latency_s"] == pytest.approx(np.percentile(lat, 99))
+    assert (lat > 0).all() and lat.max() < 1.0  # the 10 s gaps were fast-forwarded, not slept
+
+
+def test_duplicate_ids_and_bad_budget_are_rejected():
+    srv, _, _ = _server()
+    srv.submit(Job(spec={"bytes": 1}, moves=1, id=7))
+    with pytest.raises(ValueError):
+        srv.submit(Job(spec={"bytes": 1}, moves=1, id=7))
+    with pytest.raises(ValueError):
+        Server(FakeBackend(FakeClock()), hbm_budget=0)
