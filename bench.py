@@ -223,10 +223,19 @@ def run_ours(args) -> None:
     streams = np.arange(R, dtype=np.uint32) + 1_000_000 * rank
     resident = ctx.hbm_used()
 
+    # ---- kernel configuration: the autotuner's choice unless --threads is given
+    tuned = None
+    threads = args.threads
+    if threads < 0:
+        from faunus_gb300 import autotune
+        tuned = autotune.tune(ctx, first, replicas=max(8, R // 4), moves=1000, force=True,
+                              cache=Path(os.environ.get("TMPDIR", "/tmp")) / f"fau_tune_{os.getpid()}.json")
+        threads = tuned["threads"]
+
     # ---- value: device RNG, resident state
     def step(k):
         return ctx.run_batch(systems, M, seed=args.seed, counter_base=k * M, streams=streams, dp=2.0,
-                             threads=args.threads)
+                             threads=threads)
 
     for w in range(args.warmup):
         step(w)
@@ -297,8 +306,10 @@ def run_ours(args) -> None:
                                "ncutoff 8, 45^3 cells, transrot dp 2 A) x R replica chains",
                    "replicas_per_gpu": R, "moves_per_replica_per_step": M, "n_particles": base.n,
                    "kvectors": systems[0].K, "cells": "x".join(map(str, systems[0].cell_grid())),
-                   "threads_per_chain": args.threads or 160,
-                   "kernel": "pipelined chain kernel" if args.threads in (0, 160) else "chain kernel",
+                   "threads_per_chain": threads or 160,
+                   "kernel": "pipelined chain kernel" if threads in (0, 96, 160, 288) else "chain kernel",
+                   "autotune": ({"table": tuned["table"], "replicas": tuned["replicas"], "moves": tuned["moves"]}
+                                if tuned else "off (--threads given)"),
                    "l2": f"inputs larger than L2: {resident / 2**30:.1f} GiB resident per GPU",
                    "parallelism": f"replicas (dp{world})", "rng": "Philox4x32-10 on device (value); "
                    "reference mt19937 stream on host (e2e)"},
@@ -316,6 +327,10 @@ def run_ours(args) -> None:
         "gpu_launches": 3 * args.steps,
         "wall_s": wall,
     }
+    if rank == 0 and not args.no_extras:
+        line["plain_fp64_single_system"] = plain_form(ctx, base)
+        line["plain_fp64_single_system"]["batched_over_plain"] = value / line["plain_fp64_single_system"]["value"]
+        line["served"] = served(ctx, F, configs, full=args.served_full)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(base)
         line["cpu_baseline"].pop("wall_s", None)
@@ -325,6 +340,47 @@ def run_ours(args) -> None:
         s.close()
     ctx.close()
     _barrier(dist)
+
+
+def plain_form(ctx, base, moves: int = 400) -> dict:
+    """The in-GPU comparison point: the plain single-system form (FP64 accumulation,
+    one trial move per call: device pair/Ewald kernels, host Metropolis)."""
+    from faunus_gb300 import _capi as A
+    import faunus_gb300 as F
+    spec = base.copy()
+    spec.precision = A.FAU_PREC_FP64
+    g = ctx.create(spec)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 5, 6, default_seeds=False).generate(moves + 20)
+    g.run_proposals(props[:20])  # warm-up
+    t0 = time.perf_counter()
+    _, _, st = g.run_proposals(props[20:])
+    wall = time.perf_counter() - t0
+    g.close()
+    return {"value": moves / wall, "unit": "moves/s", "moves": moves,
+            "form": "FP64 pair and Ewald kernels per trial move, host Metropolis, same 20,000-ion system"}
+
+
+def served(ctx, F, configs, full: bool = False) -> dict:
+    """Served MC jobs: Poisson stream of the three single-system shapes, admitted by HBM
+    footprint, continuous batching over 608 slots.  full: the configured stream (N
+    log-uniform 64..20,000, 1e4..1e6 moves); default: the same shapes bounded to
+    N <= 5,000 and <= 2e5 moves per job, so the run takes seconds, not minutes (the
+    full stream's tail is single chains of the largest water jobs)."""
+    from faunus_gb300.serve import GpuBackend, Server, jobs_from_stream
+    if full:
+        n_jobs, rate, n_max, m_max = 1000, 320.0, 20000, 1e6
+    else:
+        n_jobs, rate, n_max, m_max = 2000, 1000.0, 5000, 2e5
+    stream = configs.served_jobs(n_jobs=n_jobs, rate_hz=rate, n_max=n_max, moves_max=m_max, seed=4)
+    jobs = jobs_from_stream(stream)
+    budget = 128 << 30
+    srv = Server(GpuBackend(ctx), hbm_budget=budget, max_slots=608, block_moves=1000, round_cycles=2e8, seed=7)
+    rep = srv.run(jobs, fast_forward=False)
+    rep.update({"jobs": n_jobs, "hbm_budget_bytes": budget, "slots": 608, "round_cycles": 2e8,
+                "stream": f"served_jobs(seed 4): Poisson {rate:g} jobs/s, primitive model / bulk Ewald / SPC/E "
+                          f"water, N log-uniform 64..{n_max}, moves log-uniform 1e4..{m_max:g}"
+                          + ("" if full else " (bounded; --served-full for 20,000 / 1e6)")})
+    return rep
 
 
 def _sm_count(dev: int) -> int:
@@ -354,12 +410,15 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--replicas", type=int, default=0, help="replica chains per GPU (0: 2 x SMs)")
+    ap.add_argument("--replicas", type=int, default=0, help="replica chains per GPU (0: 4 x SMs)")
     ap.add_argument("--moves", type=int, default=10000, help="moves per replica per step")
-    ap.add_argument("--threads", type=int, default=0,
-                    help="chain CTA size: 0 = pipelined kernel (1 producer + 4 compute warps), 128/256 = chain kernel")
+    ap.add_argument("--threads", type=int, default=-1,
+                    help="kernel configuration: -1 = autotuned; 0/160, 96, 288 = pipelined kernel with 4, 2, 8 "
+                         "compute warps; 128/256 = chain kernel")
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the plain-form and served-stream measurements")
+    ap.add_argument("--served-full", action="store_true", help="served stream at the full configured job sizes")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":

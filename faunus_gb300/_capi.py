@@ -99,7 +99,8 @@ class BatchParams(C.Structure):
                 ("counter_base", C.c_uint64), ("dp", C.c_double), ("dprot", C.c_double),
                 ("swap_interval_moves", C.c_int), ("n_swap_blocks", C.c_int),
                 ("temperatures", dptr), ("threads", C.c_int), ("streams", C.POINTER(C.c_uint32)),
-                ("counters", C.POINTER(C.c_uint64))]
+                ("counters", C.POINTER(C.c_uint64)), ("dp_per_system", dptr), ("dprot_per_system", dptr),
+                ("cycles_out", C.POINTER(C.c_uint64))]
 
 
 class BatchStats(C.Structure):

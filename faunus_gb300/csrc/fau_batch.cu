@@ -27,12 +27,13 @@ extern "C" int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device
 extern "C" int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n, int* n_groups,
                                      int* molecular_only, double* t_ref, int* knc);
 extern "C" int fau_internal_fail(int code, const char* msg);
+extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 
 namespace {
 
 // per-system summary gathered after a run
 struct SysSummary {
-    unsigned long long moves, accepted, pair_evals, k_updates;
+    unsigned long long moves, accepted, pair_evals, k_updates, cycles;
     double energy, beta_scale;
     int err, pad;
 };
@@ -41,7 +42,7 @@ __global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const DevSys& S = *sys[i];
-        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.energy, S.beta_scale, S.err, 0};
+        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, S.energy, S.beta_scale, S.err, 0};
     }
 }
 
@@ -127,14 +128,15 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         mol[i] = (uint8_t)mo;
         if (pt) tref[i] = P->temperatures[i];
     }
-    // kernel choice: threads 0 or 160 -> the pipelined kernel for every system whose device proposals
-    // are single-atom moves (the others run in the 128-thread chain kernel); 128 or 256 -> the chain
-    // kernel of that size for all systems
+    // kernel choice: threads 0, 96, 160 or 288 -> the pipelined kernel (1 producer + 4, 2, 4 or 8
+    // compute warps) for every system whose device proposals are single-atom moves (the others run
+    // in the 128-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems
     const int req = P->threads;
-    if (req != 0 && req != 128 && req != 160 && req != 256)
-        return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 128, 160 or 256");
-    const int threads = (req == 0 || req == 160) ? 128 : req;
-    const bool use_fast = req == 0 || req == 160;
+    if (req != 0 && req != 96 && req != 128 && req != 160 && req != 256 && req != 288)
+        return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 96, 128, 160, 256 or 288");
+    const bool use_fast = req == 0 || req == 96 || req == 160 || req == 288;
+    const int threads = use_fast ? 128 : req;
+    const int fwarps = req == 96 ? 2 : (req == 288 ? 8 : 4);
     std::vector<uint8_t> fast(n, 0);
     for (int i = 0; i < n; i++) {
         fau_ctx* c2;
@@ -181,9 +183,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                  off_st = al(off_sum + sizeof(SysSummary) * n), off_ctr = al(off_st + 64),
                  off_ksys = al(off_ctr + 8 * n), off_knm = al(off_ksys + sizeof(DevSys*) * n),
                  off_kids = al(off_knm + 8 * n), off_kmol = al(off_kids + 4 * n), off_kctr = al(off_kmol + n),
-                 total = al(off_kctr + 8 * n);
+                 off_kdp = al(off_kctr + 8 * n), off_kdr = al(off_kdp + 8 * n), total = al(off_kdr + 8 * n);
     unsigned char* dbuf = nullptr;
-    if (cudaMalloc(&dbuf, total) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
+    if (fau_internal_ctx_scratch(ctx, total, reinterpret_cast<void**>(&dbuf)) != FAU_OK)
+        return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
     std::vector<int> slot(n);
     for (int i = 0; i < n; i++) slot[i] = i;
     int rc = FAU_OK;
@@ -196,10 +199,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         st2 = nullptr;
         fork_ev = join_ev = nullptr;
     };
-    auto cleanup = [&]() {
-        release2();
-        cudaFree(dbuf);
-    };
+    auto cleanup = [&]() { release2(); }; // dbuf is the context's scratch
 #define BTRY(x)                                                                 \
     do {                                                                        \
         if ((x) != cudaSuccess) {                                               \
@@ -231,6 +231,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     std::vector<uint32_t> kids(n);
     std::vector<uint8_t> kmol(n);
     std::vector<unsigned long long> kctr(n, 0);
+    std::vector<double> kdp(n, P->dp), kdr(n, P->dprot);
     for (int r = 0; r < n; r++) {
         const int i = order[r];
         ksys[r] = dsys[i];
@@ -238,12 +239,20 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         kids[r] = ids[i];
         kmol[r] = mol[i];
         if (P->counters) kctr[r] = P->counters[i];
+        if (P->dp_per_system) kdp[r] = P->dp_per_system[i];
+        if (P->dprot_per_system) kdr[r] = P->dprot_per_system[i];
+        if (!(kdp[r] >= 0.0) || !(kdr[r] >= 0.0)) {
+            cleanup();
+            return fau_internal_fail(FAU_ERR_ARG, "dp and dprot must be >= 0");
+        }
     }
     BTRY(cudaMemcpyAsync(dbuf + off_ksys, ksys.data(), sizeof(DevSys*) * n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_knm, knm.data(), 8 * n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kids, kids.data(), 4 * n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kmol, kmol.data(), n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kctr, kctr.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_kdp, kdp.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    BTRY(cudaMemcpyAsync(dbuf + off_kdr, kdr.data(), 8 * n, cudaMemcpyHostToDevice, st));
     ChainArgs a{};
     a.sys = reinterpret_cast<DevSys* const*>(dbuf + off_ksys);
     a.sys_ids = reinterpret_cast<const uint32_t*>(dbuf + off_kids);
@@ -251,6 +260,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     a.dp = P->dp;
     a.dprot = P->dprot;
     a.molecular = reinterpret_cast<const uint8_t*>(dbuf + off_kmol);
+    a.dp_sys = reinterpret_cast<const double*>(dbuf + off_kdp);
+    a.dprot_sys = reinterpret_cast<const double*>(dbuf + off_kdr);
     if (P->counters) a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_kctr);
     const int nblk = pt ? P->n_swap_blocks : 1;
     if (pt) {
@@ -265,11 +276,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     ae.sys = a.sys + nfast;
     ae.sys_ids = a.sys_ids + nfast;
     ae.molecular = a.molecular + nfast;
+    ae.dp_sys = a.dp_sys + nfast;
+    ae.dprot_sys = a.dprot_sys + nfast;
     if (a.counters) ae.counters = a.counters + nfast;
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact) BTRY(prepare_chain(Ke, nce, threads, true));
-    if (nfast) BTRY(prepare_fast(Kf, ncf, 4, true));
+    if (nfast) BTRY(prepare_fast(Kf, ncf, fwarps, true));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
         BTRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -285,10 +298,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             if ((e = cudaStreamWaitEvent(st2, fork_ev, 0)) != cudaSuccess) return e;
             if ((e = launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess) return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
-            if ((e = launch_fast(a, nfast, Kf, ncf, 4, true, st)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, fwarps, true, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
-        if (nfast) return launch_fast(a, nfast, Kf, ncf, 4, true, st);
+        if (nfast) return launch_fast(a, nfast, Kf, ncf, fwarps, true, st);
         return launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };
 
@@ -382,6 +395,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         S.k_updates += (int64_t)(s1[i].k_updates - s0[i].k_updates);
         if (s1[i].err != FAU_OK && derr == FAU_OK) derr = s1[i].err;
     }
+    if (P->cycles_out)
+        for (int i = 0; i < n; i++) P->cycles_out[i] = (uint64_t)(s1[i].cycles - s0[i].cycles);
     S.swaps_attempted = (int64_t)pst[0];
     S.swaps_accepted = (int64_t)pst[1];
     S.device_ms = ms;
@@ -469,9 +484,9 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                  o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * total),
                  o_du = al(o_acc + total), bytes = al(o_du + 8 * total);
     unsigned char* dbuf = nullptr;
-    if (cudaMalloc(&dbuf, bytes) != cudaSuccess) return fau_internal_fail(FAU_ERR_OOM, "batch staging allocation");
-    auto done = [&](int code, const char* msg) {
-        cudaFree(dbuf);
+    if (fau_internal_ctx_scratch(ctx, bytes, reinterpret_cast<void**>(&dbuf)) != FAU_OK)
+        return fau_internal_fail(FAU_ERR_OOM, "batch staging allocation");
+    auto done = [&](int code, const char* msg) { // dbuf is the context's scratch
         return code == FAU_OK ? FAU_OK : fau_internal_fail(code, msg);
     };
     DevSys* const* d_sys = reinterpret_cast<DevSys* const*>(dbuf + o_sys);

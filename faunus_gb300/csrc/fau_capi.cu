@@ -52,7 +52,23 @@ struct fau_ctx {
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
     std::mutex mu;
+    // caching device allocator: the blocks of destroyed systems, by size, reused by later
+    // systems of this context (no cudaMalloc / cudaFree -- which synchronises the device --
+    // per served job); returned to the driver when the context is destroyed
+    std::multimap<size_t, void*> pool;
+    size_t pool_bytes = 0;
 };
+
+// size class of a device block: multiples of 256 B up to 4 KiB, then 1/8 steps of the
+// next power of two (at most 12.5 % slack)
+static size_t block_class(size_t b)
+{
+    if (b <= 4096) return (b + 255) & ~size_t(255);
+    size_t p = 4096;
+    while (p < b) p <<= 1;
+    const size_t step = p >> 3;
+    return (b + step - 1) / step * step;
+}
 
 struct fau_sys {
     fau_ctx* ctx = nullptr;
@@ -84,11 +100,19 @@ struct fau_sys {
 template <class T>
 static int dev_alloc(fau_sys* s, T** p, size_t count)
 {
-    const size_t b = std::max<size_t>(count, 1) * sizeof(T);
+    const size_t b = block_class(std::max<size_t>(count, 1) * sizeof(T));
     if (s->ctx->budget && s->ctx->used + b > s->ctx->budget)
         return fail(FAU_ERR_OOM, "HBM budget exceeded (%zu + %zu > %zu bytes)", s->ctx->used, b, s->ctx->budget);
     void* v = nullptr;
-    CUDA_TRY(cudaMalloc(&v, b));
+    auto it = s->ctx->pool.find(b);
+    if (it != s->ctx->pool.end()) { // a block of this class left by a destroyed system
+        v = it->second;
+        s->ctx->pool.erase(it);
+        s->ctx->pool_bytes -= b;
+    }
+    else {
+        CUDA_TRY(cudaMalloc(&v, b));
+    }
     s->allocs.push_back(v);
     s->alloc_bytes.push_back(b);
     s->bytes += b;
@@ -107,7 +131,11 @@ static int upload(fau_sys* s, T** p, const T* src, size_t count)
 
 static void free_sys(fau_sys* s)
 {
-    for (void* p : s->allocs) cudaFree(p);
+    // blocks go back to the context's pool (the caller has synchronised the stream)
+    for (size_t a = 0; a < s->allocs.size(); a++) {
+        s->ctx->pool.emplace(s->alloc_bytes[a], s->allocs[a]);
+        s->ctx->pool_bytes += s->alloc_bytes[a];
+    }
     if (s->ctx) s->ctx->used -= std::min(s->ctx->used, s->bytes);
     s->allocs.clear();
     s->alloc_bytes.clear();
@@ -341,6 +369,8 @@ int fau_ctx_destroy(fau_ctx* c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->scratch) cudaFree(c->scratch);
+    for (auto& kv : c->pool) cudaFree(kv.second);
+    c->pool.clear();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1190,6 +1220,25 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
     return FAU_OK;
 }
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+// a context-owned device scratch buffer of at least `bytes` (grown on demand; valid until the
+// next call on this context -- batched calls synchronise their stream before returning)
+int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out)
+{
+    if (bytes > c->scratch_bytes) {
+        if (c->scratch) {
+            cudaStreamSynchronize(c->stream);
+            cudaFree(c->scratch);
+            c->scratch = nullptr;
+            c->scratch_bytes = 0;
+        }
+        const size_t b = block_class(bytes);
+        CUDA_TRY(cudaMalloc(&c->scratch, b));
+        c->scratch_bytes = b;
+    }
+    *out = c->scratch;
+    return FAU_OK;
+}
 
 int fau_energy_change(fau_sys* s, const fau_proposal* p, fau_trial_result* out)
 {

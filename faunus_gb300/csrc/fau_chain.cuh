@@ -416,6 +416,7 @@ template <int NT, bool PHILOX>
 __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 {
     constexpr int NW = NT / 32;
+    const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // the system descriptor in shared memory: its fields sit on every move's dependent
     // chain, and global copies fall out of L1 under the cell-list traffic
@@ -473,6 +474,8 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
     const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
     const bool molecular_sys = A.molecular ? (A.molecular[blockIdx.x] != 0) : false;
+    const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
+    const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
     const bool detail = A.detail != nullptr;
     const int nt = S.nt;
 
@@ -500,7 +503,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
-        const Proposal p = PHILOX ? philox_proposal(S, ctr0, sys_id, A.seed, (float)A.dp, A.dprot, molecular_sys)
+        const Proposal p = PHILOX ? philox_proposal(S, ctr0, sys_id, A.seed, dp_f, dprot, molecular_sys)
                                   : load_proposal(A.props[poff]);
         prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
     }
@@ -890,7 +893,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 else if (mv + 1 < nmoves) {
                     // ---- prepare the next move
                     const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed,
-                                                                (float)A.dp, A.dprot, molecular_sys)
+                                                                dp_f, dprot, molecular_sys)
                                               : load_proposal(A.props[poff + mv + 1]);
                     prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
                     if (lane == 0) {
@@ -959,6 +962,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
         if (ms.stop) G.err = ms.stop;
         G.consumed = ms.stop ? ms.consumed : nmoves;
+        G.cycles += (unsigned long long)(clock64() - t_start);
     }
 }
 

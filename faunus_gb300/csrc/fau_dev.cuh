@@ -105,6 +105,7 @@ struct DevSys {
     unsigned long long moves, accepted, pair_evals, k_updates;
     double sum_du;
     long long consumed; // proposals performed by the last chain launch
+    unsigned long long cycles; // SM clock cycles spent in chain launches (summed)
 };
 
 // ---------------------------------------------------------------- fixed point

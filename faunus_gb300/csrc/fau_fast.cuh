@@ -366,9 +366,10 @@ __device__ __forceinline__ bool fast_decide(FF s, int flags, double du_surf, boo
 }
 
 template <int NWC, bool PHILOX>
-__global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs A)
+__global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
 {
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
+    const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // the system descriptor in shared memory: its fields sit on every move's dependent
     // chain, and global copies fall out of L1 under the cell-list traffic
@@ -437,7 +438,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         ps.poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
         ps.sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
         ps.ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
-        ps.dp_f = (float)A.dp;
+        ps.dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
         ps.energy = S.energy;
         ps.sum_du = 0.0;
         ps.e_acc = FF{0.f, 0.f};
@@ -866,6 +867,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), 4) fast_chain_kernel(ChainArgs
         for (int d = 0; d < 3; d++) G.M[d] = ps.M[d];
         if (stop) G.err = stop;
         G.consumed = stop == FAU_ERR_CAPACITY ? t + 1 : t;
+        G.cycles += (unsigned long long)(clock64() - t_start);
     }
 }
 

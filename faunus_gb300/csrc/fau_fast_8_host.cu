@@ -1,0 +1,11 @@
+// fau_fast_8_host.cu -- pipelined chain kernel instantiation: 1 producer + 8 compute warps, host proposals.
+#include "fau_fast.cuh"
+
+namespace fau {
+
+cudaError_t fast_dispatch_8_host(const ChainArgs& a, int nb, int K, int nc, cudaStream_t st, bool prep)
+{
+    return launch_fast_inst<8, false>(a, nb, K, nc, st, prep);
+}
+
+} // namespace fau

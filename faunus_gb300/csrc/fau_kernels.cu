@@ -318,6 +318,12 @@ size_t fast_smem_bytes_total(int K, int nc)
 static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox,
                                     cudaStream_t st, bool prepare_only)
 {
+    if (warps == 2)
+        return philox ? fast_dispatch_2_ph(a, nblocks, K, nc, st, prepare_only)
+                      : fast_dispatch_2_host(a, nblocks, K, nc, st, prepare_only);
+    if (warps == 8)
+        return philox ? fast_dispatch_8_ph(a, nblocks, K, nc, st, prepare_only)
+                      : fast_dispatch_8_host(a, nblocks, K, nc, st, prepare_only);
     if (warps != 4) return cudaErrorInvalidValue;
     return philox ? fast_dispatch_4_ph(a, nblocks, K, nc, st, prepare_only)
                   : fast_dispatch_4_host(a, nblocks, K, nc, st, prepare_only);

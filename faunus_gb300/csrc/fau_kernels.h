@@ -25,6 +25,8 @@ struct ChainArgs {
     unsigned long long counter_base;
     const unsigned long long* counters; // per CTA first counter (NULL: counter_base)
     double dp, dprot;
+    const double* dp_sys;        // per CTA dp / dprot (NULL: dp, dprot)
+    const double* dprot_sys;
     const uint8_t* molecular;    // per CTA: 1 -> moltransrot moves, 0 -> transrot
     // evaluate-only mode (one move, one CTA): no Metropolis, no commit; the trial is
     // written to `pending` and its Q(k) change to `pending_dq` for a later commit
@@ -65,8 +67,12 @@ constexpr int kFastMaxNc = 40;
 size_t fast_smem_bytes_total(int K, int nc);
 cudaError_t prepare_fast(int K, int nc, int warps, bool philox);
 cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox, cudaStream_t st);
+cudaError_t fast_dispatch_2_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_2_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_4_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_4_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_8_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,

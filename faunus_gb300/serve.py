@@ -8,9 +8,14 @@ molecular translate/rotate moves.  The server
     fits in the HBM budget beside the jobs already resident; a job that can
     never fit is rejected at once;
   * keeps every admitted job's state resident on the device between launches;
-  * advances all resident jobs together, ``block_moves`` moves per round, in
-    one ``fau_run_batch`` call per (dp, dprot) group -- jobs join and leave
+  * advances all resident jobs together in one ``fau_run_batch`` launch per
+    round (per-system dp and dprot; single-atom jobs in the pipelined kernel,
+    molecular ones beside them in the chain kernel) -- jobs join and leave
     between rounds, so work that arrives while others run overlaps with them;
+  * sizes each job's share of a round to a common time budget: a job's first
+    round is a ``block_moves`` calibration, after which its measured SM cycles
+    per move set how many moves fit in ``round_cycles`` (a slow chain does not
+    hold fast ones back, and a fast one does not idle while a slow one runs);
   * retires a job when its moves are done and reports, per job, the queueing
     and run time, and for the stream, p50/p99 latency (arrival -> result) and
     the aggregate moves/s.
@@ -67,6 +72,7 @@ class _Active:
     bytes: int
     done: int = 0
     admitted_s: float = 0.0
+    cycles_per_move: float = 0.0  # measured; 0 until the first round
 
 
 class GpuBackend:
@@ -83,12 +89,15 @@ class GpuBackend:
         return self.ctx.create(spec)
 
     def run(self, handles, moves: Sequence[int], *, seed: int, streams: Sequence[int], counters: Sequence[int],
-            dp: float, dprot: float) -> None:
-        """Advance each system by its move count in one launch (CUDA graph)."""
+            dp: Sequence[float], dprot: Sequence[float]) -> np.ndarray:
+        """Advance each system by its move count in one launch (CUDA graph); returns the SM
+        cycles each system's chain took."""
+        cycles = np.zeros(len(handles), dtype=np.uint64)
         self.ctx.run_batch(handles, moves_per_system=np.asarray(moves, dtype=np.int64), seed=seed,
                            streams=np.asarray(streams, dtype=np.uint32),
-                           counters=np.asarray(counters, dtype=np.uint64), dp=dp, dprot=dprot,
-                           threads=self.threads)
+                           counters=np.asarray(counters, dtype=np.uint64), dp_per_system=dp,
+                           dprot_per_system=dprot, threads=self.threads, cycles_out=cycles)
+        return cycles
 
     def result(self, handle, with_positions: bool) -> dict:
         c = handle.counters()
@@ -101,13 +110,16 @@ class GpuBackend:
 
 class Server:
     def __init__(self, backend, hbm_budget: int, max_slots: int = 608, block_moves: int = 2000, seed: int = 1,
-                 keep_positions: bool = False, clock: Callable[[], float] = time.perf_counter):
+                 keep_positions: bool = False, clock: Callable[[], float] = time.perf_counter,
+                 round_cycles: float = 2e8, min_block: int = 100):
         if hbm_budget <= 0:
             raise ValueError("hbm_budget must be positive")
         self.backend = backend
         self.budget = int(hbm_budget)
         self.max_slots = int(max_slots)
         self.block = int(block_moves)
+        self.round_cycles = float(round_cycles)
+        self.min_block = int(min_block)
         self.seed = int(seed)
         self.keep_positions = keep_positions
         self.clock = clock
@@ -117,6 +129,7 @@ class Server:
         self.moves_done = 0
         self.rounds = 0
         self.resident = 0  # footprint of the admitted jobs (the budget covers only these)
+        self.need: Dict[int, int] = {}
         self.t0 = None
 
     # ---------------------------------------------------------------- time
@@ -131,6 +144,7 @@ class Server:
             raise ValueError(f"job id {job.id} already used")
         if job.moves < 0:
             raise ValueError("negative move count")
+        self.need[job.id] = int(self.backend.footprint(job.spec))  # once per job, not per admission attempt
         self.queue.append(job)
 
     def _admit(self) -> None:
@@ -140,7 +154,7 @@ class Server:
             if job.arrival_s > now:
                 keep.append(job)
                 continue
-            need = self.backend.footprint(job.spec)
+            need = self.need[job.id]
             if need > self.budget:
                 self.results[job.id] = JobResult(job.id, f"rejected: footprint {need} B exceeds the HBM budget "
                                                          f"{self.budget} B", arrival_s=job.arrival_s,
@@ -170,22 +184,28 @@ class Server:
         self._retire()  # zero-move jobs
         if not self.active:
             return 0
-        groups: Dict[tuple, List[_Active]] = {}
-        for a in self.active.values():
-            groups.setdefault((a.job.dp, a.job.dprot), []).append(a)
+        members = list(self.active.values())
+        moves = [min(self._share(a), a.job.moves - a.done) for a in members]
+        cycles = self.backend.run([a.handle for a in members], moves, seed=self.seed,
+                                  streams=[a.job.id for a in members], counters=[a.done for a in members],
+                                  dp=[a.job.dp for a in members], dprot=[a.job.dprot for a in members])
         total = 0
-        for (dp, dprot), members in groups.items():
-            moves = [min(self.block, a.job.moves - a.done) for a in members]
-            self.backend.run([a.handle for a in members], moves, seed=self.seed,
-                             streams=[a.job.id for a in members], counters=[a.done for a in members],
-                             dp=dp, dprot=dprot)
-            for a, m in zip(members, moves):
-                a.done += m
-                total += m
+        for i, (a, m) in enumerate(zip(members, moves)):
+            a.done += m
+            total += m
+            if cycles is not None and m > 0 and cycles[i] > 0:
+                c = float(cycles[i]) / m
+                a.cycles_per_move = c if a.cycles_per_move == 0.0 else 0.5 * (a.cycles_per_move + c)
         self.moves_done += total
         self.rounds += 1
         self._retire()
         return total
+
+    def _share(self, a: _Active) -> int:
+        """Moves of job `a` that fit in this round's cycle budget."""
+        if a.cycles_per_move <= 0.0:
+            return self.block
+        return max(self.min_block, int(self.round_cycles / a.cycles_per_move))
 
     def idle(self) -> bool:
         return not self.active and not self.queue

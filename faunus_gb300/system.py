@@ -161,7 +161,9 @@ class Context:
     def run_batch(self, systems: Sequence["System"], moves=None, *, moves_per_system=None, seed: int = 1,
                   counter_base: int = 0, dp: float = 1.0, dprot: float = 0.0, swap_interval: int = 0,
                   n_swap_blocks: int = 0, temperatures=None, threads: int = 0, streams=None,
-                  counters=None) -> dict:
+                  counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None) -> dict:
+        """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
+        is a uint64 array of len(systems) that receives each system's SM cycles."""
         n = len(systems)
         arr = (C.c_void_p * n)(*[s.handle for s in systems])
         p = A.BatchParams()
@@ -186,6 +188,15 @@ class Context:
             sv = np.ascontiguousarray(streams, dtype=np.uint32)
             keep.append(sv)
             p.streams = sv.ctypes.data_as(C.POINTER(C.c_uint32))
+        for name, arr_ in (("dp_per_system", dp_per_system), ("dprot_per_system", dprot_per_system)):
+            if arr_ is not None:
+                v = np.ascontiguousarray(arr_, dtype=np.float64)
+                keep.append(v)
+                setattr(p, name, A.as_dptr(v))
+        if cycles_out is not None:
+            if cycles_out.dtype != np.uint64 or not cycles_out.flags.c_contiguous or len(cycles_out) != n:
+                raise ValueError("cycles_out must be a contiguous uint64 array with one entry per system")
+            p.cycles_out = cycles_out.ctypes.data_as(C.POINTER(C.c_uint64))
         if counters is not None:
             cv = np.ascontiguousarray(counters, dtype=np.uint64)
             keep.append(cv)

@@ -187,6 +187,10 @@ typedef struct fau_batch_params {
     const uint64_t* counters; /* optional per-system first move counter (default:
                                  counter_base); a system's moves depend only on its
                                  (seed, stream, counter), not on the rest of the batch   */
+    const double* dp_per_system;    /* optional per-system dp (overrides dp)             */
+    const double* dprot_per_system; /* optional per-system dprot (overrides dprot)       */
+    uint64_t* cycles_out;     /* optional, n entries: SM clock cycles each system's chain
+                                 took in this call (summed over swap blocks)             */
 } fau_batch_params;
 
 typedef struct fau_batch_stats {

@@ -1,6 +1,6 @@
 """GPU parity of the pipelined chain kernel (batched single-atom moves).
 
-fau_run_batch (threads 0 or 160) and fau_run_proposals_batch run every system
+fau_run_batch (threads 0, 96, 160 or 288) and fau_run_proposals_batch run every system
 whose proposals are single-atom translations in the pipelined kernel.  It must
 reproduce:
   * the chain kernel (threads=128) under the same device proposals: the same
@@ -44,14 +44,15 @@ def _energy_consistent(s):
     assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot)), (e_run, e_tot)
 
 
-@pytest.mark.parametrize("case", sorted(CASES))
-def test_pipelined_equals_chain_kernel(ctx, case):
+@pytest.mark.parametrize("case,threads", [(c, 160) for c in sorted(CASES)] +
+                         [(c, t) for c in ("primitive_model", "bulk_cells", "bulk_small_box") for t in (96, 288)])
+def test_pipelined_equals_chain_kernel(ctx, case, threads):
     spec = CASES[case]()
     a, b = ctx.create(spec), ctx.create(spec)
     if case == "bulk_3x3x3_cells":
         assert a.cell_grid() == (3, 3, 3)
     moves = 3000
-    sa = ctx.run_batch([a], moves, seed=21, streams=[5], dp=2.0, threads=0)
+    sa = ctx.run_batch([a], moves, seed=21, streams=[5], dp=2.0, threads=threads)
     sb = ctx.run_batch([b], moves, seed=21, streams=[5], dp=2.0, threads=128)
     assert sa["moves"] == sb["moves"] == moves
     assert sa["accepted"] == sb["accepted"] and sa["accepted"] > 100

@@ -36,6 +36,7 @@ class FakeBackend:
         self.spm = seconds_per_move
         self.live = []
         self.launches = []
+        self.moves_per_launch = []
 
     def footprint(self, spec):
         return spec["bytes"]
@@ -47,11 +48,14 @@ class FakeBackend:
 
     def run(self, handles, moves, *, seed, streams, counters, dp, dprot):
         self.launches.append(sorted(streams))
+        self.moves_per_launch.append(dict(zip(streams, moves)))
         for h, m, st, c in zip(handles, moves, streams, counters):
             for k in range(c, c + m):
                 h.state = (h.state * 6364136223846793005 + (seed ^ (st << 20) ^ k)) & (2**64 - 1)
             h.moves += m
-        self.clock.t += self.spm * max(moves)  # the launch lasts as long as its longest chain
+        cyc = [m * h.spec.get("cpm", 1000) for h, m in zip(handles, moves)]
+        self.clock.t += self.spm * max(c / 1000 for c in cyc)  # the launch lasts as long as its slowest chain
+        return np.array(cyc, dtype=np.uint64)
 
     def result(self, h, with_positions):
         return {"energy": float(h.state % 1000003), "accepted": h.moves // 2, "moves": h.moves,
@@ -99,7 +103,7 @@ def test_admission_waits_for_memory_and_slots():
 
 
 def test_continuous_batching_jobs_join_between_rounds():
-    srv, be, clock = _server(budget=1000, slots=8, block=1000)
+    srv, be, clock = _server(budget=1000, slots=8, block=1000, round_cycles=1e6)
     # one second per launched move would be too slow: 1 ms per 1000-move round
     be.spm = 1e-6
     jobs = [Job(spec={"bytes": 1}, moves=10000, id=0, arrival_s=0.0),
@@ -138,3 +142,15 @@ def test_duplicate_ids_and_bad_budget_are_rejected():
         srv.submit(Job(spec={"bytes": 1}, moves=1, id=7))
     with pytest.raises(ValueError):
         Server(FakeBackend(FakeClock()), hbm_budget=0)
+
+
+def test_round_shares_follow_measured_cycles_per_move():
+    """A slow job (4x the cycles per move) gets a quarter of a fast job's moves per round
+    after its calibration round, so neither waits on the other."""
+    srv, be, _ = _server(budget=100, slots=4, block=500, round_cycles=4e6, min_block=10)
+    srv.run([Job(spec={"bytes": 1, "cpm": 1000}, moves=40000, id=0),
+             Job(spec={"bytes": 1, "cpm": 4000}, moves=10000, id=1)])
+    first, second = be.moves_per_launch[0], be.moves_per_launch[1]
+    assert first == {0: 500, 1: 500}          # calibration
+    assert second == {0: 4000, 1: 1000}       # 4e6 cycles each
+    assert srv.results[0].moves == 40000 and srv.results[1].moves == 10000
