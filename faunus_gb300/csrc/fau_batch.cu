@@ -130,12 +130,12 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     }
     // kernel choice: threads 0, 96, 160 or 288 -> the pipelined kernel (1 producer + 4, 2, 4 or 8
     // compute warps) for every system whose device proposals are single-atom moves (the others run
-    // in the 128-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems
+    // in the 256-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems
     const int req = P->threads;
     if (req != 0 && req != 96 && req != 128 && req != 160 && req != 256 && req != 288)
         return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 96, 128, 160, 256 or 288");
     const bool use_fast = req == 0 || req == 96 || req == 160 || req == 288;
-    const int threads = use_fast ? 128 : req;
+    const int threads = use_fast ? 256 : req; // molecular moves: 256-thread chain CTAs measured fastest
     const int fwarps = req == 96 ? 2 : (req == 288 ? 8 : 4);
     std::vector<uint8_t> fast(n, 0);
     for (int i = 0; i < n; i++) {

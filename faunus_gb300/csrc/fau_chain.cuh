@@ -29,6 +29,8 @@
 namespace fau {
 
 constexpr int kTableAtoms = 8; // moved atoms handled with phase tables (larger groups: direct sincospi)
+constexpr int kNblChunk = 512;  // candidate groups per GroupCutoff pass of a molecular move (multiple of NT)
+constexpr uint32_t kNblNew = 1u << 30, kNblOld = 1u << 31, kNblGroup = kNblNew - 1u;
 
 struct MoveShared {
     int kind, index, m, first;
@@ -76,6 +78,15 @@ __device__ __forceinline__ int cell_index(const DevSys& S, const int* c)
 
 // GroupCutoff::cut (src/energy.h:761-768): sqdist(cm1, cm2) >= cutoff^2, FP32 on
 // fixed-point mass centres, FP64 inside a 1e-5 guard band.
+__device__ __forceinline__ bool group_cut_rec(const DevSys& S, uint4 cmrec, const double* cm, uint4 cmrec_h, int h)
+{
+    if (S.cut_g2g2 < 0.0) return false;
+    const float r2 = r2_fixed(S, cmrec, cmrec_h);
+    if (r2 < S.cut_g2g2f * 0.99999f) return false;
+    if (r2 > S.cut_g2g2f * 1.00001f) return true;
+    const double o[3] = {S.g_cm[3 * h], S.g_cm[3 * h + 1], S.g_cm[3 * h + 2]};
+    return sqdist_d(S, cm, o) >= S.cut_g2g2;
+}
 __device__ __forceinline__ bool group_cut(const DevSys& S, uint4 cmrec, const double* cm, int h)
 {
     if (S.cut_g2g2 < 0.0) return false;
@@ -148,18 +159,26 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
         p.kind = FAU_MOVE_MOLECULAR;
         p.index = (int)__umulhi(c1.x, (uint32_t)S.n_groups);
         if (dprot > 0.0) {
+            // uniform axis, angle dprot (U - 1/2); the half-angle sine/cosine and the axis come
+            // from the FP32 pipe (FP64 sin/cos is ~100 instructions on a slow pipe) and the
+            // quaternion is normalised in FP64, so rotations stay unit to FP64 precision
             const float az = fmaf(2.f, u01_24(c2.z), -1.f);
             float as, ac;
             sincospif(2.f * u01_24(c2.w), &as, &ac);
             const float axy = sqrtf(fmaxf(0.f, 1.f - az * az));
             const U4 c3 = philox({(uint32_t)ctr, (uint32_t)(ctr >> 32), sys_id, 2u}, k0, k1);
-            const double angle = dprot * ((double)u01_24(c3.x) - 0.5);
-            const double ha = 0.5 * angle;
-            const double sh = sin(ha);
-            p.quat[0] = cos(ha);
-            p.quat[1] = sh * (double)(axy * ac);
-            p.quat[2] = sh * (double)(axy * as);
-            p.quat[3] = sh * (double)az;
+            const float ha_pi = (float)dprot * (u01_24(c3.x) - 0.5f) * (0.5f / 3.14159265358979f); // angle / (2 pi)
+            float sh, ch;
+            sincospif(ha_pi, &sh, &ch);
+            const double ax = f2d_bits(axy * ac), ay = f2d_bits(axy * as), az_d = f2d_bits(az);
+            const double ra = rsqrt(__dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az_d, az_d)));
+            const double c = f2d_bits(ch), s = f2d_bits(sh) * ra;
+            const double q0 = c, q1 = s * ax, q2 = s * ay, q3 = s * az_d;
+            const double rq = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+            p.quat[0] = q0 * rq;
+            p.quat[1] = q1 * rq;
+            p.quat[2] = q2 * rq;
+            p.quat[3] = q3 * rq;
             p.rotate = true;
         }
     }
@@ -443,6 +462,8 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     __shared__ float red_s[NW];
     __shared__ int red_f[NW];
     __shared__ int nbo[27][3];
+    __shared__ uint32_t nbl[kNblChunk]; // molecular moves: neighbour groups of one chunk | interacting states
+    __shared__ int nbl_cnt[2];
 
     const float rec_pref_f = (float)S.rec_pref;
     for (int k = tid; k < K; k += NT) {
@@ -500,6 +521,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     if (tid == 0) {
         ms.prev_accept = 0;
         ms.consumed = 0;
+        nbl_cnt[0] = nbl_cnt[1] = 0;
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -675,32 +697,69 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 const int g = ms.index;
                 const uint4 cmo = ms.cmrec_old, cmn = ms.cmrec_new;
                 const double cmo_d[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
-                for (int h = tid; h < S.n_groups; h += NT) {
-                    if (h == g || (S.g_flags[h] & FAU_GROUP_ATOMIC)) continue;
-                    const bool cut_o = group_cut(S, cmo, cmo_d, h);
-                    const bool cut_n = group_cut(S, cmn, ms.cm_new, h);
-                    if (cut_o && cut_n) continue;
-                    const int hb = S.g_begin[h], he = S.g_begin[h + 1];
-                    for (int b = hb; b < he; b++) {
-                        const uint4 rb = S.rec[b];
-                        const int tb = rb.w >> 24;
-                        for (int a = 0; a < m; a++) {
-                            const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                // In chunks of kNblChunk candidate groups: (1) the GroupCutoff tests, survivors
+                // compacted into `nbl` with the states they interact in; (2) one (neighbour
+                // group, moved atom) task per thread over the list -- every thread does
+                // useful pair work instead of a few lanes running whole groups serially.
+                const int G = S.n_groups;
+                int chunk = 0;
+                for (int base = 0; base < G; base += kNblChunk, chunk++) {
+                    int* cntp = &nbl_cnt[chunk & 1];
+                    constexpr int RC = kNblChunk / NT;
+                    int gfl[RC];
+                    uint4 gcr[RC];
+#pragma unroll
+                    for (int r = 0; r < RC; r++) { // all loads first: their latencies overlap
+                        const int h = base + r * NT + tid;
+                        gfl[r] = h < G ? S.g_flags[h] : FAU_GROUP_ATOMIC;
+                        gcr[r] = h < G ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                    }
+#pragma unroll
+                    for (int r = 0; r < RC; r++) {
+                        const int h = base + r * NT + tid;
+                        uint32_t e = 0;
+                        if (h < G && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
+                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h);
+                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h);
+                            e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
+                        int wpos = 0;
+                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
+                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
+                        if (e) nbl[wpos + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)h | e;
+                    }
+                    __syncthreads();
+                    const int cnt = *cntp;
+                    if (tid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
+                    for (int task = tid; task < cnt * m; task += NT) {
+                        const int q = task / m, a = task - q * m;
+                        const uint32_t ent = nbl[q];
+                        const int h = (int)(ent & kNblGroup);
+                        const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
+                        const int hb = S.g_begin[h], he = S.g_begin[h + 1];
+                        const uint4 ra_n = ms.rec_new[a], ra_o = ms.rec_old[a];
+                        const int ta = ra_n.w >> 24;
+                        for (int b = hb; b < he; b++) {
+                            const uint4 rb = S.rec[b];
+                            const int pidx = ta * nt + (int)(rb.w >> 24);
                             const PairF p = pt[pidx];
                             float uu[2] = {0.f, 0.f};
                             bool fi[2] = {false, false}, fn[2] = {false, false};
                             float mg = 0.f;
                             for (int st = 0; st < 2; st++) {
-                                if (st ? cut_o : cut_n) continue;
-                                uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ms.rec_old[a] : ms.rec_new[a], rb),
-                                                  st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
+                                if (!(st ? do_o : do_n)) continue;
+                                uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ra_o : ra_n, rb), st ? ms.xo[a] : ms.xn[a],
+                                                  b, fi[st], fn[st], mg);
                                 n_pairs++;
                             }
                             add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
                             if (detail) scale += mg;
                         }
                     }
+                    __syncthreads();
                 }
+                if (tid == 0) nbl_cnt[0] = nbl_cnt[1] = 0;
                 for (int t = tid; t < S.n_atomic; t += NT) { // atomic groups are never cut
                     const int b = S.atomic_idx[t];
                     const uint4 rb = S.rec[b];
