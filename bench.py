@@ -9,8 +9,9 @@ advanced by M trial moves in one persistent chain-kernel launch.
   value   device-timed moves/s with all state resident in HBM, proposals
           from the on-device counter RNG (fau_run_batch).
   e2e     the same moves through the drop-in C ABI (fau_run_proposals_batch):
-          proposals drawn on the host in the reference's mt19937 order, copied
-          host->device from pinned memory, accept flags + dU copied back, all
+          proposals drawn on the host in the reference's mt19937 order, in
+          pinned host memory that the kernel reads in place (72 B per move cross
+          host->device while the chains run), accept flags + dU copied back, all
           inside the timed region.
   --impl reference
           the CPU oracle (the reference algorithm restated: all-pairs
@@ -331,6 +332,7 @@ def run_ours(args) -> None:
         line["plain_fp64_single_system"] = plain_form(ctx, base)
         line["plain_fp64_single_system"]["batched_over_plain"] = value / line["plain_fp64_single_system"]["value"]
         line["served"] = served(ctx, F, configs, full=args.served_full)
+        line["other_configs"] = other_configs(ctx, configs, R)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(base)
         line["cpu_baseline"].pop("wall_s", None)
@@ -358,6 +360,42 @@ def plain_form(ctx, base, moves: int = 400) -> dict:
     g.close()
     return {"value": moves / wall, "unit": "moves/s", "moves": moves,
             "form": "FP64 pair and Ewald kernels per trial move, host Metropolis, same 20,000-ion system"}
+
+
+def other_configs(ctx, configs, replicas: int) -> dict:
+    """Device-timed throughput of the other configurations (seconds each): the primitive
+    model (200 hard-sphere ions) and rigid SPC/E water (1,000 molecules, molecular moves)
+    as replica batches, and the 256-walker parallel-tempering ladder (N 100..5,000)."""
+    out = {}
+
+    def batch_rate(spec, R, M, **kw):
+        base = ctx.create(spec)
+        systems = [base] + [base.clone() for _ in range(R - 1)]
+        mv = spec.extra["moves"][0]
+        kw.setdefault("dp", mv.get("dp", 2.0))
+        kw.setdefault("dprot", mv.get("dprot", 0.0))
+        ctx.run_batch(systems, max(1, M // 5), seed=1, **kw)
+        st = ctx.run_batch(systems, M, seed=1, counter_base=M, **kw)
+        for s_ in systems:
+            s_.close()
+        return st["moves"] / (st["device_ms"] * 1e-3), st["pair_evals"] / (st["device_ms"] * 1e-3)
+
+    mps, pps = batch_rate(configs.primitive_model(n=200), replicas, 20000)
+    out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps}
+    mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 500)
+    out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
+                              "kernel": "chain kernel (molecular moves), 256 threads"}
+    specs, temps = configs.pt_replicas(n_rep=256)
+    systems = [ctx.create(s_) for s_ in specs]
+    st = ctx.run_batch(systems, swap_interval=2000, n_swap_blocks=5, temperatures=temps, seed=3, dp=2.0)
+    for s_ in systems:
+        s_.close()
+    out["parallel_tempering_256"] = {"moves_per_s": st["moves"] / (st["device_ms"] * 1e-3),
+                                     "swaps_attempted": st["swaps_attempted"], "swaps_accepted": st["swaps_accepted"],
+                                     "swap_interval_moves": 2000,
+                                     "note": "one graph: 5 blocks of 2,000 moves per walker + device swap kernel; "
+                                             "each block lasts as long as its largest walker (N up to 5,000)"}
+    return out
 
 
 def served(ctx, F, configs, full: bool = False) -> dict:

@@ -28,6 +28,7 @@ extern "C" int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int*
                                      int* molecular_only, double* t_ref, int* knc);
 extern "C" int fau_internal_fail(int code, const char* msg);
 extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
+extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 
 namespace {
 
@@ -425,7 +426,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     std::vector<DevSys*> dsys(n);
     std::vector<long long> nm(n), off(n);
     std::vector<int> Kv(n), ncv(n);
-    std::vector<uint8_t> has_mol(n, 0);
+    std::vector<uint8_t> fast(n, 0);
     const long long total = offsets[n];
     if (offsets[0] != 0 || total < 0) return fau_internal_fail(FAU_ERR_ARG, "offsets must start at 0");
     for (int i = 0; i < n; i++) {
@@ -439,29 +440,18 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         off[i] = offsets[i];
         Kv[i] = K;
         ncv[i] = knc;
-        for (long long m = offsets[i]; m < offsets[i + 1]; m++) {
-            const fau_proposal& p = props[m];
-            if (p.kind == FAU_MOVE_ATOMIC) {
-                if (p.index < 0 || p.index >= np) return fau_internal_fail(FAU_ERR_ARG, "particle out of range");
-            }
-            else if (p.kind == FAU_MOVE_MOLECULAR) {
-                if (p.index < 0 || p.index >= ng) return fau_internal_fail(FAU_ERR_ARG, "group out of range");
-                has_mol[i] = 1;
-            }
-            else if (p.kind != FAU_MOVE_NONE) {
-                return fau_internal_fail(FAU_ERR_ARG, "unknown proposal kind");
-            }
-        }
+        // systems of atomic groups only run in the pipelined kernel (single-atom moves), the others
+        // in the 256-thread chain kernel; the kernels check every proposal as they read it
+        fast[i] = fau_internal_sys_all_atomic(systems[i]) && knc <= kFastMaxNc;
     }
-    // systems with only single-atom (or empty) proposals run in the pipelined kernel, the rest in the
-    // 128-thread chain kernel; kernel order puts the former first
+    // kernel order puts the pipelined-kernel systems first
     std::vector<int> order;
     order.reserve(n);
     for (int i = 0; i < n; i++)
-        if (!has_mol[i] && ncv[i] <= kFastMaxNc) order.push_back(i);
+        if (fast[i]) order.push_back(i);
     const int nfast = (int)order.size();
     for (int i = 0; i < n; i++)
-        if (!(!has_mol[i] && ncv[i] <= kFastMaxNc)) order.push_back(i);
+        if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
     int Kf = 0, ncf = 0, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {
@@ -475,13 +465,24 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             nce = std::max(nce, ncv[i]);
         }
     }
-    if ((nexact && (Ke > chain_max_k(128) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
+    if ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
         (nfast && fast_smem_bytes_total(Kf, ncf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
+    // proposals in pinned host memory that the device can address are read in place by the
+    // pipelined kernel (streamed through its shared-memory ring while the chains run); otherwise
+    // they are staged with one copy
+    const fau_proposal* dprops = nullptr;
+    if (nexact == 0) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, props) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            dprops = static_cast<const fau_proposal*>(pa.devicePointer);
+        cudaGetLastError();
+    }
+    const long long staged = dprops ? 0 : total;
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t o_sys = 0, o_ksys = al(o_sys + 8 * n), o_nm = al(o_ksys + 8 * n), o_off = al(o_nm + 8 * n),
                  o_sum = al(o_off + 8 * n),
-                 o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * total),
+                 o_props = al(o_sum + sizeof(SysSummary) * n), o_acc = al(o_props + sizeof(fau_proposal) * staged),
                  o_du = al(o_acc + total), bytes = al(o_du + 8 * total);
     unsigned char* dbuf = nullptr;
     if (fau_internal_ctx_scratch(ctx, bytes, reinterpret_cast<void**>(&dbuf)) != FAU_OK)
@@ -503,8 +504,8 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         cudaMemcpyAsync(dbuf + o_ksys, ksys.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(dbuf + o_nm, knm.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(dbuf + o_off, koff.data(), 8 * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(dbuf + o_props, props, sizeof(fau_proposal) * total, cudaMemcpyHostToDevice, st) !=
-            cudaSuccess)
+        (staged && cudaMemcpyAsync(dbuf + o_props, props, sizeof(fau_proposal) * staged, cudaMemcpyHostToDevice,
+                                   st) != cudaSuccess))
         return done(FAU_ERR_CUDA, "proposal upload failed");
     gather_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_sys, n, d_sum);
     cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st);
@@ -512,7 +513,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     a.sys = reinterpret_cast<DevSys* const*>(dbuf + o_ksys);
     a.n_moves = reinterpret_cast<const long long*>(dbuf + o_nm);
     a.prop_off = reinterpret_cast<const long long*>(dbuf + o_off);
-    a.props = reinterpret_cast<const fau_proposal*>(dbuf + o_props);
+    a.props = dprops ? dprops : reinterpret_cast<const fau_proposal*>(dbuf + o_props);
     a.acc_out = acc_out ? reinterpret_cast<uint8_t*>(dbuf + o_acc) : nullptr;
     a.du_out = du_out ? reinterpret_cast<double*>(dbuf + o_du) : nullptr;
     cudaEvent_t e0, e1;
@@ -534,11 +535,11 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     if (ok && nexact) {
         if (nfast) {
             ok = cudaEventRecord(fork_ev, st) == cudaSuccess && cudaStreamWaitEvent(st2, fork_ev, 0) == cudaSuccess &&
-                 launch_chain(ae, nexact, Ke, nce, 128, false, st2) == cudaSuccess &&
+                 launch_chain(ae, nexact, Ke, nce, 256, false, st2) == cudaSuccess &&
                  cudaEventRecord(join_ev, st2) == cudaSuccess;
         }
         else {
-            ok = launch_chain(ae, nexact, Ke, nce, 128, false, st) == cudaSuccess;
+            ok = launch_chain(ae, nexact, Ke, nce, 256, false, st) == cudaSuccess;
         }
     }
     if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, 4, false, st) == cudaSuccess;

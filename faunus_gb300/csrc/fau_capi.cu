@@ -78,7 +78,7 @@ struct fau_sys {
     std::vector<size_t> alloc_bytes;
     size_t bytes = 0;
     int n = 0, n_groups = 0, K = 0;
-    bool cells = false, molecular_only = false;
+    bool cells = false, molecular_only = false, all_atomic = true;
     std::vector<int> g_begin, g_flags, group_of;
     int max_group = 0;
     int precision = FAU_PREC_FP32C;
@@ -508,6 +508,8 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
                               to_fixed(cm[3 * g + 2], h.fx_scale[2]), 0u);
     }
     s->molecular_only = molecular_only;
+    for (int g = 0; g < d->n_groups; g++)
+        if (!(d->group_flags ? (d->group_flags[g] & FAU_GROUP_ATOMIC) : 1)) s->all_atomic = false;
     s->group_of = group_of;
 
     // pair tables over internal classes
@@ -1220,6 +1222,7 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
     return FAU_OK;
 }
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
 
 // a context-owned device scratch buffer of at least `bytes` (grown on demand; valid until the
 // next call on this context -- batched calls synchronise their stream before returning)

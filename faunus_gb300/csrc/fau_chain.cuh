@@ -238,6 +238,22 @@ __device__ __forceinline__ float2 phase_exact(uint32_t P)
 static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p, int lane, float2* tab, int nc)
 {
     const int TS = 2 * nc + 1;
+    // host proposals are checked here, where they are read: an index out of range or an unknown
+    // kind ends the chain with FAU_ERR_ARG before anything is indexed with it
+    const bool bad = p.kind == FAU_MOVE_ATOMIC ? (p.index < 0 || p.index >= S.n)
+                     : p.kind == FAU_MOVE_MOLECULAR ? (p.index < 0 || p.index >= S.n_groups)
+                                                    : p.kind != FAU_MOVE_NONE;
+    if (bad) {
+        if (lane == 0) {
+            ms.kind = FAU_MOVE_NONE;
+            ms.index = -1;
+            ms.m = 0;
+            ms.first = -1;
+            ms.stop = FAU_ERR_ARG;
+        }
+        __syncwarp();
+        return;
+    }
     if (lane == 0) {
         ms.kind = p.kind;
         ms.index = p.index;

@@ -114,8 +114,11 @@ __device__ __forceinline__ void fast_proposal(const DevSys& S, const ChainArgs& 
     }
     else {
         const fau_proposal& f = ring[s % kFastRing];
-        a.kind = (f.kind == FAU_MOVE_ATOMIC || f.kind == FAU_MOVE_NONE) ? f.kind : kFastUnsupported;
-        a.i = f.index;
+        // checked where it is read: anything but an in-range single-atom move or an empty move
+        // (molecular moves run in the chain kernel) ends the chain with FAU_ERR_ARG
+        const bool ok = f.kind == FAU_MOVE_NONE || (f.kind == FAU_MOVE_ATOMIC && f.index >= 0 && f.index < S.n);
+        a.kind = ok ? f.kind : kFastUnsupported;
+        a.i = ok ? f.index : 0;
 #pragma unroll
         for (int d = 0; d < 3; d++) a.dr[d] = f.dr[d];
         a.u = f.u;

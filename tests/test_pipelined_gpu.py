@@ -163,3 +163,45 @@ def test_pipelined_parallel_tempering(ctx):
         e_run = s.running_energy()
         e_tot = s.energy_total()["total"]
         assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot))
+
+
+def _pinned_copy(arr):
+    torch = pytest.importorskip("torch")
+    raw = np.ascontiguousarray(arr)
+    t = torch.empty(raw.nbytes, dtype=torch.uint8).pin_memory()
+    view = t.numpy().view(raw.dtype)
+    view[:] = raw
+    return view, t
+
+
+def test_pipelined_reads_pinned_proposals_in_place(ctx):
+    """Proposals in pinned host memory are read by the kernel directly (no staging copy);
+    the result equals the staged run's bit for bit."""
+    spec = CASES["bulk_cells"]()
+    a, b = ctx.create(spec), ctx.create(spec)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 41, 43, default_seeds=False).generate(2000)
+    off = np.array([0, len(props)], np.int64)
+    acc_a, du_a = np.zeros(len(props), np.uint8), np.zeros(len(props))
+    ctx.run_proposals_batch([a], props, off, acc_a, du_a)
+    pinned, keep = _pinned_copy(props)
+    acc_b, du_b = np.zeros(len(props), np.uint8), np.zeros(len(props))
+    ctx.run_proposals_batch([b], pinned, off, acc_b, du_b)
+    assert np.array_equal(acc_a, acc_b) and np.array_equal(du_a, du_b)
+    assert np.array_equal(a.positions(), b.positions())
+
+
+@pytest.mark.parametrize("kind", ["atomic_system", "molecular_system"])
+def test_batch_proposals_checked_on_the_device(ctx, kind):
+    """Out-of-range indices and unknown kinds end the chain with FAU_ERR_ARG (checked by the
+    kernel as it reads each proposal), leaving the system usable."""
+    spec = CASES["bulk_cells"]() if kind == "atomic_system" else configs.spce_water(n_mol=256, L=18.6, seed=3)
+    g = ctx.create(spec)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 5, 6, default_seeds=False).generate(300)
+    off = np.array([0, len(props)], np.int64)
+    for field, value in (("index", 10 ** 6), ("kind", 7)):
+        bad = props.copy()
+        bad[field][150] = value
+        with pytest.raises(F.FauError):
+            ctx.run_proposals_batch([g], bad, off)
+    st = ctx.run_proposals_batch([g], props, off)  # still usable afterwards
+    assert st["moves"] == len(props)
