@@ -29,6 +29,7 @@ extern "C" int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int*
 extern "C" int fau_internal_fail(int code, const char* msg);
 extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
+extern "C" int fau_internal_sys_classes(const fau_sys* s);
 
 namespace {
 
@@ -155,7 +156,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     for (int i = 0; i < n; i++)
         if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
-    int Kf = 0, ncf = 0, Ke = 0, nce = 0;
+    int Kf = 0, ncf = 0, ntf = 1, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {
         int K, np, ng, mo, knc;
         fau_ctx* c2;
@@ -165,6 +166,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         if (r < nfast) {
             Kf = std::max(Kf, K);
             ncf = std::max(ncf, knc);
+            ntf = std::max(ntf, fau_internal_sys_classes(systems[order[r]]));
         }
         else {
             Ke = std::max(Ke, K);
@@ -172,7 +174,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         }
     }
     if ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
-        (nfast && fast_smem_bytes_total(Kf, ncf) > 227 * 1024))
+        (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
 
     // device argument arrays (one allocation, freed at the end of the call)
@@ -283,7 +285,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact) BTRY(prepare_chain(Ke, nce, threads, true));
-    if (nfast) BTRY(prepare_fast(Kf, ncf, fwarps, true));
+    if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
         BTRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -299,10 +301,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             if ((e = cudaStreamWaitEvent(st2, fork_ev, 0)) != cudaSuccess) return e;
             if ((e = launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess) return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
-            if ((e = launch_fast(a, nfast, Kf, ncf, fwarps, true, st)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
-        if (nfast) return launch_fast(a, nfast, Kf, ncf, fwarps, true, st);
+        if (nfast) return launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st);
         return launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };
 
@@ -453,12 +455,13 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     for (int i = 0; i < n; i++)
         if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
-    int Kf = 0, ncf = 0, Ke = 0, nce = 0;
+    int Kf = 0, ncf = 0, ntf = 1, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {
         const int i = order[r];
         if (r < nfast) {
             Kf = std::max(Kf, Kv[i]);
             ncf = std::max(ncf, ncv[i]);
+            ntf = std::max(ntf, fau_internal_sys_classes(systems[i]));
         }
         else {
             Ke = std::max(Ke, Kv[i]);
@@ -466,7 +469,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         }
     }
     if ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
-        (nfast && fast_smem_bytes_total(Kf, ncf) > 227 * 1024))
+        (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
     // proposals in pinned host memory that the device can address are read in place by the
     // pipelined kernel (streamed through its shared-memory ring while the chains run); otherwise
@@ -542,7 +545,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             ok = launch_chain(ae, nexact, Ke, nce, 256, false, st) == cudaSuccess;
         }
     }
-    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, 4, false, st) == cudaSuccess;
+    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st) == cudaSuccess;
     if (ok && nfast && a.du_out) {
         unpack_du_kernel<<<nfast, 256, 0, st>>>(a.du_out, a.prop_off, a.n_moves);
         ok = cudaGetLastError() == cudaSuccess;

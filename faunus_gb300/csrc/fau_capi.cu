@@ -1223,6 +1223,7 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
 }
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
+int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
 
 // a context-owned device scratch buffer of at least `bytes` (grown on demand; valid until the
 // next call on this context -- batched calls synchronise their stream before returning)

@@ -875,18 +875,18 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
 }
 
 // dynamic shared memory of the pipelined kernel for K k-vectors, table size nc
-__host__ __device__ inline size_t fast_smem_bytes(int K, int nc)
+__host__ __device__ inline size_t fast_smem_bytes(int K, int nc, int nt)
 {
     return (size_t)K * (sizeof(float4) + sizeof(float2) + sizeof(int2)) + (size_t)3 * 3 * (2 * nc + 1) * sizeof(float4) +
-           (size_t)kMaxITypes * kMaxITypes * sizeof(PairF);
+           (size_t)nt * nt * sizeof(PairF);
 }
 
 template <int NWC, bool PH>
-cudaError_t launch_fast_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
+cudaError_t launch_fast_inst(const ChainArgs& a, int nblocks, int K, int nc, int nt, cudaStream_t st, bool prepare_only)
 {
     // the dynamic allowance is raised on demand, never inside a stream capture: callers prepare first
     static size_t granted = 0;
-    const size_t smem = fast_smem_bytes(K, nc);
+    const size_t smem = fast_smem_bytes(K, nc, nt);
     if (smem > granted || granted == 0) {
         cudaError_t e = cudaFuncSetAttribute(fast_chain_kernel<NWC, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

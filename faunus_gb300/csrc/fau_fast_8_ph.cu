@@ -3,9 +3,9 @@
 
 namespace fau {
 
-cudaError_t fast_dispatch_8_ph(const ChainArgs& a, int nb, int K, int nc, cudaStream_t st, bool prep)
+cudaError_t fast_dispatch_8_ph(const ChainArgs& a, int nb, int K, int nc, int nt, cudaStream_t st, bool prep)
 {
-    return launch_fast_inst<8, true>(a, nb, K, nc, st, prep);
+    return launch_fast_inst<8, true>(a, nb, K, nc, nt, st, prep);
 }
 
 } // namespace fau

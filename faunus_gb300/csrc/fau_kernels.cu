@@ -309,35 +309,35 @@ cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int thr
     return chain_launch_impl(a, nblocks, K, nc, threads, philox, st, false);
 }
 
-size_t fast_smem_bytes_total(int K, int nc)
+size_t fast_smem_bytes_total(int K, int nc, int nt)
 {
     // dynamic part + the kernel's static shared memory (move slots, proposal ring, partials)
-    return fast_smem_bytes(K, nc) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
+    return fast_smem_bytes(K, nc, nt) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
 }
 
-static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox,
+static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox,
                                     cudaStream_t st, bool prepare_only)
 {
     if (warps == 2)
-        return philox ? fast_dispatch_2_ph(a, nblocks, K, nc, st, prepare_only)
-                      : fast_dispatch_2_host(a, nblocks, K, nc, st, prepare_only);
+        return philox ? fast_dispatch_2_ph(a, nblocks, K, nc, nt, st, prepare_only)
+                      : fast_dispatch_2_host(a, nblocks, K, nc, nt, st, prepare_only);
     if (warps == 8)
-        return philox ? fast_dispatch_8_ph(a, nblocks, K, nc, st, prepare_only)
-                      : fast_dispatch_8_host(a, nblocks, K, nc, st, prepare_only);
+        return philox ? fast_dispatch_8_ph(a, nblocks, K, nc, nt, st, prepare_only)
+                      : fast_dispatch_8_host(a, nblocks, K, nc, nt, st, prepare_only);
     if (warps != 4) return cudaErrorInvalidValue;
-    return philox ? fast_dispatch_4_ph(a, nblocks, K, nc, st, prepare_only)
-                  : fast_dispatch_4_host(a, nblocks, K, nc, st, prepare_only);
+    return philox ? fast_dispatch_4_ph(a, nblocks, K, nc, nt, st, prepare_only)
+                  : fast_dispatch_4_host(a, nblocks, K, nc, nt, st, prepare_only);
 }
 
-cudaError_t prepare_fast(int K, int nc, int warps, bool philox)
+cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox)
 {
     ChainArgs a{};
-    return fast_launch_impl(a, 0, K, nc, warps, philox, nullptr, true);
+    return fast_launch_impl(a, 0, K, nc, nt, warps, philox, nullptr, true);
 }
 
-cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox, cudaStream_t st)
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st)
 {
-    return fast_launch_impl(a, nblocks, K, nc, warps, philox, st, false);
+    return fast_launch_impl(a, nblocks, K, nc, nt, warps, philox, st, false);
 }
 
 // Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then

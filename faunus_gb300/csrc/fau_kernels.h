@@ -64,15 +64,15 @@ cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t,
 // pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps;
 // k-vector components up to kFastMaxNc (8-bit phase-table indices)
 constexpr int kFastMaxNc = 40;
-size_t fast_smem_bytes_total(int K, int nc);
-cudaError_t prepare_fast(int K, int nc, int warps, bool philox);
-cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int warps, bool philox, cudaStream_t st);
-cudaError_t fast_dispatch_2_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_2_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_4_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_4_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_8_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
+size_t fast_smem_bytes_total(int K, int nc, int nt);
+cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox);
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st);
+cudaError_t fast_dispatch_2_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_2_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_4_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_4_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_8_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
