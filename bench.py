@@ -120,6 +120,11 @@ def _max_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
+def replica_streams(R: int, rank: int) -> np.ndarray:
+    """Device RNG streams of one rank's replicas: disjoint across ranks (replicas only)."""
+    return np.arange(R, dtype=np.uint32) + np.uint32(1_000_000 * rank)
+
+
 def _barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -183,12 +188,13 @@ def run_reference(args) -> None:
     from faunus_gb300 import configs
     spec = configs.bulk_ewald(n_salt=10000, seed=1)
     threads = os.cpu_count() or 1
+    sample = args.cpu_sample_seconds
     for _ in range(args.warmup):
-        cpu_baseline(spec, seconds_per_thread=0.2, threads=threads)
+        cpu_baseline(spec, seconds_per_thread=0.4 * sample, threads=threads)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(spec, seconds_per_thread=0.5, threads=threads))
+        vals.append(cpu_baseline(spec, seconds_per_thread=sample, threads=threads))
     wall = time.perf_counter() - t0
     total_moves = sum(v["value"] * v["wall_s"] for v in vals)
     tot_wall = sum(v["wall_s"] for v in vals)
@@ -221,7 +227,7 @@ def run_ours(args) -> None:
     M = args.moves
     first = ctx.create(base)
     systems = [first] + [first.clone() for _ in range(R - 1)]
-    streams = np.arange(R, dtype=np.uint32) + 1_000_000 * rank
+    streams = replica_streams(R, rank)
     resident = ctx.hbm_used()
 
     # ---- kernel configuration: the autotuner's choice unless --threads is given
@@ -457,6 +463,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-form and served-stream measurements")
     ap.add_argument("--served-full", action="store_true", help="served stream at the full configured job sizes")
+    ap.add_argument("--cpu-sample-seconds", type=float, default=0.5,
+                    help="reference arm: seconds of CPU chain work per thread and step")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":
