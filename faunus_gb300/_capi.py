@@ -51,6 +51,7 @@ class SysDesc(C.Structure):
         ("bjerrum_length", C.c_double), ("coulomb_cutoff", C.c_double), ("coulomb_alpha", C.c_double),
         ("pair_cutoff", C.c_double), ("cutoff_g2g", C.c_double),
         ("ewald", EwaldDesc), ("precision", C.c_int), ("cell_capacity", C.c_int),
+        ("n_molids", C.c_int), ("cutoff_g2g_pairs", dptr),
     ]
 
 

@@ -23,7 +23,7 @@ import math
 import numpy as np
 
 from . import _capi as A
-from .system import SystemSpec, bjerrum_length, kjmol_to_kt
+from .system import SystemSpec, bjerrum_length, group_cutoff, kjmol_to_kt
 
 AVOGADRO = 6.022137e23
 
@@ -161,9 +161,13 @@ def mass_centers(pos: np.ndarray, group_begin: np.ndarray, masses: np.ndarray, L
 def spce_water(n_mol: int = 1000, L: float = 31.0, temperature: float = 300.0, epsr: float = 1.0,
                alpha: float = 0.2, rc: float = 9.0, ncutoff: float = 7.3, cutoff_g2g: float = 10.0,
                epss: float = 0.0, seed: int = 2, precision: int = A.FAU_PREC_FP32C, dp: float = 0.5,
-               dprot: float = 0.5) -> SystemSpec:
+               dprot: float = 0.5, molecules: tuple = ("SOL",)) -> SystemSpec:
     """Rigid SPC/E water (O -0.8476, H +0.4238; O-H 1 A, H-O-H 109.47 deg);
-    mass centres on a cubic lattice with random orientations."""
+    mass centres on a cubic lattice with random orientations.
+
+    With several `molecules` names, molecule g is of kind g mod len(molecules)
+    (same chemistry, distinct molecule ids), and `cutoff_g2g` may be any
+    GroupCutoff input form (a number or a {"default": .., "A B": ..} dict)."""
     rng = np.random.default_rng(seed)
     theta = math.radians(109.47) / 2
     geo = np.array([[0.0, 0.0, 0.0], [math.sin(theta), math.cos(theta), 0.0], [-math.sin(theta), math.cos(theta), 0.0]])
@@ -190,11 +194,14 @@ def spce_water(n_mol: int = 1000, L: float = 31.0, temperature: float = 300.0, e
     cm = mass_centers(pos, gb, masses, box)
     return SystemSpec(
         box=box, pos=pos, charge=charge, type=types, group_begin=gb,
-        group_flags=np.full(n_mol, A.FAU_GROUP_RIGID, dtype=np.int32), group_molid=np.zeros(n_mol, dtype=np.int32),
+        group_flags=np.full(n_mol, A.FAU_GROUP_RIGID, dtype=np.int32),
+        group_molid=(np.arange(n_mol) % len(molecules)).astype(np.int32),
         mass_center=cm, n_types=2, sigma2=sigma2, eps4=eps4, type_mass=np.array([15.999, 1.007]),
         pair_terms=A.FAU_PAIR_COULOMB | A.FAU_PAIR_LJ, coulomb_type=A.FAU_COUL_EWALD,
         bjerrum_length=bjerrum_length(epsr, temperature), coulomb_cutoff=rc, coulomb_alpha=alpha,
-        cutoff_g2g=cutoff_g2g, ewald={"alpha": alpha, "ncutoff": ncutoff, "spherical_sum": 1, "epss": epss},
+        cutoff_g2g=cutoff_g2g if not isinstance(cutoff_g2g, dict) else 0.0,
+        cutoff_g2g_pairs=group_cutoff(cutoff_g2g, molecules) if isinstance(cutoff_g2g, dict) else None,
+        ewald={"alpha": alpha, "ncutoff": ncutoff, "spherical_sum": 1, "epss": epss},
         precision=precision, temperature=temperature, name=f"spce-water N={n_mol}",
         extra={"moves": [{"kind": A.FAU_MOVE_MOLECULAR, "repeat": n_mol, "dp": dp, "dprot": dprot,
                           "groups": list(range(n_mol))}]},

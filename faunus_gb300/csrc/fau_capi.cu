@@ -214,6 +214,15 @@ int validate(const fau_sys_desc* d)
         if (!(d->ewald.alpha > 0.0)) return fail(FAU_ERR_ARG, "ewald.alpha must be positive");
         if (d->ewald.ncutoff > 127) return fail(FAU_ERR_ARG, "ewald.ncutoff above 127");
     }
+    if (d->cutoff_g2g_pairs) {
+        if (d->n_molids < 1 || d->n_molids > 4096) return fail(FAU_ERR_ARG, "n_molids %d outside [1, 4096]", d->n_molids);
+        if (!d->group_molid) return fail(FAU_ERR_ARG, "cutoff_g2g_pairs needs group_molid");
+        for (int g = 0; g < d->n_groups; g++)
+            if (d->group_molid[g] < 0 || d->group_molid[g] >= d->n_molids)
+                return fail(FAU_ERR_ARG, "group %d: molecule id %d outside [0, n_molids)", g, d->group_molid[g]);
+        for (long k = 0; k < (long)d->n_molids * d->n_molids; k++)
+            if (std::isnan(d->cutoff_g2g_pairs[k])) return fail(FAU_ERR_ARG, "cutoff_g2g_pairs holds NaN");
+    }
     if (d->precision != FAU_PREC_FP32C && d->precision != FAU_PREC_FP64)
         return fail(FAU_ERR_ARG, "unknown precision %d", d->precision);
     return FAU_OK;
@@ -313,6 +322,7 @@ size_t footprint_bytes(const fau_sys_desc* d, const Layout& lay, int cap)
     }
     b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16);
     b += sizeof(PlainMove) + 64 + sizeof(void*);
+    if (d->cutoff_g2g_pairs && d->n_molids > 0) b += g * 4 + (size_t)d->n_molids * d->n_molids * (8 + 4);
     return b;
 }
 
@@ -552,6 +562,23 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     h.rc2_pair = d->pair_cutoff > 0 ? (float)(d->pair_cutoff * d->pair_cutoff) : 0.f;
     h.rc2_pair_d = d->pair_cutoff > 0 ? d->pair_cutoff * d->pair_cutoff : 0.0;
     h.cut_g2g2 = d->cutoff_g2g > 0 ? d->cutoff_g2g * d->cutoff_g2g : -1.0;
+    std::vector<double> cut2_mol;
+    std::vector<float> cut2_molf;
+    std::vector<int> g_molid;
+    if (d->cutoff_g2g_pairs && d->n_molids > 0) { // GroupCutoff::getCutoff per molecule-kind pair
+        const size_t nm = (size_t)d->n_molids;
+        cut2_mol.resize(nm * nm);
+        cut2_molf.resize(nm * nm);
+        h.cut_g2g2 = -1.0;
+        for (size_t k = 0; k < nm * nm; k++) {
+            const double c = d->cutoff_g2g_pairs[k];
+            cut2_mol[k] = (c > 0 && std::isfinite(c)) ? c * c : -1.0;
+            cut2_molf[k] = (float)cut2_mol[k];
+            if (cut2_mol[k] >= 0.0) h.cut_g2g2 = 0.0; // some pair has a cutoff
+        }
+        g_molid.assign(d->group_molid, d->group_molid + d->n_groups);
+        h.n_mol = d->n_molids;
+    }
     h.cut_g2g2f = (float)h.cut_g2g2;
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0);
@@ -572,6 +599,11 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     UP(h.g_cm, cm);
     UP(h.g_cmrec, cmrec);
     UP(h.atomic_idx, atomic_idx);
+    if (h.n_mol > 0) {
+        UP(h.g_molid, g_molid);
+        UP(h.cut2_mol, cut2_mol);
+        UP(h.cut2_molf, cut2_molf);
+    }
     h.n_atomic = molecular_only ? 0 : (int)atomic_idx.size();
     if (!molecular_only && (int)atomic_idx.size() == n) h.n_atomic = 0; // all atomic: index = particle
     UP(h.pair, pf);
@@ -702,6 +734,7 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     DevSys& h = s->h;
     fix(h.x); fix(h.y); fix(h.z); fix(h.rec); fix(h.group_of); fix(h.itype_q); fix(h.itype_qd); fix(h.itype_self);
     fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
+    fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf);
     fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
     fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
     fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);

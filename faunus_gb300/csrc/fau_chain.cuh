@@ -77,24 +77,16 @@ __device__ __forceinline__ int cell_index(const DevSys& S, const int* c)
 }
 
 // GroupCutoff::cut (src/energy.h:761-768): sqdist(cm1, cm2) >= cutoff^2, FP32 on
-// fixed-point mass centres, FP64 inside a 1e-5 guard band.
-__device__ __forceinline__ bool group_cut_rec(const DevSys& S, uint4 cmrec, const double* cm, uint4 cmrec_h, int h)
+// fixed-point mass centres, FP64 inside a 1e-5 guard band.  c2 < 0: no cutoff.
+__device__ __forceinline__ bool group_cut_rec(const DevSys& S, uint4 cmrec, const double* cm, uint4 cmrec_h, int h,
+                                              double c2, float c2f)
 {
-    if (S.cut_g2g2 < 0.0) return false;
+    if (c2 < 0.0) return false;
     const float r2 = r2_fixed(S, cmrec, cmrec_h);
-    if (r2 < S.cut_g2g2f * 0.99999f) return false;
-    if (r2 > S.cut_g2g2f * 1.00001f) return true;
+    if (r2 < c2f * 0.99999f) return false;
+    if (r2 > c2f * 1.00001f) return true;
     const double o[3] = {S.g_cm[3 * h], S.g_cm[3 * h + 1], S.g_cm[3 * h + 2]};
-    return sqdist_d(S, cm, o) >= S.cut_g2g2;
-}
-__device__ __forceinline__ bool group_cut(const DevSys& S, uint4 cmrec, const double* cm, int h)
-{
-    if (S.cut_g2g2 < 0.0) return false;
-    const float r2 = r2_fixed(S, cmrec, S.g_cmrec[h]);
-    if (r2 < S.cut_g2g2f * 0.99999f) return false;
-    if (r2 > S.cut_g2g2f * 1.00001f) return true;
-    const double o[3] = {S.g_cm[3 * h], S.g_cm[3 * h + 1], S.g_cm[3 * h + 2]};
-    return sqdist_d(S, cm, o) >= S.cut_g2g2;
+    return sqdist_d(S, cm, o) >= c2;
 }
 
 // quaternion rotation v' = v + w t + u x t, t = 2 u x v (FP64, never contracted)
@@ -718,25 +710,34 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 // group, moved atom) task per thread over the list -- every thread does
                 // useful pair work instead of a few lanes running whole groups serially.
                 const int G = S.n_groups;
+                const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
                 int chunk = 0;
                 for (int base = 0; base < G; base += kNblChunk, chunk++) {
                     int* cntp = &nbl_cnt[chunk & 1];
                     constexpr int RC = kNblChunk / NT;
-                    int gfl[RC];
+                    int gfl[RC], gml[RC];
                     uint4 gcr[RC];
 #pragma unroll
                     for (int r = 0; r < RC; r++) { // all loads first: their latencies overlap
                         const int h = base + r * NT + tid;
                         gfl[r] = h < G ? S.g_flags[h] : FAU_GROUP_ATOMIC;
                         gcr[r] = h < G ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                        gml[r] = (h < G && S.n_mol > 0) ? S.g_molid[h] : 0;
                     }
 #pragma unroll
                     for (int r = 0; r < RC; r++) {
                         const int h = base + r * NT + tid;
                         uint32_t e = 0;
                         if (h < G && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
-                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h);
-                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h);
+                            double c2 = S.cut_g2g2;
+                            float c2f = S.cut_g2g2f;
+                            if (S.n_mol > 0) { // GroupCutoff::getCutoff(molid of g, molid of h)
+                                const int k = mol_g * S.n_mol + gml[r];
+                                c2 = S.cut2_mol[k];
+                                c2f = S.cut2_molf[k];
+                            }
+                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
+                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
                             e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
                         }
                         const unsigned bal = __ballot_sync(0xffffffffu, e != 0);

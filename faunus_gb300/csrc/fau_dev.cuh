@@ -72,8 +72,12 @@ struct DevSys {
     float lB, rc_coul, rc2_coul, alpha;
     float rc2_pair;   // 0: no truncation
     double rc2_pair_d, rc_coul_d, alpha_d, lB_d;
-    double cut_g2g2;  // group mass-centre cutoff^2 (FP64); < 0: none
+    double cut_g2g2;  // group mass-centre cutoff^2 (FP64); < 0: none (with n_mol > 0: >= 0 if any pair has one)
     float cut_g2g2f;
+    int n_mol;        // > 0: per molecule-kind pair cutoffs^2 below, indexed by g_molid
+    int* g_molid;     // n_groups molecule kinds (n_mol > 0 only)
+    double* cut2_mol; // n_mol^2 cutoffs^2 (FP64); < 0: no cutoff for that pair
+    float* cut2_molf; // FP32 copies
     PairF* pair;      // nt*nt
     double* pair_d;   // nt*nt*4 FP64 copies (s2, e4, hs2, qq)
 
@@ -244,6 +248,12 @@ __device__ __forceinline__ double sqdist_d(const DevSys& S, const double* a, con
         d[k] = __dsub_rn(v, v > S.half[k] ? S.L[k] : 0.0);
     }
     return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+
+// GroupCutoff::getCutoff(molid1, molid2)^2 of two groups (src/energy.h:740-768); < 0: none
+__device__ __forceinline__ double group_cut2(const DevSys& S, int g1, int g2)
+{
+    return S.n_mol > 0 ? S.cut2_mol[S.g_molid[g1] * S.n_mol + S.g_molid[g2]] : S.cut_g2g2;
 }
 
 // squared minimum-image distance of two fixed-point records, FP32

@@ -56,8 +56,9 @@ __global__ void total_pair_kernel(const DevSys* Sp, double* out, int* flags)
                 if (rigid_i) continue;
             }
             else if (S.cut_g2g2 >= 0.0 && !ai && !(S.g_flags[gj] & FAU_GROUP_ATOMIC)) {
+                const double c2 = group_cut2(S, gi, gj);
                 const double cmj[3] = {S.g_cm[3 * gj], S.g_cm[3 * gj + 1], S.g_cm[3 * gj + 2]};
-                if (sqdist_d(S, cmi, cmj) >= S.cut_g2g2) continue;
+                if (c2 >= 0.0 && sqdist_d(S, cmi, cmj) >= c2) continue;
             }
             const double xj[3] = {S.x[j], S.y[j], S.z[j]};
             const double u = pair_u64(S, ti, S.rec[j].w >> 24, sqdist_d(S, xi, xj));
@@ -149,11 +150,12 @@ __global__ void plain_pair_kernel(const DevSys* Sp, const PlainMove* P, double* 
             const int g = P->group;
             if (gj == g) continue;
             bool cut_o = false, cut_n = false;
-            if (S.cut_g2g2 >= 0.0 && !(S.g_flags[gj] & FAU_GROUP_ATOMIC)) {
+            const double c2 = S.cut_g2g2 >= 0.0 ? group_cut2(S, g, gj) : -1.0;
+            if (c2 >= 0.0 && !(S.g_flags[gj] & FAU_GROUP_ATOMIC)) {
                 const double cmj[3] = {S.g_cm[3 * gj], S.g_cm[3 * gj + 1], S.g_cm[3 * gj + 2]};
                 const double cmo[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
-                cut_o = sqdist_d(S, cmo, cmj) >= S.cut_g2g2;
-                cut_n = sqdist_d(S, P->cm_new, cmj) >= S.cut_g2g2;
+                cut_o = sqdist_d(S, cmo, cmj) >= c2;
+                cut_n = sqdist_d(S, P->cm_new, cmj) >= c2;
             }
             const double xj[3] = {S.x[j], S.y[j], S.z[j]};
             const int tj = S.rec[j].w >> 24;

@@ -24,6 +24,29 @@ AVOGADRO = 6.022137e23
 PI = float(np.pi)
 
 
+def group_cutoff(value, molecule_names: Sequence[str]) -> np.ndarray:
+    """GroupCutoff's mass-centre cutoff per molecule-kind pair from the reference's input
+    forms (GroupCutoff from_json, src/energy.cpp:1868-1953; KAT src/energy.cpp:1955-2002):
+
+      12.0                              every pair 12
+      {"default": 13.0}                 every pair 13
+      {"default": 13.0, "M Q": 14.0}    M-Q (both orders) 14, the rest 13
+      {"M Q": 11.0}                     M-Q 11, the rest without cutoff (+inf)
+    """
+    n = len(molecule_names)
+    index = {name: i for i, name in enumerate(molecule_names)}
+    if isinstance(value, (int, float)):
+        return np.full((n, n), float(value))
+    out = np.full((n, n), float(value.get("default", np.inf)))
+    for key, c in value.items():
+        if key == "default":
+            continue
+        a, b = key.split()
+        i, j = index[a], index[b]
+        out[i, j] = out[j, i] = float(c)
+    return out
+
+
 def bjerrum_length(epsr: float, temperature: float = 298.15) -> float:
     """Bjerrum length in angstrom (pc::bjerrumLength, src/units.h:37-41)."""
     kT = temperature * BOLTZMANN
@@ -59,6 +82,7 @@ class SystemSpec:
     coulomb_alpha: float = 0.0
     pair_cutoff: float = 0.0
     cutoff_g2g: float = 0.0
+    cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
     ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
     precision: int = A.FAU_PREC_FP32C
     cell_capacity: int = 0
@@ -127,6 +151,12 @@ class SystemSpec:
             d.ewald.epss = float(self.ewald.get("epss", 0.0))
         d.precision = int(self.precision)
         d.cell_capacity = int(self.cell_capacity)
+        if self.cutoff_g2g_pairs is not None:
+            m = np.asarray(self.cutoff_g2g_pairs, dtype=np.float64)
+            if m.ndim != 2 or m.shape[0] != m.shape[1]:
+                raise ValueError("cutoff_g2g_pairs must be a square matrix")
+            d.n_molids = int(m.shape[0])
+            d.cutoff_g2g_pairs = f64(m.reshape(-1))
         return d, keep
 
 

@@ -119,6 +119,10 @@ typedef struct fau_sys_desc {
 
     int precision;            /* fau_precision                                       */
     int cell_capacity;        /* slots per cell; 0: chosen from the initial state    */
+    int n_molids;             /* molecule kinds (group_molid < n_molids) of the matrix below */
+    const double* cutoff_g2g_pairs; /* n_molids^2 GroupCutoff::getCutoff(i, j) per molecule-kind
+                                 pair (src/energy.h:746-768); <= 0 or +inf: no cutoff for
+                                 that pair; NULL: cutoff_g2g for every pair                */
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */

@@ -342,6 +342,8 @@ struct System {
     PairParams pair;
     Ewald ewald;
     double cutoff_g2g2 = std::numeric_limits<double>::max();
+    int n_molids = 0;              // > 0: per molecule-kind pair cutoffs^2 below
+    std::vector<double> cut2_pairs;
     bool want_scale = true; // sum |u| over both states for tolerance checks (not in the reference)
     // MC bookkeeping (MetropolisMonteCarlo)
     double initial_energy = 0, sum_of_energy_changes = 0;
@@ -350,7 +352,8 @@ struct System {
     bool cut(int g1, int g2) const
     {
         if (groups[g1].atomic() || groups[g2].atomic()) return false;
-        return box.sqdist(cm[g1], cm[g2]) >= cutoff_g2g2;
+        const double c2 = n_molids > 0 ? cut2_pairs[size_t(groups[g1].molid) * n_molids + groups[g2].molid] : cutoff_g2g2;
+        return box.sqdist(cm[g1], cm[g2]) >= c2;
     }
     double u(int i, int j) const { return pair(type[i], type[j], q[i], q[j], box.sqdist(pos[i], pos[j])); }
     double mag(int i, int j) const { return pair.magnitude(type[i], type[j], q[i], q[j], box.sqdist(pos[i], pos[j])); }
@@ -795,6 +798,14 @@ static System buildSystem(const fau_sys_desc* d)
     P.alpha = d->coulomb_alpha;
     P.pair_cutoff2 = d->pair_cutoff > 0 ? d->pair_cutoff * d->pair_cutoff : 0.0;
     if (d->cutoff_g2g > 0) s.cutoff_g2g2 = d->cutoff_g2g * d->cutoff_g2g;
+    if (d->cutoff_g2g_pairs && d->n_molids > 0) { // GroupCutoff::getCutoff per molecule-kind pair
+        s.n_molids = d->n_molids;
+        s.cut2_pairs.resize(size_t(d->n_molids) * d->n_molids);
+        for (size_t k = 0; k < s.cut2_pairs.size(); k++) {
+            const double c = d->cutoff_g2g_pairs[k];
+            s.cut2_pairs[k] = (c > 0 && std::isfinite(c)) ? c * c : std::numeric_limits<double>::max();
+        }
+    }
     Ewald& E = s.ewald;
     E.enabled = d->ewald.enabled != 0;
     if (E.enabled) {

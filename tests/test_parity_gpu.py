@@ -71,6 +71,7 @@ def _compare_chain(gpu_sys, spec, props, tol, expect_bit_exact=True):
     lambda: configs.bulk_ewald(n_salt=1000, epss=1.0),
     lambda: configs.spce_water(n_mol=256, L=18.6),
     lambda: configs.spce_water(n_mol=1000),
+    lambda: configs.spce_water(n_mol=512, L=24.8, molecules=("M", "Q"), cutoff_g2g={"default": 7.0, "M Q": 10.0}),
 ])
 def test_energy_total_matches_oracle(ctx, make):
     spec = make()
@@ -143,6 +144,24 @@ def test_chain_water(ctx):
 def test_chain_small_water_box(ctx):
     spec = configs.spce_water(n_mol=256, L=18.6)
     _compare_chain(ctx.create(spec), spec, _props(spec, 2000), TOL_FP32C)
+
+
+@pytest.mark.parametrize("cut", [{"default": 7.0, "M Q": 10.0}, {"M Q": 8.0}])
+def test_chain_water_per_pair_group_cutoff(ctx, cut):
+    """GroupCutoff::getCutoff per molecule-kind pair (two kinds, M and Q) in the chain
+    kernel, the plain FP64 form and a batch of clones."""
+    spec = configs.spce_water(n_mol=512, L=24.8, molecules=("M", "Q"), cutoff_g2g=cut)
+    props = _props(spec, 1500)
+    _compare_chain(ctx.create(spec), spec, props, TOL_FP32C)
+    w = configs.spce_water(n_mol=512, L=24.8, molecules=("M", "Q"), cutoff_g2g=cut, precision=A.FAU_PREC_FP64)
+    _compare_chain(ctx.create(w), w, _props(w, 300), 1e-10)
+    base = ctx.create(spec)
+    reps = [base] + [base.clone() for _ in range(3)]
+    ctx.run_batch(reps, 500, seed=2, dp=0.5, dprot=0.5)
+    for r in reps:
+        e_run = r.running_energy()
+        r.q_rebuild()
+        assert abs(e_run - r.energy_total()["total"]) <= 1e-6 * abs(e_run)
 
 
 def test_running_energy_has_no_drift(ctx):
