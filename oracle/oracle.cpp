@@ -1001,6 +1001,26 @@ int orc_pair_u(const fau_sys_desc* d, int ta, int tb, double qa, double qb, doub
     return FAU_OK;
 }
 
+// ---- Chameleon cuboid geometry (consistency KAT, src/geometry.cpp:1320-1371): per point
+// pair, a wrapped by boundary(), vdist(a, b) and sqdist(a, b)
+int orc_geometry(const double box[3], int n, const double* a, const double* b, double* a_wrapped, double* vd,
+                 double* sq)
+{
+    Box B;
+    B.set(box);
+    for (int i = 0; i < n; i++) {
+        Vec3 p{a[3 * i], a[3 * i + 1], a[3 * i + 2]}, q{b[3 * i], b[3 * i + 1], b[3 * i + 2]};
+        const Vec3 d = B.vdist(p, q);
+        sq[i] = B.sqdist(p, q);
+        B.boundary(p);
+        for (int k = 0; k < 3; k++) {
+            a_wrapped[3 * i + k] = p[k];
+            vd[3 * i + k] = d[k];
+        }
+    }
+    return FAU_OK;
+}
+
 // ---- cell grid binning (bit-exact oracle for the device cell list)
 int orc_cell_bin(const double box[3], double min_cell, int n, const double* pos, int* cells_out, int dims_out[3],
                  int offmin_out[3], int offmax_out[3])

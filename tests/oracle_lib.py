@@ -43,6 +43,7 @@ def lib() -> C.CDLL:
             "orc_ewald_policy": ([C.c_int, A.dptr, A.dptr, A.dptr, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, C.c_int, A.dptr, A.iptr], C.c_int),
             "orc_pair_u": ([sd, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, A.dptr], C.c_int),
+            "orc_geometry": ([A.dptr, C.c_int, A.dptr, A.dptr, A.dptr, A.dptr, A.dptr], C.c_int),
             "orc_cell_bin": ([A.dptr, C.c_double, C.c_int, A.dptr, A.iptr, A.iptr, A.iptr, A.iptr], C.c_int),
             "orc_movegen_create": ([P, C.POINTER(A.MoveDesc), C.c_int, C.c_uint32, C.c_uint32, C.c_int,
                                     C.POINTER(P)], C.c_int),
@@ -199,6 +200,18 @@ def pair_u(spec, ta, tb, qa, qb, r2) -> float:
     u = C.c_double()
     _ok(lib().orc_pair_u(C.byref(d), ta, tb, qa, qb, r2, C.byref(u)), "orc_pair_u")
     return u.value
+
+
+def geometry(box, a, b):
+    """(boundary(a), vdist(a, b), sqdist(a, b)) of the oracle's cuboid Chameleon, per row."""
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(a)
+    aw, vd, sq = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+    _ok(lib().orc_geometry(A.as_dptr(box), n, A.as_dptr(a.reshape(-1)), A.as_dptr(b.reshape(-1)),
+                           A.as_dptr(aw.reshape(-1)), A.as_dptr(vd.reshape(-1)), A.as_dptr(sq)), "orc_geometry")
+    return aw, vd, sq
 
 
 def cell_bin(box, min_cell, pos):

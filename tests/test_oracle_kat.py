@@ -180,6 +180,65 @@ def test_coulomb_bjerrum_length_and_force():
     assert abs(abs(fn) - KAT["coulomb_force_norm"]) < 1e-8
 
 
+def test_functor_potential_coulomb_wca_sum():
+    """FunctorPotential (src/potentials.cpp:1333-1368): default pair set Coulomb
+    (epsr 80, plain), A-B Coulomb + WCA (LB mixing), C-C hard sphere only.  The
+    descriptor's pair terms are global; a pair without a term has its coefficient
+    zeroed (eps4 = 0 for WCA, hs_sigma2 = 0 for HS), which reproduces the per-pair
+    sets: u(a,a) = coulomb, u(b,b) = coulomb, u(a,b) = coulomb + wca; C-C is 0 just
+    outside contact and +inf just inside."""
+    lB = bjerrum_length(80.0, 298.15)
+    sig = np.array([2.2, 4.0, 2.0])  # 2 r
+    eps = np.array([0.1, 0.05, 0.0])  # kJ/mol
+    q = np.array([1.0, -1.0, 0.0])
+    s2 = (0.5 * (sig[:, None] + sig[None, :])) ** 2
+    e4 = np.zeros((3, 3))
+    e4[0, 1] = e4[1, 0] = 4 * kjmol_to_kt(math.sqrt(eps[0] * eps[1]), 298.15)
+    hs2 = np.zeros((3, 3))
+    hs2[2, 2] = s2[2, 2]
+    spec = SystemSpec(box=np.full(3, 100.0), pos=np.zeros((1, 3)), charge=np.zeros(1), type=np.zeros(1, np.int32),
+                      group_begin=np.array([0, 1], np.int32), group_flags=np.array([1], np.int32), n_types=3,
+                      sigma2=s2, eps4=e4, hs_sigma2=hs2, bjerrum_length=lB, coulomb_type=A.FAU_COUL_PLAIN,
+                      pair_terms=A.FAU_PAIR_COULOMB | A.FAU_PAIR_WCA | A.FAU_PAIR_HS)
+    r2 = 4.0  # r = (2, 0, 0)
+
+    def coulomb(a, b):
+        return lB * q[a] * q[b] / math.sqrt(r2)
+
+    def wca(a, b):
+        x = (s2[a, b] / r2) ** 3  # (sigma/r)^6
+        return 0.0 if r2 > s2[a, b] * 2 ** (1 / 3) else e4[a, b] * (x * x - x + 0.25)
+
+    assert approx(O.pair_u(spec, 0, 0, q[0], q[0], r2), coulomb(0, 0))
+    assert approx(O.pair_u(spec, 1, 1, q[1], q[1], r2), coulomb(1, 1))
+    assert wca(0, 1) > 0  # the WCA part is not trivially zero at this distance
+    assert approx(O.pair_u(spec, 0, 1, q[0], q[1], r2), coulomb(0, 1) + wca(0, 1))
+    assert O.pair_u(spec, 2, 2, 0.0, 0.0, r2 * 1.01 ** 2) == 0
+    assert O.pair_u(spec, 2, 2, 0.0, 0.0, r2 * 0.99 ** 2) == math.inf
+
+
+def test_chameleon_cuboid_consistency():
+    """Chameleon vs Cuboid (src/geometry.cpp:1320-1371, subcase "cuboid"): points
+    drawn in a box 2^(1/3) larger than the periodic cell (2, 3, 4); boundary() and
+    vdist() agree with Cuboid's (anint wrap; +-L where |d| > L/2), and
+    sqdist(a, b) = |vdist(a, b)|^2."""
+    L = np.array([2.0, 3.0, 4.0])
+    big = np.cbrt(2.0) * L
+    rng = np.random.default_rng(7)
+    a = (rng.random((100, 3)) - 0.5) * big
+    b = (rng.random((100, 3)) - 0.5) * big
+    aw, vd, sq = O.geometry(L, a, b)
+    # Cuboid::boundary / vdist (src/geometry.cpp:91-129), restated with numpy
+    anint = lambda x: np.trunc(np.where(x > 0, x + 0.5, x - 0.5))
+    cw = np.where(np.abs(a) > L / 2, a - L * anint(a / L), a)
+    d = a - b
+    cd = np.where(d > L / 2, d - L, np.where(d < -L / 2, d + L, d))
+    for x, y in ((aw, cw), (vd, cd)):
+        assert all(approx(u, v) for u, v in zip(x.ravel(), y.ravel()))
+    assert all(approx(s, float((v * v).sum())) for s, v in zip(sq, vd))
+    assert (np.abs(aw) <= L / 2 + 1e-12).all()
+
+
 def test_ewald_real_space_self_energy():
     """Real-space Ewald S = erfc(alpha r) and self energy -lB alpha/sqrt(pi) q^2,
     matching PolicyIonIon::selfEnergy (src/energy.cpp:484-518) for kappa = 0."""
