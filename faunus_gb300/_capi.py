@@ -26,7 +26,8 @@ FAU_ERR_NODEVICE = 8
 
 # pair terms / coulomb types / flags / precision / moves
 FAU_PAIR_COULOMB, FAU_PAIR_LJ, FAU_PAIR_WCA, FAU_PAIR_HS = 1, 2, 4, 8
-FAU_COUL_PLAIN, FAU_COUL_CUT, FAU_COUL_EWALD = 0, 1, 2
+FAU_COUL_PLAIN, FAU_COUL_CUT, FAU_COUL_EWALD, FAU_COUL_TRUNC = 0, 1, 2, 3
+FAU_COUL_MAX_POLY = 16
 FAU_GROUP_ATOMIC, FAU_GROUP_RIGID = 1, 2
 FAU_PREC_FP32C, FAU_PREC_FP64 = 0, 1
 FAU_MOVE_NONE, FAU_MOVE_ATOMIC, FAU_MOVE_MOLECULAR = -1, 0, 1
@@ -52,6 +53,7 @@ class SysDesc(C.Structure):
         ("pair_cutoff", C.c_double), ("cutoff_g2g", C.c_double),
         ("ewald", EwaldDesc), ("precision", C.c_int), ("cell_capacity", C.c_int),
         ("n_molids", C.c_int), ("cutoff_g2g_pairs", dptr),
+        ("coulomb_poly_n", C.c_int), ("coulomb_erfc", C.c_double), ("coulomb_poly", C.c_double * 16),
     ]
 
 

@@ -214,6 +214,17 @@ int validate(const fau_sys_desc* d)
         if (!(d->ewald.alpha > 0.0)) return fail(FAU_ERR_ARG, "ewald.alpha must be positive");
         if (d->ewald.ncutoff > 127) return fail(FAU_ERR_ARG, "ewald.ncutoff above 127");
     }
+    if (d->coulomb_type < FAU_COUL_PLAIN || d->coulomb_type > FAU_COUL_TRUNC)
+        return fail(FAU_ERR_ARG, "unknown coulomb_type %d", d->coulomb_type);
+    if (d->coulomb_type != FAU_COUL_PLAIN && (d->pair_terms & FAU_PAIR_COULOMB) && !(d->coulomb_cutoff > 0.0))
+        return fail(FAU_ERR_ARG, "coulomb_type %d needs a positive coulomb_cutoff", d->coulomb_type);
+    if (d->coulomb_type == FAU_COUL_TRUNC) {
+        if (d->coulomb_poly_n < 0 || d->coulomb_poly_n > FAU_COUL_MAX_POLY)
+            return fail(FAU_ERR_ARG, "coulomb_poly_n %d outside [0, %d]", d->coulomb_poly_n, FAU_COUL_MAX_POLY);
+        if (!std::isfinite(d->coulomb_erfc)) return fail(FAU_ERR_ARG, "non-finite coulomb_erfc");
+        for (int k = 0; k < d->coulomb_poly_n; k++)
+            if (!std::isfinite(d->coulomb_poly[k])) return fail(FAU_ERR_ARG, "non-finite coulomb_poly[%d]", k);
+    }
     if (d->cutoff_g2g_pairs) {
         if (d->n_molids < 1 || d->n_molids > 4096) return fail(FAU_ERR_ARG, "n_molids %d outside [1, 4096]", d->n_molids);
         if (!d->group_molid) return fail(FAU_ERR_ARG, "cutoff_g2g_pairs needs group_molid");
@@ -542,12 +553,22 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         }
     std::vector<float> iq(nt);
     std::vector<double> iqd(nt), iself(nt, 0.0);
-    const bool has_self = (d->pair_terms & FAU_PAIR_COULOMB) && d->coulomb_type == FAU_COUL_EWALD;
+    // self energy lB q^2 S'(0) / (2 Rc) = -1/2 lim_{r->0} (u - u~) (docs/_docs/energy.md:267-276):
+    // Ewald S'(0) = -2 alpha Rc / sqrt(pi); FAU_COUL_TRUNC S'(0) = c_1 - e 2 alpha Rc / sqrt(pi)
+    const bool has_self = (d->pair_terms & FAU_PAIR_COULOMB) &&
+                          (d->coulomb_type == FAU_COUL_EWALD || d->coulomb_type == FAU_COUL_TRUNC);
+    double self_pref = 0.0; // U_self / (lB q^2)
+    if (d->coulomb_type == FAU_COUL_EWALD) self_pref = -d->coulomb_alpha / std::sqrt(kPi);
+    if (d->coulomb_type == FAU_COUL_TRUNC) {
+        const double c1 = d->coulomb_poly_n > 1 ? d->coulomb_poly[1] : 0.0;
+        const double ds0 = c1 - d->coulomb_erfc * 2.0 * d->coulomb_alpha * d->coulomb_cutoff / std::sqrt(kPi);
+        self_pref = ds0 / (2.0 * d->coulomb_cutoff);
+    }
     for (int a = 0; a < nt; a++) {
         iq[a] = (float)lay.itype_q[a];
         iqd[a] = lay.itype_q[a];
         // NewCoulombGalore self energy for S = erfc(alpha r): -lB alpha / sqrt(pi) q^2
-        if (has_self) iself[a] = d->bjerrum_length * (-d->coulomb_alpha / std::sqrt(kPi) * iqd[a] * iqd[a]);
+        if (has_self) iself[a] = d->bjerrum_length * (self_pref * iqd[a] * iqd[a]);
     }
     h.nt = nt;
     h.terms = d->pair_terms;
@@ -559,6 +580,17 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     h.rc2_coul = (float)(d->coulomb_cutoff * d->coulomb_cutoff);
     h.alpha = (float)d->coulomb_alpha;
     h.alpha_d = d->coulomb_alpha;
+    if (d->coulomb_type == FAU_COUL_TRUNC) {
+        h.npoly = d->coulomb_poly_n;
+        for (int k = 0; k < d->coulomb_poly_n; k++) {
+            h.cpoly_d[k] = d->coulomb_poly[k];
+            h.cpoly[k] = (float)d->coulomb_poly[k];
+        }
+        h.cerfc_d = d->coulomb_erfc;
+        h.cerfc = (float)d->coulomb_erfc;
+        h.inv_rc_d = 1.0 / d->coulomb_cutoff;
+        h.inv_rc = (float)h.inv_rc_d;
+    }
     h.rc2_pair = d->pair_cutoff > 0 ? (float)(d->pair_cutoff * d->pair_cutoff) : 0.f;
     h.rc2_pair_d = d->pair_cutoff > 0 ? d->pair_cutoff * d->pair_cutoff : 0.0;
     h.cut_g2g2 = d->cutoff_g2g > 0 ? d->cutoff_g2g * d->cutoff_g2g : -1.0;

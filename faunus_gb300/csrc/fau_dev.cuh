@@ -72,6 +72,12 @@ struct DevSys {
     float lB, rc_coul, rc2_coul, alpha;
     float rc2_pair;   // 0: no truncation
     double rc2_pair_d, rc_coul_d, alpha_d, lB_d;
+    // FAU_COUL_TRUNC: S(q) = cerfc erfc(alpha r) + sum_k cpoly[k] q^k, q = r / Rc
+    int npoly;
+    float cerfc, inv_rc;
+    float cpoly[FAU_COUL_MAX_POLY];
+    double cerfc_d, inv_rc_d;
+    double cpoly_d[FAU_COUL_MAX_POLY];
     double cut_g2g2;  // group mass-centre cutoff^2 (FP64); < 0: none (with n_mol > 0: >= 0 if any pair has one)
     float cut_g2g2f;
     int n_mol;        // > 0: per molecule-kind pair cutoffs^2 below, indexed by g_molid
@@ -307,6 +313,20 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
                 const float r = __fsqrt_rn(r2);
                 c = p.qq * erfcf(S.alpha * r) * __frcp_rn(r);
             }
+            else if (S.coul_type == FAU_COUL_TRUNC) {
+                // Horner in q; the error scale is |qq/r| (|e| erfc + sum |c_k| q^k)
+                const float r = __fsqrt_rn(r2), q = r * S.inv_rc, ir = __frcp_rn(r);
+                float sp = 0.f, sa = 0.f;
+                for (int k = S.npoly - 1; k >= 0; k--) {
+                    sp = fmaf(sp, q, S.cpoly[k]);
+                    sa = fmaf(sa, q, fabsf(S.cpoly[k]));
+                }
+                float e = 0.f;
+                if (S.cerfc != 0.f) e = S.cerfc * erfcf(S.alpha * r);
+                const float pq = p.qq * ir;
+                u += pq * (sp + e);
+                m += fabsf(pq) * (sa + fabsf(e));
+            }
             else {
                 c = p.qq * rsqrtf(r2);
             }
@@ -340,6 +360,16 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
     return u;
 }
 
+// FAU_COUL_TRUNC short-range function in FP64: e erfc(alpha r) + Horner in q = r / Rc
+__device__ __forceinline__ double coul_trunc_s(const DevSys& S, double r)
+{
+    const double q = r / S.rc_coul_d;
+    double s = 0.0;
+    for (int k = S.npoly - 1; k >= 0; k--) s = s * q + S.cpoly_d[k];
+    if (S.cerfc_d != 0.0) s += S.cerfc_d * erfc(S.alpha_d * r);
+    return s;
+}
+
 // FP64 pair energy (plain form and total energy), same term order as the oracle
 __device__ __forceinline__ double pair_u64(const DevSys& S, int ta, int tb, double r2)
 {
@@ -354,7 +384,9 @@ __device__ __forceinline__ double pair_u64(const DevSys& S, int ta, int tb, doub
         else {
             const double r = sqrt(r2) + 2.220446049250313e-16;
             if (r < S.rc_coul_d) {
-                const double s = (S.coul_type == FAU_COUL_EWALD) ? erfc(S.alpha_d * r) : 1.0;
+                double s = 1.0;
+                if (S.coul_type == FAU_COUL_EWALD) s = erfc(S.alpha_d * r);
+                else if (S.coul_type == FAU_COUL_TRUNC) s = coul_trunc_s(S, r);
                 u += qq / r * s;
             }
         }

@@ -47,6 +47,97 @@ def group_cutoff(value, molecule_names: Sequence[str]) -> np.ndarray:
     return out
 
 
+def _poly_mul(a, b):
+    out = [0.0] * (len(a) + len(b) - 1)
+    for i, x in enumerate(a):
+        for j, y in enumerate(b):
+            out[i + j] += x * y
+    return out
+
+
+def _gbinom(n: int, k: int) -> float:
+    """Generalised binomial coefficient n (n-1) ... (n-k+1) / k! (n may be negative)."""
+    v = 1.0
+    for i in range(k):
+        v = v * (n - i) / (i + 1)
+    return v
+
+
+def coulomb_scheme(type: str, *, epsr: float, cutoff: float = 0.0, alpha: float = 0.0, epsrf: float = 0.0,
+                   C: int = 3, D: int = 3, order: Optional[int] = None, temperature: float = 298.15) -> dict:
+    """SystemSpec fields of a NewCoulombGalore `coulomb` block (src/potentials.cpp:1628-1700)
+    at infinite Debye length: S(q = r/Rc) of docs/_docs/energy.md:169-213 written as
+    e erfc(alpha r) + sum_k c_k q^k (FAU_COUL_TRUNC), or the plain / Ewald forms.
+
+      plain          S = 1, no cutoff
+      ewald          erfc(alpha Rc q)
+      reactionfield  1 + (epsrf - epsr)/(2 epsrf + epsr) q^3 - 3 epsrf/(2 epsrf + epsr) q
+      poisson        (1-q)^(D+1) sum_{c<C} (C-c)/C binom(D-1+c, c) q^c     (C=3, D=3)
+      qpotential     prod_{n=1..order} (1 - q^n)
+      fanourgakis    1 - 7/4 q + 21/4 q^5 - 7 q^6 + 5/2 q^7
+      fennell        erfc(alpha Rc q) - q E + (q-1) q (E + G)
+      zerodipole     erfc(alpha Rc q) - q E + (q^2-1)/2 q (E + G)
+      zahn           erfc(alpha Rc q) - (q-1) q (E + G)
+      wolf           erfc(alpha Rc q) - q E
+    with E = erfc(alpha Rc), G = 2 alpha Rc / sqrt(pi) exp(-alpha^2 Rc^2).
+    """
+    import math
+
+    lB = bjerrum_length(epsr, temperature)
+    out = {"bjerrum_length": lB, "coulomb_cutoff": float(cutoff),
+           "coulomb_alpha": float(alpha), "coulomb_erfc": 0.0, "coulomb_poly": None}
+    if type == "plain":
+        if cutoff:
+            raise ValueError("unexpected cutoff for plain: it is always infinity")
+        out.update(coulomb_type=A.FAU_COUL_PLAIN, coulomb_cutoff=0.0)
+        return out
+    if not cutoff > 0:
+        raise ValueError(f"coulomb type '{type}' needs a cutoff")
+    if type == "ewald":
+        out.update(coulomb_type=A.FAU_COUL_EWALD)
+        return out
+    E = math.erfc(alpha * cutoff)
+    G = 2 * alpha * cutoff / math.sqrt(math.pi) * math.exp(-(alpha * cutoff) ** 2)
+    e = 0.0
+    if type == "reactionfield":
+        den = 2 * epsrf + epsr
+        poly = [1.0, -3 * epsrf / den, 0.0, (epsrf - epsr) / den]
+    elif type == "poisson":
+        if C < 1 or D < -1:
+            raise ValueError("poisson needs C >= 1 and D >= -1")
+        head = [1.0]
+        for _ in range(D + 1):
+            head = _poly_mul(head, [1.0, -1.0])
+        tail = [(C - c) / C * _gbinom(D - 1 + c, c) for c in range(C)]
+        poly = _poly_mul(head, tail)
+    elif type == "qpotential":
+        if order is None or order < 1:
+            raise ValueError("qpotential needs order >= 1")
+        poly = [1.0]
+        for n in range(1, order + 1):
+            f = [0.0] * (n + 1)
+            f[0], f[n] = 1.0, -1.0
+            poly = _poly_mul(poly, f)
+    elif type == "fanourgakis":
+        poly = [1.0, -7 / 4, 0.0, 0.0, 0.0, 21 / 4, -7.0, 5 / 2]
+    elif type == "fennell":
+        e, poly = 1.0, [0.0, -E - (E + G), E + G]
+    elif type == "zerodipole":
+        e, poly = 1.0, [0.0, -E - 0.5 * (E + G), 0.0, 0.5 * (E + G)]
+    elif type == "zahn":
+        e, poly = 1.0, [0.0, E + G, -(E + G)]
+    elif type == "wolf":
+        e, poly = 1.0, [0.0, -E]
+    else:
+        raise ValueError(f"unknown coulomb type '{type}'")
+    while len(poly) > 1 and poly[-1] == 0.0:
+        poly.pop()
+    if len(poly) > A.FAU_COUL_MAX_POLY:
+        raise ValueError(f"S(q) has degree {len(poly) - 1} > {A.FAU_COUL_MAX_POLY - 1}")
+    out.update(coulomb_type=A.FAU_COUL_TRUNC, coulomb_erfc=e, coulomb_poly=np.array(poly, dtype=np.float64))
+    return out
+
+
 def bjerrum_length(epsr: float, temperature: float = 298.15) -> float:
     """Bjerrum length in angstrom (pc::bjerrumLength, src/units.h:37-41)."""
     kT = temperature * BOLTZMANN
@@ -80,6 +171,8 @@ class SystemSpec:
     bjerrum_length: float = 0.0
     coulomb_cutoff: float = 0.0
     coulomb_alpha: float = 0.0
+    coulomb_erfc: float = 0.0             # FAU_COUL_TRUNC: weight of erfc(alpha r) in S
+    coulomb_poly: Optional[np.ndarray] = None  # FAU_COUL_TRUNC: c_k of S(q) = .. + sum c_k q^k
     pair_cutoff: float = 0.0
     cutoff_g2g: float = 0.0
     cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
@@ -141,6 +234,14 @@ class SystemSpec:
         d.bjerrum_length = float(self.bjerrum_length)
         d.coulomb_cutoff = float(self.coulomb_cutoff)
         d.coulomb_alpha = float(self.coulomb_alpha)
+        d.coulomb_erfc = float(self.coulomb_erfc)
+        if self.coulomb_poly is not None:
+            cp = np.asarray(self.coulomb_poly, dtype=np.float64).reshape(-1)
+            if len(cp) > A.FAU_COUL_MAX_POLY:
+                raise ValueError("coulomb_poly has more than FAU_COUL_MAX_POLY coefficients")
+            d.coulomb_poly_n = len(cp)
+            for k, c in enumerate(cp):
+                d.coulomb_poly[k] = float(c)
         d.pair_cutoff = float(self.pair_cutoff)
         d.cutoff_g2g = float(self.cutoff_g2g)
         if self.ewald:

@@ -62,8 +62,12 @@ enum fau_pair_term {
 enum fau_coulomb_type {
     FAU_COUL_PLAIN = 0, /* S = 1, no cutoff  (Coulomb potentials.h:472-476)        */
     FAU_COUL_CUT = 1,   /* S = 1 for r < Rc, 0 beyond (poisson C=1, D=-1)         */
-    FAU_COUL_EWALD = 2  /* S = erfc(alpha r) for r < Rc, 0 beyond (kappa = 0)      */
+    FAU_COUL_EWALD = 2, /* S = erfc(alpha r) for r < Rc, 0 beyond (kappa = 0)      */
+    FAU_COUL_TRUNC = 3  /* S = e erfc(alpha r) + sum_k c_k q^k for r < Rc, 0 beyond:
+                           reactionfield, poisson, qpotential, fanourgakis, fennell,
+                           zerodipole, zahn, wolf at kappa = 0 (coulomb_poly below) */
 };
+#define FAU_COUL_MAX_POLY 16
 
 /* group flags: MoleculeData::atomic / rigid (src/molecule.h:222-279) */
 enum fau_group_flag {
@@ -123,6 +127,11 @@ typedef struct fau_sys_desc {
     const double* cutoff_g2g_pairs; /* n_molids^2 GroupCutoff::getCutoff(i, j) per molecule-kind
                                  pair (src/energy.h:746-768); <= 0 or +inf: no cutoff for
                                  that pair; NULL: cutoff_g2g for every pair                */
+    /* FAU_COUL_TRUNC: S(q) = coulomb_erfc * erfc(coulomb_alpha r) + sum_{k < coulomb_poly_n}
+       coulomb_poly[k] q^k, q = r / coulomb_cutoff; self energy lB q_i^2 S'(0) / (2 Rc)  */
+    int coulomb_poly_n;
+    double coulomb_erfc;
+    double coulomb_poly[FAU_COUL_MAX_POLY];
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */

@@ -101,6 +101,19 @@ struct PairParams {
     std::vector<double> sigma2, eps4, hs2;
     int terms = 0, coul_type = FAU_COUL_PLAIN;
     double lB = 0, rc_coul = 0, alpha = 0, pair_cutoff2 = 0;
+    // FAU_COUL_TRUNC: S(q) = cerfc erfc(alpha r) + sum_k cpoly[k] q^k (docs/_docs/energy.md:169-213
+    // at infinite Debye length; the host turns each named scheme into these coefficients)
+    double cerfc = 0;
+    std::vector<double> cpoly;
+
+    double trunc_s(double r, bool absolute) const
+    {
+        const double q = r / rc_coul;
+        double s = 0.0;
+        for (size_t k = cpoly.size(); k-- > 0;) s = s * q + (absolute ? std::fabs(cpoly[k]) : cpoly[k]);
+        if (cerfc != 0.0) s += (absolute ? std::fabs(cerfc) : cerfc) * std::erfc(alpha * r);
+        return s;
+    }
 
     double coulomb(double qa, double qb, double r2) const
     {
@@ -109,7 +122,9 @@ struct PairParams {
         // NewCoulombGalore::operator() src/potentials.h:591-598: r + epsilon, S(q), 0 beyond Rc
         const double r = std::sqrt(r2) + epsilon_dbl;
         if (r >= rc_coul) return 0.0;
-        const double s = (coul_type == FAU_COUL_EWALD) ? std::erfc(alpha * r) : 1.0;
+        double s = 1.0;
+        if (coul_type == FAU_COUL_EWALD) s = std::erfc(alpha * r);
+        else if (coul_type == FAU_COUL_TRUNC) s = trunc_s(r, false);
         return lB * (qa * qb / r * s);
     }
     double operator()(int ta, int tb, double qa, double qb, double r2) const
@@ -145,7 +160,14 @@ struct PairParams {
         if (pair_cutoff2 > 0.0 && r2 >= pair_cutoff2) return 0.0;
         const size_t ab = size_t(ta) * n_types + tb;
         double m = 0.0;
-        if (terms & FAU_PAIR_COULOMB) m += std::fabs(coulomb(qa, qb, r2));
+        if (terms & FAU_PAIR_COULOMB) {
+            if (coul_type == FAU_COUL_TRUNC) { // |qq/r| (|e| erfc + sum |c_k| q^k): S cancels to 0 at Rc
+                const double r = std::sqrt(r2) + epsilon_dbl;
+                if (r < rc_coul) m += std::fabs(lB * qa * qb / r) * trunc_s(r, true);
+            }
+            else
+                m += std::fabs(coulomb(qa, qb, r2));
+        }
         double x = sigma2[ab] / r2;
         x = x * x * x;
         const double e = std::fabs(eps4[ab]);
@@ -154,11 +176,16 @@ struct PairParams {
         return std::isfinite(m) ? m : 0.0;
     }
     // self energy per particle (NewCoulombGalore::setSelfEnergy src/potentials.cpp:1599-1604)
+    // = -1/2 lim_{r->0} (u - u~) = lB q^2 S'(0) / (2 Rc) (docs/_docs/energy.md:267-276)
     bool has_self() const { return (terms & FAU_PAIR_COULOMB) && coul_type != FAU_COUL_PLAIN; }
     double self(double q) const
     {
         if (!has_self()) return 0.0;
         if (coul_type == FAU_COUL_EWALD) return lB * (-alpha / std::sqrt(pi) * q * q);
+        if (coul_type == FAU_COUL_TRUNC) {
+            const double ds0 = (cpoly.size() > 1 ? cpoly[1] : 0.0) - cerfc * 2.0 * alpha * rc_coul / std::sqrt(pi);
+            return lB * (ds0 / (2.0 * rc_coul) * q * q);
+        }
         return 0.0; // S(q) == 1 near q = 0: no self energy
     }
 };
@@ -797,6 +824,10 @@ static System buildSystem(const fau_sys_desc* d)
     P.rc_coul = d->coulomb_cutoff;
     P.alpha = d->coulomb_alpha;
     P.pair_cutoff2 = d->pair_cutoff > 0 ? d->pair_cutoff * d->pair_cutoff : 0.0;
+    if (d->coulomb_type == FAU_COUL_TRUNC) {
+        P.cerfc = d->coulomb_erfc;
+        P.cpoly.assign(d->coulomb_poly, d->coulomb_poly + std::max(0, std::min(d->coulomb_poly_n, FAU_COUL_MAX_POLY)));
+    }
     if (d->cutoff_g2g > 0) s.cutoff_g2g2 = d->cutoff_g2g * d->cutoff_g2g;
     if (d->cutoff_g2g_pairs && d->n_molids > 0) { // GroupCutoff::getCutoff per molecule-kind pair
         s.n_molids = d->n_molids;
