@@ -103,7 +103,16 @@ class BatchParams(C.Structure):
                 ("swap_interval_moves", C.c_int), ("n_swap_blocks", C.c_int),
                 ("temperatures", dptr), ("threads", C.c_int), ("streams", C.POINTER(C.c_uint32)),
                 ("counters", C.POINTER(C.c_uint64)), ("dp_per_system", dptr), ("dprot_per_system", dptr),
-                ("cycles_out", C.POINTER(C.c_uint64))]
+                ("cycles_out", C.POINTER(C.c_uint64)), ("sampler", C.c_void_p),
+                ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int)]
+
+
+class SamplerDesc(C.Structure):
+    _fields_ = [("n_slots", C.c_int), ("rdf_type_a", C.c_int), ("rdf_type_b", C.c_int), ("rdf_dr", C.c_double),
+                ("rdf_bins", C.c_int), ("energy", C.c_int)]
+
+
+FAU_SAMPLER_MAX_BINS = 12000
 
 
 class BatchStats(C.Structure):
@@ -175,6 +184,11 @@ def _declare(lib: C.CDLL) -> None:
         "fau_get_cell_grid": ([P, iptr], C.c_int),
         "fau_get_running_energy": ([P, dptr], C.c_int),
         "fau_get_counters": ([P, C.POINTER(C.c_int64)], C.c_int),
+        "fau_sampler_create": ([P, C.POINTER(SamplerDesc), C.POINTER(P)], C.c_int),
+        "fau_sampler_destroy": ([P], C.c_int),
+        "fau_sampler_reset": ([P], C.c_int),
+        "fau_sampler_sample": ([P, C.POINTER(P), C.c_int, iptr], C.c_int),
+        "fau_sampler_read": ([P, P, dptr, P, dptr, dptr, P], C.c_int),
         "fau_set_temperature_scale": ([P, C.c_double], C.c_int),
         "fau_q_rebuild": ([P, dptr], C.c_int),
         "fau_get_q": ([P, dptr], C.c_int),

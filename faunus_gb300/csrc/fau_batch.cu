@@ -30,6 +30,10 @@ extern "C" int fau_internal_fail(int code, const char* msg);
 extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
+cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
+                                        cudaStream_t st);
+int fau_internal_sampler_slots(const fau_sampler* s);
+fau_ctx* fau_internal_sampler_ctx(const fau_sampler* s);
 
 namespace {
 
@@ -112,6 +116,15 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (cudaSetDevice(device) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "cudaSetDevice failed");
     const bool pt = P->swap_interval_moves > 0 && P->n_swap_blocks > 0;
     if (pt && !P->temperatures) return fau_internal_fail(FAU_ERR_ARG, "parallel tempering needs temperatures");
+    // blocks of moves: PT swap blocks, or sample blocks of a device sampler, or one block
+    fau_sampler* smp = P->sampler;
+    if (smp && fau_internal_sampler_ctx(smp) != ctx) return fau_internal_fail(FAU_ERR_ARG, "sampler from another context");
+    const bool sblocks = !pt && smp && P->sample_interval_moves > 0 && P->n_sample_blocks > 0;
+    if (sblocks && P->moves_per_system)
+        return fau_internal_fail(FAU_ERR_ARG, "sample blocks take a common move count (moves_per_system must be NULL)");
+    const bool blocked = pt || sblocks;
+    const long long blk_moves = pt ? P->swap_interval_moves : (sblocks ? P->sample_interval_moves : 0);
+    const int nblk = pt ? P->n_swap_blocks : (sblocks ? P->n_sample_blocks : 1);
     if (!(P->dp >= 0.0)) return fau_internal_fail(FAU_ERR_ARG, "dp must be >= 0");
 
     std::vector<DevSys*> dsys(n);
@@ -186,7 +199,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                  off_st = al(off_sum + sizeof(SysSummary) * n), off_ctr = al(off_st + 64),
                  off_ksys = al(off_ctr + 8 * n), off_knm = al(off_ksys + sizeof(DevSys*) * n),
                  off_kids = al(off_knm + 8 * n), off_kmol = al(off_kids + 4 * n), off_kctr = al(off_kmol + n),
-                 off_kdp = al(off_kctr + 8 * n), off_kdr = al(off_kdp + 8 * n), total = al(off_kdr + 8 * n);
+                 off_kdp = al(off_kctr + 8 * n), off_kdr = al(off_kdp + 8 * n), off_sslot = al(off_kdr + 8 * n),
+                 total = al(off_sslot + 4 * n);
     unsigned char* dbuf = nullptr;
     if (fau_internal_ctx_scratch(ctx, total, reinterpret_cast<void**>(&dbuf)) != FAU_OK)
         return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
@@ -218,6 +232,25 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (pt) {
         BTRY(cudaMemcpyAsync(dbuf + off_T, P->temperatures, 8 * n, cudaMemcpyHostToDevice, st));
         BTRY(cudaMemcpyAsync(dbuf + off_Tref, tref.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    }
+    int max_np = 0;
+    if (smp) {
+        const int ns = fau_internal_sampler_slots(smp);
+        std::vector<int> sslot(n);
+        for (int i = 0; i < n; i++) {
+            sslot[i] = P->sample_slots ? P->sample_slots[i] : i % ns;
+            if (sslot[i] < 0 || sslot[i] >= ns) {
+                cleanup();
+                return fau_internal_fail(FAU_ERR_ARG, "sample slot outside [0, n_slots)");
+            }
+            fau_ctx* c2;
+            int K, np, ng, mo, knc;
+            double tr;
+            DevSys* dd;
+            fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+            max_np = std::max(max_np, np);
+        }
+        BTRY(cudaMemcpyAsync(dbuf + off_sslot, sslot.data(), 4 * n, cudaMemcpyHostToDevice, st));
     }
     DevSys* const* d_sys = reinterpret_cast<DevSys* const*>(dbuf + off_sys);
     SysSummary* d_sum = reinterpret_cast<SysSummary*>(dbuf + off_sum);
@@ -266,10 +299,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     a.dp_sys = reinterpret_cast<const double*>(dbuf + off_kdp);
     a.dprot_sys = reinterpret_cast<const double*>(dbuf + off_kdr);
     if (P->counters) a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_kctr);
-    const int nblk = pt ? P->n_swap_blocks : 1;
-    if (pt) {
+    if (blocked) {
         a.n_moves = nullptr;
-        a.moves = P->swap_interval_moves;
+        a.moves = blk_moves;
     }
     else {
         a.n_moves = reinterpret_cast<const long long*>(dbuf + off_knm);
@@ -325,8 +357,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     cudaGraphExec_t exec = nullptr;
     BTRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int b = 0; b < nblk; b++) {
-        const unsigned long long cbase =
-            P->counter_base + (unsigned long long)b * (pt ? (unsigned long long)P->swap_interval_moves : 0ull);
+        const unsigned long long cbase = P->counter_base + (unsigned long long)b * (unsigned long long)blk_moves;
         if (launch_block(cbase) != cudaSuccess) {
             cudaStreamEndCapture(st, &graph);
             if (graph) cudaGraphDestroy(graph);
@@ -339,6 +370,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                                             reinterpret_cast<const double*>(dbuf + off_Tref), P->seed ^ 0x5DEECE66DULL,
                                             P->counter_base / (P->swap_interval_moves ? P->swap_interval_moves : 1) + b,
                                             reinterpret_cast<unsigned long long*>(dbuf + off_st));
+        if (smp && fau_internal_sampler_launch(smp, d_sys, n, reinterpret_cast<const int*>(dbuf + off_sslot), max_np,
+                                               st) != cudaSuccess) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cleanup();
+            return fau_internal_fail(FAU_ERR_CUDA, "sampler launch failed during capture");
+        }
     }
     BTRY(cudaStreamEndCapture(st, &graph));
     BTRY(cudaGraphInstantiate(&exec, graph, 0));

@@ -612,6 +612,7 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         h.n_mol = d->n_molids;
     }
     h.cut_g2g2f = (float)h.cut_g2g2;
+    for (size_t a = 0; a < lay.itype_type.size() && a < (size_t)kMaxITypes; a++) h.itype_type[a] = lay.itype_type[a];
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0);
     h.beta_scale = 1.0;

@@ -58,6 +58,7 @@ struct DevSys {
     float* itype_q;     // charge per internal type (FP32)
     double* itype_qd;   // FP64
     double* itype_self; // self energy per internal type (kT)
+    int itype_type[kMaxITypes]; // atom type id (Particle::id) of each internal type
 
     // groups
     int* g_begin;     // n_groups + 1

@@ -292,9 +292,13 @@ class Context:
     def run_batch(self, systems: Sequence["System"], moves=None, *, moves_per_system=None, seed: int = 1,
                   counter_base: int = 0, dp: float = 1.0, dprot: float = 0.0, swap_interval: int = 0,
                   n_swap_blocks: int = 0, temperatures=None, threads: int = 0, streams=None,
-                  counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None) -> dict:
+                  counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None,
+                  sampler: Optional["Sampler"] = None, sample_slots=None, sample_interval: int = 0,
+                  n_sample_blocks: int = 0) -> dict:
         """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
-        is a uint64 array of len(systems) that receives each system's SM cycles."""
+        is a uint64 array of len(systems) that receives each system's SM cycles.  With a
+        sampler, the systems are sampled on the device after every block of moves (the PT
+        swap blocks, or n_sample_blocks blocks of sample_interval moves, or once at the end)."""
         n = len(systems)
         arr = (C.c_void_p * n)(*[s.handle for s in systems])
         p = A.BatchParams()
@@ -332,6 +336,14 @@ class Context:
             cv = np.ascontiguousarray(counters, dtype=np.uint64)
             keep.append(cv)
             p.counters = cv.ctypes.data_as(C.POINTER(C.c_uint64))
+        if sampler is not None:
+            p.sampler = sampler.handle
+            p.sample_interval_moves = int(sample_interval)
+            p.n_sample_blocks = int(n_sample_blocks)
+            if sample_slots is not None:
+                sl = np.ascontiguousarray(sample_slots, dtype=np.int32)
+                keep.append(sl)
+                p.sample_slots = A.as_iptr(sl)
         st = A.BatchStats()
         A.check(self._lib.fau_run_batch(self.handle, arr, n, C.byref(p), C.byref(st)), "fau_run_batch")
         return st.as_dict()
@@ -538,3 +550,73 @@ class MoveGenerator:
         if self.handle:
             self._lib.fau_movegen_destroy(self.handle)
             self.handle = None
+
+
+class Sampler:
+    """Device analysis accumulators (fau_sampler): AtomRDF between atom types a and b
+    and SystemEnergy, per slot (src/analysis.cpp:339-357, 1556-1600)."""
+
+    def __init__(self, ctx: Context, n_slots: int = 1, rdf: Optional[tuple] = None, energy: bool = True):
+        """rdf = (type_a, type_b, dr, n_bins) or None."""
+        self._lib = A.lib()
+        d = A.SamplerDesc()
+        d.n_slots = int(n_slots)
+        if rdf is not None:
+            d.rdf_type_a, d.rdf_type_b, d.rdf_dr, d.rdf_bins = int(rdf[0]), int(rdf[1]), float(rdf[2]), int(rdf[3])
+        d.energy = int(bool(energy))
+        self.desc = d
+        h = C.c_void_p()
+        A.check(self._lib.fau_sampler_create(ctx.handle, C.byref(d), C.byref(h)), "fau_sampler_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.fau_sampler_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self) -> None:
+        A.check(self._lib.fau_sampler_reset(self.handle), "fau_sampler_reset")
+
+    def sample(self, systems: Sequence["System"], slots=None) -> None:
+        n = len(systems)
+        arr = (C.c_void_p * n)(*[s.handle for s in systems])
+        sl = None if slots is None else np.ascontiguousarray(slots, dtype=np.int32)
+        A.check(self._lib.fau_sampler_sample(self.handle, arr, n, None if sl is None else A.as_iptr(sl)),
+                "fau_sampler_sample")
+
+    def read(self) -> dict:
+        ns, nb = self.desc.n_slots, self.desc.rdf_bins
+        hist = np.zeros((ns, nb + 1), dtype=np.uint64)
+        vol, es, e2 = np.zeros(ns), np.zeros(ns), np.zeros(ns)
+        nr, ne = np.zeros(ns, dtype=np.int64), np.zeros(ns, dtype=np.int64)
+        A.check(self._lib.fau_sampler_read(self.handle, hist.ctypes.data if nb else None, A.as_dptr(vol),
+                                           nr.ctypes.data, A.as_dptr(es), A.as_dptr(e2), ne.ctypes.data),
+                "fau_sampler_read")
+        return {"rdf_hist": hist[:, :nb], "rdf_beyond": hist[:, nb], "rdf_volume_sum": vol, "rdf_samples": nr,
+                "energy_sum": es, "energy_sum2": e2, "energy_samples": ne}
+
+    def g_of_r(self, data: Optional[dict] = None, slots=None):
+        """(r, g) per PairFunction::_to_disk (src/analysis.cpp:724-737): r the bin's left
+        edge i dr, g = N <V> / (4 pi r^2 dr sum N) over the selected slots (default all),
+        bins with r = 0 omitted."""
+        data = data or self.read()
+        sel = slice(None) if slots is None else np.asarray(slots)
+        return rdf_normalise(data["rdf_hist"][sel].sum(0), self.desc.rdf_dr,
+                             data["rdf_volume_sum"][sel].sum() / max(1, int(data["rdf_samples"][sel].sum())))
+
+
+def rdf_normalise(hist: np.ndarray, dr: float, mean_volume: float):
+    """PairFunction::_to_disk: g(r_i) = N_i <V> / (4 pi r_i^2 dr sum_j N_j), r_i = i dr
+    (Equidistant2DTable::from_bin), skipping r = 0 (zero volume element)."""
+    hist = np.asarray(hist, dtype=np.float64)
+    r = np.arange(len(hist)) / (1.0 / dr)
+    total = hist.sum()
+    keep = r > 0
+    g = hist[keep] * mean_volume / (4.0 * np.pi * r[keep] ** 2 * dr * total)
+    return r[keep], g

@@ -184,6 +184,8 @@ typedef struct fau_run_stats {
 
 /* Parameters of a batched run over many independent systems (replicas,
  * parallel-tempering walkers or served jobs).                               */
+typedef struct fau_sampler fau_sampler; /* device analysis accumulators, see fau_sampler_create */
+
 typedef struct fau_batch_params {
     int64_t moves;            /* moves per system in this launch (when moves_per_system is NULL) */
     const int64_t* moves_per_system; /* optional per-system move counts                       */
@@ -204,6 +206,12 @@ typedef struct fau_batch_params {
     const double* dprot_per_system; /* optional per-system dprot (overrides dprot)       */
     uint64_t* cycles_out;     /* optional, n entries: SM clock cycles each system's chain
                                  took in this call (summed over swap blocks)             */
+    fau_sampler* sampler;     /* optional device analysis sampled after every block, inside
+                                 the launch's CUDA graph (no host round trip)             */
+    const int* sample_slots;  /* optional n sampler slots (default: system i -> i mod n_slots) */
+    int sample_interval_moves; /* with a sampler and no PT: blocks of this many moves per
+                                 system; under PT the swap blocks are the sample blocks   */
+    int n_sample_blocks;      /* number of sample blocks (no PT)                          */
 } fau_batch_params;
 
 typedef struct fau_batch_stats {
@@ -317,6 +325,37 @@ typedef struct fau_nonbonded_args {
     double bjerrum_length, coulomb_cutoff, coulomb_alpha, pair_cutoff;
 } fau_nonbonded_args;
 int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* args, double* energy_out, void* stream);
+
+/* ---- device analysis ------------------------------------------------------
+ * AtomRDF (src/analysis.cpp:1556-1600) and SystemEnergy (src/analysis.cpp:339-357)
+ * sampled on the device into per-slot accumulators (one slot per replica, or one
+ * slot pooling several).  AtomRDF: every pair of atoms of types a and b (i < j when
+ * a == b), |vdist| under minimum image, bin floor(r / dr) as Equidistant2DTable
+ * (src/aux/equidistant_table.h:32-39), plus the summed volume for PairFunction's
+ * normalisation g(r) = N <V> / (4 pi r^2 dr sum N) (src/analysis.cpp:724-737).
+ * SystemEnergy: sum and sum of squares of the running total energy.  Only cuboid
+ * 3-d sampling (no slicedir / thickness). */
+typedef struct fau_sampler_desc {
+    int n_slots;        /* independent accumulators                                  */
+    int rdf_type_a;     /* AtomRDF name1 / name2 as atom type ids                     */
+    int rdf_type_b;
+    double rdf_dr;      /* bin width (angstrom)                                       */
+    int rdf_bins;       /* bins kept (<= FAU_SAMPLER_MAX_BINS); 0: no RDF; farther
+                           pairs are counted in a last "beyond" column                */
+    int energy;         /* 1: sample the running total energy                         */
+} fau_sampler_desc;
+#define FAU_SAMPLER_MAX_BINS 12000
+int fau_sampler_create(fau_ctx* ctx, const fau_sampler_desc* desc, fau_sampler** out);
+int fau_sampler_destroy(fau_sampler* s);
+int fau_sampler_reset(fau_sampler* s);
+/* Sample `n` systems of the sampler's context now (asynchronous on the context's
+ * stream); slots: n slot ids, or NULL for system i -> slot i mod n_slots. */
+int fau_sampler_sample(fau_sampler* s, fau_sys* const* systems, int n, const int* slots);
+/* Copy the accumulators out (each pointer optional): rdf_hist n_slots*(rdf_bins+1)
+ * counts (last column: beyond the bins), rdf_volume_sum / rdf_samples per slot,
+ * energy_sum / energy_sum2 / energy_samples per slot. */
+int fau_sampler_read(fau_sampler* s, uint64_t* rdf_hist, double* rdf_volume_sum, int64_t* rdf_samples,
+                     double* energy_sum, double* energy_sum2, int64_t* energy_samples);
 
 /* ---- state access -------------------------------------------------------- */
 int fau_get_positions(fau_sys* sys, double* xyz_out);          /* n*3 FP64 */

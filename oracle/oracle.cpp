@@ -1052,6 +1052,36 @@ int orc_geometry(const double box[3], int n, const double* a, const double* b, d
     return FAU_OK;
 }
 
+// ---- AtomRDF histogram (src/analysis.cpp:1556-1600): pairs of atoms of types a and b
+// (i < j when a == b, AtomRDF::sampleIdentical), r = |vdist| (Chameleon, cuboid), bin
+// floor(r * (1/dr)) as Equidistant2DTable::to_bin (src/aux/equidistant_table.h:32-39);
+// bins >= n_bins are counted in hist[n_bins]
+int orc_rdf(int n, const double* pos, const int* type, const double box[3], int ta, int tb, double dr, int n_bins,
+            uint64_t* hist)
+{
+    Box B;
+    B.set(box);
+    const double dxinv = 1.0 / dr;
+    auto sample = [&](int i, int j) {
+        const Vec3 a{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, b{pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
+        const double r = std::sqrt(sqnorm(B.vdist(a, b)));
+        const long long bin = (long long)std::floor(r * dxinv);
+        hist[bin < n_bins ? bin : n_bins]++;
+    };
+    for (int i = 0; i < n; i++) {
+        if (type[i] != ta) continue;
+        if (ta == tb) {
+            for (int j = i + 1; j < n; j++)
+                if (type[j] == ta) sample(i, j);
+        }
+        else {
+            for (int j = 0; j < n; j++)
+                if (type[j] == tb) sample(i, j);
+        }
+    }
+    return FAU_OK;
+}
+
 // ---- cell grid binning (bit-exact oracle for the device cell list)
 int orc_cell_bin(const double box[3], double min_cell, int n, const double* pos, int* cells_out, int dims_out[3],
                  int offmin_out[3], int offmax_out[3])

@@ -43,6 +43,7 @@ def lib() -> C.CDLL:
             "orc_ewald_policy": ([C.c_int, A.dptr, A.dptr, A.dptr, C.c_double, C.c_double, C.c_int, C.c_double,
                                   C.c_double, C.c_int, A.dptr, A.iptr], C.c_int),
             "orc_pair_u": ([sd, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, A.dptr], C.c_int),
+            "orc_rdf": ([C.c_int, A.dptr, A.iptr, A.dptr, C.c_int, C.c_int, C.c_double, C.c_int, P], C.c_int),
             "orc_geometry": ([A.dptr, C.c_int, A.dptr, A.dptr, A.dptr, A.dptr, A.dptr], C.c_int),
             "orc_cell_bin": ([A.dptr, C.c_double, C.c_int, A.dptr, A.iptr, A.iptr, A.iptr, A.iptr], C.c_int),
             "orc_movegen_create": ([P, C.POINTER(A.MoveDesc), C.c_int, C.c_uint32, C.c_uint32, C.c_int,
@@ -212,6 +213,17 @@ def geometry(box, a, b):
     _ok(lib().orc_geometry(A.as_dptr(box), n, A.as_dptr(a.reshape(-1)), A.as_dptr(b.reshape(-1)),
                            A.as_dptr(aw.reshape(-1)), A.as_dptr(vd.reshape(-1)), A.as_dptr(sq)), "orc_geometry")
     return aw, vd, sq
+
+
+def rdf_hist(pos, types, box, ta, tb, dr, n_bins):
+    """AtomRDF pair histogram of one configuration: (n_bins,) counts and the count beyond."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    h = np.zeros(n_bins + 1, dtype=np.uint64)
+    _ok(lib().orc_rdf(len(pos), A.as_dptr(pos.reshape(-1)), A.as_iptr(types), A.as_dptr(box), ta, tb, dr, n_bins,
+                      h.ctypes.data), "orc_rdf")
+    return h[:n_bins], int(h[n_bins])
 
 
 def cell_bin(box, min_cell, pos):
