@@ -6,7 +6,7 @@ C ABI of ``include/fau_gpu.h``); this package is its Python host API.
 from . import _capi
 from ._capi import FauError
 from .system import (Context, MoveGenerator, Sampler, System, SystemSpec, bjerrum_length, footprint,
-                     group_cutoff, coulomb_scheme, kjmol_to_kt, move_descs)
+                     group_cutoff, coulomb_scheme, kjmol_to_kt, move_descs, pressure_kt)
 
 __all__ = ["Context", "Sampler", "System", "SystemSpec", "MoveGenerator", "FauError", "bjerrum_length",
-           "kjmol_to_kt", "footprint", "group_cutoff", "coulomb_scheme", "move_descs", "_capi"]
+           "kjmol_to_kt", "footprint", "group_cutoff", "coulomb_scheme", "move_descs", "pressure_kt", "_capi"]

@@ -28,6 +28,7 @@ FAU_ERR_NODEVICE = 8
 FAU_PAIR_COULOMB, FAU_PAIR_LJ, FAU_PAIR_WCA, FAU_PAIR_HS = 1, 2, 4, 8
 FAU_COUL_PLAIN, FAU_COUL_CUT, FAU_COUL_EWALD, FAU_COUL_TRUNC = 0, 1, 2, 3
 FAU_COUL_MAX_POLY = 16
+FAU_VOLUME_ISOTROPIC, FAU_VOLUME_XY, FAU_VOLUME_Z, FAU_VOLUME_ISOCHORIC = 0, 1, 2, 3
 FAU_GROUP_ATOMIC, FAU_GROUP_RIGID = 1, 2
 FAU_PREC_FP32C, FAU_PREC_FP64 = 0, 1
 FAU_MOVE_NONE, FAU_MOVE_ATOMIC, FAU_MOVE_MOLECULAR = -1, 0, 1
@@ -184,6 +185,8 @@ def _declare(lib: C.CDLL) -> None:
         "fau_get_cell_grid": ([P, iptr], C.c_int),
         "fau_get_running_energy": ([P, dptr], C.c_int),
         "fau_get_counters": ([P, C.POINTER(C.c_int64)], C.c_int),
+        "fau_get_box": ([P, dptr], C.c_int),
+        "fau_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.c_double, C.POINTER(TrialResult)], C.c_int),
         "fau_sampler_create": ([P, C.POINTER(SamplerDesc), C.POINTER(P)], C.c_int),
         "fau_sampler_destroy": ([P], C.c_int),
         "fau_sampler_reset": ([P], C.c_int),

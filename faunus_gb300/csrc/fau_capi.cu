@@ -13,6 +13,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -95,7 +96,41 @@ struct fau_sys {
     int* d_flags = nullptr;
     DevSys** d_self = nullptr; // device array holding `d` (chain kernel argument)
     bool pending = false;      // a fau_energy_change trial waits for fau_commit_pending
+    std::shared_ptr<const struct DescStore> desc; // the creating descriptor (volume moves rebuild from it)
 };
+
+// A host copy of a fau_sys_desc with its arrays (positions and mass centres excluded:
+// they live on the device).  Shared by clones.
+struct DescStore {
+    fau_sys_desc d{};
+    std::vector<double> charge, type_mass, sigma2, eps4, hs2, cut_pairs;
+    std::vector<int> type, group_begin, group_molid, group_flags;
+};
+
+static std::shared_ptr<const DescStore> store_desc(const fau_sys_desc* d)
+{
+    auto st = std::make_shared<DescStore>();
+    const size_t n = d->n_particles, g = d->n_groups, nt = d->n_types;
+    auto cp = [](auto& v, const auto* p, size_t k) {
+        if (p) v.assign(p, p + k);
+        return p ? v.data() : nullptr;
+    };
+    st->d = *d;
+    st->d.pos = nullptr;
+    st->d.group_mass_center = nullptr;
+    st->d.charge = cp(st->charge, d->charge, n);
+    st->d.type = cp(st->type, d->type, n);
+    st->d.group_begin = cp(st->group_begin, d->group_begin, g + 1);
+    st->d.group_molid = cp(st->group_molid, d->group_molid, g);
+    st->d.group_flags = cp(st->group_flags, d->group_flags, g);
+    st->d.type_mass = cp(st->type_mass, d->type_mass, nt);
+    st->d.sigma2 = cp(st->sigma2, d->sigma2, nt * nt);
+    st->d.eps4 = cp(st->eps4, d->eps4, nt * nt);
+    st->d.hs_sigma2 = cp(st->hs2, d->hs_sigma2, nt * nt);
+    const size_t nm = d->cutoff_g2g_pairs && d->n_molids > 0 ? (size_t)d->n_molids * d->n_molids : 0;
+    st->d.cutoff_g2g_pairs = nm ? cp(st->cut_pairs, d->cutoff_g2g_pairs, nm) : nullptr;
+    return st;
+}
 
 template <class T>
 static int dev_alloc(fau_sys* s, T** p, size_t count)
@@ -717,6 +752,7 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
             return bail(fail(FAU_ERR_CUDA, "q rebuild launch failed"));
     }
     if ((rc = refresh_energy(s))) return bail(rc);
+    s->desc = store_desc(d);
     *out = s;
     return FAU_OK;
 }
@@ -1267,6 +1303,191 @@ int fau_trial_group(fau_sys* s, int group, const double dr[3], const double quat
     return rc;
 }
 
+// ---------------------------------------------------------------- volume move
+namespace {
+// Chameleon::boundary for a cuboid (src/geometry.h:407-427) with the given box
+inline void wrap1(double& a, double L, double half, double inv)
+{
+    if (std::fabs(a) > half) {
+        const double t = a * inv;
+        a -= L * (int)(t > 0.0 ? t + 0.5 : t - 0.5);
+    }
+}
+} // namespace
+
+int fau_volume_move(fau_sys* s, double new_volume, int method, double pressure, double u01, fau_trial_result* out)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null system");
+    if (!(new_volume > 0.0) || !std::isfinite(new_volume)) return fail(FAU_ERR_ARG, "new volume must be positive");
+    if (method < FAU_VOLUME_ISOTROPIC || method > FAU_VOLUME_ISOCHORIC)
+        return fail(FAU_ERR_ARG, "unknown volume scaling method %d", method);
+    if (!std::isfinite(pressure)) return fail(FAU_ERR_ARG, "non-finite pressure");
+    if (s->pending) return fail(FAU_ERR_STATE, "volume move with a pending trial");
+    if (!s->desc) return fail(FAU_ERR_STATE, "system has no descriptor to rebuild from");
+    fau_ctx* ctx = s->ctx;
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    // the accepted state's energy
+    fau_energy_terms eo;
+    int rc = compute_total(s, &eo);
+    if (rc) return rc;
+    const int n = s->n, G = s->n_groups;
+    std::vector<double> x(n), y(n), z(n), cm(3 * (size_t)G);
+    DevSys cur;
+    CUDA_TRY(cudaMemcpyAsync(x.data(), s->h.x, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(y.data(), s->h.y, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(z.data(), s->h.z, 8 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(cm.data(), s->h.g_cm, 8 * 3 * (size_t)G, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&cur, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    // Cuboid::setVolume (src/geometry.cpp:57-90)
+    const double* L = s->h.L;
+    const double v_old = L[0] * L[1] * L[2];
+    double sc[3], v_target = new_volume;
+    switch (method) {
+    case FAU_VOLUME_ISOTROPIC: {
+        const double a = std::cbrt(new_volume / v_old);
+        sc[0] = sc[1] = sc[2] = a;
+        break;
+    }
+    case FAU_VOLUME_XY: {
+        const double a = std::sqrt(new_volume / v_old);
+        sc[0] = sc[1] = a;
+        sc[2] = 1.0;
+        break;
+    }
+    case FAU_VOLUME_Z:
+        sc[0] = sc[1] = 1.0;
+        sc[2] = new_volume / v_old;
+        break;
+    default: {
+        const double a = std::cbrt(new_volume / v_old);
+        sc[0] = sc[1] = a;
+        sc[2] = 1 / (a * a);
+        v_target = v_old;
+        break;
+    }
+    }
+    (void)v_target;
+    double Ln[3], hn[3], in[3];
+    for (int k = 0; k < 3; k++) {
+        Ln[k] = L[k] * sc[k];
+        hn[k] = 0.5 * Ln[k];
+        in[k] = 1.0 / Ln[k];
+    }
+    // Space::scaleVolume (src/space.cpp:249-301)
+    std::vector<double> pos(3 * (size_t)n), cmn(cm);
+    int n_count = 0; // Isobaric: particles of atomic groups + molecular groups
+    for (int g = 0; g < G; g++) {
+        const int b = s->g_begin[g], e = s->g_begin[g + 1];
+        if (e == b) continue;
+        if (s->g_flags[g] & FAU_GROUP_ATOMIC) {
+            n_count += e - b;
+            for (int i = b; i < e; i++) {
+                double p[3] = {x[i] * sc[0], y[i] * sc[1], z[i] * sc[2]};
+                for (int k = 0; k < 3; k++) {
+                    wrap1(p[k], Ln[k], hn[k], in[k]);
+                    pos[3 * (size_t)i + k] = p[k];
+                }
+            }
+        }
+        else {
+            n_count += 1;
+            double c[3], dc[3];
+            for (int k = 0; k < 3; k++) {
+                c[k] = cm[3 * (size_t)g + k] * sc[k];
+                wrap1(c[k], Ln[k], hn[k], in[k]);
+                dc[k] = c[k] - cm[3 * (size_t)g + k];
+                cmn[3 * (size_t)g + k] = c[k];
+            }
+            for (int i = b; i < e; i++) {
+                const double p0[3] = {x[i], y[i], z[i]};
+                for (int k = 0; k < 3; k++) {
+                    // Group::unwrap (src/group.h:349-356): cm + vdist(p, cm) in the old box
+                    double d = p0[k] - cm[3 * (size_t)g + k];
+                    if (d > s->h.half[k]) d -= L[k];
+                    else if (d < -s->h.half[k]) d += L[k];
+                    double p = cm[3 * (size_t)g + k] + d;
+                    p += dc[k];
+                    wrap1(p, Ln[k], hn[k], in[k]);
+                    pos[3 * (size_t)i + k] = p;
+                }
+            }
+        }
+    }
+    // the trial state: the same system rebuilt for the new box (k-vectors, A_k, cells,
+    // fixed-point records, full Q(k) in FP64, FP64 total energy)
+    fau_sys_desc nd = s->desc->d;
+    for (int k = 0; k < 3; k++) nd.box[k] = Ln[k];
+    nd.pos = pos.data();
+    nd.group_mass_center = cmn.data();
+    fau_sys* t = nullptr;
+    if ((rc = fau_sys_create(ctx, &nd, &t))) return rc;
+    auto drop = [&](fau_sys* q) {
+        cudaStreamSynchronize(st);
+        free_sys(q);
+        delete q;
+    };
+    fau_energy_terms en;
+    if ((rc = compute_total(t, &en))) {
+        drop(t);
+        return rc;
+    }
+    const double v_new = Ln[0] * Ln[1] * Ln[2];
+    // Isobaric::energy first, then the Hamiltonian's terms (inf / NaN propagate)
+    const double uo = (pressure * v_old - (double)(n_count + 1) * std::log(v_old)) + eo.total;
+    const double un = (pressure * v_new - (double)(n_count + 1) * std::log(v_new)) + en.total;
+    // getEnergyChange (src/montecarlo.cpp:193-209)
+    const double inf = std::numeric_limits<double>::infinity();
+    double du;
+    if (std::isnan(uo) && !std::isnan(un)) du = -inf;
+    else if (std::isnan(un)) du = inf;
+    else if (un >= inf) du = inf;
+    else if (uo >= inf) du = -inf;
+    else du = un - uo;
+    if (std::isnan(du)) {
+        drop(t);
+        return fail(FAU_ERR_NAN, "Metropolis error: energy cannot be NaN");
+    }
+    // metropolisCriterion (src/montecarlo.cpp:17-34)
+    const double xb = du * cur.beta_scale;
+    bool acc;
+    if (std::isinf(xb) && xb < 0) acc = true;
+    else if (-xb > 709.782712893384) acc = true;
+    else acc = u01 <= std::exp(-xb);
+    if (out) {
+        out->du = du;
+        out->du_nonbonded = en.nonbonded - eo.nonbonded;
+        out->du_ewald = (en.ewald_rec + en.ewald_surf) - (eo.ewald_rec + eo.ewald_surf);
+        out->err_scale = std::fabs(un) + std::fabs(uo);
+        out->accepted = acc;
+        out->new_inf = un >= inf;
+        out->old_inf = uo >= inf;
+        out->pad = 0;
+    }
+    // counters and PT temperature carried by whichever state is kept
+    cur.moves += 1;
+    if (acc) cur.accepted += 1;
+    fau_sys* keep = acc ? t : s;
+    DevSys* dk = keep->d;
+    CUDA_TRY(cudaMemcpyAsync(&dk->moves, &cur.moves, sizeof(cur.moves), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&dk->accepted, &cur.accepted, sizeof(cur.accepted), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&dk->pair_evals, &cur.pair_evals, sizeof(cur.pair_evals), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&dk->k_updates, &cur.k_updates, sizeof(cur.k_updates), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&dk->cycles, &cur.cycles, sizeof(cur.cycles), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(&dk->beta_scale, &cur.beta_scale, sizeof(double), cudaMemcpyHostToDevice, st));
+    if (acc) {
+        const double sdu = cur.sum_du + du;
+        CUDA_TRY(cudaMemcpyAsync(&dk->sum_du, &sdu, sizeof(double), cudaMemcpyHostToDevice, st));
+        // the caller's handle now holds the trial state; the old state's blocks go to the pool
+        t->desc = s->desc;
+        std::swap(*s, *t);
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    drop(t);
+    return pull_state(s);
+}
+
 // internal accessors used by fau_batch.cu (not part of the public header)
 int fau_internal_ctx_stream(fau_ctx* c, cudaStream_t* st, int* device)
 {
@@ -1411,6 +1632,13 @@ int fau_get_cell_grid(const fau_sys* s, int dims[3])
 {
     if (!s || !dims) return fail(FAU_ERR_ARG, "null argument");
     for (int k = 0; k < 3; k++) dims[k] = s->cells ? s->h.cdim[k] : 0;
+    return FAU_OK;
+}
+
+int fau_get_box(const fau_sys* s, double* box)
+{
+    if (!s || !box) return fail(FAU_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; k++) box[k] = s->h.L[k];
     return FAU_OK;
 }
 

@@ -138,6 +138,17 @@ def coulomb_scheme(type: str, *, epsr: float, cutoff: float = 0.0, alpha: float 
     return out
 
 
+def pressure_kt(value: float, unit: str, temperature: float = 298.15) -> float:
+    """Isobaric pressure in kT / A^3 (Isobaric::pressure_units, src/energy.cpp:903-908;
+    src/units.h:162-190: Pa / kT / 1 m^3, atm = 101325 Pa, bar = 1e5 Pa, mM = 1e-3 mol/l)."""
+    kT = BOLTZMANN * temperature
+    conv = {"P/kT": 1.0, "P/Pa": 1.0 / kT / 1e30, "P/atm": 101325.0 / kT / 1e30, "P/bar": 1e5 / kT / 1e30,
+            "P/mM": 1e-3 * AVOGADRO / 1e27}
+    if unit not in conv:
+        raise ValueError(f"unknown pressure unit '{unit}'")
+    return value * conv[unit]
+
+
 def bjerrum_length(epsr: float, temperature: float = 298.15) -> float:
     """Bjerrum length in angstrom (pc::bjerrumLength, src/units.h:37-41)."""
     kT = temperature * BOLTZMANN
@@ -482,6 +493,21 @@ class System:
 
     def accepted_moves(self) -> int:
         return self.counters()["accepted"]
+
+    def box(self) -> np.ndarray:
+        out = np.zeros(3)
+        A.check(self._lib.fau_get_box(self.handle, A.as_dptr(out)), "fau_get_box")
+        return out
+
+    def volume_move(self, new_volume: float, u: float, pressure: float = 0.0, method: str = "isotropic") -> dict:
+        """One VolumeMove to `new_volume` with the Isobaric term at `pressure` (kT/A^3, see
+        `pressure_kt`) and Metropolis uniform `u` (fau_volume_move)."""
+        m = {"isotropic": A.FAU_VOLUME_ISOTROPIC, "xy": A.FAU_VOLUME_XY, "z": A.FAU_VOLUME_Z,
+             "isochoric": A.FAU_VOLUME_ISOCHORIC}[method]
+        r = A.TrialResult()
+        A.check(self._lib.fau_volume_move(self.handle, float(new_volume), m, float(pressure), float(u), C.byref(r)),
+                "fau_volume_move")
+        return r.as_dict()
 
     def set_temperature_scale(self, scale: float) -> None:
         A.check(self._lib.fau_set_temperature_scale(self.handle, float(scale)), "fau_set_temperature_scale")

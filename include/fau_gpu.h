@@ -326,6 +326,27 @@ typedef struct fau_nonbonded_args {
 } fau_nonbonded_args;
 int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* args, double* energy_out, void* stream);
 
+/* ---- volume move ----------------------------------------------------------
+ * VolumeMove + Isobaric + Metropolis (src/move.cpp:994-1006, src/energy.cpp:884-901,
+ * src/montecarlo.cpp:139-187): the box is scaled to `new_volume` as
+ * Space::scaleVolume (src/space.cpp:249-301) -- atomic groups scale every position,
+ * molecular groups are unwrapped about their mass centre, the mass centre scaled and
+ * the atoms translated with it; boundary() in the new box -- the trial state's full
+ * energy (Nonbonded, Ewald with the new box's k-vectors and a full Q(k) update,
+ * self) is computed on the device in FP64, the Isobaric term P V - (N + 1) ln V is
+ * added to both states (N: particles of atomic groups plus molecular groups; P in
+ * kT / A^3), and the move is accepted on u01 <= exp(-dU).  On acceptance the system
+ * holds the new state (its tables rebuilt for the new box); on rejection it is
+ * unchanged.  The running energy excludes the Isobaric term. */
+enum fau_volume_method {
+    FAU_VOLUME_ISOTROPIC = 0, /* Cuboid::setVolume (src/geometry.cpp:57-90) */
+    FAU_VOLUME_XY = 1,
+    FAU_VOLUME_Z = 2,
+    FAU_VOLUME_ISOCHORIC = 3
+};
+int fau_volume_move(fau_sys* sys, double new_volume, int method, double pressure, double u01,
+                    fau_trial_result* out);
+
 /* ---- device analysis ------------------------------------------------------
  * AtomRDF (src/analysis.cpp:1556-1600) and SystemEnergy (src/analysis.cpp:339-357)
  * sampled on the device into per-slot accumulators (one slot per replica, or one
@@ -362,6 +383,7 @@ int fau_get_positions(fau_sys* sys, double* xyz_out);          /* n*3 FP64 */
 int fau_get_mass_centers(fau_sys* sys, double* xyz_out);       /* n_groups*3 */
 int fau_get_cells(fau_sys* sys, int* cell_out);                /* n cell index or -1 */
 int fau_get_cell_grid(const fau_sys* sys, int dims_out[3]);
+int fau_get_box(const fau_sys* sys, double box_out[3]);         /* cuboid side lengths */
 int fau_get_running_energy(fau_sys* sys, double* energy_out);  /* FP64 running total */
 /* Move counters since the system was created: {moves, accepted, pair
  * evaluations, k-vector updates} (Move::number_of_attempted_moves and

@@ -956,6 +956,14 @@ int orc_get_positions(orc_sys* h, double* xyz)
     }
     return FAU_OK;
 }
+int orc_get_box(orc_sys* h, double* box)
+{
+    box[0] = h->s.box.len.x;
+    box[1] = h->s.box.len.y;
+    box[2] = h->s.box.len.z;
+    return FAU_OK;
+}
+
 int orc_get_mass_centers(orc_sys* h, double* xyz)
 {
     for (size_t g = 0; g < h->s.cm.size(); g++) {
@@ -1048,6 +1056,96 @@ int orc_geometry(const double box[3], int n, const double* a, const double* b, d
             a_wrapped[3 * i + k] = p[k];
             vd[3 * i + k] = d[k];
         }
+    }
+    return FAU_OK;
+}
+
+// ---- VolumeMove + Isobaric + Metropolis (src/move.cpp:994-1006, src/energy.cpp:884-901,
+// src/montecarlo.cpp:139-187); the box scaled as Cuboid::setVolume (src/geometry.cpp:57-90) and
+// the particles as Space::scaleVolume (src/space.cpp:249-301); the trial state's Ewald gets
+// updateBox + a full Q update (Ewald::updateState with volume_change)
+int orc_volume_move(orc_sys* h, double new_volume, int method, double pressure, double u01, fau_trial_result* r)
+{
+    System& s = h->s;
+    const Terms eo = energyOf(s, CH_EVERYTHING, 0);
+    System t = s;
+    const double v_old = s.box.volume();
+    Vec3 sc{1, 1, 1};
+    if (method == FAU_VOLUME_ISOTROPIC) {
+        const double a = std::cbrt(new_volume / v_old);
+        sc = {a, a, a};
+    }
+    else if (method == FAU_VOLUME_XY) {
+        const double a = std::sqrt(new_volume / v_old);
+        sc = {a, a, 1.0};
+    }
+    else if (method == FAU_VOLUME_Z) {
+        sc = {1.0, 1.0, new_volume / v_old};
+    }
+    else {
+        const double a = std::cbrt(new_volume / v_old);
+        sc = {a, a, 1 / (a * a)};
+    }
+    const double Ln[3] = {s.box.len.x * sc.x, s.box.len.y * sc.y, s.box.len.z * sc.z};
+    t.box.set(Ln);
+    int n_count = 0;
+    for (size_t g = 0; g < s.groups.size(); g++) {
+        const Group& G = s.groups[g];
+        if (G.size() == 0) continue;
+        if (G.atomic()) {
+            n_count += G.size();
+            for (int i = G.begin; i < G.end; i++) {
+                Vec3 p{s.pos[i].x * sc.x, s.pos[i].y * sc.y, s.pos[i].z * sc.z};
+                t.box.boundary(p);
+                t.pos[i] = p;
+            }
+        }
+        else {
+            n_count += 1;
+            const Vec3 c0 = s.cm[g];
+            Vec3 c{c0.x * sc.x, c0.y * sc.y, c0.z * sc.z};
+            t.box.boundary(c);
+            t.cm[g] = c;
+            const Vec3 dc{c.x - c0.x, c.y - c0.y, c.z - c0.z};
+            for (int i = G.begin; i < G.end; i++) {
+                const Vec3 d = s.box.vdist(s.pos[i], c0); // Group::unwrap (src/group.h:349-356)
+                Vec3 p{c0.x + d.x, c0.y + d.y, c0.z + d.z};
+                p = {p.x + dc.x, p.y + dc.y, p.z + dc.z};
+                t.box.boundary(p);
+                t.pos[i] = p;
+            }
+        }
+    }
+    if (t.ewald.enabled) {
+        t.ewald.updateBox(t.box);
+        t.ewald.fullQ(t.pos, t.q);
+    }
+    const Terms en = energyOf(t, CH_EVERYTHING, 0);
+    const double v_new = t.box.volume();
+    auto total = [&](const Terms& e, double v) { // Isobaric first, then the Hamiltonian's terms
+        std::vector<double> list{pressure * v - double(n_count + 1) * std::log(v)};
+        if (s.pair.has_self()) list.push_back(e.self);
+        list.push_back(e.nb);
+        if (s.ewald.enabled) list.push_back(e.surf + e.rec);
+        return accumulateTerms(list.data(), (int)list.size());
+    };
+    const double uo = total(eo, v_old), un = total(en, v_new);
+    const double du = getEnergyChange(un, uo);
+    const int acc = metropolis(du, u01);
+    if (acc < 0) return FAU_ERR_NAN;
+    if (r) {
+        r->du = du;
+        r->du_nonbonded = en.nb - eo.nb;
+        r->du_ewald = (en.rec + en.surf) - (eo.rec + eo.surf);
+        r->err_scale = std::fabs(un) + std::fabs(uo);
+        r->accepted = acc;
+        r->new_inf = un >= infty;
+        r->old_inf = uo >= infty;
+        r->pad = 0;
+    }
+    if (acc) {
+        t.sum_of_energy_changes += du;
+        s = std::move(t);
     }
     return FAU_OK;
 }
