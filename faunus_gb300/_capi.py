@@ -31,7 +31,7 @@ FAU_COUL_MAX_POLY = 16
 FAU_VOLUME_ISOTROPIC, FAU_VOLUME_XY, FAU_VOLUME_Z, FAU_VOLUME_ISOCHORIC = 0, 1, 2, 3
 FAU_GROUP_ATOMIC, FAU_GROUP_RIGID = 1, 2
 FAU_PREC_FP32C, FAU_PREC_FP64 = 0, 1
-FAU_MOVE_NONE, FAU_MOVE_ATOMIC, FAU_MOVE_MOLECULAR = -1, 0, 1
+FAU_MOVE_NONE, FAU_MOVE_ATOMIC, FAU_MOVE_MOLECULAR, FAU_MOVE_VOLUME = -1, 0, 1, 2
 
 dptr = C.POINTER(C.c_double)
 iptr = C.POINTER(C.c_int)
@@ -55,6 +55,7 @@ class SysDesc(C.Structure):
         ("ewald", EwaldDesc), ("precision", C.c_int), ("cell_capacity", C.c_int),
         ("n_molids", C.c_int), ("cutoff_g2g_pairs", dptr),
         ("coulomb_poly_n", C.c_int), ("coulomb_erfc", C.c_double), ("coulomb_poly", C.c_double * 16),
+        ("isobaric", C.c_int), ("pressure", C.c_double),
     ]
 
 
@@ -128,7 +129,7 @@ class BatchStats(C.Structure):
 class MoveDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("repeat", C.c_double), ("dp", C.c_double), ("dprot", C.c_double),
                 ("dir", C.c_double * 3), ("n_groups", C.c_int), ("groups", iptr),
-                ("type_dp", dptr), ("type_dprot", dptr)]
+                ("type_dp", dptr), ("type_dprot", dptr), ("volume_method", C.c_int)]
 
 
 FAU_NOALLOC_MAX_PARTICLES = 65536
@@ -186,7 +187,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_get_running_energy": ([P, dptr], C.c_int),
         "fau_get_counters": ([P, C.POINTER(C.c_int64)], C.c_int),
         "fau_get_box": ([P, dptr], C.c_int),
-        "fau_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.c_double, C.POINTER(TrialResult)], C.c_int),
+        "fau_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.POINTER(TrialResult)], C.c_int),
         "fau_sampler_create": ([P, C.POINTER(SamplerDesc), C.POINTER(P)], C.c_int),
         "fau_sampler_destroy": ([P], C.c_int),
         "fau_sampler_reset": ([P], C.c_int),

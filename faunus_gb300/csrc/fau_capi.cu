@@ -271,6 +271,7 @@ int validate(const fau_sys_desc* d)
     }
     if (d->precision != FAU_PREC_FP32C && d->precision != FAU_PREC_FP64)
         return fail(FAU_ERR_ARG, "unknown precision %d", d->precision);
+    if (d->isobaric && !std::isfinite(d->pressure)) return fail(FAU_ERR_ARG, "non-finite Isobaric pressure");
     return FAU_OK;
 }
 
@@ -1080,10 +1081,59 @@ static int run_chain(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, dou
 static int plain_trial(fau_sys* s, int kind, int index, const double dr[3], const double* quat, double u01,
                        fau_trial_result* out);
 
+static int run_segment(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats);
+
+// Volume proposals split the stream: the chain runs the moves between them and
+// fau_volume_move performs each volume move in order.
 int fau_run_proposals(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats)
 {
     if (!s || (!p && n > 0)) return fail(FAU_ERR_ARG, "null argument");
     CUDA_TRY(cudaSetDevice(s->ctx->device));
+    int first_vol = -1;
+    for (int m = 0; m < n && first_vol < 0; m++)
+        if (p[m].kind == FAU_MOVE_VOLUME) first_vol = m;
+    if (first_vol < 0) return run_segment(s, p, n, acc, du, stats);
+    fau_run_stats tot{};
+    auto add = [&](const fau_run_stats& x) {
+        tot.moves += x.moves;
+        tot.accepted += x.accepted;
+        tot.pair_evals += x.pair_evals;
+        tot.k_updates += x.k_updates;
+        tot.energy_change += x.energy_change;
+        tot.max_rel_err = std::max(tot.max_rel_err, x.max_rel_err);
+        tot.device_ms += x.device_ms;
+    };
+    int a = 0, rc = FAU_OK;
+    for (int m = first_vol; m <= n; m++) {
+        if (m < n && p[m].kind != FAU_MOVE_VOLUME) continue;
+        if (m > a) {
+            fau_run_stats seg{};
+            if ((rc = run_segment(s, p + a, m - a, acc ? acc + a : nullptr, du ? du + a : nullptr, &seg))) return rc;
+            add(seg);
+        }
+        if (m == n) break;
+        const double* L = s->h.L;
+        const double v_new = std::exp(std::log(L[0] * L[1] * L[2]) + p[m].dr[0]);
+        fau_trial_result r{};
+        if ((rc = fau_volume_move(s, v_new, p[m].index, p[m].u, &r))) return rc;
+        if (acc) acc[m] = (uint8_t)r.accepted;
+        if (du) du[m] = r.du;
+        fau_run_stats one{};
+        one.moves = 1;
+        one.accepted = r.accepted;
+        one.energy_change = r.accepted ? r.du : 0.0;
+        add(one);
+        a = m + 1;
+    }
+    if (stats) {
+        tot.energy = s->h.energy;
+        *stats = tot;
+    }
+    return FAU_OK;
+}
+
+static int run_segment(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats)
+{
     if (s->precision != FAU_PREC_FP64) return run_chain(s, p, n, acc, du, nullptr, stats);
     // plain FP64 form: one move per call, host Metropolis
     int rc = pull_state(s);
@@ -1315,15 +1365,16 @@ inline void wrap1(double& a, double L, double half, double inv)
 }
 } // namespace
 
-int fau_volume_move(fau_sys* s, double new_volume, int method, double pressure, double u01, fau_trial_result* out)
+int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_trial_result* out)
 {
     if (!s) return fail(FAU_ERR_ARG, "null system");
     if (!(new_volume > 0.0) || !std::isfinite(new_volume)) return fail(FAU_ERR_ARG, "new volume must be positive");
     if (method < FAU_VOLUME_ISOTROPIC || method > FAU_VOLUME_ISOCHORIC)
         return fail(FAU_ERR_ARG, "unknown volume scaling method %d", method);
-    if (!std::isfinite(pressure)) return fail(FAU_ERR_ARG, "non-finite pressure");
     if (s->pending) return fail(FAU_ERR_STATE, "volume move with a pending trial");
     if (!s->desc) return fail(FAU_ERR_STATE, "system has no descriptor to rebuild from");
+    const bool isobaric = s->desc->d.isobaric != 0;
+    const double pressure = s->desc->d.pressure;
     fau_ctx* ctx = s->ctx;
     CUDA_TRY(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
@@ -1435,8 +1486,9 @@ int fau_volume_move(fau_sys* s, double new_volume, int method, double pressure, 
     }
     const double v_new = Ln[0] * Ln[1] * Ln[2];
     // Isobaric::energy first, then the Hamiltonian's terms (inf / NaN propagate)
-    const double uo = (pressure * v_old - (double)(n_count + 1) * std::log(v_old)) + eo.total;
-    const double un = (pressure * v_new - (double)(n_count + 1) * std::log(v_new)) + en.total;
+    auto iso = [&](double v) { return isobaric ? pressure * v - (double)(n_count + 1) * std::log(v) : 0.0; };
+    const double uo = iso(v_old) + eo.total;
+    const double un = iso(v_new) + en.total;
     // getEnergyChange (src/montecarlo.cpp:193-209)
     const double inf = std::numeric_limits<double>::infinity();
     double du;

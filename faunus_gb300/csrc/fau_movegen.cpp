@@ -56,7 +56,7 @@ V3 unit_vector(Rng& r, const double dir[3])
 }
 
 struct MoveDef {
-    int kind;
+    int kind, volume_method = 0;
     double repeat, dp, dprot;
     double dir[3];
     std::vector<int> groups;
@@ -88,17 +88,21 @@ int fau_movegen_create(const fau_sys_desc* sp, const fau_move_desc* moves, int n
     std::vector<double> w;
     for (int m = 0; m < n_moves; m++) {
         const fau_move_desc& d = moves[m];
-        if ((d.kind != FAU_MOVE_ATOMIC && d.kind != FAU_MOVE_MOLECULAR) || d.n_groups < 1 || !d.groups) {
+        const bool vol = d.kind == FAU_MOVE_VOLUME;
+        if ((d.kind != FAU_MOVE_ATOMIC && d.kind != FAU_MOVE_MOLECULAR && !vol) ||
+            (!vol && (d.n_groups < 1 || !d.groups)) ||
+            (vol && (d.volume_method < FAU_VOLUME_ISOTROPIC || d.volume_method > FAU_VOLUME_ISOCHORIC))) {
             delete g;
             return fau_internal_fail(FAU_ERR_ARG, "invalid move description");
         }
         MoveDef md;
         md.kind = d.kind;
+        md.volume_method = d.volume_method;
         md.repeat = d.repeat;
         md.dp = d.dp;
         md.dprot = d.dprot;
         for (int k = 0; k < 3; k++) md.dir[k] = d.dir[k];
-        md.groups.assign(d.groups, d.groups + d.n_groups);
+        if (!vol) md.groups.assign(d.groups, d.groups + d.n_groups);
         for (int gi : md.groups)
             if (gi < 0 || gi >= sp->n_groups) {
                 delete g;
@@ -129,7 +133,15 @@ int fau_movegen_generate(fau_movegen* g, fau_proposal* out, int n)
         std::memset(&p, 0, sizeof(p));
         p.kind = FAU_MOVE_NONE;
         const MoveDef& m = g->moves[g->pick(g->slump.engine)];
-        if (m.kind == FAU_MOVE_ATOMIC) {
+        if (m.kind == FAU_MOVE_VOLUME) {
+            // VolumeMove::setNewVolume (src/move.cpp:994-999): one slump() draw for ln V
+            if (m.dp > 0.0) {
+                p.kind = FAU_MOVE_VOLUME;
+                p.index = m.volume_method;
+                p.dr[0] = (g->slump() - 0.5) * m.dp;
+            }
+        }
+        else if (m.kind == FAU_MOVE_ATOMIC) {
             const int gi = m.groups[g->slump.range(0, (int)m.groups.size() - 1)];
             const int b = g->g_begin[gi], size = g->g_begin[gi + 1] - b;
             if (size > 0) {

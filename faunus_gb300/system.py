@@ -187,6 +187,7 @@ class SystemSpec:
     pair_cutoff: float = 0.0
     cutoff_g2g: float = 0.0
     cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
+    isobaric_pressure: Optional[float] = None  # Isobaric term's pressure (kT/A^3, see pressure_kt); None: no term
     ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
     precision: int = A.FAU_PREC_FP32C
     cell_capacity: int = 0
@@ -246,6 +247,9 @@ class SystemSpec:
         d.coulomb_cutoff = float(self.coulomb_cutoff)
         d.coulomb_alpha = float(self.coulomb_alpha)
         d.coulomb_erfc = float(self.coulomb_erfc)
+        if self.isobaric_pressure is not None:
+            d.isobaric = 1
+            d.pressure = float(self.isobaric_pressure)
         if self.coulomb_poly is not None:
             cp = np.asarray(self.coulomb_poly, dtype=np.float64).reshape(-1)
             if len(cp) > A.FAU_COUL_MAX_POLY:
@@ -499,14 +503,12 @@ class System:
         A.check(self._lib.fau_get_box(self.handle, A.as_dptr(out)), "fau_get_box")
         return out
 
-    def volume_move(self, new_volume: float, u: float, pressure: float = 0.0, method: str = "isotropic") -> dict:
-        """One VolumeMove to `new_volume` with the Isobaric term at `pressure` (kT/A^3, see
-        `pressure_kt`) and Metropolis uniform `u` (fau_volume_move)."""
-        m = {"isotropic": A.FAU_VOLUME_ISOTROPIC, "xy": A.FAU_VOLUME_XY, "z": A.FAU_VOLUME_Z,
-             "isochoric": A.FAU_VOLUME_ISOCHORIC}[method]
+    def volume_move(self, new_volume: float, u: float, method: str = "isotropic") -> dict:
+        """One VolumeMove to `new_volume` with Metropolis uniform `u` (fau_volume_move); the
+        Isobaric term is the spec's (`isobaric_pressure`)."""
         r = A.TrialResult()
-        A.check(self._lib.fau_volume_move(self.handle, float(new_volume), m, float(pressure), float(u), C.byref(r)),
-                "fau_volume_move")
+        A.check(self._lib.fau_volume_move(self.handle, float(new_volume), VOLUME_METHODS[method], float(u),
+                                          C.byref(r)), "fau_volume_move")
         return r.as_dict()
 
     def set_temperature_scale(self, scale: float) -> None:
@@ -523,11 +525,22 @@ class System:
         return float(v.value)
 
 
+VOLUME_METHODS = {"isotropic": A.FAU_VOLUME_ISOTROPIC, "xy": A.FAU_VOLUME_XY, "z": A.FAU_VOLUME_Z,
+                  "isochoric": A.FAU_VOLUME_ISOCHORIC}
+
+
 def move_descs(spec: SystemSpec, moves: Sequence[dict]):
-    """fau_move_desc array from dicts {kind, repeat, dp, dprot, dir, groups, type_dp, type_dprot}."""
+    """fau_move_desc array from dicts {kind, repeat, dp, dprot, dir, groups, type_dp, type_dprot};
+    a volume move is {kind: FAU_MOVE_VOLUME, repeat, dV, method}."""
     keep = []
     arr = (A.MoveDesc * len(moves))()
     for i, m in enumerate(moves):
+        if int(m["kind"]) == A.FAU_MOVE_VOLUME:
+            arr[i].kind = A.FAU_MOVE_VOLUME
+            arr[i].repeat = float(m.get("repeat", 1.0))
+            arr[i].dp = float(m["dV"])
+            arr[i].volume_method = VOLUME_METHODS[m.get("method", "isotropic")]
+            continue
         g = np.ascontiguousarray(m["groups"], dtype=np.int32)
         keep.append(g)
         arr[i].kind = int(m["kind"])

@@ -132,6 +132,8 @@ typedef struct fau_sys_desc {
     int coulomb_poly_n;
     double coulomb_erfc;
     double coulomb_poly[FAU_COUL_MAX_POLY];
+    int isobaric;             /* 1: the Hamiltonian has the Isobaric term (src/energy.cpp:859-901) */
+    double pressure;          /* its pressure in kT / A^3                             */
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */
@@ -161,7 +163,10 @@ typedef struct fau_trial_result {
 enum fau_move_kind {
     FAU_MOVE_NONE = -1,      /* empty Change: only the Metropolis draw is consumed */
     FAU_MOVE_ATOMIC = 0,     /* translate particle `index` by dr                    */
-    FAU_MOVE_MOLECULAR = 1   /* translate group `index` by dr, then rotate by quat  */
+    FAU_MOVE_MOLECULAR = 1,  /* translate group `index` by dr, then rotate by quat  */
+    FAU_MOVE_VOLUME = 2      /* VolumeMove (src/move.cpp:994-1006): index = fau_volume_method,
+                                dr[0] = (slump() - 0.5) dV; new volume exp(ln V + dr[0]);
+                                single-system proposal streams only                 */
 };
 typedef struct fau_proposal {
     int32_t kind;       /* fau_move_kind                                           */
@@ -333,9 +338,9 @@ int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* args, double* energy_
  * molecular groups are unwrapped about their mass centre, the mass centre scaled and
  * the atoms translated with it; boundary() in the new box -- the trial state's full
  * energy (Nonbonded, Ewald with the new box's k-vectors and a full Q(k) update,
- * self) is computed on the device in FP64, the Isobaric term P V - (N + 1) ln V is
- * added to both states (N: particles of atomic groups plus molecular groups; P in
- * kT / A^3), and the move is accepted on u01 <= exp(-dU).  On acceptance the system
+ * self) is computed on the device in FP64, the descriptor's Isobaric term
+ * P V - (N + 1) ln V, if present, is added to both states (N: particles of atomic
+ * groups plus molecular groups), and the move is accepted on u01 <= exp(-dU).  On acceptance the system
  * holds the new state (its tables rebuilt for the new box); on rejection it is
  * unchanged.  The running energy excludes the Isobaric term. */
 enum fau_volume_method {
@@ -344,8 +349,7 @@ enum fau_volume_method {
     FAU_VOLUME_Z = 2,
     FAU_VOLUME_ISOCHORIC = 3
 };
-int fau_volume_move(fau_sys* sys, double new_volume, int method, double pressure, double u01,
-                    fau_trial_result* out);
+int fau_volume_move(fau_sys* sys, double new_volume, int method, double u01, fau_trial_result* out);
 
 /* ---- device analysis ------------------------------------------------------
  * AtomRDF (src/analysis.cpp:1556-1600) and SystemEnergy (src/analysis.cpp:339-357)
@@ -403,7 +407,8 @@ int fau_get_q(fau_sys* sys, double* q_out);                    /* K complex as 2
  * (:1670-1689); randomUnitVector src/core.cpp:249-261. */
 typedef struct fau_movegen fau_movegen;
 typedef struct fau_move_desc {
-    int kind;            /* FAU_MOVE_ATOMIC (transrot) or FAU_MOVE_MOLECULAR (moltransrot) */
+    int kind;            /* FAU_MOVE_ATOMIC (transrot), FAU_MOVE_MOLECULAR (moltransrot) or
+                            FAU_MOVE_VOLUME (volume)                                      */
     double repeat;       /* weight in the move collection (Move::repeat)                  */
     double dp;           /* translational displacement                                    */
     double dprot;        /* rotational displacement (rad)                                 */
@@ -412,6 +417,8 @@ typedef struct fau_move_desc {
     const int* groups;   /* group indices                                                 */
     const double* type_dp;    /* n_types AtomData::dp, NaN = unset (transrot); may be NULL */
     const double* type_dprot; /* n_types AtomData::dprot, NaN = unset; may be NULL         */
+    int volume_method;   /* FAU_MOVE_VOLUME: fau_volume_method; dp is dV (VolumeMove::_from_json,
+                            src/move.cpp:986-993), n_groups may be 0                    */
 } fau_move_desc;
 int fau_movegen_create(const fau_sys_desc* space, const fau_move_desc* moves, int n_moves,
                        uint32_t slump_seed, uint32_t random_seed, int default_seeds,

@@ -371,6 +371,8 @@ struct System {
     double cutoff_g2g2 = std::numeric_limits<double>::max();
     int n_molids = 0;              // > 0: per molecule-kind pair cutoffs^2 below
     std::vector<double> cut2_pairs;
+    bool isobaric = false;  // Isobaric term (src/energy.cpp:859-901) with `pressure` in kT / A^3
+    double pressure = 0.0;
     bool want_scale = true; // sum |u| over both states for tolerance checks (not in the reference)
     // MC bookkeeping (MetropolisMonteCarlo)
     double initial_energy = 0, sum_of_energy_changes = 0;
@@ -667,7 +669,7 @@ static TrialOut trialGroup(System& s, int g, const Vec3& dr, const Quat* q, doub
 // MoveCollection (src/move.cpp:475-526), AtomicTranslateRotate (:190-365),
 // TranslateRotate (:1559-1723).
 struct MoveDef {
-    int kind;
+    int kind, volume_method = 0;
     double repeat, dp, dprot;
     Vec3 dir;
     std::vector<int> groups;
@@ -685,7 +687,15 @@ struct MoveGen {
         std::memset(&p, 0, sizeof(p));
         p.kind = FAU_MOVE_NONE;
         const MoveDef& m = moves[dist(slump.engine)]; // MoveCollection::sample
-        if (m.kind == FAU_MOVE_ATOMIC) {
+        if (m.kind == FAU_MOVE_VOLUME) {
+            // VolumeMove::_move / setNewVolume (src/move.cpp:994-1006): dV = 0 is an empty change
+            if (m.dp > 0.0) {
+                p.kind = FAU_MOVE_VOLUME;
+                p.index = m.volume_method;
+                p.dr[0] = (slump() - 0.5) * m.dp;
+            }
+        }
+        else if (m.kind == FAU_MOVE_ATOMIC) {
             // randomAtom: group then particle (src/move.cpp:328-346)
             const int gi = m.groups[slump.range(0, (int)m.groups.size() - 1)];
             const Group& G = sys->groups[gi];
@@ -829,6 +839,8 @@ static System buildSystem(const fau_sys_desc* d)
         P.cpoly.assign(d->coulomb_poly, d->coulomb_poly + std::max(0, std::min(d->coulomb_poly_n, FAU_COUL_MAX_POLY)));
     }
     if (d->cutoff_g2g > 0) s.cutoff_g2g2 = d->cutoff_g2g * d->cutoff_g2g;
+    s.isobaric = d->isobaric != 0;
+    s.pressure = d->pressure;
     if (d->cutoff_g2g_pairs && d->n_molids > 0) { // GroupCutoff::getCutoff per molecule-kind pair
         s.n_molids = d->n_molids;
         s.cut2_pairs.resize(size_t(d->n_molids) * d->n_molids);
@@ -905,6 +917,16 @@ int orc_trial_group(orc_sys* h, int g, const double dr[3], const double quat[4],
     return o.nan ? FAU_ERR_NAN : FAU_OK;
 }
 // Apply a proposal stream (performMove per proposal).
+int orc_volume_move(orc_sys* h, double new_volume, int method, double u01, fau_trial_result* r);
+// one performMove of a host-fed proposal
+static int orc_perform(orc_sys* h, const fau_proposal& p, fau_trial_result* r)
+{
+    if (p.kind == FAU_MOVE_ATOMIC) return orc_trial_atomic(h, p.index, p.dr, p.u, r);
+    if (p.kind == FAU_MOVE_MOLECULAR) return orc_trial_group(h, p.index, p.dr, p.quat, p.u, r);
+    if (p.kind == FAU_MOVE_VOLUME) // VolumeMove::setNewVolume (src/move.cpp:994-999)
+        return orc_volume_move(h, std::exp(std::log(h->s.box.volume()) + p.dr[0]), p.index, p.u, r);
+    return FAU_OK;
+}
 int orc_run_proposals(orc_sys* h, const fau_proposal* p, int n, uint8_t* acc_out, double* du_out,
                       fau_run_stats* st)
 {
@@ -914,11 +936,7 @@ int orc_run_proposals(orc_sys* h, const fau_proposal* p, int n, uint8_t* acc_out
     for (int m = 0; m < n; m++) {
         fau_trial_result r;
         std::memset(&r, 0, sizeof(r));
-        int rc = FAU_OK;
-        if (p[m].kind == FAU_MOVE_ATOMIC)
-            rc = orc_trial_atomic(h, p[m].index, p[m].dr, p[m].u, &r);
-        else if (p[m].kind == FAU_MOVE_MOLECULAR)
-            rc = orc_trial_group(h, p[m].index, p[m].dr, p[m].quat, p[m].u, &r);
+        const int rc = orc_perform(h, p[m], &r);
         if (rc != FAU_OK) return rc;
         if (acc_out) acc_out[m] = (uint8_t)r.accepted;
         if (du_out) du_out[m] = r.du;
@@ -937,11 +955,7 @@ int orc_run_proposals_detail(orc_sys* h, const fau_proposal* p, int n, fau_trial
     for (int m = 0; m < n; m++) {
         fau_trial_result r;
         std::memset(&r, 0, sizeof(r));
-        int rc = FAU_OK;
-        if (p[m].kind == FAU_MOVE_ATOMIC)
-            rc = orc_trial_atomic(h, p[m].index, p[m].dr, p[m].u, &r);
-        else if (p[m].kind == FAU_MOVE_MOLECULAR)
-            rc = orc_trial_group(h, p[m].index, p[m].dr, p[m].quat, p[m].u, &r);
+        const int rc = orc_perform(h, p[m], &r);
         if (rc != FAU_OK) return rc;
         out[m] = r;
     }
@@ -1064,9 +1078,10 @@ int orc_geometry(const double box[3], int n, const double* a, const double* b, d
 // src/montecarlo.cpp:139-187); the box scaled as Cuboid::setVolume (src/geometry.cpp:57-90) and
 // the particles as Space::scaleVolume (src/space.cpp:249-301); the trial state's Ewald gets
 // updateBox + a full Q update (Ewald::updateState with volume_change)
-int orc_volume_move(orc_sys* h, double new_volume, int method, double pressure, double u01, fau_trial_result* r)
+int orc_volume_move(orc_sys* h, double new_volume, int method, double u01, fau_trial_result* r)
 {
     System& s = h->s;
+    const double pressure = s.pressure;
     const Terms eo = energyOf(s, CH_EVERYTHING, 0);
     System t = s;
     const double v_old = s.box.volume();
@@ -1123,7 +1138,8 @@ int orc_volume_move(orc_sys* h, double new_volume, int method, double pressure, 
     const Terms en = energyOf(t, CH_EVERYTHING, 0);
     const double v_new = t.box.volume();
     auto total = [&](const Terms& e, double v) { // Isobaric first, then the Hamiltonian's terms
-        std::vector<double> list{pressure * v - double(n_count + 1) * std::log(v)};
+        std::vector<double> list;
+        if (s.isobaric) list.push_back(pressure * v - double(n_count + 1) * std::log(v));
         if (s.pair.has_self()) list.push_back(e.self);
         list.push_back(e.nb);
         if (s.ewald.enabled) list.push_back(e.surf + e.rec);
@@ -1217,7 +1233,8 @@ int orc_movegen_create(orc_sys* h, const fau_move_desc* moves, int n_moves, uint
         md.dp = moves[m].dp;
         md.dprot = moves[m].dprot;
         md.dir = {moves[m].dir[0], moves[m].dir[1], moves[m].dir[2]};
-        md.groups.assign(moves[m].groups, moves[m].groups + moves[m].n_groups);
+        md.volume_method = moves[m].volume_method;
+        if (moves[m].groups) md.groups.assign(moves[m].groups, moves[m].groups + moves[m].n_groups);
         const int nt = h->s.pair.n_types;
         if (moves[m].type_dp) md.type_dp.assign(moves[m].type_dp, moves[m].type_dp + nt);
         if (moves[m].type_dprot) md.type_dprot.assign(moves[m].type_dprot, moves[m].type_dprot + nt);

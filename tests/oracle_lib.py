@@ -44,7 +44,7 @@ def lib() -> C.CDLL:
                                   C.c_double, C.c_int, A.dptr, A.iptr], C.c_int),
             "orc_pair_u": ([sd, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, A.dptr], C.c_int),
             "orc_get_box": ([P, A.dptr], C.c_int),
-            "orc_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.c_double, C.POINTER(A.TrialResult)], C.c_int),
+            "orc_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.POINTER(A.TrialResult)], C.c_int),
             "orc_rdf": ([C.c_int, A.dptr, A.iptr, A.dptr, C.c_int, C.c_int, C.c_double, C.c_int, P], C.c_int),
             "orc_geometry": ([A.dptr, C.c_int, A.dptr, A.dptr, A.dptr, A.dptr, A.dptr], C.c_int),
             "orc_cell_bin": ([A.dptr, C.c_double, C.c_int, A.dptr, A.iptr, A.iptr, A.iptr, A.iptr], C.c_int),
@@ -97,9 +97,9 @@ class OracleSystem:
         _ok(lib().orc_energy_total(self.h, C.byref(t)), "orc_energy_total")
         return t.as_dict()
 
-    def volume_move(self, new_volume, method, pressure, u) -> dict:
+    def volume_move(self, new_volume, method, u) -> dict:
         r = A.TrialResult()
-        rc = lib().orc_volume_move(self.h, float(new_volume), int(method), float(pressure), float(u), C.byref(r))
+        rc = lib().orc_volume_move(self.h, float(new_volume), int(method), float(u), C.byref(r))
         out = r.as_dict()
         out["status"] = rc
         return out

@@ -71,13 +71,14 @@ def test_oracle_volume_move_equals_fresh_state(kind, method):
         spec = configs.primitive_model(n=100, seed=2)
     else:
         spec = configs.spce_water(n_mol=64, L=12.4, seed=5)
+    P = F.pressure_kt(1.0, "P/atm")
+    spec = dataclasses.replace(spec, isobaric_pressure=P)
     o = O.OracleSystem(spec)
     pos, cm, L = o.positions(), o.mass_centers(), o.box()
     v_old = float(np.prod(L))
     v_new = v_old * 1.02
-    P = F.pressure_kt(1.0, "P/atm")
     e_old = o.energy_total()["total"]
-    r = o.volume_move(v_new, {"isotropic": 0, "xy": 1, "z": 2}[method], P, 0.0)  # u = 0: always accepted
+    r = o.volume_move(v_new, {"isotropic": 0, "xy": 1, "z": 2}[method], 0.0)  # u = 0: always accepted
     assert r["status"] == 0 and r["accepted"] == 1
     fresh, Ln = _scaled_spec(spec, pos, cm, L, method, v_new)
     assert np.array_equal(o.box(), Ln)
@@ -97,10 +98,54 @@ def test_oracle_volume_move_equals_fresh_state(kind, method):
 
 
 def test_oracle_rejected_volume_move_leaves_state():
-    spec = configs.bulk_ewald(n_salt=100, molar=0.5, seed=4)
+    spec = dataclasses.replace(configs.bulk_ewald(n_salt=100, molar=0.5, seed=4), isobaric_pressure=1e3)
     o = O.OracleSystem(spec)
     pos, L, e = o.positions(), o.box(), o.energy_total()["total"]
-    r = o.volume_move(np.prod(L) * 1.5, 0, 1e3, 0.5)  # P dV is huge: rejected
+    r = o.volume_move(np.prod(L) * 1.5, 0, 0.5)  # P dV is huge: rejected
     assert r["accepted"] == 0 and r["du"] > 100
     assert np.array_equal(o.positions(), pos) and np.array_equal(o.box(), L)
     assert o.energy_total()["total"] == e
+
+
+def test_without_isobaric_term_du_is_the_hamiltonian_change():
+    spec = configs.primitive_model(n=100, seed=7)
+    o = O.OracleSystem(spec)
+    e0 = o.energy_total()["total"]
+    r = o.volume_move(float(np.prod(o.box())) * 1.01, 0, 0.0)
+    assert r["accepted"] == 1
+    assert r["du"] == pytest.approx(o.energy_total()["total"] - e0, rel=1e-12, abs=1e-12)
+
+
+def _npt_water(n_mol=64, L=12.4):
+    spec = configs.spce_water(n_mol=n_mol, L=L, seed=5)
+    spec = dataclasses.replace(spec, isobaric_pressure=F.pressure_kt(1.0, "P/atm", 300.0))
+    moves = spec.extra["moves"] + [{"kind": A.FAU_MOVE_VOLUME, "repeat": 1, "dV": 0.03, "method": "isotropic"}]
+    spec.extra["moves"] = moves
+    return spec
+
+
+def test_movegen_volume_stream_matches_oracle_generator():
+    """fau_movegen and the oracle's generator draw volume moves in the same place of the
+    reference stream (MoveCollection::sample, then one slump() for ln V, then the
+    Metropolis uniform)."""
+    spec = _npt_water()
+    gen = F.MoveGenerator(spec, spec.extra["moves"], 3, 4, default_seeds=False)
+    props = gen.generate(3000)
+    vol = props["kind"] == A.FAU_MOVE_VOLUME
+    assert 20 < vol.sum() < 100  # weight 1 against 64
+    assert (np.abs(props["dr"][vol, 0]) <= 0.015).all()
+    o = O.OracleSystem(spec)
+    og = O.OracleMoveGen(o, spec.extra["moves"], 3, 4, default_seeds=False)
+    assert np.array_equal(og.generate(3000), props)
+
+
+def test_oracle_npt_loop_equals_proposal_replay():
+    spec = _npt_water()
+    a, b = O.OracleSystem(spec), O.OracleSystem(spec)
+    ga = O.OracleMoveGen(a, spec.extra["moves"], 3, 4, default_seeds=False)
+    acc_loop, _, _ = ga.mc_run(800)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 3, 4, default_seeds=False).generate(800)
+    det = b.run_detail(props)
+    assert np.array_equal(det["accepted"].astype(np.uint8), acc_loop)
+    assert np.array_equal(a.positions(), b.positions()) and np.array_equal(a.box(), b.box())
+    assert not np.array_equal(b.box(), spec.box)  # some volume move was accepted

@@ -2,6 +2,8 @@
 boxes and positions (the scaling is IEEE-exact FP64 on both sides), dU within 1e-9 of the
 Isobaric-inclusive energy scale, counters carried, and chains of trial moves after volume moves
 (cell grids and k-vector amplitudes rebuilt for the new box) still at parity with the oracle."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -24,9 +26,9 @@ def test_volume_moves_match_oracle(ctx, kind):
         spec = configs.primitive_model(n=200, seed=2)
     else:
         spec = configs.spce_water(n_mol=256, L=18.6, seed=5)
+    spec = dataclasses.replace(spec, isobaric_pressure=F.pressure_kt(1.0, "P/atm"))
     g, o = ctx.create(spec), O.OracleSystem(spec)
     rng = np.random.default_rng(9)
-    P = F.pressure_kt(1.0, "P/atm")
     grids = {g.cell_grid()}
     n_acc = 0
     for k in range(12):
@@ -34,8 +36,8 @@ def test_volume_moves_match_oracle(ctx, kind):
         v_new = float(np.exp(np.log(v) + (rng.random() - 0.5) * 0.3))
         method = ["isotropic", "xy", "z"][k % 3]
         u = float(rng.random())
-        rg = g.volume_move(v_new, u, pressure=P, method=method)
-        ro = o.volume_move(v_new, METHODS[method], P, u)
+        rg = g.volume_move(v_new, u, method=method)
+        ro = o.volume_move(v_new, METHODS[method], u)
         assert rg["accepted"] == ro["accepted"]
         assert abs(rg["du"] - ro["du"]) <= 1e-9 * ro["err_scale"], (rg, ro)
         assert np.array_equal(g.box(), o.box())
@@ -62,10 +64,10 @@ def test_volume_moves_match_oracle(ctx, kind):
 
 
 def test_rejected_volume_move_keeps_the_system(ctx):
-    spec = configs.bulk_ewald(n_salt=500, molar=1.0, seed=6)
+    spec = dataclasses.replace(configs.bulk_ewald(n_salt=500, molar=1.0, seed=6), isobaric_pressure=1e3)
     g = ctx.create(spec)
     pos, box, e = g.positions(), g.box(), g.running_energy()
-    r = g.volume_move(float(np.prod(box)) * 1.5, 0.5, pressure=1e3)
+    r = g.volume_move(float(np.prod(box)) * 1.5, 0.5)
     assert r["accepted"] == 0
     assert np.array_equal(g.positions(), pos) and np.array_equal(g.box(), box) and g.running_energy() == e
     _compare_chain(g, spec, _props(spec, 1000), TOL_FP32C)
@@ -77,3 +79,32 @@ def test_volume_move_argument_errors(ctx):
         g.volume_move(-1.0, 0.5)
     with pytest.raises(KeyError):
         g.volume_move(1e5, 0.5, method="sphere")
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_npt_reference_stream_matches_oracle(ctx, precision):
+    """moltransrot + volume moves drawn from the reference stream (examples/water/ewald.yml's
+    move set at a smaller size), run through fau_run_proposals: the stream is split at every
+    volume move; accept sequence, dU, box and positions follow the oracle."""
+    spec = configs.spce_water(n_mol=256, L=18.6, seed=5, precision=precision)
+    spec = dataclasses.replace(spec, isobaric_pressure=F.pressure_kt(1.0, "P/atm", 300.0))
+    spec.extra["moves"] = spec.extra["moves"] + [{"kind": 2, "repeat": 1, "dV": 0.03, "method": "isotropic"}]
+    props = F.MoveGenerator(spec, spec.extra["moves"], 3, 4, default_seeds=False).generate(3000)
+    vol = props["kind"] == 2
+    assert vol.sum() > 3
+    g, o = ctx.create(spec), O.OracleSystem(spec)
+    acc_g, du_g, st = g.run_proposals(props)
+    det = o.run_detail(props)
+    mism = np.nonzero(acc_g != det["accepted"])[0]
+    first = int(mism[0]) if len(mism) else len(props)
+    sl = slice(0, first)
+    tol = np.where(vol[sl], 1e-9, TOL_FP32C if precision == 0 else 1e-10)
+    den = np.maximum(np.abs(det["du"][sl]), det["err_scale"][sl])
+    fin = np.isfinite(det["du"][sl])
+    assert (np.abs(du_g[sl] - det["du"][sl])[fin] <= (tol * np.where(den > 0, den, 1.0))[fin]).all()
+    assert acc_g[vol].sum() > 0
+    if first == len(props):
+        assert np.array_equal(g.box(), o.box())
+        assert np.array_equal(g.positions(), o.positions())
+    else:
+        assert first > len(props) // 10
