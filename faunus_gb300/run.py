@@ -101,9 +101,12 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
     e_total = system.energy_total()["total"]
     c1 = system.counters()
     du_sum = e_total - e0
-    drift = 0.0
-    e_run = system.running_energy()
-    if np.isfinite(e_total) and abs(e_total - e0) > 2.220446049250313e-16:
+    e_run = system.running_energy()  # initial energy + sum of accepted changes
+    if not np.isfinite(du_sum):  # e.g. a start with hard-sphere overlaps (infinite energy)
+        drift = float("nan")
+    elif abs(du_sum) <= 2.220446049250313e-16:
+        drift = 0.0
+    else:
         drift = (e_total - e_run) / (e0 if abs(e0) > 2.220446049250313e-16 else e_total)
     result = {"moves": {"attempted": c1["moves"] - c0["moves"], "accepted": c1["accepted"] - c0["accepted"],
                         "acceptance": {str(k): a / n for k, (a, n) in accepted.items() if n}},

@@ -39,7 +39,10 @@ def test_simulate_primitive_model(ctx, tmp_path, mode):
     setup = I.load_input(text, seed=3)
     res = simulate(setup, ctx, out_dir=tmp_path, mode=mode, macro=2, micro=5)
     assert res["moves"]["attempted"] == 2 * 5 * 60
-    assert abs(res["relative drift"]) < 1e-9
+    if np.isfinite(res["energy"]["initial"]):
+        assert abs(res["relative drift"]) < 1e-9
+    else:  # random insertion left hard-sphere overlaps: the reference reports NaN too
+        assert np.isnan(res["relative drift"]) and np.isfinite(res["energy"]["final"])
     en = res["analysis"][0]["systemenergy"]
     assert en["samples"] == 5 and np.isfinite(en["mean"])
     assert res["analysis"][1]["atomrdf"]["samples"] == 5
