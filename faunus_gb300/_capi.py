@@ -187,6 +187,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_get_running_energy": ([P, dptr], C.c_int),
         "fau_get_counters": ([P, C.POINTER(C.c_int64)], C.c_int),
         "fau_get_box": ([P, dptr], C.c_int),
+        "fau_refresh_energy": ([P, dptr], C.c_int),
         "fau_volume_move": ([P, C.c_double, C.c_int, C.c_double, C.POINTER(TrialResult)], C.c_int),
         "fau_sampler_create": ([P, C.POINTER(SamplerDesc), C.POINTER(P)], C.c_int),
         "fau_sampler_destroy": ([P], C.c_int),

@@ -1687,6 +1687,17 @@ int fau_get_cell_grid(const fau_sys* s, int dims[3])
     return FAU_OK;
 }
 
+int fau_refresh_energy(fau_sys* s, double* e)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null system");
+    if (s->pending) return fail(FAU_ERR_STATE, "refresh with a pending trial");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    const int rc = refresh_energy(s);
+    if (rc) return rc;
+    if (e) *e = s->h.energy;
+    return FAU_OK;
+}
+
 int fau_get_box(const fau_sys* s, double* box)
 {
     if (!s || !box) return fail(FAU_ERR_ARG, "null argument");

@@ -91,6 +91,8 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
                 ctx.run_batch([system], per_sweep, seed=seed, counter_base=step * per_sweep, dp=batch_dp,
                               dprot=batch_dprot)
             step += 1
+            if not np.isfinite(system.running_energy()):  # left an infinite start: sum of changes undefined
+                system.refresh_energy()
             if energy_an and step % energy_an["nstep"] == 0:
                 energy_an["samples"].append(system.running_energy())
             for r in rdf_an:
@@ -101,7 +103,7 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
     e_total = system.energy_total()["total"]
     c1 = system.counters()
     du_sum = e_total - e0
-    e_run = system.running_energy()  # initial energy + sum of accepted changes
+    e_run = system.running_energy()  # initial energy + sum of accepted changes (refreshed after an infinite start)
     if not np.isfinite(du_sum):  # e.g. a start with hard-sphere overlaps (infinite energy)
         drift = float("nan")
     elif abs(du_sum) <= 2.220446049250313e-16:

@@ -498,6 +498,12 @@ class System:
     def accepted_moves(self) -> int:
         return self.counters()["accepted"]
 
+    def refresh_energy(self) -> float:
+        """Make the FP64 total energy the running energy (fau_refresh_energy)."""
+        v = C.c_double()
+        A.check(self._lib.fau_refresh_energy(self.handle, C.byref(v)), "fau_refresh_energy")
+        return float(v.value)
+
     def box(self) -> np.ndarray:
         out = np.zeros(3)
         A.check(self._lib.fau_get_box(self.handle, A.as_dptr(out)), "fau_get_box")

@@ -389,6 +389,9 @@ int fau_get_cells(fau_sys* sys, int* cell_out);                /* n cell index o
 int fau_get_cell_grid(const fau_sys* sys, int dims_out[3]);
 int fau_get_box(const fau_sys* sys, double box_out[3]);         /* cuboid side lengths */
 int fau_get_running_energy(fau_sys* sys, double* energy_out);  /* FP64 running total */
+/* Recompute the FP64 total energy and make it the running energy (after a start
+ * from an infinite energy, where initial + sum of changes is not defined). */
+int fau_refresh_energy(fau_sys* sys, double* energy_out);
 /* Move counters since the system was created: {moves, accepted, pair
  * evaluations, k-vector updates} (Move::number_of_attempted_moves and
  * number_of_accepted_moves, src/move.h:50-59, summed over moves). */
