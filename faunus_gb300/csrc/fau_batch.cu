@@ -189,6 +189,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
         (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
+    // molecular-move systems: the pipelined molecular kernel (preparation of the next move overlapped
+    // with the current one) unless a chain-kernel size was requested; FAU_MOL_KERNEL=0 turns it off
+    bool use_mol = use_fast && nexact > 0;
+    if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
+    for (int r = nfast; r < n && use_mol; r++)
+        if (!mol[order[r]]) use_mol = false;
+    if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
 
     // device argument arrays (one allocation, freed at the end of the call)
     // every sub-buffer starts on a 16-byte boundary (8-byte fields inside)
@@ -316,7 +323,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.counters) ae.counters = a.counters + nfast;
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
-    if (nexact) BTRY(prepare_chain(Ke, nce, threads, true));
+    if (nexact) BTRY(use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true) : prepare_chain(Ke, nce, threads, true));
     if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
@@ -331,13 +338,16 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         if (nfast && nexact) {
             if ((e = cudaEventRecord(fork_ev, st)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(st2, fork_ev, 0)) != cudaSuccess) return e;
-            if ((e = launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess) return e;
+            if ((e = use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st2, false)
+                             : launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess)
+                return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
             if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
         if (nfast) return launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st);
-        return launch_chain(ae, nexact, Ke, nce, threads, true, st);
+        return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
+                       : launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };
 
     // profiling: FAU_PHASE_TIMING=1 prints the chain kernel's per-phase cycles to stderr

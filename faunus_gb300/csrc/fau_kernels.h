@@ -61,6 +61,9 @@ cudaError_t chain_dispatch_128_host(const ChainArgs&, int, int, int, cudaStream_
 cudaError_t chain_dispatch_128_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
+// pipelined molecular-move kernel (device proposals; 256 threads: 1 preparing + 7 compute warps)
+cudaError_t mol_dispatch_256(const ChainArgs&, int, int, int, cudaStream_t, bool);
+size_t mol_smem_bytes_total(int K, int nc);
 // pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps;
 // k-vector components up to kFastMaxNc (8-bit phase-table indices)
 constexpr int kFastMaxNc = 40;

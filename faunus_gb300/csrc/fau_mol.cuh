@@ -1,0 +1,465 @@
+// fau_mol.cuh -- pipelined chain kernel for molecular moves (TranslateRotate,
+// src/move.cpp:1670-1689) of rigid molecules with device (Philox) proposals.
+//
+// One CTA runs one system's Markov chain.  The chain kernel prepares move t+1
+// (FP64 translation + quaternion rotation of every atom, wrap, fixed-point
+// records, phase tables) after the Metropolis decision of move t, on the
+// critical path; measured on rigid water that preparation is a serial FP64 chain
+// of ~20k cycles per move, as long as the whole pair phase.  Here warp 0 prepares
+// move t+1 speculatively while warps 1..NW-1 evaluate move t (Ewald dQ and the
+// GroupCutoff-compacted group-vs-rest pair sum), into a second MoveShared and a
+// second set of phase tables.  After the decision and commit of move t, a
+// prepared move that picked the same group is prepared again from the committed
+// positions (the only state a molecular move's preparation reads that move t can
+// change: the moved group's atoms and mass centre).  Everything else -- term
+// order, precision, guard bands, the Q(k) bookkeeping and the FP64 decision --
+// is the chain kernel's, so both kernels give the same chains for the same
+// proposal stream, barring near ties (the compute warps sum in a different order).
+#pragma once
+
+#include "fau_chain.cuh"
+
+namespace fau {
+
+__device__ __forceinline__ void compute_barrier(int nthreads)
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
+{
+    constexpr int NW = NT / 32;
+    constexpr int NWC = NW - 1;   // compute warps
+    constexpr int NTC = NT - 32;  // compute threads
+    constexpr int RC = 2;         // candidate groups per compute thread per chunk
+    constexpr int CH = RC * NTC;  // candidate groups per chunk
+    const long long t_start = clock64();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ctid = tid - 32; // compute-thread index (warps 1..)
+    DevSys& G = *A.sys[blockIdx.x];
+    __shared__ __align__(16) DevSys Ssh;
+    for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += NT)
+        reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
+    __syncthreads();
+    const DevSys& S = Ssh;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int K = (S.flags & SYS_EWALD) ? S.K : 0;
+    const int nc = S.knc;
+    const int TS = 2 * nc + 1;
+    float2* Qb = reinterpret_cast<float2*>(smem_raw);
+    float2* pend = Qb + K;
+    float2* dlt = pend + K;
+    int* kidx = reinterpret_cast<int*>(dlt + K);
+    float* Af = reinterpret_cast<float*>(kidx + K);
+    float2* tabs = reinterpret_cast<float2*>(Af + K); // two sets of kTableAtoms * 6 * TS phase tables
+    const int tab_len = kTableAtoms * 6 * TS;
+
+    __shared__ PairF pt[kMaxITypes * kMaxITypes];
+    __shared__ MoveShared msb[2];
+    __shared__ FF red_a[NW];
+    __shared__ int red_f[NW];
+    __shared__ uint32_t nbl[CH];
+    __shared__ int nbl_cnt[2];
+    __shared__ int sh_prev_accept, sh_stop;
+    __shared__ long long sh_consumed;
+
+    const float rec_pref_f = (float)S.rec_pref;
+    for (int k = tid; k < K; k += NT) {
+        const double2 q = S.Q[k];
+        Qb[k] = make_float2((float)q.x, (float)q.y);
+        pend[k] = make_float2(0.f, 0.f);
+        dlt[k] = make_float2(0.f, 0.f);
+        int nx, ny, nz;
+        kn_unpack(S.kn[k], nx, ny, nz);
+        kidx[k] = (nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16);
+        Af[k] = rec_pref_f * S.Ak[k];
+    }
+    for (int t = tid; t < S.nt * S.nt; t += NT) pt[t] = S.pair[t];
+
+    const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
+    const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
+    const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+    const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
+    const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
+    const int nt = S.nt;
+
+    unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
+    int since_flush = 0;
+    double energy = S.energy, sum_du = 0.0;
+    double M[3] = {S.M[0], S.M[1], S.M[2]};
+    long long consumed = nmoves;
+
+    // phase timers (profiling only): warp 0 (tid 0): 6 prepare ahead, 3 wait B1, 4 decision,
+    // 5 commit (+ re-prepare), 7 B2; warp 1 (tid 32): 0 deferred Q, 1 Ewald, 2 pairs, 9 B1, 10 B2; 11 moves
+    const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
+    unsigned long long tacc[kPhaseSlots] = {0};
+    long long tprev = timing ? clock64() : 0;
+    auto tick = [&](int slot) {
+        if (timing) {
+            const long long t = clock64();
+            tacc[slot] += (unsigned long long)(t - tprev);
+            tprev = t;
+        }
+    };
+    if (tid == 0) {
+        sh_prev_accept = 0;
+        sh_stop = 0;
+        nbl_cnt[0] = nbl_cnt[1] = 0;
+    }
+    __syncthreads();
+    if (warp == 0 && nmoves > 0) {
+        const Proposal p = philox_proposal(S, ctr0, sys_id, A.seed, dp_f, dprot, true);
+        prepare_move(S, msb[0], p, lane, K ? tabs : nullptr, nc);
+    }
+    __syncthreads();
+
+    for (long long mv = 0; mv < nmoves; mv++) {
+        const int cur = (int)(mv & 1);
+        MoveShared& ms = msb[cur];
+        MoveShared& mn = msb[cur ^ 1];
+        const float2* tab = tabs + cur * tab_len;
+        float2* tab_next = tabs + (cur ^ 1) * tab_len;
+        if (sh_stop || ms.stop) { // a NaN energy change ended the chain, or a proposal was invalid
+            consumed = sh_stop ? sh_consumed : mv;
+            break;
+        }
+        const int kind = ms.kind;
+        const int m = ms.m;
+        FF accp{0.f, 0.f}, accr{0.f, 0.f};
+        int flags = 0;
+        if (warp == 0) {
+            // ---- speculative preparation of move mv+1 (reads only the group it moves)
+            if (mv + 1 < nmoves) {
+                const Proposal p =
+                    philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
+                prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);
+            }
+            tick(6);
+        }
+        else {
+            // ---- the previous move's Q(k) change (same k partition as the Ewald loop below)
+            if (sh_prev_accept) {
+                for (int k = ctid; k < K; k += NTC) {
+                    float2 pe = pend[k];
+                    const float2 d = dlt[k];
+                    pe.x += d.x;
+                    pe.y += d.y;
+                    pend[k] = pe;
+                }
+                if (++since_flush == kFlushAccepts) {
+                    since_flush = 0;
+                    for (int k = ctid; k < K; k += NTC) {
+                        double2 q = S.Q[k];
+                        const float2 pe = pend[k];
+                        q.x += (double)pe.x;
+                        q.y += (double)pe.y;
+                        S.Q[k] = q;
+                        Qb[k] = make_float2((float)q.x, (float)q.y);
+                        pend[k] = make_float2(0.f, 0.f);
+                    }
+                }
+            }
+            if (timing) {
+                tick(0);
+                if (tid == 32) tacc[11]++;
+            }
+            if (kind != FAU_MOVE_NONE) {
+                if (K) {
+                    const bool tables = m <= kTableAtoms;
+                    for (int k = ctid; k < K; k += NTC) {
+                        const int ki = kidx[k];
+                        const int ix = ki & 0xff, iy = (ki >> 8) & 0xff, iz = ki >> 16;
+                        float2 d = make_float2(0.f, 0.f);
+                        for (int a = 0; a < m; a++) {
+                            float2 eo, h;
+                            if (tables) {
+                                const float2* t = tab + a * 6 * TS;
+                                eo = cmul(t[ix], cmul(t[TS + iy], t[2 * TS + iz]));
+                                h = cmul(t[3 * TS + ix], cmul(t[4 * TS + iy], t[5 * TS + iz]));
+                            }
+                            else {
+                                const int nx = ix - nc, ny = iy - nc, nz = iz - nc;
+                                eo = eikr32(nx, ny, nz, ms.rec_old[a]);
+                                const float3 g = ms.g[a];
+                                float sh, ch;
+                                sincospif(fmaf((float)nx, g.x, fmaf((float)ny, g.y, (float)nz * g.z)), &sh, &ch);
+                                h = make_float2(ch, sh);
+                            }
+                            const float2 pp = cmul(eo, h);
+                            const float f = 2.f * ms.q[a] * h.y;
+                            d.x = fmaf(-f, pp.y, d.x);
+                            d.y = fmaf(f, pp.x, d.y);
+                        }
+                        dlt[k] = d;
+                        const float2 qb = Qb[k], pe = pend[k];
+                        const float qx = qb.x + pe.x, qy = qb.y + pe.y;
+                        const float cross = 2.f * fmaf(qx, d.x, qy * d.y);
+                        const float dd = fmaf(d.x, d.x, d.y * d.y);
+                        ff_add(accr, Af[k] * (cross + dd));
+                    }
+                    n_k += (unsigned long long)m * (unsigned long long)((K - ctid + NTC - 1) / NTC > 0
+                                                                            ? (K - ctid + NTC - 1) / NTC
+                                                                            : 0);
+                }
+                tick(1);
+                // ---- group2all(group) with GroupCutoff, in chunks of CH candidate groups
+                const int g = ms.index;
+                const uint4 cmo = ms.cmrec_old, cmn = ms.cmrec_new;
+                const double cmo_d[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
+                const int GN = S.n_groups;
+                const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
+                int chunk = 0;
+                for (int base = 0; base < GN; base += CH, chunk++) {
+                    int* cntp = &nbl_cnt[chunk & 1];
+                    int gfl[RC], gml[RC];
+                    uint4 gcr[RC];
+#pragma unroll
+                    for (int r = 0; r < RC; r++) {
+                        const int h = base + r * NTC + ctid;
+                        gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
+                        gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                        gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
+                    }
+#pragma unroll
+                    for (int r = 0; r < RC; r++) {
+                        const int h = base + r * NTC + ctid;
+                        uint32_t e = 0;
+                        if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
+                            double c2 = S.cut_g2g2;
+                            float c2f = S.cut_g2g2f;
+                            if (S.n_mol > 0) {
+                                const int kk = mol_g * S.n_mol + gml[r];
+                                c2 = S.cut2_mol[kk];
+                                c2f = S.cut2_molf[kk];
+                            }
+                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
+                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
+                            e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
+                        int wpos = 0;
+                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
+                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
+                        if (e) nbl[wpos + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)h | e;
+                    }
+                    compute_barrier(NTC);
+                    const int cnt = *cntp;
+                    if (ctid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
+                    for (int task = ctid; task < cnt * m; task += NTC) {
+                        const int q = task / m, a = task - q * m;
+                        const uint32_t ent = nbl[q];
+                        const int h = (int)(ent & kNblGroup);
+                        const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
+                        const int hb = S.g_begin[h], he = S.g_begin[h + 1];
+                        const uint4 ra_n = ms.rec_new[a], ra_o = ms.rec_old[a];
+                        const int ta = ra_n.w >> 24;
+                        for (int b = hb; b < he; b++) {
+                            const uint4 rb = S.rec[b];
+                            const int pidx = ta * nt + (int)(rb.w >> 24);
+                            const PairF p = pt[pidx];
+                            float uu[2] = {0.f, 0.f};
+                            bool fi[2] = {false, false}, fn[2] = {false, false};
+                            float mg = 0.f;
+                            for (int st = 0; st < 2; st++) {
+                                if (!(st ? do_o : do_n)) continue;
+                                uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ra_o : ra_n, rb),
+                                                  st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
+                                n_pairs++;
+                            }
+                            add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
+                        }
+                    }
+                    compute_barrier(NTC);
+                }
+                if (ctid == 0) nbl_cnt[0] = nbl_cnt[1] = 0;
+                for (int t = ctid; t < S.n_atomic; t += NTC) { // atomic groups are never cut
+                    const int b = S.atomic_idx[t];
+                    const uint4 rb = S.rec[b];
+                    const int tb = rb.w >> 24;
+                    for (int a = 0; a < m; a++) {
+                        const int pidx = (ms.rec_new[a].w >> 24) * nt + tb;
+                        const PairF p = pt[pidx];
+                        float uu[2];
+                        bool fi[2], fn[2];
+                        float mg = 0.f;
+                        for (int st = 0; st < 2; st++) {
+                            fi[st] = false;
+                            fn[st] = false;
+                            uu[st] = pair_u32(S, p, pidx, r2_fixed(S, st ? ms.rec_old[a] : ms.rec_new[a], rb),
+                                              st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
+                        }
+                        add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
+                        n_pairs += 2;
+                    }
+                }
+            }
+            tick(2);
+            accp = ff_sum(accp, accr);
+            float sc = 0.f;
+            warp_reduce(accp, accr, sc, flags, false);
+            if (lane == 0) {
+                red_a[warp] = accp;
+                red_f[warp] = flags;
+            }
+        }
+        __syncthreads(); // B1
+        tick(tid == 0 ? 3 : 9);
+
+        if (warp == 0) {
+            accp = (lane >= 1 && lane <= NWC) ? red_a[lane] : FF{0.f, 0.f};
+            flags = (lane >= 1 && lane <= NWC) ? red_f[lane] : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
+                accp = ff_sum(accp, ta);
+                flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+            }
+            int accept = 0, stop = 0;
+            if (lane == 0 && kind != FAU_MOVE_NONE) {
+                double du_surf = 0.0;
+                if (S.flags & SYS_SURFACE) {
+                    double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        const double mnv = __dadd_rn(M[d], ms.dM[d]);
+                        m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
+                        m2n = __dadd_rn(m2n, __dmul_rn(mnv, mnv));
+                    }
+                    du_surf = S.surf_pref * (m2n - m2o);
+                }
+                const double fin = ff_value(accp) + (0.0 + du_surf);
+                const double du =
+                    energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
+                const double x = du * S.beta_scale;
+                if (isnan(x)) stop = FAU_ERR_NAN;
+                else accept = metropolis(x, ms.u) ? 1 : 0;
+                if (accept) {
+                    n_acc++;
+                    sum_du += du;
+                    energy += du;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
+                }
+                if (!stop) n_mv++;
+            }
+            accept = __shfl_sync(0xffffffffu, accept, 0);
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            tick(4);
+            if (!stop && accept) {
+                // ---- commit (State::sync trial -> accepted): positions, records, mass centre
+                if (lane < m) {
+                    const int i = ms.first + lane;
+                    S.x[i] = ms.xn[lane][0];
+                    S.y[i] = ms.xn[lane][1];
+                    S.z[i] = ms.xn[lane][2];
+                    S.rec[i] = ms.rec_new[lane];
+                }
+                if (lane == 0 && kind == FAU_MOVE_MOLECULAR) {
+                    const int g = ms.index;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) S.g_cm[3 * g + d] = ms.cm_new[d];
+                    S.g_cmrec[g] = ms.cmrec_new;
+                }
+                __syncwarp();
+                __threadfence_block();
+                // the prepared next move read this group's old positions: prepare it again
+                if (mv + 1 < nmoves && mn.kind == FAU_MOVE_MOLECULAR && kind == FAU_MOVE_MOLECULAR &&
+                    mn.index == ms.index) {
+                    const Proposal p =
+                        philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
+                    prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);
+                }
+            }
+            if (lane == 0) {
+                sh_prev_accept = stop ? 0 : accept;
+                if (stop) {
+                    sh_stop = stop;
+                    sh_consumed = mv;
+                }
+            }
+            __syncwarp();
+            tick(5);
+        }
+        __syncthreads(); // B2
+        tick(tid == 0 ? 7 : 10);
+    }
+    if (timing)
+        for (int j = 0; j < kPhaseSlots; j++)
+            if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + j], tacc[j]);
+
+    // the last accepted move's Q(k) change, then everything pending into the FP64 master
+    if (sh_prev_accept && !sh_stop) {
+        for (int k = tid; k < K; k += NT) {
+            float2 pe = pend[k];
+            const float2 d = dlt[k];
+            pe.x += d.x;
+            pe.y += d.y;
+            pend[k] = pe;
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < K; k += NT) {
+        const float2 pe = pend[k];
+        if (pe.x != 0.f || pe.y != 0.f) {
+            double2 q = S.Q[k];
+            q.x += (double)pe.x;
+            q.y += (double)pe.y;
+            S.Q[k] = q;
+        }
+    }
+    __shared__ unsigned long long red_u[NW][2];
+    unsigned long long a = n_pairs, b = n_k;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        red_u[warp][0] = a;
+        red_u[warp][1] = b;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long pa = 0, kb = 0;
+        for (int w = 0; w < NW; w++) {
+            pa += red_u[w][0];
+            kb += red_u[w][1];
+        }
+        G.pair_evals += pa;
+        G.k_updates += kb;
+        G.moves += n_mv;
+        G.accepted += n_acc;
+        G.sum_du += sum_du;
+        G.energy = energy;
+#pragma unroll
+        for (int d = 0; d < 3; d++) G.M[d] = M[d];
+        if (sh_stop) G.err = sh_stop;
+        G.consumed = consumed;
+        G.cycles += (unsigned long long)(clock64() - t_start);
+    }
+}
+
+// dynamic shared memory of the molecular kernel: the chain kernel's plus a second set of tables
+__host__ __device__ inline size_t mol_smem_bytes(int K, int nc)
+{
+    return chain_smem_bytes_v2(K, nc) + (size_t)kTableAtoms * 6 * (2 * nc + 1) * sizeof(float2);
+}
+
+template <int NT>
+cudaError_t launch_mol_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
+{
+    static size_t granted = 0;
+    const size_t smem = mol_smem_bytes(K, nc);
+    if (smem > granted || granted == 0) {
+        cudaError_t e = cudaFuncSetAttribute(mol_chain_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        granted = smem;
+    }
+    if (prepare_only) return cudaSuccess;
+    mol_chain_kernel<NT><<<nblocks, NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace fau
