@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 
     // phase timers (profiling only; every phase still runs): slots
     // 0 deferred Q commit, 1 Ewald, 2 pairs, 3 reduce + barrier 1, 4 decision, 5 commit,
-    // 6 prepare next, 7 barrier 2 (warp 0); 8 compute, 9 barrier 1, 10 barrier 2 (warp 1); 11 moves
+    // 6 prepare next, 7 barrier 2 (warp 0); 8 compute, 9 barrier 1, 10 barrier 2 (warp 1); last: moves
     const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
     unsigned long long tacc[kPhaseSlots] = {0};
     long long tprev = timing ? clock64() : 0;
@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         const int m = ms.m;
         if (timing) {
             tick(0);
-            if (tid == 0) tacc[11]++;
+            if (tid == 0) tacc[kPhaseSlots - 1]++;
         }
 
         // ---- energy change of this move

@@ -273,34 +273,12 @@ __device__ __forceinline__ float r2_fixed(const DevSys& S, uint4 a, uint4 b)
 }
 
 // ---------------------------------------------------------------- pair energy, FP32
-// Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
-// overflow set `inf` instead of adding +inf, so the compensated sums stay finite.
-// The terms are discontinuous at the pair cutoff, the Coulomb cutoff and the
-// hard-sphere contact; when the FP32 distance is within 1e-5 (relative) of one of
-// them, the reference FP64 distance (sqdist of the FP64 positions xi and particle
-// j) decides which side the pair is on, so inclusion matches the FP64 oracle.
-// `xj` (optional) replaces particle j's resident FP64 position when the caller
-// knows a newer one than memory holds.  `mag` accumulates the sum of |summand|
-// over the enabled terms, LJ's r^-12 and r^-6 parts counted separately (the
-// floating-point error scale of this pair energy).
-__device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int pidx, float r2, const double* xi,
-                                          int j, bool& inf, bool& nan, float& mag, const double* xj = nullptr)
+// The enabled terms at FP32 r^2 with the cutoff decisions already made (in_pair: inside
+// the pair cutoff; in_coul: inside the Coulomb cutoff; overlap: hard-sphere contact).
+__device__ __forceinline__ float pair_core(const DevSys& S, const PairF& p, float r2, bool in_pair, bool in_coul,
+                                           bool overlap, bool& inf, bool& nan, float& mag)
 {
     const int terms = S.terms;
-    const bool cut_coul = (terms & FAU_PAIR_COULOMB) && S.coul_type != FAU_COUL_PLAIN;
-    bool in_pair = !(S.rc2_pair > 0.f && r2 >= S.rc2_pair);
-    bool in_coul = r2 < S.rc2_coul;
-    bool overlap = (terms & FAU_PAIR_HS) && r2 < p.hs2;
-    const bool near = (S.rc2_pair > 0.f && fabsf(r2 - S.rc2_pair) <= 1e-5f * S.rc2_pair) ||
-                      (cut_coul && fabsf(r2 - S.rc2_coul) <= 1e-5f * S.rc2_coul) ||
-                      ((terms & FAU_PAIR_HS) && fabsf(r2 - p.hs2) <= 1e-5f * p.hs2);
-    if (near) {
-        const double xr[3] = {xj ? xj[0] : S.x[j], xj ? xj[1] : S.y[j], xj ? xj[2] : S.z[j]};
-        const double r2d = sqdist_d(S, xi, xr);
-        in_pair = !(S.rc2_pair_d > 0.0 && r2d >= S.rc2_pair_d);
-        in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
-        overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
-    }
     if (!in_pair) return 0.f;
     float u = 0.f, m = 0.f;
     if (terms & FAU_PAIR_COULOMB) {
@@ -359,6 +337,147 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
     }
     mag += m;
     return u;
+}
+
+// N pairs away from every guard band at once, each with exactly pair_u32_far's arithmetic;
+// the loop over the pairs sits inside each term (and every per-pair condition is a
+// select), so the N dependency chains interleave instead of running one after another.
+template <int N>
+__device__ __forceinline__ void pair_far_multi(const DevSys& S, const PairF* p, const float* r2, float* u, bool* inf,
+                                               bool* nan)
+{
+    const int terms = S.terms;
+    float uu[N], mm[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        uu[j] = 0.f;
+        mm[j] = 0.f;
+    }
+    if (terms & FAU_PAIR_COULOMB) {
+        if (S.coul_type == FAU_COUL_PLAIN) {
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const float c = p[j].qq * rsqrtf(r2[j]);
+                uu[j] += c;
+                mm[j] += fabsf(c);
+            }
+        }
+        else if (S.coul_type == FAU_COUL_EWALD) {
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const float r = __fsqrt_rn(r2[j]);
+                const float cv = p[j].qq * erfcf(S.alpha * r) * __frcp_rn(r);
+                const float c = r2[j] < S.rc2_coul ? cv : 0.f;
+                uu[j] += c;
+                mm[j] += fabsf(c);
+            }
+        }
+        else if (S.coul_type == FAU_COUL_TRUNC) {
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const float r = __fsqrt_rn(r2[j]), q = r * S.inv_rc, ir = __frcp_rn(r);
+                float sp = 0.f, sa = 0.f;
+                for (int k = S.npoly - 1; k >= 0; k--) {
+                    sp = fmaf(sp, q, S.cpoly[k]);
+                    sa = fmaf(sa, q, fabsf(S.cpoly[k]));
+                }
+                float e = 0.f;
+                if (S.cerfc != 0.f) e = S.cerfc * erfcf(S.alpha * r);
+                const float pq = p[j].qq * ir;
+                const bool in = r2[j] < S.rc2_coul;
+                uu[j] += in ? pq * (sp + e) : 0.f;
+                mm[j] += in ? fabsf(pq) * (sa + fabsf(e)) : 0.f;
+                uu[j] += 0.f; // the c = 0 term of the other forms
+            }
+        }
+        else {
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const float c = r2[j] < S.rc2_coul ? p[j].qq * rsqrtf(r2[j]) : 0.f;
+                uu[j] += c;
+                mm[j] += fabsf(c);
+            }
+        }
+    }
+    if (terms & (FAU_PAIR_LJ | FAU_PAIR_WCA)) {
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            float x = p[j].s2 * __frcp_rn(r2[j]);
+            x = x * x * x;
+            if (terms & FAU_PAIR_LJ) {
+                uu[j] += p[j].e4 * (x * x - x);
+                mm[j] += fabsf(p[j].e4) * (x * x + x);
+            }
+            if (terms & FAU_PAIR_WCA) {
+                const bool in = !(r2[j] > p[j].s2 * 1.2599210498948732f);
+                uu[j] += in ? p[j].e4 * (x * x - x + 0.25f) : 0.f;
+                mm[j] += in ? fabsf(p[j].e4) * (x * x + x + 0.25f) : 0.f;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const bool in_pair = !(S.rc2_pair > 0.f && r2[j] >= S.rc2_pair);
+        const bool overlap = (terms & FAU_PAIR_HS) && r2[j] < p[j].hs2;
+        bool fi = in_pair && overlap, fn = false;
+        float v = in_pair ? uu[j] : 0.f;
+        if (in_pair && !isfinite(v)) {
+            if (isnan(v) && !(p[j].s2 == p[j].s2)) fn = true;
+            else fi = true;
+            v = 0.f;
+        }
+        u[j] = v;
+        inf[j] = fi;
+        nan[j] = fn;
+    }
+}
+
+// Whether FP32 r^2 lies within the 1e-5 guard band of a cutoff or contact distance, where
+// the FP64 distance decides (pair_u32).
+__device__ __forceinline__ bool pair_near(const DevSys& S, const PairF& p, float r2)
+{
+    const int terms = S.terms;
+    const bool cut_coul = (terms & FAU_PAIR_COULOMB) && S.coul_type != FAU_COUL_PLAIN;
+    return (S.rc2_pair > 0.f && fabsf(r2 - S.rc2_pair) <= 1e-5f * S.rc2_pair) ||
+           (cut_coul && fabsf(r2 - S.rc2_coul) <= 1e-5f * S.rc2_coul) ||
+           ((terms & FAU_PAIR_HS) && fabsf(r2 - p.hs2) <= 1e-5f * p.hs2);
+}
+
+// A pair away from every guard band (pair_near false): the FP32 decisions are exact.
+__device__ __forceinline__ float pair_u32_far(const DevSys& S, const PairF& p, float r2, bool& inf, bool& nan,
+                                              float& mag)
+{
+    const bool in_pair = !(S.rc2_pair > 0.f && r2 >= S.rc2_pair);
+    const bool in_coul = r2 < S.rc2_coul;
+    const bool overlap = (S.terms & FAU_PAIR_HS) && r2 < p.hs2;
+    return pair_core(S, p, r2, in_pair, in_coul, overlap, inf, nan, mag);
+}
+
+// Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
+// overflow set `inf` instead of adding +inf, so the compensated sums stay finite.
+// The terms are discontinuous at the pair cutoff, the Coulomb cutoff and the
+// hard-sphere contact; when the FP32 distance is within 1e-5 (relative) of one of
+// them, the reference FP64 distance (sqdist of the FP64 positions xi and particle
+// j) decides which side the pair is on, so inclusion matches the FP64 oracle.
+// `xj` (optional) replaces particle j's resident FP64 position when the caller
+// knows a newer one than memory holds.  `mag` accumulates the sum of |summand|
+// over the enabled terms, LJ's r^-12 and r^-6 parts counted separately (the
+// floating-point error scale of this pair energy).
+__device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int pidx, float r2, const double* xi,
+                                          int j, bool& inf, bool& nan, float& mag, const double* xj = nullptr)
+{
+    const int terms = S.terms;
+    bool in_pair = !(S.rc2_pair > 0.f && r2 >= S.rc2_pair);
+    bool in_coul = r2 < S.rc2_coul;
+    bool overlap = (terms & FAU_PAIR_HS) && r2 < p.hs2;
+    if (pair_near(S, p, r2)) {
+        const double xr[3] = {xj ? xj[0] : S.x[j], xj ? xj[1] : S.y[j], xj ? xj[2] : S.z[j]};
+        const double r2d = sqdist_d(S, xi, xr);
+        in_pair = !(S.rc2_pair_d > 0.0 && r2d >= S.rc2_pair_d);
+        in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
+        overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
+    }
+    return pair_core(S, p, r2, in_pair, in_coul, overlap, inf, nan, mag);
 }
 
 // FAU_COUL_TRUNC short-range function in FP64: e erfc(alpha r) + Horner in q = r / Rc

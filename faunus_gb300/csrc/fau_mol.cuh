@@ -26,14 +26,52 @@ __device__ __forceinline__ void compute_barrier(int nthreads)
     asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
+// One (neighbour group, moved atom) task for an NB-site neighbour: its NB records loaded
+// together, the 2 NB pair distances formed, and -- unless one lies in a guard band, where
+// pair_u32's FP64 check must decide (returns false) -- all pair energies evaluated at once,
+// then accumulated in the per-pair order of the general path.
+template <int NB>
+__device__ __forceinline__ bool mol_task_fast(const DevSys& S, const PairF* pt, int nt, int ta, uint4 ra_n, uint4 ra_o,
+                                              int hb, bool do_n, bool do_o, FF& acc, int& flags,
+                                              unsigned long long& n_pairs)
+{
+    uint4 rb[NB];
+#pragma unroll
+    for (int j = 0; j < NB; j++) rb[j] = S.rec[hb + j];
+    PairF pp[2 * NB];
+    float r2[2 * NB];
+    bool near = false;
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        const PairF p = pt[ta * nt + (int)(rb[j].w >> 24)];
+        pp[j] = p;
+        pp[NB + j] = p;
+        r2[j] = r2_fixed(S, ra_n, rb[j]);
+        r2[NB + j] = r2_fixed(S, ra_o, rb[j]);
+        near |= (do_n && pair_near(S, p, r2[j])) || (do_o && pair_near(S, p, r2[NB + j]));
+    }
+    if (near) return false;
+    float u[2 * NB];
+    bool fi[2 * NB], fn[2 * NB];
+    pair_far_multi<2 * NB>(S, pp, r2, u, fi, fn);
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        add_pair(acc, flags, do_n ? u[j] : 0.f, do_o ? u[NB + j] : 0.f, do_n && fi[j], do_o && fi[NB + j],
+                 do_n && fn[j], do_o && fn[NB + j]);
+    }
+    n_pairs += (unsigned long long)NB * ((do_n ? 1 : 0) + (do_o ? 1 : 0));
+    return true;
+}
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
 {
     constexpr int NW = NT / 32;
     constexpr int NWC = NW - 1;   // compute warps
     constexpr int NTC = NT - 32;  // compute threads
-    constexpr int RC = 2;         // candidate groups per compute thread per chunk
-    constexpr int CH = RC * NTC;  // candidate groups per chunk
+    constexpr int RC = 6;         // candidate groups per compute thread per chunk (1344: one chunk
+    constexpr int CH = RC * NTC;  // covers a 1,000-molecule system, one barrier pair per move)
+    constexpr int SB = 2;         // candidates whose loads are in flight together
     const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ctid = tid - 32; // compute-thread index (warps 1..)
@@ -59,7 +97,8 @@ __global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
     __shared__ MoveShared msb[2];
     __shared__ FF red_a[NW];
     __shared__ int red_f[NW];
-    __shared__ uint32_t nbl[CH];
+    __shared__ uint32_t nbl[CH];   // neighbour group | interacting states
+    __shared__ uint32_t nbl_b[CH]; // its first particle | atom count << 24
     __shared__ int nbl_cnt[2];
     __shared__ int sh_prev_accept, sh_stop;
     __shared__ long long sh_consumed;
@@ -91,7 +130,8 @@ __global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
     long long consumed = nmoves;
 
     // phase timers (profiling only): warp 0 (tid 0): 6 prepare ahead, 3 wait B1, 4 decision,
-    // 5 commit (+ re-prepare), 7 B2; warp 1 (tid 32): 0 deferred Q, 1 Ewald, 2 pairs, 9 B1, 10 B2; 11 moves
+    // 5 commit (+ re-prepare), 7 B2; warp 1 (tid 32): 0 deferred Q, 1 Ewald, 11 GroupCutoff passes,
+    // 12 pair tasks, 2 the rest of the pairs, 9 B1, 10 B2; last: moves
     const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
     unsigned long long tacc[kPhaseSlots] = {0};
     long long tprev = timing ? clock64() : 0;
@@ -162,7 +202,7 @@ __global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
             }
             if (timing) {
                 tick(0);
-                if (tid == 32) tacc[11]++;
+                if (tid == 32) tacc[kPhaseSlots - 1]++;
             }
             if (kind != FAU_MOVE_NONE) {
                 if (K) {
@@ -212,48 +252,64 @@ __global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
                 int chunk = 0;
                 for (int base = 0; base < GN; base += CH, chunk++) {
                     int* cntp = &nbl_cnt[chunk & 1];
-                    int gfl[RC], gml[RC];
-                    uint4 gcr[RC];
+                    for (int r0 = 0; r0 < RC; r0 += SB) {
+                        if (base + r0 * NTC >= GN) break; // uniform: the ballots below stay full-warp
+                        int gfl[SB], gml[SB], gb0[SB], gb1[SB];
+                        uint4 gcr[SB];
 #pragma unroll
-                    for (int r = 0; r < RC; r++) {
-                        const int h = base + r * NTC + ctid;
-                        gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
-                        gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
-                        gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
-                    }
-#pragma unroll
-                    for (int r = 0; r < RC; r++) {
-                        const int h = base + r * NTC + ctid;
-                        uint32_t e = 0;
-                        if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
-                            double c2 = S.cut_g2g2;
-                            float c2f = S.cut_g2g2f;
-                            if (S.n_mol > 0) {
-                                const int kk = mol_g * S.n_mol + gml[r];
-                                c2 = S.cut2_mol[kk];
-                                c2f = S.cut2_molf[kk];
-                            }
-                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
-                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
-                            e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
+                        for (int r = 0; r < SB; r++) { // all loads first: their latencies overlap
+                            const int h = base + (r0 + r) * NTC + ctid;
+                            gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
+                            gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                            gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
+                            gb0[r] = h < GN ? S.g_begin[h] : 0;
+                            gb1[r] = h < GN ? S.g_begin[h + 1] : 0;
                         }
-                        const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
-                        int wpos = 0;
-                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
-                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
-                        if (e) nbl[wpos + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)h | e;
+#pragma unroll
+                        for (int r = 0; r < SB; r++) {
+                            const int h = base + (r0 + r) * NTC + ctid;
+                            uint32_t e = 0;
+                            if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
+                                double c2 = S.cut_g2g2;
+                                float c2f = S.cut_g2g2f;
+                                if (S.n_mol > 0) {
+                                    const int kk = mol_g * S.n_mol + gml[r];
+                                    c2 = S.cut2_mol[kk];
+                                    c2f = S.cut2_molf[kk];
+                                }
+                                const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
+                                const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
+                                e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
+                            }
+                            const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
+                            int wpos = 0;
+                            if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
+                            wpos = __shfl_sync(0xffffffffu, wpos, 0);
+                            if (e) {
+                                const int slot = wpos + __popc(bal & ((1u << lane) - 1u));
+                                nbl[slot] = (uint32_t)h | e;
+                                nbl_b[slot] = (uint32_t)gb0[r] | ((uint32_t)(gb1[r] - gb0[r]) << 24);
+                            }
+                        }
                     }
                     compute_barrier(NTC);
+                    tick(11);
                     const int cnt = *cntp;
                     if (ctid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
                     for (int task = ctid; task < cnt * m; task += NTC) {
                         const int q = task / m, a = task - q * m;
                         const uint32_t ent = nbl[q];
-                        const int h = (int)(ent & kNblGroup);
                         const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
-                        const int hb = S.g_begin[h], he = S.g_begin[h + 1];
+                        const uint32_t hbn = nbl_b[q];
+                        const int hb = (int)(hbn & 0xFFFFFFu), nb = (int)(hbn >> 24), he = hb + nb;
                         const uint4 ra_n = ms.rec_new[a], ra_o = ms.rec_old[a];
                         const int ta = ra_n.w >> 24;
+                        // 3- and 4-site neighbours away from every guard band: all pairs of both
+                        // states evaluated together (pair_far_multi)
+                        bool done = false;
+                        if (nb == 3) done = mol_task_fast<3>(S, pt, nt, ta, ra_n, ra_o, hb, do_n, do_o, accp, flags, n_pairs);
+                        else if (nb == 4) done = mol_task_fast<4>(S, pt, nt, ta, ra_n, ra_o, hb, do_n, do_o, accp, flags, n_pairs);
+                        if (done) continue;
                         for (int b = hb; b < he; b++) {
                             const uint4 rb = S.rec[b];
                             const int pidx = ta * nt + (int)(rb.w >> 24);
@@ -271,6 +327,7 @@ __global__ void __launch_bounds__(NT) mol_chain_kernel(ChainArgs A)
                         }
                     }
                     compute_barrier(NTC);
+                    tick(12);
                 }
                 if (ctid == 0) nbl_cnt[0] = nbl_cnt[1] = 0;
                 for (int t = ctid; t < S.n_atomic; t += NTC) { // atomic groups are never cut
@@ -446,19 +503,19 @@ __host__ __device__ inline size_t mol_smem_bytes(int K, int nc)
     return chain_smem_bytes_v2(K, nc) + (size_t)kTableAtoms * 6 * (2 * nc + 1) * sizeof(float2);
 }
 
-template <int NT>
+template <int NT, int MINB>
 cudaError_t launch_mol_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
 {
     static size_t granted = 0;
     const size_t smem = mol_smem_bytes(K, nc);
     if (smem > granted || granted == 0) {
-        cudaError_t e = cudaFuncSetAttribute(mol_chain_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mol_chain_kernel<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         granted = smem;
     }
     if (prepare_only) return cudaSuccess;
-    mol_chain_kernel<NT><<<nblocks, NT, smem, st>>>(a);
+    mol_chain_kernel<NT, MINB><<<nblocks, NT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
