@@ -416,7 +416,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         cudaFree(d_phase);
         static const char* names_e[kPhaseSlots] = {"deferred_q", "ewald", "pairs", "reduce+B1", "decision", "commit",
                                                    "prepare", "B2(w0)", "compute(w1)", "B1(w1)", "B2(w1)",
-                                                   "cutoff_pass(w1)", "pair_tasks(w1)", "moves"};
+                                                   "cutoff_pass(w1)", "pair_tasks(w1)", "prep:proposal",
+                                                   "prep:positions", "prep:tables", "moves"};
         static const char* names_f[kFastPhaseSlots] = {
             "P:commit_data", "P:prepare", "P:copies", "P:B1", "P:decision", "P:commit", "P:B2",
             "C:preload", "C:ewald", "C:pairs", "C:sums", "C:B1", "C:decision", "C:q_update", "C:B2", "moves",

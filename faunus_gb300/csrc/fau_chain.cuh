@@ -227,8 +227,10 @@ __device__ __forceinline__ float2 phase_exact(uint32_t P)
 // src/move.cpp:225-240; Group::translate src/group.cpp:115-123 then Group::rotate
 // src/group.cpp:110-113, src/geometry.h:613-627), fixed-point records, cells, and
 // the phase tables of the moved atoms.
-static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p, int lane, float2* tab, int nc)
+static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms, const Proposal& p, int lane, float2* tab, int nc,
+                                                 unsigned long long* tsub = nullptr)
 {
+    const long long tp0 = tsub ? clock64() : 0;
     const int TS = 2 * nc + 1;
     // host proposals are checked here, where they are read: an index out of range or an unknown
     // kind ends the chain with FAU_ERR_ARG before anything is indexed with it
@@ -360,6 +362,7 @@ static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms
         ms.first = -1;
     }
     __syncwarp();
+    const long long tp1 = tsub ? clock64() : 0;
     // phase tables: per atom (a < min(m, kTableAtoms)), per axis d, n = 0..nc
     if (tab && m <= kTableAtoms) {
         const int per_atom = 6 * (nc + 1);
@@ -383,6 +386,11 @@ static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms
             t[nc + n] = v;
             t[nc - n] = make_float2(v.x, -v.y);
         }
+    }
+    if (tsub) { // profiling: positions, then phase tables
+        const long long tp2 = clock64();
+        tsub[0] += (unsigned long long)(tp1 - tp0);
+        tsub[1] += (unsigned long long)(tp2 - tp1);
     }
 }
 

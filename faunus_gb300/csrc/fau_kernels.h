@@ -35,7 +35,7 @@ struct ChainArgs {
     // optional per-CTA phase timers (clock64 cycles, kPhaseSlots per CTA) for profiling
     unsigned long long* phase_cycles;
 };
-constexpr int kPhaseSlots = 14;     // chain kernel (last slot: move count)
+constexpr int kPhaseSlots = 17;     // chain kernel (last slot: move count)
 constexpr int kFastPhaseSlots = 24; // pipelined kernel (the per-CTA stride of phase_cycles for both)
 
 // One trial move held for a later commit (plain FP64 form and evaluate-only mode).

@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
             if (mv + 1 < nmoves) {
                 const Proposal p =
                     philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
-                prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);
+                tick(13);
+                prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc, timing ? &tacc[14] : nullptr);
             }
             tick(6);
         }

@@ -5,24 +5,40 @@
 
 namespace fau {
 
-// resident CTAs per SM the register allocation is sized for (FAU_MOL_MINB: 2, 3 or 4)
-static int mol_minb()
+// Registers are sized for 2 or 3 resident CTAs per SM (128 or 80 per thread; 80 spills more,
+// a full wave of 3 per SM measured ~4 % faster than one of 2).  A launch takes the size
+// whose waves fill the SMs better: e.g. 608 chains on 152 SMs run as 2 waves of 2 per SM,
+// 456 or 912 as waves of 3.  FAU_MOL_MINB=2 or 3 fixes it.
+static int mol_minb(int nblocks)
 {
-    static int v = [] {
+    static int forced = [] {
         const char* e = std::getenv("FAU_MOL_MINB");
-        const int x = e ? std::atoi(e) : 2;
-        return (x == 3 || x == 4) ? x : 2;
+        const int x = e ? std::atoi(e) : 0;
+        return (x == 2 || x == 3) ? x : 0;
     }();
-    return v;
+    if (forced) return forced;
+    static int sms = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    auto fill = [&](int o, double speed) {
+        const long long per_wave = (long long)o * sms;
+        const long long waves = (nblocks + per_wave - 1) / per_wave;
+        return speed * (double)nblocks / (double)(waves * per_wave);
+    };
+    return fill(3, 1.04) > fill(2, 1.0) ? 3 : 2;
 }
 
 cudaError_t mol_dispatch_256(const ChainArgs& a, int nb, int K, int nc, cudaStream_t st, bool prep)
 {
-    switch (mol_minb()) {
-    case 3: return launch_mol_inst<256, 3>(a, nb, K, nc, st, prep);
-    case 4: return launch_mol_inst<256, 4>(a, nb, K, nc, st, prep);
-    default: return launch_mol_inst<256, 2>(a, nb, K, nc, st, prep);
+    if (prep) { // both register sizes get their shared-memory allowance before any capture
+        const cudaError_t e = launch_mol_inst<256, 2>(a, nb, K, nc, st, true);
+        return e != cudaSuccess ? e : launch_mol_inst<256, 3>(a, nb, K, nc, st, true);
     }
+    return mol_minb(nb) == 3 ? launch_mol_inst<256, 3>(a, nb, K, nc, st, false)
+                             : launch_mol_inst<256, 2>(a, nb, K, nc, st, false);
 }
 
 size_t mol_smem_bytes_total(int K, int nc)
