@@ -390,7 +390,7 @@ def other_configs(ctx, configs, replicas: int) -> dict:
     out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps}
     mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 500)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
-                              "kernel": "chain kernel (molecular moves), 256 threads"}
+                              "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
     specs, temps = configs.pt_replicas(n_rep=256)
     systems = [ctx.create(s_) for s_ in specs]
     st = ctx.run_batch(systems, swap_interval=2000, n_swap_blocks=5, temperatures=temps, seed=3, dp=2.0)
