@@ -221,7 +221,11 @@ def run_ours(args) -> None:
     from faunus_gb300 import configs
 
     ctx = F.Context(local)
-    base = configs.bulk_ewald(n_salt=10000, seed=1)
+    water = args.workload == "water"
+    if water and not args.value_only:
+        raise SystemExit("--workload water is a profiling case: use it with --value-only")
+    base = configs.spce_water(n_mol=1000) if water else configs.bulk_ewald(n_salt=10000, seed=1)
+    dp, dprot = (0.5, 0.5) if water else (2.0, 0.0)
     sms = _sm_count(local)
     R = args.replicas or 4 * sms  # four chains per SM: the pipelined kernel's occupancy limit
     M = args.moves
@@ -233,6 +237,8 @@ def run_ours(args) -> None:
     # ---- kernel configuration: the autotuner's choice unless --threads is given
     tuned = None
     threads = args.threads
+    if water:
+        threads = max(threads, 0)  # molecular moves: the pipelined molecular kernel
     if threads < 0:
         from faunus_gb300 import autotune
         tuned = autotune.tune(ctx, first, replicas=max(8, R // 4), moves=1000, force=True,
@@ -241,8 +247,8 @@ def run_ours(args) -> None:
 
     # ---- value: device RNG, resident state
     def step(k):
-        return ctx.run_batch(systems, M, seed=args.seed, counter_base=k * M, streams=streams, dp=2.0,
-                             threads=threads)
+        return ctx.run_batch(systems, M, seed=args.seed, counter_base=k * M, streams=streams, dp=dp,
+                             dprot=dprot, threads=threads)
 
     for w in range(args.warmup):
         step(w)
@@ -265,7 +271,8 @@ def run_ours(args) -> None:
     if args.value_only:
         if rank == 0:
             print(json.dumps({"metric": "MC trial moves/sec", "value": value, "unit": "moves/s",
-                              "ms_per_step": 1e3 * dev_s / args.steps, "replicas": R, "moves": M}), flush=True)
+                              "ms_per_step": 1e3 * dev_s / args.steps, "replicas": R, "moves": M,
+                              "workload": args.workload}), flush=True)
         ctx.close()
         _barrier(dist)
         return
@@ -466,6 +473,8 @@ def main():
     ap.add_argument("--cpu-sample-seconds", type=float, default=0.5,
                     help="reference arm: seconds of CPU chain work per thread and step")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
+    ap.add_argument("--workload", default="bulk", choices=["bulk", "water"],
+                    help="water: 1,000 rigid SPC/E molecules, molecular moves (profiling case, with --value-only)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
