@@ -214,6 +214,24 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _hbm_roofline(bytes_per_move, moves_per_s_per_gpu):
+    """The HBM side of the roofline: DRAM bytes per move measured by ncu on the same kernel
+    (cold cache) x moves/s, against the measured copy bandwidth of MEASURED_PEAKS.json.  Not
+    the binding bound: each chain's state stays in shared memory and L2 between moves."""
+    peaks = Path(__file__).resolve().parent / "MEASURED_PEAKS.json"
+    try:
+        peak = float(json.loads(peaks.read_text())["hbm_gbs"])
+        src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError, KeyError):
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    if not bytes_per_move:
+        return None
+    achieved = bytes_per_move * moves_per_s_per_gpu / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_move": bytes_per_move, "peak_source": src,
+            "note": "DRAM bytes per move measured by ncu (cold cache), not algorithmic bytes"}
+
+
 def run_ours(args) -> None:
     dist, rank, local, world = _dist_init(args.gpus)
     import faunus_gb300 as F
@@ -337,6 +355,7 @@ def run_ours(args) -> None:
                      "peak_source": "measured FP32 FMA probe (fau_measure_fp32_peak) in this run",
                      "work": f"{FLOPS_PER_K_UPDATE:g} flop per k-vector x moved atom + {FLOPS_PER_PAIR:g} per pair",
                      "traffic_source": src},
+        "roofline_hbm": _hbm_roofline(bytes_per_move, value / world),
         "clocks": clk,
         "gpu_launches": 3 * args.steps,
         "wall_s": wall,
