@@ -1,0 +1,69 @@
+"""Extract the reference's example runs into compact fixtures.
+
+Reads, as data, from the Faunus tree given on the command line (default: /root/reference):
+
+  examples/bulk: bulk.yml (the input, converted with the package's YAML reader),
+    bulk.state.json (the state the run saved at its end) and bulk.out.json (its output:
+    Bjerrum length and the final energies of the particle-self-energy and nonbonded
+    terms) -> bulk_example.json (input + expected values with provenance) and
+    bulk_example_state.npz (particle ids, positions, charges);
+  examples/minimal: minimal.yml and minimal.out.json (SystemEnergy mean over its run, the
+    statistical fixture) -> minimal_example.json.
+
+The tests read only the written files.
+"""
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+from faunus_gb300 import yason  # noqa: E402
+
+ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+
+
+def main() -> None:
+    ex = ROOT / "examples" / "bulk"
+    inp = yason.loads((ex / "bulk.yml").read_text())
+    state = json.loads((ex / "bulk.state.json").read_text())
+    out = json.loads((ex / "bulk.out.json").read_text())
+    nb = out["energy"][0]["hamiltonian"][1]["nonbonded"]
+    coul = next(p["coulomb"] for p in nb["pairpot"] if "coulomb" in p)
+    final = next(a["systemenergy"]["final"] for a in out["analysis"] if "systemenergy" in a)
+    fixture = {
+        "provenance": {"input": "examples/bulk/bulk.yml", "state": "examples/bulk/bulk.state.json",
+                       "output": "examples/bulk/bulk.out.json", "git revision": out["git revision"],
+                       "compiler": out["compiler"]},
+        "input": inp,
+        "geometry": state["geometry"],
+        "groups": state["groups"],
+        "expected": {"bjerrum_length": coul["lB"], "self": final[0], "nonbonded": final[1],
+                     "temperature": out["temperature"]},
+    }
+    (HERE / "bulk_example.json").write_text(json.dumps(fixture, indent=1))
+    parts = state["particles"]
+    mex = ROOT / "examples" / "minimal"
+    mout = json.loads((mex / "minimal.out.json").read_text())
+    se = next(a["systemenergy"] for a in mout["analysis"] if "systemenergy" in a)
+    mv = mout["moves"][0]["transrot"]
+    fpot = mout["energy"][0]["hamiltonian"][1]["nonbonded"]["pairpot"]["functor potential"]["default"]
+    mlb = next(t["coulomb"]["lB"] for t in fpot if "coulomb" in t)
+    (HERE / "minimal_example.json").write_text(json.dumps({
+        "provenance": {"input": "examples/minimal/minimal.yml", "output": "examples/minimal/minimal.out.json",
+                       "git revision": mout["git revision"], "compiler": mout["compiler"]},
+        "input": yason.loads((mex / "minimal.yml").read_text()),
+        "expected": {"bjerrum_length": mlb, "systemenergy_mean": se["mean"], "systemenergy_samples": se["samples"],
+                     "systemenergy_nstep": se["nstep"], "moves": mv["moves"], "acceptance": mv["acceptance"],
+                     "temperature": mout["temperature"]},
+    }, indent=1))
+    np.savez_compressed(HERE / "bulk_example_state.npz",
+                        id=np.array([p["id"] for p in parts], dtype=np.int32),
+                        pos=np.array([p["pos"] for p in parts], dtype=np.float64),
+                        q=np.array([p["q"] for p in parts], dtype=np.float64))
+
+
+if __name__ == "__main__":
+    main()

@@ -213,3 +213,14 @@ def test_bulk_example_golden():
     assert abs(e["nonbonded"] - exp["nonbonded"]) <= 5e-4 * abs(exp["nonbonded"])
     assert e["self"] == pytest.approx(7.0 / 8.0 * exp["self"], rel=1e-12)
     assert s.moves[0]["repeat"] == 1.0 and list(s.moves[0]["type_dp"]) == [1.0, 0.5]
+
+
+def test_minimal_example_input():
+    """examples/minimal: FunctorPotential default [LJ (LB), plain Coulomb epsr 80] on 20 NaCl
+    at 300 K; the Bjerrum length equals the reference's reported value to the last digit."""
+    fx = json.loads((GOLDEN / "minimal_example.json").read_text())
+    s = I.load_input(fx["input"])
+    assert s.spec.n == 40 and s.spec.pair_terms == A.FAU_PAIR_COULOMB | A.FAU_PAIR_LJ
+    assert s.spec.coulomb_type == A.FAU_COUL_PLAIN
+    assert s.spec.bjerrum_length == pytest.approx(fx["expected"]["bjerrum_length"], rel=1e-15)
+    assert math.isfinite(O.OracleSystem(s.spec).energy_total()["total"])
