@@ -8,7 +8,9 @@ Reads, as data, from the Faunus tree given on the command line (default: /root/r
     terms) -> bulk_example.json (input + expected values with provenance) and
     bulk_example_state.npz (particle ids, positions, charges);
   examples/minimal: minimal.yml and minimal.out.json (SystemEnergy mean over its run, the
-    statistical fixture) -> minimal_example.json.
+    statistical fixture) -> minimal_example.json;
+  examples/langevin: montecarlo_lj.yml, montecarlo_lj.out.json and rdf_mc.dat (the AtomRDF
+    g(r) its MC run wrote) -> montecarlo_lj_example.json.
 
 The tests read only the written files.
 """
@@ -59,6 +61,19 @@ def main() -> None:
                      "systemenergy_nstep": se["nstep"], "moves": mv["moves"], "acceptance": mv["acceptance"],
                      "temperature": mout["temperature"]},
     }, indent=1))
+    lex = ROOT / "examples" / "langevin"
+    lout = json.loads((lex / "montecarlo_lj.out.json").read_text())
+    rdf = next(a["atomrdf"] for a in lout["analysis"] if "atomrdf" in a)
+    table = [[float(x) for x in line.split()] for line in (lex / "rdf_mc.dat").read_text().splitlines()
+             if line.strip() and not line.startswith("#")]
+    lmv = lout["moves"][0]["transrot"]
+    (HERE / "montecarlo_lj_example.json").write_text(json.dumps({
+        "provenance": {"input": "examples/langevin/montecarlo_lj.yml", "output": "examples/langevin/montecarlo_lj.out.json",
+                       "rdf": "examples/langevin/rdf_mc.dat", "git revision": lout["git revision"]},
+        "input": yason.loads((lex / "montecarlo_lj.yml").read_text()),
+        "expected": {"rdf_samples": rdf["samples"], "dr": rdf["dr"], "nstep": rdf["nstep"], "moves": lmv["moves"],
+                     "acceptance": lmv["acceptance"], "rdf": table},
+    }))
     np.savez_compressed(HERE / "bulk_example_state.npz",
                         id=np.array([p["id"] for p in parts], dtype=np.int32),
                         pos=np.array([p["pos"] for p in parts], dtype=np.float64),
