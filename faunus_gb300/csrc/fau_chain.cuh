@@ -142,13 +142,15 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
     p.quat[0] = 1.0;
     p.quat[1] = p.quat[2] = p.quat[3] = 0.0;
     if (!molecular) {
-        p.kind = FAU_MOVE_ATOMIC;
+        // no displacement is an empty Change, as AtomicTranslateRotate::_move makes it (src/move.cpp:267-293)
+        p.kind = dp > 0.f ? FAU_MOVE_ATOMIC : FAU_MOVE_NONE;
         const uint32_t n = S.n_atomic > 0 ? (uint32_t)S.n_atomic : (uint32_t)S.n;
         const uint32_t j = __umulhi(c1.x, n);
         p.index = S.n_atomic > 0 ? S.atomic_idx[j] : (int)j;
     }
     else {
-        p.kind = FAU_MOVE_MOLECULAR;
+        // no translation and no rotation is an empty Change (TranslateRotate::_move, src/move.cpp:1670-1689)
+        p.kind = (dp > 0.f || dprot > 0.0) ? FAU_MOVE_MOLECULAR : FAU_MOVE_NONE;
         p.index = (int)__umulhi(c1.x, (uint32_t)S.n_groups);
         if (dprot > 0.0) {
             // uniform axis, angle dprot (U - 1/2); the half-angle sine/cosine and the axis come

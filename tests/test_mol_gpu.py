@@ -81,3 +81,19 @@ def test_molecular_kernel_parallel_tempering_and_counters(ctx):
     assert sum(x["moves"] for x in c) == 8000 and sum(x["accepted"] for x in c) == st["accepted"]
     for r in reps:
         _consistent(r)
+
+
+@pytest.mark.parametrize("dp,dprot", [(0.5, 0.0), (0.0, 0.5), (0.0, 0.0)])
+def test_molecular_kernel_translation_rotation_only_and_empty_moves(ctx, dp, dprot):
+    spec = configs.spce_water(n_mol=256, L=18.6, seed=11)
+    a, b = ctx.create(spec), ctx.create(spec)
+    pos0 = a.positions()
+    sa = ctx.run_batch([a], 1500, seed=3, dp=dp, dprot=dprot, threads=0)
+    sb = ctx.run_batch([b], 1500, seed=3, dp=dp, dprot=dprot, threads=256)
+    assert sa["moves"] == sb["moves"] and sa["accepted"] == sb["accepted"]
+    assert np.array_equal(a.positions(), b.positions())
+    if dp == 0.0 and dprot == 0.0:  # empty changes: nothing moves, nothing is counted as a move
+        assert sa["moves"] == 0 and np.array_equal(a.positions(), pos0)
+    else:
+        assert sa["accepted"] > 100
+    _consistent(a)
