@@ -54,9 +54,12 @@ _PROBE = r"""
 #define O(t, f) printf(#t "." #f " %zu\n", offsetof(t, f));
 int main(void) {
   S(fau_ewald_desc) S(fau_sys_desc) S(fau_energy_terms) S(fau_trial_result) S(fau_proposal)
-  S(fau_run_stats) S(fau_batch_params) S(fau_batch_stats) S(fau_move_desc)
+  S(fau_run_stats) S(fau_batch_params) S(fau_batch_stats) S(fau_move_desc) S(fau_sampler_desc)
   O(fau_sys_desc, ewald) O(fau_sys_desc, precision) O(fau_sys_desc, pair_cutoff) O(fau_sys_desc, n_types)
   O(fau_proposal, u) O(fau_batch_params, temperatures) O(fau_move_desc, groups) O(fau_trial_result, accepted)
+  O(fau_sys_desc, cutoff_g2g_pairs) O(fau_sys_desc, coulomb_poly) O(fau_sys_desc, pressure)
+  O(fau_batch_params, sampler) O(fau_batch_params, n_sample_blocks) O(fau_move_desc, volume_method)
+  O(fau_sampler_desc, rdf_dr) O(fau_sampler_desc, energy)
   return 0;
 }
 """
@@ -71,13 +74,20 @@ def test_struct_layouts_match_header(tmp_path):
                                                                check=True).stdout.split("\n") if line)
     sizes = {"fau_ewald_desc": A.EwaldDesc, "fau_sys_desc": A.SysDesc, "fau_energy_terms": A.EnergyTerms,
              "fau_trial_result": A.TrialResult, "fau_proposal": A.Proposal, "fau_run_stats": A.RunStats,
-             "fau_batch_params": A.BatchParams, "fau_batch_stats": A.BatchStats, "fau_move_desc": A.MoveDesc}
+             "fau_batch_params": A.BatchParams, "fau_batch_stats": A.BatchStats, "fau_move_desc": A.MoveDesc,
+             "fau_sampler_desc": A.SamplerDesc}
     for name, cls in sizes.items():
         assert int(out[name]) == C.sizeof(cls), name
     offs = {"fau_sys_desc.ewald": A.SysDesc.ewald.offset, "fau_sys_desc.precision": A.SysDesc.precision.offset,
             "fau_sys_desc.pair_cutoff": A.SysDesc.pair_cutoff.offset, "fau_sys_desc.n_types": A.SysDesc.n_types.offset,
             "fau_proposal.u": A.Proposal.u.offset, "fau_batch_params.temperatures": A.BatchParams.temperatures.offset,
-            "fau_move_desc.groups": A.MoveDesc.groups.offset, "fau_trial_result.accepted": A.TrialResult.accepted.offset}
+            "fau_move_desc.groups": A.MoveDesc.groups.offset, "fau_trial_result.accepted": A.TrialResult.accepted.offset,
+            "fau_sys_desc.cutoff_g2g_pairs": A.SysDesc.cutoff_g2g_pairs.offset,
+            "fau_sys_desc.coulomb_poly": A.SysDesc.coulomb_poly.offset, "fau_sys_desc.pressure": A.SysDesc.pressure.offset,
+            "fau_batch_params.sampler": A.BatchParams.sampler.offset,
+            "fau_batch_params.n_sample_blocks": A.BatchParams.n_sample_blocks.offset,
+            "fau_move_desc.volume_method": A.MoveDesc.volume_method.offset,
+            "fau_sampler_desc.rdf_dr": A.SamplerDesc.rdf_dr.offset, "fau_sampler_desc.energy": A.SamplerDesc.energy.offset}
     for k, v in offs.items():
         assert int(out[k]) == v, k
 
