@@ -342,9 +342,11 @@ __device__ __forceinline__ float pair_core(const DevSys& S, const PairF& p, floa
 // N pairs away from every guard band at once, each with exactly pair_u32_far's arithmetic;
 // the loop over the pairs sits inside each term (and every per-pair condition is a
 // select), so the N dependency chains interleave instead of running one after another.
+// lj[j] false: the LJ/WCA terms of pair j are skipped -- only where they are exactly zero
+// (4 eps = 0, sigma finite, r^2 far enough from 0 that (s/r)^12 cannot overflow).
 template <int N>
 __device__ __forceinline__ void pair_far_multi(const DevSys& S, const PairF* p, const float* r2, float* u, bool* inf,
-                                               bool* nan)
+                                               bool* nan, const bool* lj)
 {
     const int terms = S.terms;
     float uu[N], mm[N];
@@ -402,6 +404,7 @@ __device__ __forceinline__ void pair_far_multi(const DevSys& S, const PairF* p, 
     if (terms & (FAU_PAIR_LJ | FAU_PAIR_WCA)) {
 #pragma unroll
         for (int j = 0; j < N; j++) {
+            if (!lj[j]) continue;
             float x = p[j].s2 * __frcp_rn(r2[j]);
             x = x * x * x;
             if (terms & FAU_PAIR_LJ) {

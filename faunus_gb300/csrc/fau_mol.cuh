@@ -51,9 +51,19 @@ __device__ __forceinline__ bool mol_task_fast(const DevSys& S, const PairF* pt, 
         near |= (do_n && pair_near(S, p, r2[j])) || (do_o && pair_near(S, p, r2[NB + j]));
     }
     if (near) return false;
+    // the LJ/WCA part of pair j is skipped where it is exactly zero for every lane of the warp
+    // (tasks are ordered by moved atom, so a warp mostly shares it: for SPC/E only O-O pairs remain)
+    bool lj[2 * NB];
+    const unsigned act = __activemask();
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+        const float tiny = pp[j].s2 * 1e-6f;
+        const bool need = !(pp[j].e4 == 0.f) || !(pp[j].s2 == pp[j].s2) || r2[j] < tiny || r2[NB + j] < tiny;
+        lj[j] = lj[NB + j] = __any_sync(act, need) != 0;
+    }
     float u[2 * NB];
     bool fi[2 * NB], fn[2 * NB];
-    pair_far_multi<2 * NB>(S, pp, r2, u, fi, fn);
+    pair_far_multi<2 * NB>(S, pp, r2, u, fi, fn, lj);
 #pragma unroll
     for (int j = 0; j < NB; j++) {
         add_pair(acc, flags, do_n ? u[j] : 0.f, do_o ? u[NB + j] : 0.f, do_n && fi[j], do_o && fi[NB + j],
@@ -298,7 +308,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                     const int cnt = *cntp;
                     if (ctid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
                     for (int task = ctid; task < cnt * m; task += NTC) {
-                        const int q = task / m, a = task - q * m;
+                        const int a = task / cnt, q = task - a * cnt; // moved-atom major
                         const uint32_t ent = nbl[q];
                         const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
                         const uint32_t hbn = nbl_b[q];
