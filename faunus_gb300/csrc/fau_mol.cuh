@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     __shared__ int red_f[NW];
     __shared__ uint32_t nbl[CH];   // neighbour group | interacting states
     __shared__ uint32_t nbl_b[CH]; // its first particle | atom count << 24
-    __shared__ int nbl_cnt[2];
+    __shared__ int nbl_cnt[3];
     __shared__ int sh_prev_accept, sh_stop;
     __shared__ long long sh_consumed;
 
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     if (tid == 0) {
         sh_prev_accept = 0;
         sh_stop = 0;
-        nbl_cnt[0] = nbl_cnt[1] = 0;
+        nbl_cnt[0] = nbl_cnt[1] = nbl_cnt[2] = 0;
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -254,59 +254,56 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                                                                             : 0);
                 }
                 tick(1);
-                // ---- group2all(group) with GroupCutoff, in chunks of CH candidate groups
+                // ---- group2all(group) with GroupCutoff
                 const int g = ms.index;
                 const uint4 cmo = ms.cmrec_old, cmn = ms.cmrec_new;
                 const double cmo_d[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
                 const int GN = S.n_groups;
                 const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
-                int chunk = 0;
-                for (int base = 0; base < GN; base += CH, chunk++) {
-                    int* cntp = &nbl_cnt[chunk & 1];
-                    for (int r0 = 0; r0 < RC; r0 += SB) {
-                        if (base + r0 * NTC >= GN) break; // uniform: the ballots below stay full-warp
-                        int gfl[SB], gml[SB], gb0[SB], gb1[SB];
-                        uint4 gcr[SB];
+                // GroupCutoff tests of SB candidates per thread starting at `base`; the survivors
+                // are counted in *cntp and listed (up to `cap` of them) with the states they
+                // interact in and their particle extents
+                auto compact = [&](int base, int* cntp, int cap) {
+                    int gfl[SB], gml[SB], gb0[SB], gb1[SB];
+                    uint4 gcr[SB];
 #pragma unroll
-                        for (int r = 0; r < SB; r++) { // all loads first: their latencies overlap
-                            const int h = base + (r0 + r) * NTC + ctid;
-                            gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
-                            gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
-                            gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
-                            gb0[r] = h < GN ? S.g_begin[h] : 0;
-                            gb1[r] = h < GN ? S.g_begin[h + 1] : 0;
+                    for (int r = 0; r < SB; r++) { // all loads first: their latencies overlap
+                        const int h = base + r * NTC + ctid;
+                        gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
+                        gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                        gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
+                        gb0[r] = h < GN ? S.g_begin[h] : 0;
+                        gb1[r] = h < GN ? S.g_begin[h + 1] : 0;
+                    }
+#pragma unroll
+                    for (int r = 0; r < SB; r++) {
+                        const int h = base + r * NTC + ctid;
+                        uint32_t e = 0;
+                        if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
+                            double c2 = S.cut_g2g2;
+                            float c2f = S.cut_g2g2f;
+                            if (S.n_mol > 0) {
+                                const int kk = mol_g * S.n_mol + gml[r];
+                                c2 = S.cut2_mol[kk];
+                                c2f = S.cut2_molf[kk];
+                            }
+                            const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
+                            const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
+                            e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
                         }
-#pragma unroll
-                        for (int r = 0; r < SB; r++) {
-                            const int h = base + (r0 + r) * NTC + ctid;
-                            uint32_t e = 0;
-                            if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
-                                double c2 = S.cut_g2g2;
-                                float c2f = S.cut_g2g2f;
-                                if (S.n_mol > 0) {
-                                    const int kk = mol_g * S.n_mol + gml[r];
-                                    c2 = S.cut2_mol[kk];
-                                    c2f = S.cut2_molf[kk];
-                                }
-                                const bool cut_o = group_cut_rec(S, cmo, cmo_d, gcr[r], h, c2, c2f);
-                                const bool cut_n = group_cut_rec(S, cmn, ms.cm_new, gcr[r], h, c2, c2f);
-                                e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
-                            }
-                            const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
-                            int wpos = 0;
-                            if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
-                            wpos = __shfl_sync(0xffffffffu, wpos, 0);
-                            if (e) {
-                                const int slot = wpos + __popc(bal & ((1u << lane) - 1u));
-                                nbl[slot] = (uint32_t)h | e;
-                                nbl_b[slot] = (uint32_t)gb0[r] | ((uint32_t)(gb1[r] - gb0[r]) << 24);
-                            }
+                        const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
+                        int wpos = 0;
+                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
+                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
+                        const int slot = wpos + __popc(bal & ((1u << lane) - 1u));
+                        if (e && slot < cap) {
+                            nbl[slot] = (uint32_t)h | e;
+                            nbl_b[slot] = (uint32_t)gb0[r] | ((uint32_t)(gb1[r] - gb0[r]) << 24);
                         }
                     }
-                    compute_barrier(NTC);
-                    tick(11);
-                    const int cnt = *cntp;
-                    if (ctid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
+                };
+                // one (neighbour group, moved atom) task per thread over the cnt listed groups
+                auto pair_tasks = [&](int cnt) {
                     for (int task = ctid; task < cnt * m; task += NTC) {
                         const int a = task / cnt, q = task - a * cnt; // moved-atom major
                         const uint32_t ent = nbl[q];
@@ -337,10 +334,36 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                             add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
                         }
                     }
+                };
+                // one pass over every candidate group: a single barrier pair per move while the
+                // survivors fit the list (GroupCutoff keeps ~140 of any number of waters)
+                for (int base = 0; base < GN; base += SB * NTC) compact(base, &nbl_cnt[0], CH);
+                compute_barrier(NTC);
+                tick(11);
+                const int total = nbl_cnt[0];
+                if (total <= CH) {
+                    pair_tasks(total);
                     compute_barrier(NTC);
                     tick(12);
                 }
-                if (ctid == 0) nbl_cnt[0] = nbl_cnt[1] = 0;
+                else { // more survivors than list slots (long or no cutoff): chunks of CH candidates
+                    int chunk = 0;
+                    for (int base = 0; base < GN; base += CH, chunk++) {
+                        int* cntp = &nbl_cnt[1 + (chunk & 1)];
+                        for (int r0 = 0; r0 < RC; r0 += SB) {
+                            if (base + r0 * NTC >= GN) break; // uniform: the ballots stay full-warp
+                            compact(base + r0 * NTC, cntp, CH);
+                        }
+                        compute_barrier(NTC);
+                        tick(11);
+                        const int cnt = *cntp;
+                        if (ctid == 0) nbl_cnt[1 + ((chunk + 1) & 1)] = 0;
+                        pair_tasks(cnt);
+                        compute_barrier(NTC);
+                        tick(12);
+                    }
+                }
+                if (ctid == 0) nbl_cnt[0] = nbl_cnt[1] = nbl_cnt[2] = 0;
                 for (int t = ctid; t < S.n_atomic; t += NTC) { // atomic groups are never cut
                     const int b = S.atomic_idx[t];
                     const uint4 rb = S.rec[b];

@@ -21,6 +21,8 @@ CASES = {
     "water_surface": lambda: configs.spce_water(n_mol=256, L=18.6, seed=5, epss=1.0),
     "water_two_kinds": lambda: configs.spce_water(n_mol=512, L=24.8, seed=6, molecules=("M", "Q"),
                                                   cutoff_g2g={"default": 7.0, "M Q": 10.0}),
+    "water_4000": lambda: configs.spce_water(n_mol=4000, L=49.3, seed=12),            # one pass, G > list size
+    "water_2000_no_cutoff": lambda: configs.spce_water(n_mol=2000, L=39.1, seed=13, cutoff_g2g=0.0),  # chunks
     "water_reaction_field": lambda: dataclasses.replace(
         configs.spce_water(n_mol=256, L=18.6, seed=7), ewald=None,
         **F.coulomb_scheme("reactionfield", epsr=1.0, cutoff=9.0, epsrf=80.0, temperature=300.0)),
