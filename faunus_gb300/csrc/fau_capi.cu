@@ -367,7 +367,7 @@ size_t footprint_bytes(const fau_sys_desc* d, const Layout& lay, int cap)
         const size_t nc = (size_t)lay.cdim[0] * lay.cdim[1] * lay.cdim[2];
         b += nc * 4 + nc * (size_t)cap * 16 + n * 8;
     }
-    b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16);
+    b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16 + 8 + 8);
     b += sizeof(PlainMove) + 64 + sizeof(void*);
     if (d->cutoff_g2g_pairs && d->n_molids > 0) b += g * 4 + (size_t)d->n_molids * d->n_molids * (8 + 4);
     return b;
@@ -723,6 +723,10 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         UP(h.Ak, akf);
         UP(h.Akd, lay.ew.Ak);
         if ((rc = dev_alloc(s, &h.Q, lay.K))) return bail(rc);
+        if ((rc = dev_alloc(s, &h.qpend, lay.K)) || (rc = dev_alloc(s, &h.qdlt, lay.K))) return bail(rc);
+        if (cudaMemsetAsync(h.qpend, 0, sizeof(float2) * lay.K, ctx->stream) != cudaSuccess ||
+            cudaMemsetAsync(h.qdlt, 0, sizeof(float2) * lay.K, ctx->stream) != cudaSuccess)
+            return bail(fail(FAU_ERR_CUDA, "pending Q(k) initialisation failed"));
         const double V = d->box[0] * d->box[1] * d->box[2];
         h.rec_pref = 2 * kPi * d->bjerrum_length / V;
         const double const_inf = d->ewald.epss < 1 ? 0.0 : 1.0;
@@ -804,7 +808,7 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     DevSys& h = s->h;
     fix(h.x); fix(h.y); fix(h.z); fix(h.rec); fix(h.group_of); fix(h.itype_q); fix(h.itype_qd); fix(h.itype_self);
     fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
-    fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf);
+    fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf); fix(h.qpend); fix(h.qdlt);
     fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
     fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
     fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);
@@ -816,6 +820,8 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     DevSys nd = h;
     nd.energy = cur.energy;
     nd.beta_scale = cur.beta_scale;
+    nd.q_valid = cur.q_valid;
+    nd.q_since = cur.q_since;
     for (int k = 0; k < 3; k++) nd.M[k] = cur.M[k];
     nd.cap = cur.cap;
     nd.err = 0;
@@ -867,6 +873,7 @@ static int pull_state(fau_sys* s)
 static int compute_total(fau_sys* s, fau_energy_terms* t)
 {
     cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(launch_fold_q(s->d, s->K, st)); // Q(k) = master + pending changes
     CUDA_TRY(cudaMemsetAsync(s->d_partials, 0, kTotalPartials * sizeof(double), st));
     CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, 4 * sizeof(int), st));
     CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_partials, s->d_flags, st));
@@ -1179,6 +1186,7 @@ static double hb(double a, double L, double half, double inv)
 static int plain_trial(fau_sys* s, int kind, int index, const double dr[3], const double* quat, double u01,
                        fau_trial_result* out)
 {
+    CUDA_TRY(launch_fold_q(s->d, s->K, s->ctx->stream)); // the plain kernels read the FP64 master
     cudaStream_t st = s->ctx->stream;
     PlainMove pm{};
     pm.kind = kind;
@@ -1743,6 +1751,7 @@ int fau_get_q(fau_sys* s, double* q)
     if (!s || !q) return fail(FAU_ERR_ARG, "null argument");
     if (s->K == 0) return FAU_OK;
     CUDA_TRY(cudaSetDevice(s->ctx->device));
+    CUDA_TRY(launch_fold_q(s->d, s->K, s->ctx->stream));
     CUDA_TRY(cudaMemcpyAsync(q, s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     return FAU_OK;
@@ -1758,6 +1767,7 @@ int fau_q_rebuild(fau_sys* s, double* drift)
     CUDA_TRY(cudaSetDevice(s->ctx->device));
     cudaStream_t st = s->ctx->stream;
     std::vector<double2> before(s->K), after(s->K);
+    CUDA_TRY(launch_fold_q(s->d, s->K, st));
     CUDA_TRY(cudaMemcpyAsync(before.data(), s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(launch_q_rebuild(s->d, s->K, s->h.Q, st));
     CUDA_TRY(cudaMemcpyAsync(after.data(), s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, st));

@@ -487,8 +487,8 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     for (int k = tid; k < K; k += NT) {
         const double2 q = S.Q[k];
         Qb[k] = make_float2((float)q.x, (float)q.y);
-        pend[k] = make_float2(0.f, 0.f);
-        dlt[k] = make_float2(0.f, 0.f);
+        pend[k] = S.qpend[k]; // where the previous launch left the pending changes
+        dlt[k] = S.qdlt[k];
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
         kidx[k] = (nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16);
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     const int nt = S.nt;
 
     unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
-    int since_flush = 0;
+    int since_flush = S.q_since;
     double energy = S.energy, sum_du = 0.0;
     double M[3] = {S.M[0], S.M[1], S.M[2]};
 
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         }
     };
     if (tid == 0) {
-        ms.prev_accept = 0;
+        ms.prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         ms.consumed = 0;
         nbl_cnt[0] = nbl_cnt[1] = 0;
     }
@@ -1001,24 +1001,11 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         for (int j = 0; j < kPhaseSlots; j++)
             if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + j], tacc[j]);
 
-    // the last accepted move's Q(k) change, then everything pending into the FP64 master
-    if (ms.prev_accept) {
-        for (int k = tid; k < K; k += NT) {
-            float2 pe = pend[k];
-            const float2 d = dlt[k];
-            pe.x += d.x;
-            pe.y += d.y;
-            pend[k] = pe;
-        }
-    }
+    // the pending changes stay pending: the next launch continues from them exactly as the next
+    // move would (the host folds them into the master before it reads Q)
     for (int k = tid; k < K; k += NT) {
-        const float2 pe = pend[k];
-        if (pe.x != 0.f || pe.y != 0.f) {
-            double2 q = S.Q[k];
-            q.x += (double)pe.x;
-            q.y += (double)pe.y;
-            S.Q[k] = q;
-        }
+        S.qpend[k] = pend[k];
+        S.qdlt[k] = dlt[k];
     }
     __shared__ unsigned long long red_u[NW][2];
     unsigned long long a = n_pairs, b = n_k;
@@ -1048,6 +1035,8 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
         if (ms.stop) G.err = ms.stop;
         G.consumed = ms.stop ? ms.consumed : nmoves;
+        G.q_valid = K ? ms.prev_accept : 0;
+        G.q_since = K ? since_flush : 0;
         G.cycles += (unsigned long long)(clock64() - t_start);
     }
 }

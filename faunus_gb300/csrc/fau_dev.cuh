@@ -104,6 +104,11 @@ struct DevSys {
     float* Ak;
     double* Akd;
     double2* Q;       // FP64 master
+    // accepted Q(k) changes not yet flushed into the master, kept across launches so that a chain
+    // split into several launches evolves exactly as in one (Q = master + qpend [+ qdlt if q_valid])
+    float2* qpend;    // FP32 pending sums
+    float2* qdlt;     // the last accepted move's change, folded into qpend by the next move
+    int q_valid, q_since; // qdlt pending; accepts since the last flush into the master
     double rec_pref;  // 2 pi lB / V
     double surf_pref; // const_inf 2 pi lB / ((2 epss + 1) V)
     double M[3];      // sum q r (surface term)

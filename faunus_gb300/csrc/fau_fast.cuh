@@ -424,7 +424,9 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
     const float rec_pref_f = (float)S.rec_pref;
     for (int k = tid; k < K; k += NT) {
         const double2 q = S.Q[k];
-        kq[k] = make_float4((float)q.x, (float)q.y, 0.f, 0.f);
+        const float2 pe = S.qpend[k]; // where the previous launch left the pending changes
+        kq[k] = make_float4((float)q.x, (float)q.y, pe.x, pe.y);
+        dlt[k] = S.qdlt[k];
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
         kaf[k] = make_int2((nx + nc) | ((TS + ny + nc) << 8) | ((2 * TS + nz + nc) << 16),
@@ -468,7 +470,8 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
     };
 
     unsigned long long n_pairs = 0;
-    int since_flush = 0, q_pending = 0; // compute threads: accepts since the FP64 flush; dQ not yet folded in
+    // compute threads: accepts since the FP64 flush; dQ not yet folded in (carried across launches)
+    int since_flush = S.q_since, q_pending = S.q_valid;
 
     // move 0: its scalar part, then tables and cell entries by every thread
     if (producer && !PHILOX) {
@@ -834,21 +837,17 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
     if (A.phase_cycles && tid < kFastPhaseSlots && tsm[tid])
         atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + tid], tsm[tid]);
 
-    // the last accepted move's change and everything pending into the FP64 master Q
+    // the pending changes stay pending: the next launch continues from them exactly as the next
+    // move would (the host folds them into the master before it reads Q)
     if (!producer) {
         for (int k = ctid; k < K; k += NTC) {
-            float4 qq = kq[k];
-            if (q_pending) {
-                const float2 d = dlt[k];
-                qq.z += d.x;
-                qq.w += d.y;
-            }
-            if (qq.z != 0.f || qq.w != 0.f) {
-                double2 q = S.Q[k];
-                q.x += (double)qq.z;
-                q.y += (double)qq.w;
-                S.Q[k] = q;
-            }
+            const float4 qq = kq[k];
+            S.qpend[k] = make_float2(qq.z, qq.w);
+            S.qdlt[k] = dlt[k];
+        }
+        if (ctid == 0) {
+            G.q_valid = K ? q_pending : 0;
+            G.q_since = K ? since_flush : 0;
         }
     }
     unsigned long long pa = n_pairs;

@@ -98,6 +98,41 @@ __global__ void total_misc_kernel(const DevSys* Sp, double* out)
 // Q_k = sum_j q_j e^{i k.r_j} from the FP64 master positions with k = 2 pi n / L
 // and k.r = (kx x + ky y) + kz z, as PolicyIonIon::updateComplex
 // (src/energy.cpp:191-206).  One CTA per k.
+// the pending FP32 changes (and the last accepted move's, if not yet added) into the FP64
+// master, as a chain's flush does; one block
+__global__ void fold_q_kernel(DevSys* Sp)
+{
+    DevSys& S = *Sp;
+    const bool valid = S.q_valid != 0;
+    for (int k = threadIdx.x; k < S.K; k += blockDim.x) {
+        float2 pe = S.qpend[k];
+        if (valid) {
+            const float2 d = S.qdlt[k];
+            pe.x += d.x;
+            pe.y += d.y;
+        }
+        if (pe.x != 0.f || pe.y != 0.f) {
+            double2 q = S.Q[k];
+            q.x += (double)pe.x;
+            q.y += (double)pe.y;
+            S.Q[k] = q;
+        }
+        S.qpend[k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        S.q_valid = 0;
+        S.q_since = 0;
+    }
+}
+
+cudaError_t launch_fold_q(DevSys* dsys, int K, cudaStream_t st)
+{
+    if (K <= 0) return cudaSuccess;
+    fold_q_kernel<<<1, 256, 0, st>>>(dsys);
+    return cudaGetLastError();
+}
+
 __global__ void q_rebuild_kernel(const DevSys* Sp, double2* out)
 {
     const DevSys& S = *Sp;

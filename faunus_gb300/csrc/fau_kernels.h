@@ -78,6 +78,7 @@ cudaError_t fast_dispatch_8_host(const ChainArgs&, int, int, int, int, cudaStrea
 cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
+cudaError_t launch_fold_q(DevSys* dsys, int K, cudaStream_t st); // pending Q(k) changes into the master
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
                             int* flags, cudaStream_t st);
 cudaError_t launch_plain_commit(DevSys* dsys, const PlainMove* pm, int K, const double2* dq, cudaStream_t st);

@@ -117,8 +117,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     for (int k = tid; k < K; k += NT) {
         const double2 q = S.Q[k];
         Qb[k] = make_float2((float)q.x, (float)q.y);
-        pend[k] = make_float2(0.f, 0.f);
-        dlt[k] = make_float2(0.f, 0.f);
+        pend[k] = S.qpend[k]; // where the previous launch left the pending changes
+        dlt[k] = S.qdlt[k];
         int nx, ny, nz;
         kn_unpack(S.kn[k], nx, ny, nz);
         kidx[k] = (nx + nc) | ((ny + nc) << 8) | ((nz + nc) << 16);
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     const int nt = S.nt;
 
     unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
-    int since_flush = 0;
+    int since_flush = S.q_since; // counted by the compute threads
     double energy = S.energy, sum_du = 0.0;
     double M[3] = {S.M[0], S.M[1], S.M[2]};
     long long consumed = nmoves;
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         }
     };
     if (tid == 0) {
-        sh_prev_accept = 0;
+        sh_prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         sh_stop = 0;
         nbl_cnt[0] = nbl_cnt[1] = nbl_cnt[2] = 0;
     }
@@ -479,26 +479,14 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         for (int j = 0; j < kPhaseSlots; j++)
             if (tacc[j]) atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + j], tacc[j]);
 
-    // the last accepted move's Q(k) change, then everything pending into the FP64 master
-    if (sh_prev_accept && !sh_stop) {
-        for (int k = tid; k < K; k += NT) {
-            float2 pe = pend[k];
-            const float2 d = dlt[k];
-            pe.x += d.x;
-            pe.y += d.y;
-            pend[k] = pe;
-        }
-    }
+    // the pending changes stay pending: the next launch continues from them exactly as the next
+    // move would (the host folds them into the master before it reads Q)
     __syncthreads();
     for (int k = tid; k < K; k += NT) {
-        const float2 pe = pend[k];
-        if (pe.x != 0.f || pe.y != 0.f) {
-            double2 q = S.Q[k];
-            q.x += (double)pe.x;
-            q.y += (double)pe.y;
-            S.Q[k] = q;
-        }
+        S.qpend[k] = pend[k];
+        S.qdlt[k] = dlt[k];
     }
+    if (tid == 32) G.q_since = K ? since_flush : 0;
     __shared__ unsigned long long red_u[NW][2];
     unsigned long long a = n_pairs, b = n_k;
 #pragma unroll
@@ -527,6 +515,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
         if (sh_stop) G.err = sh_stop;
         G.consumed = consumed;
+        G.q_valid = K ? sh_prev_accept : 0;
         G.cycles += (unsigned long long)(clock64() - t_start);
     }
 }
