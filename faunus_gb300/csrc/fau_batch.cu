@@ -48,7 +48,7 @@ __global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const DevSys& S = *sys[i];
-        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, S.energy, S.beta_scale, S.err, 0};
+        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, sys_energy(S), S.beta_scale, S.err, 0};
     }
 }
 
@@ -67,8 +67,8 @@ __global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const d
     const int parity = r0.x & 1;
     for (int s = parity; s + 1 < n; s += 2) {
         const int a = slot_sys[s], b = slot_sys[s + 1];
-        const double Ea = sys[a]->energy * Tref[a];
-        const double Eb = sys[b]->energy * Tref[b];
+        const double Ea = sys_energy(*sys[a]) * Tref[a];
+        const double Eb = sys_energy(*sys[b]) * Tref[b];
         const double x = (1.0 / T[s] - 1.0 / T[s + 1]) * (Ea - Eb);
         const U4 r = philox({(uint32_t)round, (uint32_t)(round >> 32), (uint32_t)s, 8u}, k0, k1);
         const double u = u01_53(r.x, r.y);

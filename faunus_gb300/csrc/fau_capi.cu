@@ -819,6 +819,8 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
         return bail(fail(FAU_ERR_CUDA, "clone state read failed"));
     DevSys nd = h;
     nd.energy = cur.energy;
+    nd.e_acc_hi = cur.e_acc_hi;
+    nd.e_acc_lo = cur.e_acc_lo;
     nd.beta_scale = cur.beta_scale;
     nd.q_valid = cur.q_valid;
     nd.q_since = cur.q_since;
@@ -859,7 +861,7 @@ static int pull_state(fau_sys* s)
     DevSys tmp;
     CUDA_TRY(cudaMemcpyAsync(&tmp, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, s->ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
-    s->h.energy = tmp.energy;
+    s->h.energy = sys_energy(tmp);
     for (int k = 0; k < 3; k++) s->h.M[k] = tmp.M[k];
     s->h.err = tmp.err;
     s->h.moves = tmp.moves;
@@ -921,7 +923,9 @@ static int refresh_energy(fau_sys* s)
     int rc = compute_total(s, &t);
     if (rc) return rc;
     s->h.energy = t.total;
+    const float zero2[2] = {0.f, 0.f};
     CUDA_TRY(cudaMemcpyAsync(&s->d->energy, &t.total, sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(&s->d->e_acc_hi, zero2, sizeof(zero2), cudaMemcpyHostToDevice, s->ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     return FAU_OK;
 }

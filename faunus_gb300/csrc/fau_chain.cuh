@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
 
     unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
     int since_flush = S.q_since;
-    double energy = S.energy, sum_du = 0.0;
+    double energy = sys_energy(S), sum_du = 0.0; // the pipelined kernel's unfolded part folded in
     double M[3] = {S.M[0], S.M[1], S.M[2]};
 
     // phase timers (profiling only; every phase still runs): slots
@@ -1031,6 +1031,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
         G.accepted += n_acc;
         G.sum_du += sum_du;
         G.energy = energy;
+        G.e_acc_hi = G.e_acc_lo = 0.f;
 #pragma unroll
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
         if (ms.stop) G.err = ms.stop;

@@ -114,10 +114,11 @@ struct DevSys {
     double M[3];      // sum q r (surface term)
 
     // running state
-    double energy;     // running total energy (kT), FP64
+    double energy;     // running total energy (kT), FP64 (see sys_energy)
     double beta_scale; // multiplies dU in the Metropolis test (PT temperature ladder)
     int err;           // fau_status raised on the device
     int pad4;
+    float e_acc_hi, e_acc_lo; // the pipelined kernel's float-float sum of accepted changes not yet in `energy`
     unsigned long long moves, accepted, pair_evals, k_updates;
     double sum_du;
     long long consumed; // proposals performed by the last chain launch
@@ -266,6 +267,13 @@ __device__ __forceinline__ double sqdist_d(const DevSys& S, const double* a, con
 __device__ __forceinline__ double group_cut2(const DevSys& S, int g1, int g2)
 {
     return S.n_mol > 0 ? S.cut2_mol[S.g_molid[g1] * S.n_mol + S.g_molid[g2]] : S.cut_g2g2;
+}
+
+// the running total energy: the FP64 sum plus the pipelined kernel's unfolded float-float part,
+// which stays unfolded across launches (a chain split into launches sums as in one)
+__host__ __device__ inline double sys_energy(const DevSys& S)
+{
+    return S.energy + ((double)S.e_acc_hi + (double)S.e_acc_lo);
 }
 
 // squared minimum-image distance of two fixed-point records, FP32

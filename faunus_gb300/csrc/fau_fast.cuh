@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
         ps.dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
         ps.energy = S.energy;
         ps.sum_du = 0.0;
-        ps.e_acc = FF{0.f, 0.f};
+        ps.e_acc = FF{S.e_acc_hi, S.e_acc_lo}; // carried over from the previous launch
         ps.n_acc = ps.n_mv = 0;
 #pragma unroll
         for (int d = 0; d < 3; d++) ps.M[d] = S.M[d];
@@ -860,11 +860,14 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
         for (int w = 0; w < NWC; w++) sp += red_u[w][0];
         G.pair_evals += sp;
         G.k_updates += ps.n_mv * (unsigned long long)K; // every k-vector once per single-atom move
-        const double acc = ff_value(ps.e_acc);
+        // the float-float part stays unfolded for the next launch; sum_du counts it once
+        const double acc = ff_value(ps.e_acc), acc0 = (double)S.e_acc_hi + (double)S.e_acc_lo;
         G.moves += ps.n_mv;
         G.accepted += ps.n_acc;
-        G.sum_du += ps.sum_du + acc;
-        G.energy = ps.energy + acc;
+        G.sum_du += ps.sum_du + (acc - acc0);
+        G.energy = ps.energy;
+        G.e_acc_hi = ps.e_acc.hi;
+        G.e_acc_lo = ps.e_acc.lo;
 #pragma unroll
         for (int d = 0; d < 3; d++) G.M[d] = ps.M[d];
         if (stop) G.err = stop;

@@ -123,7 +123,7 @@ __global__ void slot_sum_kernel(DevSys* const* sys, int n, const int* slots, int
             cr++;
         }
         if (energy) {
-            const double e = S.energy;
+            const double e = sys_energy(S);
             e1 += e;
             e2 += e * e;
             ce++;

@@ -1,11 +1,11 @@
 """The continuous-batching server on the device: a job's result is the same
 alone and in a mix of jobs that join and leave around it -- the same moves
-(device RNG keyed by job id and move counter), bit-identical positions and
-acceptance counts, and the running energy within 1e-9 relative (the server
-sizes each job's share of a round from measured cycles, so launch boundaries
-differ between runs, and each launch folds the FP32 pending Q(k) sums into the
-FP64 master at its end); p50/p99 latency and throughput are reported; an
-over-size job is rejected without disturbing the others."""
+(device RNG keyed by job id and move counter), bit-identical positions,
+acceptance counts and running energy, although the server sizes each job's share
+of a round from measured cycles so launch boundaries differ between the runs
+(pending Q(k) changes and partial energy sums stay on the device across launches);
+p50/p99 latency and throughput are reported; an over-size job is rejected without
+disturbing the others."""
 import numpy as np
 import pytest
 
@@ -39,7 +39,7 @@ def test_served_job_same_alone_and_in_mix(ctx, kind):
     assert a.status == b.status == "done" and a.moves == b.moves == 6000
     assert np.array_equal(a.positions, b.positions)
     assert a.accepted == b.accepted
-    assert abs(a.energy - b.energy) <= 1e-9 * max(1.0, abs(a.energy))
+    assert a.energy == b.energy
 
 
 def test_served_stream_reports_latency_and_rejects_oversize(ctx):
