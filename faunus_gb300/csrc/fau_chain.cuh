@@ -90,6 +90,28 @@ __device__ __forceinline__ bool group_cut_rec(const DevSys& S, uint4 cmrec, cons
 }
 
 // quaternion rotation v' = v + w t + u x t, t = 2 u x v (FP64, never contracted)
+// The neighbour-group list of a molecular move: warp v lists its GroupCutoff survivors in its
+// own segment [v * seg, v * seg + wc[v]) in (row, lane) order. The list order, and with it the
+// order of every pair sum, is then independent of the order in which warps arrive, so dU is
+// reproducible bit for bit. Slot of the q-th listed group:
+template <int NWL>
+__device__ __forceinline__ int nbl_slot(int q, const int (&wc)[NWL], int seg)
+{
+    int off = 0;
+    bool found = false;
+#pragma unroll
+    for (int v = 0; v < NWL; v++) {
+        if (!found && q >= wc[v]) {
+            q -= wc[v];
+            off += seg;
+        }
+        else {
+            found = true;
+        }
+    }
+    return off + q;
+}
+
 __device__ __forceinline__ void quat_rotate(const double* q, double* v)
 {
     const double ux = q[1], uy = q[2], uz = q[3], w = q[0];
@@ -449,8 +471,9 @@ __device__ __forceinline__ void warp_reduce(FF& a, FF& b, float& sc, int& flags,
     flags = __reduce_or_sync(0xffffffffu, flags);
 }
 
+// at most 128 registers a thread: two 256-thread (four 128-thread) systems per SM
 template <int NT, bool PHILOX>
-__global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
+__global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs A)
 {
     constexpr int NW = NT / 32;
     const long long t_start = clock64();
@@ -481,7 +504,7 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     __shared__ int red_f[NW];
     __shared__ int nbo[27][3];
     __shared__ uint32_t nbl[kNblChunk]; // molecular moves: neighbour groups of one chunk | interacting states
-    __shared__ int nbl_cnt[2];
+    __shared__ int nbl_wcnt[NW];        // survivors each warp listed in its segment
 
     const float rec_pref_f = (float)S.rec_pref;
     for (int k = tid; k < K; k += NT) {
@@ -539,7 +562,6 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
     if (tid == 0) {
         ms.prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         ms.consumed = 0;
-        nbl_cnt[0] = nbl_cnt[1] = 0;
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -721,10 +743,10 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                 // useful pair work instead of a few lanes running whole groups serially.
                 const int G = S.n_groups;
                 const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
-                int chunk = 0;
-                for (int base = 0; base < G; base += kNblChunk, chunk++) {
-                    int* cntp = &nbl_cnt[chunk & 1];
+                for (int base = 0; base < G; base += kNblChunk) {
                     constexpr int RC = kNblChunk / NT;
+                    constexpr int SEG = RC * 32; // each warp tests RC * 32 candidates per chunk
+                    int wc = 0;
                     int gfl[RC], gml[RC];
                     uint4 gcr[RC];
 #pragma unroll
@@ -751,17 +773,20 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                             e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
                         }
                         const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
-                        int wpos = 0;
-                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
-                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
-                        if (e) nbl[wpos + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)h | e;
+                        if (e) nbl[warp * SEG + wc + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)h | e;
+                        wc += __popc(bal);
                     }
+                    if (lane == 0) nbl_wcnt[warp] = wc;
                     __syncthreads();
-                    const int cnt = *cntp;
-                    if (tid == 0) nbl_cnt[(chunk + 1) & 1] = 0;
+                    int wcl[NW], cnt = 0;
+#pragma unroll
+                    for (int v = 0; v < NW; v++) {
+                        wcl[v] = nbl_wcnt[v];
+                        cnt += wcl[v];
+                    }
                     for (int task = tid; task < cnt * m; task += NT) {
                         const int q = task / m, a = task - q * m;
-                        const uint32_t ent = nbl[q];
+                        const uint32_t ent = nbl[nbl_slot(q, wcl, SEG)];
                         const int h = (int)(ent & kNblGroup);
                         const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
                         const int hb = S.g_begin[h], he = S.g_begin[h + 1];
@@ -786,7 +811,6 @@ __global__ void __launch_bounds__(NT) chain_kernel(ChainArgs A)
                     }
                     __syncthreads();
                 }
-                if (tid == 0) nbl_cnt[0] = nbl_cnt[1] = 0;
                 for (int t = tid; t < S.n_atomic; t += NT) { // atomic groups are never cut
                     const int b = S.atomic_idx[t];
                     const uint4 rb = S.rec[b];

@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     constexpr int NTC = NT - 32;  // compute threads
     constexpr int RC = 6;         // candidate groups per compute thread per chunk (1344: one chunk
     constexpr int CH = RC * NTC;  // covers a 1,000-molecule system, one barrier pair per move)
-    constexpr int SB = 2;         // candidates whose loads are in flight together
+    constexpr int SB = 2;         // candidates whose loads are in flight together (RC % SB == 0)
+    constexpr int SEG = RC * 32;  // list slots of one compute warp (its candidates in one chunk)
     const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ctid = tid - 32; // compute-thread index (warps 1..)
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     __shared__ int red_f[NW];
     __shared__ uint32_t nbl[CH];   // neighbour group | interacting states
     __shared__ uint32_t nbl_b[CH]; // its first particle | atom count << 24
-    __shared__ int nbl_cnt[3];
+    __shared__ int nbl_wcnt[2][NWC]; // survivors per compute warp: single pass | current chunk
     __shared__ int sh_prev_accept, sh_stop;
     __shared__ long long sh_consumed;
 
@@ -155,7 +156,6 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     if (tid == 0) {
         sh_prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         sh_stop = 0;
-        nbl_cnt[0] = nbl_cnt[1] = nbl_cnt[2] = 0;
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -261,9 +261,9 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 const int GN = S.n_groups;
                 const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
                 // GroupCutoff tests of SB candidates per thread starting at `base`; the survivors
-                // are counted in *cntp and listed (up to `cap` of them) with the states they
-                // interact in and their particle extents
-                auto compact = [&](int base, int* cntp, int cap) {
+                // are counted in the warp's wc and listed in the warp's own segment (nbl_slot),
+                // up to SEG of them, with the states they interact in and their particle extents
+                auto compact = [&](int base, int& wc) {
                     int gfl[SB], gml[SB], gb0[SB], gb1[SB];
                     uint4 gcr[SB];
 #pragma unroll
@@ -292,23 +292,34 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                             e = (cut_n ? 0u : kNblNew) | (cut_o ? 0u : kNblOld);
                         }
                         const unsigned bal = __ballot_sync(0xffffffffu, e != 0);
-                        int wpos = 0;
-                        if (lane == 0 && bal) wpos = atomicAdd(cntp, __popc(bal));
-                        wpos = __shfl_sync(0xffffffffu, wpos, 0);
-                        const int slot = wpos + __popc(bal & ((1u << lane) - 1u));
-                        if (e && slot < cap) {
-                            nbl[slot] = (uint32_t)h | e;
-                            nbl_b[slot] = (uint32_t)gb0[r] | ((uint32_t)(gb1[r] - gb0[r]) << 24);
+                        const int slot = wc + __popc(bal & ((1u << lane) - 1u));
+                        if (e && slot < SEG) {
+                            nbl[(warp - 1) * SEG + slot] = (uint32_t)h | e;
+                            nbl_b[(warp - 1) * SEG + slot] = (uint32_t)gb0[r] | ((uint32_t)(gb1[r] - gb0[r]) << 24);
                         }
+                        wc += __popc(bal);
                     }
                 };
+                // the compute warps' survivor counts (after a barrier); over: a segment overflowed
+                auto read_counts = [&](const int* src, int (&wcl)[NWC], bool& over) {
+                    int cnt = 0;
+                    over = false;
+#pragma unroll
+                    for (int v = 0; v < NWC; v++) {
+                        wcl[v] = src[v];
+                        cnt += wcl[v];
+                        over |= wcl[v] > SEG;
+                    }
+                    return cnt;
+                };
                 // one (neighbour group, moved atom) task per thread over the cnt listed groups
-                auto pair_tasks = [&](int cnt) {
+                auto pair_tasks = [&](const int (&wcl)[NWC], int cnt) {
                     for (int task = ctid; task < cnt * m; task += NTC) {
                         const int a = task / cnt, q = task - a * cnt; // moved-atom major
-                        const uint32_t ent = nbl[q];
+                        const int sl = nbl_slot(q, wcl, SEG);
+                        const uint32_t ent = nbl[sl];
                         const bool do_n = (ent & kNblNew) != 0, do_o = (ent & kNblOld) != 0;
-                        const uint32_t hbn = nbl_b[q];
+                        const uint32_t hbn = nbl_b[sl];
                         const int hb = (int)(hbn & 0xFFFFFFu), nb = (int)(hbn >> 24), he = hb + nb;
                         const uint4 ra_n = ms.rec_new[a], ra_o = ms.rec_old[a];
                         const int ta = ra_n.w >> 24;
@@ -335,35 +346,41 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                         }
                     }
                 };
-                // one pass over every candidate group: a single barrier pair per move while the
-                // survivors fit the list (GroupCutoff keeps ~140 of any number of waters)
-                for (int base = 0; base < GN; base += SB * NTC) compact(base, &nbl_cnt[0], CH);
+                // one pass over every candidate group: a single barrier pair per move while each
+                // warp's survivors fit its segment (GroupCutoff keeps ~140 of any number of waters)
+                int wl[NWC];
+                bool over;
+                {
+                    int wc = 0;
+                    for (int base = 0; base < GN; base += SB * NTC) compact(base, wc);
+                    if (lane == 0) nbl_wcnt[0][warp - 1] = wc;
+                }
                 compute_barrier(NTC);
                 tick(11);
-                const int total = nbl_cnt[0];
-                if (total <= CH) {
-                    pair_tasks(total);
+                const int total = read_counts(nbl_wcnt[0], wl, over);
+                if (!over) {
+                    pair_tasks(wl, total);
                     compute_barrier(NTC);
                     tick(12);
                 }
-                else { // more survivors than list slots (long or no cutoff): chunks of CH candidates
-                    int chunk = 0;
-                    for (int base = 0; base < GN; base += CH, chunk++) {
-                        int* cntp = &nbl_cnt[1 + (chunk & 1)];
+                else { // more survivors than a segment holds (long or no cutoff): chunks of CH
+                       // candidates, SEG of them per warp (the single-pass counts stay untouched:
+                       // every warp has read them to take this branch)
+                    for (int base = 0; base < GN; base += CH) {
+                        int wc = 0;
                         for (int r0 = 0; r0 < RC; r0 += SB) {
                             if (base + r0 * NTC >= GN) break; // uniform: the ballots stay full-warp
-                            compact(base + r0 * NTC, cntp, CH);
+                            compact(base + r0 * NTC, wc);
                         }
+                        if (lane == 0) nbl_wcnt[1][warp - 1] = wc;
                         compute_barrier(NTC);
                         tick(11);
-                        const int cnt = *cntp;
-                        if (ctid == 0) nbl_cnt[1 + ((chunk + 1) & 1)] = 0;
-                        pair_tasks(cnt);
+                        const int cnt = read_counts(nbl_wcnt[1], wl, over);
+                        pair_tasks(wl, cnt);
                         compute_barrier(NTC);
                         tick(12);
                     }
                 }
-                if (ctid == 0) nbl_cnt[0] = nbl_cnt[1] = nbl_cnt[2] = 0;
                 for (int t = ctid; t < S.n_atomic; t += NTC) { // atomic groups are never cut
                     const int b = S.atomic_idx[t];
                     const uint4 rb = S.rec[b];
