@@ -6,7 +6,9 @@ C ABI of ``include/fau_gpu.h``); this package is its Python host API.
 from . import _capi
 from ._capi import FauError
 from .system import (Context, MoveGenerator, Sampler, System, SystemSpec, bjerrum_length, footprint,
-                     group_cutoff, coulomb_scheme, kjmol_to_kt, move_descs, pressure_kt)
+                     group_cutoff, coulomb_scheme, kjmol_to_kt, move_descs, pressure_kt, splined, andrea_spline,
+                     andrea_eval)
 
 __all__ = ["Context", "Sampler", "System", "SystemSpec", "MoveGenerator", "FauError", "bjerrum_length",
-           "kjmol_to_kt", "footprint", "group_cutoff", "coulomb_scheme", "move_descs", "pressure_kt", "_capi"]
+           "kjmol_to_kt", "footprint", "group_cutoff", "coulomb_scheme", "move_descs", "pressure_kt",
+           "splined", "andrea_spline", "andrea_eval", "_capi"]

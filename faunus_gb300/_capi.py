@@ -25,7 +25,7 @@ FAU_ERR_STATE = 7
 FAU_ERR_NODEVICE = 8
 
 # pair terms / coulomb types / flags / precision / moves
-FAU_PAIR_COULOMB, FAU_PAIR_LJ, FAU_PAIR_WCA, FAU_PAIR_HS = 1, 2, 4, 8
+FAU_PAIR_COULOMB, FAU_PAIR_LJ, FAU_PAIR_WCA, FAU_PAIR_HS, FAU_PAIR_SPLINE = 1, 2, 4, 8, 16
 FAU_COUL_PLAIN, FAU_COUL_CUT, FAU_COUL_EWALD, FAU_COUL_TRUNC = 0, 1, 2, 3
 FAU_COUL_MAX_POLY = 16
 FAU_VOLUME_ISOTROPIC, FAU_VOLUME_XY, FAU_VOLUME_Z, FAU_VOLUME_ISOCHORIC = 0, 1, 2, 3
@@ -56,7 +56,16 @@ class SysDesc(C.Structure):
         ("n_molids", C.c_int), ("cutoff_g2g_pairs", dptr),
         ("coulomb_poly_n", C.c_int), ("coulomb_erfc", C.c_double), ("coulomb_poly", C.c_double * 16),
         ("isobaric", C.c_int), ("pressure", C.c_double),
+        ("spline_begin", iptr), ("spline_r2", dptr), ("spline_coef", dptr), ("spline_hs", iptr),
     ]
+
+
+class SplineOpts(C.Structure):
+    _fields_ = [("utol", C.c_double), ("ftol", C.c_double), ("u_at_rmin", C.c_double), ("u_at_rmax", C.c_double),
+                ("rmax_start", C.c_double), ("hardsphere", C.c_int), ("pad", C.c_int)]
+
+
+SCALAR_FN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
 
 
 class EnergyTerms(C.Structure):
@@ -200,6 +209,10 @@ def _declare(lib: C.CDLL) -> None:
         "fau_movegen_create": ([C.POINTER(SysDesc), C.POINTER(MoveDesc), C.c_int, C.c_uint32, C.c_uint32, C.c_int,
                                 C.POINTER(P)], C.c_int),
         "fau_movegen_destroy": ([P], C.c_int),
+        "fau_andrea_generate": ([SCALAR_FN, P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, dptr, dptr,
+                                 iptr], C.c_int),
+        "fau_spline_tabulate": ([C.POINTER(SysDesc), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                 C.POINTER(SplineOpts), C.c_int, dptr, dptr, iptr, iptr], C.c_int),
         "fau_movegen_generate": ([P, P, C.c_int], C.c_int),
         "fau_movegen_get_state": ([P, C.c_char_p, C.c_size_t], C.c_int),
         "fau_movegen_set_state": ([P, C.c_char_p], C.c_int),

@@ -103,8 +103,8 @@ struct fau_sys {
 // they live on the device).  Shared by clones.
 struct DescStore {
     fau_sys_desc d{};
-    std::vector<double> charge, type_mass, sigma2, eps4, hs2, cut_pairs;
-    std::vector<int> type, group_begin, group_molid, group_flags;
+    std::vector<double> charge, type_mass, sigma2, eps4, hs2, cut_pairs, spl_r2, spl_coef;
+    std::vector<int> type, group_begin, group_molid, group_flags, spl_begin, spl_hs;
 };
 
 static std::shared_ptr<const DescStore> store_desc(const fau_sys_desc* d)
@@ -129,6 +129,18 @@ static std::shared_ptr<const DescStore> store_desc(const fau_sys_desc* d)
     st->d.hs_sigma2 = cp(st->hs2, d->hs_sigma2, nt * nt);
     const size_t nm = d->cutoff_g2g_pairs && d->n_molids > 0 ? (size_t)d->n_molids * d->n_molids : 0;
     st->d.cutoff_g2g_pairs = nm ? cp(st->cut_pairs, d->cutoff_g2g_pairs, nm) : nullptr;
+    if (d->pair_terms & FAU_PAIR_SPLINE) { // validated: nt^2 + 1 offsets, >= 2 knots a pair
+        const size_t np = nt * nt, knots = (size_t)d->spline_begin[np];
+        st->d.spline_begin = cp(st->spl_begin, d->spline_begin, np + 1);
+        st->d.spline_r2 = cp(st->spl_r2, d->spline_r2, knots);
+        st->d.spline_coef = cp(st->spl_coef, d->spline_coef, 6 * (knots - np));
+        st->d.spline_hs = cp(st->spl_hs, d->spline_hs, np);
+    }
+    else {
+        st->d.spline_begin = nullptr;
+        st->d.spline_r2 = st->d.spline_coef = nullptr;
+        st->d.spline_hs = nullptr;
+    }
     return st;
 }
 
@@ -272,6 +284,27 @@ int validate(const fau_sys_desc* d)
     if (d->precision != FAU_PREC_FP32C && d->precision != FAU_PREC_FP64)
         return fail(FAU_ERR_ARG, "unknown precision %d", d->precision);
     if (d->isobaric && !std::isfinite(d->pressure)) return fail(FAU_ERR_ARG, "non-finite Isobaric pressure");
+    if (d->pair_terms & ~(FAU_PAIR_COULOMB | FAU_PAIR_LJ | FAU_PAIR_WCA | FAU_PAIR_HS | FAU_PAIR_SPLINE))
+        return fail(FAU_ERR_ARG, "unknown pair_terms bits 0x%x", d->pair_terms);
+    if (d->pair_terms & FAU_PAIR_SPLINE) {
+        if (!d->spline_begin || !d->spline_r2 || !d->spline_coef)
+            return fail(FAU_ERR_ARG, "FAU_PAIR_SPLINE needs spline_begin, spline_r2 and spline_coef");
+        const long np = (long)d->n_types * d->n_types;
+        if (d->spline_begin[0] != 0) return fail(FAU_ERR_ARG, "spline_begin must start at 0");
+        for (long ab = 0; ab < np; ab++) {
+            const long b0 = d->spline_begin[ab], b1 = d->spline_begin[ab + 1];
+            if (b1 - b0 < 2 || b1 - b0 > (1 << 20))
+                return fail(FAU_ERR_ARG, "type pair %ld: %ld spline knots (2 .. 2^20)", ab, b1 - b0);
+            for (long k = b0; k < b1; k++) {
+                const double z = d->spline_r2[k];
+                if (!std::isfinite(z) || z < 0.0 || (k > b0 && !(z > d->spline_r2[k - 1])))
+                    return fail(FAU_ERR_ARG, "type pair %ld: spline knots must be finite, >= 0 and ascending", ab);
+            }
+            for (long k = 6 * (b0 - ab); k < 6 * (b1 - ab - 1); k++)
+                if (!std::isfinite(d->spline_coef[k]))
+                    return fail(FAU_ERR_ARG, "type pair %ld: non-finite spline coefficient", ab);
+        }
+    }
     return FAU_OK;
 }
 
@@ -370,6 +403,13 @@ size_t footprint_bytes(const fau_sys_desc* d, const Layout& lay, int cap)
     b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16 + 8 + 8);
     b += sizeof(PlainMove) + 64 + sizeof(void*);
     if (d->cutoff_g2g_pairs && d->n_molids > 0) b += g * 4 + (size_t)d->n_molids * d->n_molids * (8 + 4);
+    if (d->pair_terms & FAU_PAIR_SPLINE) { // every class pair a copy of its atom-type pair's table
+        size_t most = 0;
+        const size_t T = d->n_types;
+        for (size_t ab = 0; ab < T * T; ab++)
+            most = std::max(most, (size_t)(d->spline_begin[ab + 1] - d->spline_begin[ab]));
+        b += nt * nt * (sizeof(SplineP) + most * (4 + 8 + 6 * (4 + 8)) + kSplineGrid * 4);
+    }
     return b;
 }
 
@@ -677,6 +717,60 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     if (!molecular_only && (int)atomic_idx.size() == n) h.n_atomic = 0; // all atomic: index = particle
     UP(h.pair, pf);
     UP(h.pair_d, pd);
+    if (d->pair_terms & FAU_PAIR_SPLINE) { // nonbonded_splined: the atom-type pair tables per class pair
+        std::vector<SplineP> spl(nt * nt);
+        std::vector<float> zf, cf;
+        std::vector<double> zd, cd;
+        std::vector<int> grid;
+        std::vector<int> at(T * T, -1); // atom-type pair -> its first class pair (tables shared)
+        for (int a = 0; a < nt; a++)
+            for (int b = 0; b < nt; b++) {
+                const int ab = lay.itype_type[a] * T + lay.itype_type[b];
+                if (at[ab] >= 0) {
+                    spl[a * nt + b] = spl[at[ab]];
+                    continue;
+                }
+                at[ab] = a * nt + b;
+                const int b0 = d->spline_begin[ab], m = d->spline_begin[ab + 1] - b0;
+                const double* z = d->spline_r2 + b0;
+                const double* c = d->spline_coef + 6 * (size_t)(b0 - ab);
+                SplineP q{};
+                q.zmin_d = z[0];
+                q.zmax_d = z[m - 1];
+                q.zmin = (float)z[0];
+                q.zmax = (float)z[m - 1];
+                q.knot0 = (int)zf.size();
+                q.coef0 = (int)cf.size();
+                q.pieces = m - 1;
+                q.grid0 = (int)grid.size();
+                q.grid_n = kSplineGrid;
+                q.inv_h = (float)(kSplineGrid / (z[m - 1] - z[0]));
+                q.hs = d->spline_hs ? (d->spline_hs[ab] != 0) : 0;
+                for (int k = 0; k < m; k++) {
+                    zf.push_back((float)z[k]);
+                    zd.push_back(z[k]);
+                }
+                for (int k = 0; k < 6 * (m - 1); k++) {
+                    cf.push_back((float)c[k]);
+                    cd.push_back(c[k]);
+                }
+                // each cell's start: the last piece whose lower knot is at or below it
+                const double hz = (z[m - 1] - z[0]) / kSplineGrid;
+                int i = 0;
+                for (int g = 0; g < kSplineGrid; g++) {
+                    const double zg = z[0] + g * hz;
+                    while (i < m - 2 && z[i + 1] <= zg) i++;
+                    grid.push_back(i);
+                }
+                spl[a * nt + b] = q;
+            }
+        UP(h.spl, spl);
+        UP(h.spl_zf, zf);
+        UP(h.spl_zd, zd);
+        UP(h.spl_cf, cf);
+        UP(h.spl_cd, cd);
+        UP(h.spl_grid, grid);
+    }
 
     // cell list
     if (lay.cells) {
@@ -809,6 +903,7 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     fix(h.x); fix(h.y); fix(h.z); fix(h.rec); fix(h.group_of); fix(h.itype_q); fix(h.itype_qd); fix(h.itype_self);
     fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
     fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf); fix(h.qpend); fix(h.qdlt);
+    fix(h.spl); fix(h.spl_zf); fix(h.spl_zd); fix(h.spl_cf); fix(h.spl_cd); fix(h.spl_grid);
     fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
     fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
     fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);

@@ -40,6 +40,20 @@ struct PairF {
     float s2, e4, hs2, qq; // sigma^2, 4 eps, hard-sphere sigma^2, lB qa qb
 };
 
+// FAU_PAIR_SPLINE table of one (itype a, itype b) class pair (the atom types' KnotData)
+struct SplineP {
+    double zmin_d, zmax_d; // first and last knot (r^2), FP64
+    float zmin, zmax;      // the same, FP32 (round to nearest)
+    float inv_h;           // index-grid cells per unit r^2 over [zmin, zmax]
+    int knot0;             // first knot in spl_zf / spl_zd
+    int coef0;             // first coefficient in spl_cf / spl_cd (6 a piece)
+    int pieces;            // knots - 1
+    int grid0, grid_n;     // index grid in spl_grid: the piece holding each cell's start
+    int hs;                // +inf at r^2 <= zmin (hardsphere_repulsion)
+    int pad;
+};
+constexpr int kSplineGrid = 256; // index-grid cells a pair (at most)
+
 struct DevSys {
     // geometry (cuboid)
     double L[3], half[3], inv[3];
@@ -87,6 +101,13 @@ struct DevSys {
     float* cut2_molf; // FP32 copies
     PairF* pair;      // nt*nt
     double* pair_d;   // nt*nt*4 FP64 copies (s2, e4, hs2, qq)
+    // FAU_PAIR_SPLINE: tables per class pair (nt*nt SplineP), knots and coefficients
+    SplineP* spl;
+    float* spl_zf;
+    double* spl_zd;
+    float* spl_cf;
+    double* spl_cd;
+    int* spl_grid;
 
     // cell list
     int cdim[3], ncell;
@@ -469,6 +490,52 @@ __device__ __forceinline__ float pair_u32_far(const DevSys& S, const PairF& p, f
     return pair_core(S, p, r2, in_pair, in_coul, overlap, inf, nan, mag);
 }
 
+// FAU_PAIR_SPLINE, FP32: the piece z_i < r2 <= z_{i+1} (Andrea::eval's lower_bound,
+// src/tabulate.h:188-207) from the index grid and a short scan either way, then Horner in
+// dz = r2 - z_i. `mag` gets sum_k |c_k| |dz|^k, the error scale of the evaluation.
+__device__ __forceinline__ float spline_u32(const DevSys& S, const SplineP& q, float r2, float& mag)
+{
+    int g = (int)((r2 - q.zmin) * q.inv_h);
+    g = min(max(g, 0), q.grid_n - 1);
+    int i = S.spl_grid[q.grid0 + g];
+    const float* z = S.spl_zf + q.knot0;
+    while (i > 0 && !(r2 > z[i])) i--;
+    while (i < q.pieces - 1 && r2 > z[i + 1]) i++;
+    const float* c = S.spl_cf + q.coef0 + 6 * i;
+    const float dz = r2 - z[i], adz = fabsf(dz);
+    float s = 0.f, a = 0.f;
+#pragma unroll
+    for (int k = 5; k > 0; k--) {
+        s = dz * (s + c[k]);
+        a = adz * (a + fabsf(c[k]));
+    }
+    mag += a + fabsf(c[0]);
+    return s + c[0];
+}
+
+// FAU_PAIR_SPLINE, FP64 (totals and the plain form): lower_bound over the FP64 knots
+__device__ __forceinline__ double spline_u64(const DevSys& S, const SplineP& q, double r2)
+{
+    const double* z = S.spl_zd + q.knot0;
+    int first = 0, count = q.pieces + 1;
+    while (count > 0) {
+        const int step = count / 2;
+        if (z[first + step] < r2) {
+            first += step + 1;
+            count -= step + 1;
+        }
+        else {
+            count = step;
+        }
+    }
+    const int i = min(max(first - 1, 0), q.pieces - 1);
+    const double* c = S.spl_cd + q.coef0 + 6 * i;
+    const double dz = r2 - z[i];
+    double s = 0.0;
+    for (int k = 5; k > 0; k--) s = dz * (s + c[k]);
+    return s + c[0];
+}
+
 // Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
 // overflow set `inf` instead of adding +inf, so the compensated sums stay finite.
 // The terms are discontinuous at the pair cutoff, the Coulomb cutoff and the
@@ -486,12 +553,32 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
     bool in_pair = !(S.rc2_pair > 0.f && r2 >= S.rc2_pair);
     bool in_coul = r2 < S.rc2_coul;
     bool overlap = (terms & FAU_PAIR_HS) && r2 < p.hs2;
-    if (pair_near(S, p, r2)) {
+    auto r2_fp64 = [&]() {
         const double xr[3] = {xj ? xj[0] : S.x[j], xj ? xj[1] : S.y[j], xj ? xj[2] : S.z[j]};
-        const double r2d = sqdist_d(S, xi, xr);
+        return sqdist_d(S, xi, xr);
+    };
+    if (pair_near(S, p, r2)) {
+        const double r2d = r2_fp64();
         in_pair = !(S.rc2_pair_d > 0.0 && r2d >= S.rc2_pair_d);
         in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
         overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
+    }
+    if (terms & FAU_PAIR_SPLINE) { // SplinedPotential::operator() src/potentials.h:807-823
+        if (!in_pair) return 0.f;
+        const SplineP& q = S.spl[pidx];
+        bool above = r2 >= q.zmax, inside = r2 > q.zmin;
+        if (fabsf(r2 - q.zmax) <= 1e-5f * q.zmax || fabsf(r2 - q.zmin) <= 1e-5f * q.zmin) {
+            const double r2d = r2_fp64(); // the table's ends decide on the FP64 distance
+            above = r2d >= q.zmax_d;
+            inside = r2d > q.zmin_d;
+        }
+        if (above) return 0.f;
+        if (inside) return spline_u32(S, q, r2, mag);
+        if (q.hs) {
+            inf = true;
+            return 0.f;
+        }
+        // below the first knot: the exact terms
     }
     return pair_core(S, p, r2, in_pair, in_coul, overlap, inf, nan, mag);
 }
@@ -510,6 +597,12 @@ __device__ __forceinline__ double coul_trunc_s(const DevSys& S, double r)
 __device__ __forceinline__ double pair_u64(const DevSys& S, int ta, int tb, double r2)
 {
     if (S.rc2_pair_d > 0.0 && r2 >= S.rc2_pair_d) return 0.0;
+    if (S.terms & FAU_PAIR_SPLINE) {
+        const SplineP& q = S.spl[ta * S.nt + tb];
+        if (r2 >= q.zmax_d) return 0.0;
+        if (r2 > q.zmin_d) return spline_u64(S, q, r2);
+        if (q.hs) return __longlong_as_double(0x7ff0000000000000ULL);
+    }
     const double* P = S.pair_d + 4 * (ta * S.nt + tb);
     const double s2 = P[0], e4 = P[1], hs2 = P[2], qq = P[3];
     double u = 0.0;

@@ -35,6 +35,7 @@ __device__ __forceinline__ bool mol_task_fast(const DevSys& S, const PairF* pt, 
                                               int hb, bool do_n, bool do_o, FF& acc, int& flags,
                                               unsigned long long& n_pairs)
 {
+    if (S.terms & FAU_PAIR_SPLINE) return false; // tabulated pairs: the general path
     uint4 rb[NB];
 #pragma unroll
     for (int j = 0; j < NB; j++) rb[j] = S.rec[hb + j];

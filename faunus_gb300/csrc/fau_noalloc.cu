@@ -114,6 +114,8 @@ extern "C" int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* a, double*
     if (!a || !energy_out) return fau_internal_fail(FAU_ERR_ARG, "null argument");
     if (a->coulomb_type < FAU_COUL_PLAIN || a->coulomb_type > FAU_COUL_EWALD)
         return fau_internal_fail(FAU_ERR_ARG, "coulomb_type: plain, cut or ewald only");
+    if (a->pair_terms & ~(FAU_PAIR_COULOMB | FAU_PAIR_LJ | FAU_PAIR_WCA | FAU_PAIR_HS))
+        return fau_internal_fail(FAU_ERR_ARG, "pair_terms: coulomb, LJ, WCA and HS only (no spline tables)");
     if (a->n_particles < 1 || a->n_particles > FAU_NOALLOC_MAX_PARTICLES)
         return fau_internal_fail(FAU_ERR_ARG,
                                  "n_particles outside [1, FAU_NOALLOC_MAX_PARTICLES = 65536]: the shared scratch "

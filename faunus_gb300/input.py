@@ -20,6 +20,8 @@ Supported subset (anything else raises NotImplementedError naming the key):
   energy: nonbonded_coulomblj / _newcoulomblj / _coulombwca / _pm / _coulombhs / _pmwca
     (src/energy.cpp:1280-1327), nonbonded / nonbonded_exact (FunctorPotential:
     "default" and "A B" lists of coulomb / lennardjones / wca / hardsphere),
+    nonbonded_splined (the same lists tabulated: utol, ftol, u_at_rmin, u_at_rmax, rmax,
+    hardsphere; src/potentials.cpp:1513-1553),
     cutoff_g2g (number or per molecule pair), Ewald when coulomb type is ewald
     (src/energy.cpp:1134-1160), isobaric (P/atm, P/bar, P/kT, P/mM, P/Pa);
   moves: transrot, moltransrot, volume (src/move.cpp:190-222, 1580-1613, 986-993);
@@ -38,7 +40,7 @@ import numpy as np
 from . import _capi as A
 from . import yason
 from .system import (AVOGADRO, SystemSpec, bjerrum_length, coulomb_scheme, group_cutoff, kjmol_to_kt,
-                     pressure_kt)
+                     pressure_kt, splined)
 
 NAN = float("nan")
 
@@ -260,6 +262,7 @@ def load_input(src, seed: int = 0) -> Setup:
 
     # energy
     fields: Dict[str, Any] = {"pair_terms": 0}
+    spline_opts: Optional[dict] = None
     for name, block in _items(j.get("energy"), "energy"):
         if name == "isobaric":
             units = [k for k in block if k.startswith("P/")]
@@ -269,8 +272,23 @@ def load_input(src, seed: int = 0) -> Setup:
             continue
         if not name.startswith("nonbonded"):
             raise NotImplementedError(f"energy term '{name}'")
-        if name in ("nonbonded", "nonbonded_exact"):
+        if name == "nonbonded_cached":
+            raise NotImplementedError("energy term 'nonbonded_cached' (FP32 group-pair energy cache)")
+        if name in ("nonbonded", "nonbonded_exact", "nonbonded_splined"):
             _functor(block, fields, sig, eps, names, T)
+            if name == "nonbonded_splined":  # SplinedPotential::from_json, src/potentials.cpp:1513-1553
+                rmax = block.get("rmax")
+                cg = block.get("cutoff_g2g")
+                if isinstance(cg, (int, float)):
+                    rmax = float(cg)
+                elif isinstance(cg, dict):
+                    if "default" not in cg:
+                        raise ValueError("nonbonded_splined: an object cutoff_g2g needs a 'default' (the spline's rmax)")
+                    rmax = float(cg["default"])
+                spline_opts = {"utol": float(block.get("utol", 1e-3)), "ftol": float(block.get("ftol", 1e-2)),
+                               "u_at_rmin": float(block.get("u_at_rmin", 20.0)),
+                               "u_at_rmax": float(block.get("u_at_rmax", 1e-6)),
+                               "rmax": rmax, "hardsphere": bool(block.get("hardsphere", False))}
         else:
             parts = {"nonbonded_coulomblj": ("coulomb", "lennardjones"),
                      "nonbonded_newcoulomblj": ("coulomb", "lennardjones"),
@@ -302,6 +320,8 @@ def load_input(src, seed: int = 0) -> Setup:
                       group_flags=group_flags, group_molid=group_molid, n_types=nt, type_mass=mw,
                       temperature=T, name=str(Path(src).name) if isinstance(src, (str, Path)) and
                       "\n" not in str(src) and Path(str(src)).exists() else "input", **fields)
+    if spline_opts is not None:
+        spec = splined(spec, q_t, sig, **spline_opts)
     if spec.n_groups:
         cm = np.zeros((spec.n_groups, 3))
         for g in range(spec.n_groups):
@@ -354,7 +374,8 @@ def _functor(block: dict, fields: dict, sig, eps, names, T: float) -> None:
     lists = {}
     default = block.get("default", [])
     for key, lst in block.items():
-        if key in ("default", "cutoff_g2g", "selfenergy"):
+        if key in ("default", "cutoff_g2g", "selfenergy", "utol", "ftol", "u_at_rmin", "u_at_rmax", "rmax",
+                   "hardsphere", "to_disk"):
             continue
         a, b = key.split()
         lists[(names.index(a), names.index(b))] = lst

@@ -9,6 +9,7 @@ physical constants.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -160,6 +161,30 @@ def kjmol_to_kt(x: float, temperature: float = 298.15) -> float:
     return x / (temperature * BOLTZMANN) / AVOGADRO * 1e3
 
 
+def andrea_spline(f, zmin: float, zmax: float, utol: float, ftol: float = -1.0, cap: int = 1201):
+    """Tabulate::Andrea::generate (src/tabulate.h:212-298) of a Python function f(z) on
+    ]zmin, zmax] through fau_andrea_generate: (knots ascending, coefficients (pieces, 6))."""
+    cb = A.SCALAR_FN(lambda z, _ctx: float(f(z)))
+    z = np.zeros(cap)
+    c = np.zeros(6 * cap)
+    n = C.c_int()
+    A.check(A.lib().fau_andrea_generate(cb, None, float(zmin), float(zmax), float(utol), float(ftol), cap,
+                                        A.as_dptr(z), A.as_dptr(c), C.byref(n)), "fau_andrea_generate")
+    m = n.value
+    return z[:m].copy(), c[:6 * (m - 1)].reshape(m - 1, 6).copy()
+
+
+def andrea_eval(knots: np.ndarray, coef: np.ndarray, z: float) -> float:
+    """Andrea::eval (src/tabulate.h:188-207): Horner in z - z_i on the piece z_i < z <= z_{i+1}."""
+    i = int(np.searchsorted(knots, z, side="left")) - 1
+    i = min(max(i, 0), len(knots) - 2)
+    dz = z - knots[i]
+    s = 0.0
+    for k in range(5, 0, -1):
+        s = dz * (s + coef[i][k])
+    return s + coef[i][0]
+
+
 @dataclass
 class SystemSpec:
     """Space + Hamiltonian of one system, as numpy arrays (see fau_sys_desc)."""
@@ -188,6 +213,7 @@ class SystemSpec:
     cutoff_g2g: float = 0.0
     cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
     isobaric_pressure: Optional[float] = None  # Isobaric term's pressure (kT/A^3, see pressure_kt); None: no term
+    spline: Optional[dict] = None         # FAU_PAIR_SPLINE tables: begin (T*T+1), r2, coef, hs (see splined)
     ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
     precision: int = A.FAU_PREC_FP32C
     cell_capacity: int = 0
@@ -273,7 +299,60 @@ class SystemSpec:
                 raise ValueError("cutoff_g2g_pairs must be a square matrix")
             d.n_molids = int(m.shape[0])
             d.cutoff_g2g_pairs = f64(m.reshape(-1))
+        if self.spline is not None:
+            d.spline_begin = i32(self.spline["begin"])
+            d.spline_r2 = f64(self.spline["r2"])
+            d.spline_coef = f64(self.spline["coef"])
+            d.spline_hs = i32(self.spline.get("hs"))
         return d, keep
+
+
+def splined(spec: "SystemSpec", type_charge, type_sigma, *, utol: float = 1e-3, ftol: float = 1e-2,
+            u_at_rmin: float = 20.0, u_at_rmax: float = 1e-6, rmax: Optional[float] = None,
+            hardsphere: bool = False) -> "SystemSpec":
+    """nonbonded_splined: the spec's pair terms tabulated per atom-type pair as
+    SplinedPotential::from_json does (src/potentials.cpp:1513-1553; the defaults are its own),
+    through fau_spline_tabulate with the atom types' charges and sigmas (AtomData q, sigma).
+
+    Returns a copy with FAU_PAIR_SPLINE and the tables.  Every pair is zero beyond its table's
+    last knot, so pair_cutoff is set just beyond the longest table (the device's cell lists
+    then follow the tables without changing any energy); a smaller positive pair_cutoff
+    already in the spec is kept."""
+    T = int(spec.n_types)
+    base = spec.copy()
+    base.spline = None
+    base.pair_terms = int(base.pair_terms) & ~A.FAU_PAIR_SPLINE
+    d, keep = base.to_desc()
+    opts = A.SplineOpts(float(utol), float(ftol), float(u_at_rmin), float(u_at_rmax),
+                        float(rmax) if rmax else 0.0, int(bool(hardsphere)), 0)
+    cap = 1201
+    tables = {}
+    for a in range(T):
+        for b in range(a + 1):
+            z = np.zeros(cap)
+            c = np.zeros(6 * cap)
+            n, hs = C.c_int(), C.c_int()
+            A.check(A.lib().fau_spline_tabulate(C.byref(d), a, b, float(type_charge[a]), float(type_charge[b]),
+                                                0.5 * (float(type_sigma[a]) + float(type_sigma[b])), C.byref(opts),
+                                                cap, A.as_dptr(z), A.as_dptr(c), C.byref(n), C.byref(hs)),
+                    "fau_spline_tabulate")
+            m = n.value
+            tables[a, b] = tables[b, a] = (z[:m].copy(), c[:6 * (m - 1)].copy(), hs.value)
+    begin, r2, coef, hsl = [0], [], [], []
+    for a in range(T):
+        for b in range(T):
+            z, c, h = tables[a, b]
+            begin.append(begin[-1] + len(z))
+            r2.append(z)
+            coef.append(c)
+            hsl.append(h)
+    out = base
+    out.spline = {"begin": np.array(begin, np.int32), "r2": np.concatenate(r2), "coef": np.concatenate(coef),
+                  "hs": np.array(hsl, np.int32)}
+    out.pair_terms = int(out.pair_terms) | A.FAU_PAIR_SPLINE
+    reach = math.sqrt(max(float(t[0][-1]) for t in tables.values())) * (1.0 + 1e-9)
+    out.pair_cutoff = reach if not spec.pair_cutoff > 0 else min(float(spec.pair_cutoff), reach)
+    return out
 
 
 class Context:

@@ -55,7 +55,10 @@ enum fau_pair_term {
     FAU_PAIR_COULOMB = 1 << 0, /* lB qi qj S(r) / r                             */
     FAU_PAIR_LJ = 1 << 1,      /* 4 eps [(s/r)^12 - (s/r)^6]   potentials.h:42-49  */
     FAU_PAIR_WCA = 1 << 2,     /* LJ + eps, zero beyond 2^(1/6) s   :151-160     */
-    FAU_PAIR_HS = 1 << 3       /* +inf when r < s                   :203-207     */
+    FAU_PAIR_HS = 1 << 3,      /* +inf when r < s                   :203-207     */
+    FAU_PAIR_SPLINE = 1 << 4   /* nonbonded_splined: the sum of the terms above
+                                  tabulated per atom-type pair (spline_* below;
+                                  SplinedPotential src/potentials.h:770-824)      */
 };
 
 /* Coulomb short-range function S(q = r/Rc) (docs/_docs/energy.md:169-205). */
@@ -134,6 +137,15 @@ typedef struct fau_sys_desc {
     double coulomb_poly[FAU_COUL_MAX_POLY];
     int isobaric;             /* 1: the Hamiltonian has the Isobaric term (src/energy.cpp:859-901) */
     double pressure;          /* its pressure in kT / A^3                             */
+    /* FAU_PAIR_SPLINE: per atom-type pair ab = a * n_types + b, Andrea spline knots z_0 < ... <
+       z_m in r^2 with 6 coefficients an interval (KnotData, src/potentials.h:773-780; made by
+       fau_spline_tabulate). SplinedPotential::operator() (src/potentials.h:807-823): 0 for
+       r^2 >= z_m; sum_k c_k (r^2 - z_i)^k on the interval z_i < r^2 <= z_{i+1} (Andrea::eval,
+       src/tabulate.h:188-207); for r^2 <= z_0, +inf if spline_hs, else the exact terms.        */
+    const int* spline_begin;  /* n_types^2 + 1 offsets into spline_r2; >= 2 knots a pair    */
+    const double* spline_r2;  /* the knots of every pair, ascending within a pair          */
+    const double* spline_coef;/* 6 an interval; pair ab's start at 6 (spline_begin[ab] - ab) */
+    const int* spline_hs;     /* n_types^2 KnotData::hardsphere_repulsion; NULL: none       */
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */
@@ -432,6 +444,35 @@ int fau_movegen_generate(fau_movegen* gen, fau_proposal* out, int n);
 /* Serialise / restore both engines (std::mt19937 text form, as Random::to_json). */
 int fau_movegen_get_state(const fau_movegen* gen, char* buf, size_t buflen);
 int fau_movegen_set_state(fau_movegen* gen, const char* state);
+
+/* ---- splined pair potentials (host only) ----------------------------------
+ * Tabulate::Andrea::generate (src/tabulate.h:212-298): quintic pieces in z = r^2 that match
+ * f, f' and f'' (central differences, step 1e-4) at both ends, each as long as 11 checks keep
+ * |spline - f| <= utol and, with ftol > 0, |spline' - f'| <= ftol; knots from zmax down to zmin,
+ * at most 1200 intervals. Writes the knots (ascending) and 6 coefficients an interval; *n_knots
+ * = intervals + 1; FAU_ERR_ARG when cap is too small or no interval meets the tolerance. */
+typedef double (*fau_scalar_fn)(double z, void* ctx);
+int fau_andrea_generate(fau_scalar_fn f, void* ctx, double zmin, double zmax, double utol, double ftol,
+                        int cap, double* r2_out, double* coef_out, int* n_knots);
+
+/* SplinedPotential::from_json + createKnots (src/potentials.cpp:1513-1597) for atom types a, b:
+ * f = the sum of desc's pair terms (FAU_PAIR_SPLINE ignored) between two particles of those
+ * types with charges charge_a, charge_b; rmin from `rmin_start` (0.5 (sigma_a + sigma_b)) moved
+ * in steps of 0.01 until |f| is within [u_at_rmin / 1.1, 1.1 u_at_rmin] (findLowerDistance),
+ * rmax from `rmax_start` (<= 0: 10 rmin_start) moved out until |f| <= u_at_rmax
+ * (findUpperDistance); hardsphere_repulsion kept only where the spline at rmin^2 + 0.01 is >= 0. */
+typedef struct fau_spline_opts {
+    double utol;       /* default 1e-3 kT                                                   */
+    double ftol;       /* default 1e-2; <= 0: no derivative check                          */
+    double u_at_rmin;  /* default 20 kT                                                     */
+    double u_at_rmax;  /* default 1e-6 kT                                                   */
+    double rmax_start; /* "rmax" or the cutoff_g2g default; <= 0: 10 rmin_start             */
+    int hardsphere;    /* "hardsphere": +inf below the first knot where repulsive           */
+    int pad;
+} fau_spline_opts;
+int fau_spline_tabulate(const fau_sys_desc* desc, int type_a, int type_b, double charge_a, double charge_b,
+                        double rmin_start, const fau_spline_opts* opts, int cap, double* r2_out,
+                        double* coef_out, int* n_knots, int* hs_out);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,33 @@ struct PairParams {
     // at infinite Debye length; the host turns each named scheme into these coefficients)
     double cerfc = 0;
     std::vector<double> cpoly;
+    // FAU_PAIR_SPLINE: KnotData per atom-type pair (src/potentials.h:773-780): knots z in r^2
+    // from spl_begin[ab], 6 coefficients a piece from 6 (spl_begin[ab] - ab)
+    std::vector<int> spl_begin, spl_hs;
+    std::vector<double> spl_z, spl_c;
+
+    // Andrea::eval src/tabulate.h:188-207: the piece z_i < z <= z_{i+1} by lower_bound, then
+    // Horner in z - z_i (absolute: the sum of |c_k| |dz|^k instead)
+    double spline(size_t ab, double r2, bool absolute) const
+    {
+        const double* z = spl_z.data() + spl_begin[ab];
+        const int m = spl_begin[ab + 1] - spl_begin[ab];
+        long i = (long)(std::lower_bound(z, z + m, r2) - z) - 1;
+        i = std::min(std::max(i, 0L), (long)m - 2);
+        const double* c = spl_c.data() + 6 * (size_t(spl_begin[ab]) - ab) + 6 * i;
+        const double dz = absolute ? std::fabs(r2 - z[i]) : r2 - z[i];
+        double sum = 0;
+        for (int k = 5; k > 0; k--) sum = dz * (sum + (absolute ? std::fabs(c[k]) : c[k]));
+        return sum + (absolute ? std::fabs(c[0]) : c[0]);
+    }
+    // SplinedPotential::operator() src/potentials.h:807-823: 1 spline, 0 beyond the last knot,
+    // -1 +inf (hard sphere), 2 the exact terms
+    int spline_region(size_t ab, double r2) const
+    {
+        if (r2 >= spl_z[spl_begin[ab + 1] - 1]) return 0;
+        if (r2 > spl_z[spl_begin[ab]]) return 1;
+        return spl_hs[ab] ? -1 : 2;
+    }
 
     double trunc_s(double r, bool absolute) const
     {
@@ -131,6 +158,12 @@ struct PairParams {
     {
         if (pair_cutoff2 > 0.0 && r2 >= pair_cutoff2) return 0.0;
         const size_t ab = size_t(ta) * n_types + tb;
+        if (terms & FAU_PAIR_SPLINE) {
+            const int reg = spline_region(ab, r2);
+            if (reg == 0) return 0.0;
+            if (reg == 1) return spline(ab, r2, false);
+            if (reg < 0) return infty;
+        }
         double u = 0.0;
         if (terms & FAU_PAIR_COULOMB) u += coulomb(qa, qb, r2);
         if (terms & FAU_PAIR_LJ) { // LennardJones src/potentials.h:42-49
@@ -159,6 +192,11 @@ struct PairParams {
     {
         if (pair_cutoff2 > 0.0 && r2 >= pair_cutoff2) return 0.0;
         const size_t ab = size_t(ta) * n_types + tb;
+        if (terms & FAU_PAIR_SPLINE) {
+            const int reg = spline_region(ab, r2);
+            if (reg == 1) return spline(ab, r2, true);
+            if (reg != 2) return 0.0;
+        }
         double m = 0.0;
         if (terms & FAU_PAIR_COULOMB) {
             if (coul_type == FAU_COUL_TRUNC) { // |qq/r| (|e| erfc + sum |c_k| q^k): S cancels to 0 at Rc
@@ -837,6 +875,17 @@ static System buildSystem(const fau_sys_desc* d)
     if (d->coulomb_type == FAU_COUL_TRUNC) {
         P.cerfc = d->coulomb_erfc;
         P.cpoly.assign(d->coulomb_poly, d->coulomb_poly + std::max(0, std::min(d->coulomb_poly_n, FAU_COUL_MAX_POLY)));
+    }
+    if ((d->pair_terms & FAU_PAIR_SPLINE) && d->spline_begin && d->spline_r2 && d->spline_coef) {
+        const size_t np = size_t(nt) * nt, knots = size_t(d->spline_begin[np]);
+        P.spl_begin.assign(d->spline_begin, d->spline_begin + np + 1);
+        P.spl_z.assign(d->spline_r2, d->spline_r2 + knots);
+        P.spl_c.assign(d->spline_coef, d->spline_coef + 6 * (knots - np));
+        P.spl_hs.assign(np, 0);
+        if (d->spline_hs) P.spl_hs.assign(d->spline_hs, d->spline_hs + np);
+    }
+    else {
+        P.terms &= ~FAU_PAIR_SPLINE;
     }
     if (d->cutoff_g2g > 0) s.cutoff_g2g2 = d->cutoff_g2g * d->cutoff_g2g;
     s.isobaric = d->isobaric != 0;

@@ -59,7 +59,8 @@ int main(void) {
   O(fau_proposal, u) O(fau_batch_params, temperatures) O(fau_move_desc, groups) O(fau_trial_result, accepted)
   O(fau_sys_desc, cutoff_g2g_pairs) O(fau_sys_desc, coulomb_poly) O(fau_sys_desc, pressure)
   O(fau_batch_params, sampler) O(fau_batch_params, n_sample_blocks) O(fau_move_desc, volume_method)
-  O(fau_sampler_desc, rdf_dr) O(fau_sampler_desc, energy)
+  O(fau_sampler_desc, rdf_dr) O(fau_sampler_desc, energy) S(fau_spline_opts)
+  O(fau_sys_desc, spline_begin) O(fau_sys_desc, spline_hs) O(fau_spline_opts, hardsphere)
   return 0;
 }
 """
@@ -75,7 +76,7 @@ def test_struct_layouts_match_header(tmp_path):
     sizes = {"fau_ewald_desc": A.EwaldDesc, "fau_sys_desc": A.SysDesc, "fau_energy_terms": A.EnergyTerms,
              "fau_trial_result": A.TrialResult, "fau_proposal": A.Proposal, "fau_run_stats": A.RunStats,
              "fau_batch_params": A.BatchParams, "fau_batch_stats": A.BatchStats, "fau_move_desc": A.MoveDesc,
-             "fau_sampler_desc": A.SamplerDesc}
+             "fau_sampler_desc": A.SamplerDesc, "fau_spline_opts": A.SplineOpts}
     for name, cls in sizes.items():
         assert int(out[name]) == C.sizeof(cls), name
     offs = {"fau_sys_desc.ewald": A.SysDesc.ewald.offset, "fau_sys_desc.precision": A.SysDesc.precision.offset,
@@ -87,7 +88,10 @@ def test_struct_layouts_match_header(tmp_path):
             "fau_batch_params.sampler": A.BatchParams.sampler.offset,
             "fau_batch_params.n_sample_blocks": A.BatchParams.n_sample_blocks.offset,
             "fau_move_desc.volume_method": A.MoveDesc.volume_method.offset,
-            "fau_sampler_desc.rdf_dr": A.SamplerDesc.rdf_dr.offset, "fau_sampler_desc.energy": A.SamplerDesc.energy.offset}
+            "fau_sampler_desc.rdf_dr": A.SamplerDesc.rdf_dr.offset, "fau_sampler_desc.energy": A.SamplerDesc.energy.offset,
+            "fau_sys_desc.spline_begin": A.SysDesc.spline_begin.offset,
+            "fau_sys_desc.spline_hs": A.SysDesc.spline_hs.offset,
+            "fau_spline_opts.hardsphere": A.SplineOpts.hardsphere.offset}
     for k, v in offs.items():
         assert int(out[k]) == v, k
 
