@@ -493,7 +493,8 @@ __device__ __forceinline__ float pair_u32_far(const DevSys& S, const PairF& p, f
 // FAU_PAIR_SPLINE, FP32: the piece z_i < r2 <= z_{i+1} (Andrea::eval's lower_bound,
 // src/tabulate.h:188-207) from the index grid and a short scan either way, then Horner in
 // dz = r2 - z_i. `mag` gets sum_k |c_k| |dz|^k, the error scale of the evaluation.
-__device__ __forceinline__ float spline_u32(const DevSys& S, const SplineP& q, float r2, float& mag)
+// Not inlined: the kernels keep the register allocation of the unsplined terms.
+static __device__ __noinline__ float spline_u32(const DevSys& S, const SplineP& q, float r2, float& mag)
 {
     int g = (int)((r2 - q.zmin) * q.inv_h);
     g = min(max(g, 0), q.grid_n - 1);
@@ -545,7 +546,9 @@ __device__ __forceinline__ double spline_u64(const DevSys& S, const SplineP& q, 
 // `xj` (optional) replaces particle j's resident FP64 position when the caller
 // knows a newer one than memory holds.  `mag` accumulates the sum of |summand|
 // over the enabled terms, LJ's r^-12 and r^-6 parts counted separately (the
-// floating-point error scale of this pair energy).
+// floating-point error scale of this pair energy).  SPL false leaves out the
+// FAU_PAIR_SPLINE tables (for callers that dispatch splined systems elsewhere).
+template <bool SPL = true>
 __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int pidx, float r2, const double* xi,
                                           int j, bool& inf, bool& nan, float& mag, const double* xj = nullptr)
 {
@@ -563,7 +566,7 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
         in_coul = __dadd_rn(sqrt(r2d), 2.220446049250313e-16) < S.rc_coul_d;
         overlap = (terms & FAU_PAIR_HS) && r2d < S.pair_d[4 * pidx + 2];
     }
-    if (terms & FAU_PAIR_SPLINE) { // SplinedPotential::operator() src/potentials.h:807-823
+    if (SPL && (terms & FAU_PAIR_SPLINE)) { // SplinedPotential::operator() src/potentials.h:807-823
         if (!in_pair) return 0.f;
         const SplineP& q = S.spl[pidx];
         bool above = r2 >= q.zmax, inside = r2 > q.zmin;
@@ -578,7 +581,7 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
             inf = true;
             return 0.f;
         }
-        // below the first knot: the exact terms
+        // at or below the first knot: the exact terms
     }
     return pair_core(S, p, r2, in_pair, in_coul, overlap, inf, nan, mag);
 }

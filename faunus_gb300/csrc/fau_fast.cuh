@@ -323,19 +323,23 @@ struct PairOut {
     int flags; // F_* bits of this state
 };
 
-// one state of one pair (a single call site keeps the kernel's code small)
+// one state of one pair (a single call site keeps the kernel's code small); SPL: the
+// instance of splined systems' kernel body (fast_chain_kernel), so that the others keep the
+// unsplined register allocation
+template <bool SPL>
 static __device__ __noinline__ PairOut fast_pair_state(const DevSys& S, PairF p, int pidx, float r2, const double* xi,
                                                         int j, const double* xj, bool is_new)
 {
     bool inf = false, nan = false;
     float mag = 0.f;
-    const float u = pair_u32(S, p, pidx, r2, xi, j, inf, nan, mag, xj);
+    const float u = pair_u32<SPL>(S, p, pidx, r2, xi, j, inf, nan, mag, xj);
     PairOut o;
     o.u = u;
     o.mag = mag;
     o.flags = is_new ? ((inf ? F_NEW_INF : 0) | (nan ? F_NEW_NAN : 0)) : ((inf ? F_OLD_INF : 0) | (nan ? F_OLD_NAN : 0));
     return o;
 }
+
 
 // Metropolis decision shared by every thread: FP32 unless the exponential is
 // within 1e-4 of u (or an infinity, NaN or the surface term is involved), then
@@ -368,8 +372,8 @@ __device__ __forceinline__ bool fast_decide(FF s, int flags, double du_surf, boo
     return metropolis(x, u);
 }
 
-template <int NWC, bool PHILOX>
-__global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
+template <int NWC, bool PHILOX, bool SPL>
+__device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
 {
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
     const long long t_start = clock64();
@@ -684,8 +688,8 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
                     if (q < nv && (ent & (st ? kEntOld : kEntNew))) {
                         const int j = cells ? (int)(rj.w & 0xFFFFFFu) : wbase + src + (2 * rr + (second ? 1 : 0)) * NTC;
                         const int pidx = ti * nt + (int)(rj.w >> 24);
-                        const PairOut o = fast_pair_state(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
-                                                          st ? m.xo : m.xn, j, nullptr, st == 0);
+                        const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
+                                                               st ? m.xo : m.xn, j, nullptr, st == 0);
                         ff_add(accp, st ? -o.u : o.u);
                         flags |= o.flags;
                         n_pairs++;
@@ -874,6 +878,15 @@ __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 :
         G.consumed = stop == FAU_ERR_CAPACITY ? t + 1 : t;
         G.cycles += (unsigned long long)(clock64() - t_start);
     }
+}
+
+// The body twice, selected per CTA by its system: splined systems (FAU_PAIR_SPLINE) get their
+// own instance, so the pair path of the others compiles exactly as without the tables.
+template <int NWC, bool PHILOX>
+__global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
+{
+    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true>(A);
+    else fast_chain_body<NWC, PHILOX, false>(A);
 }
 
 // dynamic shared memory of the pipelined kernel for K k-vectors, table size nc
