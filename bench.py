@@ -414,7 +414,7 @@ def other_configs(ctx, configs, replicas: int) -> dict:
 
     mps, pps = batch_rate(configs.primitive_model(n=200), replicas, 20000)
     out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps}
-    mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 500)
+    mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 5000)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
                               "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
     specs, temps = configs.pt_replicas(n_rep=256)
