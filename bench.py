@@ -444,9 +444,10 @@ def served(ctx, F, configs, full: bool = False) -> dict:
     stream = configs.served_jobs(n_jobs=n_jobs, rate_hz=rate, n_max=n_max, moves_max=m_max, seed=4)
     jobs = jobs_from_stream(stream)
     budget = 128 << 30
-    srv = Server(GpuBackend(ctx), hbm_budget=budget, max_slots=608, block_moves=1000, round_cycles=2e8, seed=7)
+    srv = Server(GpuBackend(ctx), hbm_budget=budget, max_slots=608, seed=7, time_slice_s=0.025)
     rep = srv.run(jobs, fast_forward=False)
-    rep.update({"jobs": n_jobs, "hbm_budget_bytes": budget, "slots": 608, "round_cycles": 2e8,
+    rep.update({"jobs": n_jobs, "hbm_budget_bytes": budget, "slots": 608,
+                "rounds_are": "25 ms time slices: each chain runs until it has had 25 ms of device time",
                 "stream": f"served_jobs(seed 4): Poisson {rate:g} jobs/s, primitive model / bulk Ewald / SPC/E "
                           f"water, N log-uniform 64..{n_max}, moves log-uniform 1e4..{m_max:g}"
                           + ("" if full else " (bounded; --served-full for 20,000 / 1e6)")})

@@ -115,7 +115,8 @@ class BatchParams(C.Structure):
                 ("temperatures", dptr), ("threads", C.c_int), ("streams", C.POINTER(C.c_uint32)),
                 ("counters", C.POINTER(C.c_uint64)), ("dp_per_system", dptr), ("dprot_per_system", dptr),
                 ("cycles_out", C.POINTER(C.c_uint64)), ("sampler", C.c_void_p),
-                ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int)]
+                ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int),
+                ("time_budget_ns", C.c_uint64), ("moves_out", C.POINTER(C.c_int64))]
 
 
 class SamplerDesc(C.Structure):

@@ -42,13 +42,15 @@ struct SysSummary {
     unsigned long long moves, accepted, pair_evals, k_updates, cycles;
     double energy, beta_scale;
     int err, pad;
+    long long consumed; // proposals performed by the system's last chain launch
 };
 
 __global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const DevSys& S = *sys[i];
-        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, sys_energy(S), S.beta_scale, S.err, 0};
+        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, sys_energy(S), S.beta_scale, S.err, 0,
+                  S.consumed};
     }
 }
 
@@ -312,6 +314,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     }
     else {
         a.n_moves = reinterpret_cast<const long long*>(dbuf + off_knm);
+        a.time_budget_ns = P->time_budget_ns; // chains may end early; moves_out reports how far
     }
     // the same arguments shifted to the chain-kernel systems
     ChainArgs ae = a;
@@ -450,6 +453,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     }
     if (P->cycles_out)
         for (int i = 0; i < n; i++) P->cycles_out[i] = (uint64_t)(s1[i].cycles - s0[i].cycles);
+    if (P->moves_out) // blocked launches run every block in full; otherwise the one launch's count
+        for (int i = 0; i < n; i++) P->moves_out[i] = blocked ? (int64_t)blk_moves * nblk : (int64_t)s1[i].consumed;
     S.swaps_attempted = (int64_t)pst[0];
     S.swaps_accepted = (int64_t)pst[1];
     S.device_ms = ms;

@@ -559,9 +559,13 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
             tprev = t;
         }
     };
+    __shared__ unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
+    __shared__ long long sh_up_at;       // >= 0: the time budget ended the launch after this many moves
     if (tid == 0) {
         ms.prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         ms.consumed = 0;
+        sh_t0 = global_ns();
+        sh_up_at = -1;
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -572,7 +576,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
     __syncthreads();
 
     for (long long mv = 0; mv < nmoves; mv++) {
-        if (ms.stop) break;
+        if (ms.stop || sh_up_at >= 0) break;
         // ---- the previous move's Q(k) change (State::sync trial -> accepted, deferred)
         if (ms.prev_accept) {
             for (int k = tid; k < K; k += NT) {
@@ -1018,6 +1022,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                 tick(6);
             }
         }
+        if (tid == 0 && A.time_budget_ns && global_ns() - sh_t0 >= A.time_budget_ns) sh_up_at = mv + 1;
         __syncthreads(); // B2
         tick(tid == 0 ? 7 : 10);
     }
@@ -1059,7 +1064,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
 #pragma unroll
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
         if (ms.stop) G.err = ms.stop;
-        G.consumed = ms.stop ? ms.consumed : nmoves;
+        G.consumed = ms.stop ? ms.consumed : (sh_up_at >= 0 ? sh_up_at : nmoves);
         G.q_valid = K ? ms.prev_accept : 0;
         G.q_since = K ? since_flush : 0;
         G.cycles += (unsigned long long)(clock64() - t_start);

@@ -298,6 +298,14 @@ __host__ __device__ inline double sys_energy(const DevSys& S)
 }
 
 // squared minimum-image distance of two fixed-point records, FP32
+// the GPU's global nanosecond timer (PTX %globaltimer)
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ float r2_fixed(const DevSys& S, uint4 a, uint4 b)
 {
     const float dx = (float)(int32_t)(a.x - b.x) * S.fx_len[0];

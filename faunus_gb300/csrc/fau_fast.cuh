@@ -407,6 +407,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
     __shared__ float itq[kMaxITypes];
     __shared__ double itqd[kMaxITypes];
     __shared__ fau_proposal ring[PHILOX ? 1 : kFastRing];
+    __shared__ unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
+    __shared__ int sh_up;                // the time budget is spent
     __shared__ unsigned long long red_u[NWC][2];
     // phase timers (profiling only; every phase still runs), accumulated by thread 0 (producer) and
     // thread 32 (first compute warp): 0 commit data, 1 prepare t+1, 2 copies of t+2, 3 barrier 1,
@@ -455,6 +457,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
 #pragma unroll
         for (int d = 0; d < 3; d++) ps.M[d] = S.M[d];
         mvb[2].kind = FAU_MOVE_NONE; // "previous move" of move 0
+        sh_t0 = global_ns();
+        sh_up = 0;
     }
     __syncthreads();
     const bool cells = (S.flags & SYS_CELLS) != 0;
@@ -831,10 +835,15 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
             hit = fast_parallel(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc);
         }
         tick(tid == 0 ? 6 : 13);
+        if (A.time_budget_ns && tid == 0 && global_ns() - sh_t0 >= A.time_budget_ns) sh_up = 1;
         hit = __syncthreads_or(hit) != 0; // B1: commit, tables and entries visible
         if (hit && producer && lane == 0) mvb[(t + 1) % 3].conflict |= FC_CELLS;
         tick(tid == 0 ? 6 : 14);
         prev_accept = accept;
+        if (sh_up) { // the time budget is spent: the launch ends after move t
+            t++;
+            break;
+        }
     }
     if (producer && lane == 0) cp_async_wait<0>();
     __syncthreads();

@@ -34,6 +34,9 @@ struct ChainArgs {
     double2* pending_dq;
     // optional per-CTA phase timers (clock64 cycles, kPhaseSlots per CTA) for profiling
     unsigned long long* phase_cycles;
+    // > 0: a CTA ends its chain at the first move boundary after this many ns of its own
+    // (globaltimer); G.consumed then holds the moves done
+    unsigned long long time_budget_ns;
 };
 constexpr int kPhaseSlots = 17;     // chain kernel (last slot: move count)
 constexpr int kFastPhaseSlots = 24; // pipelined kernel (the per-CTA stride of phase_cycles for both)

@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     __shared__ uint32_t nbl[CH];   // neighbour group | interacting states
     __shared__ uint32_t nbl_b[CH]; // its first particle | atom count << 24
     __shared__ int nbl_wcnt[2][NWC]; // survivors per compute warp: single pass | current chunk
-    __shared__ int sh_prev_accept, sh_stop;
+    __shared__ int sh_prev_accept, sh_stop, sh_time_up;
+    __shared__ unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
     __shared__ long long sh_consumed;
 
     const float rec_pref_f = (float)S.rec_pref;
@@ -157,6 +158,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     if (tid == 0) {
         sh_prev_accept = S.q_valid; // the previous launch's last accepted change, if not yet folded
         sh_stop = 0;
+        sh_time_up = 0;
+        sh_t0 = global_ns();
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
@@ -171,8 +174,8 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         MoveShared& mn = msb[cur ^ 1];
         const float2* tab = tabs + cur * tab_len;
         float2* tab_next = tabs + (cur ^ 1) * tab_len;
-        if (sh_stop || ms.stop) { // a NaN energy change ended the chain, or a proposal was invalid
-            consumed = sh_stop ? sh_consumed : mv;
+        if (sh_stop || ms.stop || sh_time_up) { // a NaN energy change ended the chain, a proposal
+            consumed = sh_stop ? sh_consumed : mv; // was invalid, or the time budget is spent
             break;
         }
         const int kind = ms.kind;
@@ -486,6 +489,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                     sh_stop = stop;
                     sh_consumed = mv;
                 }
+                if (A.time_budget_ns && global_ns() - sh_t0 >= A.time_budget_ns) sh_time_up = 1;
             }
             __syncwarp();
             tick(5);

@@ -12,10 +12,12 @@ molecular translate/rotate moves.  The server
     round (per-system dp and dprot; single-atom jobs in the pipelined kernel,
     molecular ones beside them in the chain kernel) -- jobs join and leave
     between rounds, so work that arrives while others run overlaps with them;
-  * sizes each job's share of a round to a common time budget: a job's first
-    round is a ``block_moves`` calibration, after which its measured SM cycles
-    per move set how many moves fit in ``round_cycles`` (a slow chain does not
-    hold fast ones back, and a fast one does not idle while a slow one runs);
+  * gives every job the same device time a round: with ``time_slice_s`` each
+    chain runs until it has had that much time of its own (the kernels stop at
+    the first move boundary past it and report the moves done), so no chain
+    waits for another's share; without it, a job's first round is a
+    ``block_moves`` calibration, after which its measured SM cycles per move
+    set how many moves fit in ``round_cycles``;
   * retires a job when its moves are done and reports, per job, the queueing
     and run time, and for the stream, p50/p99 latency (arrival -> result) and
     the aggregate moves/s.
@@ -99,6 +101,19 @@ class GpuBackend:
                            dprot_per_system=dprot, threads=self.threads, cycles_out=cycles)
         return cycles
 
+    def run_timed(self, handles, moves: Sequence[int], time_budget_s: float, *, seed: int,
+                  streams: Sequence[int], counters: Sequence[int], dp: Sequence[float],
+                  dprot: Sequence[float]) -> np.ndarray:
+        """Advance each system by up to its move count, each chain ending at the first move
+        boundary after time_budget_s of its own (one launch); returns the moves each performed."""
+        done = np.zeros(len(handles), dtype=np.int64)
+        self.ctx.run_batch(handles, moves_per_system=np.asarray(moves, dtype=np.int64), seed=seed,
+                           streams=np.asarray(streams, dtype=np.uint32),
+                           counters=np.asarray(counters, dtype=np.uint64), dp_per_system=dp,
+                           dprot_per_system=dprot, threads=self.threads, time_budget_s=time_budget_s,
+                           moves_out=done)
+        return done
+
     def result(self, handle, with_positions: bool) -> dict:
         c = handle.counters()
         return {"energy": handle.running_energy(), "accepted": c["accepted"], "moves": c["moves"],
@@ -111,7 +126,11 @@ class GpuBackend:
 class Server:
     def __init__(self, backend, hbm_budget: int, max_slots: int = 608, block_moves: int = 2000, seed: int = 1,
                  keep_positions: bool = False, clock: Callable[[], float] = time.perf_counter,
-                 round_cycles: float = 2e8, min_block: int = 100):
+                 round_cycles: float = 2e8, min_block: int = 100, time_slice_s: Optional[float] = None):
+        """time_slice_s: rounds are time slices -- every resident job runs until its chain has
+        had that much device time or its moves are done (backend.run_timed), so no chain waits
+        for the slowest share of a round; None: shares of round_cycles from measured cycles
+        per move (backend.run)."""
         if hbm_budget <= 0:
             raise ValueError("hbm_budget must be positive")
         self.backend = backend
@@ -120,6 +139,9 @@ class Server:
         self.block = int(block_moves)
         self.round_cycles = float(round_cycles)
         self.min_block = int(min_block)
+        self.time_slice = None if time_slice_s is None else float(time_slice_s)
+        if self.time_slice is not None and not self.time_slice > 0:
+            raise ValueError("time_slice_s must be positive")
         self.seed = int(seed)
         self.keep_positions = keep_positions
         self.clock = clock
@@ -185,17 +207,24 @@ class Server:
         if not self.active:
             return 0
         members = list(self.active.values())
-        moves = [min(self._share(a), a.job.moves - a.done) for a in members]
-        cycles = self.backend.run([a.handle for a in members], moves, seed=self.seed,
-                                  streams=[a.job.id for a in members], counters=[a.done for a in members],
-                                  dp=[a.job.dp for a in members], dprot=[a.job.dprot for a in members])
+        kw = dict(seed=self.seed, streams=[a.job.id for a in members], counters=[a.done for a in members],
+                  dp=[a.job.dp for a in members], dprot=[a.job.dprot for a in members])
         total = 0
-        for i, (a, m) in enumerate(zip(members, moves)):
-            a.done += m
-            total += m
-            if cycles is not None and m > 0 and cycles[i] > 0:
-                c = float(cycles[i]) / m
-                a.cycles_per_move = c if a.cycles_per_move == 0.0 else 0.5 * (a.cycles_per_move + c)
+        if self.time_slice is not None:
+            ran = self.backend.run_timed([a.handle for a in members], [a.job.moves - a.done for a in members],
+                                         self.time_slice, **kw)
+            for a, m in zip(members, ran):
+                a.done += int(m)
+                total += int(m)
+        else:
+            moves = [min(self._share(a), a.job.moves - a.done) for a in members]
+            cycles = self.backend.run([a.handle for a in members], moves, **kw)
+            for i, (a, m) in enumerate(zip(members, moves)):
+                a.done += m
+                total += m
+                if cycles is not None and m > 0 and cycles[i] > 0:
+                    c = float(cycles[i]) / m
+                    a.cycles_per_move = c if a.cycles_per_move == 0.0 else 0.5 * (a.cycles_per_move + c)
         self.moves_done += total
         self.rounds += 1
         self._retire()

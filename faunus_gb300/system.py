@@ -388,11 +388,14 @@ class Context:
                   n_swap_blocks: int = 0, temperatures=None, threads: int = 0, streams=None,
                   counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None,
                   sampler: Optional["Sampler"] = None, sample_slots=None, sample_interval: int = 0,
-                  n_sample_blocks: int = 0) -> dict:
+                  n_sample_blocks: int = 0, time_budget_s: Optional[float] = None, moves_out=None) -> dict:
         """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
         is a uint64 array of len(systems) that receives each system's SM cycles.  With a
         sampler, the systems are sampled on the device after every block of moves (the PT
-        swap blocks, or n_sample_blocks blocks of sample_interval moves, or once at the end)."""
+        swap blocks, or n_sample_blocks blocks of sample_interval moves, or once at the end).
+        time_budget_s: each chain ends at the first move boundary after that much time of its
+        own (or after its move count); moves_out (int64, one entry a system) receives the
+        moves each performed -- continue a chain at counter + moves done."""
         n = len(systems)
         arr = (C.c_void_p * n)(*[s.handle for s in systems])
         p = A.BatchParams()
@@ -438,6 +441,14 @@ class Context:
                 sl = np.ascontiguousarray(sample_slots, dtype=np.int32)
                 keep.append(sl)
                 p.sample_slots = A.as_iptr(sl)
+        if time_budget_s is not None:
+            if not time_budget_s > 0:
+                raise ValueError("time_budget_s must be positive")
+            p.time_budget_ns = int(time_budget_s * 1e9)
+        if moves_out is not None:
+            if moves_out.dtype != np.int64 or not moves_out.flags.c_contiguous or len(moves_out) != n:
+                raise ValueError("moves_out must be a contiguous int64 array with one entry per system")
+            p.moves_out = moves_out.ctypes.data_as(C.POINTER(C.c_int64))
         st = A.BatchStats()
         A.check(self._lib.fau_run_batch(self.handle, arr, n, C.byref(p), C.byref(st)), "fau_run_batch")
         return st.as_dict()

@@ -229,6 +229,11 @@ typedef struct fau_batch_params {
     int sample_interval_moves; /* with a sampler and no PT: blocks of this many moves per
                                  system; under PT the swap blocks are the sample blocks   */
     int n_sample_blocks;      /* number of sample blocks (no PT)                          */
+    uint64_t time_budget_ns;  /* > 0 (no PT, no sampler): each system's chain ends at the first
+                                 move boundary after this many ns of its own, or after its
+                                 move count; a chain split this way continues exactly as one
+                                 launch would (resume it at counter + moves done)        */
+    int64_t* moves_out;       /* optional, n entries: moves (proposals) each system performed */
 } fau_batch_params;
 
 typedef struct fau_batch_stats {

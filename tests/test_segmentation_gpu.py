@@ -35,3 +35,29 @@ def test_launch_segmentation_is_invisible(ctx, case):
     assert np.array_equal(a.mass_centers(), b.mass_centers())
     assert a.running_energy() == b.running_energy()
     assert np.array_equal(a.q(), b.q())  # fau_get_q folds the pending changes the same way for both
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_time_budgeted_launches_are_invisible(ctx, name):
+    """Launches cut short by a device-time budget continue exactly where they stopped:
+    repeated until done, they end bit-identical to one launch; moves_out reports each
+    system's moves."""
+    make, kw = CASES[name]
+    spec = make()
+    a, b = ctx.create(spec), ctx.create(spec)
+    ctx.run_batch([a], 3000, seed=9, **kw)
+    done, launches = 0, 0
+    while done < 3000:
+        out = np.zeros(1, np.int64)
+        ctx.run_batch([b], moves_per_system=[3000 - done], seed=9, counters=[done], time_budget_s=2e-4,
+                      moves_out=out, **kw)
+        assert 1 <= out[0] <= 3000 - done
+        done += int(out[0])
+        launches += 1
+    assert launches > 1 and done == 3000
+    assert np.array_equal(a.positions(), b.positions())
+    assert a.running_energy() == b.running_energy()
+    assert np.array_equal(a.q(), b.q())
+    out = np.zeros(1, np.int64)
+    ctx.run_batch([b], 500, seed=9, counter_base=3000, moves_out=out, **kw)
+    assert out[0] == 500

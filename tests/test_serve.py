@@ -57,6 +57,21 @@ class FakeBackend:
         self.clock.t += self.spm * max(c / 1000 for c in cyc)  # the launch lasts as long as its slowest chain
         return np.array(cyc, dtype=np.uint64)
 
+    def run_timed(self, handles, moves, time_budget_s, *, seed, streams, counters, dp, dprot):
+        """each chain runs moves of cpm cycles at 1 GHz until its time is spent (at least one)"""
+        done = []
+        for h, m, st, c in zip(handles, moves, streams, counters):
+            per = h.spec.get("cpm", 1000) * 1e-9
+            k = min(m, max(1, int(time_budget_s / per + 1e-9))) if m > 0 else 0
+            for j in range(c, c + k):
+                h.state = (h.state * 6364136223846793005 + (seed ^ (st << 20) ^ j)) & (2**64 - 1)
+            h.moves += k
+            done.append(k)
+        self.launches.append(sorted(streams))
+        self.moves_per_launch.append(dict(zip(streams, done)))
+        self.clock.t += max(k * h.spec.get("cpm", 1000) * 1e-9 for k, h in zip(done, handles))
+        return np.array(done, dtype=np.int64)
+
     def result(self, h, with_positions):
         return {"energy": float(h.state % 1000003), "accepted": h.moves // 2, "moves": h.moves,
                 "positions": None}
@@ -142,6 +157,23 @@ def test_duplicate_ids_and_bad_budget_are_rejected():
         srv.submit(Job(spec={"bytes": 1}, moves=1, id=7))
     with pytest.raises(ValueError):
         Server(FakeBackend(FakeClock()), hbm_budget=0)
+
+
+def test_time_slices_same_result_and_no_chain_waits():
+    """In time-slice rounds each chain runs for the slice (a slow job does fewer moves per
+    round, never holding fast ones back); results equal those of the cycle-share rounds."""
+    jobs = lambda: [Job(spec={"bytes": 1, "cpm": 1000}, moves=40000, id=0),
+                    Job(spec={"bytes": 1, "cpm": 4000}, moves=10000, id=1),
+                    Job(spec={"bytes": 1, "cpm": 2000}, moves=7, id=2)]
+    a, _, _ = _server(budget=100, slots=4, block=500, round_cycles=4e6)
+    a.run(jobs())
+    b, be, _ = _server(budget=100, slots=4, time_slice_s=4e-3)
+    b.run(jobs())
+    assert be.moves_per_launch[0] == {0: 4000, 1: 1000, 2: 7}
+    for i in range(3):
+        assert a.results[i].energy == b.results[i].energy and b.results[i].moves == a.results[i].moves
+    with pytest.raises(ValueError):
+        _server(time_slice_s=0.0)
 
 
 def test_round_shares_follow_measured_cycles_per_move():

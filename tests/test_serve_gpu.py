@@ -2,10 +2,10 @@
 alone and in a mix of jobs that join and leave around it -- the same moves
 (device RNG keyed by job id and move counter), bit-identical positions,
 acceptance counts and running energy, although the server sizes each job's share
-of a round from measured cycles so launch boundaries differ between the runs
-(pending Q(k) changes and partial energy sums stay on the device across launches);
-p50/p99 latency and throughput are reported; an over-size job is rejected without
-disturbing the others."""
+of a round from measured cycles (or from device time, in time-slice rounds) so
+launch boundaries differ between the runs (pending Q(k) changes and partial
+energy sums stay on the device across launches); p50/p99 latency and throughput
+are reported; an over-size job is rejected without disturbing the others."""
 import numpy as np
 import pytest
 
@@ -26,17 +26,21 @@ def _job(kind, jid, moves, arrival=0.0):
     return Job(spec=spec, moves=moves, id=jid, dp=dp, dprot=dprot, arrival_s=arrival)
 
 
-@pytest.mark.parametrize("kind", ["pm", "bulk", "water"])
-def test_served_job_same_alone_and_in_mix(ctx, kind):
+@pytest.mark.parametrize("kind,slice_s", [("pm", None), ("bulk", None), ("water", None), ("pm", 2e-4),
+                                          ("bulk", 1e-4), ("water", 5e-4)])
+def test_served_job_same_alone_and_in_mix(ctx, kind, slice_s):
     budget = 2 << 30
     alone = Server(GpuBackend(ctx), hbm_budget=budget, block_moves=1500, seed=9, keep_positions=True)
     alone.run([_job(kind, 17, 6000)])
-    mix = Server(GpuBackend(ctx), hbm_budget=budget, block_moves=1500, seed=9, keep_positions=True)
+    mix = Server(GpuBackend(ctx), hbm_budget=budget, block_moves=1500, seed=9, keep_positions=True,
+                 time_slice_s=slice_s)
     others = [_job("pm", 3, 2500), _job("bulk", 4, 9000), _job("water", 5, 4000, arrival=0.0),
               _job("bulk", 6, 3000, arrival=0.002)]
     mix.run(others[:2] + [_job(kind, 17, 6000)] + others[2:])
     a, b = alone.results[17], mix.results[17]
     assert a.status == b.status == "done" and a.moves == b.moves == 6000
+    if slice_s:
+        assert mix.rounds > 2  # the job took several time slices
     assert np.array_equal(a.positions, b.positions)
     assert a.accepted == b.accepted
     assert a.energy == b.energy
