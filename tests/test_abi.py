@@ -61,6 +61,7 @@ int main(void) {
   O(fau_batch_params, sampler) O(fau_batch_params, n_sample_blocks) O(fau_move_desc, volume_method)
   O(fau_sampler_desc, rdf_dr) O(fau_sampler_desc, energy) S(fau_spline_opts)
   O(fau_sys_desc, spline_begin) O(fau_sys_desc, spline_hs) O(fau_spline_opts, hardsphere)
+  O(fau_batch_params, time_budget_ns) O(fau_batch_params, moves_out)
   return 0;
 }
 """
@@ -91,7 +92,9 @@ def test_struct_layouts_match_header(tmp_path):
             "fau_sampler_desc.rdf_dr": A.SamplerDesc.rdf_dr.offset, "fau_sampler_desc.energy": A.SamplerDesc.energy.offset,
             "fau_sys_desc.spline_begin": A.SysDesc.spline_begin.offset,
             "fau_sys_desc.spline_hs": A.SysDesc.spline_hs.offset,
-            "fau_spline_opts.hardsphere": A.SplineOpts.hardsphere.offset}
+            "fau_spline_opts.hardsphere": A.SplineOpts.hardsphere.offset,
+            "fau_batch_params.time_budget_ns": A.BatchParams.time_budget_ns.offset,
+            "fau_batch_params.moves_out": A.BatchParams.moves_out.offset}
     for k, v in offs.items():
         assert int(out[k]) == v, k
 
