@@ -403,6 +403,7 @@ size_t footprint_bytes(const fau_sys_desc* d, const Layout& lay, int cap)
     b += (size_t)lay.K * (4 + 4 + 8 + 16 + 16 + 8 + 8);
     b += sizeof(PlainMove) + 64 + sizeof(void*);
     if (d->cutoff_g2g_pairs && d->n_molids > 0) b += g * 4 + (size_t)d->n_molids * d->n_molids * (8 + 4);
+    b += g * 64; // mass-centre cells of molecular groups (at most ~16 slots a group in practice)
     if (d->pair_terms & FAU_PAIR_SPLINE) { // every class pair a copy of its atom-type pair's table
         size_t most = 0;
         const size_t T = d->n_types;
@@ -688,6 +689,70 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         h.n_mol = d->n_molids;
     }
     h.cut_g2g2f = (float)h.cut_g2g2;
+    // mass-centre cells of the molecular groups: as wide as the largest cutoff between molecule
+    // kinds that have molecular groups (+1e-9), when every such pair has one and some axis holds
+    // more than three; the molecular kernel lists them at its start and keeps them current
+    std::vector<int> gc_cnt0;
+    if (!s->all_atomic) {
+        std::vector<char> used(std::max(1, h.n_mol), 0);
+        for (int g = 0; g < d->n_groups; g++)
+            if (!(d->group_flags ? (d->group_flags[g] & FAU_GROUP_ATOMIC) : 1)) used[h.n_mol > 0 ? g_molid[g] : 0] = 1;
+        double rc2 = -1.0;
+        bool finite = true;
+        if (h.n_mol > 0) {
+            for (int a = 0; a < h.n_mol; a++)
+                for (int b = 0; b < h.n_mol; b++) {
+                    if (!used[a] || !used[b]) continue;
+                    const double c2 = cut2_mol[(size_t)a * h.n_mol + b];
+                    if (c2 < 0.0) finite = false;
+                    rc2 = std::max(rc2, c2);
+                }
+        }
+        else {
+            finite = h.cut_g2g2 >= 0.0;
+            rc2 = h.cut_g2g2;
+        }
+        if (finite && rc2 > 0.0) {
+            const double rc = std::sqrt(rc2) * (1.0 + 1e-9);
+            int gd[3];
+            long tot = 1;
+            bool wide = true;
+            for (int k = 0; k < 3; k++) {
+                gd[k] = (int)std::floor(d->box[k] / rc);
+                wide = wide && gd[k] >= 3;
+                tot *= std::max(gd[k], 1);
+            }
+            if (wide && tot > 27 && tot <= (1L << 20)) {
+                std::vector<int> cnt(tot, 0);
+                int nmol = 0;
+                for (int g = 0; g < d->n_groups; g++) {
+                    if (d->group_flags ? (d->group_flags[g] & FAU_GROUP_ATOMIC) : 1) continue;
+                    int c[3];
+                    for (int k = 0; k < 3; k++) {
+                        int v = (int)std::floor((cm[3 * g + k] + 0.5 * d->box[k]) * (gd[k] / d->box[k]));
+                        c[k] = std::min(std::max(v, 0), gd[k] - 1);
+                    }
+                    cnt[c[0] + gd[0] * (c[1] + gd[1] * c[2])]++;
+                    nmol++;
+                }
+                const int maxc = *std::max_element(cnt.begin(), cnt.end());
+                const int want = std::max(64, std::max(2 * maxc, 4 * (int)std::ceil(nmol / (double)tot)));
+                int cap = 32, sh = 5;
+                while (cap < want) {
+                    cap *= 2;
+                    sh++;
+                }
+                for (int k = 0; k < 3; k++) {
+                    h.gdim[k] = gd[k];
+                    h.ginv[k] = gd[k] / d->box[k];
+                }
+                h.gncell = (int)tot;
+                h.gcap = cap;
+                h.gshift = sh;
+                gc_cnt0.assign(tot, 0);
+            }
+        }
+    }
     for (size_t a = 0; a < lay.itype_type.size() && a < (size_t)kMaxITypes; a++) h.itype_type[a] = lay.itype_type[a];
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0);
@@ -717,6 +782,11 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     if (!molecular_only && (int)atomic_idx.size() == n) h.n_atomic = 0; // all atomic: index = particle
     UP(h.pair, pf);
     UP(h.pair_d, pd);
+    if (h.gncell > 0) { // contents listed by the molecular kernel at its start
+        std::vector<int> lst((size_t)h.gncell * h.gcap, 0);
+        UP(h.gc_cnt, gc_cnt0);
+        UP(h.gc_list, lst);
+    }
     if (d->pair_terms & FAU_PAIR_SPLINE) { // nonbonded_splined: the atom-type pair tables per class pair
         std::vector<SplineP> spl(nt * nt);
         std::vector<float> zf, cf;
@@ -904,6 +974,7 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
     fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf); fix(h.qpend); fix(h.qdlt);
     fix(h.spl); fix(h.spl_zf); fix(h.spl_zd); fix(h.spl_cf); fix(h.spl_cd); fix(h.spl_grid);
+    fix(h.gc_cnt); fix(h.gc_list);
     fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
     fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
     fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);

@@ -99,6 +99,13 @@ struct DevSys {
     int* g_molid;     // n_groups molecule kinds (n_mol > 0 only)
     double* cut2_mol; // n_mol^2 cutoffs^2 (FP64); < 0: no cutoff for that pair
     float* cut2_molf; // FP32 copies
+    // mass-centre cells of the molecular groups (the molecular kernel's GroupCutoff candidates),
+    // at least as wide as the largest group cutoff; rebuilt at each launch of that kernel
+    int gdim[3], gncell;  // gncell 0: every group is a candidate
+    int gcap, gshift;     // slots a cell (a power of two >= 32) and its log2
+    double ginv[3];       // cells per unit length
+    int* gc_cnt;          // gncell counts
+    int* gc_list;         // gncell * gcap group indices, ascending within a cell
     PairF* pair;      // nt*nt
     double* pair_d;   // nt*nt*4 FP64 copies (s2, e4, hs2, qq)
     // FAU_PAIR_SPLINE: tables per class pair (nt*nt SplineP), knots and coefficients

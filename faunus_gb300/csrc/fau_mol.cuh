@@ -74,8 +74,91 @@ __device__ __forceinline__ bool mol_task_fast(const DevSys& S, const PairF* pt, 
     return true;
 }
 
-template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
+// mass-centre cell of an FP64 mass centre: floor((x + L/2) / side), clamped to the grid
+__device__ __forceinline__ int gcell_of(const DevSys& S, const double* x, int* c3)
+{
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int v = (int)floor(__dmul_rn(__dadd_rn(x[d], S.half[d]), S.ginv[d]));
+        c3[d] = min(max(v, 0), S.gdim[d] - 1);
+    }
+    return c3[0] + S.gdim[0] * (c3[1] + S.gdim[1] * c3[2]);
+}
+
+// The cells whose groups are GroupCutoff candidates of one molecular move: every cell within
+// one of the moved group's old or new cell (a box of at most 4 x 4 x 4 for a move shorter than
+// a cell); n = -1 for a longer move (every group is a candidate) or without cells.
+template <bool B>
+struct ByCell { // compile-time choice of the candidate enumeration (separate code for each)
+    static constexpr bool value = B;
+};
+
+struct GBox {
+    int n, c_old, c_new, pad;
+    int cells[64];
+};
+
+__device__ __forceinline__ void gbox_prepare(const DevSys& S, const MoveShared& ms, GBox& b, int lane)
+{
+    if (S.gncell == 0 || ms.kind != FAU_MOVE_MOLECULAR || ms.stop) {
+        if (lane == 0) b.n = -1;
+        return;
+    }
+    int co[3], cn[3], start[3], span[3];
+    const int c_old = gcell_of(S, S.g_cm + 3 * ms.index, co);
+    const int c_new = gcell_of(S, ms.cm_new, cn);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int G = S.gdim[d];
+        int dd = cn[d] - co[d]; // minimum-image cell offset
+        if (2 * dd > G) dd -= G;
+        else if (2 * dd < -G) dd += G;
+        const int lo = min(0, dd) - 1, hi = max(0, dd) + 1;
+        span[d] = hi - lo + 1;
+        start[d] = co[d] + lo;
+        if (span[d] >= G) {
+            span[d] = G;
+            start[d] = 0;
+        }
+    }
+    const int n = span[0] * span[1] * span[2];
+    for (int e = lane; e < 64 && e < n; e += 32) {
+        const int ex = e % span[0], ey = (e / span[0]) % span[1], ez = e / (span[0] * span[1]);
+        int w[3] = {start[0] + ex, start[1] + ey, start[2] + ez};
+#pragma unroll
+        for (int d = 0; d < 3; d++) w[d] = (w[d] % S.gdim[d] + S.gdim[d]) % S.gdim[d];
+        b.cells[e] = w[0] + S.gdim[0] * (w[1] + S.gdim[1] * w[2]);
+    }
+    if (lane == 0) {
+        b.n = n <= 64 ? n : -1;
+        b.c_old = c_old;
+        b.c_new = c_new;
+    }
+}
+
+// the kernel's static shared memory, declared once for both instances of its body
+template <int NT>
+struct __align__(16) MolShared {
+    static constexpr int NW = NT / 32, NWC = NW - 1, CH = 6 * (NT - 32);
+    DevSys Ssh;
+    PairF pt[kMaxITypes * kMaxITypes];
+    MoveShared msb[2];
+    FF red_a[NW];
+    int red_f[NW];
+    uint32_t nbl[CH];   // neighbour group | interacting states
+    uint32_t nbl_b[CH]; // its first particle | atom count << 24
+    int nbl_wcnt[2][NWC]; // survivors per compute warp: single pass | current chunk
+    int sh_prev_accept, sh_stop, sh_time_up, pad;
+    GBox gbx[2];        // the candidate cells of moves mv (gbx[mv & 1]) and mv + 1
+    unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
+    long long sh_consumed;
+    unsigned long long red_u[NW][2];
+};
+
+// CELLS: the system has mass-centre cells (its GroupCutoff candidates come from them); the
+// body is compiled for each case, so systems without cells run exactly the code they had
+template <int NT, bool CELLS>
+__device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>& sm)
 {
     constexpr int NW = NT / 32;
     constexpr int NWC = NW - 1;   // compute warps
@@ -84,11 +167,12 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     constexpr int CH = RC * NTC;  // covers a 1,000-molecule system, one barrier pair per move)
     constexpr int SB = 2;         // candidates whose loads are in flight together (RC % SB == 0)
     constexpr int SEG = RC * 32;  // list slots of one compute warp (its candidates in one chunk)
+    static_assert(CH == MolShared<NT>::CH, "list size");
     const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ctid = tid - 32; // compute-thread index (warps 1..)
     DevSys& G = *A.sys[blockIdx.x];
-    __shared__ __align__(16) DevSys Ssh;
+    DevSys& Ssh = sm.Ssh;
     for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += NT)
         reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
     __syncthreads();
@@ -105,16 +189,19 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
     float2* tabs = reinterpret_cast<float2*>(Af + K); // two sets of kTableAtoms * 6 * TS phase tables
     const int tab_len = kTableAtoms * 6 * TS;
 
-    __shared__ PairF pt[kMaxITypes * kMaxITypes];
-    __shared__ MoveShared msb[2];
-    __shared__ FF red_a[NW];
-    __shared__ int red_f[NW];
-    __shared__ uint32_t nbl[CH];   // neighbour group | interacting states
-    __shared__ uint32_t nbl_b[CH]; // its first particle | atom count << 24
-    __shared__ int nbl_wcnt[2][NWC]; // survivors per compute warp: single pass | current chunk
-    __shared__ int sh_prev_accept, sh_stop, sh_time_up;
-    __shared__ unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
-    __shared__ long long sh_consumed;
+    auto& pt = sm.pt;
+    auto& msb = sm.msb;
+    auto& red_a = sm.red_a;
+    auto& red_f = sm.red_f;
+    auto& nbl = sm.nbl;
+    auto& nbl_b = sm.nbl_b;
+    auto& nbl_wcnt = sm.nbl_wcnt;
+    int& sh_prev_accept = sm.sh_prev_accept;
+    int& sh_stop = sm.sh_stop;
+    int& sh_time_up = sm.sh_time_up;
+    auto& gbx = sm.gbx;
+    unsigned long long& sh_t0 = sm.sh_t0;
+    long long& sh_consumed = sm.sh_consumed;
 
     const float rec_pref_f = (float)S.rec_pref;
     for (int k = tid; k < K; k += NT) {
@@ -161,10 +248,46 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         sh_time_up = 0;
         sh_t0 = global_ns();
     }
+    if constexpr (CELLS) {
+        // list the molecular groups by mass-centre cell, ascending within each cell (the lists
+        // depend only on the mass centres: a chain split into launches sees the same ones)
+        for (int c = tid; c < S.gncell; c += NT) S.gc_cnt[c] = 0;
+        __syncthreads();
+        for (int h = tid; h < S.n_groups; h += NT) {
+            if (S.g_flags[h] & FAU_GROUP_ATOMIC) continue;
+            int c3[3];
+            const int c = gcell_of(S, S.g_cm + 3 * h, c3);
+            const int slot = atomicAdd(&S.gc_cnt[c], 1);
+            if (slot < S.gcap) S.gc_list[(size_t)c * S.gcap + slot] = h;
+        }
+        __syncthreads();
+        for (int c = tid; c < S.gncell; c += NT) {
+            const int n = S.gc_cnt[c];
+            if (n > S.gcap) {
+                sh_stop = FAU_ERR_CAPACITY; // no move runs: the caller sees the capacity error
+                sh_consumed = 0;
+                continue;
+            }
+            int* l = S.gc_list + (size_t)c * S.gcap;
+            for (int i = 1; i < n; i++) { // insertion sort of a few dozen indices
+                const int v = l[i];
+                int j = i - 1;
+                while (j >= 0 && l[j] > v) {
+                    l[j + 1] = l[j];
+                    j--;
+                }
+                l[j + 1] = v;
+            }
+        }
+    }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
         const Proposal p = philox_proposal(S, ctr0, sys_id, A.seed, dp_f, dprot, true);
         prepare_move(S, msb[0], p, lane, K ? tabs : nullptr, nc);
+        if constexpr (CELLS) {
+            __syncwarp();
+            gbox_prepare(S, msb[0], gbx[0], lane);
+        }
     }
     __syncthreads();
 
@@ -189,6 +312,10 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                     philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
                 tick(13);
                 prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc, timing ? &tacc[14] : nullptr);
+                if constexpr (CELLS) {
+                    __syncwarp();
+                    gbox_prepare(S, mn, gbx[cur ^ 1], lane);
+                }
             }
             tick(6);
         }
@@ -264,26 +391,79 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 const double cmo_d[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
                 const int GN = S.n_groups;
                 const int mol_g = S.n_mol > 0 ? S.g_molid[g] : 0;
+                // The candidates: every group, or (mass-centre cells) the groups listed in the
+                // move's candidate cells, in rounds of 32 slots of one cell.  Each warp holds the
+                // cells' counts and the first round of each (lanes e and e + 32 for cell e).
+                const GBox& gb = gbx[cur];
+                const bool by_cell = CELLS && gb.n > 0;
+                struct CellRounds {
+                    int cnt_lo, cnt_hi, ex_lo, ex_hi, rounds;
+                };
+                auto cell_rounds = [&]() {
+                    CellRounds c{0, 0, 0, 0, 0};
+                    if (lane < gb.n) c.cnt_lo = min(S.gc_cnt[gb.cells[lane]], S.gcap);
+                    if (lane + 32 < gb.n) c.cnt_hi = min(S.gc_cnt[gb.cells[lane + 32]], S.gcap);
+                    const int r_lo = (c.cnt_lo + 31) >> 5, r_hi = (c.cnt_hi + 31) >> 5;
+                    int in_lo = r_lo, in_hi = r_hi;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int a = __shfl_up_sync(0xffffffffu, in_lo, o), b = __shfl_up_sync(0xffffffffu, in_hi, o);
+                        if (lane >= o) {
+                            in_lo += a;
+                            in_hi += b;
+                        }
+                    }
+                    in_hi += __shfl_sync(0xffffffffu, in_lo, 31);
+                    c.ex_lo = in_lo - r_lo;
+                    c.ex_hi = in_hi - r_hi;
+                    c.rounds = __shfl_sync(0xffffffffu, in_hi, 31);
+                    return c;
+                };
+                // candidate q (q >> 5 is the same in a whole warp): its group, or -1
+                auto cand = [&](auto cells, const CellRounds& c, int q) -> int {
+                    if constexpr (!decltype(cells)::value) {
+                        return q < GN ? q : -1;
+                    }
+                    else {
+                        const int u = q >> 5;
+                        if (u >= c.rounds) return -1;
+                        const int e = __popc(__ballot_sync(0xffffffffu, lane < gb.n && c.ex_lo <= u)) +
+                                      __popc(__ballot_sync(0xffffffffu, lane + 32 < gb.n && c.ex_hi <= u)) - 1;
+                        int first, cnt;
+                        if (e < 32) {
+                            first = __shfl_sync(0xffffffffu, c.ex_lo, e);
+                            cnt = __shfl_sync(0xffffffffu, c.cnt_lo, e);
+                        }
+                        else {
+                            first = __shfl_sync(0xffffffffu, c.ex_hi, e - 32);
+                            cnt = __shfl_sync(0xffffffffu, c.cnt_hi, e - 32);
+                        }
+                        const int slot = ((u - first) << 5) + lane;
+                        return slot < cnt ? S.gc_list[(size_t)gb.cells[e] * S.gcap + slot] : -1;
+                    }
+                };
                 // GroupCutoff tests of SB candidates per thread starting at `base`; the survivors
                 // are counted in the warp's wc and listed in the warp's own segment (nbl_slot),
                 // up to SEG of them, with the states they interact in and their particle extents
-                auto compact = [&](int base, int& wc) {
-                    int gfl[SB], gml[SB], gb0[SB], gb1[SB];
+                auto compact = [&](auto cells, const CellRounds& c, int base, int& wc) {
+                    int hh[SB], gfl[SB], gml[SB], gb0[SB], gb1[SB];
                     uint4 gcr[SB];
 #pragma unroll
+                    for (int r = 0; r < SB; r++) hh[r] = cand(cells, c, base + r * NTC + ctid);
+#pragma unroll
                     for (int r = 0; r < SB; r++) { // all loads first: their latencies overlap
-                        const int h = base + r * NTC + ctid;
-                        gfl[r] = h < GN ? S.g_flags[h] : FAU_GROUP_ATOMIC;
-                        gcr[r] = h < GN ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
-                        gml[r] = (h < GN && S.n_mol > 0) ? S.g_molid[h] : 0;
-                        gb0[r] = h < GN ? S.g_begin[h] : 0;
-                        gb1[r] = h < GN ? S.g_begin[h + 1] : 0;
+                        const int h = hh[r];
+                        gfl[r] = h >= 0 ? S.g_flags[h] : FAU_GROUP_ATOMIC;
+                        gcr[r] = h >= 0 ? S.g_cmrec[h] : make_uint4(0, 0, 0, 0);
+                        gml[r] = (h >= 0 && S.n_mol > 0) ? S.g_molid[h] : 0;
+                        gb0[r] = h >= 0 ? S.g_begin[h] : 0;
+                        gb1[r] = h >= 0 ? S.g_begin[h + 1] : 0;
                     }
 #pragma unroll
                     for (int r = 0; r < SB; r++) {
-                        const int h = base + r * NTC + ctid;
+                        const int h = hh[r];
                         uint32_t e = 0;
-                        if (h < GN && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
+                        if (h >= 0 && h != g && !(gfl[r] & FAU_GROUP_ATOMIC)) {
                             double c2 = S.cut_g2g2;
                             float c2f = S.cut_g2g2f;
                             if (S.n_mol > 0) {
@@ -356,7 +536,14 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 bool over;
                 {
                     int wc = 0;
-                    for (int base = 0; base < GN; base += SB * NTC) compact(base, wc);
+                    if (by_cell) {
+                        const CellRounds c = cell_rounds();
+                        for (int base = 0; base < c.rounds * 32; base += SB * NTC) compact(ByCell<true>{}, c, base, wc);
+                    }
+                    else {
+                        const CellRounds c{0, 0, 0, 0, 0};
+                        for (int base = 0; base < GN; base += SB * NTC) compact(ByCell<false>{}, c, base, wc);
+                    }
                     if (lane == 0) nbl_wcnt[0][warp - 1] = wc;
                 }
                 compute_barrier(NTC);
@@ -370,11 +557,14 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 else { // more survivors than a segment holds (long or no cutoff): chunks of CH
                        // candidates, SEG of them per warp (the single-pass counts stay untouched:
                        // every warp has read them to take this branch)
-                    for (int base = 0; base < GN; base += CH) {
+                    const CellRounds c = by_cell ? cell_rounds() : CellRounds{0, 0, 0, 0, 0};
+                    const int n_cand = by_cell ? c.rounds * 32 : GN;
+                    for (int base = 0; base < n_cand; base += CH) {
                         int wc = 0;
                         for (int r0 = 0; r0 < RC; r0 += SB) {
-                            if (base + r0 * NTC >= GN) break; // uniform: the ballots stay full-warp
-                            compact(base + r0 * NTC, wc);
+                            if (base + r0 * NTC >= n_cand) break; // uniform: the ballots stay full-warp
+                            if (by_cell) compact(ByCell<true>{}, c, base + r0 * NTC, wc);
+                            else compact(ByCell<false>{}, c, base + r0 * NTC, wc);
                         }
                         if (lane == 0) nbl_wcnt[1][warp - 1] = wc;
                         compute_barrier(NTC);
@@ -427,7 +617,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 accp = ff_sum(accp, ta);
                 flags |= __shfl_xor_sync(0xffffffffu, flags, o);
             }
-            int accept = 0, stop = 0;
+            int accept = 0, stop = 0, cell_full = 0;
             if (lane == 0 && kind != FAU_MOVE_NONE) {
                 double du_surf = 0.0;
                 if (S.flags & SYS_SURFACE) {
@@ -472,6 +662,29 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
 #pragma unroll
                     for (int d = 0; d < 3; d++) S.g_cm[3 * g + d] = ms.cm_new[d];
                     S.g_cmrec[g] = ms.cmrec_new;
+                    const GBox& gb = gbx[cur];
+                    if (CELLS && gb.c_old != gb.c_new) { // the group changes mass-centre cell
+                        int* lo = S.gc_list + (size_t)gb.c_old * S.gcap;
+                        const int no = min(S.gc_cnt[gb.c_old], S.gcap);
+                        int i = 0;
+                        while (i < no && lo[i] != g) i++;
+                        for (; i + 1 < no; i++) lo[i] = lo[i + 1];
+                        S.gc_cnt[gb.c_old] = no - 1;
+                        int* ln = S.gc_list + (size_t)gb.c_new * S.gcap;
+                        const int nn = S.gc_cnt[gb.c_new];
+                        if (nn >= S.gcap) {
+                            cell_full = 1; // listed nowhere until the next launch lists every group again
+                        }
+                        else {
+                            int j = nn;
+                            while (j > 0 && ln[j - 1] > g) {
+                                ln[j] = ln[j - 1];
+                                j--;
+                            }
+                            ln[j] = g;
+                            S.gc_cnt[gb.c_new] = nn + 1;
+                        }
+                    }
                 }
                 __syncwarp();
                 __threadfence_block();
@@ -481,6 +694,10 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                     const Proposal p =
                         philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
                     prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);
+                    if constexpr (CELLS) {
+                        __syncwarp();
+                        gbox_prepare(S, mn, gbx[cur ^ 1], lane);
+                    }
                 }
             }
             if (lane == 0) {
@@ -488,6 +705,10 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
                 if (stop) {
                     sh_stop = stop;
                     sh_consumed = mv;
+                }
+                else if (cell_full) { // this move is committed; the chain ends after it
+                    sh_stop = FAU_ERR_CAPACITY;
+                    sh_consumed = mv + 1;
                 }
                 if (A.time_budget_ns && global_ns() - sh_t0 >= A.time_budget_ns) sh_time_up = 1;
             }
@@ -509,7 +730,7 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         S.qdlt[k] = dlt[k];
     }
     if (tid == 32) G.q_since = K ? since_flush : 0;
-    __shared__ unsigned long long red_u[NW][2];
+    auto& red_u = sm.red_u;
     unsigned long long a = n_pairs, b = n_k;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -541,6 +762,14 @@ __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
         G.q_valid = K ? sh_prev_accept : 0;
         G.cycles += (unsigned long long)(clock64() - t_start);
     }
+}
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
+{
+    __shared__ MolShared<NT> sm;
+    if (A.sys[blockIdx.x]->gncell > 0) mol_chain_body<NT, true>(A, sm);
+    else mol_chain_body<NT, false>(A, sm);
 }
 
 // dynamic shared memory of the molecular kernel: the chain kernel's plus a second set of tables

@@ -1,6 +1,8 @@
 """GPU parity of the pipelined molecular-move kernel (fau_run_batch with the default
 kernel choice runs every molecular-move system in it; threads=256 forces the chain
-kernel).  Under the same device proposals both kernels must give the same chain --
+kernel; systems wide enough for more than 3 x 3 x 3 mass-centre cells of the largest
+group cutoff take their GroupCutoff candidates from those cells, the chain kernel from every
+group).  Under the same device proposals both kernels must give the same chain --
 the same accept count and bit-identical FP64 positions and mass centres -- barring a
 near tie (u between the two FP32C energy changes' exponentials); the running energy
 must agree with an FP64 recomputation; a batch mixing atomic systems (pipelined
@@ -21,7 +23,10 @@ CASES = {
     "water_surface": lambda: configs.spce_water(n_mol=256, L=18.6, seed=5, epss=1.0),
     "water_two_kinds": lambda: configs.spce_water(n_mol=512, L=24.8, seed=6, molecules=("M", "Q"),
                                                   cutoff_g2g={"default": 7.0, "M Q": 10.0}),
-    "water_4000": lambda: configs.spce_water(n_mol=4000, L=49.3, seed=12),            # one pass, G > list size
+    "water_4000": lambda: configs.spce_water(n_mol=4000, L=49.3, seed=12),            # mass-centre cells 4^3
+    "water_6666": lambda: configs.spce_water(n_mol=6666, L=58.5, seed=14),            # mass-centre cells 5^3
+    "water_4000_two_kinds": lambda: configs.spce_water(n_mol=4000, L=49.3, seed=15, molecules=("M", "Q"),
+                                                       cutoff_g2g={"default": 7.0, "M Q": 10.0}),
     "water_2000_no_cutoff": lambda: configs.spce_water(n_mol=2000, L=39.1, seed=13, cutoff_g2g=0.0),  # chunks
     "water_reaction_field": lambda: dataclasses.replace(
         configs.spce_water(n_mol=256, L=18.6, seed=7), ewald=None,
