@@ -30,6 +30,7 @@ extern "C" int fau_internal_fail(int code, const char* msg);
 extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
+extern "C" int fau_internal_sys_regrow(fau_sys* s);
 cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
                                         cudaStream_t st);
 int fau_internal_sampler_slots(const fau_sampler* s);
@@ -465,6 +466,17 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         // clear the device error flags so the systems stay usable
         for (int i = 0; i < n; i++) cudaMemsetAsync(&dsys[i]->err, 0, sizeof(int), st);
         cudaStreamSynchronize(st);
+        if (derr == FAU_ERR_CAPACITY) {
+            // a chain filled a cell: its move is committed and its chain stopped after it; the
+            // cells are regrown so that the caller can continue every system at counter + moves_out
+            for (int i = 0; i < n; i++)
+                if (s1[i].err == FAU_ERR_CAPACITY) {
+                    const int e = fau_internal_sys_regrow(systems[i]);
+                    if (e != FAU_OK) return e;
+                }
+            return fau_internal_fail(derr, "a cell list filled up: capacity doubled; continue the systems at "
+                                           "counter + moves_out");
+        }
         return fau_internal_fail(derr, "a system in the batch reported a device error");
     }
     return rc;

@@ -1741,6 +1741,27 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
+// after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
+// lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)
+int fau_internal_sys_regrow(fau_sys* s)
+{
+    int rc = FAU_OK;
+    if (s->cells && (rc = rebuild_cells(s, 2 * s->h.cap))) return rc;
+    if (s->h.gncell > 0) {
+        const int cap = 2 * s->h.gcap, sh = s->h.gshift + 1;
+        int* nl = nullptr;
+        if ((rc = dev_alloc(s, &nl, (size_t)s->h.gncell * cap))) return rc;
+        s->h.gc_list = nl;
+        s->h.gcap = cap;
+        s->h.gshift = sh;
+        cudaStream_t st = s->ctx->stream;
+        CUDA_TRY(cudaMemcpyAsync(&s->d->gc_list, &nl, sizeof(nl), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(&s->d->gcap, &cap, sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(&s->d->gshift, &sh, sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return FAU_OK;
+}
 
 // a context-owned device scratch buffer of at least `bytes` (grown on demand; valid until the
 // next call on this context -- batched calls synchronise their stream before returning)

@@ -37,6 +37,8 @@ from typing import Callable, Dict, List, Optional, Sequence
 
 import numpy as np
 
+from . import _capi as A
+from ._capi import FauError
 from .system import Context, SystemSpec, footprint
 
 
@@ -107,11 +109,17 @@ class GpuBackend:
         """Advance each system by up to its move count, each chain ending at the first move
         boundary after time_budget_s of its own (one launch); returns the moves each performed."""
         done = np.zeros(len(handles), dtype=np.int64)
-        self.ctx.run_batch(handles, moves_per_system=np.asarray(moves, dtype=np.int64), seed=seed,
-                           streams=np.asarray(streams, dtype=np.uint32),
-                           counters=np.asarray(counters, dtype=np.uint64), dp_per_system=dp,
-                           dprot_per_system=dprot, threads=self.threads, time_budget_s=time_budget_s,
-                           moves_out=done)
+        try:
+            self.ctx.run_batch(handles, moves_per_system=np.asarray(moves, dtype=np.int64), seed=seed,
+                               streams=np.asarray(streams, dtype=np.uint32),
+                               counters=np.asarray(counters, dtype=np.uint64), dp_per_system=dp,
+                               dprot_per_system=dprot, threads=self.threads, time_budget_s=time_budget_s,
+                               moves_out=done)
+        except FauError as e:
+            # a chain filled a cell list: the library doubled it; every chain's progress is in
+            # `done`, and the next round continues from there
+            if e.status != A.FAU_ERR_CAPACITY:
+                raise
         return done
 
     def result(self, handle, with_positions: bool) -> dict:

@@ -186,3 +186,27 @@ def test_round_shares_follow_measured_cycles_per_move():
     assert first == {0: 500, 1: 500}          # calibration
     assert second == {0: 4000, 1: 1000}       # 4e6 cycles each
     assert srv.results[0].moves == 40000 and srv.results[1].moves == 10000
+
+
+def test_gpu_backend_keeps_progress_when_a_cell_list_fills():
+    """fau_run_batch reports FAU_ERR_CAPACITY after doubling the full cell list; the moves each
+    chain made are in moves_out, so the time-sliced backend returns them and the next round
+    continues; other errors still raise."""
+    from faunus_gb300._capi import FAU_ERR_ARG, FAU_ERR_CAPACITY, FauError
+    from faunus_gb300.serve import GpuBackend
+
+    class Ctx:
+        def __init__(self, status):
+            self.status = status
+
+        def run_batch(self, handles, moves_per_system=None, moves_out=None, **kw):
+            moves_out[:] = np.minimum(moves_per_system, 7)
+            raise FauError(self.status, "fau_run_batch", "full cell")
+
+    be = GpuBackend(Ctx(FAU_ERR_CAPACITY))
+    done = be.run_timed([object(), object()], [100, 3], 0.01, seed=1, streams=[1, 2], counters=[0, 0],
+                        dp=[1.0, 1.0], dprot=[0.0, 0.0])
+    assert list(done) == [7, 3]
+    with pytest.raises(FauError):
+        GpuBackend(Ctx(FAU_ERR_ARG)).run_timed([object()], [5], 0.01, seed=1, streams=[1], counters=[0],
+                                                dp=[1.0], dprot=[0.0])

@@ -61,3 +61,48 @@ def test_served_stream_reports_latency_and_rejects_oversize(ctx):
     assert rep["p50_latency_s"] is not None and rep["p99_latency_s"] >= rep["p50_latency_s"] > 0
     assert rep["moves"] == sum(j.moves for j in jobs if j.id != 999)
     assert srv.resident == 0
+
+
+
+def test_batched_chain_continues_after_a_full_cell_list(ctx):
+    """fau_run_batch stops a chain that fills a cell after that move, doubles the cell list and
+    reports FAU_ERR_CAPACITY with every chain's progress in moves_out; continued from there the
+    chain ends exactly as one whose cells never fill (no interactions: every move accepted)."""
+    from faunus_gb300 import FauError, SystemSpec
+    from faunus_gb300 import _capi as A
+    L, c = 40.0, 40.0 / 3
+    centres = np.array([[(i + 0.5) * c - L / 2, (j + 0.5) * c - L / 2, (k + 0.5) * c - L / 2]
+                        for i in range(3) for j in range(3) for k in range(3)])
+    pos = np.concatenate([centres, centres[1:8] + 0.1])  # one per cell, 2 in cells 1..7: capacity 8
+    n = len(pos)
+
+    def make(cap):
+        return ctx.create(SystemSpec(box=np.full(3, L), pos=pos.copy(), charge=np.zeros(n),
+                                     type=np.zeros(n, np.int32), group_begin=np.array([0, n], np.int32),
+                                     group_flags=np.array([1], np.int32), n_types=1, pair_terms=0,
+                                     pair_cutoff=12.0, cell_capacity=cap))
+
+    a, b = make(1), make(64)
+    # fill cell (0,0,0) to its capacity of 8 with host proposals (no overflow yet)
+    props = np.zeros(7, dtype=A.PROPOSAL_DTYPE)
+    props["kind"] = A.FAU_MOVE_ATOMIC
+    props["index"] = np.arange(27, 34)
+    props["dr"] = centres[0] + 0.2 * np.arange(1, 8)[:, None] / 8 - pos[27:34]
+    props["u"] = 0.0
+    for s in (a, b):
+        s.run_proposals(props)
+        assert (s.cells() == 0).sum() == 8
+    total, done, fills = 4000, 0, 0
+    while done < total:
+        out = np.zeros(1, np.int64)
+        try:
+            ctx.run_batch([a], moves_per_system=[total - done], seed=2, counters=[done], dp=9.0, threads=160,
+                          moves_out=out)
+        except FauError as e:
+            assert e.status == A.FAU_ERR_CAPACITY
+            fills += 1
+        done += int(out[0])
+    ctx.run_batch([b], total, seed=2, dp=9.0, threads=160)
+    assert fills >= 1
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.cells(), b.cells())
