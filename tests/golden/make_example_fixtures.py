@@ -10,7 +10,11 @@ Reads, as data, from the Faunus tree given on the command line (default: /root/r
   examples/minimal: minimal.yml and minimal.out.json (SystemEnergy mean over its run, the
     statistical fixture) -> minimal_example.json;
   examples/langevin: montecarlo_lj.yml, montecarlo_lj.out.json and rdf_mc.dat (the AtomRDF
-    g(r) its MC run wrote) -> montecarlo_lj_example.json.
+    g(r) its MC run wrote) -> montecarlo_lj_example.json;
+  examples/cluster: cluster.yml (nonbonded_splined water; its molecule structure read from
+    water.xyz into the input, its cluster move and analyses other than SystemEnergy left out),
+    cluster.state.json (the state its run started from) and cluster.out.json (SystemEnergy at
+    that start, 2 decimals) -> cluster_example.json.
 
 The tests read only the written files.
 """
@@ -74,6 +78,35 @@ def main() -> None:
         "expected": {"rdf_samples": rdf["samples"], "dr": rdf["dr"], "nstep": rdf["nstep"], "moves": lmv["moves"],
                      "acceptance": lmv["acceptance"], "rdf": table},
     }))
+    cex = ROOT / "examples" / "cluster"
+    cinp = yason.loads((cex / "cluster.yml").read_text())
+    xyz = (cex / "water.xyz").read_text().split("\n")
+    natoms = int(xyz[0].split()[0])
+    structure = []
+    for line in xyz[2:2 + natoms]:
+        name, x, y, z = line.split()[:4]
+        structure.append({name: [float(x), float(y), float(z)]})
+    for item in cinp["moleculelist"]:
+        for name, props in item.items():
+            if props.get("structure") == "water.xyz":
+                props["structure"] = structure
+    cinp["moves"] = [m for m in cinp["moves"] if "moltransrot" in m]
+    cinp["analysis"] = [a for a in cinp["analysis"] if "systemenergy" in a]
+    cout = json.loads((cex / "cluster.out.json").read_text())
+    cstate = json.loads((cex / "cluster.state.json").read_text())
+    cse = next(a["systemenergy"] for a in cout["analysis"] if "systemenergy" in a)
+    cnb = cout["energy"][0]["hamiltonian"][0]["nonbonded"]
+    ccoul = next(p["coulomb"] for p in cnb["pairpot"] if "coulomb" in p)
+    (HERE / "cluster_example.json").write_text(json.dumps({
+        "provenance": {"input": "examples/cluster/cluster.yml (+ water.xyz; cluster move and other analyses "
+                                "left out)", "state": "examples/cluster/cluster.state.json",
+                       "output": "examples/cluster/cluster.out.json", "git revision": cout["git revision"],
+                       "compiler": cout["compiler"]},
+        "input": cinp,
+        "state": cstate,
+        "expected": {"bjerrum_length": ccoul["lB"], "systemenergy_init": cse["init"],
+                     "temperature": cout["temperature"]},
+    }, indent=1))
     np.savez_compressed(HERE / "bulk_example_state.npz",
                         id=np.array([p["id"] for p in parts], dtype=np.int32),
                         pos=np.array([p["pos"] for p in parts], dtype=np.float64),

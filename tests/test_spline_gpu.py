@@ -127,3 +127,24 @@ def test_molecular_kernel_water(ctx):
     _energy_consistent(a)
     # and the chain kernel against the oracle on host proposals
     _compare_chain(ctx.create(spec), spec, _props(spec, 1500), TOL_FP32C)
+
+
+@pytest.mark.parametrize("dp", [2.0, 20.0])
+def test_reference_cluster_example(ctx, dp):
+    """examples/cluster (ten splined waters in a 40 A box: 4 x 4 x 4 mass-centre cells of the
+    10 A group cutoff): device total equal to the oracle's; the molecular kernel (candidates
+    from the cells; dp 20 moves span more than a cell's neighbours, every group a candidate)
+    gives the chain kernel's chain."""
+    from test_spline import _cluster_example
+    spec, _ = _cluster_example()
+    g = ctx.create(spec)
+    eg, eo = g.energy_total(), O.OracleSystem(spec).energy_total()
+    for key in ("self", "nonbonded", "total"):
+        assert abs(eg[key] - eo[key]) <= 1e-9 * max(1.0, abs(eo[key])), key
+    a, b = ctx.create(spec), ctx.create(spec)
+    sa = ctx.run_batch([a], 4000, seed=5, dp=dp, dprot=1.0, threads=0)
+    sb = ctx.run_batch([b], 4000, seed=5, dp=dp, dprot=1.0, threads=256)
+    assert sa["accepted"] == sb["accepted"] > 100
+    assert np.array_equal(a.positions(), b.positions())
+    assert abs(a.running_energy() - b.running_energy()) <= 1e-9 * abs(b.running_energy())
+    _energy_consistent(a)
