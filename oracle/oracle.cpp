@@ -2,8 +2,8 @@
  * oracle.cpp -- TEST INFRASTRUCTURE ONLY.
  *
  * A CPU, FP64, IEEE (no fast-math, no FMA contraction) restatement of the
- * Faunus Metropolis Monte Carlo energy hot path.  It is the checker for the
- * GB300 library and the CPU baseline that bench.py times; nothing in the
+ * Faunus Metropolis Monte Carlo energy hot path.  The tests compare the GB300
+ * library against it, and bench.py times it as the CPU baseline; nothing in the
  * product path may call it.  Every function cites the reference file:line it
  * follows (paths relative to the Faunus source tree).
  *

@@ -1,6 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
-Test infrastructure only: the oracle is the checker, never the product path.
+Test infrastructure only: the tests compare the product against the oracle; the product
+path never calls it.
 """
 from __future__ import annotations
 
