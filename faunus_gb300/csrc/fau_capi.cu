@@ -1044,7 +1044,7 @@ static int compute_total(fau_sys* s, fau_energy_terms* t)
     CUDA_TRY(launch_fold_q(s->d, s->K, st)); // Q(k) = master + pending changes
     CUDA_TRY(cudaMemsetAsync(s->d_partials, 0, kTotalPartials * sizeof(double), st));
     CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, 4 * sizeof(int), st));
-    CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_partials, s->d_flags, st));
+    CUDA_TRY(launch_total(s->d, s->n, s->K, s->d_partials, s->d_flags, st, s->cells));
     std::vector<double> part(kTotalPartials);
     int f[4];
     DevSys tmp;

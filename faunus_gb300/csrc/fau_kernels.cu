@@ -72,6 +72,49 @@ __global__ void total_pair_kernel(const DevSys* Sp, double* out, int* flags)
     if (threadIdx.x == 0) out[blockIdx.x] = s; // per-block partial: summed in block order on the host
 }
 
+// The same sum for systems of atomic groups with a cell list (every pair term is zero beyond
+// the pair cutoff, no wider than a cell): particle i pairs with the j > i of its neighbour
+// cells, O(N x neighbours) instead of O(N^2).
+__global__ void total_pair_cells_kernel(const DevSys* Sp, double* out, int* flags)
+{
+    const DevSys& S = *Sp;
+    __shared__ double red[32];
+    double e = 0.0;
+    int f = 0;
+    const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1,
+              nbz = S.off_max[2] - S.off_min[2] + 1;
+    const int items = nbx * nby * nbz * S.cap;
+    for (long long i = blockIdx.x; i < S.n; i += gridDim.x) {
+        const double xi[3] = {S.x[i], S.y[i], S.z[i]};
+        const int ti = S.rec[i].w >> 24;
+        const int ci = S.cell_of[i];
+        const int c0[3] = {ci % S.cdim[0], (ci / S.cdim[0]) % S.cdim[1], ci / (S.cdim[0] * S.cdim[1])};
+        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+            const int nb = it / S.cap, slot = it - nb * S.cap;
+            const int o[3] = {nb % nbx + S.off_min[0], (nb / nbx) % nby + S.off_min[1], nb / (nbx * nby) + S.off_min[2]};
+            int w[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                w[d] = c0[d] + o[d];
+                if (w[d] < 0) w[d] += S.cdim[d];
+                else if (w[d] >= S.cdim[d]) w[d] -= S.cdim[d];
+            }
+            const int c = w[0] + S.cdim[0] * (w[1] + S.cdim[1] * w[2]);
+            if (slot >= S.cell_cnt[c]) continue;
+            const long long j = S.cell_rec[(size_t)c * S.cap + slot].w & 0xFFFFFFu;
+            if (j <= i) continue;
+            const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+            const double u = pair_u64(S, ti, S.rec[j].w >> 24, sqdist_d(S, xi, xj));
+            if (isnan(u)) f |= 2;
+            else if (isinf(u)) f |= 1;
+            else e += u;
+        }
+    }
+    const double s = block_sum_d(e, red);
+    if (f) atomicOr(flags, f);
+    if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
 // out[2b] = sum_k A_k |Q_k|^2, out[2b+1] = sum_i self(i), per block b
 __global__ void total_misc_kernel(const DevSys* Sp, double* out)
 {
@@ -380,10 +423,11 @@ cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, 
 // Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then
 // 2 * kTotalMiscBlocks (reciprocal, self) pairs; unused blocks write nothing, so
 // the caller zeroes the buffer first.  Deterministic: no floating-point atomics.
-cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st)
+cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st, bool cells)
 {
     int blocks = n < kTotalPairBlocks ? (n > 0 ? n : 1) : kTotalPairBlocks;
-    total_pair_kernel<<<blocks, 256, 0, st>>>(dsys, d_out, d_flags);
+    if (cells) total_pair_cells_kernel<<<blocks, 256, 0, st>>>(dsys, d_out, d_flags);
+    else total_pair_kernel<<<blocks, 256, 0, st>>>(dsys, d_out, d_flags);
     int kb = (K + n + 255) / 256;
     if (kb < 1) kb = 1;
     if (kb > kTotalMiscBlocks) kb = kTotalMiscBlocks;

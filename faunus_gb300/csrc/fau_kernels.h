@@ -79,7 +79,9 @@ cudaError_t fast_dispatch_4_host(const ChainArgs&, int, int, int, int, cudaStrea
 cudaError_t fast_dispatch_4_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_8_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
-cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st);
+// cells: the system's groups are all atomic and it has a cell list (O(N x neighbours) pair sum)
+cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st,
+                         bool cells = false);
 cudaError_t launch_q_rebuild(const DevSys* dsys, int K, double2* out, cudaStream_t st);
 cudaError_t launch_fold_q(DevSys* dsys, int K, cudaStream_t st); // pending Q(k) changes into the master
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
