@@ -17,6 +17,9 @@ CASES = {
     "chain_bulk": (lambda: configs.bulk_ewald(n_salt=1000, seed=5), dict(dp=2.0, threads=256)),
     "molecular_water": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=6), dict(dp=0.5, dprot=0.5, threads=0)),
     "chain_water": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=7), dict(dp=0.5, dprot=0.5, threads=256)),
+    # 4 x 4 x 4 mass-centre cells: the lists rebuilt at each launch equal the ones kept current
+    "molecular_water_cells": (lambda: configs.spce_water(n_mol=4000, L=49.3, seed=8),
+                              dict(dp=0.5, dprot=0.5, threads=0)),
 }
 
 
