@@ -538,6 +538,25 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     if ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
         (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
+    // systems of molecular groups only whose proposals are all molecular (or empty) run in the
+    // pipelined molecular kernel when every other-than-single-atom system qualifies; otherwise
+    // the chain kernel runs them (it takes every proposal kind)
+    bool use_mol = nexact > 0;
+    if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
+    for (int r = nfast; r < n && use_mol; r++) {
+        const int i = order[r];
+        fau_ctx* c2;
+        int K, np, ng, mo, knc;
+        double tr;
+        DevSys* dd;
+        fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+        if (!mo) use_mol = false;
+        for (long long m = off[i]; m < off[i] + nm[i] && use_mol; m++)
+            if (props[m].kind != FAU_MOVE_MOLECULAR && props[m].kind != FAU_MOVE_NONE) use_mol = false;
+    }
+    if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
+    if (use_mol && mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true) != cudaSuccess)
+        return fau_internal_fail(FAU_ERR_CUDA, "molecular kernel attributes");
     // proposals in pinned host memory that the device can address are read in place by the
     // pipelined kernel (streamed through its shared-memory ring while the chains run); otherwise
     // they are staged with one copy
@@ -605,11 +624,13 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     if (ok && nexact) {
         if (nfast) {
             ok = cudaEventRecord(fork_ev, st) == cudaSuccess && cudaStreamWaitEvent(st2, fork_ev, 0) == cudaSuccess &&
-                 launch_chain(ae, nexact, Ke, nce, 256, false, st2) == cudaSuccess &&
+                 (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st2, false)
+                          : launch_chain(ae, nexact, Ke, nce, 256, false, st2)) == cudaSuccess &&
                  cudaEventRecord(join_ev, st2) == cudaSuccess;
         }
         else {
-            ok = launch_chain(ae, nexact, Ke, nce, 256, false, st) == cudaSuccess;
+            ok = (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
+                          : launch_chain(ae, nexact, Ke, nce, 256, false, st)) == cudaSuccess;
         }
     }
     if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st) == cudaSuccess;

@@ -221,6 +221,12 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
     const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
     const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
+    const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
+    // move idx's proposal: the host's (A.props, checked by prepare_move) or the device RNG's
+    auto proposal = [&](long long idx) -> Proposal {
+        return A.props ? load_proposal(A.props[poff + idx])
+                       : philox_proposal(S, ctr0 + (unsigned long long)idx, sys_id, A.seed, dp_f, dprot, true);
+    };
     const int nt = S.nt;
 
     unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
@@ -228,6 +234,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     double energy = sys_energy(S), sum_du = 0.0; // the pipelined kernel's unfolded part folded in
     double M[3] = {S.M[0], S.M[1], S.M[2]};
     long long consumed = nmoves;
+    int err_code = 0; // the status that ended the chain early (FAU_ERR_*), 0 if none
 
     // phase timers (profiling only): warp 0 (tid 0): 6 prepare ahead, 3 wait B1, 4 decision,
     // 5 commit (+ re-prepare), 7 B2; warp 1 (tid 32): 0 deferred Q, 1 Ewald, 11 GroupCutoff passes,
@@ -282,7 +289,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     }
     __syncthreads();
     if (warp == 0 && nmoves > 0) {
-        const Proposal p = philox_proposal(S, ctr0, sys_id, A.seed, dp_f, dprot, true);
+        const Proposal p = proposal(0);
         prepare_move(S, msb[0], p, lane, K ? tabs : nullptr, nc);
         if constexpr (CELLS) {
             __syncwarp();
@@ -299,6 +306,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         float2* tab_next = tabs + (cur ^ 1) * tab_len;
         if (sh_stop || ms.stop || sh_time_up) { // a NaN energy change ended the chain, a proposal
             consumed = sh_stop ? sh_consumed : mv; // was invalid, or the time budget is spent
+            err_code = sh_stop ? sh_stop : ms.stop;
             break;
         }
         const int kind = ms.kind;
@@ -308,8 +316,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         if (warp == 0) {
             // ---- speculative preparation of move mv+1 (reads only the group it moves)
             if (mv + 1 < nmoves) {
-                const Proposal p =
-                    philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
+                const Proposal p = proposal(mv + 1);
                 tick(13);
                 prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc, timing ? &tacc[14] : nullptr);
                 if constexpr (CELLS) {
@@ -618,6 +625,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 flags |= __shfl_xor_sync(0xffffffffu, flags, o);
             }
             int accept = 0, stop = 0, cell_full = 0;
+            double du_out = 0.0;
             if (lane == 0 && kind != FAU_MOVE_NONE) {
                 double du_surf = 0.0;
                 if (S.flags & SYS_SURFACE) {
@@ -634,6 +642,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 const double du =
                     energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
                 const double x = du * S.beta_scale;
+                du_out = du;
                 if (isnan(x)) stop = FAU_ERR_NAN;
                 else accept = metropolis(x, ms.u) ? 1 : 0;
                 if (accept) {
@@ -644,6 +653,10 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                     for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
                 }
                 if (!stop) n_mv++;
+            }
+            if (lane == 0) { // per-move outputs of host-proposal batches
+                if (A.acc_out) A.acc_out[poff + mv] = (uint8_t)accept;
+                if (A.du_out) A.du_out[poff + mv] = du_out;
             }
             accept = __shfl_sync(0xffffffffu, accept, 0);
             stop = __shfl_sync(0xffffffffu, stop, 0);
@@ -691,8 +704,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 // the prepared next move read this group's old positions: prepare it again
                 if (mv + 1 < nmoves && mn.kind == FAU_MOVE_MOLECULAR && kind == FAU_MOVE_MOLECULAR &&
                     mn.index == ms.index) {
-                    const Proposal p =
-                        philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed, dp_f, dprot, true);
+                    const Proposal p = proposal(mv + 1);
                     prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);
                     if constexpr (CELLS) {
                         __syncwarp();
@@ -757,7 +769,12 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         G.e_acc_hi = G.e_acc_lo = 0.f;
 #pragma unroll
         for (int d = 0; d < 3; d++) G.M[d] = M[d];
-        if (sh_stop) G.err = sh_stop;
+        // a stop in the last move ends the loop without passing its top
+        if (!err_code && sh_stop) {
+            err_code = sh_stop;
+            consumed = sh_consumed;
+        }
+        if (err_code) G.err = err_code;
         G.consumed = consumed;
         G.q_valid = K ? sh_prev_accept : 0;
         G.cycles += (unsigned long long)(clock64() - t_start);

@@ -104,3 +104,30 @@ def test_molecular_kernel_translation_rotation_only_and_empty_moves(ctx, dp, dpr
     else:
         assert sa["accepted"] > 100
     _consistent(a)
+
+
+def test_molecular_kernel_host_proposals(ctx):
+    """fau_run_proposals_batch runs systems of molecules whose proposals are all molecular (the
+    reference's moltransrot stream) in the pipelined molecular kernel: its chain matches the
+    FP64 oracle and is the chain kernel's (fau_run_proposals) bit for bit."""
+    import oracle_lib  # noqa: F401  (the oracle comparison helper below loads it)
+    from test_pipelined_gpu import _oracle_compare
+    specs = [configs.spce_water(n_mol=256, L=18.6, seed=31), configs.spce_water(n_mol=4000, L=49.3, seed=32)]
+    M = 1500
+    props = [F.MoveGenerator(s, s.extra["moves"], 71 + i, 73 + i, default_seeds=False).generate(M)
+             for i, s in enumerate(specs)]
+    systems = [ctx.create(s) for s in specs]
+    allp = np.concatenate(props)
+    off = np.arange(len(specs) + 1, dtype=np.int64) * M
+    acc = np.zeros(len(allp), np.uint8)
+    du = np.zeros(len(allp))
+    st = ctx.run_proposals_batch(systems, allp, off, acc, du)
+    assert st["moves"] > 0
+    for i, (s, spec) in enumerate(zip(systems, specs)):
+        sl = slice(i * M, (i + 1) * M)
+        assert _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i]) > 100
+        c = ctx.create(spec)
+        acc_c, du_c, _ = c.run_proposals(props[i])
+        assert np.array_equal(acc_c.astype(np.uint8), acc[sl])
+        assert np.array_equal(c.positions(), s.positions())
+        assert np.allclose(du_c, du[sl], rtol=1e-9, atol=1e-9)
