@@ -66,6 +66,8 @@ cudaError_t chain_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_
 cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t, bool);
 // pipelined molecular-move kernel (device proposals; 256 threads: 1 preparing + 7 compute warps)
 cudaError_t mol_dispatch_256(const ChainArgs&, int, int, int, cudaStream_t, bool);
+cudaError_t mol_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_t, bool); // host proposals
+int mol_minb(int nblocks); // CTAs per SM the molecular kernel's registers are sized for
 size_t mol_smem_bytes_total(int K, int nc);
 // pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps;
 // k-vector components up to kFastMaxNc (8-bit phase-table indices)

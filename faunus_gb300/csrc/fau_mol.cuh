@@ -156,8 +156,10 @@ struct __align__(16) MolShared {
 };
 
 // CELLS: the system has mass-centre cells (its GroupCutoff candidates come from them); the
-// body is compiled for each case, so systems without cells run exactly the code they had
-template <int NT, bool CELLS>
+// body is compiled for each case, so systems without cells run exactly the code they had.
+// HOST: proposals from A.props (checked by prepare_move), accept flags and dU written to
+// A.acc_out / A.du_out; otherwise the device RNG's proposals.
+template <int NT, bool CELLS, bool HOST>
 __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>& sm)
 {
     constexpr int NW = NT / 32;
@@ -224,8 +226,8 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
     // move idx's proposal: the host's (A.props, checked by prepare_move) or the device RNG's
     auto proposal = [&](long long idx) -> Proposal {
-        return A.props ? load_proposal(A.props[poff + idx])
-                       : philox_proposal(S, ctr0 + (unsigned long long)idx, sys_id, A.seed, dp_f, dprot, true);
+        if constexpr (HOST) return load_proposal(A.props[poff + idx]);
+        else return philox_proposal(S, ctr0 + (unsigned long long)idx, sys_id, A.seed, dp_f, dprot, true);
     };
     const int nt = S.nt;
 
@@ -654,9 +656,11 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 }
                 if (!stop) n_mv++;
             }
-            if (lane == 0) { // per-move outputs of host-proposal batches
-                if (A.acc_out) A.acc_out[poff + mv] = (uint8_t)accept;
-                if (A.du_out) A.du_out[poff + mv] = du_out;
+            if constexpr (HOST) {
+                if (lane == 0) { // per-move outputs of host-proposal batches
+                    if (A.acc_out) A.acc_out[poff + mv] = (uint8_t)accept;
+                    if (A.du_out) A.du_out[poff + mv] = du_out;
+                }
             }
             accept = __shfl_sync(0xffffffffu, accept, 0);
             stop = __shfl_sync(0xffffffffu, stop, 0);
@@ -781,12 +785,12 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     }
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, bool HOST>
 __global__ void __launch_bounds__(NT, MINB) mol_chain_kernel(ChainArgs A)
 {
     __shared__ MolShared<NT> sm;
-    if (A.sys[blockIdx.x]->gncell > 0) mol_chain_body<NT, true>(A, sm);
-    else mol_chain_body<NT, false>(A, sm);
+    if (A.sys[blockIdx.x]->gncell > 0) mol_chain_body<NT, true, HOST>(A, sm);
+    else mol_chain_body<NT, false, HOST>(A, sm);
 }
 
 // dynamic shared memory of the molecular kernel: the chain kernel's plus a second set of tables
@@ -795,19 +799,19 @@ __host__ __device__ inline size_t mol_smem_bytes(int K, int nc)
     return chain_smem_bytes_v2(K, nc) + (size_t)kTableAtoms * 6 * (2 * nc + 1) * sizeof(float2);
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, bool HOST>
 cudaError_t launch_mol_inst(const ChainArgs& a, int nblocks, int K, int nc, cudaStream_t st, bool prepare_only)
 {
     static size_t granted = 0;
     const size_t smem = mol_smem_bytes(K, nc);
     if (smem > granted || granted == 0) {
-        cudaError_t e = cudaFuncSetAttribute(mol_chain_kernel<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mol_chain_kernel<NT, MINB, HOST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         granted = smem;
     }
     if (prepare_only) return cudaSuccess;
-    mol_chain_kernel<NT, MINB><<<nblocks, NT, smem, st>>>(a);
+    mol_chain_kernel<NT, MINB, HOST><<<nblocks, NT, smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// fau_mol_256.cu -- pipelined molecular-move kernel instantiation: 256 threads (1 + 7 warps).
+// fau_mol_256.cu -- pipelined molecular-move kernel instantiation: 256 threads (1 + 7 warps),
+// device proposals (host proposals: fau_mol_256_host.cu).
 #include "fau_mol.cuh"
 
 #include <cstdlib>
@@ -9,7 +10,7 @@ namespace fau {
 // a full wave of 3 per SM measured ~4 % faster than one of 2).  A launch takes the size
 // whose waves fill the SMs better: e.g. 608 chains on 152 SMs run as 2 waves of 2 per SM,
 // 456 or 912 as waves of 3.  FAU_MOL_MINB=2 or 3 fixes it.
-static int mol_minb(int nblocks)
+int mol_minb(int nblocks)
 {
     static int forced = [] {
         const char* e = std::getenv("FAU_MOL_MINB");
@@ -33,12 +34,14 @@ static int mol_minb(int nblocks)
 
 cudaError_t mol_dispatch_256(const ChainArgs& a, int nb, int K, int nc, cudaStream_t st, bool prep)
 {
-    if (prep) { // both register sizes get their shared-memory allowance before any capture
-        const cudaError_t e = launch_mol_inst<256, 2>(a, nb, K, nc, st, true);
-        return e != cudaSuccess ? e : launch_mol_inst<256, 3>(a, nb, K, nc, st, true);
+    if (prep) { // every instance gets its shared-memory allowance before any capture
+        cudaError_t e = launch_mol_inst<256, 2, false>(a, nb, K, nc, st, true);
+        if (e == cudaSuccess) e = launch_mol_inst<256, 3, false>(a, nb, K, nc, st, true);
+        return e != cudaSuccess ? e : mol_dispatch_256_host(a, nb, K, nc, st, true);
     }
-    return mol_minb(nb) == 3 ? launch_mol_inst<256, 3>(a, nb, K, nc, st, false)
-                             : launch_mol_inst<256, 2>(a, nb, K, nc, st, false);
+    if (a.props) return mol_dispatch_256_host(a, nb, K, nc, st, false);
+    return mol_minb(nb) == 3 ? launch_mol_inst<256, 3, false>(a, nb, K, nc, st, false)
+                             : launch_mol_inst<256, 2, false>(a, nb, K, nc, st, false);
 }
 
 size_t mol_smem_bytes_total(int K, int nc)
