@@ -189,6 +189,8 @@ def load_input(src, seed: int = 0) -> Setup:
     """Build a Setup from a Faunus input (dict, JSON/YAML text or file path).  `seed`
     seeds the random insertion of `insertmolecules`."""
     j = _read(src)
+    base_dir = Path(src).parent if isinstance(src, Path) or (
+        isinstance(src, str) and "\n" not in src and Path(src).exists()) else None
     known = {"temperature", "random", "geometry", "mcloop", "atomlist", "moleculelist", "insertmolecules",
              "energy", "moves", "analysis", "reactionlist", "groups", "particles", "implicit_reservoir"}
     extra = set(j) - known
@@ -218,14 +220,29 @@ def load_input(src, seed: int = 0) -> Setup:
     mdefs = []
     for m, p in mols:
         atomic = bool(p.get("atomic", False))
+        if "traj" in p:
+            raise NotImplementedError(f"molecule '{m}': traj (conformation library)")
+        if p.get("implicit"):  # a reaction's reservoir species, never in the space
+            mdefs.append({"atomic": True, "rigid": False, "types": [], "xyz": None, "implicit": True})
+            continue
+        if "structure" in p and isinstance(p["structure"], str):
+            # an .xyz file beside the input (MoleculeData::from_json: count, comment, name x y z)
+            if base_dir is None or not p["structure"].endswith(".xyz"):
+                raise NotImplementedError(f"molecule '{m}': structure file '{p['structure']}' "
+                                          "(xyz files beside an input file are read)")
+            lines = (base_dir / p["structure"]).read_text().split("\n")
+            count = int(lines[0].split()[0])
+            p = dict(p, structure=[{ln.split()[0]: [float(v) for v in ln.split()[1:4]]} for ln in lines[2:2 + count]])
         if "structure" in p:
             st = _items(p["structure"], f"molecule {m} structure")
             mdefs.append({"atomic": atomic, "rigid": bool(p.get("rigid", False)),
                           "types": [names.index(a) for a, _ in st],
                           "xyz": np.array([xyz for _, xyz in st], dtype=np.float64)})
-        else:
+        elif "atoms" in p:
             mdefs.append({"atomic": atomic, "rigid": bool(p.get("rigid", False)),
-                          "types": [names.index(a) for a in p.get("atoms", [])], "xyz": None})
+                          "types": [names.index(a) for a in p["atoms"]], "xyz": None})
+        else:
+            raise ValueError(f"molecule '{m}' needs atoms or a structure")
 
     # insertmolecules -> groups (InsertMoleculesInSpace; inactive groups are left out)
     rng = np.random.default_rng(seed)
@@ -236,6 +253,8 @@ def load_input(src, seed: int = 0) -> Setup:
             continue
         mid = mnames.index(m)
         md = mdefs[mid]
+        if md.get("implicit"):
+            raise NotImplementedError(f"inserting implicit molecule '{m}'")
         n = int(p["N"]) if "N" in p else int(round(float(p["molarity"]) * V * AVOGADRO / 1e27))
         if md["atomic"]:
             t = np.tile(md["types"], n)
