@@ -225,6 +225,8 @@ def load_input(src, seed: int = 0) -> Setup:
         if p.get("implicit"):  # a reaction's reservoir species, never in the space
             mdefs.append({"atomic": True, "rigid": False, "types": [], "xyz": None, "implicit": True})
             continue
+        if "structure" in p and isinstance(p["structure"], dict):
+            raise NotImplementedError(f"molecule '{m}': structure from {sorted(p['structure'])} (sequence input)")
         if "structure" in p and isinstance(p["structure"], str):
             # an .xyz file beside the input (MoleculeData::from_json: count, comment, name x y z)
             if base_dir is None or not p["structure"].endswith(".xyz"):

@@ -8,9 +8,18 @@ inputs use -- block mappings and sequences, sequence items that open a mapping
 ``#!`` first line -- and returns the same Python objects PyYAML would (int,
 float, bool, None, str, list, dict).  Anchors, tags, multi-line scalars and
 multiple documents are not supported and raise ValueError.
+
+Like the reference script, which renders the file with jinja2 first
+(scripts/yason.py:160-165), ``loads`` renders the template forms Faunus inputs
+use: ``{% set name = expression %}`` lines and ``{{ expression }}`` with numbers,
+the names set before, + - * / // % ** and parentheses; a value renders as
+Python's str() of it, as jinja2 prints it.  Other template constructs raise
+ValueError.
 """
 from __future__ import annotations
 
+import ast
+import operator
 import re
 from typing import Any, List, Tuple
 
@@ -228,8 +237,57 @@ def _block(lines: List[Tuple[int, str]], i: int, indent: int) -> Tuple[Any, int]
     return out, i
 
 
+_SET = re.compile(r"^\{%-?\s*set\s+([A-Za-z_]\w*)\s*=\s*(.+?)\s*-?%\}$")
+_EXPR = re.compile(r"\{\{\s*(.+?)\s*\}\}")
+_BINOPS = {ast.Add: operator.add, ast.Sub: operator.sub, ast.Mult: operator.mul, ast.Div: operator.truediv,
+           ast.FloorDiv: operator.floordiv, ast.Mod: operator.mod, ast.Pow: operator.pow}
+
+
+def _evaluate(expr: str, names: dict) -> Any:
+    """An arithmetic template expression over numbers and the names set so far."""
+    def ev(node):
+        if isinstance(node, ast.Expression):
+            return ev(node.body)
+        if isinstance(node, ast.Constant) and isinstance(node.value, (int, float)):
+            return node.value
+        if isinstance(node, ast.Name):
+            if node.id not in names:
+                raise ValueError(f"template name {node.id!r} is not set")
+            return names[node.id]
+        if isinstance(node, ast.UnaryOp) and isinstance(node.op, (ast.USub, ast.UAdd)):
+            v = ev(node.operand)
+            return -v if isinstance(node.op, ast.USub) else v
+        if isinstance(node, ast.BinOp) and type(node.op) in _BINOPS:
+            return _BINOPS[type(node.op)](ev(node.left), ev(node.right))
+        raise ValueError(f"unsupported template expression {expr!r}")
+    try:
+        tree = ast.parse(expr.strip(), mode="eval")
+    except SyntaxError as e:
+        raise ValueError(f"unsupported template expression {expr!r}") from e
+    return ev(tree)
+
+
+def render(text: str) -> str:
+    """The jinja2 forms of Faunus inputs: `{% set %}` lines and `{{ expression }}`."""
+    if "{%" not in text and "{{" not in text:
+        return text
+    names: dict = {}
+    out = []
+    for line in text.split("\n"):
+        m = _SET.match(line.strip())
+        if m:
+            names[m.group(1)] = _evaluate(m.group(2), names)
+            continue
+        line = _EXPR.sub(lambda mm: str(_evaluate(mm.group(1), names)), line)
+        if "{%" in line or "{{" in line:
+            raise ValueError(f"unsupported template construct in {line.strip()!r}")
+        out.append(line)
+    return "\n".join(out)
+
+
 def loads(text: str) -> Any:
-    """Parse one YAML document of the supported subset."""
+    """Parse one YAML document of the supported subset (templates rendered first)."""
+    text = render(text)
     lines = []
     for n, raw in enumerate(text.splitlines()):
         if n == 0 and raw.startswith("#!"):

@@ -248,3 +248,18 @@ def test_reference_example_inputs_load_or_name_what_is_missing():
             unsupported.append(f.name)
     assert {"minimal.yml", "bulk.yml", "ewald.yml", "water.yml"} <= set(loaded)
     assert len(loaded) + len(unsupported) >= 30
+
+
+def test_templates_rendered_as_the_reference_script_does():
+    """The reference's yason.py renders inputs with jinja2 before YAML: `{% set %}` lines and
+    `{{ expression }}` (arithmetic over the names set) render to Python's str() of the value."""
+    text = "{% set N = 50 %}\n{% set eps = 0.05*2.5 %}\n{% set pH = 7.0 %}\n" \
+           "a: {{2*N}}\nb: {{ eps }}\nc: [{{ 10**(-pH) }}, {{3/N}}]\nd: {N: {{ N }}}\n"
+    assert yason.render(text).split("\n")[:2] == ["a: 100", "b: 0.125"]
+    assert yason.loads(text) == {"a": 100, "b": 0.125, "c": [1e-07, 0.06], "d": {"N": 50}}
+    with pytest.raises(ValueError):
+        yason.loads("a: {{ undefined }}\n")
+    with pytest.raises(ValueError):
+        yason.loads("a: {% for i in range(3) %}Q{% endfor %}\n")
+    with pytest.raises(ValueError):
+        yason.loads("{% set x = __import__('os') %}\na: 1\n")
