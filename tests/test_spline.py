@@ -233,3 +233,29 @@ def test_reference_cluster_example_energy():
     n_pairs = close // 2 * 9
     assert abs(es["total"] - ee["total"]) <= 1e-3 * n_pairs
     assert es["self"] == ee["self"]
+
+
+def test_tabulate_argument_errors():
+    import ctypes as C
+    spec = _salt()
+    d, keep = spec.to_desc()
+    opts = A.SplineOpts(1e-3, 1e-2, 20.0, 1e-6, 0.0, 0, 0)
+    z, c = np.zeros(4), np.zeros(24)
+    n, hs = C.c_int(), C.c_int()
+    lib = A.lib()
+    # a table larger than the output capacity, a type out of range, a non-positive rmin
+    assert lib.fau_spline_tabulate(C.byref(d), 0, 0, 1.0, 1.0, 3.0, C.byref(opts), 4, A.as_dptr(z),
+                                   A.as_dptr(c), C.byref(n), C.byref(hs)) == A.FAU_ERR_ARG
+    assert lib.fau_spline_tabulate(C.byref(d), 5, 0, 1.0, 1.0, 3.0, C.byref(opts), 4, A.as_dptr(z),
+                                   A.as_dptr(c), C.byref(n), C.byref(hs)) == A.FAU_ERR_ARG
+    assert lib.fau_spline_tabulate(C.byref(d), 0, 0, 1.0, 1.0, 0.0, C.byref(opts), 4, A.as_dptr(z),
+                                   A.as_dptr(c), C.byref(n), C.byref(hs)) == A.FAU_ERR_ARG
+    assert b"spline" in lib.fau_last_error()
+
+
+def test_input_splined_options_reach_the_tables():
+    hard = load_input(_SPLINED_INPUT.replace("      utol: 0.0001\n", "      utol: 0.0001\n      hardsphere: true\n"))
+    assert list(hard.spec.spline["hs"]) == [1, 1, 1, 1]
+    coarse = load_input(_SPLINED_INPUT.replace("utol: 0.0001", "utol: 0.01"))
+    fine = load_input(_SPLINED_INPUT)
+    assert len(coarse.spec.spline["r2"]) < len(fine.spec.spline["r2"])
