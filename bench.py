@@ -38,13 +38,6 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# algorithmic work per unit (flops; add/mul/compare = 1, FMA = 2)
-FLOPS_PER_K_UPDATE = 37.0    # per k-vector per moved atom: midpoint phase (12), sin(D/2) (9), dQ (3),
-                             # pending fold (2), dU_rec term (7), accumulation (4)
-FLOPS_PER_PAIR = 38.0        # per pair interaction (LJ + Ewald real space)
-BYTES_PER_PAIR_CANDIDATE = 16.0
-
-
 def _env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
@@ -140,26 +133,30 @@ def _sum_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
-def _profile_traffic():
-    """DRAM bytes per move of the pipelined chain kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "fast_chain_kernel_bulk_ewald.json"
-    if p.exists():
-        try:
-            d = json.loads(p.read_text())
-            return float(d["dram_bytes_per_move"]), d.get("source", str(p.name))
-        except (ValueError, KeyError):
-            pass
-    return None, None
-
-
-def cpu_baseline(spec, seconds_per_thread: float = 1.0, threads: int | None = None) -> dict:
+def cpu_baseline(spec, seconds_per_thread: float = 1.0, threads: int | None = None, check=None) -> dict:
     """The oracle (reference algorithm restated in C++) on the host cores:
-    one chain per thread, a bounded number of moves per chain."""
+    one chain per thread, a bounded number of moves per chain.  check: optional
+    (proposals, device dU) of a fresh copy of `spec` run on the device in this run; the
+    oracle replays the proposals and the device dU is compared with its FP64 dU."""
     sys.path.insert(0, str(ROOT / "tests"))
     import ctypes as C
 
     import oracle_lib as O
     from faunus_gb300.system import move_descs
+
+    parity = None
+    if check is not None:
+        props, du_dev, acc_dev = check
+        det = O.OracleSystem(spec).run_detail(props)
+        same = np.nonzero(det["accepted"].astype(np.uint8) != acc_dev)[0]
+        upto = int(same[0]) + 1 if len(same) else len(props)
+        fin = np.isfinite(det["du"][:upto])
+        parity = {"moves": len(props), "compared": int(fin.sum()), "identical_accepts_until": upto,
+                  **O.du_errors(du_dev[:upto][fin], det["du"][:upto][fin], det["err_scale"][:upto][fin]),
+                  "definition": "rel_scaled = |dU_dev - dU_fp64| / max(|dU|, S) (S: sum of |summands|; "
+                                "tolerance 1e-6); rel_du = |dU_dev - dU_fp64| / |dU| for |dU| > 1e-3 kT",
+                  "source": "device dU of the reference-stream proposals through fau_run_proposals_batch vs "
+                            "the FP64 oracle replaying them"}
 
     threads = threads or os.cpu_count() or 1
     d, keep = spec.to_desc()
@@ -175,9 +172,12 @@ def cpu_baseline(spec, seconds_per_thread: float = 1.0, threads: int | None = No
     rc = L.orc_bench_chains(C.byref(d), arr, 1, threads, threads, m, C.byref(mps), C.byref(wall))
     if rc != 0:
         raise RuntimeError(f"oracle bench failed: {rc}")
-    return {"value": mps.value, "unit": "moves/s", "cores": threads, "kind": "port",
-            "sample": f"{threads} chains x {m} moves of the 20,000-ion bulk Ewald system, one chain per thread "
-                      f"({wall.value:.1f} s wall)", "wall_s": wall.value, "moves_per_chain": m}
+    out = {"value": mps.value, "unit": "moves/s", "cores": threads, "kind": "port",
+           "sample": f"{threads} chains x {m} moves of the 20,000-ion bulk Ewald system, one chain per thread "
+                     f"({wall.value:.1f} s wall)", "wall_s": wall.value, "moves_per_chain": m}
+    if parity is not None:
+        out["du_parity"] = parity
+    return out
 
 
 def run_reference(args) -> None:
@@ -214,31 +214,40 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-# algorithmic bytes of the path: per k-vector and move 12 B k-vector + 4 B A_k + 16 B Q(k) read,
-# per accepted move 16 B Q(k) written a k-vector, per candidate particle 20 B (x, y, z, q, type)
-BYTES_PER_K_READ, BYTES_PER_K_WRITE, BYTES_PER_CANDIDATE = 32, 16, 20
-
-
-def _hbm_roofline(alg_bytes_per_s, dram_bytes_per_move, moves_per_launch, alg_bytes_per_move):
-    """The HBM roofline: the path's algorithmic bytes per second against the measured copy
-    bandwidth of MEASURED_PEAKS.json; `traffic` the DRAM bytes of one launch from the ncu
-    capture of the same kernel (cold cache) -- far below the algorithmic bytes, because each
-    chain keeps its k-vector table, A_k and Q(k) in shared memory and its particles in L2."""
-    peaks = Path(__file__).resolve().parent / "MEASURED_PEAKS.json"
-    try:
-        peak = float(json.loads(peaks.read_text())["hbm_gbs"])
-        src = "measured (MEASURED_PEAKS.json hbm_gbs)"
-    except (OSError, ValueError, KeyError):
-        peak, src = 6800.0, "fallback 6.8 TB/s"
-    achieved = alg_bytes_per_s / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": dram_bytes_per_move * moves_per_launch if dram_bytes_per_move else None,
-            "algorithmic_bytes_per_move": alg_bytes_per_move, "dram_bytes_per_move": dram_bytes_per_move,
-            "peak_source": src,
-            "work": f"{BYTES_PER_K_READ} B read per k-vector and move + {BYTES_PER_K_WRITE} B written per "
-                    f"k-vector and accepted move + {BYTES_PER_CANDIDATE} B per candidate particle",
-            "note": "algorithmic bytes are served from shared memory and L2; traffic = ncu DRAM bytes of "
-                    "one launch (8 KB a move, cold cache)"}
+def _roofline(R, stats, dev_ms, kv, fp32_peak, sms, sm_mhz):
+    """The contract's HBM form for the pipelined chain kernel (algorithmic bytes per launch over its
+    device time against the measured copy bandwidth; `traffic` the DRAM bytes of one launch from the
+    committed ncu capture of the same kernel) and every other fraction faunus_gb300.roofline
+    defines, with the one that binds."""
+    from faunus_gb300 import roofline as RL
+    moves = sum(s["moves"] for s in stats)
+    pairs = sum(s["pair_evals"] for s in stats)
+    acc = sum(s["accepted"] for s in stats)
+    launches = len(stats)
+    mps = moves / (dev_ms * 1e-3)
+    alg_b = RL.single_atom_bytes(pairs, moves, acc, kv) / moves
+    flops = RL.single_atom_flops(pairs, moves, kv, ewald_pair=True) / moves
+    prof = RL.kernel_profile("fast_chain_kernel_bulk_ewald")
+    fr = RL.fractions(mps, alg_b, flops, fp32_peak, sms, sm_mhz, prof)
+    per_launch_moves = moves / launches
+    hbm = fr["hbm"]
+    line = {"bound": "hbm", "achieved": hbm["achieved_gbs"], "peak": hbm["peak_gbs"], "unit": "GB/s",
+            "frac": hbm["frac"],
+            "traffic": prof["dram_bytes_per_move"] * per_launch_moves if prof and prof.get("dram_bytes_per_move")
+            else None,
+            "peak_source": hbm["peak_source"], "algorithmic_bytes_per_move": alg_b,
+            "work": f"{RL.BYTES_PER_K_READ} B read per k-vector and move + {RL.BYTES_PER_K_WRITE} B written per "
+                    f"k-vector and accepted move + {RL.BYTES_PER_CANDIDATE_FP32} B per candidate particle "
+                    "(faunus_gb300/roofline.py)",
+            "note": "the algorithmic bytes are served from shared memory (k-vectors, A_k, Q(k)) and L2 "
+                    "(particles); `traffic` is the measured DRAM bytes of one launch"}
+    others = {k: v for k, v in fr.items() if k != "hbm"}
+    others["flops_per_move"] = flops
+    others["work"] = (f"{RL.FLOPS_PER_K_SINGLE_ATOM_MOVE:g} flop per k-vector and move + "
+                      f"{RL.FLOPS_PER_PAIR_LJ_EWALD:g} per pair interaction (faunus_gb300/roofline.py)")
+    if prof:
+        others["profile_source"] = prof.get("source")
+    return line, others
 
 
 def run_ours(args) -> None:
@@ -304,42 +313,67 @@ def run_ours(args) -> None:
         _barrier(dist)
         return
 
-    # ---- e2e: reference-stream proposals through the C ABI, host buffers
+    # ---- e2e: reference-stream proposals through the C ABI, host buffers.  Each step's proposals
+    # are drawn on the host (mt19937 in the reference's order, as the caller's Move code would) into
+    # one of two pinned buffers while the device runs the previous step from the other; the kernel
+    # reads its buffer in place; accept flags and dU come back.  Generation, copies and kernels are
+    # all inside the timed region.
     gens = [F.MoveGenerator(base, base.extra["moves"], 7 + i, 11 + i, default_seeds=False) for i in range(R)]
     offsets = np.arange(R + 1, dtype=np.int64) * M
-    props_buf, acc_buf, du_buf = _pinned(R * M)
+    bufs = [_pinned(R * M) for _ in range(2)]
+    gen_threads = max(1, min(16, (os.cpu_count() or 2) - 1))
+    pool = cf.ThreadPoolExecutor(max_workers=gen_threads)
 
-    def fill():
-        def one(i):
-            props_buf[i * M:(i + 1) * M] = gens[i].generate(M)
-        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-            list(ex.map(one, range(R)))
+    def fill(buf):
+        t = time.perf_counter()
+        props = buf[0]
+        chunk = (R + gen_threads - 1) // gen_threads
+
+        def part(c):
+            for i in range(c * chunk, min(R, (c + 1) * chunk)):
+                props[i * M:(i + 1) * M] = gens[i].generate(M)
+        list(pool.map(part, range(gen_threads)))
+        return time.perf_counter() - t
 
     e2e_systems = systems
-    for _ in range(max(1, args.warmup // 2)):
-        fill()
-        ctx.run_proposals_batch(e2e_systems, props_buf, offsets, acc_buf, du_buf)
-    e2e_s = 0.0
+    for w in range(max(1, args.warmup // 2)):
+        fill(bufs[0])
+        ctx.run_proposals_batch(e2e_systems, bufs[0][0], offsets, bufs[0][1], bufs[0][2])
+    gen_s = []
+    kern_s = []
     e2e_moves = 0
-    for _ in range(args.steps):
-        fill()  # the step's inputs (drawn by the caller's Move code), outside the timed region
-        _barrier(dist)
-        t1 = time.perf_counter()
-        st = ctx.run_proposals_batch(e2e_systems, props_buf, offsets, acc_buf, du_buf)
-        e2e_s += time.perf_counter() - t1
+    _barrier(dist)
+    t1 = time.perf_counter()
+    gen_s.append(fill(bufs[0]))
+    for k in range(args.steps):
+        cur = bufs[k % 2]
+        nxt = pool.submit(fill, bufs[(k + 1) % 2]) if k + 1 < args.steps else None
+        tk = time.perf_counter()
+        st = ctx.run_proposals_batch(e2e_systems, cur[0], offsets, cur[1], cur[2])
+        kern_s.append(time.perf_counter() - tk)
         e2e_moves += st["moves"]
-    e2e_s = _max_over_ranks(dist, e2e_s)
+        if nxt is not None:
+            gen_s.append(nxt.result())
+    e2e_wall = time.perf_counter() - t1
+    e2e_s = _max_over_ranks(dist, e2e_wall)
     e2e_value = _sum_over_ranks(dist, e2e_moves) / e2e_s
+    pool.shutdown()
 
-    # ---- roofline of the chain kernel: HBM (algorithmic bytes) and the FP32 pipe
+    # ---- parity of this run's device dU: a fresh copy of the system, the reference stream's first
+    # moves through the same entry point (checked against the oracle in the CPU-baseline leg)
+    chk = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        fresh = ctx.create(base)
+        pg = F.MoveGenerator(base, base.extra["moves"], 7, 11, default_seeds=False).generate(args.parity_moves)
+        acc_c = np.zeros(len(pg), np.uint8)
+        du_c = np.zeros(len(pg))
+        ctx.run_proposals_batch([fresh], pg, np.array([0, len(pg)], np.int64), acc_c, du_c)
+        fresh.close()
+        chk = (pg, du_c, acc_c)
+
+    # ---- roofline of the pipelined chain kernel
     peak = ctx.fp32_peak_tflops()
-    flops = FLOPS_PER_K_UPDATE * kup + FLOPS_PER_PAIR * pairs
-    achieved = flops / (dev_ms * 1e-3) / 1e12
-    bytes_per_move, src = _profile_traffic()
-    traffic = bytes_per_move * (moves / args.steps) if bytes_per_move else None
-    kv = systems[0].K
-    alg_bytes = BYTES_PER_K_READ * kup + BYTES_PER_K_WRITE * kv * acc + BYTES_PER_CANDIDATE * pairs / 2
-    hbm = _hbm_roofline(alg_bytes / (dev_ms * 1e-3), bytes_per_move, moves / args.steps, alg_bytes / max(moves, 1))
+    roof, roof_other = _roofline(R, stats, dev_ms, systems[0].K, peak, sms, clk.get("sm_mhz"))
 
     line = {
         "metric": "MC trial moves/sec", "value": value, "unit": "moves/s", "n_gpus": world,
@@ -361,13 +395,15 @@ def run_ours(args) -> None:
         "k_updates_per_s": _sum_over_ranks(dist, kup) / dev_s,
         "acceptance": acc / max(moves, 1),
         "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": int(R * M * 72 + 8 * (R + 1)),
-                "d2h_bytes_per_step": int(R * M * 9)},
-        "roofline": hbm,
-        "roofline_fp32": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                          "frac": achieved / peak if peak else None, "traffic": traffic,
-                          "peak_source": "measured FP32 FMA probe (fau_measure_fp32_peak) in this run",
-                          "work": f"{FLOPS_PER_K_UPDATE:g} flop per k-vector x moved atom + {FLOPS_PER_PAIR:g} per pair",
-                          "traffic_source": src},
+                "d2h_bytes_per_step": int(R * M * 9),
+                "covers": "host proposal generation (reference mt19937 stream, "
+                          f"{gen_threads} host threads, double-buffered) + host->device reads of the pinned "
+                          "proposals + kernels + accept flags and dU back",
+                "generation_s_per_step": statistics.mean(gen_s), "call_s_per_step": statistics.mean(kern_s),
+                "generation_moves_per_s": R * M / statistics.mean(gen_s),
+                "wall_s": e2e_wall},
+        "roofline": roof,
+        "roofline_other": roof_other,
         "clocks": clk,
         "gpu_launches": 3 * args.steps,
         "wall_s": wall,
@@ -376,10 +412,14 @@ def run_ours(args) -> None:
         line["plain_fp64_single_system"] = plain_form(ctx, base)
         line["plain_fp64_single_system"]["batched_over_plain"] = value / line["plain_fp64_single_system"]["value"]
         line["served"] = served(ctx, F, configs, full=args.served_full)
-        line["other_configs"] = other_configs(ctx, configs, R)
+        line["other_configs"] = other_configs(ctx, configs, R, sweeps=args.pt_sweeps, pt_blocks=args.pt_blocks,
+                                              pt_budget_s=args.pt_budget_s)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(base)
+        line["cpu_baseline"] = cpu_baseline(base, check=chk)
         line["cpu_baseline"].pop("wall_s", None)
+        if "du_parity" in line["cpu_baseline"]:
+            line["du_rel_err_max"] = {k: line["cpu_baseline"]["du_parity"][k]
+                                      for k in ("rel_scaled_max", "rel_du_max", "rel_du_median")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     for s in systems:
@@ -406,7 +446,7 @@ def plain_form(ctx, base, moves: int = 400) -> dict:
             "form": "FP64 pair and Ewald kernels per trial move, host Metropolis, same 20,000-ion system"}
 
 
-def other_configs(ctx, configs, replicas: int) -> dict:
+def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: int = 2, pt_budget_s: float = 60.0) -> dict:
     """Device-timed throughput of the other configurations (seconds each): the primitive
     model (200 hard-sphere ions) and rigid SPC/E water (1,000 molecules, molecular moves)
     as replica batches, and the 256-walker parallel-tempering ladder (N 100..5,000)."""
@@ -429,17 +469,42 @@ def other_configs(ctx, configs, replicas: int) -> dict:
     mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 5000)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
                               "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
+    out["parallel_tempering_256"] = parallel_tempering(ctx, configs, sweeps, pt_blocks, pt_budget_s)
+    return out
+
+
+def parallel_tempering(ctx, configs, sweeps: int, blocks: int, budget_s: float) -> dict:
+    """Config 3: 256 primitive-model walkers, N ~ U{100..5000}, T 250-400 K geometric, a swap
+    round every `sweeps` sweeps of each walker (sweeps x N_i moves per walker between rounds), all
+    blocks and swap rounds in one CUDA graph.  A one-sweep calibration block measures each walker's
+    cycles per move first; the configured sweeps run when the predicted time of the blocks fits
+    `budget_s` (the longest walker sets a block's length), otherwise the most sweeps that fit."""
     specs, temps = configs.pt_replicas(n_rep=256)
     systems = [ctx.create(s_) for s_ in specs]
-    st = ctx.run_batch(systems, swap_interval=2000, n_swap_blocks=5, temperatures=temps, seed=3, dp=2.0)
+    n = np.array([s_.n for s_ in specs], np.int64)
+    cyc = np.zeros(len(specs), np.uint64)
+    cal = ctx.run_batch(systems, moves_per_system=n, swap_interval=1, n_swap_blocks=1, temperatures=temps, seed=3,
+                        dp=2.0, cycles_out=cyc)
+    sec_per_sweep = float(cal["device_ms"]) * 1e-3
+    run_sweeps = sweeps
+    if sec_per_sweep * sweeps * blocks > budget_s:
+        run_sweeps = max(1, int(budget_s / (sec_per_sweep * blocks)))
+    lens = n * run_sweeps
+    st = ctx.run_batch(systems, moves_per_system=lens, swap_interval=1, n_swap_blocks=blocks, temperatures=temps,
+                       seed=3, dp=2.0, counter_base=1)
     for s_ in systems:
         s_.close()
-    out["parallel_tempering_256"] = {"moves_per_s": st["moves"] / (st["device_ms"] * 1e-3),
-                                     "swaps_attempted": st["swaps_attempted"], "swaps_accepted": st["swaps_accepted"],
-                                     "swap_interval_moves": 2000,
-                                     "note": "one graph: 5 blocks of 2,000 moves per walker + device swap kernel; "
-                                             "each block lasts as long as its largest walker (N up to 5,000)"}
-    return out
+    longest = int(np.argmax(cyc))
+    return {"moves_per_s": st["moves"] / (st["device_ms"] * 1e-3), "moves": st["moves"],
+            "device_s": st["device_ms"] * 1e-3, "swap_rounds": blocks,
+            "sweeps_between_swaps": run_sweeps, "configured_sweeps_between_swaps": sweeps,
+            "swaps_attempted": st["swaps_attempted"], "swaps_accepted": st["swaps_accepted"],
+            "swap_acceptance": st["swaps_accepted"] / max(1, st["swaps_attempted"]),
+            "walkers": len(specs), "particles_total": int(n.sum()),
+            "calibration_s_per_sweep": sec_per_sweep,
+            "longest_walker": {"n": int(n[longest]), "cycles_per_move": float(cyc[longest]) / float(n[longest])},
+            "note": ("walker i moves sweeps x N_i times between swap rounds (ParallelTempering every 1,000 sweeps); "
+                     "a block lasts as long as its longest chain; walkers start in descending order of work")}
 
 
 def served(ctx, F, configs, full: bool = False) -> dict:
@@ -502,8 +567,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-form and served-stream measurements")
     ap.add_argument("--served-full", action="store_true", help="served stream at the full configured job sizes")
+    ap.add_argument("--parity-moves", type=int, default=2000,
+                    help="moves of the device dU checked against the oracle in the CPU-baseline leg")
     ap.add_argument("--cpu-sample-seconds", type=float, default=0.5,
                     help="reference arm: seconds of CPU chain work per thread and step")
+    ap.add_argument("--pt-sweeps", type=int, default=1000, help="parallel tempering: sweeps between swap rounds")
+    ap.add_argument("--pt-blocks", type=int, default=2, help="parallel tempering: swap rounds measured")
+    ap.add_argument("--pt-budget-s", type=float, default=60.0,
+                    help="parallel tempering: device seconds allowed; fewer sweeps run if the calibration predicts more")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
     ap.add_argument("--workload", default="bulk", choices=["bulk", "water"],
                     help="water: 1,000 rigid SPC/E molecules, molecular moves (profiling case, with --value-only)")

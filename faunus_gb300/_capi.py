@@ -116,7 +116,8 @@ class BatchParams(C.Structure):
                 ("counters", C.POINTER(C.c_uint64)), ("dp_per_system", dptr), ("dprot_per_system", dptr),
                 ("cycles_out", C.POINTER(C.c_uint64)), ("sampler", C.c_void_p),
                 ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int),
-                ("time_budget_ns", C.c_uint64), ("moves_out", C.POINTER(C.c_int64))]
+                ("time_budget_ns", C.c_uint64), ("moves_out", C.POINTER(C.c_int64)),
+                ("swap_slots_out", iptr), ("swap_energy_out", dptr)]
 
 
 class SamplerDesc(C.Structure):
@@ -207,6 +208,10 @@ def _declare(lib: C.CDLL) -> None:
         "fau_set_temperature_scale": ([P, C.c_double], C.c_int),
         "fau_q_rebuild": ([P, dptr], C.c_int),
         "fau_get_q": ([P, dptr], C.c_int),
+        "fau_get_kvectors": ([P, iptr, dptr, dptr], C.c_int),
+        "fau_sys_state_size": ([P, C.POINTER(C.c_size_t)], C.c_int),
+        "fau_sys_save_state": ([P, P, C.c_size_t], C.c_int),
+        "fau_sys_load_state": ([P, P, C.c_size_t], C.c_int),
         "fau_movegen_create": ([C.POINTER(SysDesc), C.POINTER(MoveDesc), C.c_int, C.c_uint32, C.c_uint32, C.c_int,
                                 C.POINTER(P)], C.c_int),
         "fau_movegen_destroy": ([P], C.c_int),

@@ -59,12 +59,17 @@ __global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
 // slot_sys[s]: system holding temperature slot s; T[s]: slot temperatures;
 // Tref[i]: temperature system i's parameters were built for (its kT unit).
 // Energies are converted to absolute units (kT_ref * T_ref) and pairs
-// (s, s+1) with s = parity, parity + 2, ... are exchanged with probability
-// min(1, exp[(1/T_s - 1/T_{s+1}) (E_a - E_b)]).
+// (s, s+1) with s = parity, parity + 2, ... are exchanged as metropolisCriterion
+// (src/montecarlo.cpp:17-34) decides on dU = -x, x = (1/T_s - 1/T_{s+1}) (E_a - E_b):
+// accept when u <= exp(x) (always for x >= 0; never for a NaN).  The optional logs
+// receive each system's running energy at the round and the slot order after it.
 __global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const double* T, const double* Tref,
-                               uint64_t seed, unsigned long long round, unsigned long long* stats)
+                               uint64_t seed, unsigned long long round, unsigned long long* stats,
+                               double* energy_log, int* slots_log)
 {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (energy_log)
+        for (int i = 0; i < n; i++) energy_log[i] = sys_energy(*sys[i]);
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     const U4 r0 = philox({(uint32_t)round, (uint32_t)(round >> 32), 0xFFFFFFFFu, 7u}, k0, k1);
     const int parity = r0.x & 1;
@@ -78,7 +83,7 @@ __global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const d
         stats[0]++;
         bool acc = false;
         if (x >= 0.0) acc = true;
-        else if (isfinite(x)) acc = u < exp(x);
+        else if (!isnan(x)) acc = u <= exp(x);
         if (acc) {
             stats[1]++;
             slot_sys[s] = b;
@@ -87,6 +92,8 @@ __global__ void pt_swap_kernel(DevSys* const* sys, int n, int* slot_sys, const d
             sys[b]->beta_scale = Tref[b] / T[s];
         }
     }
+    if (slots_log)
+        for (int s = 0; s < n; s++) slots_log[s] = slot_sys[s];
 }
 
 // the pipelined kernel writes each move's energy change as a packed float-float pair
@@ -128,6 +135,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     const bool blocked = pt || sblocks;
     const long long blk_moves = pt ? P->swap_interval_moves : (sblocks ? P->sample_interval_moves : 0);
     const int nblk = pt ? P->n_swap_blocks : (sblocks ? P->n_sample_blocks : 1);
+    // parallel tempering with a block length per walker (moves_per_system: e.g. 1,000 sweeps each)
+    const bool pt_lens = pt && P->moves_per_system;
+    const bool pt_log = pt && (P->swap_slots_out || P->swap_energy_out);
     if (!(P->dp >= 0.0)) return fau_internal_fail(FAU_ERR_ARG, "dp must be >= 0");
 
     std::vector<DevSys*> dsys(n);
@@ -172,6 +182,25 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     for (int i = 0; i < n; i++)
         if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
+    // within each kernel, chains in descending order of their work (moves x particles): the CTAs
+    // are handed to the SMs in index order, so the longest chains start first, one to an SM while
+    // SMs remain, and the short ones fill in beside them (results depend only on each system's
+    // seed, stream and counter, never on this order)
+    {
+        std::vector<double> cost(n);
+        for (int i = 0; i < n; i++) {
+            fau_ctx* c2;
+            int K, np, ng, mo, knc;
+            double tr;
+            DevSys* dd;
+            fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+            const double len = blocked && !pt_lens ? (double)blk_moves : (double)nm[i];
+            cost[i] = len * (double)(np + K);
+        }
+        auto by_cost = [&](int x, int y) { return cost[x] > cost[y]; };
+        std::stable_sort(order.begin(), order.begin() + nfast, by_cost);
+        std::stable_sort(order.begin() + nfast, order.end(), by_cost);
+    }
     int Kf = 0, ncf = 0, ntf = 1, Ke = 0, nce = 0;
     for (int r = 0; r < n; r++) {
         int K, np, ng, mo, knc;
@@ -210,7 +239,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                  off_ksys = al(off_ctr + 8 * n), off_knm = al(off_ksys + sizeof(DevSys*) * n),
                  off_kids = al(off_knm + 8 * n), off_kmol = al(off_kids + 4 * n), off_kctr = al(off_kmol + n),
                  off_kdp = al(off_kctr + 8 * n), off_kdr = al(off_kdp + 8 * n), off_sslot = al(off_kdr + 8 * n),
-                 total = al(off_sslot + 4 * n);
+                 off_bctr = al(off_sslot + 4 * n), off_elog = al(off_bctr + 8 * (size_t)n * nblk),
+                 off_slog = al(off_elog + (pt_log ? 8 * (size_t)n * nblk : 0)),
+                 total = al(off_slog + (pt_log ? 4 * (size_t)n * nblk : 0));
     unsigned char* dbuf = nullptr;
     if (fau_internal_ctx_scratch(ctx, total, reinterpret_cast<void**>(&dbuf)) != FAU_OK)
         return fau_internal_fail(FAU_ERR_OOM, "batch argument allocation");
@@ -297,6 +328,17 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     BTRY(cudaMemcpyAsync(dbuf + off_kids, kids.data(), 4 * n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kmol, kmol.data(), n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kctr, kctr.data(), 8 * n, cudaMemcpyHostToDevice, st));
+    // blocked launches: each block's first move counter per CTA (a walker's block b starts at
+    // its counter + b times its own block length)
+    std::vector<unsigned long long> bctr;
+    if (blocked) {
+        bctr.resize((size_t)n * nblk);
+        for (int b = 0; b < nblk; b++)
+            for (int r = 0; r < n; r++)
+                bctr[(size_t)b * n + r] =
+                    kctr[r] + (unsigned long long)b * (unsigned long long)(pt_lens ? knm[r] : blk_moves);
+        BTRY(cudaMemcpyAsync(dbuf + off_bctr, bctr.data(), 8 * bctr.size(), cudaMemcpyHostToDevice, st));
+    }
     BTRY(cudaMemcpyAsync(dbuf + off_kdp, kdp.data(), 8 * n, cudaMemcpyHostToDevice, st));
     BTRY(cudaMemcpyAsync(dbuf + off_kdr, kdr.data(), 8 * n, cudaMemcpyHostToDevice, st));
     ChainArgs a{};
@@ -310,7 +352,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     a.dprot_sys = reinterpret_cast<const double*>(dbuf + off_kdr);
     if (P->counters) a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_kctr);
     if (blocked) {
-        a.n_moves = nullptr;
+        a.n_moves = pt_lens ? reinterpret_cast<const long long*>(dbuf + off_knm) : nullptr;
         a.moves = blk_moves;
     }
     else {
@@ -335,9 +377,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         BTRY(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
     }
     // one block of moves: the pipelined kernel on `st`, the chain kernel on a forked stream
-    auto launch_block = [&](unsigned long long cbase) -> cudaError_t {
-        a.counter_base = cbase;
-        ae.counter_base = cbase;
+    auto launch_block = [&](int b) -> cudaError_t {
+        if (blocked) { // this block's first counters (the CTA's counter + b block lengths)
+            a.counters = reinterpret_cast<const unsigned long long*>(dbuf + off_bctr) + (size_t)b * n;
+            ae.counters = a.counters + nfast;
+        }
+        a.counter_base = P->counter_base;
+        ae.counter_base = P->counter_base;
         cudaError_t e = cudaSuccess;
         if (nfast && nexact) {
             if ((e = cudaEventRecord(fork_ev, st)) != cudaSuccess) return e;
@@ -371,8 +417,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     cudaGraphExec_t exec = nullptr;
     BTRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int b = 0; b < nblk; b++) {
-        const unsigned long long cbase = P->counter_base + (unsigned long long)b * (unsigned long long)blk_moves;
-        if (launch_block(cbase) != cudaSuccess) {
+        if (launch_block(b) != cudaSuccess) {
             cudaStreamEndCapture(st, &graph);
             if (graph) cudaGraphDestroy(graph);
             cleanup();
@@ -383,7 +428,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                                             reinterpret_cast<const double*>(dbuf + off_T),
                                             reinterpret_cast<const double*>(dbuf + off_Tref), P->seed ^ 0x5DEECE66DULL,
                                             P->counter_base / (P->swap_interval_moves ? P->swap_interval_moves : 1) + b,
-                                            reinterpret_cast<unsigned long long*>(dbuf + off_st));
+                                            reinterpret_cast<unsigned long long*>(dbuf + off_st),
+                                            pt_log ? reinterpret_cast<double*>(dbuf + off_elog) + (size_t)b * n : nullptr,
+                                            pt_log ? reinterpret_cast<int*>(dbuf + off_slog) + (size_t)b * n : nullptr);
         if (smp && fau_internal_sampler_launch(smp, d_sys, n, reinterpret_cast<const int*>(dbuf + off_sslot), max_np,
                                                st) != cudaSuccess) {
             cudaStreamEndCapture(st, &graph);
@@ -401,6 +448,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     unsigned long long pst[8] = {0};
     BTRY(cudaMemcpyAsync(s1.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st));
     BTRY(cudaMemcpyAsync(pst, dbuf + off_st, 64, cudaMemcpyDeviceToHost, st));
+    if (pt_log && P->swap_energy_out)
+        BTRY(cudaMemcpyAsync(P->swap_energy_out, dbuf + off_elog, 8 * (size_t)n * nblk, cudaMemcpyDeviceToHost, st));
+    if (pt_log && P->swap_slots_out)
+        BTRY(cudaMemcpyAsync(P->swap_slots_out, dbuf + off_slog, 4 * (size_t)n * nblk, cudaMemcpyDeviceToHost, st));
     const cudaError_t se = cudaStreamSynchronize(st);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -455,7 +506,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (P->cycles_out)
         for (int i = 0; i < n; i++) P->cycles_out[i] = (uint64_t)(s1[i].cycles - s0[i].cycles);
     if (P->moves_out) // blocked launches run every block in full; otherwise the one launch's count
-        for (int i = 0; i < n; i++) P->moves_out[i] = blocked ? (int64_t)blk_moves * nblk : (int64_t)s1[i].consumed;
+        for (int i = 0; i < n; i++)
+            P->moves_out[i] = blocked ? (int64_t)(pt_lens ? nm[i] : blk_moves) * nblk : (int64_t)s1[i].consumed;
     S.swaps_attempted = (int64_t)pst[0];
     S.swaps_accepted = (int64_t)pst[1];
     S.device_ms = ms;

@@ -1004,6 +1004,155 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     return FAU_OK;
 }
 
+// ---------------------------------------------------------------- exact device state (checkpoints)
+static int rebuild_cells(fau_sys* s, int cap);
+static int pull_state(fau_sys* s);
+namespace {
+constexpr uint32_t kStateMagic = 0x53554146u; // "FAUS"
+constexpr uint32_t kStateVersion = 1;
+
+struct StateHeader {
+    uint32_t magic, version;
+    int32_t n, n_groups, K, ncell, cap, precision;
+    double box[3];
+    // running scalars of the device struct
+    double energy, beta_scale, sum_du, M[3];
+    float e_acc_hi, e_acc_lo;
+    int32_t q_valid, q_since;
+    uint64_t moves, accepted, pair_evals, k_updates, cycles;
+};
+
+// the device arrays a chain changes, in blob order: (device pointer, bytes)
+std::vector<std::pair<void*, size_t>> state_arrays(const fau_sys* s)
+{
+    const DevSys& h = s->h;
+    const size_t n = s->n, g = s->n_groups, K = s->K;
+    std::vector<std::pair<void*, size_t>> a = {
+        {h.x, 8 * n}, {h.y, 8 * n}, {h.z, 8 * n}, {h.rec, 16 * n}, {h.g_cm, h.g_cm ? 24 * g : 0},
+        {h.g_cmrec, h.g_cmrec ? 16 * g : 0}, {h.Q, 16 * K}, {h.qpend, h.qpend ? 8 * K : 0},
+        {h.qdlt, h.qdlt ? 8 * K : 0}};
+    if (s->cells) {
+        const size_t nc = (size_t)h.ncell, cap = (size_t)h.cap;
+        a.push_back({h.cell_cnt, 4 * nc});
+        a.push_back({h.cell_rec, 16 * nc * cap});
+        a.push_back({h.cell_of, 4 * n});
+        a.push_back({h.slot_of, 4 * n});
+    }
+    return a;
+}
+} // namespace
+
+int fau_sys_state_size(const fau_sys* s, size_t* bytes)
+{
+    if (!s || !bytes) return fail(FAU_ERR_ARG, "null argument");
+    size_t b = sizeof(StateHeader);
+    for (auto& a : state_arrays(s)) b += a.second;
+    *bytes = b;
+    return FAU_OK;
+}
+
+int fau_sys_save_state(fau_sys* s, void* buf, size_t bytes)
+{
+    if (!s || !buf) return fail(FAU_ERR_ARG, "null argument");
+    if (s->pending) return fail(FAU_ERR_STATE, "a trial is pending (fau_commit_pending first)");
+    size_t need = 0;
+    fau_sys_state_size(s, &need);
+    if (bytes < need) return fail(FAU_ERR_ARG, "state buffer of %zu bytes, %zu needed", bytes, need);
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    DevSys cur;
+    CUDA_TRY(cudaMemcpyAsync(&cur, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+    char* out = static_cast<char*>(buf);
+    size_t off = sizeof(StateHeader);
+    for (auto& a : state_arrays(s)) {
+        if (a.second) CUDA_TRY(cudaMemcpyAsync(out + off, a.first, a.second, cudaMemcpyDeviceToHost, st));
+        off += a.second;
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    StateHeader hd{};
+    hd.magic = kStateMagic;
+    hd.version = kStateVersion;
+    hd.n = s->n;
+    hd.n_groups = s->n_groups;
+    hd.K = s->K;
+    hd.ncell = s->cells ? cur.ncell : 0;
+    hd.cap = s->cells ? cur.cap : 0;
+    hd.precision = s->precision;
+    for (int k = 0; k < 3; k++) {
+        hd.box[k] = cur.L[k];
+        hd.M[k] = cur.M[k];
+    }
+    hd.energy = cur.energy;
+    hd.beta_scale = cur.beta_scale;
+    hd.sum_du = cur.sum_du;
+    hd.e_acc_hi = cur.e_acc_hi;
+    hd.e_acc_lo = cur.e_acc_lo;
+    hd.q_valid = cur.q_valid;
+    hd.q_since = cur.q_since;
+    hd.moves = cur.moves;
+    hd.accepted = cur.accepted;
+    hd.pair_evals = cur.pair_evals;
+    hd.k_updates = cur.k_updates;
+    hd.cycles = cur.cycles;
+    std::memcpy(out, &hd, sizeof hd);
+    return FAU_OK;
+}
+
+int fau_sys_load_state(fau_sys* s, const void* buf, size_t bytes)
+{
+    if (!s || !buf) return fail(FAU_ERR_ARG, "null argument");
+    if (s->pending) return fail(FAU_ERR_STATE, "a trial is pending (fau_commit_pending first)");
+    if (bytes < sizeof(StateHeader)) return fail(FAU_ERR_ARG, "state of %zu bytes is too short", bytes);
+    StateHeader hd;
+    std::memcpy(&hd, buf, sizeof hd);
+    if (hd.magic != kStateMagic || hd.version != kStateVersion) return fail(FAU_ERR_ARG, "not a system state");
+    const int ncell = s->cells ? s->h.ncell : 0;
+    if (hd.n != s->n || hd.n_groups != s->n_groups || hd.K != s->K || hd.ncell != ncell ||
+        hd.precision != s->precision)
+        return fail(FAU_ERR_ARG, "state of another system shape (particles, groups, k-vectors or cells)");
+    for (int k = 0; k < 3; k++)
+        if (hd.box[k] != s->h.L[k])
+            return fail(FAU_ERR_ARG, "state of another box: make the system with the saved box");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = s->ctx->stream;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (s->cells && hd.cap != s->h.cap) { // the saved list had grown: the same capacity first
+        int rc = rebuild_cells(s, hd.cap);
+        if (rc) return rc;
+    }
+    size_t need = 0;
+    fau_sys_state_size(s, &need);
+    if (bytes != need) return fail(FAU_ERR_ARG, "state of %zu bytes, %zu expected", bytes, need);
+    const char* in = static_cast<const char*>(buf);
+    size_t off = sizeof(StateHeader);
+    for (auto& a : state_arrays(s)) {
+        if (a.second) CUDA_TRY(cudaMemcpyAsync(a.first, in + off, a.second, cudaMemcpyHostToDevice, st));
+        off += a.second;
+    }
+    DevSys cur;
+    CUDA_TRY(cudaMemcpyAsync(&cur, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    cur.energy = hd.energy;
+    cur.beta_scale = hd.beta_scale;
+    cur.sum_du = hd.sum_du;
+    cur.e_acc_hi = hd.e_acc_hi;
+    cur.e_acc_lo = hd.e_acc_lo;
+    cur.q_valid = hd.q_valid;
+    cur.q_since = hd.q_since;
+    for (int k = 0; k < 3; k++) cur.M[k] = hd.M[k];
+    cur.moves = hd.moves;
+    cur.accepted = hd.accepted;
+    cur.pair_evals = hd.pair_evals;
+    cur.k_updates = hd.k_updates;
+    cur.cycles = hd.cycles;
+    cur.err = 0;
+    CUDA_TRY(cudaMemcpyAsync(s->d, &cur, sizeof(DevSys), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    s->h.energy = hd.energy;
+    s->h.beta_scale = hd.beta_scale;
+    return pull_state(s);
+}
+
 int fau_sys_destroy(fau_sys* s)
 {
     if (!s) return FAU_OK;
@@ -1945,6 +2094,28 @@ int fau_get_q(fau_sys* s, double* q)
     CUDA_TRY(launch_fold_q(s->d, s->K, s->ctx->stream));
     CUDA_TRY(cudaMemcpyAsync(q, s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_get_kvectors(fau_sys* s, int* n_out, double* k_out, double* ak_out)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null argument");
+    if (s->K == 0) return FAU_OK;
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    std::vector<int> kn(s->K);
+    std::vector<double> ak(s->K);
+    CUDA_TRY(cudaMemcpyAsync(kn.data(), s->h.kn, sizeof(int) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(ak.data(), s->h.Akd, sizeof(double) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    for (int k = 0; k < s->K; k++) {
+        const int n[3] = {(kn[k] & 0xff) - 128, ((kn[k] >> 8) & 0xff) - 128, ((kn[k] >> 16) & 0xff) - 128};
+        for (int d = 0; d < 3; d++) {
+            if (n_out) n_out[3 * k + d] = n[d];
+            // (2 pi) (n / L), as PolicyIonIon::updateBox forms it
+            if (k_out) k_out[3 * k + d] = 2 * kPi * (double(n[d]) / s->h.L[d]);
+        }
+        if (ak_out) ak_out[k] = ak[k];
+    }
     return FAU_OK;
 }
 

@@ -53,23 +53,26 @@ struct MoveShared {
 // cell coordinates of a position: fixed-point fast path; the FP64 reference formula
 // floor((x + L/2) / cell_len) (src/celllistimpl.h:139-143, src/sasa.cpp:466-468)
 // decides within 2^-18 of a cell boundary, so binning is bit-exact.
+// one axis d: x the FP64 coordinate, u its fixed-point record
+__device__ __forceinline__ int cell_coord1(const DevSys& S, double x, uint32_t u, int d)
+{
+    const uint32_t s = u + 0x80000000u;
+    const unsigned long long prod = (unsigned long long)s * (unsigned long long)S.cdim[d];
+    int v = (int)(prod >> 32);
+    const uint32_t frac = (uint32_t)prod;
+    if (frac < (1u << 14) || frac > 0xFFFFFFFFu - (1u << 14)) {
+        const double t = __dadd_rn(x, __dmul_rn(0.5, S.L[d]));
+        v = (int)floor(__ddiv_rn(t, S.cell_len[d]));
+    }
+    if (v < 0) v += S.cdim[d] * (abs(v) / S.cdim[d] + 1);
+    else if (v >= S.cdim[d]) v -= S.cdim[d] * (v / S.cdim[d]);
+    return v;
+}
 __device__ __forceinline__ void cell_coords(const DevSys& S, const double* x, uint4 r, int* c)
 {
     const uint32_t u[3] = {r.x, r.y, r.z};
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const uint32_t s = u[d] + 0x80000000u;
-        const unsigned long long prod = (unsigned long long)s * (unsigned long long)S.cdim[d];
-        int v = (int)(prod >> 32);
-        const uint32_t frac = (uint32_t)prod;
-        if (frac < (1u << 14) || frac > 0xFFFFFFFFu - (1u << 14)) {
-            const double t = __dadd_rn(x[d], __dmul_rn(0.5, S.L[d]));
-            v = (int)floor(__ddiv_rn(t, S.cell_len[d]));
-        }
-        if (v < 0) v += S.cdim[d] * (abs(v) / S.cdim[d] + 1);
-        else if (v >= S.cdim[d]) v -= S.cdim[d] * (v / S.cdim[d]);
-        c[d] = v;
-    }
+    for (int d = 0; d < 3; d++) c[d] = cell_coord1(S, x[d], u[d], d);
 }
 __device__ __forceinline__ int cell_index(const DevSys& S, const int* c)
 {
@@ -159,7 +162,9 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
     p.dr[2] = f2d_bits(z * len);
     const unsigned long long v = ((unsigned long long)(c2.x >> 5) << 26) | (c2.y >> 6);
     p.u = u53_bits(v);
-    p.uf = (float)(uint32_t)(v >> 29) * 5.9604644775390625e-8f; // top 24 bits, 2^-24
+    // u truncated to float (relative error below 2^-23, as for host proposals): an absolute 2^-24
+    // grid would let the FP32 prefilter misjudge u within 2^-24 of a threshold below 6e-4
+    p.uf = d2f_trunc01(p.u);
     p.rotate = false;
     p.quat[0] = 1.0;
     p.quat[1] = p.quat[2] = p.quat[3] = 0.0;

@@ -120,6 +120,10 @@ struct DevSys {
     int cdim[3], ncell;
     int off_min[3], off_max[3];
     int cap, pad2;
+    // reciprocal multipliers of cdim[0] and cdim[0] cdim[1] (cell index -> coordinates by
+    // multiply-high, exact while ncell times the divisor stays below 2^32); 0: divide.  Set by the
+    // pipelined kernel in its shared copy of the descriptor
+    uint32_t cmag0, cmag01;
     double cell_len[3];
     int* cell_cnt;
     uint4* cell_rec;

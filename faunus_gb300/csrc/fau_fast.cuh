@@ -35,6 +35,8 @@ namespace fau {
 constexpr int kFastEntries = 64; // cells listed per move: union box (<= 4x4x4) or two stencils (<= 54)
 constexpr int kFastRing = 64;    // host proposals staged in shared memory, refilled 32 at a time
 constexpr int kFastFlushAccepts = 256; // FP32 pending Q deltas flushed to the FP64 master every N accepts
+constexpr int kFastStagePerThread = 4; // pair records staged in shared memory per compute thread and round
+__host__ __device__ constexpr int fast_stage_items(int nwc) { return kFastStagePerThread * 32 * nwc; }
 
 enum : int { FC_SELF = 1, FC_CELLS = 2 };
 constexpr int kFastUnsupported = -2; // proposal kind this kernel does not handle (FAU_MOVE_NONE is -1)
@@ -99,31 +101,26 @@ __device__ __forceinline__ void cp_async_wait()
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <bool PHILOX>
-__device__ __forceinline__ void fast_proposal(const DevSys& S, const ChainArgs& A, const fau_proposal* ring, long long s,
-                                              unsigned long long ctr0, uint32_t sys_id, float dp_f, Ahead& a)
+// A staged proposal (the single-atom fields of fau_proposal).
+struct FastProp {
+    int kind, index;
+    double dr[3];
+    double u;
+};
+
+// The proposal of move s from the ring into `a` (producer lane 0).  Host proposals are checked
+// where they are read: anything but an in-range single-atom move or an empty move (molecular
+// moves run in the chain kernel) ends the chain with FAU_ERR_ARG.
+__device__ __forceinline__ void fast_proposal(const DevSys& S, const FastProp* ring, long long s, Ahead& a)
 {
-    if (PHILOX) {
-        const Proposal p = philox_proposal(S, ctr0 + (unsigned long long)s, sys_id, A.seed, dp_f, 0.0, false);
-        a.kind = p.kind;
-        a.i = p.index;
+    const FastProp& f = ring[s % kFastRing];
+    const bool ok = f.kind == FAU_MOVE_NONE || (f.kind == FAU_MOVE_ATOMIC && f.index >= 0 && f.index < S.n);
+    a.kind = ok ? f.kind : kFastUnsupported;
+    a.i = ok ? f.index : 0;
 #pragma unroll
-        for (int d = 0; d < 3; d++) a.dr[d] = p.dr[d];
-        a.u = p.u;
-        a.uf = p.uf;
-    }
-    else {
-        const fau_proposal& f = ring[s % kFastRing];
-        // checked where it is read: anything but an in-range single-atom move or an empty move
-        // (molecular moves run in the chain kernel) ends the chain with FAU_ERR_ARG
-        const bool ok = f.kind == FAU_MOVE_NONE || (f.kind == FAU_MOVE_ATOMIC && f.index >= 0 && f.index < S.n);
-        a.kind = ok ? f.kind : kFastUnsupported;
-        a.i = ok ? f.index : 0;
-#pragma unroll
-        for (int d = 0; d < 3; d++) a.dr[d] = f.dr[d];
-        a.u = f.u;
-        a.uf = d2f_trunc01(f.u);
-    }
+    for (int d = 0; d < 3; d++) a.dr[d] = f.dr[d];
+    a.u = f.u;
+    a.uf = d2f_trunc01(f.u);
 }
 
 // start the copies of the moved particle's state (lane 0; complete after the next wait)
@@ -218,10 +215,16 @@ static __device__ __forceinline__ void fast_scalar(const DevSys& S, FastMove& m,
     if (cells) {
         const int co = a.cell;
         int c[3], cn[3];
-        // the old cell's coordinates: the binning of the old position, checked against the cell
-        // the particle is listed in (divisions only if they ever differ)
-        cell_coords(S, xo, ro, c);
-        if (cell_index(S, c) != co) {
+        // the old cell's coordinates: those of the cell the particle is listed in
+        if (S.cmag01) {
+            const uint32_t c01 = (uint32_t)(S.cdim[0] * S.cdim[1]);
+            const uint32_t z = __umulhi((uint32_t)co, S.cmag01), r = (uint32_t)co - z * c01;
+            const uint32_t y = __umulhi(r, S.cmag0);
+            c[0] = (int)(r - y * (uint32_t)S.cdim[0]);
+            c[1] = (int)y;
+            c[2] = (int)z;
+        }
+        else {
             c[0] = co % S.cdim[0];
             c[1] = (co / S.cdim[0]) % S.cdim[1];
             c[2] = co / (S.cdim[0] * S.cdim[1]);
@@ -372,8 +375,34 @@ __device__ __forceinline__ bool fast_decide(FF s, int flags, double du_surf, boo
     return metropolis(x, u);
 }
 
+// The kernel's static shared memory, declared once in the kernel: the body is inlined twice
+// (splined and unsplined systems), and __shared__ variables declared in it would be allocated
+// once per inlined copy.
+template <int NWC>
+struct __align__(16) FastShared {
+    DevSys Ssh;             // the system descriptor
+    FastMove mvb[3];        // move t, t+1 and the one the producer fills
+    Ahead ahs[2];           // move s: ahs[s & 1]
+    CommitPre cps[2];       // move s: cps[s & 1]
+    FF red_a[2][NWC];
+    int red_f[2][NWC];
+    float itq[kMaxITypes];
+    double itqd[kMaxITypes];
+    FastProp ring[kFastRing]; // proposals, filled 32 at a time by the producer warp
+    unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
+    int sh_up;                // the time budget is spent
+    unsigned long long red_u[NWC][2];
+    // phase timers (profiling only; every phase still runs), accumulated by thread 0 (producer) and
+    // thread 32 (first compute warp): 0 commit data, 1 prepare t+1, 2 copies of t+2, 3 barrier 1,
+    // 4 decision, 5 commit, 6 conflict barrier | 7 stage, 8 Ewald, 9 pairs, 10 warp sums,
+    // 11 barrier 1, 12 decision, 13 Q update, 14 conflict barrier | 15 moves | inside prepare:
+    // 16 scalar part, 17 phase tables, 18 cell entries | 21 proposal
+    unsigned long long tsm[kFastPhaseSlots];
+    ProdState ps;
+};
+
 template <int NWC, bool PHILOX, bool SPL>
-__device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
+__device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<NWC>& sh)
 {
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
     const long long t_start = clock64();
@@ -381,7 +410,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
     // the system descriptor in shared memory: its fields sit on every move's dependent
     // chain, and global copies fall out of L1 under the cell-list traffic
     DevSys& G = *A.sys[blockIdx.x];
-    __shared__ __align__(16) DevSys Ssh;
+    DevSys& Ssh = sh.Ssh;
     for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += NT)
         reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
     __syncthreads();
@@ -398,25 +427,24 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
     int2* kaf = reinterpret_cast<int2*>(dlt + K);     // {table entries of nx, ny, nz (8 bits each), (2 pi lB / V) A_k}
     float4* tabs = reinterpret_cast<float4*>(kaf + K); // 3 slots x 3 axes x TS phase-table entries {mid, h}
     PairF* pt = reinterpret_cast<PairF*>(tabs + 3 * 3 * TS);
+    // a round of pair records (cell slots, or particles without cells), copied in by the compute
+    // thread that owns the slot: warp w's items are w's lanes' (no other warp reads them)
+    uint4* stage = reinterpret_cast<uint4*>(pt + nt * nt);
+    constexpr int KST = fast_stage_items(NWC), KI = kFastStagePerThread;
 
-    __shared__ FastMove mvb[3];
-    __shared__ Ahead ahs[2];       // move s: ahs[s & 1]
-    __shared__ CommitPre cps[2];   // move s: cps[s & 1]
-    __shared__ FF red_a[2][NWC];
-    __shared__ int red_f[2][NWC];
-    __shared__ float itq[kMaxITypes];
-    __shared__ double itqd[kMaxITypes];
-    __shared__ fau_proposal ring[PHILOX ? 1 : kFastRing];
-    __shared__ unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
-    __shared__ int sh_up;                // the time budget is spent
-    __shared__ unsigned long long red_u[NWC][2];
-    // phase timers (profiling only; every phase still runs), accumulated by thread 0 (producer) and
-    // thread 32 (first compute warp): 0 commit data, 1 prepare t+1, 2 copies of t+2, 3 barrier 1,
-    // 4 decision, 5 commit, 6 conflict barrier | 7 preload, 8 Ewald, 9 pairs, 10 warp sums,
-    // 11 barrier 1, 12 decision, 13 Q update, 14 conflict barrier | 15 moves | inside prepare:
-    // 16 scalar part, 17 phase tables, 18 cell entries | 19 pairs: preloaded part | 21 proposal
-    __shared__ unsigned long long tsm[kFastPhaseSlots];
-    __shared__ ProdState ps;
+    auto& mvb = sh.mvb;
+    auto& ahs = sh.ahs;
+    auto& cps = sh.cps;
+    auto& red_a = sh.red_a;
+    auto& red_f = sh.red_f;
+    auto& itq = sh.itq;
+    auto& itqd = sh.itqd;
+    auto& ring = sh.ring;
+    auto& sh_t0 = sh.sh_t0;
+    auto& sh_up = sh.sh_up;
+    auto& red_u = sh.red_u;
+    auto& tsm = sh.tsm;
+    auto& ps = sh.ps;
     const bool timing = A.phase_cycles != nullptr && (tid == 0 || tid == 32);
     if (tid < kFastPhaseSlots) tsm[tid] = 0;
     auto tick = [&](int slot) {
@@ -446,6 +474,12 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
 
     const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
     if (tid == 0) {
+        // cell index -> coordinates by multiply-high: q = umulhi(n, floor((2^32 - 1) / d) + 1) is
+        // n / d exactly for n d < 2^32 (n < ncell)
+        const unsigned long long d0 = (unsigned long long)Ssh.cdim[0], d01 = d0 * (unsigned long long)Ssh.cdim[1];
+        const bool exact = (Ssh.flags & SYS_CELLS) && (unsigned long long)Ssh.ncell * d01 < (1ull << 32);
+        Ssh.cmag0 = exact ? (uint32_t)(0xFFFFFFFFull / d0 + 1) : 0u;
+        Ssh.cmag01 = exact ? (uint32_t)(0xFFFFFFFFull / d01 + 1) : 0u;
         ps.poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
         ps.sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
         ps.ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
@@ -467,14 +501,29 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
     const int cap_shift = cells ? __ffs(cap) - 1 : 0;
     const float beta_f = (float)S.beta_scale;
 
-    // proposals [s0, s0 + 32) into their ring slots (host proposals)
+    // proposals [s0, s0 + 32) into their ring slots, lane w taking move s0 + w: the host's
+    // (single-atom fields of fau_proposal), or device proposals drawn here, all 32 at once --
+    // philox_proposal's single-atom arithmetic (fau_chain.cuh), so both kernels make the same moves
     auto ring_fill = [&](long long s0) {
-        const long long e = s0 + 32 < nmoves ? s0 + 32 : nmoves;
-        if (e <= s0) return;
-        const int words = (int)(e - s0) * (int)(sizeof(fau_proposal) / 8);
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(A.props + ps.poff + s0);
-        unsigned long long* dst = reinterpret_cast<unsigned long long*>(ring + (s0 % kFastRing));
-        for (int w = lane; w < words; w += 32) dst[w] = src[w];
+        const long long s = s0 + lane;
+        if (s >= nmoves) return;
+        FastProp& f = ring[s % kFastRing];
+        if (PHILOX) {
+            const Proposal p = philox_proposal(S, ps.ctr0 + (unsigned long long)s, ps.sys_id, A.seed, ps.dp_f, 0.0, false);
+            f.kind = p.kind;
+            f.index = p.index;
+#pragma unroll
+            for (int d = 0; d < 3; d++) f.dr[d] = p.dr[d];
+            f.u = p.u;
+        }
+        else {
+            const fau_proposal& h = A.props[ps.poff + s];
+            f.kind = h.kind;
+            f.index = h.index;
+#pragma unroll
+            for (int d = 0; d < 3; d++) f.dr[d] = h.dr[d];
+            f.u = h.u;
+        }
     };
 
     unsigned long long n_pairs = 0;
@@ -482,19 +531,19 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
     int since_flush = S.q_since, q_pending = S.q_valid;
 
     // move 0: its scalar part, then tables and cell entries by every thread
-    if (producer && !PHILOX) {
+    if (producer) {
         ring_fill(0);
         ring_fill(32);
         __syncwarp();
     }
     if (producer && lane == 0 && nmoves > 0) {
-        fast_proposal<PHILOX>(S, A, ring, 0, ps.ctr0, ps.sys_id, ps.dp_f, ahs[0]);
+        fast_proposal(S, ring, 0, ahs[0]);
         fast_load(S, ahs[0]);
         cp_async_commit();
         cp_async_wait<0>();
         fast_scalar(S, mvb[0], ahs[0], nullptr, itq, itqd, nullptr);
         if (nmoves > 1) {
-            fast_proposal<PHILOX>(S, A, ring, 1, ps.ctr0, ps.sys_id, ps.dp_f, ahs[1]);
+            fast_proposal(S, ring, 1, ahs[1]);
             fast_load(S, ahs[1]);
         }
         fast_commit_loads(S, mvb[0], cps[0]);
@@ -518,7 +567,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
         const int rb = (int)(t & 1);
         if (timing && tid == 0) tsm[15]++;
         if (producer) {
-            if (!PHILOX && (t & 31) == 0 && t >= 32) {
+            if ((t & 31) == 0 && t >= 32) {
                 ring_fill(t + 32); // proposals [t+32, t+64): first read at move t+30
                 __syncwarp();
             }
@@ -565,7 +614,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
                     tick(1);
                     if (t + 2 < nmoves) {
                         Ahead& a2 = ahs[t & 1];
-                        fast_proposal<PHILOX>(S, A, ring, t + 2, ps.ctr0, ps.sys_id, ps.dp_f, a2);
+                        fast_proposal(S, ring, t + 2, a2);
                         tick(21);
                         fast_load(S, a2);
                     }
@@ -580,20 +629,20 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
             const uint4 ro = m.ro, rn = m.rn;
             const int ti = rn.w >> 24;
             const int n_items = cells ? (m.nue << cap_shift) : S.n;
-            auto load_item = [&](int it, uint4& rj, uint32_t& ent) {
-                if (cells) {
-                    ent = m.ent[it >> cap_shift];
-                    rj = S.cell_rec[(size_t)(ent & kEntCell) * cap + (it & (cap - 1))];
-                }
-                else {
-                    ent = kEntNew | kEntOld;
-                    rj = S.rec[it];
-                }
+            auto item_src = [&](int it) -> const uint4* {
+                return cells ? S.cell_rec + (size_t)(m.ent[it >> cap_shift] & kEntCell) * cap + (it & (cap - 1))
+                             : S.rec + it;
             };
-            uint4 r0 = make_uint4(0, 0, 0, kEmptySlot), r1 = r0;
-            uint32_t e0 = 0, e1 = 0;
-            if (ctid < n_items) load_item(ctid, r0, e0);
-            if (ctid + NTC < n_items) load_item(ctid + NTC, r1, e1);
+            // this thread's records of a round [r0, r0 + KST): asynchronous copies into the stage
+            auto stage_round = [&](int r0) {
+#pragma unroll
+                for (int k = 0; k < KI; k++) {
+                    const int it = r0 + ctid + k * NTC;
+                    if (it < n_items) cp_async(&stage[it - r0], item_src(it), 16);
+                }
+                cp_async_commit();
+            };
+            stage_round(0); // lands while the Ewald loop runs
             tick(7);
             // ---- Ewald: one k-vector per thread and step, two independent accumulators.  The
             // last accepted move's Q(k) change (State::sync trial -> accepted) is folded in here,
@@ -648,55 +697,61 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
             int flags = 0;
             tick(8);
 
-            // ---- pairs: items in rounds of two per lane; the occupied ones (non-empty slot, not the
-            // moved particle, in a stencil) are compacted across the warp and each lane evaluates
-            // one (pair, state) task, so a sparse neighbourhood costs one pass, not one per item
+            // ---- pairs: the staged records of a round; the occupied ones (non-empty slot, not the
+            // moved particle, in a stencil) are counted per warp and each lane evaluates one
+            // (pair, state) task, reading its record from the stage, so a sparse neighbourhood costs
+            // one pass per round, not one per slot
             const unsigned FULL = 0xffffffffu;
             const int wbase = (warp - 1) * 32;
-            for (int rr = 0; 2 * rr * NTC < n_items; rr++) {
-                const int ita = ctid + 2 * rr * NTC, itb = ita + NTC;
-                uint4 ra, rb2;
-                uint32_t ea = 0, eb = 0;
-                if (rr == 0) {
-                    ra = r0;
-                    ea = e0;
-                    rb2 = r1;
-                    eb = e1;
+            for (int r0 = 0; r0 < n_items; r0 += KST) {
+                if (r0 > 0) { // beyond the first round (large cells or all pairs): stage the next round
+                    __syncwarp();
+                    stage_round(r0);
                 }
-                else {
-                    if (rr == 1) tick(19);
-                    ra = rb2 = make_uint4(0, 0, 0, kEmptySlot);
-                    if (ita < n_items) load_item(ita, ra, ea);
-                    if (itb < n_items) load_item(itb, rb2, eb);
+                cp_async_wait<0>();
+                __syncwarp(); // every lane's copies visible to the warp
+                unsigned occ[KI];
+                int nv = 0;
+#pragma unroll
+                for (int k = 0; k < KI; k++) {
+                    const int it = r0 + ctid + k * NTC;
+                    bool o = false;
+                    if (it < n_items) {
+                        const uint4 r = stage[it - r0];
+                        const uint32_t e = cells ? m.ent[it >> cap_shift] : (kEntNew | kEntOld);
+                        o = r.w != kEmptySlot && (e & (kEntNew | kEntOld)) && (cells ? (int)(r.w & 0xFFFFFFu) : it) != i;
+                    }
+                    occ[k] = __ballot_sync(FULL, o);
+                    nv += __popc(occ[k]);
                 }
-                auto occupied = [&](const uint4& r, uint32_t e, int it) {
-                    if (it >= n_items || r.w == kEmptySlot || !(e & (kEntNew | kEntOld))) return false;
-                    return (cells ? (int)(r.w & 0xFFFFFFu) : it) != i;
-                };
-                const unsigned ba = __ballot_sync(FULL, occupied(ra, ea, ita));
-                const unsigned bb = __ballot_sync(FULL, occupied(rb2, eb, itb));
-                const int na = __popc(ba), nv = na + __popc(bb);
                 for (int base = 0; base < 2 * nv; base += 32) {
                     const int task = base + lane, q = task >> 1, st = task & 1;
-                    const bool second = q >= na;
-                    int src = 0;
-                    if (q < nv) src = (int)__fns(second ? bb : ba, 0, (second ? q - na : q) + 1);
-                    // the source lane's item (both of its items travel; this lane picks one)
-                    const uint4 xa = make_uint4(__shfl_sync(FULL, ra.x, src), __shfl_sync(FULL, ra.y, src),
-                                                __shfl_sync(FULL, ra.z, src), __shfl_sync(FULL, ra.w, src));
-                    const uint4 xb = make_uint4(__shfl_sync(FULL, rb2.x, src), __shfl_sync(FULL, rb2.y, src),
-                                                __shfl_sync(FULL, rb2.z, src), __shfl_sync(FULL, rb2.w, src));
-                    const uint32_t xea = __shfl_sync(FULL, ea, src), xeb = __shfl_sync(FULL, eb, src);
-                    const uint4 rj = second ? xb : xa;
-                    const uint32_t ent = second ? xeb : xea;
-                    if (q < nv && (ent & (st ? kEntOld : kEntNew))) {
-                        const int j = cells ? (int)(rj.w & 0xFFFFFFu) : wbase + src + (2 * rr + (second ? 1 : 0)) * NTC;
-                        const int pidx = ti * nt + (int)(rj.w >> 24);
-                        const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
-                                                               st ? m.xo : m.xn, j, nullptr, st == 0);
-                        ff_add(accp, st ? -o.u : o.u);
-                        flags |= o.flags;
-                        n_pairs++;
+                    if (q < nv) {
+                        // the q-th occupied record of this warp's round: its mask k and rank in it
+                        int qq = q, k = 0;
+                        unsigned mk = occ[0];
+#pragma unroll
+                        for (int kk = 1; kk < KI; kk++) {
+                            const int c = __popc(mk);
+                            if (k == kk - 1 && qq >= c) {
+                                qq -= c;
+                                k = kk;
+                                mk = occ[kk];
+                            }
+                        }
+                        const int src = (int)__fns(mk, 0, qq + 1);
+                        const int it = r0 + wbase + src + k * NTC;
+                        const uint4 rj = stage[it - r0];
+                        const uint32_t ent = cells ? m.ent[it >> cap_shift] : (kEntNew | kEntOld);
+                        if (ent & (st ? kEntOld : kEntNew)) {
+                            const int j = cells ? (int)(rj.w & 0xFFFFFFu) : it;
+                            const int pidx = ti * nt + (int)(rj.w >> 24);
+                            const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
+                                                                   st ? m.xo : m.xn, j, nullptr, st == 0);
+                            ff_add(accp, st ? -o.u : o.u);
+                            flags |= o.flags;
+                            n_pairs++;
+                        }
                     }
                 }
             }
@@ -822,7 +877,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
                 if (producer && lane == 0) {
                     Ahead& an = ahs[(t + 1) & 1];
                     cp_async_wait<0>();
-                    fast_proposal<PHILOX>(S, A, ring, t + 1, ps.ctr0, ps.sys_id, ps.dp_f, an);
+                    fast_proposal(S, ring, t + 1, an);
                     fast_load(S, an);
                     cp_async_commit();
                     cp_async_wait<0>();
@@ -894,15 +949,17 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A)
 template <int NWC, bool PHILOX>
 __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
 {
-    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true>(A);
-    else fast_chain_body<NWC, PHILOX, false>(A);
+    __shared__ FastShared<NWC> sh;
+    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true>(A, sh);
+    else fast_chain_body<NWC, PHILOX, false>(A, sh);
 }
 
-// dynamic shared memory of the pipelined kernel for K k-vectors, table size nc
-__host__ __device__ inline size_t fast_smem_bytes(int K, int nc, int nt)
+// dynamic shared memory of the pipelined kernel for K k-vectors, table size nc, nt classes and
+// NWC compute warps (their staged pair records come last)
+__host__ __device__ inline size_t fast_smem_bytes(int K, int nc, int nt, int nwc)
 {
     return (size_t)K * (sizeof(float4) + sizeof(float2) + sizeof(int2)) + (size_t)3 * 3 * (2 * nc + 1) * sizeof(float4) +
-           (size_t)nt * nt * sizeof(PairF);
+           (size_t)nt * nt * sizeof(PairF) + (size_t)fast_stage_items(nwc) * sizeof(uint4);
 }
 
 template <int NWC, bool PH>
@@ -910,7 +967,7 @@ cudaError_t launch_fast_inst(const ChainArgs& a, int nblocks, int K, int nc, int
 {
     // the dynamic allowance is raised on demand, never inside a stream capture: callers prepare first
     static size_t granted = 0;
-    const size_t smem = fast_smem_bytes(K, nc, nt);
+    const size_t smem = fast_smem_bytes(K, nc, nt, NWC);
     if (smem > granted || granted == 0) {
         cudaError_t e = cudaFuncSetAttribute(fast_chain_kernel<NWC, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

@@ -392,7 +392,7 @@ cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int thr
 size_t fast_smem_bytes_total(int K, int nc, int nt)
 {
     // dynamic part + the kernel's static shared memory (move slots, proposal ring, partials)
-    return fast_smem_bytes(K, nc, nt) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
+    return fast_smem_bytes(K, nc, nt, 8) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
 }
 
 static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox,

@@ -14,6 +14,11 @@
 // share it and it keeps the last call's contents; each call overwrites the
 // first n entries before reading them, so nothing has to start at zero.  Calls
 // that overlap on the GPU (different streams or host threads) race on it.
+//
+// The array's device address is looked up once per CUDA context (the first call
+// on a device, or the first after that device's context was destroyed and made
+// again, e.g. by cudaDeviceReset): make such a call before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -29,7 +34,39 @@ static __device__ __align__(256) double g_noalloc_partial[FAU_NOALLOC_MAX_PARTIC
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-double* g_partial_ptr[kMaxDevices] = {nullptr}; // device address of the array, per device
+// device address of the array per device, and the id of the context it was looked up in: a
+// context made again (after cudaDeviceReset) loads the module again, possibly elsewhere
+double* g_partial_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_partial_ctx[kMaxDevices] = {0};
+
+// the unique id of the calling thread's current context (cuCtxGetId through the runtime's
+// driver entry points, so that the library needs no link against the driver library); 0 if
+// the driver does not provide it
+unsigned long long current_context_id()
+{
+    using get_current_t = CUresult (*)(CUcontext*);
+    using get_id_t = CUresult (*)(CUcontext, unsigned long long*);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<get_current_t>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<get_id_t>(f);
+        cudaGetLastError();
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS) return id;
+    return 0;
+}
 
 // u(r) of one pair, FP64, terms in the order coulomb, LJ, WCA, HS (as the oracle and
 // CombinedPairPotential::operator() src/potentials_base.h:234-240)
@@ -74,7 +111,10 @@ __global__ void noalloc_pair_kernel(fau_nonbonded_args a, double* partial)
         for (int j = i + 1 + threadIdx.x; j < a.n_particles; j += blockDim.x) {
             double d[3];
             for (int k = 0; k < 3; k++) {
-                const double v = fabs(xi[k] - a.pos[3 * j + k]);
+                double v = fabs(xi[k] - a.pos[3 * j + k]);
+                // positions outside [-L/2, L/2] (an engine that has not wrapped them): whole box
+                // lengths first (fmod is exact), then the reference's single subtraction
+                if (v >= a.box[k]) v = fmod(v, a.box[k]);
                 d[k] = v - (v > half[k] ? a.box[k] : 0.0);
             }
             const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
@@ -126,7 +166,15 @@ extern "C" int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* a, double*
         return fau_internal_fail(FAU_ERR_ARG, "LJ/WCA need sigma2 and eps4");
     if ((a->pair_terms & FAU_PAIR_HS) && !a->hs_sigma2) return fau_internal_fail(FAU_ERR_ARG, "HS needs hs_sigma2");
     for (int k = 0; k < 3; k++)
-        if (!(a->box[k] > 0.0)) return fau_internal_fail(FAU_ERR_ARG, "box lengths must be positive");
+        if (!(a->box[k] > 0.0) || !std::isfinite(a->box[k]))
+            return fau_internal_fail(FAU_ERR_ARG, "box lengths must be positive and finite");
+    // the settings the system entry point (fau_sys_create) also rejects
+    if ((a->pair_terms & FAU_PAIR_COULOMB) && a->coulomb_type != FAU_COUL_PLAIN && !(a->coulomb_cutoff > 0.0))
+        return fau_internal_fail(FAU_ERR_ARG, "coulomb_type cut or ewald needs a positive coulomb_cutoff");
+    if ((a->pair_terms & FAU_PAIR_COULOMB) && a->coulomb_type == FAU_COUL_EWALD && !(a->coulomb_alpha >= 0.0))
+        return fau_internal_fail(FAU_ERR_ARG, "coulomb_alpha must be >= 0");
+    if (std::isnan(a->pair_cutoff))
+        return fau_internal_fail(FAU_ERR_ARG, "pair_cutoff is NaN (<= 0 means no truncation)");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
@@ -134,15 +182,20 @@ extern "C" int fau_nonbonded_energy_noalloc(const fau_nonbonded_args* a, double*
     }
     double* partial = nullptr;
     {
-        // set-up, once per device with that device current: the host-side name of the
-        // array is not a device address, so look the address up and keep it
+        // set-up, once per device and context with that device current: the host-side name of
+        // the array is not a device address, so look the address up and keep it
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_partial_ptr[dev]) {
-            const cudaError_t e = cudaGetSymbolAddress((void**)&g_partial_ptr[dev], g_noalloc_partial);
+        const unsigned long long cid = current_context_id();
+        if (!g_partial_ptr[dev] || cid != g_partial_ctx[dev]) {
+            double* ptr = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_partial);
             if (e != cudaSuccess) {
                 g_partial_ptr[dev] = nullptr;
                 return fau_internal_fail(FAU_ERR_CUDA, cudaGetErrorString(e));
             }
+            g_partial_ptr[dev] = ptr;
+            // the context is current now (the lookup made it so if it was not)
+            g_partial_ctx[dev] = current_context_id();
         }
         partial = g_partial_ptr[dev];
     }

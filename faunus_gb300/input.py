@@ -29,6 +29,7 @@ Supported subset (anything else raises NotImplementedError naming the key):
 """
 from __future__ import annotations
 
+import base64
 import json
 import math
 from dataclasses import dataclass, field
@@ -38,6 +39,7 @@ from typing import Any, Dict, List, Optional
 import numpy as np
 
 from . import _capi as A
+from . import ubjson
 from . import yason
 from .system import (AVOGADRO, SystemSpec, bjerrum_length, coulomb_scheme, group_cutoff, kjmol_to_kt,
                      pressure_kt, splined)
@@ -72,8 +74,12 @@ def _items(lst, what: str):
 def _read(src) -> dict:
     if isinstance(src, dict):
         return src
+    if isinstance(src, (bytes, bytearray)):
+        return ubjson.loads(bytes(src))
     if isinstance(src, Path) or (isinstance(src, str) and "\n" not in src and Path(src).exists()):
         p = Path(src)
+        if p.suffix == ".ubj":  # Universal Binary JSON state file (src/faunus.cpp:430-470)
+            return ubjson.loads(p.read_bytes())
         text = p.read_text()
         return json.loads(text) if p.suffix == ".json" else yason.loads(text)
     text = str(src)
@@ -495,8 +501,39 @@ def state_json(setup: Setup, positions: np.ndarray, box: np.ndarray, mass_center
             "particles": parts, "reactionlist": [], "implicit_reservoir": []}
 
 
-def save_state(setup: Setup, system, path) -> dict:
-    """Write the state of a resident System (positions, box, mass centres) as JSON."""
+ENGINE_NAME = "Mersenne Twister (std::mt19937)"
+DEVICE_STATE_KEY = "fau-device-state"
+
+
+def save_state(setup: Setup, system, path, movegen=None, device_state: bool = True) -> dict:
+    """SaveState (src/analysis.cpp:586-690): the state of a resident System -- positions, box,
+    mass centres -- as JSON, or as Universal Binary JSON for a `.ubj` path.  With the move
+    generator, its two mt19937 engines as "random-move" and "random-global" (saverandom: the
+    reference's Random::to_json form, src/random.cpp:35-46).  device_state adds the system's
+    exact device state (base64 of fau_sys_save_state, a key the reference ignores), from which
+    resume_state continues the chain bit for bit."""
     st = state_json(setup, system.positions(), system.box(), system.mass_centers())
-    Path(path).write_text(json.dumps(st))
+    if movegen is not None:
+        slump, rnd = movegen.state().split("\n")
+        st["random-move"] = {"seed": slump, "engine": ENGINE_NAME}
+        st["random-global"] = {"seed": rnd, "engine": ENGINE_NAME}
+    if device_state:
+        st[DEVICE_STATE_KEY] = base64.b64encode(system.save_state()).decode("ascii")
+    p = Path(path)
+    if p.suffix == ".ubj":
+        p.write_bytes(ubjson.dumps(st))
+    else:
+        p.write_text(json.dumps(st))
     return st
+
+
+def resume_state(state, system=None, movegen=None) -> None:
+    """The other half of a restart (MetropolisMonteCarlo::restore, src/montecarlo.cpp:116-137):
+    the engines of "random-move" / "random-global" into the move generator, and the exact device
+    state, when the file carries one, into a system made from the state's setup
+    (apply_state)."""
+    st = _read(state)
+    if movegen is not None and "random-move" in st and "random-global" in st:
+        movegen.set_state(st["random-move"]["seed"] + "\n" + st["random-global"]["seed"])
+    if system is not None and DEVICE_STATE_KEY in st:
+        system.load_state(base64.b64decode(st[DEVICE_STATE_KEY]))

@@ -9,7 +9,8 @@ stream (``mode="reference"``: mt19937 on the host, every move kind including
 volume moves, through fau_run_proposals) or from the device's counter-based RNG
 (``mode="batch"``: fau_run_batch, single-atom or molecular moves, no volume moves).
 SystemEnergy samples the running energy and AtomRDF the pair histogram on the
-device (fau_sampler); savestate writes the reference's state JSON.  The result
+device (fau_sampler); savestate writes the reference's state file (JSON, or UBJSON for .ubj)
+with the RNG engines and the exact device state, from which ``resume`` continues bit for bit.  The result
 mirrors the reference's output JSON: per-move acceptance, energy statistics,
 analysis sample counts and the relative energy drift
 (MetropolisMonteCarlo::relativeEnergyDrift, src/montecarlo.cpp:85-98).
@@ -23,12 +24,16 @@ from typing import Optional
 import numpy as np
 
 from . import _capi as A
-from .input import Setup, save_state
+from .input import Setup, resume_state, save_state
 from .system import MoveGenerator, Sampler
 
 
 def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: int = 1,
-             macro: Optional[int] = None, micro: Optional[int] = None) -> dict:
+             macro: Optional[int] = None, micro: Optional[int] = None, resume=None, first_step: int = 0) -> dict:
+    """resume: a state saved by an earlier run (dict or path; setup already carries its positions
+    through apply_state) whose engines and exact device state continue the chain; first_step:
+    the sweeps that run already made (the device RNG's counter and the analyses' step count
+    continue from it)."""
     out = Path(out_dir)
     out.mkdir(parents=True, exist_ok=True)
     spec = setup.spec
@@ -56,6 +61,8 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
         gen = MoveGenerator(spec, setup.moves, seed, seed + 1, default_seeds=fixed)
     elif mode != "batch":
         raise ValueError(f"unknown mode '{mode}'")
+    if resume is not None:
+        resume_state(resume, system, gen)
 
     # analyses
     energy_an, rdf_an, saves = None, [], []
@@ -76,7 +83,7 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
             saves.append(p.get("file"))
     e0 = system.energy_total()["total"]
     c0 = system.counters()
-    step = 0
+    step = first_step
     accepted = {}
     for _ in range(macro):
         for _ in range(micro):
@@ -133,8 +140,8 @@ def simulate(setup: Setup, ctx, *, out_dir=".", mode: str = "reference", seed: i
         result["analysis"].append({"atomrdf": entry})
         r["sampler"].close()
     for f in saves:
-        if f and f.endswith(".json"):
-            save_state(setup, system, out / f)
+        if f and (f.endswith(".json") or f.endswith(".ubj")):
+            save_state(setup, system, out / f, movegen=gen)
     (out / "out.json").write_text(json.dumps(result, indent=1))
     system.close()
     return result

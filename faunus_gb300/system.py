@@ -388,14 +388,19 @@ class Context:
                   n_swap_blocks: int = 0, temperatures=None, threads: int = 0, streams=None,
                   counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None,
                   sampler: Optional["Sampler"] = None, sample_slots=None, sample_interval: int = 0,
-                  n_sample_blocks: int = 0, time_budget_s: Optional[float] = None, moves_out=None) -> dict:
+                  n_sample_blocks: int = 0, time_budget_s: Optional[float] = None, moves_out=None,
+                  swap_log: bool = False) -> dict:
         """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
         is a uint64 array of len(systems) that receives each system's SM cycles.  With a
         sampler, the systems are sampled on the device after every block of moves (the PT
         swap blocks, or n_sample_blocks blocks of sample_interval moves, or once at the end).
         time_budget_s: each chain ends at the first move boundary after that much time of its
         own (or after its move count); moves_out (int64, one entry a system) receives the
-        moves each performed -- continue a chain at counter + moves done."""
+        moves each performed -- continue a chain at counter + moves done.  Under parallel
+        tempering moves_per_system gives each walker's block length between swaps, and
+        swap_log=True adds the record of every round to the result: "swap_slots"
+        (n_swap_blocks, n) systems per temperature slot after each round, "swap_energy"
+        (n_swap_blocks, n) each system's running energy when the round was decided."""
         n = len(systems)
         arr = (C.c_void_p * n)(*[s.handle for s in systems])
         p = A.BatchParams()
@@ -449,9 +454,17 @@ class Context:
             if moves_out.dtype != np.int64 or not moves_out.flags.c_contiguous or len(moves_out) != n:
                 raise ValueError("moves_out must be a contiguous int64 array with one entry per system")
             p.moves_out = moves_out.ctypes.data_as(C.POINTER(C.c_int64))
+        log = None
+        if swap_log and n_swap_blocks > 0:
+            log = (np.zeros((n_swap_blocks, n), np.int32), np.zeros((n_swap_blocks, n)))
+            p.swap_slots_out = A.as_iptr(log[0])
+            p.swap_energy_out = A.as_dptr(log[1])
         st = A.BatchStats()
         A.check(self._lib.fau_run_batch(self.handle, arr, n, C.byref(p), C.byref(st)), "fau_run_batch")
-        return st.as_dict()
+        out = st.as_dict()
+        if log is not None:
+            out["swap_slots"], out["swap_energy"] = log
+        return out
 
 
     def run_proposals_batch(self, systems: Sequence["System"], props: np.ndarray, offsets: np.ndarray,
@@ -614,6 +627,26 @@ class System:
         out = np.zeros(2 * max(self.K, 1), dtype=np.float64)
         A.check(self._lib.fau_get_q(self.handle, A.as_dptr(out)), "fau_get_q")
         return out[: 2 * self.K].view(np.complex128)
+
+    def save_state(self) -> bytes:
+        """The exact device state (fau_sys_save_state): load it into a system made from the same
+        spec with the saved box, and its chains continue bit for bit."""
+        n = C.c_size_t()
+        A.check(self._lib.fau_sys_state_size(self.handle, C.byref(n)), "fau_sys_state_size")
+        buf = (C.c_char * n.value)()
+        A.check(self._lib.fau_sys_save_state(self.handle, buf, n.value), "fau_sys_save_state")
+        return bytes(buf)
+
+    def load_state(self, blob: bytes) -> None:
+        buf = C.create_string_buffer(blob, len(blob))
+        A.check(self._lib.fau_sys_load_state(self.handle, buf, len(blob)), "fau_sys_load_state")
+
+    def kvectors(self):
+        """The resident k-vector table: ((K, 3) wavevectors (2 pi)(n / L), (K,) A_k)."""
+        kv = np.zeros((max(self.K, 1), 3))
+        ak = np.zeros(max(self.K, 1))
+        A.check(self._lib.fau_get_kvectors(self.handle, None, A.as_dptr(kv), A.as_dptr(ak)), "fau_get_kvectors")
+        return kv[: self.K], ak[: self.K]
 
     def q_rebuild(self) -> float:
         v = C.c_double()

@@ -205,7 +205,9 @@ typedef struct fau_sampler fau_sampler; /* device analysis accumulators, see fau
 
 typedef struct fau_batch_params {
     int64_t moves;            /* moves per system in this launch (when moves_per_system is NULL) */
-    const int64_t* moves_per_system; /* optional per-system move counts                       */
+    const int64_t* moves_per_system; /* optional per-system move counts; under parallel tempering
+                                 each walker's block length between swaps (e.g. 1,000 sweeps
+                                 = 1000 N_i moves), replacing swap_interval_moves for it   */
     uint64_t seed;            /* counter-based RNG key                                    */
     uint64_t counter_base;    /* first move counter (continue a stream across launches)   */
     double dp;                /* translational displacement (angstrom)                    */
@@ -234,6 +236,13 @@ typedef struct fau_batch_params {
                                  move count; a chain split this way continues exactly as one
                                  launch would (resume it at counter + moves done)        */
     int64_t* moves_out;       /* optional, n entries: moves (proposals) each system performed */
+    /* parallel-tempering record (both optional, n_swap_blocks * n entries, round-major): the
+       system holding each temperature slot after each round's swaps, and each system's running
+       energy (kT of its own Hamiltonian) when the round's swaps were decided.  With the slot
+       order of the round before (identity before the first), the temperatures and the
+       counter-based uniforms, every swap decision can be recomputed by the caller.        */
+    int* swap_slots_out;
+    double* swap_energy_out;
 } fau_batch_params;
 
 typedef struct fau_batch_stats {
@@ -270,6 +279,18 @@ int fau_sys_destroy(fau_sys* sys);
  * reference builds a second State from one input, src/montecarlo.cpp:101-111):
  * replicas and jobs that share an initial state.  Counters start at zero. */
 int fau_sys_clone(const fau_sys* src, fau_sys** out);
+/* Checkpoint and resume: the exact device state of a system -- positions, fixed-point records,
+ * mass centres, Q(k) with its FP32 pending sums, the cell lists in their slot order, the running
+ * energy and its float-float part, the surface dipole, the temperature scale and the counters --
+ * as an opaque blob of fau_sys_state_size bytes.  Loaded into a system made from the same
+ * descriptor (with the saved box), the chains continue bit for bit as if never stopped: the
+ * reference's state file (SaveState src/analysis.cpp:586-690, with its random-move and
+ * random-global engines, src/faunus.cpp:430-470) carries positions only, whose rebuilt Q(k) and
+ * cell order would change the last bits of later energy changes.  Device-RNG chains resume at
+ * their next (seed, stream, counter); host streams from fau_movegen_get_state. */
+int fau_sys_state_size(const fau_sys* sys, size_t* bytes);
+int fau_sys_save_state(fau_sys* sys, void* buf, size_t bytes);
+int fau_sys_load_state(fau_sys* sys, const void* buf, size_t bytes);
 /* Number of Ewald k-vectors (0 without Ewald). */
 int fau_sys_num_kvectors(const fau_sys* sys, int* k);
 
@@ -301,7 +322,17 @@ int fau_run_proposals(fau_sys* sys, const fau_proposal* proposals, int n,
                       uint8_t* accepted_out, double* du_out, fau_run_stats* stats);
 
 /* Advance n independent systems with device-generated (Philox4x32-10)
- * proposals in one launch per swap block; PT swaps between blocks. */
+ * proposals in one launch per swap block; PT swaps between blocks.
+ * Parallel tempering (ParallelTempering::_move, src/move.cpp:883-923, with
+ * OddEvenPartner::generate, src/mpicontroller.cpp:69-83): round r draws the
+ * partner parity p from Philox4x32-10 keyed by (seed ^ 0x5DEECE66D) at counter
+ * {r, r >> 32, 0xFFFFFFFF, 7} (p = word0 & 1); temperature slots s = p, p + 2, ...
+ * pair with s + 1 and exchange when u <= exp(x), u the 53-bit uniform of the
+ * words 0, 1 at counter {r, r >> 32, s, 8}, x = (1/T_s - 1/T_{s+1}) (E_a - E_b),
+ * E the running energies in absolute units (kT_i T_i of each walker's own
+ * Hamiltonian).  r = counter_base / swap_interval_moves + block.  Walkers run
+ * in descending order of their block's cost (moves x particles), so that the
+ * largest begin first, each on an SM of its own while SMs remain. */
 int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* params,
                   fau_batch_stats* stats);
 
@@ -329,13 +360,17 @@ int fau_measure_fp32_peak(fau_ctx* ctx, double* tflops_out);
  * Scratch: one file-scope device array of FAU_NOALLOC_MAX_PARTICLES doubles
  * (512 KiB) that every GPU loading this library holds until the process exits;
  * larger n_particles is rejected with FAU_ERR_ARG.  The first call on a device
- * looks up the array's device address; make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * (and the first after its context was made again, e.g. by cudaDeviceReset)
+ * looks up the array's device address; make that call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * Positions need not be wrapped: separations are reduced by whole box lengths
+ * before the minimum image.  coulomb_cutoff must be > 0 for the cut and ewald
+ * forms; pair_cutoff <= 0 means no truncation (as in fau_sys_desc). */
 #define FAU_NOALLOC_MAX_PARTICLES 65536
 typedef struct fau_nonbonded_args {
     int n_particles;
     double box[3];
-    const double* pos;        /* device, n*3 xyz inside [-L/2, L/2]  */
+    const double* pos;        /* device, n*3 xyz                     */
     const double* charge;     /* device, n                           */
     const int* type;          /* device, n                           */
     int n_types;
@@ -418,6 +453,9 @@ int fau_set_temperature_scale(fau_sys* sys, double scale);     /* beta multiplie
  * |Q_cumulative - Q_rebuilt| before replacing (drift of the running Q). */
 int fau_q_rebuild(fau_sys* sys, double* max_abs_drift_out);
 int fau_get_q(fau_sys* sys, double* q_out);                    /* K complex as 2K doubles */
+/* The resident Ewald k-vector table in its order (PolicyIonIon::updateBox, src/energy.cpp:133-186):
+ * n_out 3K integer vectors n, k_out 3K wavevectors (2 pi)(n / L), ak_out K FP64 A_k; each optional. */
+int fau_get_kvectors(fau_sys* sys, int* n_out, double* k_out, double* ak_out);
 
 /* ---- host move generator (reference RNG stream) ---------------------------
  * std::mt19937 streams `slump` (Move::slump, src/move.cpp:21) and `random`

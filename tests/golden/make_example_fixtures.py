@@ -1,6 +1,7 @@
 """Extract the reference's example runs into compact fixtures.
 
-Reads, as data, from the Faunus tree given on the command line (default: /root/reference):
+Reads, as data, from the Faunus source tree given as the one command-line argument
+(`python make_example_fixtures.py <faunus tree>`):
 
   examples/bulk: bulk.yml (the input, converted with the package's YAML reader),
     bulk.state.json (the state the run saved at its end) and bulk.out.json (its output:
@@ -11,6 +12,8 @@ Reads, as data, from the Faunus tree given on the command line (default: /root/r
     statistical fixture) -> minimal_example.json;
   examples/langevin: montecarlo_lj.yml, montecarlo_lj.out.json and rdf_mc.dat (the AtomRDF
     g(r) its MC run wrote) -> montecarlo_lj_example.json;
+  examples/multipole: multipole.state.ubj (a state file the reference wrote as Universal Binary
+    JSON) -> multipole.state.ubj, byte for byte (the UBJSON reader and writer are pinned on it);
   examples/cluster: cluster.yml (nonbonded_splined water; its molecule structure read from
     water.xyz into the input, its cluster move and analyses other than SystemEnergy left out),
     cluster.state.json (the state its run started from) and cluster.out.json (SystemEnergy at
@@ -28,7 +31,9 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parents[1]))
 from faunus_gb300 import yason  # noqa: E402
 
-ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    raise SystemExit("usage: python make_example_fixtures.py <path of a Faunus source tree>")
+ROOT = Path(sys.argv[1])
 
 
 def main() -> None:
@@ -113,5 +118,10 @@ def main() -> None:
                         q=np.array([p["q"] for p in parts], dtype=np.float64))
 
 
+def copy_state_ubj() -> None:
+    (HERE / "multipole.state.ubj").write_bytes((ROOT / "examples" / "multipole" / "multipole.state.ubj").read_bytes())
+
+
 if __name__ == "__main__":
     main()
+    copy_state_ubj()

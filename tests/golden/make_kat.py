@@ -1,7 +1,7 @@
 """Extract the reference's hot-path known-answer values into kat.json.
 
-Reads the doctest sources of the Faunus tree given on the command line
-(default: /root/reference) as TEXT, checks that each cited line still holds
+Reads the doctest sources of the Faunus source tree given as the one
+command-line argument (`python make_kat.py <faunus tree>`) as TEXT, checks that each cited line still holds
 the expected statement, and writes the numbers with their file:line
 provenance.  The tests read only kat.json.
 """
@@ -10,7 +10,9 @@ import re
 import sys
 from pathlib import Path
 
-ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    raise SystemExit("usage: python make_kat.py <path of a Faunus source tree>")
+ROOT = Path(sys.argv[1])
 NUM = r"(-?\d+\.\d+(?:[eE]-?\d+)?)"
 
 # (key, file, line, regex with one capture group)

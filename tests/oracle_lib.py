@@ -67,6 +67,30 @@ def lib() -> C.CDLL:
     return _lib
 
 
+# The two error denominators of a device energy change against the oracle's FP64 value:
+#   rel_scaled = |dU_gpu - dU_fp64| / max(|dU|, S), S the sum of |summand| the change is summed
+#                from (the tolerance's definition, <= 1e-6);
+#   rel_du     = |dU_gpu - dU_fp64| / |dU| over moves with |dU| > 1e-3 kT: its median is held
+#                to TOL_REL_DU_MEDIAN; its maximum is reported (where the terms cancel, |dU| << S
+#                and the FP32 rounding of the summands, bounded through S, dominates).
+DU_FLOOR = 1e-3
+TOL_REL_DU_MEDIAN = 1e-6
+
+
+def du_errors(du_g, du_o, scale) -> dict:
+    du_g, du_o, scale = np.asarray(du_g), np.asarray(du_o), np.asarray(scale)
+    err = np.abs(du_g - du_o)
+    den = np.maximum(np.abs(du_o), scale)
+    rel_s = err / np.where(den > 0, den, 1.0)
+    big = np.abs(du_o) > DU_FLOOR
+    rel_d = err[big] / np.abs(du_o[big])
+    return {"rel_scaled_max": float(rel_s.max(initial=0.0)), "rel_scaled_p99": float(np.quantile(rel_s, 0.99))
+            if len(rel_s) else 0.0, "rel_du_max": float(rel_d.max(initial=0.0)),
+            "rel_du_p99": float(np.quantile(rel_d, 0.99)) if len(rel_d) else 0.0,
+            "rel_du_median": float(np.median(rel_d)) if len(rel_d) else 0.0,
+            "moves_du_above_floor": int(big.sum())}
+
+
 def _ok(rc: int, where: str) -> None:
     if rc != 0:
         raise RuntimeError(f"{where}: oracle status {rc}")

@@ -67,7 +67,7 @@ def test_pipelined_equals_chain_kernel(ctx, case, threads):
     _energy_consistent(a)
 
 
-def _oracle_compare(g_pos, acc_g, du_g, spec, props):
+def _oracle_compare(g_pos, acc_g, du_g, spec, props, label=""):
     o = O.OracleSystem(spec)
     det = o.run_detail(props)
     acc_o, du_o, scale = det["accepted"].astype(np.uint8), det["du"], det["err_scale"]
@@ -76,10 +76,11 @@ def _oracle_compare(g_pos, acc_g, du_g, spec, props):
     sl = slice(0, first + 1 if first < len(props) else first)
     fin = np.isfinite(du_o[sl])
     assert np.array_equal(np.isfinite(du_g[sl]), fin)
-    err = np.abs(du_g[sl][fin] - du_o[sl][fin])
-    den = np.maximum(np.abs(du_o[sl][fin]), scale[sl][fin])
-    rel = err / np.where(den > 0, den, 1.0)
-    assert rel.max(initial=0.0) <= TOL, f"max rel err {rel.max():.3e}"
+    rep = O.du_errors(du_g[sl][fin], du_o[sl][fin], scale[sl][fin])
+    print(f"PARITY {label} moves={len(props)} " + " ".join(f"{k}={v:.3e}" if isinstance(v, float) else f"{k}={v}"
+                                                          for k, v in rep.items()))
+    assert rep["rel_scaled_max"] <= TOL, f"max rel err {rep['rel_scaled_max']:.3e}"
+    assert rep["rel_du_median"] <= O.TOL_REL_DU_MEDIAN, f"median err / |dU| {rep['rel_du_median']:.3e}"
     if len(mism):
         m = first
         lo, hi = sorted([math.exp(-min(du_g[m], 700)), math.exp(-min(du_o[m], 700))])
@@ -105,9 +106,26 @@ def test_pipelined_host_proposals_match_oracle(ctx):
     assert st["moves"] == len(allp)
     for i, (s, spec) in enumerate(zip(systems, specs)):
         sl = slice(i * M, (i + 1) * M)
-        n_acc = _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i])
+        n_acc = _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i], label=f"host_batch_{i}")
         assert n_acc > 100
         _energy_consistent(s)
+
+
+def test_pipelined_full_size_bulk_matches_oracle(ctx):
+    """The benchmarked kernel (fast_chain_kernel, host-proposal instance, 4 compute warps) on the
+    benchmarked system: 20,000 ions, K = 1152, 45^3 cells, 2,500 reference-stream moves."""
+    spec = configs.bulk_ewald(n_salt=10000, seed=1)
+    g = ctx.create(spec)
+    assert g.cell_grid() == (45, 45, 45) and g.K == 1152
+    props = F.MoveGenerator(spec, spec.extra["moves"], 7, 11, default_seeds=False).generate(2500)
+    off = np.array([0, len(props)], np.int64)
+    acc = np.zeros(len(props), np.uint8)
+    du = np.zeros(len(props))
+    st = ctx.run_proposals_batch([g], props, off, acc, du)
+    assert st["moves"] == len(props)
+    n_acc = _oracle_compare(g.positions(), acc, du, spec, props, label="bulk_ewald_20000_fast")
+    assert n_acc > 1000
+    _energy_consistent(g)
 
 
 def test_pipelined_empty_moves_and_reference_move_counts(ctx):

@@ -13,6 +13,8 @@ import pytest
 from faunus_gb300 import _capi as A
 from faunus_gb300 import configs
 
+import oracle_lib as O
+
 pytestmark = pytest.mark.gpu
 
 
@@ -42,23 +44,77 @@ def _args(spec, torch):
     return a, keep
 
 
-@pytest.mark.parametrize("make", [lambda: configs.primitive_model(n=200),
-                                  lambda: configs.bulk_ewald(n_salt=1000)])
-def test_noalloc_energy_matches_system_entry_point(ctx, make):
+def _call(a, out, stream=None):
+    A.check(A.lib().fau_nonbonded_energy_noalloc(C.byref(a), C.c_void_p(out.data_ptr()),
+                                                 C.c_void_p(stream) if stream else None),
+            "fau_nonbonded_energy_noalloc")
+
+
+def _plain_coulomb_wca():
+    spec = configs.primitive_model(n=200, hs=False)
+    spec.coulomb_type = A.FAU_COUL_PLAIN
+    spec.pair_cutoff = 0.0
+    return spec
+
+
+CASES = {
+    "cut_coulomb_wca_hs": lambda: configs.primitive_model(n=200),
+    "ewald_real_space_lj": lambda: configs.bulk_ewald(n_salt=1000),
+    "plain_coulomb_wca": _plain_coulomb_wca,
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_noalloc_energy_matches_system_entry_point(ctx, case):
+    """Two calls in a row (they share the scratch array) against the system entry point's
+    FP64 total and the oracle's nonbonded energy."""
     torch = pytest.importorskip("torch")
-    spec = make()
+    spec = CASES[case]()
     ref = ctx.create(spec).energy_total()["nonbonded"]
+    ref_o = O.OracleSystem(spec).energy_total()["nonbonded"]
+    assert abs(ref - ref_o) <= 1e-9 * max(1.0, abs(ref_o))
     a, keep = _args(spec, torch)
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
-    lib = A.lib()
-    for _ in range(2):  # two calls in a row share the scratch array
+    for _ in range(2):
         out.fill_(float("nan"))
         torch.cuda.synchronize()
-        A.check(lib.fau_nonbonded_energy_noalloc(C.byref(a), C.c_void_p(out.data_ptr()), None),
-                "fau_nonbonded_energy_noalloc")
+        _call(a, out)
         torch.cuda.synchronize()
         e = float(out.item())
         assert abs(e - ref) <= 1e-9 * max(1.0, abs(ref)), (e, ref)
+        assert abs(e - ref_o) <= 1e-9 * max(1.0, abs(ref_o)), (e, ref_o)
+
+
+def test_noalloc_on_a_caller_stream_with_unwrapped_positions(ctx):
+    """The caller's stream carries the work; positions shifted by whole box lengths (an engine
+    that does not wrap) give the energy of the wrapped configuration."""
+    torch = pytest.importorskip("torch")
+    spec = configs.bulk_ewald(n_salt=1000, seed=3)
+    ref_o = O.OracleSystem(spec).energy_total()["nonbonded"]
+    shifted = spec.copy()
+    rng = np.random.default_rng(1)
+    shifted.pos = spec.pos + spec.box * rng.integers(-2, 3, size=spec.pos.shape)
+    a, keep = _args(shifted, torch)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    s.synchronize()
+    _call(a, out, s.cuda_stream)
+    s.synchronize()
+    e = float(out.item())
+    assert abs(e - ref_o) <= 1e-9 * max(1.0, abs(ref_o)), (e, ref_o)
+
+
+def test_noalloc_rejects_bad_settings(ctx):
+    torch = pytest.importorskip("torch")
+    spec = configs.primitive_model(n=200)
+    a, keep = _args(spec, torch)
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    a.coulomb_cutoff = 0.0
+    assert A.lib().fau_nonbonded_energy_noalloc(C.byref(a), C.c_void_p(out.data_ptr()), None) == A.FAU_ERR_ARG
+    a.coulomb_cutoff = spec.coulomb_cutoff
+    a.pair_cutoff = float("nan")
+    assert A.lib().fau_nonbonded_energy_noalloc(C.byref(a), C.c_void_p(out.data_ptr()), None) == A.FAU_ERR_ARG
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch(ctx):
