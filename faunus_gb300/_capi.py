@@ -117,7 +117,7 @@ class BatchParams(C.Structure):
                 ("cycles_out", C.POINTER(C.c_uint64)), ("sampler", C.c_void_p),
                 ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int),
                 ("time_budget_ns", C.c_uint64), ("moves_out", C.POINTER(C.c_int64)),
-                ("swap_slots_out", iptr), ("swap_energy_out", dptr)]
+                ("swap_slots_out", iptr), ("swap_energy_out", dptr), ("no_audit", C.c_int)]
 
 
 class SamplerDesc(C.Structure):
@@ -131,7 +131,8 @@ FAU_SAMPLER_MAX_BINS = 12000
 class BatchStats(C.Structure):
     _fields_ = [("moves", C.c_int64), ("accepted", C.c_int64), ("pair_evals", C.c_int64),
                 ("k_updates", C.c_int64), ("swaps_attempted", C.c_int64), ("swaps_accepted", C.c_int64),
-                ("device_ms", C.c_double)]
+                ("device_ms", C.c_double), ("du_err_scaled_max", C.c_double), ("du_err_rel_max", C.c_double),
+                ("du_err_samples", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -209,6 +210,7 @@ def _declare(lib: C.CDLL) -> None:
         "fau_q_rebuild": ([P, dptr], C.c_int),
         "fau_get_q": ([P, dptr], C.c_int),
         "fau_get_kvectors": ([P, iptr, dptr, dptr], C.c_int),
+        "fau_get_audit": ([P, dptr, C.POINTER(C.c_int64)], C.c_int),
         "fau_sys_state_size": ([P, C.POINTER(C.c_size_t)], C.c_int),
         "fau_sys_save_state": ([P, P, C.c_size_t], C.c_int),
         "fau_sys_load_state": ([P, P, C.c_size_t], C.c_int),

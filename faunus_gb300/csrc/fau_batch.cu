@@ -44,14 +44,17 @@ struct SysSummary {
     double energy, beta_scale;
     int err, pad;
     long long consumed; // proposals performed by the system's last chain launch
+    double audit_scaled, audit_rel;
+    unsigned long long audit_samples;
 };
 
 __global__ void gather_kernel(DevSys* const* sys, int n, SysSummary* out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const DevSys& S = *sys[i];
-        out[i] = {S.moves, S.accepted, S.pair_evals, S.k_updates, S.cycles, sys_energy(S), S.beta_scale, S.err, 0,
-                  S.consumed};
+        out[i] = {S.moves,      S.accepted, S.pair_evals, S.k_updates,        S.cycles,        sys_energy(S),
+                  S.beta_scale, S.err,      0,            S.consumed,         S.audit_scaled_max, S.audit_rel_max,
+                  S.audit_samples};
     }
 }
 
@@ -344,6 +347,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     ChainArgs a{};
     a.sys = reinterpret_cast<DevSys* const*>(dbuf + off_ksys);
     a.sys_ids = reinterpret_cast<const uint32_t*>(dbuf + off_kids);
+    a.audit = P->no_audit ? 0 : 1;
     a.seed = P->seed;
     a.dp = P->dp;
     a.dprot = P->dprot;
@@ -393,9 +397,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                 return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
             if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
+            if (a.audit && (e = launch_fast_audit(a.sys, nfast, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
-        if (nfast) return launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st);
+        if (nfast) {
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
+            return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
+        }
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
                        : launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };
@@ -502,6 +510,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         S.pair_evals += (int64_t)(s1[i].pair_evals - s0[i].pair_evals);
         S.k_updates += (int64_t)(s1[i].k_updates - s0[i].k_updates);
         if (s1[i].err != FAU_OK && derr == FAU_OK) derr = s1[i].err;
+        S.du_err_scaled_max = std::max(S.du_err_scaled_max, s1[i].audit_scaled);
+        S.du_err_rel_max = std::max(S.du_err_rel_max, s1[i].audit_rel);
+        S.du_err_samples += (int64_t)(s1[i].audit_samples - s0[i].audit_samples);
     }
     if (P->cycles_out)
         for (int i = 0; i < n; i++) P->cycles_out[i] = (uint64_t)(s1[i].cycles - s0[i].cycles);
@@ -652,6 +663,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
     cudaMemcpyAsync(s0.data(), d_sum, sizeof(SysSummary) * n, cudaMemcpyDeviceToHost, st);
     ChainArgs a{};
     a.sys = reinterpret_cast<DevSys* const*>(dbuf + o_ksys);
+    a.audit = 1;
     a.n_moves = reinterpret_cast<const long long*>(dbuf + o_nm);
     a.prop_off = reinterpret_cast<const long long*>(dbuf + o_off);
     a.props = dprops ? dprops : reinterpret_cast<const fau_proposal*>(dbuf + o_props);
@@ -686,6 +698,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         }
     }
     if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st) == cudaSuccess;
+    if (ok && nfast) ok = launch_fast_audit(a.sys, nfast, st) == cudaSuccess;
     if (ok && nfast && a.du_out) {
         unpack_du_kernel<<<nfast, 256, 0, st>>>(a.du_out, a.prop_off, a.n_moves);
         ok = cudaGetLastError() == cudaSuccess;
@@ -722,6 +735,9 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         S.pair_evals += (int64_t)(s1[i].pair_evals - s0[i].pair_evals);
         S.k_updates += (int64_t)(s1[i].k_updates - s0[i].k_updates);
         if (s1[i].err != FAU_OK && derr == FAU_OK) derr = s1[i].err;
+        S.du_err_scaled_max = std::max(S.du_err_scaled_max, s1[i].audit_scaled);
+        S.du_err_rel_max = std::max(S.du_err_rel_max, s1[i].audit_rel);
+        S.du_err_samples += (int64_t)(s1[i].audit_samples - s0[i].audit_samples);
     }
     S.device_ms = ms;
     if (stats) *stats = S;

@@ -910,6 +910,8 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     if ((rc = dev_alloc(s, &s->d_partials, kTotalPartials))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_flags, 4))) return bail(rc);
     if (lay.K > 0 && (rc = dev_alloc(s, &s->d_dq, lay.K))) return bail(rc);
+    // the pipelined kernel's audit probe record (systems of atomic groups run in it)
+    if (s->all_atomic && (rc = dev_alloc(s, &h.audit_rec, kAuditRecBytes))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d, 1))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_self, 1))) return bail(rc);
     if (cudaMemcpyAsync(s->d, &h, sizeof(DevSys), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
@@ -974,7 +976,7 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     fix(h.g_begin); fix(h.g_flags); fix(h.g_cm); fix(h.g_cmrec); fix(h.atomic_idx); fix(h.pair); fix(h.pair_d);
     fix(h.g_molid); fix(h.cut2_mol); fix(h.cut2_molf); fix(h.qpend); fix(h.qdlt);
     fix(h.spl); fix(h.spl_zf); fix(h.spl_zd); fix(h.spl_cf); fix(h.spl_cd); fix(h.spl_grid);
-    fix(h.gc_cnt); fix(h.gc_list);
+    fix(h.gc_cnt); fix(h.gc_list); fix(h.audit_rec);
     fix(h.cell_cnt); fix(h.cell_rec); fix(h.cell_of); fix(h.slot_of); fix(h.kn); fix(h.Ak); fix(h.Akd); fix(h.Q);
     fix(s->d); fix(s->d_self); fix(s->d_props); fix(s->d_acc); fix(s->d_du); fix(s->d_detail); fix(s->d_plain);
     fix(s->d_dq); fix(s->d_res); fix(s->d_partials); fix(s->d_flags);
@@ -995,6 +997,9 @@ int fau_sys_clone(const fau_sys* src, fau_sys** out)
     nd.err = 0;
     nd.moves = nd.accepted = nd.pair_evals = nd.k_updates = 0;
     nd.sum_du = 0.0;
+    nd.audit_scaled_max = nd.audit_rel_max = 0.0;
+    nd.audit_samples = 0;
+    nd.audit_pending = 0;
     h = nd;
     if (cudaMemcpyAsync(s->d, &nd, sizeof(DevSys), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
         cudaMemcpyAsync(s->d_self, &s->d, sizeof(DevSys*), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
@@ -2094,6 +2099,21 @@ int fau_get_q(fau_sys* s, double* q)
     CUDA_TRY(launch_fold_q(s->d, s->K, s->ctx->stream));
     CUDA_TRY(cudaMemcpyAsync(q, s->h.Q, sizeof(double2) * s->K, cudaMemcpyDeviceToHost, s->ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return FAU_OK;
+}
+
+int fau_get_audit(fau_sys* s, double err_out[2], int64_t* samples)
+{
+    if (!s) return fail(FAU_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(s->ctx->device));
+    DevSys cur;
+    CUDA_TRY(cudaMemcpyAsync(&cur, s->d, sizeof(DevSys), cudaMemcpyDeviceToHost, s->ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    if (err_out) {
+        err_out[0] = cur.audit_scaled_max;
+        err_out[1] = cur.audit_rel_max;
+    }
+    if (samples) *samples = (int64_t)cur.audit_samples;
     return FAU_OK;
 }
 

@@ -155,7 +155,17 @@ struct DevSys {
     double sum_du;
     long long consumed; // proposals performed by the last chain launch
     unsigned long long cycles; // SM clock cycles spent in chain launches (summed)
+    // the pipelined kernel's audit: the largest error of its FP32 energy changes against FP64
+    // re-evaluations of its probe moves, relative to max(|dU|, S) and to |dU| (|dU| > 1e-3 kT),
+    // and the probes evaluated, since the system was made
+    double audit_scaled_max, audit_rel_max;
+    unsigned long long audit_samples;
+    // the last probe's record (kAuditRecBytes, device; NULL: no audit) and its FP32 energy change
+    unsigned char* audit_rec;
+    double audit_du;
+    int audit_pending, pad5;
 };
+constexpr size_t kAuditRecBytes = 640; // a probe move of the pipelined kernel
 
 // ---------------------------------------------------------------- fixed point
 __host__ __device__ inline uint32_t to_fixed(double x, double scale)
@@ -533,8 +543,9 @@ static __device__ __noinline__ float spline_u32(const DevSys& S, const SplineP& 
     return s + c[0];
 }
 
-// FAU_PAIR_SPLINE, FP64 (totals and the plain form): lower_bound over the FP64 knots
-__device__ __forceinline__ double spline_u64(const DevSys& S, const SplineP& q, double r2)
+// FAU_PAIR_SPLINE, FP64 (totals and the plain form): lower_bound over the FP64 knots; absolute:
+// the magnitude sum_k |c_k| |dz|^k instead (the error scale of the evaluation)
+__device__ __forceinline__ double spline_u64(const DevSys& S, const SplineP& q, double r2, bool absolute = false)
 {
     const double* z = S.spl_zd + q.knot0;
     int first = 0, count = q.pieces + 1;
@@ -550,10 +561,10 @@ __device__ __forceinline__ double spline_u64(const DevSys& S, const SplineP& q, 
     }
     const int i = min(max(first - 1, 0), q.pieces - 1);
     const double* c = S.spl_cd + q.coef0 + 6 * i;
-    const double dz = r2 - z[i];
+    const double dz = absolute ? fabs(r2 - z[i]) : r2 - z[i];
     double s = 0.0;
-    for (int k = 5; k > 0; k--) s = dz * (s + c[k]);
-    return s + c[0];
+    for (int k = 5; k > 0; k--) s = dz * (s + (absolute ? fabs(c[k]) : c[k]));
+    return s + (absolute ? fabs(c[0]) : c[0]);
 }
 
 // Sum of enabled terms (coulomb, LJ, WCA, HS).  Hard-sphere overlap and FP32
@@ -606,12 +617,12 @@ __device__ __forceinline__ float pair_u32(const DevSys& S, const PairF& p, int p
 }
 
 // FAU_COUL_TRUNC short-range function in FP64: e erfc(alpha r) + Horner in q = r / Rc
-__device__ __forceinline__ double coul_trunc_s(const DevSys& S, double r)
+__device__ __forceinline__ double coul_trunc_s(const DevSys& S, double r, bool absolute = false)
 {
     const double q = r / S.rc_coul_d;
     double s = 0.0;
-    for (int k = S.npoly - 1; k >= 0; k--) s = s * q + S.cpoly_d[k];
-    if (S.cerfc_d != 0.0) s += S.cerfc_d * erfc(S.alpha_d * r);
+    for (int k = S.npoly - 1; k >= 0; k--) s = s * q + (absolute ? fabs(S.cpoly_d[k]) : S.cpoly_d[k]);
+    if (S.cerfc_d != 0.0) s += (absolute ? fabs(S.cerfc_d) : S.cerfc_d) * erfc(S.alpha_d * r);
     return s;
 }
 
@@ -658,6 +669,44 @@ __device__ __forceinline__ double pair_u64(const DevSys& S, int ta, int tb, doub
     }
     if ((S.terms & FAU_PAIR_HS) && r2 < hs2) u += __longlong_as_double(0x7ff0000000000000ULL);
     return u;
+}
+
+// The error scale of a pair energy in FP64, as the parity tolerance defines it: the sum of
+// |summand| over the enabled terms, the r^-12 and r^-6 parts of LJ / WCA counted separately (they
+// cancel near r = sigma, where the rounding of any evaluation scales with their sum); the
+// truncated-Coulomb polynomial by its |coefficients|; a splined pair by sum_k |c_k| |dz|^k.
+__device__ __forceinline__ double pair_mag64(const DevSys& S, int ta, int tb, double r2)
+{
+    if (S.rc2_pair_d > 0.0 && r2 >= S.rc2_pair_d) return 0.0;
+    const int ab = ta * S.nt + tb;
+    if (S.terms & FAU_PAIR_SPLINE) {
+        const SplineP& q = S.spl[ab];
+        if (r2 >= q.zmax_d) return 0.0;
+        if (r2 > q.zmin_d) return spline_u64(S, q, r2, true);
+        if (q.hs) return 0.0;
+    }
+    const double* P = S.pair_d + 4 * ab;
+    const double s2 = P[0], e4 = fabs(P[1]), qq = P[3];
+    double m = 0.0;
+    if (S.terms & FAU_PAIR_COULOMB) {
+        if (S.coul_type == FAU_COUL_PLAIN) {
+            m += fabs(qq / sqrt(r2));
+        }
+        else {
+            const double r = sqrt(r2) + 2.220446049250313e-16;
+            if (r < S.rc_coul_d) {
+                double sv = 1.0;
+                if (S.coul_type == FAU_COUL_EWALD) sv = erfc(S.alpha_d * r);
+                else if (S.coul_type == FAU_COUL_TRUNC) sv = coul_trunc_s(S, r, true);
+                m += fabs(qq / r * sv);
+            }
+        }
+    }
+    double x = s2 / r2;
+    x = x * x * x;
+    if (S.terms & FAU_PAIR_LJ) m += e4 * (x * x + x);
+    if ((S.terms & FAU_PAIR_WCA) && !(r2 > s2 * 1.2599210498948732)) m += e4 * (x * x + x + 0.25);
+    return isfinite(m) ? m : 0.0;
 }
 
 __device__ __forceinline__ void kn_unpack(int v, int& nx, int& ny, int& nz)

@@ -35,7 +35,8 @@ namespace fau {
 constexpr int kFastEntries = 64; // cells listed per move: union box (<= 4x4x4) or two stencils (<= 54)
 constexpr int kFastRing = 64;    // host proposals staged in shared memory, refilled 32 at a time
 constexpr int kFastFlushAccepts = 256; // FP32 pending Q deltas flushed to the FP64 master every N accepts
-constexpr int kFastStagePerThread = 4; // pair records staged in shared memory per compute thread and round
+constexpr int kFastStagePerThread = 4; // pair records staged in shared memory per compute thread: two
+                                       // half-rounds of two, one filling while the other is evaluated
 __host__ __device__ constexpr int fast_stage_items(int nwc) { return kFastStagePerThread * 32 * nwc; }
 
 enum : int { FC_SELF = 1, FC_CELLS = 2 };
@@ -54,6 +55,8 @@ struct FastMove {
     float uf, q;
     uint32_t ent[kFastEntries]; // cell | kEntNew (trial state reads it) | kEntOld (accepted state)
 };
+
+static_assert(sizeof(FastMove) <= kAuditRecBytes && sizeof(FastMove) % 4 == 0, "audit record size");
 
 // The move after next: its proposal (written by lane 0) and the moved particle's
 // resident state, copied from global memory asynchronously one move early.
@@ -344,6 +347,69 @@ static __device__ __noinline__ PairOut fast_pair_state(const DevSys& S, PairF p,
 }
 
 
+// FP64 re-evaluation of move m's energy change (the audit probe): thread ctid of NTC's share --
+// its k-vectors and its cell slots (or particles), both states -- as (dU, S) partials, S the
+// parity tolerance's error scale (pairs: pair_mag64 in both states; a k-vector:
+// A_k (|2 Re(Q* d)| + |d|^2)).  Reciprocal
+// space: Q(k) as the chain holds it (FP64 master plus the FP32 pending sums),
+// d = q (e^{i k.xn} - e^{i k.xo}) from FP64 phases; pairs: pair_u64 of the FP64 squared distances
+// to the resident positions.
+__device__ __forceinline__ double2 fast_audit(const DevSys& S, const FastMove& m, int K, int ctid, int NTC, int n_items,
+                                              int cap_shift, bool cells)
+{
+    double du = 0.0, sc = 0.0;
+    if (K) {
+        const double q = S.itype_qd[m.ro.w >> 24];
+        for (int k = ctid; k < K; k += NTC) {
+            int nx, ny, nz;
+            kn_unpack(S.kn[k], nx, ny, nz);
+            // phase / pi = 2 n.x / L
+            const double po = 2.0 * ((nx * m.xo[0]) * S.inv[0] + (ny * m.xo[1]) * S.inv[1] + (nz * m.xo[2]) * S.inv[2]);
+            const double pn = 2.0 * ((nx * m.xn[0]) * S.inv[0] + (ny * m.xn[1]) * S.inv[1] + (nz * m.xn[2]) * S.inv[2]);
+            double so, co, sn, cn;
+            sincospi(po, &so, &co);
+            sincospi(pn, &sn, &cn);
+            const double dx = q * (cn - co), dy = q * (sn - so);
+            const double2 qm = S.Q[k];
+            const float2 pe = S.qpend[k];
+            const double qx = qm.x + (double)pe.x, qy = qm.y + (double)pe.y;
+            const double a = S.rec_pref * S.Akd[k];
+            const double cross = 2.0 * (qx * dx + qy * dy), dd = dx * dx + dy * dy;
+            du += a * (cross + dd);
+            sc += a * (fabs(cross) + dd);
+        }
+    }
+    const int ti = (int)(m.rn.w >> 24);
+    for (int it = ctid; it < n_items; it += NTC) {
+        uint4 rj;
+        uint32_t e;
+        if (cells) {
+            e = m.ent[it >> cap_shift];
+            rj = S.cell_rec[(size_t)(e & kEntCell) * S.cap + (it & (S.cap - 1))];
+        }
+        else {
+            e = kEntNew | kEntOld;
+            rj = S.rec[it];
+        }
+        if (rj.w == kEmptySlot) continue;
+        const int j = cells ? (int)(rj.w & 0xFFFFFFu) : it;
+        if (j == m.i) continue;
+        const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+        const int tj = (int)(rj.w >> 24);
+        if (e & kEntNew) {
+            const double r2 = sqdist_d(S, m.xn, xj);
+            du += pair_u64(S, ti, tj, r2);
+            sc += pair_mag64(S, ti, tj, r2);
+        }
+        if (e & kEntOld) {
+            const double r2 = sqdist_d(S, m.xo, xj);
+            du -= pair_u64(S, ti, tj, r2);
+            sc += pair_mag64(S, ti, tj, r2);
+        }
+    }
+    return make_double2(du, sc);
+}
+
 // Metropolis decision shared by every thread: FP32 unless the exponential is
 // within 1e-4 of u (or an infinity, NaN or the surface term is involved), then
 // the exact FP64 form metropolisCriterion (src/montecarlo.cpp:17-34) on the
@@ -427,10 +493,10 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     int2* kaf = reinterpret_cast<int2*>(dlt + K);     // {table entries of nx, ny, nz (8 bits each), (2 pi lB / V) A_k}
     float4* tabs = reinterpret_cast<float4*>(kaf + K); // 3 slots x 3 axes x TS phase-table entries {mid, h}
     PairF* pt = reinterpret_cast<PairF*>(tabs + 3 * 3 * TS);
-    // a round of pair records (cell slots, or particles without cells), copied in by the compute
-    // thread that owns the slot: warp w's items are w's lanes' (no other warp reads them)
+    // pair records (cell slots, or particles without cells) in two half-round buffers, copied in by
+    // the compute thread that owns the slot: warp w's items are w's lanes' (no other warp reads them)
     uint4* stage = reinterpret_cast<uint4*>(pt + nt * nt);
-    constexpr int KST = fast_stage_items(NWC), KI = kFastStagePerThread;
+    constexpr int KI = kFastStagePerThread / 2, HST = KI * NTC; // records a thread stages and items per half-round
 
     auto& mvb = sh.mvb;
     auto& ahs = sh.ahs;
@@ -473,6 +539,9 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     }
 
     const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
+    // the audit probe: one more move (the chain's next proposal) evaluated after the last one on
+    // the final state, never decided or committed; fast_audit_kernel re-evaluates it in FP64
+    const long long nloop = nmoves + (A.audit && nmoves > 0 ? 1 : 0);
     if (tid == 0) {
         // cell index -> coordinates by multiply-high: q = umulhi(n, floor((2^32 - 1) / d) + 1) is
         // n / d exactly for n d < 2^32 (n < ncell)
@@ -506,7 +575,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     // philox_proposal's single-atom arithmetic (fau_chain.cuh), so both kernels make the same moves
     auto ring_fill = [&](long long s0) {
         const long long s = s0 + lane;
-        if (s >= nmoves) return;
+        if (s >= nloop) return;
         FastProp& f = ring[s % kFastRing];
         if (PHILOX) {
             const Proposal p = philox_proposal(S, ps.ctr0 + (unsigned long long)s, ps.sys_id, A.seed, ps.dp_f, 0.0, false);
@@ -516,8 +585,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             for (int d = 0; d < 3; d++) f.dr[d] = p.dr[d];
             f.u = p.u;
         }
-        else {
-            const fau_proposal& h = A.props[ps.poff + s];
+        else { // host streams: the probe repeats the last proposal on the final state
+            const fau_proposal& h = A.props[ps.poff + (s < nmoves ? s : nmoves - 1)];
             f.kind = h.kind;
             f.index = h.index;
 #pragma unroll
@@ -526,7 +595,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         }
     };
 
-    unsigned long long n_pairs = 0;
+    unsigned int n_pairs = 0; // this thread's pair evaluations in this launch
     // compute threads: accepts since the FP64 flush; dQ not yet folded in (carried across launches)
     int since_flush = S.q_since, q_pending = S.q_valid;
 
@@ -542,7 +611,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         cp_async_commit();
         cp_async_wait<0>();
         fast_scalar(S, mvb[0], ahs[0], nullptr, itq, itqd, nullptr);
-        if (nmoves > 1) {
+        if (nloop > 1) {
             fast_proposal(S, ring, 1, ahs[1]);
             fast_load(S, ahs[1]);
         }
@@ -554,9 +623,10 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     __syncthreads();
 
     int prev_accept = 0, stop = 0;
+    bool probed = false;
     if (timing) ps.tprev[tid >> 5] = clock64();
     long long t = 0;
-    for (; t < nmoves; t++) {
+    for (; t < nloop; t++) {
         const int b = (int)(t % 3);
         FastMove& m = mvb[b];
         if (m.stop) {
@@ -600,7 +670,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                     m.du_surf = S.surf_pref * (m2n - m2o);
                 }
                 tick(0);
-                if (t + 1 < nmoves) {
+                if (t + 1 < nloop) {
                     const FastMove& pm = mvb[(t + 2) % 3]; // move t-1
                     Ahead& an = ahs[(t + 1) & 1];
                     if (t >= 1 && prev_accept && pm.kind == FAU_MOVE_ATOMIC && an.kind == FAU_MOVE_ATOMIC &&
@@ -612,7 +682,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                     }
                     fast_scalar(S, mvb[(t + 1) % 3], an, &m, itq, itqd, timing ? tsm : nullptr);
                     tick(1);
-                    if (t + 2 < nmoves) {
+                    if (t + 2 < nloop) {
                         Ahead& a2 = ahs[t & 1];
                         fast_proposal(S, ring, t + 2, a2);
                         tick(21);
@@ -633,16 +703,20 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 return cells ? S.cell_rec + (size_t)(m.ent[it >> cap_shift] & kEntCell) * cap + (it & (cap - 1))
                              : S.rec + it;
             };
-            // this thread's records of a round [r0, r0 + KST): asynchronous copies into the stage
-            auto stage_round = [&](int r0) {
+            // this thread's records of half-round h (items [h HST, (h + 1) HST)): asynchronous copies
+            // into buffer h & 1, one commit group a half-round
+            auto stage_half = [&](int h) {
+                uint4* buf = stage + (h & 1) * HST;
 #pragma unroll
                 for (int k = 0; k < KI; k++) {
-                    const int it = r0 + ctid + k * NTC;
-                    if (it < n_items) cp_async(&stage[it - r0], item_src(it), 16);
+                    const int it = h * HST + ctid + k * NTC;
+                    if (it < n_items) cp_async(&buf[ctid + k * NTC], item_src(it), 16);
                 }
                 cp_async_commit();
             };
-            stage_round(0); // lands while the Ewald loop runs
+            const int n_half = (n_items + HST - 1) / HST;
+            stage_half(0); // the first two half-rounds land while the Ewald loop runs
+            if (n_half > 1) stage_half(1);
             tick(7);
             // ---- Ewald: one k-vector per thread and step, two independent accumulators.  The
             // last accepted move's Q(k) change (State::sync trial -> accepted) is folded in here,
@@ -697,62 +771,71 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             int flags = 0;
             tick(8);
 
-            // ---- pairs: the staged records of a round; the occupied ones (non-empty slot, not the
-            // moved particle, in a stencil) are counted per warp and each lane evaluates one
-            // (pair, state) task, reading its record from the stage, so a sparse neighbourhood costs
-            // one pass per round, not one per slot
+            // ---- pairs: the staged records of a round.  A (record, state) pair is a task when the slot
+            // is occupied by another particle, the state's stencil holds its cell, and the state's
+            // FP32 r^2 lies below the pair cutoff with twice the FP64 guard band: beyond it every term
+            // is exactly 0 with no flag (pair_u32), so leaving it out changes no sum.  The tasks are
+            // counted per warp and each lane evaluates one, reading its record from the stage, so a
+            // round costs one pass per 32 tasks
             const unsigned FULL = 0xffffffffu;
             const int wbase = (warp - 1) * 32;
-            for (int r0 = 0; r0 < n_items; r0 += KST) {
-                if (r0 > 0) { // beyond the first round (large cells or all pairs): stage the next round
-                    __syncwarp();
-                    stage_round(r0);
-                }
-                cp_async_wait<0>();
+            const float cut2 = S.rc2_pair > 0.f ? S.rc2_pair * 1.00002f : __int_as_float(0x7f800000);
+            for (int h = 0; h < n_half; h++) {
+                // half-round h complete (h + 1, when there is one, may still be in flight)
+                if (h + 1 < n_half) cp_async_wait<1>();
+                else cp_async_wait<0>();
                 __syncwarp(); // every lane's copies visible to the warp
-                unsigned occ[KI];
+                const uint4* buf = stage + (h & 1) * HST;
+                const int r0 = h * HST;
+                unsigned occ[2 * KI]; // per staged record k: [2k] trial state, [2k + 1] accepted state
                 int nv = 0;
 #pragma unroll
                 for (int k = 0; k < KI; k++) {
                     const int it = r0 + ctid + k * NTC;
-                    bool o = false;
+                    bool on = false, oo = false;
                     if (it < n_items) {
-                        const uint4 r = stage[it - r0];
+                        const uint4 r = buf[ctid + k * NTC];
                         const uint32_t e = cells ? m.ent[it >> cap_shift] : (kEntNew | kEntOld);
-                        o = r.w != kEmptySlot && (e & (kEntNew | kEntOld)) && (cells ? (int)(r.w & 0xFFFFFFu) : it) != i;
+                        if (r.w != kEmptySlot && (cells ? (int)(r.w & 0xFFFFFFu) : it) != i) {
+                            on = (e & kEntNew) && r2_fixed(S, rn, r) < cut2;
+                            oo = (e & kEntOld) && r2_fixed(S, ro, r) < cut2;
+                        }
                     }
-                    occ[k] = __ballot_sync(FULL, o);
-                    nv += __popc(occ[k]);
+                    occ[2 * k] = __ballot_sync(FULL, on);
+                    occ[2 * k + 1] = __ballot_sync(FULL, oo);
+                    nv += __popc(occ[2 * k]) + __popc(occ[2 * k + 1]);
                 }
-                for (int base = 0; base < 2 * nv; base += 32) {
-                    const int task = base + lane, q = task >> 1, st = task & 1;
+                for (int base = 0; base < nv; base += 32) {
+                    const int q = base + lane;
                     if (q < nv) {
-                        // the q-th occupied record of this warp's round: its mask k and rank in it
-                        int qq = q, k = 0;
+                        // the q-th task of this warp's half-round: its mask and rank in it
+                        int qq = q, mi = 0;
                         unsigned mk = occ[0];
 #pragma unroll
-                        for (int kk = 1; kk < KI; kk++) {
+                        for (int kk = 1; kk < 2 * KI; kk++) {
                             const int c = __popc(mk);
-                            if (k == kk - 1 && qq >= c) {
+                            if (mi == kk - 1 && qq >= c) {
                                 qq -= c;
-                                k = kk;
+                                mi = kk;
                                 mk = occ[kk];
                             }
                         }
                         const int src = (int)__fns(mk, 0, qq + 1);
-                        const int it = r0 + wbase + src + k * NTC;
-                        const uint4 rj = stage[it - r0];
-                        const uint32_t ent = cells ? m.ent[it >> cap_shift] : (kEntNew | kEntOld);
-                        if (ent & (st ? kEntOld : kEntNew)) {
-                            const int j = cells ? (int)(rj.w & 0xFFFFFFu) : it;
-                            const int pidx = ti * nt + (int)(rj.w >> 24);
-                            const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
-                                                                   st ? m.xo : m.xn, j, nullptr, st == 0);
-                            ff_add(accp, st ? -o.u : o.u);
-                            flags |= o.flags;
-                            n_pairs++;
-                        }
+                        const int st = mi & 1; // 1: the accepted state
+                        const int slot = wbase + src + (mi >> 1) * NTC;
+                        const uint4 rj = buf[slot];
+                        const int j = cells ? (int)(rj.w & 0xFFFFFFu) : r0 + slot;
+                        const int pidx = ti * nt + (int)(rj.w >> 24);
+                        const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
+                                                               st ? m.xo : m.xn, j, nullptr, st == 0);
+                        ff_add(accp, st ? -o.u : o.u);
+                        flags |= o.flags;
+                        if (t < nmoves) n_pairs++; // not the audit probe's
                     }
+                }
+                if (h + 2 < n_half) { // refill this buffer with half-round h + 2
+                    __syncwarp(); // every lane done reading it
+                    stage_half(h + 2);
                 }
             }
             tick(9);
@@ -767,6 +850,10 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         }
         __syncthreads(); // B0
         tick(tid == 0 ? 3 : 11);
+        if (t == nmoves) { // the audit probe: evaluated only
+            probed = true;
+            break;
+        }
 
         // ---- decision, identical in every thread
         int accept = 0;
@@ -871,7 +958,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         // ---- the next move: re-prepared if it moves the particle just committed, then its
         // phase tables and cell entries by every thread
         bool hit = false;
-        if (t + 1 < nmoves) {
+        if (t + 1 < nloop) {
             FastMove& nm = mvb[(t + 1) % 3];
             if (accept && (nm.conflict & FC_SELF)) {
                 if (producer && lane == 0) {
@@ -902,6 +989,24 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     }
     if (producer && lane == 0) cp_async_wait<0>();
     __syncthreads();
+    // the audit probe's record: its FP32 energy change (the warp partials the loop left before B0)
+    // and the move itself, for fast_audit_kernel after this launch
+    if (probed && G.audit_rec) {
+        const FastMove& pm = mvb[t % 3];
+        const int words = (int)(sizeof(FastMove) / 4);
+        for (int w = tid; w < words; w += NT)
+            reinterpret_cast<uint32_t*>(G.audit_rec)[w] = reinterpret_cast<const uint32_t*>(&pm)[w];
+        if (tid == 0) {
+            FF s32{0.f, 0.f};
+            int fl = 0;
+            for (int w = 0; w < NWC; w++) {
+                s32 = ff_sum(s32, red_a[t & 1][w]);
+                fl |= red_f[t & 1][w];
+            }
+            G.audit_du = ff_value(s32) + (surface && pm.kind == FAU_MOVE_ATOMIC ? pm.du_surf : 0.0);
+            G.audit_pending = pm.kind == FAU_MOVE_ATOMIC && fl == 0 ? 1 : 0; // finite in both states
+        }
+    }
     if (A.phase_cycles && tid < kFastPhaseSlots && tsm[tid])
         atomicAdd(&A.phase_cycles[blockIdx.x * kFastPhaseSlots + tid], tsm[tid]);
 

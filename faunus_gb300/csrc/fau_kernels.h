@@ -37,6 +37,9 @@ struct ChainArgs {
     // > 0: a CTA ends its chain at the first move boundary after this many ns of its own
     // (globaltimer); G.consumed then holds the moves done
     unsigned long long time_budget_ns;
+    // 1: after its last move each chain of the pipelined kernel evaluates one more (its next
+    // proposal) on the final state without deciding it and leaves it for fast_audit_kernel
+    int audit;
 };
 constexpr int kPhaseSlots = 17;     // chain kernel (last slot: move count)
 constexpr int kFastPhaseSlots = 24; // pipelined kernel (the per-CTA stride of phase_cycles for both)
@@ -73,6 +76,8 @@ size_t mol_smem_bytes_total(int K, int nc);
 // k-vector components up to kFastMaxNc (8-bit phase-table indices)
 constexpr int kFastMaxNc = 40;
 size_t fast_smem_bytes_total(int K, int nc, int nt);
+// the FP64 audit of the pipelined kernel's probe moves (one CTA per system of `sys`)
+cudaError_t launch_fast_audit(DevSys* const* sys, int n, cudaStream_t st);
 cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox);
 cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st);
 cudaError_t fast_dispatch_2_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);

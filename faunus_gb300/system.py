@@ -389,7 +389,7 @@ class Context:
                   counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None,
                   sampler: Optional["Sampler"] = None, sample_slots=None, sample_interval: int = 0,
                   n_sample_blocks: int = 0, time_budget_s: Optional[float] = None, moves_out=None,
-                  swap_log: bool = False) -> dict:
+                  swap_log: bool = False, audit: bool = True) -> dict:
         """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
         is a uint64 array of len(systems) that receives each system's SM cycles.  With a
         sampler, the systems are sampled on the device after every block of moves (the PT
@@ -454,6 +454,7 @@ class Context:
             if moves_out.dtype != np.int64 or not moves_out.flags.c_contiguous or len(moves_out) != n:
                 raise ValueError("moves_out must be a contiguous int64 array with one entry per system")
             p.moves_out = moves_out.ctypes.data_as(C.POINTER(C.c_int64))
+        p.no_audit = 0 if audit else 1
         log = None
         if swap_log and n_swap_blocks > 0:
             log = (np.zeros((n_swap_blocks, n), np.int32), np.zeros((n_swap_blocks, n)))
@@ -640,6 +641,14 @@ class System:
     def load_state(self, blob: bytes) -> None:
         buf = C.create_string_buffer(blob, len(blob))
         A.check(self._lib.fau_sys_load_state(self.handle, buf, len(blob)), "fau_sys_load_state")
+
+    def audit(self) -> dict:
+        """The pipelined kernel's audit of this system (fau_get_audit): the largest error of its FP32
+        energy changes against FP64 re-evaluations of its probe moves."""
+        e = np.zeros(2)
+        n = C.c_int64()
+        A.check(self._lib.fau_get_audit(self.handle, A.as_dptr(e), C.byref(n)), "fau_get_audit")
+        return {"rel_scaled_max": float(e[0]), "rel_du_max": float(e[1]), "samples": int(n.value)}
 
     def kvectors(self):
         """The resident k-vector table: ((K, 3) wavevectors (2 pi)(n / L), (K,) A_k)."""

@@ -195,7 +195,9 @@ typedef struct fau_run_stats {
     int64_t k_updates;      /* Ewald k-vector x moved-atom phase updates          */
     double energy_change;   /* sum of accepted dU (sum_of_energy_changes)         */
     double energy;          /* running total energy after the run                 */
-    double max_rel_err;     /* unused by the device path (set to 0)               */
+    double max_rel_err;     /* 0 from this single-system entry point; the error against FP64
+                               is audited for systems that run in the pipelined kernel
+                               (fau_batch_stats.du_err_*, fau_get_audit)            */
     double device_ms;       /* device time of the run (CUDA events)               */
 } fau_run_stats;
 
@@ -243,6 +245,7 @@ typedef struct fau_batch_params {
        counter-based uniforms, every swap decision can be recomputed by the caller.        */
     int* swap_slots_out;
     double* swap_energy_out;
+    int no_audit;             /* 1: no audit probe (see fau_batch_stats.du_err_*)           */
 } fau_batch_params;
 
 typedef struct fau_batch_stats {
@@ -253,6 +256,14 @@ typedef struct fau_batch_stats {
     int64_t swaps_attempted;
     int64_t swaps_accepted;
     double device_ms;
+    /* The error of the FP32 energy changes against FP64, for every launch: after its last move
+     * each chain of the pipelined kernel evaluates one more (its next proposal, not decided or
+     * committed) and an FP64 re-evaluation of the same move on the same state follows.  Largest
+     * |dU32 - dU64| / max(|dU64|, S) (S: the sum of |summands|) and / |dU64| (|dU64| > 1e-3 kT)
+     * over the batch's systems since they were made, and the probes of this call. */
+    double du_err_scaled_max;
+    double du_err_rel_max;
+    int64_t du_err_samples;
 } fau_batch_stats;
 
 typedef struct fau_ctx fau_ctx;
@@ -456,6 +467,10 @@ int fau_get_q(fau_sys* sys, double* q_out);                    /* K complex as 2
 /* The resident Ewald k-vector table in its order (PolicyIonIon::updateBox, src/energy.cpp:133-186):
  * n_out 3K integer vectors n, k_out 3K wavevectors (2 pi)(n / L), ak_out K FP64 A_k; each optional. */
 int fau_get_kvectors(fau_sys* sys, int* n_out, double* k_out, double* ak_out);
+/* The system's audit since it was made (systems run in the pipelined kernel): err_out[0] the
+ * largest |dU32 - dU64| / max(|dU64|, S), err_out[1] the largest / |dU64| (|dU64| > 1e-3 kT);
+ * samples the probes evaluated. */
+int fau_get_audit(fau_sys* sys, double err_out[2], int64_t* samples);
 
 /* ---- host move generator (reference RNG stream) ---------------------------
  * std::mt19937 streams `slump` (Move::slump, src/move.cpp:21) and `random`

@@ -71,7 +71,8 @@ def lib() -> C.CDLL:
 #   rel_scaled = |dU_gpu - dU_fp64| / max(|dU|, S), S the sum of |summand| the change is summed
 #                from (the tolerance's definition, <= 1e-6);
 #   rel_du     = |dU_gpu - dU_fp64| / |dU| over moves with |dU| > 1e-3 kT: its median is held
-#                to TOL_REL_DU_MEDIAN; its maximum is reported (where the terms cancel, |dU| << S
+#                to TOL_REL_DU_MEDIAN on the benchmark forms (bulk Ewald, primitive model) and
+#                reported elsewhere; its maximum is reported (where the terms cancel, |dU| << S
 #                and the FP32 rounding of the summands, bounded through S, dominates).
 DU_FLOOR = 1e-3
 TOL_REL_DU_MEDIAN = 1e-6

@@ -61,7 +61,7 @@ int main(void) {
   O(fau_batch_params, sampler) O(fau_batch_params, n_sample_blocks) O(fau_move_desc, volume_method)
   O(fau_sampler_desc, rdf_dr) O(fau_sampler_desc, energy) S(fau_spline_opts)
   O(fau_sys_desc, spline_begin) O(fau_sys_desc, spline_hs) O(fau_spline_opts, hardsphere)
-  O(fau_batch_params, time_budget_ns) O(fau_batch_params, moves_out) O(fau_batch_params, swap_energy_out)
+  O(fau_batch_params, time_budget_ns) O(fau_batch_params, moves_out) O(fau_batch_params, swap_energy_out) O(fau_batch_params, no_audit) O(fau_batch_stats, du_err_samples)
   return 0;
 }
 """

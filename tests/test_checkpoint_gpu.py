@@ -92,6 +92,9 @@ def test_simulate_resumes_from_its_state_file(ctx, tmp_path, mode, suffix):
     from test_input import PM
 
     text = PM.replace("    - systemenergy: {file: energy.dat, nstep: 10}", f"    - savestate: {{file: state{suffix}}}")
+    # one dp for every moved atom type (what batch mode's device proposals take)
+    text = text.replace("    - transrot: {molecule: chloride, repeat: 5}", "    - transrot: {molecule: chloride, repeat: N}")
+    text = text.replace("r: 2.5, dp: 10", "r: 2.5, dp: 20")
     simulate(I.load_input(text, seed=3), ctx, out_dir=tmp_path / "a", mode=mode, macro=1, micro=6)
     simulate(I.load_input(text, seed=3), ctx, out_dir=tmp_path / "b", mode=mode, macro=1, micro=3)
     saved = tmp_path / "b" / f"state{suffix}"

@@ -32,7 +32,7 @@ def _props(spec, n, seeds=(11, 13)):
     return F.MoveGenerator(spec, spec.extra["moves"], seeds[0], seeds[1], default_seeds=False).generate(n)
 
 
-def _compare_chain(gpu_sys, spec, props, tol, expect_bit_exact=True, label=""):
+def _compare_chain(gpu_sys, spec, props, tol, expect_bit_exact=True, label="", median_tol=None):
     acc_g, du_g, st = gpu_sys.run_proposals(props)
     o = O.OracleSystem(spec)
     det = o.run_detail(props)
@@ -51,10 +51,11 @@ def _compare_chain(gpu_sys, spec, props, tol, expect_bit_exact=True, label=""):
     errs = O.du_errors(du_g[sl][fin], du_o[sl][fin], scale[sl][fin])
     print(f"PARITY {label or spec.name} moves={len(props)} near_ties={len(mism)} " +
           " ".join(f"{k}={v:.3e}" if isinstance(v, float) else f"{k}={v}" for k, v in errs.items()))
-    # single-atom moves: the median error relative to |dU| itself is held too (rigid molecules'
-    # changes sum 9 site pairs per neighbour that cancel far more, so there only S bounds it)
-    if tol >= TOL_FP32C and np.all(spec.group_flags & A.FAU_GROUP_ATOMIC):
-        assert errs["rel_du_median"] <= O.TOL_REL_DU_MEDIAN, f"median err / |dU| {errs['rel_du_median']:.3e}"
+    # the benchmark forms (bulk Ewald, primitive model): the median error relative to |dU| itself
+    # is held too; elsewhere (truncated-Coulomb polynomials, rigid molecules' nine site pairs a
+    # neighbour) the summands cancel more and S bounds the error
+    if median_tol is not None:
+        assert errs["rel_du_median"] <= median_tol, f"median err / |dU| {errs['rel_du_median']:.3e}"
     report = {"moves": len(props), "accepted": int(acc_g[:first].sum()), "max_rel_err": float(rel.max(initial=0)),
               "near_ties": len(mism) > 0, "first_mismatch": first, "stats": st, "errors": errs}
     if len(mism):
@@ -114,7 +115,7 @@ def test_kvector_table_matches_oracle(ctx, make, K):
 def test_chain_primitive_model(ctx):
     """Config 0 as specified: 1e5 reference-stream moves of the 200-ion primitive model."""
     spec = configs.primitive_model(n=200)
-    rep, _ = _compare_chain(ctx.create(spec), spec, _props(spec, 100000), TOL_FP32C)
+    rep, _ = _compare_chain(ctx.create(spec), spec, _props(spec, 100000), TOL_FP32C, median_tol=O.TOL_REL_DU_MEDIAN)
     assert rep["accepted"] > 5000
 
 
@@ -122,7 +123,7 @@ def test_chain_bulk_ewald_small(ctx):
     spec = configs.bulk_ewald(n_salt=1000)
     g = ctx.create(spec)
     assert g.cell_grid() == (21, 21, 21)
-    rep, o = _compare_chain(g, spec, _props(spec, 5000), TOL_FP32C)
+    rep, o = _compare_chain(g, spec, _props(spec, 5000), TOL_FP32C, median_tol=O.TOL_REL_DU_MEDIAN)
     assert rep["accepted"] > 1000
     if not rep["near_ties"]:
         # device cell list equals the reference grid binning of the final positions
@@ -145,7 +146,7 @@ def test_chain_bulk_ewald_full_size(ctx):
     spec = configs.bulk_ewald(n_salt=10000)
     g = ctx.create(spec)
     assert g.cell_grid() == (45, 45, 45) and g.K == 1152
-    rep, _ = _compare_chain(g, spec, _props(spec, 1000), TOL_FP32C)
+    rep, _ = _compare_chain(g, spec, _props(spec, 1000), TOL_FP32C, median_tol=O.TOL_REL_DU_MEDIAN)
     assert rep["accepted"] > 200
 
 

@@ -67,7 +67,7 @@ def test_pipelined_equals_chain_kernel(ctx, case, threads):
     _energy_consistent(a)
 
 
-def _oracle_compare(g_pos, acc_g, du_g, spec, props, label=""):
+def _oracle_compare(g_pos, acc_g, du_g, spec, props, label="", median_tol=None):
     o = O.OracleSystem(spec)
     det = o.run_detail(props)
     acc_o, du_o, scale = det["accepted"].astype(np.uint8), det["du"], det["err_scale"]
@@ -80,7 +80,8 @@ def _oracle_compare(g_pos, acc_g, du_g, spec, props, label=""):
     print(f"PARITY {label} moves={len(props)} " + " ".join(f"{k}={v:.3e}" if isinstance(v, float) else f"{k}={v}"
                                                           for k, v in rep.items()))
     assert rep["rel_scaled_max"] <= TOL, f"max rel err {rep['rel_scaled_max']:.3e}"
-    assert rep["rel_du_median"] <= O.TOL_REL_DU_MEDIAN, f"median err / |dU| {rep['rel_du_median']:.3e}"
+    if median_tol is not None:  # the benchmark forms: the median relative to |dU| itself too
+        assert rep["rel_du_median"] <= median_tol, f"median err / |dU| {rep['rel_du_median']:.3e}"
     if len(mism):
         m = first
         lo, hi = sorted([math.exp(-min(du_g[m], 700)), math.exp(-min(du_o[m], 700))])
@@ -106,7 +107,8 @@ def test_pipelined_host_proposals_match_oracle(ctx):
     assert st["moves"] == len(allp)
     for i, (s, spec) in enumerate(zip(systems, specs)):
         sl = slice(i * M, (i + 1) * M)
-        n_acc = _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i], label=f"host_batch_{i}")
+        n_acc = _oracle_compare(s.positions(), acc[sl], du[sl], spec, props[i], label=f"host_batch_{i}",
+                                median_tol=O.TOL_REL_DU_MEDIAN)
         assert n_acc > 100
         _energy_consistent(s)
 
@@ -123,7 +125,8 @@ def test_pipelined_full_size_bulk_matches_oracle(ctx):
     du = np.zeros(len(props))
     st = ctx.run_proposals_batch([g], props, off, acc, du)
     assert st["moves"] == len(props)
-    n_acc = _oracle_compare(g.positions(), acc, du, spec, props, label="bulk_ewald_20000_fast")
+    n_acc = _oracle_compare(g.positions(), acc, du, spec, props, label="bulk_ewald_20000_fast",
+                            median_tol=O.TOL_REL_DU_MEDIAN)
     assert n_acc > 1000
     _energy_consistent(g)
 
@@ -223,3 +226,28 @@ def test_batch_proposals_checked_on_the_device(ctx, kind):
             ctx.run_proposals_batch([g], bad, off)
     st = ctx.run_proposals_batch([g], props, off)  # still usable afterwards
     assert st["moves"] == len(props)
+
+
+def test_audit_reports_the_error_against_fp64(ctx):
+    """Every launch's result carries its error against FP64: after its last move each chain
+    evaluates a probe move that an FP64 re-evaluation then checks; the probe changes nothing
+    (the chains equal unaudited ones bit for bit)."""
+    specs = [configs.bulk_ewald(n_salt=1000, seed=2), configs.primitive_model(n=200, seed=1),
+             configs.bulk_ewald(n_salt=500, epss=1.0, seed=5)]
+    a = [ctx.create(s) for s in specs]
+    b = [ctx.create(s) for s in specs]
+    st = ctx.run_batch(a, 2000, seed=3, dp=2.0, threads=0)
+    assert st["du_err_samples"] == len(specs)
+    assert 0.0 < st["du_err_scaled_max"] <= TOL
+    for s in a:
+        au = s.audit()
+        assert au["samples"] == 1 and au["rel_scaled_max"] <= TOL
+    sb = ctx.run_batch(b, 2000, seed=3, dp=2.0, threads=0, audit=False)
+    assert sb["du_err_samples"] == 0
+    assert st["pair_evals"] == sb["pair_evals"]
+    for x, y in zip(a, b):
+        assert np.array_equal(x.positions(), y.positions()) and x.running_energy() == y.running_energy()
+    # host streams are audited too (the probe repeats the last proposal on the final state)
+    props = F.MoveGenerator(specs[0], specs[0].extra["moves"], 3, 4, default_seeds=False).generate(500)
+    st2 = ctx.run_proposals_batch([a[0]], props, np.array([0, len(props)], np.int64))
+    assert st2["du_err_samples"] == 1 and a[0].audit()["samples"] == 2
