@@ -36,6 +36,14 @@ cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, in
 int fau_internal_sampler_slots(const fau_sampler* s);
 fau_ctx* fau_internal_sampler_ctx(const fau_sampler* s);
 
+// FAU_ERR_CUDA with the failing call and the runtime's name and text of the error (a fault in
+// one of the batch's kernels surfaces at the first synchronising call after the graph)
+static int fau_internal_fail_cuda(cudaError_t e, const char* what)
+{
+    const std::string msg = std::string(what) + " failed: " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fau_internal_fail(FAU_ERR_CUDA, msg.c_str());
+}
+
 namespace {
 
 // per-system summary gathered after a run
@@ -167,7 +175,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 96, 128, 160, 256 or 288");
     const bool use_fast = req == 0 || req == 96 || req == 160 || req == 288;
     const int threads = use_fast ? 256 : req; // molecular moves: 256-thread chain CTAs measured fastest
-    const int fwarps = req == 96 ? 2 : (req == 288 ? 8 : 4);
+    int fwarps = req == 96 ? 2 : (req == 288 ? 8 : 4);
     std::vector<uint8_t> fast(n, 0);
     for (int i = 0; i < n; i++) {
         fau_ctx* c2;
@@ -231,6 +239,18 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     for (int r = nfast; r < n && use_mol; r++)
         if (!mol[order[r]]) use_mol = false;
     if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
+    // threads 0: the pipelined kernel's width for this launch.  When every chain fits on the GPU at
+    // once in CTAs of 8 compute warps (two to an SM, shared memory allowing) each chain gets those:
+    // its moves take less time, and a block (parallel tempering) lasts as long as its longest
+    // chain.  More chains than that keep CTAs of 4, so that four chains share an SM; so do served
+    // (time-budgeted) launches and launches beside the chain kernel.  One pipelined launch a block.
+    if (req == 0 && nfast > 0 && nexact == 0 && P->time_budget_ns == 0) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 0;
+        const size_t per_cta = fast_smem_bytes_total(Kf, ncf, ntf) + 1024; // + the runtime's reserve
+        const int per_sm = (int)std::min<size_t>(2, (size_t)228 * 1024 / per_cta);
+        if (nfast <= per_sm * sms) fwarps = 8;
+    }
 
     // device argument arrays (one allocation, freed at the end of the call)
     // every sub-buffer starts on a 16-byte boundary (8-byte fields inside)
@@ -263,9 +283,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     auto cleanup = [&]() { release2(); }; // dbuf is the context's scratch
 #define BTRY(x)                                                                 \
     do {                                                                        \
-        if ((x) != cudaSuccess) {                                               \
+        const cudaError_t be_ = (x);                                            \
+        if (be_ != cudaSuccess) {                                               \
             cleanup();                                                          \
-            return fau_internal_fail(FAU_ERR_CUDA, "batch: " #x " failed");      \
+            return fau_internal_fail_cuda(be_, "batch: " #x);                   \
         }                                                                       \
     } while (0)
     BTRY(cudaMemcpyAsync(dbuf + off_sys, dsys.data(), sizeof(DevSys*) * n, cudaMemcpyHostToDevice, st));

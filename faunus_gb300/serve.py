@@ -80,9 +80,11 @@ class _Active:
 
 
 class GpuBackend:
-    """The device through the C ABI: one resident system per job."""
+    """The device through the C ABI: one resident system per job.  `threads` is a fixed
+    kernel width (160: the pipelined kernel with 4 compute warps, molecular jobs in the chain
+    kernel), so that a job's chain is the same whatever other jobs share its launches."""
 
-    def __init__(self, ctx: Context, threads: int = 0):
+    def __init__(self, ctx: Context, threads: int = 160):
         self.ctx = ctx
         self.threads = threads
 

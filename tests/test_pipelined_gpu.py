@@ -251,3 +251,29 @@ def test_audit_reports_the_error_against_fp64(ctx):
     props = F.MoveGenerator(specs[0], specs[0].extra["moves"], 3, 4, default_seeds=False).generate(500)
     st2 = ctx.run_proposals_batch([a[0]], props, np.array([0, len(props)], np.int64))
     assert st2["du_err_samples"] == 1 and a[0].audit()["samples"] == 2
+
+
+def test_launch_width_follows_the_chain_count(ctx):
+    """threads=0 gives the pipelined chains CTAs of 8 compute warps when all of them fit on the GPU
+    at once (two to an SM) and CTAs of 4 when there are more; each chain equals the same system run
+    alone at that width (threads 288 or 160), bit for bit."""
+    big, small = configs.primitive_model(n=2000, L=50.0 * 10 ** (1 / 3), seed=6), configs.bulk_ewald(n_salt=500, seed=7)
+    mix = [ctx.create(big), ctx.create(small)]
+    st = ctx.run_batch(mix, 1500, seed=5, streams=[1, 2], dp=2.0, threads=0)
+    assert st["moves"] == 3000 and st["du_err_samples"] == 2
+    alone_big, alone_small = ctx.create(big), ctx.create(small)
+    ctx.run_batch([alone_big], 1500, seed=5, streams=[1], dp=2.0, threads=288)
+    ctx.run_batch([alone_small], 1500, seed=5, streams=[2], dp=2.0, threads=288)
+    for x, y in ((mix[0], alone_big), (mix[1], alone_small)):
+        assert np.array_equal(x.positions(), y.positions()) and x.running_energy() == y.running_energy()
+    _energy_consistent(mix[0])
+    # more chains than two 8-warp CTAs per SM: CTAs of 4
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    spec = configs.primitive_model(n=100, seed=8)
+    base = ctx.create(spec)
+    many = [base] + [base.clone() for _ in range(2 * sms)]
+    ctx.run_batch(many, 400, seed=5, streams=np.arange(len(many)), dp=2.0, threads=0)
+    four = ctx.create(spec)
+    ctx.run_batch([four], 400, seed=5, streams=[0], dp=2.0, threads=160)
+    assert np.array_equal(many[0].positions(), four.positions()) and many[0].running_energy() == four.running_energy()
