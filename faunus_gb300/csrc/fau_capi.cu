@@ -1895,6 +1895,7 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
+int fau_internal_sys_sparse(const fau_sys* s) { return fast_sparse_cells(s->cells, s->n, s->h.ncell) ? 1 : 0; }
 // after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
 // lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)
 int fau_internal_sys_regrow(fau_sys* s)

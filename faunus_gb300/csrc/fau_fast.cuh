@@ -262,17 +262,20 @@ static __device__ __forceinline__ void fast_scalar(const DevSys& S, FastMove& m,
     sub(23);
 }
 
-// All threads of the CTA but the producer warp (busy committing): the phase tables
-// (threads 32, 33, ...) and the cell entries (threads NT-1, NT-2, ...) of the move whose
-// scalar part is in `m`.  Returns whether this thread's entries include a cell `prev`
-// (the move evaluated just before) rewrote.
+// All threads of the CTA but the producer warp (busy committing): the phase tables and the
+// cell entries of the move whose scalar part is in `m`.  Dense layout: tables by threads 32,
+// 33, ..., entries by threads NT-1, NT-2, ...; SPARSE: entry e by thread 32 + e (the thread
+// that stages that cell's records), which also starts the copy of the cell's particle count
+// into cnt[e], and the tables from the top.  Returns whether this thread's entries include a
+// cell `prev` (the move evaluated just before) rewrote.
+template <bool SPARSE>
 __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, const FastMove& prev, int tid, int NT,
-                                              float4* T, int nc)
+                                              float4* T, int nc, int* cnt)
 {
     if (m.kind != FAU_MOVE_ATOMIC) return false;
     const int TS = 2 * nc + 1;
     if (T && tid >= 32) { // per axis and n = -nc..nc: {mid, h}, mid = e^{i n (phi + pi g)}, h = e^{i n pi g}
-        for (int e = tid - 32; e < 3 * (nc + 1); e += NT - 32) {
+        for (int e = SPARSE ? NT - 1 - tid : tid - 32; e < 3 * (nc + 1); e += NT - 32) {
             const int ax = e / (nc + 1), n = e - ax * (nc + 1);
             const uint4 ro = m.ro;
             const uint32_t u = ax == 0 ? ro.x : (ax == 1 ? ro.y : ro.z);
@@ -289,7 +292,7 @@ __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, cons
         const int nue = m.nue;
         const int pc_o = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_old : -1;
         const int pc_n = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_new : -1;
-        for (int e = NT - 1 - tid; tid >= 32 && e < nue; e += NT - 32) {
+        for (int e = SPARSE ? tid - 32 : NT - 1 - tid; tid >= 32 && e < nue; e += NT - 32) {
             int c[3];
             uint32_t mask;
             if (m.uni) { // one box holding both stencils; each cell flags the states whose stencil contains it
@@ -319,6 +322,10 @@ __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, cons
             const int cell = cell_index(S, c);
             hit = hit || cell == pc_o || cell == pc_n;
             m.ent[e] = (uint32_t)cell | mask;
+            if (SPARSE) { // read again after the barrier when the commit in flight rewrites a cell (hit)
+                cp_async(&cnt[e], S.cell_cnt + cell, 4);
+                cp_async_commit();
+            }
         }
     }
     return hit;
@@ -458,6 +465,10 @@ struct __align__(16) FastShared {
     unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
     int sh_up;                // the time budget is spent
     unsigned long long red_u[NWC][2];
+    // sparse cell lists: each stencil cell's particle count (per move slot, copied in by the
+    // cell's entry thread) and the state flags of each compactly staged record
+    int cntb[3][kFastEntries];
+    unsigned char sflag[kFastStagePerThread * 32 * NWC];
     // phase timers (profiling only; every phase still runs), accumulated by thread 0 (producer) and
     // thread 32 (first compute warp): 0 commit data, 1 prepare t+1, 2 copies of t+2, 3 barrier 1,
     // 4 decision, 5 commit, 6 conflict barrier | 7 stage, 8 Ewald, 9 pairs, 10 warp sums,
@@ -467,7 +478,7 @@ struct __align__(16) FastShared {
     ProdState ps;
 };
 
-template <int NWC, bool PHILOX, bool SPL>
+template <int NWC, bool PHILOX, bool SPL, bool SPARSE>
 __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<NWC>& sh)
 {
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
@@ -481,6 +492,10 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
     __syncthreads();
     const DevSys& S = Ssh;
+    if (SPARSE && !(S.flags & SYS_CELLS)) { // the host launches the sparse body for cell lists only
+        if (tid == 0) G.err = FAU_ERR_STATE;
+        return;
+    }
     const bool producer = warp == 0;
     const int ctid = tid - 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -497,6 +512,9 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     // the compute thread that owns the slot: warp w's items are w's lanes' (no other warp reads them)
     uint4* stage = reinterpret_cast<uint4*>(pt + nt * nt);
     constexpr int KI = kFastStagePerThread / 2, HST = KI * NTC; // records a thread stages and items per half-round
+    // SPARSE (cell lists holding about one particle a cell or fewer): only the occupied slots are
+    // staged, compactly, each warp in its own region of RW records (a round), from its lanes' cells
+    constexpr int RW = KI * 32;
 
     auto& mvb = sh.mvb;
     auto& ahs = sh.ahs;
@@ -619,11 +637,12 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         cp_async_commit();
     }
     __syncthreads();
-    if (nmoves > 0) fast_parallel(S, mvb[0], mvb[2], tid, NT, K ? tabs : nullptr, nc);
+    if (nmoves > 0) fast_parallel<SPARSE>(S, mvb[0], mvb[2], tid, NT, K ? tabs : nullptr, nc, sh.cntb[0]);
     __syncthreads();
 
     int prev_accept = 0, stop = 0;
     bool probed = false;
+    bool recnt = false;
     if (timing) ps.tprev[tid >> 5] = clock64();
     long long t = 0;
     for (; t < nloop; t++) {
@@ -714,9 +733,54 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 }
                 cp_async_commit();
             };
-            const int n_half = (n_items + HST - 1) / HST;
-            stage_half(0); // the first two half-rounds land while the Ewald loop runs
-            if (n_half > 1) stage_half(1);
+            // SPARSE: this lane's stencil cell (entry e = ctid), its particle count (read again now
+            // when the last commit rewrote a cell of the stencil), and the records' place in the
+            // warp's compact region: an exclusive prefix over the warp's lanes
+            uint4* buf_w = stage + (warp - 1) * RW;
+            unsigned char* fl_w = sh.sflag + (warp - 1) * RW;
+            uint32_t my_ent = 0;
+            int my_cnt = 0, my_off = 0, w_total = 0;
+            auto stage_sparse = [&](int h) { // records [h RW, (h + 1) RW) of the warp's list
+                const uint4* src = S.cell_rec + (size_t)(my_ent & kEntCell) * cap;
+                const unsigned char f = (unsigned char)(my_ent >> 30);
+                for (int j = 0; j < my_cnt; j++) {
+                    const int c = my_off + j - h * RW;
+                    if (c >= 0 && c < RW) {
+                        cp_async(&buf_w[c], src + j, 16);
+                        fl_w[c] = f;
+                    }
+                }
+                cp_async_commit();
+            };
+            int n_half = 0;
+            if constexpr (SPARSE) {
+                if (ctid < m.nue) {
+                    int* cnt = sh.cntb[b];
+                    my_ent = m.ent[ctid];
+                    if (recnt) {
+                        cp_async_wait<0>(); // the earlier copy lands first
+                        cp_async(&cnt[ctid], S.cell_cnt + (my_ent & kEntCell), 4);
+                        cp_async_commit();
+                    }
+                    cp_async_wait<0>();
+                    my_cnt = min(max(cnt[ctid], 0), cap);
+                }
+                int incl = my_cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                my_off = incl - my_cnt;
+                w_total = __shfl_sync(0xffffffffu, incl, 31);
+                n_half = (w_total + RW - 1) / RW; // rounds of RW records
+                if (n_half > 0) stage_sparse(0); // lands while the Ewald loop runs
+            }
+            else {
+                n_half = (n_items + HST - 1) / HST;
+                stage_half(0); // the first two half-rounds land while the Ewald loop runs
+                if (n_half > 1) stage_half(1);
+            }
             tick(7);
             // ---- Ewald: one k-vector per thread and step, two independent accumulators.  The
             // last accepted move's Q(k) change (State::sync trial -> accepted) is folded in here,
@@ -780,7 +844,62 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             const unsigned FULL = 0xffffffffu;
             const int wbase = (warp - 1) * 32;
             const float cut2 = S.rc2_pair > 0.f ? S.rc2_pair * 1.00002f : __int_as_float(0x7f800000);
-            for (int h = 0; h < n_half; h++) {
+            for (int h = 0; SPARSE && h < n_half; h++) {
+                // round h of the warp's compact list: every record is an occupied slot of a stencil
+                // cell, with that cell's state flags (bit 0 trial state, bit 1 accepted state)
+                if (h > 0) {
+                    __syncwarp(); // every lane done reading the previous round
+                    stage_sparse(h);
+                }
+                cp_async_wait<0>();
+                __syncwarp();
+                const int nrec = min(RW, w_total - h * RW);
+                unsigned occ[2 * KI];
+                int nv = 0;
+#pragma unroll
+                for (int k = 0; k < KI; k++) {
+                    const int it = lane + 32 * k;
+                    bool on = false, oo = false;
+                    if (it < nrec) {
+                        const uint4 r = buf_w[it];
+                        const uint32_t f = fl_w[it];
+                        if (r.w != kEmptySlot && (int)(r.w & 0xFFFFFFu) != i) {
+                            on = (f & 1u) && r2_fixed(S, rn, r) < cut2;
+                            oo = (f & 2u) && r2_fixed(S, ro, r) < cut2;
+                        }
+                    }
+                    occ[2 * k] = __ballot_sync(FULL, on);
+                    occ[2 * k + 1] = __ballot_sync(FULL, oo);
+                    nv += __popc(occ[2 * k]) + __popc(occ[2 * k + 1]);
+                }
+                for (int base = 0; base < nv; base += 32) {
+                    const int q = base + lane;
+                    if (q < nv) {
+                        int qq = q, mi = 0;
+                        unsigned mk = occ[0];
+#pragma unroll
+                        for (int kk = 1; kk < 2 * KI; kk++) {
+                            const int c = __popc(mk);
+                            if (mi == kk - 1 && qq >= c) {
+                                qq -= c;
+                                mi = kk;
+                                mk = occ[kk];
+                            }
+                        }
+                        const int src = (int)__fns(mk, 0, qq + 1);
+                        const int st = mi & 1;
+                        const uint4 rj = buf_w[src + (mi >> 1) * 32];
+                        const int j = (int)(rj.w & 0xFFFFFFu);
+                        const int pidx = ti * nt + (int)(rj.w >> 24);
+                        const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
+                                                               st ? m.xo : m.xn, j, nullptr, st == 0);
+                        ff_add(accp, st ? -o.u : o.u);
+                        flags |= o.flags;
+                        if (t < nmoves) n_pairs++;
+                    }
+                }
+            }
+            for (int h = 0; !SPARSE && h < n_half; h++) {
                 // half-round h complete (h + 1, when there is one, may still be in flight)
                 if (h + 1 < n_half) cp_async_wait<1>();
                 else cp_async_wait<0>();
@@ -974,11 +1093,13 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 }
                 __syncthreads();
             }
-            hit = fast_parallel(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc);
+            hit = fast_parallel<SPARSE>(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc,
+                                        sh.cntb[(t + 1) % 3]);
         }
         tick(tid == 0 ? 6 : 13);
         if (A.time_budget_ns && tid == 0 && global_ns() - sh_t0 >= A.time_budget_ns) sh_up = 1;
         hit = __syncthreads_or(hit) != 0; // B1: commit, tables and entries visible
+        recnt = hit; // SPARSE: the next move's counts of cells this commit rewrote are read again
         if (hit && producer && lane == 0) mvb[(t + 1) % 3].conflict |= FC_CELLS;
         tick(tid == 0 ? 6 : 14);
         prev_accept = accept;
@@ -987,7 +1108,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             break;
         }
     }
-    if (producer && lane == 0) cp_async_wait<0>();
+    cp_async_wait<0>(); // no copy outlives the CTA (the producer's loads, sparse cell counts)
     __syncthreads();
     // the audit probe's record: its FP32 energy change (the warp partials the loop left before B0)
     // and the move itself, for fast_audit_kernel after this launch
@@ -1051,12 +1172,14 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
 
 // The body twice, selected per CTA by its system: splined systems (FAU_PAIR_SPLINE) get their
 // own instance, so the pair path of the others compiles exactly as without the tables.
-template <int NWC, bool PHILOX>
+template <int NWC, bool PHILOX, bool SPARSE>
 __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
 {
     __shared__ FastShared<NWC> sh;
-    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true>(A, sh);
-    else fast_chain_body<NWC, PHILOX, false>(A, sh);
+    // SPARSE: launched only for systems whose cell lists hold about a particle a cell or fewer
+    // (fast_sparse_cells); splined systems take the dense body
+    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true, false>(A, sh);
+    else fast_chain_body<NWC, PHILOX, false, SPARSE>(A, sh);
 }
 
 // dynamic shared memory of the pipelined kernel for K k-vectors, table size nc, nt classes and
@@ -1067,20 +1190,20 @@ __host__ __device__ inline size_t fast_smem_bytes(int K, int nc, int nt, int nwc
            (size_t)nt * nt * sizeof(PairF) + (size_t)fast_stage_items(nwc) * sizeof(uint4);
 }
 
-template <int NWC, bool PH>
+template <int NWC, bool PH, bool SPARSE = false>
 cudaError_t launch_fast_inst(const ChainArgs& a, int nblocks, int K, int nc, int nt, cudaStream_t st, bool prepare_only)
 {
     // the dynamic allowance is raised on demand, never inside a stream capture: callers prepare first
     static size_t granted = 0;
     const size_t smem = fast_smem_bytes(K, nc, nt, NWC);
     if (smem > granted || granted == 0) {
-        cudaError_t e = cudaFuncSetAttribute(fast_chain_kernel<NWC, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(fast_chain_kernel<NWC, PH, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         granted = smem;
     }
     if (prepare_only) return cudaSuccess;
-    fast_chain_kernel<NWC, PH><<<nblocks, 32 * (NWC + 1), smem, st>>>(a);
+    fast_chain_kernel<NWC, PH, SPARSE><<<nblocks, 32 * (NWC + 1), smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,12 @@
+// fau_fast_4s_host.cu -- pipelined chain kernel instantiation: 1 producer + 4 compute warps, host proposals,
+// sparse cell lists (only the occupied slots of a move's stencil cells are staged).
+#include "fau_fast.cuh"
+
+namespace fau {
+
+cudaError_t fast_dispatch_4_host_sparse(const ChainArgs& a, int nb, int K, int nc, int nt, cudaStream_t st, bool prep)
+{
+    return launch_fast_inst<4, false, true>(a, nb, K, nc, nt, st, prep);
+}
+
+} // namespace fau

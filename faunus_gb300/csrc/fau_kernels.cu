@@ -391,13 +391,16 @@ cudaError_t launch_chain(const ChainArgs& a, int nblocks, int K, int nc, int thr
 
 size_t fast_smem_bytes_total(int K, int nc, int nt)
 {
-    // dynamic part + the kernel's static shared memory (move slots, proposal ring, partials)
-    return fast_smem_bytes(K, nc, nt, 8) + 3 * sizeof(FastMove) + kFastRing * sizeof(fau_proposal) + 1024;
+    // dynamic part + the kernel's static shared memory (the widest instance's)
+    return fast_smem_bytes(K, nc, nt, 8) + sizeof(FastShared<8>);
 }
 
 static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox,
-                                    cudaStream_t st, bool prepare_only)
+                                    cudaStream_t st, bool prepare_only, bool sparse)
 {
+    if (warps == 4 && sparse)
+        return philox ? fast_dispatch_4_ph_sparse(a, nblocks, K, nc, nt, st, prepare_only)
+                      : fast_dispatch_4_host_sparse(a, nblocks, K, nc, nt, st, prepare_only);
     if (warps == 2)
         return philox ? fast_dispatch_2_ph(a, nblocks, K, nc, nt, st, prepare_only)
                       : fast_dispatch_2_host(a, nblocks, K, nc, nt, st, prepare_only);
@@ -409,15 +412,16 @@ static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int 
                   : fast_dispatch_4_host(a, nblocks, K, nc, nt, st, prepare_only);
 }
 
-cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox)
+cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox, bool sparse)
 {
     ChainArgs a{};
-    return fast_launch_impl(a, 0, K, nc, nt, warps, philox, nullptr, true);
+    return fast_launch_impl(a, 0, K, nc, nt, warps, philox, nullptr, true, sparse);
 }
 
-cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st)
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st,
+                        bool sparse)
 {
-    return fast_launch_impl(a, nblocks, K, nc, nt, warps, philox, st, false);
+    return fast_launch_impl(a, nblocks, K, nc, nt, warps, philox, st, false, sparse);
 }
 
 // Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then
