@@ -117,7 +117,9 @@ class BatchParams(C.Structure):
                 ("cycles_out", C.POINTER(C.c_uint64)), ("sampler", C.c_void_p),
                 ("sample_slots", iptr), ("sample_interval_moves", C.c_int), ("n_sample_blocks", C.c_int),
                 ("time_budget_ns", C.c_uint64), ("moves_out", C.POINTER(C.c_int64)),
-                ("swap_slots_out", iptr), ("swap_energy_out", dptr), ("no_audit", C.c_int)]
+                ("swap_slots_out", iptr), ("swap_energy_out", dptr), ("no_audit", C.c_int),
+                ("volume_interval_moves", C.c_int), ("n_volume_blocks", C.c_int), ("volume_dv", C.c_double),
+                ("volume_method", C.c_int)]
 
 
 class SamplerDesc(C.Structure):
@@ -132,7 +134,7 @@ class BatchStats(C.Structure):
     _fields_ = [("moves", C.c_int64), ("accepted", C.c_int64), ("pair_evals", C.c_int64),
                 ("k_updates", C.c_int64), ("swaps_attempted", C.c_int64), ("swaps_accepted", C.c_int64),
                 ("device_ms", C.c_double), ("du_err_scaled_max", C.c_double), ("du_err_rel_max", C.c_double),
-                ("du_err_samples", C.c_int64)]
+                ("du_err_samples", C.c_int64), ("volume_attempted", C.c_int64), ("volume_accepted", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -126,7 +126,90 @@ __global__ void reset_beta_kernel(DevSys* const* sys, int n)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) sys[i]->beta_scale = 1.0;
 }
 
+// Philox4x32-10 on the host (Salmon, Moraes, Dror & Shaw, SC'11, published constants), the same
+// generator the device draws its proposals and swap decisions from
+void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; r++) {
+        const unsigned long long p0 = 0xD2511F53ull * c[0], p1 = 0xCD9E8D57ull * c[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = (uint32_t)p1;
+        c[2] = n2;
+        c[3] = (uint32_t)p0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+double u01_53_host(uint32_t a, uint32_t b)
+{
+    return (double)((((unsigned long long)(a >> 5)) << 26) | (b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
 } // namespace
+
+extern "C" double fau_internal_sys_volume(const fau_sys* s);
+
+// NPT blocks: each block's moves through fau_run_batch (one graph launch), then one VolumeMove
+// per system (VolumeMove::_move and setNewVolume, src/move.cpp:994-1006, decided as
+// fau_volume_move decides it)
+static int run_volume_blocks(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* P,
+                             fau_batch_stats* stats)
+{
+    const long long iv = P->volume_interval_moves;
+    fau_batch_stats S{};
+    std::vector<uint64_t> ctr(n), cyc(n), cyc_b(n);
+    const unsigned long long key = P->seed ^ 0x5DEECE66DULL;
+    for (int b = 0; b < P->n_volume_blocks; b++) {
+        fau_batch_params sub = *P;
+        sub.volume_interval_moves = 0;
+        sub.n_volume_blocks = 0;
+        sub.moves = iv;
+        sub.moves_out = nullptr;
+        sub.cycles_out = P->cycles_out ? cyc_b.data() : nullptr;
+        for (int i = 0; i < n; i++) ctr[i] = (P->counters ? P->counters[i] : 0ull) + (uint64_t)b * (uint64_t)iv;
+        sub.counters = ctr.data();
+        fau_batch_stats sb{};
+        int rc = fau_run_batch(ctx, systems, n, &sub, &sb);
+        if (rc != FAU_OK) return rc;
+        S.moves += sb.moves;
+        S.accepted += sb.accepted;
+        S.pair_evals += sb.pair_evals;
+        S.k_updates += sb.k_updates;
+        S.device_ms += sb.device_ms;
+        S.du_err_scaled_max = std::max(S.du_err_scaled_max, sb.du_err_scaled_max);
+        S.du_err_rel_max = std::max(S.du_err_rel_max, sb.du_err_rel_max);
+        S.du_err_samples += sb.du_err_samples;
+        if (P->cycles_out)
+            for (int i = 0; i < n; i++) cyc[i] += cyc_b[i];
+        if (!(P->volume_dv > 0.0)) continue; // VolumeMove::_move: no change without a displacement
+        for (int i = 0; i < n; i++) {
+            const uint32_t stream = P->streams ? P->streams[i] : (uint32_t)i;
+            const unsigned long long v =
+                ((P->counters ? P->counters[i] : 0ull) + P->counter_base) / (unsigned long long)iv + (unsigned long long)b;
+            uint32_t w[4] = {(uint32_t)v, (uint32_t)(v >> 32), stream, 9u};
+            philox_host(w, (uint32_t)key, (uint32_t)(key >> 32));
+            const double ua = u01_53_host(w[0], w[1]), ub = u01_53_host(w[2], w[3]);
+            const double V = fau_internal_sys_volume(systems[i]);
+            const double nv = std::exp(std::log(V) + (ua - 0.5) * P->volume_dv);
+            fau_trial_result tr{};
+            if ((rc = fau_volume_move(systems[i], nv, P->volume_method, ub, &tr)) != FAU_OK) return rc;
+            S.moves += 1;
+            S.volume_attempted += 1;
+            if (tr.accepted) {
+                S.accepted += 1;
+                S.volume_accepted += 1;
+            }
+        }
+    }
+    if (P->moves_out)
+        for (int i = 0; i < n; i++)
+            P->moves_out[i] = (int64_t)P->n_volume_blocks * (iv + (P->volume_dv > 0.0 ? 1 : 0));
+    if (P->cycles_out)
+        for (int i = 0; i < n; i++) P->cycles_out[i] = cyc[i];
+    if (stats) *stats = S;
+    return FAU_OK;
+}
 
 extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* P,
                              fau_batch_stats* stats)
@@ -151,6 +234,17 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     const bool pt_lens = pt && P->moves_per_system;
     const bool pt_log = pt && (P->swap_slots_out || P->swap_energy_out);
     if (!(P->dp >= 0.0)) return fau_internal_fail(FAU_ERR_ARG, "dp must be >= 0");
+    if (P->volume_interval_moves != 0 || P->n_volume_blocks != 0) {
+        if (P->volume_interval_moves <= 0 || P->n_volume_blocks <= 0)
+            return fau_internal_fail(FAU_ERR_ARG, "volume blocks need volume_interval_moves > 0 and n_volume_blocks > 0");
+        if (pt || smp || P->time_budget_ns || P->moves_per_system)
+            return fau_internal_fail(FAU_ERR_ARG, "volume blocks take one move count and no PT, sampler or time budget");
+        if (!(P->volume_dv >= 0.0) || !std::isfinite(P->volume_dv))
+            return fau_internal_fail(FAU_ERR_ARG, "volume_dv must be finite and >= 0");
+        if (P->volume_method < FAU_VOLUME_ISOTROPIC || P->volume_method > FAU_VOLUME_ISOCHORIC)
+            return fau_internal_fail(FAU_ERR_ARG, "unknown volume scaling method");
+        return run_volume_blocks(ctx, systems, n, P, stats);
+    }
 
     std::vector<DevSys*> dsys(n);
     std::vector<long long> nm(n);

@@ -1860,6 +1860,9 @@ int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_t
     CUDA_TRY(cudaMemcpyAsync(&dk->k_updates, &cur.k_updates, sizeof(cur.k_updates), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(&dk->cycles, &cur.cycles, sizeof(cur.cycles), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(&dk->beta_scale, &cur.beta_scale, sizeof(double), cudaMemcpyHostToDevice, st));
+    // the audit history (the error against FP64 since the system was made) stays with the system
+    CUDA_TRY(cudaMemcpyAsync(&dk->audit_scaled_max, &cur.audit_scaled_max, 2 * sizeof(double) + sizeof(unsigned long long),
+                             cudaMemcpyHostToDevice, st));
     if (acc) {
         const double sdu = cur.sum_du + du;
         CUDA_TRY(cudaMemcpyAsync(&dk->sum_du, &sdu, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1895,6 +1898,7 @@ int fau_internal_sys_view(fau_sys* s, fau_ctx** ctx, DevSys** d, int* K, int* n,
 int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
+double fau_internal_sys_volume(const fau_sys* s) { return s->h.L[0] * s->h.L[1] * s->h.L[2]; }
 int fau_internal_sys_sparse(const fau_sys* s) { return fast_sparse_cells(s->cells, s->n, s->h.ncell) ? 1 : 0; }
 // after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
 // lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)

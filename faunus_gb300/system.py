@@ -389,7 +389,8 @@ class Context:
                   counters=None, dp_per_system=None, dprot_per_system=None, cycles_out=None,
                   sampler: Optional["Sampler"] = None, sample_slots=None, sample_interval: int = 0,
                   n_sample_blocks: int = 0, time_budget_s: Optional[float] = None, moves_out=None,
-                  swap_log: bool = False, audit: bool = True) -> dict:
+                  swap_log: bool = False, audit: bool = True, volume_interval: int = 0, n_volume_blocks: int = 0,
+                  volume_dv: float = 0.0, volume_method: int = 0) -> dict:
         """Advance the systems with device proposals (fau_run_batch).  cycles_out, if given,
         is a uint64 array of len(systems) that receives each system's SM cycles.  With a
         sampler, the systems are sampled on the device after every block of moves (the PT
@@ -400,7 +401,10 @@ class Context:
         tempering moves_per_system gives each walker's block length between swaps, and
         swap_log=True adds the record of every round to the result: "swap_slots"
         (n_swap_blocks, n) systems per temperature slot after each round, "swap_energy"
-        (n_swap_blocks, n) each system's running energy when the round was decided."""
+        (n_swap_blocks, n) each system's running energy when the round was decided.
+        NPT: n_volume_blocks blocks of volume_interval moves per system, each followed by one
+        VolumeMove per system with logarithmic displacement volume_dv and scaling volume_method
+        (fau_volume_method); "volume_attempted" / "volume_accepted" count them."""
         n = len(systems)
         arr = (C.c_void_p * n)(*[s.handle for s in systems])
         p = A.BatchParams()
@@ -455,6 +459,10 @@ class Context:
                 raise ValueError("moves_out must be a contiguous int64 array with one entry per system")
             p.moves_out = moves_out.ctypes.data_as(C.POINTER(C.c_int64))
         p.no_audit = 0 if audit else 1
+        p.volume_interval_moves = int(volume_interval)
+        p.n_volume_blocks = int(n_volume_blocks)
+        p.volume_dv = float(volume_dv)
+        p.volume_method = int(volume_method)
         log = None
         if swap_log and n_swap_blocks > 0:
             log = (np.zeros((n_swap_blocks, n), np.int32), np.zeros((n_swap_blocks, n)))

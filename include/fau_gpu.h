@@ -253,6 +253,17 @@ typedef struct fau_batch_params {
     int* swap_slots_out;
     double* swap_energy_out;
     int no_audit;             /* 1: no audit probe (see fau_batch_stats.du_err_*)           */
+    /* NPT in the batch (no PT, sampler or time budget; `moves` for every system): n_volume_blocks
+       blocks of volume_interval_moves moves per system, each followed by one VolumeMove per
+       system (src/move.cpp:994-1006): V' = exp(ln V + (u_a - 1/2) volume_dv), scaled by
+       volume_method (fau_volume_method) and decided as fau_volume_move decides it on u_b.  u_a
+       and u_b: Philox4x32-10 keyed by seed ^ 0x5DEECE66D on the counter (v mod 2^32, v / 2^32,
+       stream, 9) for the system's volume move v = (counter + counter_base) / volume_interval_moves
+       + block, as 53-bit uniforms from words (0, 1) and (2, 3); volume_dv = 0: no volume move */
+    int volume_interval_moves;
+    int n_volume_blocks;
+    double volume_dv;
+    int volume_method;
 } fau_batch_params;
 
 typedef struct fau_batch_stats {
@@ -271,6 +282,8 @@ typedef struct fau_batch_stats {
     double du_err_scaled_max;
     double du_err_rel_max;
     int64_t du_err_samples;
+    int64_t volume_attempted; /* volume moves of NPT blocks (also counted in moves/accepted) */
+    int64_t volume_accepted;
 } fau_batch_stats;
 
 typedef struct fau_ctx fau_ctx;
