@@ -29,6 +29,7 @@
 // warp partials in two.
 #pragma once
 #include "fau_chain.cuh"
+#include "fau_fp64int.cuh"
 
 namespace fau {
 
@@ -464,6 +465,7 @@ struct __align__(16) FastShared {
     FastProp ring[kFastRing]; // proposals, filled 32 at a time by the producer warp
     unsigned long long sh_t0; // globaltimer at the start (time-budgeted launches)
     int sh_up;                // the time budget is spent
+    int sh_acc;               // the producer's decision of the move: bit 0 accepted, bit 1 NaN stop
     unsigned long long red_u[NWC][2];
     // sparse cell lists: each stencil cell's particle count (per move slot, copied in by the
     // cell's entry thread) and the state flags of each compactly staged record
@@ -753,7 +755,9 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 cp_async_commit();
             };
             int n_half = 0;
-            if constexpr (SPARSE) {
+            // SPARSE: started part-way through the Ewald loop, when the counts copied in during the
+            // last move have landed; the records then land during the rest of it
+            auto stage_sparse0 = [&]() {
                 if (ctid < m.nue) {
                     int* cnt = sh.cntb[b];
                     my_ent = m.ent[ctid];
@@ -774,9 +778,9 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 my_off = incl - my_cnt;
                 w_total = __shfl_sync(0xffffffffu, incl, 31);
                 n_half = (w_total + RW - 1) / RW; // rounds of RW records
-                if (n_half > 0) stage_sparse(0); // lands while the Ewald loop runs
-            }
-            else {
+                if (n_half > 0) stage_sparse(0);
+            };
+            if constexpr (!SPARSE) {
                 n_half = (n_items + HST - 1) / HST;
                 stage_half(0); // the first two half-rounds land while the Ewald loop runs
                 if (n_half > 1) stage_half(1);
@@ -824,12 +828,22 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                     return __int_as_float(ka.y) * (f * fmaf(2.f, r, f));
                 };
                 int k = ctid;
+                if constexpr (SPARSE) {
+                    for (int it = 0; it < 2 && k + NTC < K; it++, k += 2 * NTC) {
+                        const float ta = ewald_k(k), tb = ewald_k(k + NTC);
+                        ff_add(acc0, ta + tb);
+                    }
+                    stage_sparse0();
+                }
                 for (; k + NTC < K; k += 2 * NTC) {
                     const float ta = ewald_k(k), tb = ewald_k(k + NTC);
                     ff_add(acc0, ta + tb);
                 }
                 if (k < K) ff_add(acc1, ewald_k(k));
                 q_pending = 0;
+            }
+            else if constexpr (SPARSE) {
+                stage_sparse0();
             }
             FF accp = ff_sum(acc0, acc1);
             int flags = 0;
@@ -974,113 +988,110 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             break;
         }
 
-        // ---- decision, identical in every thread
+        // ---- decision by the producer warp (the warp partials summed as a tree, the same order
+        // in every lane); the compute warps go on to the next move and read it after B1
         int accept = 0;
         bool nan_stop = false;
-        double du_surf = 0.0;
-        FF s{0.f, 0.f};
-        int fl = 0;
-        if (kind == FAU_MOVE_ATOMIC) {
-#pragma unroll
-            for (int w = 0; w < NWC; w++) {
-                s = ff_sum(s, red_a[rb][w]);
-                fl |= red_f[rb][w];
-            }
-            if (surface) du_surf = m.du_surf;
-            accept = fast_decide(s, fl, du_surf, surface, S.beta_scale, beta_f, m.u, m.uf, nan_stop) ? 1 : 0;
-        }
-        if (nan_stop) {
-            stop = FAU_ERR_NAN;
-            break;
-        }
-        tick(tid == 0 ? 4 : 12);
-        if (producer && lane == 0) {
-            FF dff{0.f, 0.f}; // this move's energy change as float-float (written packed to du_out)
+        if (producer) {
+            double du_surf = 0.0;
+            FF s{0.f, 0.f};
+            int fl = 0;
             if (kind == FAU_MOVE_ATOMIC) {
-                ps.n_mv++;
-                if (fl == 0 && !surface) {
-                    dff = s;
-                    if (accept) {
-                        ps.n_acc++;
-                        ps.e_acc = ff_sum(ps.e_acc, s);
-                    }
-                }
-                else if (accept || A.du_out) {
-                    const double du = energy_change(ff_value(s) + du_surf, fl & F_NEW_INF, fl & F_OLD_INF,
-                                                    fl & F_NEW_NAN, fl & F_OLD_NAN);
-                    dff.hi = (float)du;
-                    dff.lo = isfinite(du) ? (float)(du - (double)dff.hi) : 0.f;
-                    if (accept) {
-                        ps.n_acc++;
-                        const double acc = ff_value(ps.e_acc);
-                        ps.energy += acc + du;
-                        ps.sum_du += acc + du;
-                        ps.e_acc = FF{0.f, 0.f};
-                    }
-                }
-            }
-            const long long po = ps.poff + t;
-            if (A.acc_out) A.acc_out[po] = (uint8_t)accept;
-            if (A.du_out) // packed {hi, lo}; a kernel after the launch turns the range into doubles
-                reinterpret_cast<float2*>(A.du_out)[po] = make_float2(dff.hi, dff.lo);
-            if (accept && surface) {
+                FF part[NWC];
 #pragma unroll
-                for (int d = 0; d < 3; d++) ps.M[d] = __dadd_rn(ps.M[d], m.dM[d]);
-            }
-            if (accept) { // commit (State::sync trial -> accepted): positions, record, cell list
-                cp_async_wait<1>();
-                const CommitPre& cp_cur = cps[t & 1];
-                const int i = m.i;
-                S.x[i] = m.xn[0];
-                S.y[i] = m.xn[1];
-                S.z[i] = m.xn[2];
-                S.rec[i] = m.rn;
-                const bool sane = cp_cur.so >= 0 && cp_cur.so < cap &&
-                                  (m.cell_old == m.cell_new ||
-                                   (cp_cur.cnt_o >= 1 && cp_cur.cnt_o <= cap && cp_cur.cnt_n >= 0));
-                if (cells && !sane) {
-                    G.err = FAU_ERR_STATE; // inconsistent cell list: leave it untouched
+                for (int w = 0; w < NWC; w++) {
+                    part[w] = red_a[rb][w];
+                    fl |= red_f[rb][w];
                 }
-                else if (cells) {
-                    const int co = m.cell_old, cn = m.cell_new;
-                    if (co == cn || m.cap_full) {
-                        // a full destination keeps the particle listed in its old cell: the host regrows the list
-                        S.cell_rec[(size_t)co * cap + cp_cur.so] = m.rn;
-                    }
-                    else {
-                        const int last = cp_cur.cnt_o - 1;
-                        if (cp_cur.so != last) {
-                            S.cell_rec[(size_t)co * cap + cp_cur.so] = cp_cur.last;
-                            S.slot_of[cp_cur.last.w & 0xFFFFFFu] = cp_cur.so;
+#pragma unroll
+                for (int h = 1; h < NWC; h <<= 1)
+#pragma unroll
+                    for (int w = 0; w + h < NWC; w += 2 * h) part[w] = ff_sum(part[w], part[w + h]);
+                s = part[0];
+                if (surface) du_surf = m.du_surf;
+                accept = fast_decide(s, fl, du_surf, surface, S.beta_scale, beta_f, m.u, m.uf, nan_stop) ? 1 : 0;
+            }
+            if (nan_stop) accept = 0;
+            tick(4);
+            if (lane == 0 && !nan_stop) {
+                FF dff{0.f, 0.f}; // this move's energy change as float-float (written packed to du_out)
+                if (kind == FAU_MOVE_ATOMIC) {
+                    ps.n_mv++;
+                    if (fl == 0 && !surface) {
+                        dff = s;
+                        if (accept) {
+                            ps.n_acc++;
+                            ps.e_acc = ff_sum(ps.e_acc, s);
                         }
-                        S.cell_rec[(size_t)co * cap + last] = make_uint4(0u, 0u, 0u, kEmptySlot);
-                        S.cell_cnt[co] = last;
-                        S.cell_rec[(size_t)cn * cap + cp_cur.cnt_n] = m.rn;
-                        S.cell_cnt[cn] = cp_cur.cnt_n + 1;
-                        S.cell_of[i] = cn;
-                        S.slot_of[i] = cp_cur.cnt_n;
+                    }
+                    else if (accept || A.du_out) {
+                        const double du = energy_change(ff_value(s) + du_surf, fl & F_NEW_INF, fl & F_OLD_INF,
+                                                        fl & F_NEW_NAN, fl & F_OLD_NAN);
+                        dff.hi = (float)du;
+                        dff.lo = isfinite(du) ? (float)(du - (double)dff.hi) : 0.f;
+                        if (accept) {
+                            ps.n_acc++;
+                            const double acc = ff_value(ps.e_acc);
+                            ps.energy += acc + du;
+                            ps.sum_du += acc + du;
+                            ps.e_acc = FF{0.f, 0.f};
+                        }
                     }
                 }
+                const long long po = ps.poff + t;
+                if (A.acc_out) A.acc_out[po] = (uint8_t)accept;
+                if (A.du_out) // packed {hi, lo}; a kernel after the launch turns the range into doubles
+                    reinterpret_cast<float2*>(A.du_out)[po] = make_float2(dff.hi, dff.lo);
+                if (accept && surface) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) ps.M[d] = __dadd_rn(ps.M[d], m.dM[d]);
+                }
+                if (accept) { // commit (State::sync trial -> accepted): positions, record, cell list
+                    cp_async_wait<1>();
+                    const CommitPre& cp_cur = cps[t & 1];
+                    const int i = m.i;
+                    S.x[i] = m.xn[0];
+                    S.y[i] = m.xn[1];
+                    S.z[i] = m.xn[2];
+                    S.rec[i] = m.rn;
+                    const bool sane = cp_cur.so >= 0 && cp_cur.so < cap &&
+                                      (m.cell_old == m.cell_new ||
+                                       (cp_cur.cnt_o >= 1 && cp_cur.cnt_o <= cap && cp_cur.cnt_n >= 0));
+                    if (cells && !sane) {
+                        G.err = FAU_ERR_STATE; // inconsistent cell list: leave it untouched
+                    }
+                    else if (cells) {
+                        const int co = m.cell_old, cn = m.cell_new;
+                        if (co == cn || m.cap_full) {
+                            // a full destination keeps the particle listed in its old cell: the host regrows the list
+                            S.cell_rec[(size_t)co * cap + cp_cur.so] = m.rn;
+                        }
+                        else {
+                            const int last = cp_cur.cnt_o - 1;
+                            if (cp_cur.so != last) {
+                                S.cell_rec[(size_t)co * cap + cp_cur.so] = cp_cur.last;
+                                S.slot_of[cp_cur.last.w & 0xFFFFFFu] = cp_cur.so;
+                            }
+                            S.cell_rec[(size_t)co * cap + last] = make_uint4(0u, 0u, 0u, kEmptySlot);
+                            S.cell_cnt[co] = last;
+                            S.cell_rec[(size_t)cn * cap + cp_cur.cnt_n] = m.rn;
+                            S.cell_cnt[cn] = cp_cur.cnt_n + 1;
+                            S.cell_of[i] = cn;
+                            S.slot_of[i] = cp_cur.cnt_n;
+                        }
+                    }
+                }
+                tick(5);
             }
-            tick(5);
+            if (lane == 0) sh.sh_acc = accept | (nan_stop ? 2 : 0);
         }
-        if (accept) {
-            if (!producer && K) { // this thread's share of Q(k) += dQ(k), folded into the next Ewald pass
-                q_pending = 1;
-                since_flush++;
-            }
-            if (m.cap_full) {
-                stop = FAU_ERR_CAPACITY;
-                break;
-            }
-        }
-        // ---- the next move: re-prepared if it moves the particle just committed, then its
-        // phase tables and cell entries by every thread
+        // ---- the next move: re-prepared (after a barrier) if it moves the particle of this
+        // move and this move was accepted, then its phase tables and cell entries by every thread
         bool hit = false;
         if (t + 1 < nloop) {
             FastMove& nm = mvb[(t + 1) % 3];
-            if (accept && (nm.conflict & FC_SELF)) {
-                if (producer && lane == 0) {
+            if (nm.conflict & FC_SELF) {
+                if (producer && lane == 0 && accept) {
                     Ahead& an = ahs[(t + 1) & 1];
                     cp_async_wait<0>();
                     fast_proposal(S, ring, t + 1, an);
@@ -1098,10 +1109,28 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         }
         tick(tid == 0 ? 6 : 13);
         if (A.time_budget_ns && tid == 0 && global_ns() - sh_t0 >= A.time_budget_ns) sh_up = 1;
-        hit = __syncthreads_or(hit) != 0; // B1: commit, tables and entries visible
+        hit = __syncthreads_or(hit) != 0; // B1: decision, commit, tables and entries visible
         recnt = hit; // SPARSE: the next move's counts of cells this commit rewrote are read again
         if (hit && producer && lane == 0) mvb[(t + 1) % 3].conflict |= FC_CELLS;
         tick(tid == 0 ? 6 : 14);
+        {
+            const int af = sh.sh_acc;
+            accept = af & 1;
+            if (af & 2) { // a NaN energy change: the launch ends before this move
+                stop = FAU_ERR_NAN;
+                break;
+            }
+        }
+        if (accept) {
+            if (!producer && K) { // this thread's share of Q(k) += dQ(k), folded into the next Ewald pass
+                q_pending = 1;
+                since_flush++;
+            }
+            if (m.cap_full) { // committed; the launch ends after it
+                stop = FAU_ERR_CAPACITY;
+                break;
+            }
+        }
         prev_accept = accept;
         if (sh_up) { // the time budget is spent: the launch ends after move t
             t++;
