@@ -29,7 +29,6 @@
 // warp partials in two.
 #pragma once
 #include "fau_chain.cuh"
-#include "fau_fp64int.cuh"
 
 namespace fau {
 
