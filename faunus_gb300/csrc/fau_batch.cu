@@ -31,6 +31,7 @@ extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
 extern "C" int fau_internal_sys_sparse(const fau_sys* s);
+extern "C" int fau_internal_sys_maxe(const fau_sys* s);
 extern "C" int fau_internal_sys_regrow(fau_sys* s);
 cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
                                         cudaStream_t st);
@@ -278,7 +279,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         double tr;
         DevSys* dd;
         fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
-        fast[i] = use_fast && !mol[i] && knc <= kFastMaxNc;
+        // a finite maxenergy: the chain kernel (the only one that forms each state's term sums)
+        fast[i] = use_fast && !mol[i] && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
     }
     std::vector<int> order;   // kernel order: pipelined-kernel systems first
     order.reserve(n);
@@ -332,7 +334,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     bool use_mol = use_fast && nexact > 0;
     if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
     for (int r = nfast; r < n && use_mol; r++)
-        if (!mol[order[r]]) use_mol = false;
+        if (!mol[order[r]] || fau_internal_sys_maxe(systems[order[r]])) use_mol = false;
     if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
     // sparse cell lists in every pipelined system: the instance that stages only occupied slots
     bool sparse = nfast > 0;
@@ -693,7 +695,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         ncv[i] = knc;
         // systems of atomic groups only run in the pipelined kernel (single-atom moves), the others
         // in the 256-thread chain kernel; the kernels check every proposal as they read it
-        fast[i] = fau_internal_sys_all_atomic(systems[i]) && knc <= kFastMaxNc;
+        fast[i] = fau_internal_sys_all_atomic(systems[i]) && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
     }
     // kernel order puts the pipelined-kernel systems first
     std::vector<int> order;
@@ -732,7 +734,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         double tr;
         DevSys* dd;
         fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
-        if (!mo) use_mol = false;
+        if (!mo || fau_internal_sys_maxe(systems[i])) use_mol = false;
         for (long long m = off[i]; m < off[i] + nm[i] && use_mol; m++)
             if (props[m].kind != FAU_MOVE_MOLECULAR && props[m].kind != FAU_MOVE_NONE) use_mol = false;
     }

@@ -284,6 +284,7 @@ int validate(const fau_sys_desc* d)
     if (d->precision != FAU_PREC_FP32C && d->precision != FAU_PREC_FP64)
         return fail(FAU_ERR_ARG, "unknown precision %d", d->precision);
     if (d->isobaric && !std::isfinite(d->pressure)) return fail(FAU_ERR_ARG, "non-finite Isobaric pressure");
+    if (d->maxenergy_set && std::isnan(d->maxenergy)) return fail(FAU_ERR_ARG, "maxenergy is NaN");
     if (d->pair_terms & ~(FAU_PAIR_COULOMB | FAU_PAIR_LJ | FAU_PAIR_WCA | FAU_PAIR_HS | FAU_PAIR_SPLINE))
         return fail(FAU_ERR_ARG, "unknown pair_terms bits 0x%x", d->pair_terms);
     if (d->pair_terms & FAU_PAIR_SPLINE) {
@@ -757,6 +758,8 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0);
     h.beta_scale = 1.0;
+    h.maxe = d->maxenergy_set ? 1 : 0;
+    h.maxenergy = d->maxenergy_set ? d->maxenergy : std::numeric_limits<double>::infinity();
 
 #define UP(dst, vec) \
     if ((rc = upload(s, &dst, vec.data(), vec.size()))) return bail(rc)
@@ -1222,7 +1225,8 @@ static int compute_total(fau_sys* s, fau_energy_terms* t)
     t->ewald_rec = (tmp.flags & SYS_EWALD) ? tmp.rec_pref * r[1] : 0.0;
     double m2 = (tmp.M[0] * tmp.M[0] + tmp.M[1] * tmp.M[1]) + tmp.M[2] * tmp.M[2];
     t->ewald_surf = (tmp.flags & SYS_SURFACE) ? tmp.surf_pref * m2 : 0.0;
-    // Hamiltonian::energy: [self], nonbonded, [ewald]; early break on +inf or NaN
+    // Hamiltonian::energy: [self], nonbonded, [ewald]; early break on a term >= maxenergy (+inf
+    // unless set) or NaN
     double list[3];
     int nl = 0;
     if (tmp.flags & SYS_SELF) list[nl++] = t->self;
@@ -1231,7 +1235,7 @@ static int compute_total(fau_sys* s, fau_energy_terms* t)
     double sum = 0.0;
     for (int i = 0; i < nl; i++) {
         sum += list[i];
-        if (list[i] >= inf || std::isnan(list[i])) break;
+        if (list[i] >= tmp.maxenergy || std::isnan(list[i])) break;
     }
     t->total = sum;
     return FAU_OK;
@@ -1465,7 +1469,8 @@ int fau_run_proposals(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, do
 
 static int run_segment(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats)
 {
-    if (s->precision != FAU_PREC_FP64) return run_chain(s, p, n, acc, du, nullptr, stats);
+    // a finite maxenergy: the chain kernel, the form that stops each state's term sum
+    if (s->precision != FAU_PREC_FP64 || s->h.maxe) return run_chain(s, p, n, acc, du, nullptr, stats);
     // plain FP64 form: one move per call, host Metropolis
     int rc = pull_state(s);
     if (rc) return rc;
@@ -1651,7 +1656,7 @@ int fau_trial_atomic(fau_sys* s, int particle, const double dr[3], double u01, f
     if (!(s->g_flags[s->group_of[particle]] & FAU_GROUP_ATOMIC))
         return fail(FAU_ERR_ARG, "single-atom move inside a molecular group is not supported");
     // the system's precision decides the form: plain FP64 or the FP32C chain kernel
-    if (s->precision == FAU_PREC_FP64) return plain_trial(s, FAU_MOVE_ATOMIC, particle, dr, nullptr, u01, out);
+    if (s->precision == FAU_PREC_FP64 && !s->h.maxe) return plain_trial(s, FAU_MOVE_ATOMIC, particle, dr, nullptr, u01, out);
     fau_proposal p{};
     p.kind = FAU_MOVE_ATOMIC;
     p.index = particle;
@@ -1671,7 +1676,7 @@ int fau_trial_group(fau_sys* s, int group, const double dr[3], const double quat
     if (s->g_flags[group] & FAU_GROUP_ATOMIC) return fail(FAU_ERR_ARG, "molecular move of an atomic group");
     if (s->g_begin[group + 1] - s->g_begin[group] > kMaxGroupAtoms)
         return fail(FAU_ERR_ARG, "group larger than %d atoms", kMaxGroupAtoms);
-    if (s->precision == FAU_PREC_FP64) return plain_trial(s, FAU_MOVE_MOLECULAR, group, dr, quat, u01, out);
+    if (s->precision == FAU_PREC_FP64 && !s->h.maxe) return plain_trial(s, FAU_MOVE_MOLECULAR, group, dr, quat, u01, out);
     fau_proposal p{};
     p.kind = FAU_MOVE_MOLECULAR;
     p.index = group;
@@ -1819,8 +1824,14 @@ int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_t
     const double v_new = Ln[0] * Ln[1] * Ln[2];
     // Isobaric::energy first, then the Hamiltonian's terms (inf / NaN propagate)
     auto iso = [&](double v) { return isobaric ? pressure * v - (double)(n_count + 1) * std::log(v) : 0.0; };
-    const double uo = iso(v_old) + eo.total;
-    const double un = iso(v_new) + en.total;
+    // the Isobaric term ends the sum when it reaches maxenergy (the other terms' stop is in total)
+    const double maxe = s->h.maxenergy;
+    auto with_iso = [&](double vi, double total) {
+        const double ti = iso(vi);
+        return (isobaric && !(ti < maxe)) ? ti : ti + total;
+    };
+    const double uo = with_iso(v_old, eo.total);
+    const double un = with_iso(v_new, en.total);
     // getEnergyChange (src/montecarlo.cpp:193-209)
     const double inf = std::numeric_limits<double>::infinity();
     double du;
@@ -1899,6 +1910,7 @@ int fau_internal_fail(int code, const char* msg) { return fail(code, "%s", msg);
 int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0; }
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
 double fau_internal_sys_volume(const fau_sys* s) { return s->h.L[0] * s->h.L[1] * s->h.L[2]; }
+int fau_internal_sys_maxe(const fau_sys* s) { return s->h.maxe; }
 int fau_internal_sys_sparse(const fau_sys* s) { return fast_sparse_cells(s->cells, s->n, s->h.ncell) ? 1 : 0; }
 // after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
 // lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)

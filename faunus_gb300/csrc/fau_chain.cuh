@@ -507,6 +507,9 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
     __shared__ FF red_a[NW], red_b[NW];
     __shared__ float red_s[NW];
     __shared__ int red_f[NW];
+    // a finite maxenergy: the trial state's Nonbonded sum and the accepted state's reciprocal
+    // energy, reduced beside the energy change
+    __shared__ FF red_n[NW], red_o[NW];
     __shared__ int nbo[27][3];
     __shared__ uint32_t nbl[kNblChunk]; // molecular moves: neighbour groups of one chunk | interacting states
     __shared__ int nbl_wcnt[NW];        // survivors each warp listed in its segment
@@ -613,6 +616,8 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
 
         // ---- energy change of this move
         FF accp{0.f, 0.f}, accr{0.f, 0.f};
+        FF accn{0.f, 0.f}, acco{0.f, 0.f}; // maxenergy: sum u(trial state), sum A_k |Q_k|^2 (accepted)
+        const bool maxe = S.maxe != 0;
         float scale = 0.f;
         int flags = 0;
         if (kind != FAU_MOVE_NONE) {
@@ -637,6 +642,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                         const float dd = fmaf(d.x, d.x, d.y * d.y);
                         ff_add(accr, af * (cross + dd));
                         if (detail) scale += af * (fabsf(cross) + dd);
+                        if (maxe) ff_add(acco, af * fmaf(qx, qx, qy * qy));
                     }
                 }
                 else {
@@ -673,6 +679,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                         const float af = Af[k];
                         ff_add(accr, af * (cross + dd));
                         if (detail) scale += af * (fabsf(cross) + dd);
+                        if (maxe) ff_add(acco, af * fmaf(qx, qx, qy * qy));
                     }
                 }
                 n_k += (unsigned long long)m * (unsigned long long)((K - tid + NT - 1) / NT > 0 ? (K - tid + NT - 1) / NT : 0);
@@ -714,8 +721,13 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                             bool inf = false, nan = false;
                             float mg = 0.f;
                             const float u = pair_u32(S, pt[pidx], pidx, r2_fixed(S, ri, rj), xi, j, inf, nan, mg);
-                            if (state) add_pair(accp, flags, u, 0.f, inf, false, nan, false);
-                            else add_pair(accp, flags, 0.f, u, false, inf, false, nan);
+                            if (state) {
+                                add_pair(accp, flags, u, 0.f, inf, false, nan, false);
+                                if (maxe) ff_add(accn, u);
+                            }
+                            else {
+                                add_pair(accp, flags, 0.f, u, false, inf, false, nan);
+                            }
                             if (detail) scale += mg;
                             n_pairs++;
                         }
@@ -737,6 +749,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                                               fi[st], fn[st], mg);
                         }
                         add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
+                        if (maxe) ff_add(accn, uu[0]);
                         if (detail) scale += mg;
                         n_pairs += 2;
                     }
@@ -815,6 +828,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                                 n_pairs++;
                             }
                             add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
+                            if (maxe) ff_add(accn, uu[0]);
                             if (detail) scale += mg;
                         }
                     }
@@ -837,6 +851,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                                               st ? ms.xo[a] : ms.xn[a], b, fi[st], fn[st], mg);
                         }
                         add_pair(accp, flags, uu[0], uu[1], fi[0], fi[1], fn[0], fn[1]);
+                        if (maxe) ff_add(accn, uu[0]);
                         if (detail) scale += mg;
                         n_pairs += 2;
                     }
@@ -846,13 +861,23 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
 
         tick(tid == 0 ? 2 : 8);
         // ---- reduce: per warp, then warp 0 (B1)
-        if (!detail) accp = ff_sum(accp, accr);
-        warp_reduce(accp, accr, scale, flags, detail);
+        const bool sep = detail || maxe; // the pair and reciprocal parts kept apart
+        if (!sep) accp = ff_sum(accp, accr);
+        warp_reduce(accp, accr, scale, flags, sep);
+        if (maxe) {
+            float sc_n = 0.f;
+            int fl_n = 0;
+            warp_reduce(accn, acco, sc_n, fl_n, true);
+        }
         if (lane == 0) {
             red_a[warp] = accp;
             red_b[warp] = accr;
             red_s[warp] = scale;
             red_f[warp] = flags;
+            if (maxe) {
+                red_n[warp] = accn;
+                red_o[warp] = acco;
+            }
         }
         __syncthreads();
         tick(tid == 0 ? 3 : 9);
@@ -862,11 +887,21 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
             accr = lane < NW ? red_b[lane] : FF{0.f, 0.f};
             scale = lane < NW ? red_s[lane] : 0.f;
             flags = lane < NW ? red_f[lane] : 0;
+            if (maxe) {
+                accn = lane < NW ? red_n[lane] : FF{0.f, 0.f};
+                acco = lane < NW ? red_o[lane] : FF{0.f, 0.f};
+            }
 #pragma unroll
             for (int o = NW / 2; o > 0; o >>= 1) {
                 FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
                 accp = ff_sum(accp, ta);
-                if (detail) {
+                if (maxe) {
+                    FF tn{__shfl_xor_sync(0xffffffffu, accn.hi, o), __shfl_xor_sync(0xffffffffu, accn.lo, o)};
+                    accn = ff_sum(accn, tn);
+                    FF to{__shfl_xor_sync(0xffffffffu, acco.hi, o), __shfl_xor_sync(0xffffffffu, acco.lo, o)};
+                    acco = ff_sum(acco, to);
+                }
+                if (sep) {
                     FF tb{__shfl_xor_sync(0xffffffffu, accr.hi, o), __shfl_xor_sync(0xffffffffu, accr.lo, o)};
                     accr = ff_sum(accr, tb);
                     scale += __shfl_xor_sync(0xffffffffu, scale, o);
@@ -877,11 +912,11 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
             double du = 0.0;
             if (lane == 0) {
                 if (kind != FAU_MOVE_NONE) {
-                    const double du_nb = ff_value(accp); // without detail: pair + reciprocal together
-                    const double du_rec = detail ? ff_value(accr) : 0.0;
-                    double du_surf = 0.0;
+                    const double du_nb = ff_value(accp); // without detail or maxe: pair + reciprocal together
+                    const double du_rec = sep ? ff_value(accr) : 0.0;
+                    double du_surf = 0.0, m2o = 0.0;
                     if (S.flags & SYS_SURFACE) {
-                        double m2o = 0.0, m2n = 0.0;
+                        double m2n = 0.0;
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
                             const double mn = __dadd_rn(M[d], ms.dM[d]);
@@ -892,6 +927,28 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                     }
                     const double fin = du_nb + (du_rec + du_surf);
                     du = energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
+                    if (maxe && flags == 0) {
+                        // Hamiltonian::energy (src/energy.cpp:1227-1241) per state: self, Nonbonded,
+                        // Ewald, summed up to the first term >= maxenergy.  Self is the same in
+                        // both states; Nonbonded is this move's partial energy (new - old = du_nb)
+                        const double Mx = S.maxenergy;
+                        double self = 0.0;
+                        if (S.flags & SYS_SELF)
+                            for (int a = 0; a < m; a++) self += S.itype_self[ms.rec_new[a].w >> 24];
+                        if ((S.flags & SYS_SELF) && !(self < Mx)) {
+                            du = 0.0; // both sums end at the self term
+                        }
+                        else {
+                            const double nn = ff_value(accn), no = nn - du_nb;
+                            const bool tn = !(nn < Mx), to = !(no < Mx);
+                            if (tn || to) {
+                                // the Ewald term of each state (reciprocal + surface), absolute
+                                const double eo = (S.flags & SYS_EWALD) ? ff_value(acco) + S.surf_pref * m2o : 0.0;
+                                const double en = eo + (du_rec + du_surf);
+                                du = du_nb + ((tn ? 0.0 : en) - (to ? 0.0 : eo));
+                            }
+                        }
+                    }
                     const double x = du * S.beta_scale;
                     if (A.pending) { // evaluate only: the caller's Metropolis decides
                         PlainMove& P = *A.pending;

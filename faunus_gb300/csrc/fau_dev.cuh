@@ -164,6 +164,10 @@ struct DevSys {
     unsigned char* audit_rec;
     double audit_du;
     int audit_pending, pad5;
+    // Hamiltonian maxenergy (src/energy.cpp:1227-1241): maxe 1 when finite; the chain kernel then
+    // sums each state's terms (self, Nonbonded, Ewald) up to the first >= maxenergy
+    double maxenergy;
+    int maxe, pad6;
 };
 constexpr size_t kAuditRecBytes = 640; // a probe move of the pipelined kernel
 

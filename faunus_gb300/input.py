@@ -23,7 +23,7 @@ Supported subset (anything else raises NotImplementedError naming the key):
     nonbonded_splined (the same lists tabulated: utol, ftol, u_at_rmin, u_at_rmax, rmax,
     hardsphere; src/potentials.cpp:1513-1553),
     cutoff_g2g (number or per molecule pair), Ewald when coulomb type is ewald
-    (src/energy.cpp:1134-1160), isobaric (P/atm, P/bar, P/kT, P/mM, P/Pa);
+    (src/energy.cpp:1134-1160), isobaric (P/atm, P/bar, P/kT, P/mM, P/Pa), maxenergy;
   moves: transrot, moltransrot, volume (src/move.cpp:190-222, 1580-1613, 986-993);
   analysis: kept as given (systemenergy, atomrdf and savestate drive ``simulate``).
 """
@@ -291,6 +291,9 @@ def load_input(src, seed: int = 0) -> Setup:
     fields: Dict[str, Any] = {"pair_terms": 0}
     spline_opts: Optional[dict] = None
     for name, block in _items(j.get("energy"), "energy"):
+        if name == "maxenergy":  # Hamiltonian's maximum_allowed_energy (src/energy.cpp:1189-1193)
+            fields["maxenergy"] = float(block)
+            continue
         if name == "isobaric":
             units = [k for k in block if k.startswith("P/")]
             if len(units) != 1:

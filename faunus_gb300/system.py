@@ -213,6 +213,7 @@ class SystemSpec:
     cutoff_g2g: float = 0.0
     cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
     isobaric_pressure: Optional[float] = None  # Isobaric term's pressure (kT/A^3, see pressure_kt); None: no term
+    maxenergy: Optional[float] = None     # Hamiltonian maxenergy (kT): terms summed up to the first >= it; None: +inf
     spline: Optional[dict] = None         # FAU_PAIR_SPLINE tables: begin (T*T+1), r2, coef, hs (see splined)
     ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
     precision: int = A.FAU_PREC_FP32C
@@ -276,6 +277,9 @@ class SystemSpec:
         if self.isobaric_pressure is not None:
             d.isobaric = 1
             d.pressure = float(self.isobaric_pressure)
+        if self.maxenergy is not None and self.maxenergy != math.inf:
+            d.maxenergy_set = 1
+            d.maxenergy = float(self.maxenergy)
         if self.coulomb_poly is not None:
             cp = np.asarray(self.coulomb_poly, dtype=np.float64).reshape(-1)
             if len(cp) > A.FAU_COUL_MAX_POLY:

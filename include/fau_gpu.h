@@ -146,6 +146,12 @@ typedef struct fau_sys_desc {
     const double* spline_r2;  /* the knots of every pair, ascending within a pair          */
     const double* spline_coef;/* 6 an interval; pair ab's start at 6 (spline_begin[ab] - ab) */
     const int* spline_hs;     /* n_types^2 KnotData::hardsphere_repulsion; NULL: none       */
+    /* Hamiltonian::energy's `maxenergy` (src/energy.cpp:1189-1193, 1227-1241): each state's terms
+       (self, Nonbonded, Ewald) are summed in order up to and including the first that is
+       >= maxenergy or NaN.  maxenergy_set 0: +inf (every term summed).  Systems with it set
+       run in the chain kernel (FP32C form, whatever their precision), also in batches.     */
+    int maxenergy_set;
+    double maxenergy;
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */

@@ -411,6 +411,7 @@ struct System {
     std::vector<double> cut2_pairs;
     bool isobaric = false;  // Isobaric term (src/energy.cpp:859-901) with `pressure` in kT / A^3
     double pressure = 0.0;
+    double maxenergy = infty; // Hamiltonian maxenergy
     bool want_scale = true; // sum |u| over both states for tolerance checks (not in the reference)
     // MC bookkeeping (MetropolisMonteCarlo)
     double initial_energy = 0, sum_of_energy_changes = 0;
@@ -504,13 +505,14 @@ struct Terms {
 };
 
 // Hamiltonian::energy src/energy.cpp:1227-1241: terms in order, early break on
-// >= maxenergy (+inf) or NaN, summed with std::accumulate.
-static double accumulateTerms(const double* t, int n)
+// >= maxenergy (maximum_allowed_energy, +inf unless set, src/energy.cpp:1189-1193) or NaN,
+// summed with std::accumulate.
+static double accumulateTerms(const double* t, int n, double maxenergy)
 {
     std::vector<double> latest;
     for (int i = 0; i < n; i++) {
         latest.push_back(t[i]);
-        if (t[i] >= infty || std::isnan(t[i])) break;
+        if (t[i] >= maxenergy || std::isnan(t[i])) break;
     }
     double s = 0.0;
     for (double v : latest) s += v;
@@ -544,7 +546,7 @@ static Terms energyOf(const System& s, ChangeKind kind, int index)
         t.rec = s.ewald.reciprocal(s.box);
         list.push_back(t.surf + t.rec); // Ewald::energy src/energy.cpp:581-587
     }
-    t.total = accumulateTerms(list.data(), (int)list.size());
+    t.total = accumulateTerms(list.data(), (int)list.size(), s.maxenergy);
     return t;
 }
 
@@ -611,6 +613,10 @@ static TrialOut trialAtom(System& s, int i, const Vec3& dr, double u01)
     const Terms en = energyOf(s, CH_ATOM, i);
     addScale();
     if (s.want_scale) scale += ewaldScale(s, Qacc);
+    // a sum that stopped before the Ewald term (maxenergy): the energy change then carries the
+    // other state's whole Ewald energy, which joins the error scale
+    if (s.want_scale && (!(en.nb < s.maxenergy) || !(eo.nb < s.maxenergy)))
+        scale += std::fabs(en.rec + en.surf) + std::fabs(eo.rec + eo.surf);
     out.du = getEnergyChange(en.total, eo.total);
     out.du_nb = en.nb - eo.nb;
     out.du_ew = (en.rec + en.surf) - (eo.rec + eo.surf);
@@ -683,6 +689,10 @@ static TrialOut trialGroup(System& s, int g, const Vec3& dr, const Quat* q, doub
     const Terms en = energyOf(s, CH_GROUP, g);
     addScale();
     if (s.want_scale) scale += ewaldScale(s, Qacc);
+    // a sum that stopped before the Ewald term (maxenergy): the energy change then carries the
+    // other state's whole Ewald energy, which joins the error scale
+    if (s.want_scale && (!(en.nb < s.maxenergy) || !(eo.nb < s.maxenergy)))
+        scale += std::fabs(en.rec + en.surf) + std::fabs(eo.rec + eo.surf);
     out.du = getEnergyChange(en.total, eo.total);
     out.du_nb = en.nb - eo.nb;
     out.du_ew = (en.rec + en.surf) - (eo.rec + eo.surf);
@@ -889,6 +899,7 @@ static System buildSystem(const fau_sys_desc* d)
     }
     if (d->cutoff_g2g > 0) s.cutoff_g2g2 = d->cutoff_g2g * d->cutoff_g2g;
     s.isobaric = d->isobaric != 0;
+    s.maxenergy = d->maxenergy_set ? d->maxenergy : infty;
     s.pressure = d->pressure;
     if (d->cutoff_g2g_pairs && d->n_molids > 0) { // GroupCutoff::getCutoff per molecule-kind pair
         s.n_molids = d->n_molids;
@@ -1192,7 +1203,7 @@ int orc_volume_move(orc_sys* h, double new_volume, int method, double u01, fau_t
         if (s.pair.has_self()) list.push_back(e.self);
         list.push_back(e.nb);
         if (s.ewald.enabled) list.push_back(e.surf + e.rec);
-        return accumulateTerms(list.data(), (int)list.size());
+        return accumulateTerms(list.data(), (int)list.size(), s.maxenergy);
     };
     const double uo = total(eo, v_old), un = total(en, v_new);
     const double du = getEnergyChange(un, uo);
