@@ -30,7 +30,6 @@ extern "C" int fau_internal_fail(int code, const char* msg);
 extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
-extern "C" int fau_internal_sys_sparse(const fau_sys* s);
 extern "C" int fau_internal_sys_maxe(const fau_sys* s);
 extern "C" int fau_internal_sys_regrow(fau_sys* s);
 cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
@@ -336,9 +335,6 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     for (int r = nfast; r < n && use_mol; r++)
         if (!mol[order[r]] || fau_internal_sys_maxe(systems[order[r]])) use_mol = false;
     if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
-    // sparse cell lists in every pipelined system: the instance that stages only occupied slots
-    bool sparse = nfast > 0;
-    for (int r = 0; r < nfast && sparse; r++) sparse = fau_internal_sys_sparse(systems[order[r]]) != 0;
     // threads 0: the pipelined kernel's width for this launch.  When every chain fits on the GPU at
     // once in CTAs of 8 compute warps (two to an SM, shared memory allowing) each chain gets those:
     // its moves take less time, and a block (parallel tempering) lasts as long as its longest
@@ -495,7 +491,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact) BTRY(use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true) : prepare_chain(Ke, nce, threads, true));
-    if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true, sparse));
+    if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
         BTRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -517,12 +513,12 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                              : launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess)
                 return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
-            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st, sparse)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
             if (a.audit && (e = launch_fast_audit(a.sys, nfast, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
         if (nfast) {
-            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st, sparse)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
@@ -818,9 +814,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                           : launch_chain(ae, nexact, Ke, nce, 256, false, st)) == cudaSuccess;
         }
     }
-    bool sparse = nfast > 0;
-    for (int r = 0; r < nfast && sparse; r++) sparse = fau_internal_sys_sparse(systems[order[r]]) != 0;
-    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st, sparse) == cudaSuccess;
+    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st) == cudaSuccess;
     if (ok && nfast) ok = launch_fast_audit(a.sys, nfast, st) == cudaSuccess;
     if (ok && nfast && a.du_out) {
         unpack_du_kernel<<<nfast, 256, 0, st>>>(a.du_out, a.prop_off, a.n_moves);

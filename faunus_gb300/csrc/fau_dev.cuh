@@ -33,6 +33,8 @@ enum SysFlags : int {
     SYS_EWALD = 1 << 1,
     SYS_SURFACE = 1 << 2, // Ewald surface term active (epss >= 1)
     SYS_SELF = 1 << 3,    // ParticleSelfEnergy present
+    SYS_OCC = 1 << 4,     // the pipelined kernel stages the occupied slots of stencil cells only
+    SYS_SPREAD = 1 << 5,  // ... with the stencil's cells spread over all compute warps (dense cells)
 };
 
 // pair parameters for one (itype a, itype b) class pair, FP32

@@ -264,14 +264,16 @@ static __device__ __forceinline__ void fast_scalar(const DevSys& S, FastMove& m,
 
 // All threads of the CTA but the producer warp (busy committing): the phase tables and the
 // cell entries of the move whose scalar part is in `m`.  Dense layout: tables by threads 32,
-// 33, ..., entries by threads NT-1, NT-2, ...; SPARSE: entry e by thread 32 + e (the thread
-// that stages that cell's records), which also starts the copy of the cell's particle count
-// into cnt[e], and the tables from the top.  Returns whether this thread's entries include a
-// cell `prev` (the move evaluated just before) rewrote.
-template <bool SPARSE>
+// 33, ..., entries by threads NT-1, NT-2, ...; SPARSE: entry e by the compute thread that stages
+// that cell's records -- thread 32 + e, or with SYS_SPREAD (dense cells) lane e / NWC of compute
+// warp e mod NWC, so that every warp holds a share of the stencil -- which also starts the copy
+// of the cell's particle count into cnt[e]; the tables from the top.  Returns whether this thread's entries include a cell `prev` (the move
+// evaluated just before) rewrote.
+template <int MODE>
 __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, const FastMove& prev, int tid, int NT,
                                               float4* T, int nc, int* cnt)
 {
+    constexpr bool SPARSE = MODE != 0;
     if (m.kind != FAU_MOVE_ATOMIC) return false;
     const int TS = 2 * nc + 1;
     if (T && tid >= 32) { // per axis and n = -nc..nc: {mid, h}, mid = e^{i n (phi + pi g)}, h = e^{i n pi g}
@@ -292,7 +294,10 @@ __device__ __forceinline__ bool fast_parallel(const DevSys& S, FastMove& m, cons
         const int nue = m.nue;
         const int pc_o = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_old : -1;
         const int pc_n = prev.kind == FAU_MOVE_ATOMIC ? prev.cell_new : -1;
-        for (int e = SPARSE ? tid - 32 : NT - 1 - tid; tid >= 32 && e < nue; e += NT - 32) {
+        const int nwc = NT / 32 - 1;
+        constexpr bool spread = MODE == 2;
+        for (int e = SPARSE ? (spread ? ((tid - 32) & 31) * nwc + ((tid - 32) >> 5) : tid - 32) : NT - 1 - tid;
+             tid >= 32 && e < nue; e += SPARSE ? 64 : NT - 32) {
             int c[3];
             uint32_t mask;
             if (m.uni) { // one box holding both stencils; each cell flags the states whose stencil contains it
@@ -479,9 +484,13 @@ struct __align__(16) FastShared {
     ProdState ps;
 };
 
-template <int NWC, bool PHILOX, bool SPL, bool SPARSE>
+// MODE: 0 whole cells (or all particles); 1 the occupied slots of dilute cells (entries with the
+// first warps' lanes, copied cell by cell); 2 the occupied slots of dense cells (entries spread
+// over all compute warps, each warp's list copied by all its lanes)
+template <int NWC, bool PHILOX, bool SPL, int MODE>
 __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<NWC>& sh)
 {
+    constexpr bool SPARSE = MODE != 0;
     constexpr int NT = 32 * (NWC + 1), NTC = 32 * NWC;
     const long long t_start = clock64();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -493,10 +502,6 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
     __syncthreads();
     const DevSys& S = Ssh;
-    if (SPARSE && !(S.flags & SYS_CELLS)) { // the host launches the sparse body for cell lists only
-        if (tid == 0) G.err = FAU_ERR_STATE;
-        return;
-    }
     const bool producer = warp == 0;
     const int ctid = tid - 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -513,8 +518,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     // the compute thread that owns the slot: warp w's items are w's lanes' (no other warp reads them)
     uint4* stage = reinterpret_cast<uint4*>(pt + nt * nt);
     constexpr int KI = kFastStagePerThread / 2, HST = KI * NTC; // records a thread stages and items per half-round
-    // SPARSE (cell lists holding about one particle a cell or fewer): only the occupied slots are
-    // staged, compactly, each warp in its own region of RW records (a round), from its lanes' cells
+    // SPARSE (MODE 1, 2): only the occupied slots are staged, compactly, each warp in its own
+    // region of two buffers of RW records (one round each), from the stencil cells its lanes hold
     constexpr int RW = KI * 32;
 
     auto& mvb = sh.mvb;
@@ -584,6 +589,9 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     }
     __syncthreads();
     const bool cells = (S.flags & SYS_CELLS) != 0;
+    // SPARSE (the bodies the kernel runs for systems flagged SYS_OCC, which have cells): the
+    // occupied slots of the stencil cells only; otherwise whole cells or all particles
+    constexpr bool occ = SPARSE;
     const bool surface = (S.flags & SYS_SURFACE) != 0;
     const int cap = S.cap;
     const int cap_shift = cells ? __ffs(cap) - 1 : 0;
@@ -638,7 +646,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
         cp_async_commit();
     }
     __syncthreads();
-    if (nmoves > 0) fast_parallel<SPARSE>(S, mvb[0], mvb[2], tid, NT, K ? tabs : nullptr, nc, sh.cntb[0]);
+    if (nmoves > 0) fast_parallel<MODE>(S, mvb[0], mvb[2], tid, NT, K ? tabs : nullptr, nc, sh.cntb[0]);
     __syncthreads();
 
     int prev_accept = 0, stop = 0;
@@ -734,21 +742,50 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 }
                 cp_async_commit();
             };
-            // SPARSE: this lane's stencil cell (entry e = ctid), its particle count (read again now
+            // SPARSE: this lane's stencil cell (entry my_e), its particle count (read again now
             // when the last commit rewrote a cell of the stencil), and the records' place in the
-            // warp's compact region: an exclusive prefix over the warp's lanes
-            uint4* buf_w = stage + (warp - 1) * RW;
-            unsigned char* fl_w = sh.sflag + (warp - 1) * RW;
+            // warp's compact list: an exclusive prefix over the warp's lanes.  The list is copied
+            // by all lanes, RW records a round into one of two buffers of the warp's region
+            const int my_e = MODE == 2 ? lane * NWC + (warp - 1) : ctid;
+            const int n_ent = my_e < m.nue ? 1 : 0;
+            const int w_ent = __popc(__ballot_sync(0xffffffffu, n_ent)); // entries of this warp: lanes 0..
+            uint4* buf_w = stage + (warp - 1) * 2 * RW;
+            unsigned char* fl_w = sh.sflag + (warp - 1) * 2 * RW;
             uint32_t my_ent = 0;
             int my_cnt = 0, my_off = 0, w_total = 0;
+            bool per_cell = MODE == 1; // cell by cell (dilute cells); 2: by all lanes of the warp
             auto stage_sparse = [&](int h) { // records [h RW, (h + 1) RW) of the warp's list
-                const uint4* src = S.cell_rec + (size_t)(my_ent & kEntCell) * cap;
-                const unsigned char f = (unsigned char)(my_ent >> 30);
-                for (int j = 0; j < my_cnt; j++) {
-                    const int c = my_off + j - h * RW;
-                    if (c >= 0 && c < RW) {
-                        cp_async(&buf_w[c], src + j, 16);
-                        fl_w[c] = f;
+                uint4* dst = buf_w + (h & 1) * RW;
+                unsigned char* fd = fl_w + (h & 1) * RW;
+                if (MODE == 1 || per_cell) {
+                    const uint4* src = S.cell_rec + (size_t)(my_ent & kEntCell) * cap;
+                    const unsigned char f = (unsigned char)(my_ent >> 30);
+                    for (int j = 0; j < my_cnt; j++) {
+                        const int c = my_off + j - h * RW;
+                        if (c >= 0 && c < RW) {
+                            cp_async(&dst[c], src + j, 16);
+                            fd[c] = f;
+                        }
+                    }
+                    cp_async_commit();
+                    return;
+                }
+#pragma unroll
+                for (int k = 0; k < KI; k++) {
+                    const int c = h * RW + lane + 32 * k;
+                    // the entry holding record c: the last of the warp's entries starting at or before it
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int mid = lo + step;
+                        const int om = __shfl_sync(0xffffffffu, my_off, mid & 31);
+                        if (mid < w_ent && om <= c) lo = mid;
+                    }
+                    const uint32_t ent = __shfl_sync(0xffffffffu, my_ent, lo);
+                    const int oo = __shfl_sync(0xffffffffu, my_off, lo);
+                    if (c < w_total) {
+                        cp_async(&dst[lane + 32 * k], S.cell_rec + (size_t)(ent & kEntCell) * cap + (c - oo), 16);
+                        fd[lane + 32 * k] = (unsigned char)(ent >> 30);
                     }
                 }
                 cp_async_commit();
@@ -757,16 +794,16 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             // SPARSE: started part-way through the Ewald loop, when the counts copied in during the
             // last move have landed; the records then land during the rest of it
             auto stage_sparse0 = [&]() {
-                if (ctid < m.nue) {
+                if (n_ent) {
                     int* cnt = sh.cntb[b];
-                    my_ent = m.ent[ctid];
+                    my_ent = m.ent[my_e];
                     if (recnt) {
                         cp_async_wait<0>(); // the earlier copy lands first
-                        cp_async(&cnt[ctid], S.cell_cnt + (my_ent & kEntCell), 4);
+                        cp_async(&cnt[my_e], S.cell_cnt + (my_ent & kEntCell), 4);
                         cp_async_commit();
                     }
                     cp_async_wait<0>();
-                    my_cnt = min(max(cnt[ctid], 0), cap);
+                    my_cnt = min(max(cnt[my_e], 0), cap);
                 }
                 int incl = my_cnt;
 #pragma unroll
@@ -776,10 +813,12 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 }
                 my_off = incl - my_cnt;
                 w_total = __shfl_sync(0xffffffffu, incl, 31);
+                if constexpr (MODE == 2) per_cell = __reduce_max_sync(0xffffffffu, (unsigned)my_cnt) <= 4u;
                 n_half = (w_total + RW - 1) / RW; // rounds of RW records
                 if (n_half > 0) stage_sparse(0);
+                if (n_half > 1) stage_sparse(1);
             };
-            if constexpr (!SPARSE) {
+            if constexpr (!occ) {
                 n_half = (n_items + HST - 1) / HST;
                 stage_half(0); // the first two half-rounds land while the Ewald loop runs
                 if (n_half > 1) stage_half(1);
@@ -841,7 +880,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 if (k < K) ff_add(acc1, ewald_k(k));
                 q_pending = 0;
             }
-            else if constexpr (SPARSE) {
+            else if constexpr (occ) {
                 stage_sparse0();
             }
             FF accp = ff_sum(acc0, acc1);
@@ -857,15 +896,14 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             const unsigned FULL = 0xffffffffu;
             const int wbase = (warp - 1) * 32;
             const float cut2 = S.rc2_pair > 0.f ? S.rc2_pair * 1.00002f : __int_as_float(0x7f800000);
-            for (int h = 0; SPARSE && h < n_half; h++) {
+            for (int h = 0; occ && h < n_half; h++) {
                 // round h of the warp's compact list: every record is an occupied slot of a stencil
                 // cell, with that cell's state flags (bit 0 trial state, bit 1 accepted state)
-                if (h > 0) {
-                    __syncwarp(); // every lane done reading the previous round
-                    stage_sparse(h);
-                }
-                cp_async_wait<0>();
+                if (h + 1 < n_half) cp_async_wait<1>(); // round h landed (h + 1 may still be in flight)
+                else cp_async_wait<0>();
                 __syncwarp();
+                const uint4* bw = buf_w + (h & 1) * RW;
+                const unsigned char* fw = fl_w + (h & 1) * RW;
                 const int nrec = min(RW, w_total - h * RW);
                 unsigned occ[2 * KI];
                 int nv = 0;
@@ -874,8 +912,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                     const int it = lane + 32 * k;
                     bool on = false, oo = false;
                     if (it < nrec) {
-                        const uint4 r = buf_w[it];
-                        const uint32_t f = fl_w[it];
+                        const uint4 r = bw[it];
+                        const uint32_t f = fw[it];
                         if (r.w != kEmptySlot && (int)(r.w & 0xFFFFFFu) != i) {
                             on = (f & 1u) && r2_fixed(S, rn, r) < cut2;
                             oo = (f & 2u) && r2_fixed(S, ro, r) < cut2;
@@ -901,7 +939,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                         }
                         const int src = (int)__fns(mk, 0, qq + 1);
                         const int st = mi & 1;
-                        const uint4 rj = buf_w[src + (mi >> 1) * 32];
+                        const uint4 rj = bw[src + (mi >> 1) * 32];
                         const int j = (int)(rj.w & 0xFFFFFFu);
                         const int pidx = ti * nt + (int)(rj.w >> 24);
                         const PairOut o = fast_pair_state<SPL>(S, pt[pidx], pidx, r2_fixed(S, st ? ro : rn, rj),
@@ -911,8 +949,12 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                         if (t < nmoves) n_pairs++;
                     }
                 }
+                if (h + 2 < n_half) { // refill this buffer with round h + 2
+                    __syncwarp(); // every lane done reading it
+                    stage_sparse(h + 2);
+                }
             }
-            for (int h = 0; !SPARSE && h < n_half; h++) {
+            for (int h = 0; !occ && h < n_half; h++) {
                 // half-round h complete (h + 1, when there is one, may still be in flight)
                 if (h + 1 < n_half) cp_async_wait<1>();
                 else cp_async_wait<0>();
@@ -1103,7 +1145,7 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
                 }
                 __syncthreads();
             }
-            hit = fast_parallel<SPARSE>(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc,
+            hit = fast_parallel<MODE>(S, nm, m, tid, NT, K ? tabs + ((t + 1) % 3) * 3 * TS : nullptr, nc,
                                         sh.cntb[(t + 1) % 3]);
         }
         tick(tid == 0 ? 6 : 13);
@@ -1198,16 +1240,22 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
     }
 }
 
-// The body twice, selected per CTA by its system: splined systems (FAU_PAIR_SPLINE) get their
-// own instance, so the pair path of the others compiles exactly as without the tables.
+// The body up to four times, selected per CTA by its system: splined systems (FAU_PAIR_SPLINE)
+// get their own instance, so the pair path of the others compiles exactly as without the tables,
+// and the three staging modes each theirs.
 template <int NWC, bool PHILOX, bool SPARSE>
 __global__ void __launch_bounds__(32 * (NWC + 1), NWC <= 2 ? 6 : (NWC <= 4 ? 4 : 2)) fast_chain_kernel(ChainArgs A)
 {
     __shared__ FastShared<NWC> sh;
-    // SPARSE: launched only for systems whose cell lists hold about a particle a cell or fewer
-    // (fast_sparse_cells); splined systems take the dense body
-    if (A.sys[blockIdx.x]->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true, false>(A, sh);
-    else fast_chain_body<NWC, PHILOX, false, SPARSE>(A, sh);
+    // SPARSE instances: systems flagged SYS_OCC (fast_occupied_slots; cell lists) run the body
+    // that stages the occupied slots of stencil cells, the others the whole-cell body; splined
+    // systems their own.  The choice depends only on the system.
+    const DevSys* G = A.sys[blockIdx.x];
+    const bool occ = SPARSE && (G->flags & SYS_OCC) && (G->flags & SYS_CELLS);
+    if (G->terms & FAU_PAIR_SPLINE) fast_chain_body<NWC, PHILOX, true, 0>(A, sh);
+    else if (occ && (G->flags & SYS_SPREAD)) fast_chain_body<NWC, PHILOX, false, SPARSE ? 2 : 0>(A, sh);
+    else if (occ) fast_chain_body<NWC, PHILOX, false, SPARSE ? 1 : 0>(A, sh);
+    else fast_chain_body<NWC, PHILOX, false, 0>(A, sh);
 }
 
 // dynamic shared memory of the pipelined kernel for K k-vectors, table size nc, nt classes and

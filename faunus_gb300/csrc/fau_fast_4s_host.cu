@@ -1,5 +1,5 @@
 // fau_fast_4s_host.cu -- pipelined chain kernel instantiation: 1 producer + 4 compute warps, host proposals,
-// sparse cell lists (only the occupied slots of a move's stencil cells are staged).
+// cell lists staged by their occupied slots only.
 #include "fau_fast.cuh"
 
 namespace fau {

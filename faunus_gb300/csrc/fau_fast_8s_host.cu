@@ -1,0 +1,12 @@
+// fau_fast_8s_host.cu -- pipelined chain kernel instantiation: 1 producer + 8 compute warps, host proposals,
+// cell lists staged by their occupied slots only.
+#include "fau_fast.cuh"
+
+namespace fau {
+
+cudaError_t fast_dispatch_8_host_sparse(const ChainArgs& a, int nb, int K, int nc, int nt, cudaStream_t st, bool prep)
+{
+    return launch_fast_inst<8, false, true>(a, nb, K, nc, nt, st, prep);
+}
+
+} // namespace fau
