@@ -57,7 +57,7 @@ class SysDesc(C.Structure):
         ("coulomb_poly_n", C.c_int), ("coulomb_erfc", C.c_double), ("coulomb_poly", C.c_double * 16),
         ("isobaric", C.c_int), ("pressure", C.c_double),
         ("spline_begin", iptr), ("spline_r2", dptr), ("spline_coef", dptr), ("spline_hs", iptr),
-        ("maxenergy_set", C.c_int), ("maxenergy", C.c_double),
+        ("maxenergy_set", C.c_int), ("maxenergy", C.c_double), ("cell_staging", C.c_int),
     ]
 
 

@@ -31,6 +31,7 @@ extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
 extern "C" int fau_internal_sys_maxe(const fau_sys* s);
+extern "C" int fau_internal_sys_occ(const fau_sys* s);
 extern "C" int fau_internal_sys_regrow(fau_sys* s);
 cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
                                         cudaStream_t st);
@@ -309,6 +310,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         std::stable_sort(order.begin() + nfast, order.end(), by_cost);
     }
     int Kf = 0, ncf = 0, ntf = 1, Ke = 0, nce = 0;
+    bool occf = false; // a pipelined system stages occupied slots: the instance holding that body
     for (int r = 0; r < n; r++) {
         int K, np, ng, mo, knc;
         fau_ctx* c2;
@@ -319,6 +321,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             Kf = std::max(Kf, K);
             ncf = std::max(ncf, knc);
             ntf = std::max(ntf, fau_internal_sys_classes(systems[order[r]]));
+            occf = occf || fau_internal_sys_occ(systems[order[r]]);
         }
         else {
             Ke = std::max(Ke, K);
@@ -491,7 +494,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact) BTRY(use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true) : prepare_chain(Ke, nce, threads, true));
-    if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true));
+    if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true, occf));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
         BTRY(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -513,12 +516,12 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                              : launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess)
                 return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
-            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, occf, st)) != cudaSuccess) return e;
             if (a.audit && (e = launch_fast_audit(a.sys, nfast, st)) != cudaSuccess) return e;
             return cudaStreamWaitEvent(st, join_ev, 0);
         }
         if (nfast) {
-            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, st)) != cudaSuccess) return e;
+            if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, occf, st)) != cudaSuccess) return e;
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
@@ -703,12 +706,14 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         if (!fast[i]) order.push_back(i);
     const int nexact = n - nfast;
     int Kf = 0, ncf = 0, ntf = 1, Ke = 0, nce = 0;
+    bool occf = false;
     for (int r = 0; r < n; r++) {
         const int i = order[r];
         if (r < nfast) {
             Kf = std::max(Kf, Kv[i]);
             ncf = std::max(ncf, ncv[i]);
             ntf = std::max(ntf, fau_internal_sys_classes(systems[i]));
+            occf = occf || fau_internal_sys_occ(systems[i]);
         }
         else {
             Ke = std::max(Ke, Kv[i]);
@@ -814,7 +819,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                           : launch_chain(ae, nexact, Ke, nce, 256, false, st)) == cudaSuccess;
         }
     }
-    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, st) == cudaSuccess;
+    if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, occf, st) == cudaSuccess;
     if (ok && nfast) ok = launch_fast_audit(a.sys, nfast, st) == cudaSuccess;
     if (ok && nfast && a.du_out) {
         unpack_du_kernel<<<nfast, 256, 0, st>>>(a.du_out, a.prop_off, a.n_moves);

@@ -757,7 +757,7 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     for (size_t a = 0; a < lay.itype_type.size() && a < (size_t)kMaxITypes; a++) h.itype_type[a] = lay.itype_type[a];
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0) |
-              (fast_occupied_slots(lay.cells) ? SYS_OCC : 0) |
+              ((fast_occupied_slots(lay.cells) && d->cell_staging == 0) ? SYS_OCC : 0) |
               (fast_spread_cells(lay.cells, n, lay.cdim[0] * lay.cdim[1] * lay.cdim[2]) ? SYS_SPREAD : 0);
     h.beta_scale = 1.0;
     h.maxe = d->maxenergy_set ? 1 : 0;
@@ -1913,6 +1913,7 @@ int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
 double fau_internal_sys_volume(const fau_sys* s) { return s->h.L[0] * s->h.L[1] * s->h.L[2]; }
 int fau_internal_sys_maxe(const fau_sys* s) { return s->h.maxe; }
+int fau_internal_sys_occ(const fau_sys* s) { return (s->h.flags & SYS_OCC) && (s->h.flags & SYS_CELLS) ? 1 : 0; }
 // after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
 // lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)
 int fau_internal_sys_regrow(fau_sys* s)

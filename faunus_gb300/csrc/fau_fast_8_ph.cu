@@ -1,0 +1,12 @@
+// fau_fast_8_ph.cu -- pipelined chain kernel instantiation: 1 producer + 8 compute warps, device (Philox) proposals,
+// whole cells only (launches with no system flagged for occupied-slot staging).
+#include "fau_fast.cuh"
+
+namespace fau {
+
+cudaError_t fast_dispatch_8_ph(const ChainArgs& a, int nb, int K, int nc, int nt, cudaStream_t st, bool prep)
+{
+    return launch_fast_inst<8, true, false>(a, nb, K, nc, nt, st, prep);
+}
+
+} // namespace fau

@@ -396,29 +396,33 @@ size_t fast_smem_bytes_total(int K, int nc, int nt)
 }
 
 static cudaError_t fast_launch_impl(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox,
-                                    cudaStream_t st, bool prepare_only)
+                                    bool occ, cudaStream_t st, bool prepare_only)
 {
-    if (warps == 4)
+    if (warps == 4 && occ)
         return philox ? fast_dispatch_4_ph_sparse(a, nblocks, K, nc, nt, st, prepare_only)
                       : fast_dispatch_4_host_sparse(a, nblocks, K, nc, nt, st, prepare_only);
-    if (warps == 8)
-        return philox ? fast_dispatch_8_ph_sparse(a, nblocks, K, nc, nt, st, prepare_only)
-                      : fast_dispatch_8_host_sparse(a, nblocks, K, nc, nt, st, prepare_only);
+    if (warps == 4)
+        return philox ? fast_dispatch_4_ph(a, nblocks, K, nc, nt, st, prepare_only)
+                      : fast_dispatch_4_host(a, nblocks, K, nc, nt, st, prepare_only);
+    if (warps == 8 && philox)
+        return occ ? fast_dispatch_8_ph_sparse(a, nblocks, K, nc, nt, st, prepare_only)
+                   : fast_dispatch_8_ph(a, nblocks, K, nc, nt, st, prepare_only);
     if (warps == 2)
         return philox ? fast_dispatch_2_ph(a, nblocks, K, nc, nt, st, prepare_only)
                       : fast_dispatch_2_host(a, nblocks, K, nc, nt, st, prepare_only);
     return cudaErrorInvalidValue;
 }
 
-cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox)
+cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox, bool occ)
 {
     ChainArgs a{};
-    return fast_launch_impl(a, 0, K, nc, nt, warps, philox, nullptr, true);
+    return fast_launch_impl(a, 0, K, nc, nt, warps, philox, occ, nullptr, true);
 }
 
-cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st)
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, bool occ,
+                        cudaStream_t st)
 {
-    return fast_launch_impl(a, nblocks, K, nc, nt, warps, philox, st, false);
+    return fast_launch_impl(a, nblocks, K, nc, nt, warps, philox, occ, st, false);
 }
 
 // Partials layout in d_out: [0, kTotalPairBlocks) pair sums per block, then

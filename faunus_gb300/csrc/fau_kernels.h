@@ -78,10 +78,14 @@ constexpr int kFastMaxNc = 40;
 size_t fast_smem_bytes_total(int K, int nc, int nt);
 // the FP64 audit of the pipelined kernel's probe moves (one CTA per system of `sys`)
 cudaError_t launch_fast_audit(DevSys* const* sys, int n, cudaStream_t st);
-// 4 and 8 compute warps: instances that stage either the occupied slots of a move's stencil
-// cells (systems flagged SYS_OCC, chosen per CTA) or whole cells; 2 compute warps: whole cells
-cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox);
-cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, cudaStream_t st);
+// occ: a system of the launch is flagged SYS_OCC.  Then 4 and 8 compute warps run the instance
+// holding every staging body, each CTA choosing by its system; otherwise the instance holding
+// only the whole-cell body (the same code for those systems, without the register pressure of
+// the occupied-slot bodies, which spill in the combined kernel).  2 compute warps: whole cells.
+// 8 compute warps take device (Philox) proposals only.
+cudaError_t prepare_fast(int K, int nc, int nt, int warps, bool philox, bool occ);
+cudaError_t launch_fast(const ChainArgs& a, int nblocks, int K, int nc, int nt, int warps, bool philox, bool occ,
+                        cudaStream_t st);
 // the occupied-slot rules, fixed per system when it is made: any cell list stages its occupied
 // slots only (from 0.2 particles a cell in dilute salt to tens in dense primitive models); with
 // more particles than cells the stencil's cells are spread over all compute warps, otherwise
@@ -90,9 +94,11 @@ inline bool fast_occupied_slots(bool cells) { return cells; }
 inline bool fast_spread_cells(bool cells, int n, int ncell) { return cells && n > ncell; }
 cudaError_t fast_dispatch_2_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_2_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_4_host(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_4_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
+cudaError_t fast_dispatch_8_ph(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_4_host_sparse(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_4_ph_sparse(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
-cudaError_t fast_dispatch_8_host_sparse(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 cudaError_t fast_dispatch_8_ph_sparse(const ChainArgs&, int, int, int, int, cudaStream_t, bool);
 // cells: the system's groups are all atomic and it has a cell list (O(N x neighbours) pair sum)
 cudaError_t launch_total(const DevSys* dsys, int n, int K, double* d_out, int* d_flags, cudaStream_t st,

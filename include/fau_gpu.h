@@ -152,6 +152,10 @@ typedef struct fau_sys_desc {
        run in the chain kernel (FP32C form, whatever their precision), also in batches.     */
     int maxenergy_set;
     double maxenergy;
+    /* pipelined kernel, systems with a cell list: 0 = each move copies the occupied slots of its
+       stencil cells only (the library's choice); 1 = whole cells.  Batches that mix system
+       shapes (a job server) run faster when every chain takes the same code path.           */
+    int cell_staging;
 } fau_sys_desc;
 
 /* Per-term energies in kT (Hamiltonian term order: self, nonbonded, ewald). */

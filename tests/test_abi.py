@@ -63,6 +63,7 @@ int main(void) {
   O(fau_sys_desc, spline_begin) O(fau_sys_desc, spline_hs) O(fau_spline_opts, hardsphere)
   O(fau_batch_params, time_budget_ns) O(fau_batch_params, moves_out) O(fau_batch_params, swap_energy_out) O(fau_batch_params, no_audit) O(fau_batch_stats, du_err_samples)
   O(fau_batch_params, volume_dv) O(fau_batch_params, volume_method) O(fau_batch_stats, volume_accepted) O(fau_sys_desc, maxenergy)
+  O(fau_sys_desc, cell_staging)
   return 0;
 }
 """
@@ -99,7 +100,8 @@ def test_struct_layouts_match_header(tmp_path):
             "fau_batch_params.volume_dv": A.BatchParams.volume_dv.offset,
             "fau_batch_params.volume_method": A.BatchParams.volume_method.offset,
             "fau_batch_stats.volume_accepted": A.BatchStats.volume_accepted.offset,
-            "fau_sys_desc.maxenergy": A.SysDesc.maxenergy.offset}
+            "fau_sys_desc.maxenergy": A.SysDesc.maxenergy.offset,
+            "fau_sys_desc.cell_staging": A.SysDesc.cell_staging.offset}
     for k, v in offs.items():
         assert int(out[k]) == v, k
 

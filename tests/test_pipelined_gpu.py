@@ -175,6 +175,31 @@ def test_pipelined_alone_equals_in_mix(ctx):
     assert np.array_equal(b1.positions(), b2.positions())
 
 
+def test_whole_cell_body_is_the_same_in_either_instance(ctx):
+    """A launch whose systems all stage whole cells (no cell list, or cell_staging=1) runs the
+    kernel instance holding that body alone; beside a system staging occupied slots, the instance
+    holding every body.  A chain is the same, bit for bit, in either; whole-cell and occupied-slot
+    staging of one system agree to the energy tolerance."""
+    import dataclasses
+    bulk = configs.bulk_ewald(n_salt=500, seed=11)
+    whole = dataclasses.replace(bulk, cell_staging=1)
+    pm = configs.primitive_model(n=200, seed=12)
+    alone = [ctx.create(whole), ctx.create(pm)]
+    for i, s in enumerate(alone):
+        ctx.run_batch([s], 3000, seed=9, streams=[i], counters=[0], dp=2.0, threads=160)
+    mixed = [ctx.create(whole), ctx.create(pm), ctx.create(bulk)]
+    ctx.run_batch(mixed, 3000, seed=9, streams=[0, 1, 2], counters=[0] * 3, dp=2.0, threads=160)
+    for x, y in zip(alone, mixed):
+        assert np.array_equal(x.positions(), y.positions()) and x.running_energy() == y.running_energy()
+    occ = ctx.create(bulk)
+    ctx.run_batch([occ], 3000, seed=9, streams=[0], counters=[0], dp=2.0, threads=160)
+    if np.array_equal(occ.positions(), alone[0].positions()):  # barring a near tie, the same chain
+        e = alone[0].energy_total()["total"]
+        assert abs(occ.running_energy() - alone[0].running_energy()) <= 1e-6 * max(1.0, abs(e))
+    for s in alone + mixed + [occ]:
+        _energy_consistent(s)
+
+
 def test_pipelined_parallel_tempering(ctx):
     specs, temps = configs.pt_replicas(n_rep=8, n_min=100, n_max=300)
     systems = [ctx.create(s) for s in specs]
