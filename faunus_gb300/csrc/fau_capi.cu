@@ -245,6 +245,7 @@ int validate(const fau_sys_desc* d)
     for (int k = 0; k < 3; k++)
         if (!(d->box[k] > 0.0)) return fail(FAU_ERR_ARG, "box lengths must be positive");
     if (d->n_types < 1) return fail(FAU_ERR_ARG, "n_types must be >= 1");
+    if (d->cell_staging < 0 || d->cell_staging > 2) return fail(FAU_ERR_ARG, "cell_staging must be 0, 1 or 2");
     for (int i = 0; i < d->n_particles; i++) {
         if (d->type[i] < 0 || d->type[i] >= d->n_types) return fail(FAU_ERR_ARG, "particle %d: type out of range", i);
         for (int k = 0; k < 3; k++) {
@@ -755,10 +756,11 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
         }
     }
     for (size_t a = 0; a < lay.itype_type.size() && a < (size_t)kMaxITypes; a++) h.itype_type[a] = lay.itype_type[a];
+    const bool spread = fast_spread_cells(lay.cells, n, lay.cdim[0] * lay.cdim[1] * lay.cdim[2]);
+    const bool occ = fast_occupied_slots(lay.cells) && (d->cell_staging == 0 || (d->cell_staging == 2 && spread));
     h.flags = (lay.cells ? SYS_CELLS : 0) | (d->ewald.enabled ? SYS_EWALD : 0) |
               ((d->ewald.enabled && d->ewald.epss >= 1.0) ? SYS_SURFACE : 0) | (has_self ? SYS_SELF : 0) |
-              ((fast_occupied_slots(lay.cells) && d->cell_staging == 0) ? SYS_OCC : 0) |
-              (fast_spread_cells(lay.cells, n, lay.cdim[0] * lay.cdim[1] * lay.cdim[2]) ? SYS_SPREAD : 0);
+              (occ ? SYS_OCC : 0) | (spread ? SYS_SPREAD : 0);
     h.beta_scale = 1.0;
     h.maxe = d->maxenergy_set ? 1 : 0;
     h.maxenergy = d->maxenergy_set ? d->maxenergy : std::numeric_limits<double>::infinity();

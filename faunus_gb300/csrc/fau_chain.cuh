@@ -182,7 +182,9 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
         if (dprot > 0.0) {
             // uniform axis, angle dprot (U - 1/2); the half-angle sine/cosine and the axis come
             // from the FP32 pipe (FP64 sin/cos is ~100 instructions on a slow pipe) and the
-            // quaternion is normalised in FP64, so rotations stay unit to FP64 precision
+            // quaternion (cos, sin a) is normalised once in FP64, so rotations stay unit to FP64
+            // precision.  The FP32 axis' norm (1 within 2^-22) scales tan(angle / 2) by the same
+            // factor whatever the sign of the angle, so the proposal stays symmetric.
             const float az = fmaf(2.f, u01_24(c2.z), -1.f);
             float as, ac;
             sincospif(2.f * u01_24(c2.w), &as, &ac);
@@ -192,8 +194,7 @@ static __device__ __noinline__ Proposal philox_proposal(const DevSys& S, unsigne
             float sh, ch;
             sincospif(ha_pi, &sh, &ch);
             const double ax = f2d_bits(axy * ac), ay = f2d_bits(axy * as), az_d = f2d_bits(az);
-            const double ra = rsqrt(__dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az_d, az_d)));
-            const double c = f2d_bits(ch), s = f2d_bits(sh) * ra;
+            const double c = f2d_bits(ch), s = f2d_bits(sh);
             const double q0 = c, q1 = s * ax, q2 = s * ay, q3 = s * az_d;
             const double rq = rsqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
             p.quat[0] = q0 * rq;
@@ -221,18 +222,20 @@ __device__ __forceinline__ Proposal load_proposal(const fau_proposal& f)
     return p;
 }
 
+// (xn - xo) / L of axis d under minimum image; |v| > L/2 compared as bit patterns
+__device__ __forceinline__ float min_image_frac1(const DevSys& S, double xn, double xo, int d)
+{
+    double v = __dsub_rn(xn, xo);
+    const long long b = __double_as_longlong(v);
+    if ((b & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(S.half[d])) v = b < 0 ? __dadd_rn(v, S.L[d]) : __dsub_rn(v, S.L[d]);
+    return (float)v * S.inv_f[d];
+}
+
 // (xn - xo) / L per axis under minimum image (Chameleon::vdist src/geometry.h:429-458)
 __device__ __forceinline__ float3 min_image_frac(const DevSys& S, const double* xn, const double* xo)
 {
-    float g[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        double v = __dsub_rn(xn[d], xo[d]);
-        if (v > S.half[d]) v = __dsub_rn(v, S.L[d]);
-        else if (v < -S.half[d]) v = __dadd_rn(v, S.L[d]);
-        g[d] = (float)v * S.inv_f[d];
-    }
-    return make_float3(g[0], g[1], g[2]);
+    return make_float3(min_image_frac1(S, xn[0], xo[0], 0), min_image_frac1(S, xn[1], xo[1], 1),
+                       min_image_frac1(S, xn[2], xo[2], 2));
 }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
@@ -327,63 +330,70 @@ static __device__ __noinline__ void prepare_move(const DevSys& S, MoveShared& ms
         }
     }
     else if (p.kind == FAU_MOVE_MOLECULAR) {
+        // One lane per (atom, axis), ten atoms a round: the FP64 pipe issues one warp instruction
+        // per 64 cycles whatever the number of active lanes, so the three coordinates' chains
+        // share each instruction.  Every lane runs the same operations on the same values as a
+        // per-atom evaluation (Group::translate, Group::rotate, geometry.h:613-627), so the
+        // positions are the same bits; the rotation's cross products take the other two
+        // coordinates from the atom's other lanes.
         const int g = p.index;
         const int b = S.g_begin[g];
         m = S.g_begin[g + 1] - b;
-        double cm[3];
-#pragma unroll
-        for (int d = 0; d < 3; d++)
-            cm[d] = boundary1(__dadd_rn(S.g_cm[3 * g + d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
-        double dM[3] = {0, 0, 0};
-        if (lane < m && m <= kMaxGroupAtoms) {
-            const int i = b + lane;
-            const double xo[3] = {S.x[i], S.y[i], S.z[i]};
-            double v[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) v[d] = boundary1(__dadd_rn(xo[d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
+        const unsigned FULL = 0xffffffffu;
+        const int dl = lane % 3, la = lane / 3, lb = lane - dl;
+        const int l1 = lb + (dl + 1) % 3, l2 = lb + (dl + 2) % 3; // lanes of axes d+1, d+2 (mod 3)
+        const double Ld = S.L[dl], hd = S.half[dl], id = S.inv[dl];
+        const double cmd = boundary1(__dadd_rn(S.g_cm[3 * g + dl], p.dr[dl]), Ld, hd, id);
+        const double u1 = p.quat[1 + (dl + 1) % 3], u2 = p.quat[1 + (dl + 2) % 3];
+        const double* X = dl == 0 ? S.x : (dl == 1 ? S.y : S.z);
+        double dMs = 0.0; // lanes 0..2: the group's dipole change, summed in atom order
+        for (int a0 = 0; m <= kMaxGroupAtoms && a0 < m; a0 += 10) { // uniform over the warp
+            const int a = a0 + la;
+            const bool act = lane < 30 && a < m;
+            const int i = b + (act ? a : 0);
+            const double xo = X[i];
+            double v = boundary1(__dadd_rn(xo, p.dr[dl]), Ld, hd, id);
             if (p.rotate) {
-#pragma unroll
-                for (int d = 0; d < 3; d++) v[d] = boundary1(__dsub_rn(v[d], cm[d]), S.L[d], S.half[d], S.inv[d]);
-                quat_rotate(p.quat, v);
-#pragma unroll
-                for (int d = 0; d < 3; d++) v[d] = boundary1(__dadd_rn(v[d], cm[d]), S.L[d], S.half[d], S.inv[d]);
+                v = boundary1(__dsub_rn(v, cmd), Ld, hd, id);
+                const double v1 = __shfl_sync(FULL, v, l1), v2 = __shfl_sync(FULL, v, l2);
+                double t = __dsub_rn(__dmul_rn(u1, v2), __dmul_rn(u2, v1)); // t = 2 u x v
+                t = __dadd_rn(t, t);
+                const double t1 = __shfl_sync(FULL, t, l1), t2 = __shfl_sync(FULL, t, l2);
+                const double c = __dsub_rn(__dmul_rn(u1, t2), __dmul_rn(u2, t1)); // u x t
+                v = __dadd_rn(__dadd_rn(v, __dmul_rn(p.quat[0], t)), c);
+                v = boundary1(__dadd_rn(v, cmd), Ld, hd, id);
             }
             const uint4 ro = S.rec[i];
-            uint4 rn;
-            rn.x = to_fixed(v[0], S.fx_scale[0]);
-            rn.y = to_fixed(v[1], S.fx_scale[1]);
-            rn.z = to_fixed(v[2], S.fx_scale[2]);
-            rn.w = ro.w;
-            ms.rec_old[lane] = ro;
-            ms.rec_new[lane] = rn;
             const double q = S.itype_qd[ro.w >> 24];
-            ms.q[lane] = (float)q;
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                ms.xn[lane][d] = v[d];
-                ms.xo[lane][d] = xo[d];
-                dM[d] = __dmul_rn(q, __dsub_rn(v[d], xo[d]));
+            const double dMa = __dmul_rn(q, __dsub_rn(v, xo));
+            if (act) {
+                reinterpret_cast<uint32_t*>(&ms.rec_new[a])[dl] = to_fixed(v, S.fx_scale[dl]);
+                ms.xn[a][dl] = v;
+                ms.xo[a][dl] = xo;
+                reinterpret_cast<float*>(&ms.g[a])[dl] = min_image_frac1(S, v, xo, dl);
+                if (dl == 0) {
+                    ms.rec_old[a] = ro;
+                    ms.rec_new[a].w = ro.w;
+                    ms.q[a] = (float)q;
+                }
             }
-            ms.g[lane] = min_image_frac(S, v, xo);
+            const int na = min(10, m - a0);
+            for (int k = 0; k < na; k++) { // lane d adds atom a0 + k's component d
+                const double x = __shfl_sync(FULL, dMa, 3 * k + dl);
+                if (lane < 3) dMs = __dadd_rn(dMs, x);
+            }
         }
-#pragma unroll
-        for (int d = 0; d < 3; d++) { // sum over the group's atoms in atom order
-            double acc = 0.0;
-            for (int a = 0; a < m && a < 32; a++) acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, dM[d], a));
-            dM[d] = acc;
+        if (lane < 3) {
+            ms.cm_new[dl] = cmd;
+            ms.dM[dl] = dMs;
+            reinterpret_cast<uint32_t*>(&ms.cmrec_new)[dl] = to_fixed(cmd, S.fx_scale[dl]);
         }
         if (lane == 0) {
             ms.m = m;
             ms.first = b;
             if (m > kMaxGroupAtoms) ms.stop = FAU_ERR_ARG;
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                ms.cm_new[d] = cm[d];
-                ms.dM[d] = dM[d];
-            }
             ms.cmrec_old = S.g_cmrec[g];
-            ms.cmrec_new = make_uint4(to_fixed(cm[0], S.fx_scale[0]), to_fixed(cm[1], S.fx_scale[1]),
-                                      to_fixed(cm[2], S.fx_scale[2]), 0u);
+            ms.cmrec_new.w = 0u;
         }
     }
     else if (lane == 0) {

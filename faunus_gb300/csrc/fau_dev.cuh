@@ -292,7 +292,10 @@ __device__ __forceinline__ float d2f_trunc01(double u)
 // Chameleon::boundary (reference src/geometry.h:407-427) with anint (:132-135).
 __device__ __forceinline__ double boundary1(double a, double L, double half, double inv)
 {
-    if (fabs(a) > half) {
+    // |a| > half (half > 0) compared as bit patterns on the integer pipe: an FP64 compare is an
+    // FP64-pipe instruction, one warp instruction per 64 cycles on this GPU (NaN takes the branch
+    // and stays NaN, as it does untouched)
+    if ((__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFLL) > __double_as_longlong(half)) {
         const double t = __dmul_rn(a, inv);
         const int n = (int)(t > 0.0 ? __dadd_rn(t, 0.5) : __dsub_rn(t, 0.5));
         a = __dsub_rn(a, __dmul_rn(L, (double)n));

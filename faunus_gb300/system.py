@@ -214,7 +214,8 @@ class SystemSpec:
     cutoff_g2g_pairs: Optional[np.ndarray] = None  # (n_molids, n_molids) per molecule-kind pair; see group_cutoff
     isobaric_pressure: Optional[float] = None  # Isobaric term's pressure (kT/A^3, see pressure_kt); None: no term
     maxenergy: Optional[float] = None     # Hamiltonian maxenergy (kT): terms summed up to the first >= it; None: +inf
-    cell_staging: int = 0                 # pipelined kernel: 0 occupied slots of stencil cells, 1 whole cells
+    cell_staging: int = 0                 # pipelined kernel: 0 occupied slots of stencil cells, 1 whole cells,
+                                          # 2 occupied slots when there are more particles than cells
     spline: Optional[dict] = None         # FAU_PAIR_SPLINE tables: begin (T*T+1), r2, coef, hs (see splined)
     ewald: Optional[dict] = None          # alpha, ncutoff, spherical_sum, epss
     precision: int = A.FAU_PREC_FP32C

@@ -153,8 +153,9 @@ typedef struct fau_sys_desc {
     int maxenergy_set;
     double maxenergy;
     /* pipelined kernel, systems with a cell list: 0 = each move copies the occupied slots of its
-       stencil cells only (the library's choice); 1 = whole cells.  Batches that mix system
-       shapes (a job server) run faster when every chain takes the same code path.           */
+       stencil cells only (the library's choice); 1 = whole cells; 2 = occupied slots when the
+       system holds more particles than cells, else whole cells.  Batches that mix system shapes
+       (a job server) run faster when most chains take the same code path.                   */
     int cell_staging;
 } fau_sys_desc;
 
