@@ -456,8 +456,10 @@ def plain_form(ctx, base, moves: int = 400) -> dict:
 
 def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: int = 2, pt_budget_s: float = 60.0) -> dict:
     """Device-timed throughput of the other configurations (seconds each): the primitive
-    model (200 hard-sphere ions) and rigid SPC/E water (1,000 molecules, molecular moves)
-    as replica batches, and the 256-walker parallel-tempering ladder (N 100..5,000)."""
+    model (200 hard-sphere ions; FP32C and, as specified, FP64) and rigid SPC/E water (1,000
+    molecules, molecular moves) as replica batches, and the 256-walker parallel-tempering ladder
+    (N 100..5,000)."""
+    from faunus_gb300 import _capi as A
     out = {}
 
     def batch_rate(spec, R, M, **kw):
@@ -474,6 +476,11 @@ def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: in
 
     mps, pps = batch_rate(configs.primitive_model(n=200), replicas, 20000)
     out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps}
+    # the primitive model as specified, in FP64: FP64 replica chains (fau_fp64.cu)
+    mps, pps = batch_rate(configs.primitive_model(n=200, precision=A.FAU_PREC_FP64), replicas, 20000)
+    out["primitive_model_200_fp64"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
+                                       "kernel": "FP64 replica chains (plain FP64 pair sums and decision, "
+                                                 "all pairs, one CTA per system)"}
     mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 5000)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
                               "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
@@ -502,6 +509,18 @@ def parallel_tempering(ctx, configs, sweeps: int, blocks: int, budget_s: float) 
                        seed=3, dp=2.0, counter_base=1)
     for s_ in systems:
         s_.close()
+    # the uniform-replica comparison at equal total particles: 256 walkers of the ladder's mean
+    # size at its middle temperature, 10 sweeps each
+    nm = int(round(n.mean() / 2) * 2)
+    uni = configs.primitive_model(n=nm, L=50.0 * (nm / 200.0) ** (1.0 / 3.0), lB=7.1 * 298.0 / 316.0,
+                                  temperature=316.0, seed=5)
+    ub = ctx.create(uni)
+    usys = [ub] + [ub.clone() for _ in range(len(specs) - 1)]
+    ctx.run_batch(usys, nm, seed=1, dp=2.0)
+    su = ctx.run_batch(usys, 10 * nm, seed=1, counter_base=nm, dp=2.0)
+    for s_ in usys:
+        s_.close()
+    uni_mps = su["moves"] / (su["device_ms"] * 1e-3)
     longest = int(np.argmax(cyc))
     return {"moves_per_s": st["moves"] / (st["device_ms"] * 1e-3), "moves": st["moves"],
             "device_s": st["device_ms"] * 1e-3, "swap_rounds": blocks,
@@ -509,6 +528,10 @@ def parallel_tempering(ctx, configs, sweeps: int, blocks: int, budget_s: float) 
             "swaps_attempted": st["swaps_attempted"], "swaps_accepted": st["swaps_accepted"],
             "swap_acceptance": st["swaps_accepted"] / max(1, st["swaps_attempted"]),
             "walkers": len(specs), "particles_total": int(n.sum()),
+            "uniform_equivalent": {"walkers": len(specs), "n": nm, "moves_per_s": uni_mps,
+                                   "pt_over_uniform": st["moves"] / (st["device_ms"] * 1e-3) / uni_mps,
+                                   "what": "the same number of walkers of the ladder's mean size (equal total "
+                                           "particles), no swaps, 10 sweeps each"},
             "calibration_s_per_sweep": sec_per_sweep,
             "longest_walker": {"n": int(n[longest]), "cycles_per_move": float(cyc[longest]) / float(n[longest])},
             "note": ("walker i moves sweeps x N_i times between swap rounds (ParallelTempering every 1,000 sweeps); "

@@ -31,6 +31,7 @@ extern "C" int fau_internal_ctx_scratch(fau_ctx* c, size_t bytes, void** out);
 extern "C" int fau_internal_sys_all_atomic(const fau_sys* s);
 extern "C" int fau_internal_sys_classes(const fau_sys* s);
 extern "C" int fau_internal_sys_maxe(const fau_sys* s);
+extern "C" int fau_internal_sys_fp64(const fau_sys* s);
 extern "C" int fau_internal_sys_occ(const fau_sys* s);
 extern "C" int fau_internal_sys_regrow(fau_sys* s);
 cudaError_t fau_internal_sampler_launch(fau_sampler* s, DevSys* const* d_sys, int n, const int* d_slots, int max_n,
@@ -151,6 +152,24 @@ double u01_53_host(uint32_t a, uint32_t b)
 
 extern "C" double fau_internal_sys_volume(const fau_sys* s);
 
+namespace {
+const char* const kFp64Mixed = "a batch holds FP64 systems (FAU_PREC_FP64) only or none";
+const char* const kFp64Form = "FP64 chains run single-atom (or empty) moves on systems without a finite maxenergy";
+
+// 1: every system of the batch is an FP64 system, 0: none is; -1: both kinds; -2: an FP64 system
+// the FP64 chain kernel does not run (a finite maxenergy, or molecular moves where `mol` flags them)
+int fp64_batch(fau_sys* const* systems, int n, const uint8_t* mol)
+{
+    int k = 0;
+    for (int i = 0; i < n; i++) k += fau_internal_sys_fp64(systems[i]);
+    if (k == 0) return 0;
+    if (k != n) return -1;
+    for (int i = 0; i < n; i++)
+        if (fau_internal_sys_maxe(systems[i]) || (mol && mol[i])) return -2;
+    return 1;
+}
+} // namespace
+
 // NPT blocks: each block's moves through fau_run_batch (one graph launch), then one VolumeMove
 // per system (VolumeMove::_move and setNewVolume, src/move.cpp:994-1006, decided as
 // fau_volume_move decides it)
@@ -263,6 +282,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         mol[i] = (uint8_t)mo;
         if (pt) tref[i] = P->temperatures[i];
     }
+    // systems made with FAU_PREC_FP64 run in the FP64 chain kernel: a batch holds FP64 systems only
+    // or none, and their chains are single-atom moves without a finite maxenergy
+    const int f64 = fp64_batch(systems, n, mol.data());
+    if (f64 < 0) return f64 == -1 ? fau_internal_fail(FAU_ERR_ARG, kFp64Mixed) : fau_internal_fail(FAU_ERR_ARG, kFp64Form);
     // kernel choice: threads 0, 96, 160 or 288 -> the pipelined kernel (1 producer + 4, 2, 4 or 8
     // compute warps) for every system whose device proposals are single-atom moves (the others run
     // in the 256-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems
@@ -280,7 +303,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         DevSys* dd;
         fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
         // a finite maxenergy: the chain kernel (the only one that forms each state's term sums)
-        fast[i] = use_fast && !mol[i] && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
+        fast[i] = !f64 && use_fast && !mol[i] && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
     }
     std::vector<int> order;   // kernel order: pipelined-kernel systems first
     order.reserve(n);
@@ -328,12 +351,13 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             nce = std::max(nce, knc);
         }
     }
-    if ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
-        (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
+    if (f64 ? fp64_smem_bytes(Ke) + 16384 > 227 * 1024
+            : ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
+               (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024)))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
     // molecular-move systems: the pipelined molecular kernel (preparation of the next move overlapped
     // with the current one) unless a chain-kernel size was requested; FAU_MOL_KERNEL=0 turns it off
-    bool use_mol = use_fast && nexact > 0;
+    bool use_mol = !f64 && use_fast && nexact > 0;
     if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
     for (int r = nfast; r < n && use_mol; r++)
         if (!mol[order[r]] || fau_internal_sys_maxe(systems[order[r]])) use_mol = false;
@@ -493,7 +517,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.counters) ae.counters = a.counters + nfast;
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
-    if (nexact) BTRY(use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true) : prepare_chain(Ke, nce, threads, true));
+    if (nexact)
+        BTRY(f64       ? prepare_fp64(Ke, true)
+             : use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true)
+                       : prepare_chain(Ke, nce, threads, true));
     if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true, occf));
     if (nfast && nexact) {
         BTRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
@@ -524,6 +551,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, occf, st)) != cudaSuccess) return e;
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
+        if (f64) return launch_fp64(ae, nexact, Ke, true, st);
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
                        : launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };
@@ -696,6 +724,16 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         // in the 256-thread chain kernel; the kernels check every proposal as they read it
         fast[i] = fau_internal_sys_all_atomic(systems[i]) && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
     }
+    // FP64 systems: the FP64 chain kernel (a batch holds FP64 systems only or none; their proposals
+    // are single-atom or empty moves)
+    const int f64 = fp64_batch(systems, n, nullptr);
+    if (f64 < 0) return f64 == -1 ? fau_internal_fail(FAU_ERR_ARG, kFp64Mixed) : fau_internal_fail(FAU_ERR_ARG, kFp64Form);
+    if (f64) {
+        for (long long m = 0; m < total; m++)
+            if (props[m].kind != FAU_MOVE_ATOMIC && props[m].kind != FAU_MOVE_NONE)
+                return fau_internal_fail(FAU_ERR_ARG, kFp64Form);
+        for (int i = 0; i < n; i++) fast[i] = 0;
+    }
     // kernel order puts the pipelined-kernel systems first
     std::vector<int> order;
     order.reserve(n);
@@ -720,13 +758,15 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             nce = std::max(nce, ncv[i]);
         }
     }
-    if ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
-        (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024))
+    if (f64 ? fp64_smem_bytes(Ke) + 16384 > 227 * 1024
+            : ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
+               (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024)))
         return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
+    if (f64 && prepare_fp64(Ke, false) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "FP64 chain kernel attributes");
     // systems of molecular groups only whose proposals are all molecular (or empty) run in the
     // pipelined molecular kernel when every other-than-single-atom system qualifies; otherwise
     // the chain kernel runs them (it takes every proposal kind)
-    bool use_mol = nexact > 0;
+    bool use_mol = !f64 && nexact > 0;
     if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
     for (int r = nfast; r < n && use_mol; r++) {
         const int i = order[r];
@@ -813,6 +853,9 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                  (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st2, false)
                           : launch_chain(ae, nexact, Ke, nce, 256, false, st2)) == cudaSuccess &&
                  cudaEventRecord(join_ev, st2) == cudaSuccess;
+        }
+        else if (f64) {
+            ok = launch_fp64(ae, nexact, Ke, false, st) == cudaSuccess;
         }
         else {
             ok = (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)

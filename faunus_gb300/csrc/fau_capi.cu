@@ -1915,6 +1915,7 @@ int fau_internal_sys_all_atomic(const fau_sys* s) { return s->all_atomic ? 1 : 0
 int fau_internal_sys_classes(const fau_sys* s) { return s->h.nt; }
 double fau_internal_sys_volume(const fau_sys* s) { return s->h.L[0] * s->h.L[1] * s->h.L[2]; }
 int fau_internal_sys_maxe(const fau_sys* s) { return s->h.maxe; }
+int fau_internal_sys_fp64(const fau_sys* s) { return s->precision == FAU_PREC_FP64 ? 1 : 0; }
 int fau_internal_sys_occ(const fau_sys* s) { return (s->h.flags & SYS_OCC) && (s->h.flags & SYS_CELLS) ? 1 : 0; }
 // after a batched chain stopped on a full cell: twice the capacity of the particle cells (their
 // lists rebuilt from the positions) and of the mass-centre cells (listed again by the next launch)

@@ -1,0 +1,355 @@
+// fau_fp64.cu -- FP64 replica chains: the persistent Metropolis chain of single-atom moves in
+// plain FP64 arithmetic, one CTA per system, for systems made with FAU_PREC_FP64.
+//
+// The arithmetic of the plain single-system FP64 form (plain_pair_kernel, plain_ewald_kernel and
+// the host decision of fau_trial_atomic) run as a batched chain: the move, its energy change,
+// the Metropolis decision and the commit stay on the device, so a batch of FP64 systems runs as
+// a persistent launch instead of one host round trip a move.  One loop iteration is one
+// MetropolisMonteCarlo::performMove (src/montecarlo.cpp:139-187) of AtomicTranslateRotate
+// (src/move.cpp:225-293):
+//
+//   thread 0     the proposal (device Philox stream or the caller's proposals), the trial
+//                position (IEEE FP64 add, boundary) and its fixed-point record
+//   all threads  the pair energy of the moved atom in both states against every other particle
+//                (Nonbonded group2all + groupInternal, src/energy.h:886-914,1183-1195: the
+//                pair cutoff makes every pair beyond it exactly 0, so no cell list is needed),
+//                FP64 pair_u64 on FP64 minimum-image distances; the reciprocal-space change
+//                d_k = q (e^{i k.r_new} - e^{i k.r_old}) from FP64 phases and
+//                A_k (|Q_k + d_k|^2 - |Q_k|^2) (src/energy.cpp:219-247,524-531)
+//   thread 0     the surface-term change (src/energy.cpp:466-482), getEnergyChange and
+//                metropolisCriterion (src/montecarlo.cpp:17-34,193-209) on the FP64 sum, and
+//                on accept the commit (positions, record, cell list)
+//   all threads  Q_k += d_k on accept (Ewald::sync, src/energy.cpp:640-658)
+//
+// Every sum is FP64 in a fixed order (per thread, then a shuffle tree, then the warps in index
+// order), so a chain's result depends only on its system, proposals and seed.
+#include "fau_chain.cuh"
+
+namespace fau {
+namespace {
+
+constexpr int kF64Threads = 128;
+constexpr int kF64Warps = kF64Threads / 32;
+
+// the move in flight, written by thread 0
+struct F64Move {
+    int kind, i, ti, stop;
+    uint4 rn;
+    double xo[3], xn[3], dM[3];
+    double u;
+};
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <bool PHILOX>
+__global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
+{
+    const long long t_start = clock64();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    DevSys& G = *A.sys[blockIdx.x];
+    __shared__ __align__(16) DevSys Ssh;
+    for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += kF64Threads)
+        reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
+    __shared__ F64Move mv;
+    __shared__ double red_p[kF64Warps], red_r[kF64Warps];
+    __shared__ int red_f[kF64Warps];
+    __shared__ int sh_acc, sh_stop, sh_up;
+    __shared__ unsigned long long sh_t0;
+    extern __shared__ __align__(16) unsigned char f64_smem[];
+    double2* dq = reinterpret_cast<double2*>(f64_smem); // this move's change of Q(k)
+    __syncthreads();
+    const DevSys& S = Ssh;
+    const int K = (S.flags & SYS_EWALD) ? S.K : 0;
+
+    // changes of Q(k) an FP32 chain left pending go into the FP64 master first (as fold_q_kernel
+    // folds them), so that the phases below read Q as the chain holds it
+    if (K) {
+        for (int k = tid; k < K; k += kF64Threads) {
+            float2 pe = S.qpend[k];
+            if (S.q_valid) {
+                const float2 d = S.qdlt[k];
+                pe.x += d.x;
+                pe.y += d.y;
+            }
+            if (pe.x != 0.f || pe.y != 0.f) {
+                double2 q = S.Q[k];
+                q.x += (double)pe.x;
+                q.y += (double)pe.y;
+                S.Q[k] = q;
+            }
+            S.qpend[k] = make_float2(0.f, 0.f);
+        }
+    }
+
+    const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
+    const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
+    const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
+    const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+    const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
+    const double twopi = 6.283185307179586476925286766559;
+
+    // thread 0's running state
+    double energy = sys_energy(S), sum_du = 0.0;
+    double M[3] = {S.M[0], S.M[1], S.M[2]};
+    unsigned long long n_acc = 0, n_mv = 0;
+    if (tid == 0) {
+        sh_t0 = global_ns();
+        sh_up = 0;
+    }
+    int stop = 0;
+    long long t = 0;
+    for (; t < nmoves; t++) {
+        // ---- the proposal and its trial state (thread 0)
+        if (tid == 0) {
+            const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)t, sys_id, A.seed, dp_f, 0.0, false)
+                                      : load_proposal(A.props[poff + t]);
+            // the caller's proposals are checked where they are read: an out-of-range index or
+            // any kind but a single-atom or empty move ends the chain with FAU_ERR_ARG
+            const bool ok = p.kind == FAU_MOVE_NONE || (p.kind == FAU_MOVE_ATOMIC && p.index >= 0 && p.index < S.n);
+            mv.stop = ok ? 0 : FAU_ERR_ARG;
+            mv.kind = ok ? p.kind : FAU_MOVE_NONE;
+            mv.u = p.u;
+            mv.i = -1;
+            if (mv.kind == FAU_MOVE_ATOMIC) {
+                const int i = p.index;
+                const uint4 ro = S.rec[i];
+                const double xo[3] = {S.x[i], S.y[i], S.z[i]};
+                mv.i = i;
+                mv.ti = (int)(ro.w >> 24);
+                double xn[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    xn[d] = boundary1(__dadd_rn(xo[d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
+                    mv.xo[d] = xo[d];
+                    mv.xn[d] = xn[d];
+                }
+                mv.rn = make_uint4(to_fixed(xn[0], S.fx_scale[0]), to_fixed(xn[1], S.fx_scale[1]),
+                                   to_fixed(xn[2], S.fx_scale[2]), ro.w);
+                if (S.flags & SYS_SURFACE) {
+                    const double q = S.itype_qd[mv.ti];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) mv.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
+                }
+            }
+        }
+        __syncthreads(); // B0: the move visible
+        if (mv.stop) {
+            stop = mv.stop;
+            break;
+        }
+        const int kind = mv.kind;
+        if (kind == FAU_MOVE_ATOMIC) {
+            const int i = mv.i, ti = mv.ti;
+            const double xn[3] = {mv.xn[0], mv.xn[1], mv.xn[2]};
+            const double xo[3] = {mv.xo[0], mv.xo[1], mv.xo[2]};
+            double ep = 0.0, er = 0.0;
+            int f = 0;
+            for (int j = tid; j < S.n; j += kF64Threads) {
+                if (j == i) continue;
+                const int tj = (int)(S.rec[j].w >> 24);
+                const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+                const double un = pair_u64(S, ti, tj, sqdist_d(S, xn, xj));
+                const double uo = pair_u64(S, ti, tj, sqdist_d(S, xo, xj));
+                if (isnan(un)) f |= F_NEW_NAN;
+                else if (isinf(un)) f |= F_NEW_INF;
+                else ep += un;
+                if (isnan(uo)) f |= F_OLD_NAN;
+                else if (isinf(uo)) f |= F_OLD_INF;
+                else ep -= uo;
+            }
+            if (K) {
+                const double q = S.itype_qd[ti];
+                for (int k = tid; k < K; k += kF64Threads) {
+                    int nx, ny, nz;
+                    kn_unpack(S.kn[k], nx, ny, nz);
+                    const double kx = twopi * ((double)nx / S.L[0]), ky = twopi * ((double)ny / S.L[1]),
+                                 kz = twopi * ((double)nz / S.L[2]);
+                    const double pn = (kx * xn[0] + ky * xn[1]) + kz * xn[2];
+                    const double po = (kx * xo[0] + ky * xo[1]) + kz * xo[2];
+                    double sn, cn, so, co;
+                    sincos(pn, &sn, &cn);
+                    sincos(po, &so, &co);
+                    const double dx = q * cn - q * co, dy = q * sn - q * so;
+                    dq[k] = make_double2(dx, dy);
+                    const double2 Q = S.Q[k];
+                    const double nq2 = (Q.x + dx) * (Q.x + dx) + (Q.y + dy) * (Q.y + dy);
+                    const double oq2 = Q.x * Q.x + Q.y * Q.y;
+                    er += S.Akd[k] * (nq2 - oq2);
+                }
+            }
+            ep = warp_sum_d(ep);
+            er = warp_sum_d(er);
+            f = (int)__reduce_or_sync(0xffffffffu, (unsigned)f);
+            if (lane == 0) {
+                red_p[warp] = ep;
+                red_r[warp] = er;
+                red_f[warp] = f;
+            }
+        }
+        __syncthreads(); // B1: the warp partials visible
+
+        // ---- decision and commit (thread 0)
+        if (tid == 0) {
+            int accept = 0, st = 0;
+            double du = 0.0;
+            if (kind == FAU_MOVE_ATOMIC) {
+                double ep = 0.0, er = 0.0;
+                int f = 0;
+#pragma unroll
+                for (int w = 0; w < kF64Warps; w++) {
+                    ep += red_p[w];
+                    er += red_r[w];
+                    f |= red_f[w];
+                }
+                const double du_rec = K ? S.rec_pref * er : 0.0;
+                double du_surf = 0.0;
+                if (S.flags & SYS_SURFACE) {
+                    double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        const double mn = __dadd_rn(M[d], mv.dM[d]);
+                        m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
+                        m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
+                    }
+                    du_surf = S.surf_pref * (m2n - m2o);
+                }
+                du = energy_change(ep + (du_rec + du_surf), f & F_NEW_INF, f & F_OLD_INF, f & F_NEW_NAN, f & F_OLD_NAN);
+                const double x = du * S.beta_scale;
+                if (isnan(x)) st = FAU_ERR_NAN; // metropolisCriterion throws: the launch ends before this move
+                else accept = metropolis(x, mv.u) ? 1 : 0;
+                if (!st) n_mv++;
+            }
+            if (!st) {
+                if (A.acc_out) A.acc_out[poff + t] = (uint8_t)accept;
+                if (A.du_out) A.du_out[poff + t] = du;
+            }
+            if (accept) { // State::sync trial -> accepted: positions, record, cell list
+                n_acc++;
+                sum_du += du;
+                energy += du;
+                const int i = mv.i;
+                if (S.flags & SYS_SURFACE) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], mv.dM[d]);
+                }
+                S.x[i] = mv.xn[0];
+                S.y[i] = mv.xn[1];
+                S.z[i] = mv.xn[2];
+                const uint4 rn = mv.rn;
+                S.rec[i] = rn;
+                if (S.flags & SYS_CELLS) {
+                    const int co = S.cell_of[i];
+                    int cc[3];
+                    cell_coords(S, mv.xn, rn, cc);
+                    const int cn = cell_index(S, cc);
+                    const int so = S.slot_of[i];
+                    if (co == cn) {
+                        S.cell_rec[(size_t)co * S.cap + so] = rn;
+                    }
+                    else {
+                        const int last = S.cell_cnt[co] - 1;
+                        if (so != last) {
+                            const uint4 mvd = S.cell_rec[(size_t)co * S.cap + last];
+                            S.cell_rec[(size_t)co * S.cap + so] = mvd;
+                            S.slot_of[mvd.w & 0xFFFFFFu] = so;
+                        }
+                        S.cell_rec[(size_t)co * S.cap + last] = make_uint4(0u, 0u, 0u, kEmptySlot);
+                        S.cell_cnt[co] = last;
+                        const int sn = S.cell_cnt[cn];
+                        if (sn >= S.cap) {
+                            // a full destination keeps the particle listed in its old cell: the move
+                            // is committed and the launch ends after it; the host regrows the list
+                            S.cell_rec[(size_t)co * S.cap + last] = rn;
+                            S.slot_of[i] = last;
+                            S.cell_cnt[co] = last + 1;
+                            st = FAU_ERR_CAPACITY;
+                        }
+                        else {
+                            S.cell_rec[(size_t)cn * S.cap + sn] = rn;
+                            S.cell_cnt[cn] = sn + 1;
+                            S.cell_of[i] = cn;
+                            S.slot_of[i] = sn;
+                        }
+                    }
+                }
+            }
+            sh_acc = accept;
+            sh_stop = st;
+            if (A.time_budget_ns && global_ns() - sh_t0 >= A.time_budget_ns) sh_up = 1;
+        }
+        __syncthreads(); // B2: the decision visible
+        if (sh_acc && K) // each thread its own k-vectors, as it wrote d_k above
+            for (int k = tid; k < K; k += kF64Threads) {
+                double2 q = S.Q[k];
+                const double2 d = dq[k];
+                q.x += d.x;
+                q.y += d.y;
+                S.Q[k] = q;
+            }
+        if (sh_stop) {
+            stop = sh_stop;
+            if (stop == FAU_ERR_CAPACITY) t++; // committed
+            break;
+        }
+        if (sh_up) { // the time budget is spent: the launch ends after move t
+            t++;
+            break;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        G.pair_evals += 2ull * (unsigned long long)(S.n > 0 ? S.n - 1 : 0) * n_mv;
+        G.k_updates += n_mv * (unsigned long long)K;
+        G.moves += n_mv;
+        G.accepted += n_acc;
+        G.sum_du += sum_du;
+        G.energy = energy;
+        G.e_acc_hi = G.e_acc_lo = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) G.M[d] = M[d];
+        G.q_valid = 0;
+        G.q_since = 0;
+        if (stop) G.err = stop;
+        G.consumed = t;
+        G.cycles += (unsigned long long)(clock64() - t_start);
+    }
+}
+
+template <bool PH>
+cudaError_t launch_fp64_inst(const ChainArgs& a, int nblocks, int K, cudaStream_t st, bool prepare_only)
+{
+    // the dynamic allowance is raised on demand, never inside a stream capture: callers prepare first
+    static size_t granted = 0;
+    const size_t smem = fp64_smem_bytes(K);
+    if (smem > granted || granted == 0) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(fp64_chain_kernel<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        granted = smem;
+    }
+    if (prepare_only) return cudaSuccess;
+    fp64_chain_kernel<PH><<<nblocks, kF64Threads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+size_t fp64_smem_bytes(int K) { return (size_t)(K > 0 ? K : 0) * sizeof(double2); }
+
+cudaError_t prepare_fp64(int K, bool philox)
+{
+    return philox ? launch_fp64_inst<true>(ChainArgs{}, 0, K, nullptr, true)
+                  : launch_fp64_inst<false>(ChainArgs{}, 0, K, nullptr, true);
+}
+
+cudaError_t launch_fp64(const ChainArgs& a, int nblocks, int K, bool philox, cudaStream_t st)
+{
+    return philox ? launch_fp64_inst<true>(a, nblocks, K, st, false) : launch_fp64_inst<false>(a, nblocks, K, st, false);
+}
+
+} // namespace fau

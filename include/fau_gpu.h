@@ -81,7 +81,9 @@ enum fau_group_flag {
 /* arithmetic of the dU evaluation */
 enum fau_precision {
     FAU_PREC_FP32C = 0, /* FP32 pair/Ewald terms, compensated sums, FP64 totals */
-    FAU_PREC_FP64 = 1   /* plain FP64 evaluation (in-GPU comparison form)        */
+    FAU_PREC_FP64 = 1   /* plain FP64 evaluation: one move per call in the
+                           single-system calls (the in-GPU comparison form),
+                           persistent FP64 chains in the batch calls          */
 };
 
 /* Ewald reciprocal space, EwaldData (src/energy.cpp:28-59), PBC policy. */
@@ -374,13 +376,18 @@ int fau_run_proposals(fau_sys* sys, const fau_proposal* proposals, int n,
  * E the running energies in absolute units (kT_i T_i of each walker's own
  * Hamiltonian).  r = counter_base / swap_interval_moves + block.  Walkers run
  * in descending order of their block's cost (moves x particles), so that the
- * largest begin first, each on an SM of its own while SMs remain. */
+ * largest begin first, each on an SM of its own while SMs remain.
+ * Systems made with FAU_PREC_FP64 run as FP64 replica chains (the plain FP64
+ * form's pair sums, Ewald phases and Metropolis decision, all on the device;
+ * single-atom moves; no finite maxenergy): a batch holds FP64 systems only or
+ * none, else FAU_ERR_ARG. */
 int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* params,
                   fau_batch_stats* stats);
 
 /* Host-fed proposals for n systems in one launch (one CTA per system):
  * proposals[offsets[i] .. offsets[i+1]) belong to systems[i].  accepted_out
- * and du_out (optional) are indexed like proposals. */
+ * and du_out (optional) are indexed like proposals.  FP64 systems run as FP64
+ * replica chains, as in fau_run_batch (single-atom or empty proposals only). */
 int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_proposal* proposals,
                             const int64_t* offsets, uint8_t* accepted_out, double* du_out,
                             fau_batch_stats* stats);
