@@ -258,9 +258,15 @@ def run_ours(args) -> None:
 
     ctx = F.Context(local)
     water = args.workload == "water"
-    if water and not args.value_only:
-        raise SystemExit("--workload water is a profiling case: use it with --value-only")
-    base = configs.spce_water(n_mol=1000) if water else configs.bulk_ewald(n_salt=10000, seed=1)
+    fp64 = args.workload in ("pm_fp64", "bulk_fp64")
+    if args.workload != "bulk" and not args.value_only:
+        raise SystemExit(f"--workload {args.workload} is a profiling case: use it with --value-only")
+    if water:
+        base = configs.spce_water(n_mol=1000)
+    elif args.workload == "pm_fp64":
+        base = configs.primitive_model(n=200, precision=A.FAU_PREC_FP64)
+    else:
+        base = configs.bulk_ewald(n_salt=10000, seed=1, precision=A.FAU_PREC_FP64 if fp64 else A.FAU_PREC_FP32C)
     dp, dprot = (0.5, 0.5) if water else (2.0, 0.0)
     sms = _sm_count(local)
     R = args.replicas or 4 * sms  # four chains per SM: the pipelined kernel's occupancy limit
@@ -273,8 +279,8 @@ def run_ours(args) -> None:
     # ---- kernel configuration: the autotuner's choice unless --threads is given
     tuned = None
     threads = args.threads
-    if water:
-        threads = max(threads, 0)  # molecular moves: the pipelined molecular kernel
+    if water or fp64:
+        threads = max(threads, 0)  # molecular moves: the pipelined molecular kernel; FP64: FP64 chains
     if threads < 0:
         from faunus_gb300 import autotune
         # measured at the replica count this run uses: the CTA size that fits the most chains
@@ -481,6 +487,11 @@ def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: in
     out["primitive_model_200_fp64"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
                                        "kernel": "FP64 replica chains (plain FP64 pair sums and decision, "
                                                  "all pairs, one CTA per system)"}
+    # the benchmark system itself as FP64 replica chains: what the FP32C form gains over FP64
+    mps, pps = batch_rate(configs.bulk_ewald(n_salt=10000, seed=1, precision=A.FAU_PREC_FP64), replicas, 1000)
+    out["bulk_ewald_20000_fp64"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
+                                    "kernel": "FP64 replica chains (FP64 pairs over each state's cell stencil, "
+                                              "FP64 sin/cos of k.r for the K = 1152 k-vectors)"}
     mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 5000)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
                               "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
@@ -609,8 +620,10 @@ def main():
     ap.add_argument("--pt-budget-s", type=float, default=60.0,
                     help="parallel tempering: device seconds allowed; fewer sweeps run if the calibration predicts more")
     ap.add_argument("--value-only", action="store_true", help="device-timed value only (profiling case)")
-    ap.add_argument("--workload", default="bulk", choices=["bulk", "water"],
-                    help="water: 1,000 rigid SPC/E molecules, molecular moves (profiling case, with --value-only)")
+    ap.add_argument("--workload", default="bulk", choices=["bulk", "water", "pm_fp64", "bulk_fp64"],
+                    help="profiling cases, with --value-only: water (1,000 rigid SPC/E molecules, molecular "
+                         "moves), pm_fp64 / bulk_fp64 (the 200-ion primitive model / the bulk system as FP64 "
+                         "replica chains)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

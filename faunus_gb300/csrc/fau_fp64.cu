@@ -10,10 +10,11 @@
 //
 //   thread 0     the proposal (device Philox stream or the caller's proposals), the trial
 //                position (IEEE FP64 add, boundary) and its fixed-point record
-//   all threads  the pair energy of the moved atom in both states against every other particle
-//                (Nonbonded group2all + groupInternal, src/energy.h:886-914,1183-1195: the
-//                pair cutoff makes every pair beyond it exactly 0, so no cell list is needed),
-//                FP64 pair_u64 on FP64 minimum-image distances; the reciprocal-space change
+//   all threads  the pair energy of the moved atom in both states (Nonbonded group2all +
+//                groupInternal, src/energy.h:886-914,1183-1195) against every other particle,
+//                or with a cell list against the particles of each state's 3x3x3 stencil (pair_u64
+//                is exactly 0 beyond the pair cutoff, so both sums hold the same terms), FP64
+//                pair_u64 on FP64 minimum-image distances; the reciprocal-space change
 //                d_k = q (e^{i k.r_new} - e^{i k.r_old}) from FP64 phases and
 //                A_k (|Q_k + d_k|^2 - |Q_k|^2) (src/energy.cpp:219-247,524-531)
 //   thread 0     the surface-term change (src/energy.cpp:466-482), getEnergyChange and
@@ -34,10 +35,14 @@ constexpr int kF64Warps = kF64Threads / 32;
 // the move in flight, written by thread 0
 struct F64Move {
     int kind, i, ti, stop;
+    int cell_old, cell_new;
+    int cc_o[3], cc_n[3]; // cell coordinates of the old and the new position
     uint4 rn;
     double xo[3], xn[3], dM[3];
     double u;
 };
+
+__device__ __forceinline__ int wrap_cell1(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 __device__ __forceinline__ double warp_sum_d(double v)
 {
@@ -135,6 +140,15 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
 #pragma unroll
                     for (int d = 0; d < 3; d++) mv.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
                 }
+                if (S.flags & SYS_CELLS) { // the old cell is the one the particle is listed in
+                    const int co = S.cell_of[i];
+                    mv.cell_old = co;
+                    mv.cc_o[0] = co % S.cdim[0];
+                    mv.cc_o[1] = (co / S.cdim[0]) % S.cdim[1];
+                    mv.cc_o[2] = co / (S.cdim[0] * S.cdim[1]);
+                    cell_coords(S, xn, mv.rn, mv.cc_n);
+                    mv.cell_new = cell_index(S, mv.cc_n);
+                }
             }
         }
         __syncthreads(); // B0: the move visible
@@ -149,18 +163,53 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
             const double xo[3] = {mv.xo[0], mv.xo[1], mv.xo[2]};
             double ep = 0.0, er = 0.0;
             int f = 0;
-            for (int j = tid; j < S.n; j += kF64Threads) {
-                if (j == i) continue;
-                const int tj = (int)(S.rec[j].w >> 24);
-                const double xj[3] = {S.x[j], S.y[j], S.z[j]};
-                const double un = pair_u64(S, ti, tj, sqdist_d(S, xn, xj));
-                const double uo = pair_u64(S, ti, tj, sqdist_d(S, xo, xj));
-                if (isnan(un)) f |= F_NEW_NAN;
-                else if (isinf(un)) f |= F_NEW_INF;
-                else ep += un;
-                if (isnan(uo)) f |= F_OLD_NAN;
-                else if (isinf(uo)) f |= F_OLD_INF;
-                else ep -= uo;
+            if (S.flags & SYS_CELLS) {
+                // each state over the stencil of its own cell (GridOffsets3D, src/celllistimpl.cpp:
+                // 15-31): every particle within the pair cutoff of a position lies in the stencil
+                // of that position's cell, and pair_u64 is exactly 0 beyond the cutoff
+                const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1,
+                          nbz = S.off_max[2] - S.off_min[2] + 1;
+                const int cap = S.cap, cap_shift = __ffs(cap) - 1;
+                const int per_state = (nbx * nby * nbz) << cap_shift;
+                for (int s = tid; s < 2 * per_state; s += kF64Threads) {
+                    const int st = s >= per_state ? 1 : 0; // 0: the trial state, 1: the accepted state
+                    const int r = s - st * per_state, e = r >> cap_shift;
+                    const int o[3] = {e % nbx + S.off_min[0], (e / nbx) % nby + S.off_min[1], e / (nbx * nby) + S.off_min[2]};
+                    int c[3];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) c[d] = wrap_cell1((st ? mv.cc_o[d] : mv.cc_n[d]) + o[d], S.cdim[d]);
+                    const uint4 rj = S.cell_rec[(size_t)cell_index(S, c) * cap + (r & (cap - 1))];
+                    if (rj.w == kEmptySlot) continue;
+                    const int j = (int)(rj.w & 0xFFFFFFu);
+                    if (j == i) continue;
+                    const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+                    const double u = pair_u64(S, ti, (int)(rj.w >> 24), sqdist_d(S, st ? xo : xn, xj));
+                    if (st == 0) {
+                        if (isnan(u)) f |= F_NEW_NAN;
+                        else if (isinf(u)) f |= F_NEW_INF;
+                        else ep += u;
+                    }
+                    else {
+                        if (isnan(u)) f |= F_OLD_NAN;
+                        else if (isinf(u)) f |= F_OLD_INF;
+                        else ep -= u;
+                    }
+                }
+            }
+            else {
+                for (int j = tid; j < S.n; j += kF64Threads) {
+                    if (j == i) continue;
+                    const int tj = (int)(S.rec[j].w >> 24);
+                    const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+                    const double un = pair_u64(S, ti, tj, sqdist_d(S, xn, xj));
+                    const double uo = pair_u64(S, ti, tj, sqdist_d(S, xo, xj));
+                    if (isnan(un)) f |= F_NEW_NAN;
+                    else if (isinf(un)) f |= F_NEW_INF;
+                    else ep += un;
+                    if (isnan(uo)) f |= F_OLD_NAN;
+                    else if (isinf(uo)) f |= F_OLD_INF;
+                    else ep -= uo;
+                }
             }
             if (K) {
                 const double q = S.itype_qd[ti];
@@ -243,10 +292,7 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
                 const uint4 rn = mv.rn;
                 S.rec[i] = rn;
                 if (S.flags & SYS_CELLS) {
-                    const int co = S.cell_of[i];
-                    int cc[3];
-                    cell_coords(S, mv.xn, rn, cc);
-                    const int cn = cell_index(S, cc);
+                    const int co = mv.cell_old, cn = mv.cell_new;
                     const int so = S.slot_of[i];
                     if (co == cn) {
                         S.cell_rec[(size_t)co * S.cap + so] = rn;
