@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["fau_kernels.cu", "fau_capi.cu", "fau_batch.cu", "fau_movegen.cpp", "fau_noalloc.cu",
            "fau_chain_128_host.cu", "fau_chain_128_ph.cu", "fau_chain_256_host.cu", "fau_chain_256_ph.cu",
            "fau_fast_2_ph.cu", "fau_fast_2_host.cu", "fau_fast_4_ph.cu", "fau_fast_4_host.cu", "fau_fast_8_ph.cu",
-           "fau_fast_4s_ph.cu", "fau_fast_4s_host.cu", "fau_fast_8s_ph.cu", "fau_sampler.cu", "fau_mol_256.cu", "fau_mol_256_host.cu",
+           "fau_fast_4s_ph.cu", "fau_fast_4s_host.cu", "fau_fast_8s_ph.cu", "fau_sampler.cu", "fau_mol_256.cu", "fau_mol_256_host.cu", "fau_mol_512.cu",
            "fau_spline.cpp", "fau_audit.cu", "fau_fp64.cu"]
 
 

@@ -288,11 +288,14 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (f64 < 0) return f64 == -1 ? fau_internal_fail(FAU_ERR_ARG, kFp64Mixed) : fau_internal_fail(FAU_ERR_ARG, kFp64Form);
     // kernel choice: threads 0, 96, 160 or 288 -> the pipelined kernel (1 producer + 4, 2, 4 or 8
     // compute warps) for every system whose device proposals are single-atom moves (the others run
-    // in the 256-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems
+    // in the 256-thread chain kernel); 128 or 256 -> the chain kernel of that size for all systems;
+    // 512 -> as 0, with molecular-move systems in 512-thread CTAs of the pipelined molecular kernel
+    // (1 preparing + 15 compute warps, one CTA an SM: each chain's moves take less time)
     const int req = P->threads;
-    if (req != 0 && req != 96 && req != 128 && req != 160 && req != 256 && req != 288)
-        return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 96, 128, 160, 256 or 288");
-    const bool use_fast = req == 0 || req == 96 || req == 160 || req == 288;
+    if (req != 0 && req != 96 && req != 128 && req != 160 && req != 256 && req != 288 && req != 512)
+        return fau_internal_fail(FAU_ERR_ARG, "threads must be 0, 96, 128, 160, 256, 288 or 512");
+    bool mol512 = req == 512;
+    const bool use_fast = req == 0 || req == 96 || req == 160 || req == 288 || mol512;
     const int threads = use_fast ? 256 : req; // molecular moves: 256-thread chain CTAs measured fastest
     int fwarps = req == 96 ? 2 : (req == 288 ? 8 : 4);
     std::vector<uint8_t> fast(n, 0);
@@ -361,7 +364,17 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (const char* mk = std::getenv("FAU_MOL_KERNEL"); mk && mk[0] == '0') use_mol = false;
     for (int r = nfast; r < n && use_mol; r++)
         if (!mol[order[r]] || fau_internal_sys_maxe(systems[order[r]])) use_mol = false;
-    if (use_mol && mol_smem_bytes_total(Ke, nce) + 24576 > 227 * 1024) use_mol = false;
+    if (use_mol && mol_smem_bytes_total(Ke, nce) + (mol512 ? 36864 : 24576) > 227 * 1024) use_mol = false;
+    // threads 0, molecular chains alone in the launch: 512-thread CTAs when every chain fits on the
+    // GPU at once with one CTA an SM and no time budget applies (a chain's moves take 20-30 % less
+    // time; with more chains than SMs four 256-thread CTAs an SM hold more work).  The width sets
+    // the FP32 summation order, so a chain depends on it, as for the pipelined single-atom kernel.
+    if (req == 0 && use_mol && nfast == 0 && P->time_budget_ns == 0 &&
+        mol_smem_bytes_total(Ke, nce) + 36864 <= 227 * 1024) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 0;
+        if (nexact <= sms) mol512 = true;
+    }
     // threads 0: the pipelined kernel's width for this launch.  When every chain fits on the GPU at
     // once in CTAs of 8 compute warps (two to an SM, shared memory allowing) each chain gets those:
     // its moves take less time, and a block (parallel tempering) lasts as long as its longest
@@ -519,7 +532,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact)
         BTRY(f64       ? prepare_fp64(Ke, true)
-             : use_mol ? mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true)
+             : use_mol ? (mol512 ? mol_dispatch_512(ChainArgs{}, 0, Ke, nce, nullptr, true)
+                                 : mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true))
                        : prepare_chain(Ke, nce, threads, true));
     if (nfast) BTRY(prepare_fast(Kf, ncf, ntf, fwarps, true, occf));
     if (nfast && nexact) {
@@ -539,7 +553,8 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         if (nfast && nexact) {
             if ((e = cudaEventRecord(fork_ev, st)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(st2, fork_ev, 0)) != cudaSuccess) return e;
-            if ((e = use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st2, false)
+            if ((e = use_mol ? (mol512 ? mol_dispatch_512(ae, nexact, Ke, nce, st2, false)
+                                       : mol_dispatch_256(ae, nexact, Ke, nce, st2, false))
                              : launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess)
                 return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
@@ -552,6 +567,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
         if (f64) return launch_fp64(ae, nexact, Ke, true, st);
+        if (use_mol && mol512) return mol_dispatch_512(ae, nexact, Ke, nce, st, false);
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
                        : launch_chain(ae, nexact, Ke, nce, threads, true, st);
     };

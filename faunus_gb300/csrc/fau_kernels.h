@@ -70,6 +70,7 @@ cudaError_t chain_dispatch_256_ph(const ChainArgs&, int, int, int, cudaStream_t,
 // pipelined molecular-move kernel (device proposals; 256 threads: 1 preparing + 7 compute warps)
 cudaError_t mol_dispatch_256(const ChainArgs&, int, int, int, cudaStream_t, bool);
 cudaError_t mol_dispatch_256_host(const ChainArgs&, int, int, int, cudaStream_t, bool); // host proposals
+cudaError_t mol_dispatch_512(const ChainArgs&, int, int, int, cudaStream_t, bool);      // 1 + 15 warps, device proposals
 int mol_minb(int nblocks); // CTAs per SM the molecular kernel's registers are sized for
 size_t mol_smem_bytes_total(int K, int nc);
 // pipelined chain kernel (single-atom moves only): 1 producer warp + `warps` compute warps;

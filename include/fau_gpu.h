@@ -232,13 +232,18 @@ typedef struct fau_batch_params {
     int n_swap_blocks;        /* number of swap blocks when swap_interval_moves > 0       */
     const double* temperatures; /* n temperatures (K) of the PT ladder, or NULL             */
     int threads;              /* CTA size: 96, 160, 288 -> the pipelined kernel with 2, 4, 8
-                                 compute warps (molecular systems: the 256-thread chain
-                                 kernel); 128, 256 -> the chain kernel for every system;
+                                 compute warps (molecular systems: the pipelined molecular
+                                 kernel in 256-thread CTAs); 512 -> as 160, molecular
+                                 systems in 512-thread CTAs (1 preparing + 15 compute warps);
+                                 128, 256 -> the chain kernel for every system;
                                  0 -> chosen per launch: 8 compute warps when every pipelined
                                  chain fits on the GPU at once (two CTAs an SM) and no chain
-                                 kernel or time budget shares the launch, else 4.  The width
-                                 sets the FP32 summation order: a fixed width keeps a
-                                 system's chain independent of the rest of the batch     */
+                                 kernel or time budget shares the launch, else 4; molecular
+                                 systems alone in a launch without a time budget in
+                                 512-thread CTAs when every chain fits at once (one an SM),
+                                 else 256.  The width sets the FP32 summation order: a fixed
+                                 width keeps a system's chain independent of the rest of
+                                 the batch                                              */
     const uint32_t* streams;  /* optional per-system RNG stream ids (default: batch index)  */
     const uint64_t* counters; /* optional per-system first move counter (default:
                                  counter_base); a system's moves depend only on its

@@ -11,6 +11,8 @@ q (e^{i k.r_new} - e^{i k.r_old}) from sin/cos of k.r, whose rounding (a few ulp
 are held to 1e-10 max(|dU|, S) + 1e-11 kT, and the chain to the plain FP64 form, which evaluates
 the same arithmetic one move per call, within 1e-13 kT.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -144,3 +146,50 @@ def test_fp64_chain_rejects_molecular_proposals(ctx):
     with pytest.raises(F.FauError, match="single-atom"):
         ctx.run_proposals_batch([w], props, np.array([0, 10], np.int64))
     w.close()
+
+
+def _two_spheres(pos, sigma2=16.0, terms=A.FAU_PAIR_HS | A.FAU_PAIR_COULOMB):
+    return F.SystemSpec(box=np.full(3, 20.0), pos=np.array(pos, dtype=float), charge=np.array([1.0, -1.0]),
+                        type=np.zeros(2, np.int32), group_begin=np.array([0, 2], np.int32),
+                        group_flags=np.array([A.FAU_GROUP_ATOMIC], np.int32), n_types=1,
+                        hs_sigma2=np.full((1, 1), 16.0), sigma2=np.full((1, 1), sigma2),
+                        eps4=np.full((1, 1), 1.0), pair_terms=terms, coulomb_type=A.FAU_COUL_PLAIN,
+                        bjerrum_length=7.0, precision=A.FAU_PREC_FP64)
+
+
+def _moves(rows):
+    p = np.zeros(len(rows), dtype=A.PROPOSAL_DTYPE)
+    for m, (i, dr, u) in enumerate(rows):
+        p["kind"][m] = A.FAU_MOVE_ATOMIC
+        p["index"][m] = i
+        p["dr"][m] = dr
+        p["u"][m] = u
+    return p
+
+
+def test_fp64_chain_infinities_follow_get_energy_change(ctx):
+    """Hard-sphere overlaps in an FP64 chain: into overlap +inf (rejected, unless u = 0, as
+    u <= exp(-dU) has it), out of overlap -inf (accepted); the oracle decides the same."""
+    spec = _two_spheres([[0, 0, 0], [5, 0, 0]])
+    props = _moves([(1, (-2.0, 0, 0), 0.5), (1, (-2.0, 0, 0), 0.0), (1, (2.0, 0, 0), 0.999)])
+    g = ctx.create(spec)
+    acc = np.zeros(3, np.uint8)
+    du = np.zeros(3)
+    ctx.run_proposals_batch([g], props, np.array([0, 3], np.int64), acc, du)
+    det = O.OracleSystem(spec).run_detail(props)
+    assert list(acc) == [0, 1, 1] == list(det["accepted"].astype(np.uint8))
+    assert du[0] == math.inf and du[1] == math.inf and du[2] == -math.inf
+    assert np.array_equal(np.sign(du), np.sign(det["du"]))
+
+
+def test_fp64_chain_nan_pair_energy_is_rejected(ctx):
+    """A missing coefficient makes both states NaN: getEnergyChange maps a NaN trial energy to
+    +inf (src/montecarlo.cpp:198-200), rejected, and the chain goes on."""
+    spec = _two_spheres([[0, 0, 0], [5, 0, 0]], sigma2=float("nan"), terms=A.FAU_PAIR_WCA)
+    props = _moves([(1, (0.5, 0, 0), 0.5), (0, (0.0, 0.5, 0), 0.5)])
+    g = ctx.create(spec)
+    acc = np.ones(2, np.uint8)
+    du = np.zeros(2)
+    st = ctx.run_proposals_batch([g], props, np.array([0, 2], np.int64), acc, du)
+    assert st["moves"] == 2
+    assert list(acc) == [0, 0] and du[0] == math.inf and du[1] == math.inf

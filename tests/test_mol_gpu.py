@@ -1,6 +1,7 @@
 """GPU parity of the pipelined molecular-move kernel (fau_run_batch with the default
-kernel choice runs every molecular-move system in it; threads=256 forces the chain
-kernel; systems wide enough for more than 3 x 3 x 3 mass-centre cells of the largest
+kernel choice runs every molecular-move system in it, in 512-thread CTAs when every molecular
+chain of the launch fits on the GPU at once, else in 256-thread CTAs (threads=160 fixes those);
+threads=256 forces the chain kernel; systems wide enough for more than 3 x 3 x 3 mass-centre cells of the largest
 group cutoff take their GroupCutoff candidates from those cells, the chain kernel from every
 group).  Under the same device proposals both kernels must give the same chain --
 the same accept count and bit-identical FP64 positions and mass centres -- barring a
@@ -41,12 +42,15 @@ def _consistent(s):
     assert abs(e_run - e_tot) <= 1e-6 * max(1.0, abs(e_tot)), (e_run, e_tot)
 
 
+@pytest.mark.parametrize("threads", [0, 160])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_molecular_kernel_equals_chain_kernel(ctx, case):
+def test_molecular_kernel_equals_chain_kernel(ctx, case, threads):
+    """threads 0: a launch of one molecular chain runs it in a 512-thread CTA (1 preparing + 15
+    compute warps); 160: the 256-thread CTA (1 + 7)."""
     spec = CASES[case]()
     a, b = ctx.create(spec), ctx.create(spec)
     moves = 3000
-    sa = ctx.run_batch([a], moves, seed=17, streams=[3], dp=0.5, dprot=0.5, threads=0)
+    sa = ctx.run_batch([a], moves, seed=17, streams=[3], dp=0.5, dprot=0.5, threads=threads)
     sb = ctx.run_batch([b], moves, seed=17, streams=[3], dp=0.5, dprot=0.5, threads=256)
     assert sa["moves"] == sb["moves"] == moves
     assert sa["accepted"] == sb["accepted"] and sa["accepted"] > 300

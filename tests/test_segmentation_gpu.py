@@ -15,11 +15,15 @@ pytestmark = pytest.mark.gpu
 CASES = {
     "pipelined_bulk": (lambda: configs.bulk_ewald(n_salt=1000, seed=4), dict(dp=2.0, threads=160)),
     "chain_bulk": (lambda: configs.bulk_ewald(n_salt=1000, seed=5), dict(dp=2.0, threads=256)),
-    "molecular_water": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=6), dict(dp=0.5, dprot=0.5, threads=0)),
+    # fixed widths: with threads 0 a launch of one molecular chain takes 512-thread CTAs and a
+    # time-budgeted one 256, and the width sets the FP32 summation order
+    "molecular_water": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=6), dict(dp=0.5, dprot=0.5, threads=160)),
+    "molecular_water_512": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=6),
+                            dict(dp=0.5, dprot=0.5, threads=512)),
     "chain_water": (lambda: configs.spce_water(n_mol=256, L=18.6, seed=7), dict(dp=0.5, dprot=0.5, threads=256)),
     # 4 x 4 x 4 mass-centre cells: the lists rebuilt at each launch equal the ones kept current
     "molecular_water_cells": (lambda: configs.spce_water(n_mol=4000, L=49.3, seed=8),
-                              dict(dp=0.5, dprot=0.5, threads=0)),
+                              dict(dp=0.5, dprot=0.5, threads=160)),
 }
 
 
