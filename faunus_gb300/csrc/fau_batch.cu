@@ -154,19 +154,34 @@ extern "C" double fau_internal_sys_volume(const fau_sys* s);
 
 namespace {
 const char* const kFp64Mixed = "a batch holds FP64 systems (FAU_PREC_FP64) only or none";
-const char* const kFp64Form = "FP64 chains run single-atom (or empty) moves on systems without a finite maxenergy";
+const char* const kFp64Form = "FP64 chains run systems without a finite maxenergy";
 
 // 1: every system of the batch is an FP64 system, 0: none is; -1: both kinds; -2: an FP64 system
-// the FP64 chain kernel does not run (a finite maxenergy, or molecular moves where `mol` flags them)
-int fp64_batch(fau_sys* const* systems, int n, const uint8_t* mol)
+// the FP64 chain kernel does not run (a finite maxenergy)
+int fp64_batch(fau_sys* const* systems, int n)
 {
     int k = 0;
     for (int i = 0; i < n; i++) k += fau_internal_sys_fp64(systems[i]);
     if (k == 0) return 0;
     if (k != n) return -1;
     for (int i = 0; i < n; i++)
-        if (fau_internal_sys_maxe(systems[i]) || (mol && mol[i])) return -2;
+        if (fau_internal_sys_maxe(systems[i])) return -2;
     return 1;
+}
+
+// the largest group count of the batch (the FP64 kernel's per-group GroupCutoff flags)
+int max_groups(fau_sys* const* systems, int n)
+{
+    int g = 0;
+    for (int i = 0; i < n; i++) {
+        fau_ctx* c2;
+        DevSys* dd;
+        int K, np, ng, mo, knc;
+        double tr;
+        fau_internal_sys_view(systems[i], &c2, &dd, &K, &np, &ng, &mo, &tr, &knc);
+        g = std::max(g, ng);
+    }
+    return g;
 }
 } // namespace
 
@@ -283,8 +298,9 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
         if (pt) tref[i] = P->temperatures[i];
     }
     // systems made with FAU_PREC_FP64 run in the FP64 chain kernel: a batch holds FP64 systems only
-    // or none, and their chains are single-atom moves without a finite maxenergy
-    const int f64 = fp64_batch(systems, n, mol.data());
+    // or none, without a finite maxenergy
+    const int f64 = fp64_batch(systems, n);
+    const int g64 = f64 > 0 ? max_groups(systems, n) : 0;
     if (f64 < 0) return f64 == -1 ? fau_internal_fail(FAU_ERR_ARG, kFp64Mixed) : fau_internal_fail(FAU_ERR_ARG, kFp64Form);
     // kernel choice: threads 0, 96, 160 or 288 -> the pipelined kernel (1 producer + 4, 2, 4 or 8
     // compute warps) for every system whose device proposals are single-atom moves (the others run
@@ -354,10 +370,10 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             nce = std::max(nce, knc);
         }
     }
-    if (f64 ? fp64_smem_bytes(Ke) + 16384 > 227 * 1024
+    if (f64 ? fp64_smem_bytes(Ke, g64) + 16384 > 227 * 1024
             : ((nexact && (Ke > chain_max_k(threads) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
                (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024)))
-        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
+        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors (FP64 chains: k-vectors and groups) for the chain kernel");
     // molecular-move systems: the pipelined molecular kernel (preparation of the next move overlapped
     // with the current one) unless a chain-kernel size was requested; FAU_MOL_KERNEL=0 turns it off
     bool use_mol = !f64 && use_fast && nexact > 0;
@@ -531,7 +547,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
     if (a.n_moves) ae.n_moves = a.n_moves + nfast;
     // set the kernels' shared-memory attributes before the capture starts
     if (nexact)
-        BTRY(f64       ? prepare_fp64(Ke, true)
+        BTRY(f64       ? prepare_fp64(Ke, g64, true)
              : use_mol ? (mol512 ? mol_dispatch_512(ChainArgs{}, 0, Ke, nce, nullptr, true)
                                  : mol_dispatch_256(ChainArgs{}, 0, Ke, nce, nullptr, true))
                        : prepare_chain(Ke, nce, threads, true));
@@ -566,7 +582,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, occf, st)) != cudaSuccess) return e;
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
-        if (f64) return launch_fp64(ae, nexact, Ke, true, st);
+        if (f64) return launch_fp64(ae, nexact, Ke, g64, true, st);
         if (use_mol && mol512) return mol_dispatch_512(ae, nexact, Ke, nce, st, false);
         return use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
                        : launch_chain(ae, nexact, Ke, nce, threads, true, st);
@@ -740,16 +756,12 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         // in the 256-thread chain kernel; the kernels check every proposal as they read it
         fast[i] = fau_internal_sys_all_atomic(systems[i]) && knc <= kFastMaxNc && !fau_internal_sys_maxe(systems[i]);
     }
-    // FP64 systems: the FP64 chain kernel (a batch holds FP64 systems only or none; their proposals
-    // are single-atom or empty moves)
-    const int f64 = fp64_batch(systems, n, nullptr);
+    // FP64 systems: the FP64 chain kernel (a batch holds FP64 systems only or none)
+    const int f64 = fp64_batch(systems, n);
     if (f64 < 0) return f64 == -1 ? fau_internal_fail(FAU_ERR_ARG, kFp64Mixed) : fau_internal_fail(FAU_ERR_ARG, kFp64Form);
-    if (f64) {
-        for (long long m = 0; m < total; m++)
-            if (props[m].kind != FAU_MOVE_ATOMIC && props[m].kind != FAU_MOVE_NONE)
-                return fau_internal_fail(FAU_ERR_ARG, kFp64Form);
+    const int g64 = f64 > 0 ? max_groups(systems, n) : 0;
+    if (f64)
         for (int i = 0; i < n; i++) fast[i] = 0;
-    }
     // kernel order puts the pipelined-kernel systems first
     std::vector<int> order;
     order.reserve(n);
@@ -774,11 +786,12 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             nce = std::max(nce, ncv[i]);
         }
     }
-    if (f64 ? fp64_smem_bytes(Ke) + 16384 > 227 * 1024
+    if (f64 ? fp64_smem_bytes(Ke, g64) + 16384 > 227 * 1024
             : ((nexact && (Ke > chain_max_k(256) || chain_smem_bytes(Ke, nce) + 16384 > 227 * 1024)) ||
                (nfast && fast_smem_bytes_total(Kf, ncf, ntf) > 227 * 1024)))
-        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors for the chain kernel");
-    if (f64 && prepare_fp64(Ke, false) != cudaSuccess) return fau_internal_fail(FAU_ERR_CUDA, "FP64 chain kernel attributes");
+        return fau_internal_fail(FAU_ERR_ARG, "too many k-vectors (FP64 chains: k-vectors and groups) for the chain kernel");
+    if (f64 && prepare_fp64(Ke, g64, false) != cudaSuccess)
+        return fau_internal_fail(FAU_ERR_CUDA, "FP64 chain kernel attributes");
     // systems of molecular groups only whose proposals are all molecular (or empty) run in the
     // pipelined molecular kernel when every other-than-single-atom system qualifies; otherwise
     // the chain kernel runs them (it takes every proposal kind)
@@ -871,7 +884,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                  cudaEventRecord(join_ev, st2) == cudaSuccess;
         }
         else if (f64) {
-            ok = launch_fp64(ae, nexact, Ke, false, st) == cudaSuccess;
+            ok = launch_fp64(ae, nexact, Ke, g64, false, st) == cudaSuccess;
         }
         else {
             ok = (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)

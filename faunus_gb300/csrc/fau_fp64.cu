@@ -1,25 +1,28 @@
-// fau_fp64.cu -- FP64 replica chains: the persistent Metropolis chain of single-atom moves in
-// plain FP64 arithmetic, one CTA per system, for systems made with FAU_PREC_FP64.
+// fau_fp64.cu -- FP64 replica chains: the persistent Metropolis chain in plain FP64 arithmetic,
+// one CTA per system, for systems made with FAU_PREC_FP64.
 //
 // The arithmetic of the plain single-system FP64 form (plain_pair_kernel, plain_ewald_kernel and
-// the host decision of fau_trial_atomic) run as a batched chain: the move, its energy change,
-// the Metropolis decision and the commit stay on the device, so a batch of FP64 systems runs as
-// a persistent launch instead of one host round trip a move.  One loop iteration is one
-// MetropolisMonteCarlo::performMove (src/montecarlo.cpp:139-187) of AtomicTranslateRotate
-// (src/move.cpp:225-293):
+// the host decision of fau_trial_atomic / fau_trial_group) run as a batched chain: the move, its
+// energy change, the Metropolis decision and the commit stay on the device, so a batch of FP64
+// systems runs as a persistent launch instead of one host round trip a move.  One loop
+// iteration is one MetropolisMonteCarlo::performMove (src/montecarlo.cpp:139-187) of
+// AtomicTranslateRotate (src/move.cpp:225-293) or TranslateRotate (src/move.cpp:1670-1689):
 //
-//   thread 0     the proposal (device Philox stream or the caller's proposals), the trial
-//                position (IEEE FP64 add, boundary) and its fixed-point record
-//   all threads  the pair energy of the moved atom in both states (Nonbonded group2all +
-//                groupInternal, src/energy.h:886-914,1183-1195) against every other particle,
-//                or with a cell list against the particles of each state's 3x3x3 stencil (pair_u64
-//                is exactly 0 beyond the pair cutoff, so both sums hold the same terms), FP64
-//                pair_u64 on FP64 minimum-image distances; the reciprocal-space change
-//                d_k = q (e^{i k.r_new} - e^{i k.r_old}) from FP64 phases and
-//                A_k (|Q_k + d_k|^2 - |Q_k|^2) (src/energy.cpp:219-247,524-531)
+//   warp 0       the proposal (device Philox stream or the caller's proposals) and the trial
+//                positions: prepare_move, the chain kernel's IEEE FP64 translation, rotation
+//                about the new mass centre and wrapping, with fixed-point records
+//   all threads  molecular moves: the GroupCutoff decision of every other group in both states
+//                (mass-centre distances, src/energy.h:761-768)
+//   all threads  the pair energy of the moved atoms in both states (Nonbonded group2all +
+//                groupInternal, src/energy.h:886-914,1156-1195) against every other particle,
+//                or for a single atom with a cell list against the particles of each state's
+//                3x3x3 stencil (pair_u64 is exactly 0 beyond the pair cutoff, so both sums hold
+//                the same terms), FP64 pair_u64 on FP64 minimum-image distances; the
+//                reciprocal-space change d_k = sum_a q_a (e^{i k.r_new} - e^{i k.r_old}) from
+//                FP64 phases and A_k (|Q_k + d_k|^2 - |Q_k|^2) (src/energy.cpp:219-247,524-531)
 //   thread 0     the surface-term change (src/energy.cpp:466-482), getEnergyChange and
 //                metropolisCriterion (src/montecarlo.cpp:17-34,193-209) on the FP64 sum, and
-//                on accept the commit (positions, record, cell list)
+//                on accept the commit (positions, records, cell list or mass centre)
 //   all threads  Q_k += d_k on accept (Ewald::sync, src/energy.cpp:640-658)
 //
 // Every sum is FP64 in a fixed order (per thread, then a shuffle tree, then the warps in index
@@ -32,16 +35,6 @@ namespace {
 constexpr int kF64Threads = 128;
 constexpr int kF64Warps = kF64Threads / 32;
 
-// the move in flight, written by thread 0
-struct F64Move {
-    int kind, i, ti, stop;
-    int cell_old, cell_new;
-    int cc_o[3], cc_n[3]; // cell coordinates of the old and the new position
-    uint4 rn;
-    double xo[3], xn[3], dM[3];
-    double u;
-};
-
 __device__ __forceinline__ int wrap_cell1(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 __device__ __forceinline__ double warp_sum_d(double v)
@@ -49,6 +42,15 @@ __device__ __forceinline__ double warp_sum_d(double v)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// one pair energy of the trial (NEW) or the accepted state into the sum and the inf/NaN flags
+template <bool NEW>
+__device__ __forceinline__ void add_state(double u, double& e, int& f)
+{
+    if (isnan(u)) f |= NEW ? F_NEW_NAN : F_OLD_NAN;
+    else if (isinf(u)) f |= NEW ? F_NEW_INF : F_OLD_INF;
+    else e += NEW ? u : -u;
 }
 
 template <bool PHILOX>
@@ -60,48 +62,51 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
     __shared__ __align__(16) DevSys Ssh;
     for (int w = tid; w < (int)(sizeof(DevSys) / 8); w += kF64Threads)
         reinterpret_cast<unsigned long long*>(&Ssh)[w] = reinterpret_cast<const unsigned long long*>(&G)[w];
-    __shared__ F64Move mv;
+    __shared__ MoveShared ms;
     __shared__ double red_p[kF64Warps], red_r[kF64Warps];
     __shared__ int red_f[kF64Warps];
     __shared__ int sh_acc, sh_stop, sh_up;
     __shared__ unsigned long long sh_t0;
     extern __shared__ __align__(16) unsigned char f64_smem[];
-    double2* dq = reinterpret_cast<double2*>(f64_smem); // this move's change of Q(k)
     __syncthreads();
     const DevSys& S = Ssh;
     const int K = (S.flags & SYS_EWALD) ? S.K : 0;
+    double2* dq = reinterpret_cast<double2*>(f64_smem); // this move's change of Q(k)
+    // per group, molecular moves: bit 0 the trial state's mass centres lie beyond the group
+    // cutoff, bit 1 the accepted state's
+    uint8_t* gcut = f64_smem + (size_t)K * sizeof(double2);
 
     // changes of Q(k) an FP32 chain left pending go into the FP64 master first (as fold_q_kernel
     // folds them), so that the phases below read Q as the chain holds it
-    if (K) {
-        for (int k = tid; k < K; k += kF64Threads) {
-            float2 pe = S.qpend[k];
-            if (S.q_valid) {
-                const float2 d = S.qdlt[k];
-                pe.x += d.x;
-                pe.y += d.y;
-            }
-            if (pe.x != 0.f || pe.y != 0.f) {
-                double2 q = S.Q[k];
-                q.x += (double)pe.x;
-                q.y += (double)pe.y;
-                S.Q[k] = q;
-            }
-            S.qpend[k] = make_float2(0.f, 0.f);
+    for (int k = tid; k < K; k += kF64Threads) {
+        float2 pe = S.qpend[k];
+        if (S.q_valid) {
+            const float2 d = S.qdlt[k];
+            pe.x += d.x;
+            pe.y += d.y;
         }
+        if (pe.x != 0.f || pe.y != 0.f) {
+            double2 q = S.Q[k];
+            q.x += (double)pe.x;
+            q.y += (double)pe.y;
+            S.Q[k] = q;
+        }
+        S.qpend[k] = make_float2(0.f, 0.f);
     }
 
     const long long nmoves = A.n_moves ? A.n_moves[blockIdx.x] : A.moves;
     const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
     const uint32_t sys_id = A.sys_ids ? A.sys_ids[blockIdx.x] : blockIdx.x;
     const unsigned long long ctr0 = A.counters ? A.counters[blockIdx.x] + A.counter_base : A.counter_base;
+    const bool molecular_sys = A.molecular ? (A.molecular[blockIdx.x] != 0) : false;
     const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
+    const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
     const double twopi = 6.283185307179586476925286766559;
 
     // thread 0's running state
     double energy = sys_energy(S), sum_du = 0.0;
     double M[3] = {S.M[0], S.M[1], S.M[2]};
-    unsigned long long n_acc = 0, n_mv = 0;
+    unsigned long long n_acc = 0, n_mv = 0, n_pairs = 0, n_k = 0;
     if (tid == 0) {
         sh_t0 = global_ns();
         sh_up = 0;
@@ -109,64 +114,58 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
     int stop = 0;
     long long t = 0;
     for (; t < nmoves; t++) {
-        // ---- the proposal and its trial state (thread 0)
-        if (tid == 0) {
-            const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)t, sys_id, A.seed, dp_f, 0.0, false)
+        // ---- the proposal and its trial positions (warp 0; prepare_move checks the caller's
+        // proposals where it reads them: a bad index or kind ends the chain with FAU_ERR_ARG)
+        if (warp == 0) {
+            const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)t, sys_id, A.seed, dp_f, dprot,
+                                                        molecular_sys)
                                       : load_proposal(A.props[poff + t]);
-            // the caller's proposals are checked where they are read: an out-of-range index or
-            // any kind but a single-atom or empty move ends the chain with FAU_ERR_ARG
-            const bool ok = p.kind == FAU_MOVE_NONE || (p.kind == FAU_MOVE_ATOMIC && p.index >= 0 && p.index < S.n);
-            mv.stop = ok ? 0 : FAU_ERR_ARG;
-            mv.kind = ok ? p.kind : FAU_MOVE_NONE;
-            mv.u = p.u;
-            mv.i = -1;
-            if (mv.kind == FAU_MOVE_ATOMIC) {
-                const int i = p.index;
-                const uint4 ro = S.rec[i];
-                const double xo[3] = {S.x[i], S.y[i], S.z[i]};
-                mv.i = i;
-                mv.ti = (int)(ro.w >> 24);
-                double xn[3];
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    xn[d] = boundary1(__dadd_rn(xo[d], p.dr[d]), S.L[d], S.half[d], S.inv[d]);
-                    mv.xo[d] = xo[d];
-                    mv.xn[d] = xn[d];
-                }
-                mv.rn = make_uint4(to_fixed(xn[0], S.fx_scale[0]), to_fixed(xn[1], S.fx_scale[1]),
-                                   to_fixed(xn[2], S.fx_scale[2]), ro.w);
-                if (S.flags & SYS_SURFACE) {
-                    const double q = S.itype_qd[mv.ti];
-#pragma unroll
-                    for (int d = 0; d < 3; d++) mv.dM[d] = __dmul_rn(q, __dsub_rn(xn[d], xo[d]));
-                }
-                if (S.flags & SYS_CELLS) { // the old cell is the one the particle is listed in
-                    const int co = S.cell_of[i];
-                    mv.cell_old = co;
-                    mv.cc_o[0] = co % S.cdim[0];
-                    mv.cc_o[1] = (co / S.cdim[0]) % S.cdim[1];
-                    mv.cc_o[2] = co / (S.cdim[0] * S.cdim[1]);
-                    cell_coords(S, xn, mv.rn, mv.cc_n);
-                    mv.cell_new = cell_index(S, mv.cc_n);
-                }
-            }
+            prepare_move(S, ms, p, lane, nullptr, 0);
         }
         __syncthreads(); // B0: the move visible
-        if (mv.stop) {
-            stop = mv.stop;
+        if (ms.stop) {
+            stop = ms.stop;
             break;
         }
-        const int kind = mv.kind;
-        if (kind == FAU_MOVE_ATOMIC) {
-            const int i = mv.i, ti = mv.ti;
-            const double xn[3] = {mv.xn[0], mv.xn[1], mv.xn[2]};
-            const double xo[3] = {mv.xo[0], mv.xo[1], mv.xo[2]};
+        const int kind = ms.kind, m = ms.m, first = ms.first;
+        if (kind == FAU_MOVE_MOLECULAR) { // GroupCutoff of every other group, both states
+            const int g = ms.index;
+            for (int h = tid; h < S.n_groups; h += kF64Threads) {
+                bool cut_o = false, cut_n = false;
+                const double c2 = S.cut_g2g2 >= 0.0 ? group_cut2(S, g, h) : -1.0;
+                if (h != g && c2 >= 0.0 && !(S.g_flags[h] & FAU_GROUP_ATOMIC)) {
+                    const double cmh[3] = {S.g_cm[3 * h], S.g_cm[3 * h + 1], S.g_cm[3 * h + 2]};
+                    const double cmo[3] = {S.g_cm[3 * g], S.g_cm[3 * g + 1], S.g_cm[3 * g + 2]};
+                    cut_o = sqdist_d(S, cmo, cmh) >= c2;
+                    cut_n = sqdist_d(S, ms.cm_new, cmh) >= c2;
+                }
+                gcut[h] = (uint8_t)((cut_n ? 1 : 0) | (cut_o ? 2 : 0));
+            }
+            __syncthreads();
+        }
+        if (kind != FAU_MOVE_NONE) {
             double ep = 0.0, er = 0.0;
             int f = 0;
-            if (S.flags & SYS_CELLS) {
+            if (kind == FAU_MOVE_MOLECULAR) {
+                const int g = ms.index;
+                for (int j = tid; j < S.n; j += kF64Threads) {
+                    const int gj = S.group_of[j];
+                    if (gj == g) continue;
+                    const int fc = gcut[gj];
+                    const int tj = (int)(S.rec[j].w >> 24);
+                    const double xj[3] = {S.x[j], S.y[j], S.z[j]};
+                    for (int a = 0; a < m; a++) {
+                        const int ti = (int)(ms.rec_old[a].w >> 24);
+                        if (!(fc & 1)) add_state<true>(pair_u64(S, ti, tj, sqdist_d(S, ms.xn[a], xj)), ep, f);
+                        if (!(fc & 2)) add_state<false>(pair_u64(S, ti, tj, sqdist_d(S, ms.xo[a], xj)), ep, f);
+                    }
+                }
+            }
+            else if (S.flags & SYS_CELLS) {
                 // each state over the stencil of its own cell (GridOffsets3D, src/celllistimpl.cpp:
                 // 15-31): every particle within the pair cutoff of a position lies in the stencil
-                // of that position's cell, and pair_u64 is exactly 0 beyond the cutoff
+                // of that position's cell
+                const int i = first, ti = (int)(ms.rec_old[0].w >> 24);
                 const int nbx = S.off_max[0] - S.off_min[0] + 1, nby = S.off_max[1] - S.off_min[1] + 1,
                           nbz = S.off_max[2] - S.off_min[2] + 1;
                 const int cap = S.cap, cap_shift = __ffs(cap) - 1;
@@ -177,53 +176,44 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
                     const int o[3] = {e % nbx + S.off_min[0], (e / nbx) % nby + S.off_min[1], e / (nbx * nby) + S.off_min[2]};
                     int c[3];
 #pragma unroll
-                    for (int d = 0; d < 3; d++) c[d] = wrap_cell1((st ? mv.cc_o[d] : mv.cc_n[d]) + o[d], S.cdim[d]);
+                    for (int d = 0; d < 3; d++) c[d] = wrap_cell1((st ? ms.cc_old[d] : ms.cc_new[d]) + o[d], S.cdim[d]);
                     const uint4 rj = S.cell_rec[(size_t)cell_index(S, c) * cap + (r & (cap - 1))];
                     if (rj.w == kEmptySlot) continue;
                     const int j = (int)(rj.w & 0xFFFFFFu);
                     if (j == i) continue;
                     const double xj[3] = {S.x[j], S.y[j], S.z[j]};
-                    const double u = pair_u64(S, ti, (int)(rj.w >> 24), sqdist_d(S, st ? xo : xn, xj));
-                    if (st == 0) {
-                        if (isnan(u)) f |= F_NEW_NAN;
-                        else if (isinf(u)) f |= F_NEW_INF;
-                        else ep += u;
-                    }
-                    else {
-                        if (isnan(u)) f |= F_OLD_NAN;
-                        else if (isinf(u)) f |= F_OLD_INF;
-                        else ep -= u;
-                    }
+                    const double u = pair_u64(S, ti, (int)(rj.w >> 24), sqdist_d(S, st ? ms.xo[0] : ms.xn[0], xj));
+                    if (st == 0) add_state<true>(u, ep, f);
+                    else add_state<false>(u, ep, f);
                 }
             }
             else {
+                const int i = first, ti = (int)(ms.rec_old[0].w >> 24);
                 for (int j = tid; j < S.n; j += kF64Threads) {
                     if (j == i) continue;
                     const int tj = (int)(S.rec[j].w >> 24);
                     const double xj[3] = {S.x[j], S.y[j], S.z[j]};
-                    const double un = pair_u64(S, ti, tj, sqdist_d(S, xn, xj));
-                    const double uo = pair_u64(S, ti, tj, sqdist_d(S, xo, xj));
-                    if (isnan(un)) f |= F_NEW_NAN;
-                    else if (isinf(un)) f |= F_NEW_INF;
-                    else ep += un;
-                    if (isnan(uo)) f |= F_OLD_NAN;
-                    else if (isinf(uo)) f |= F_OLD_INF;
-                    else ep -= uo;
+                    add_state<true>(pair_u64(S, ti, tj, sqdist_d(S, ms.xn[0], xj)), ep, f);
+                    add_state<false>(pair_u64(S, ti, tj, sqdist_d(S, ms.xo[0], xj)), ep, f);
                 }
             }
             if (K) {
-                const double q = S.itype_qd[ti];
                 for (int k = tid; k < K; k += kF64Threads) {
                     int nx, ny, nz;
                     kn_unpack(S.kn[k], nx, ny, nz);
                     const double kx = twopi * ((double)nx / S.L[0]), ky = twopi * ((double)ny / S.L[1]),
                                  kz = twopi * ((double)nz / S.L[2]);
-                    const double pn = (kx * xn[0] + ky * xn[1]) + kz * xn[2];
-                    const double po = (kx * xo[0] + ky * xo[1]) + kz * xo[2];
-                    double sn, cn, so, co;
-                    sincos(pn, &sn, &cn);
-                    sincos(po, &so, &co);
-                    const double dx = q * cn - q * co, dy = q * sn - q * so;
+                    double dx = 0.0, dy = 0.0;
+                    for (int a = 0; a < m; a++) {
+                        const double q = S.itype_qd[ms.rec_old[a].w >> 24];
+                        const double pn = (kx * ms.xn[a][0] + ky * ms.xn[a][1]) + kz * ms.xn[a][2];
+                        const double po = (kx * ms.xo[a][0] + ky * ms.xo[a][1]) + kz * ms.xo[a][2];
+                        double sn, cn, so, co;
+                        sincos(pn, &sn, &cn);
+                        sincos(po, &so, &co);
+                        dx += q * cn - q * co;
+                        dy += q * sn - q * so;
+                    }
                     dq[k] = make_double2(dx, dy);
                     const double2 Q = S.Q[k];
                     const double nq2 = (Q.x + dx) * (Q.x + dx) + (Q.y + dy) * (Q.y + dy);
@@ -246,7 +236,7 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
         if (tid == 0) {
             int accept = 0, st = 0;
             double du = 0.0;
-            if (kind == FAU_MOVE_ATOMIC) {
+            if (kind != FAU_MOVE_NONE) {
                 double ep = 0.0, er = 0.0;
                 int f = 0;
 #pragma unroll
@@ -261,7 +251,7 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
                     double m2o = 0.0, m2n = 0.0;
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
-                        const double mn = __dadd_rn(M[d], mv.dM[d]);
+                        const double mn = __dadd_rn(M[d], ms.dM[d]);
                         m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
                         m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
                     }
@@ -270,29 +260,41 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
                 du = energy_change(ep + (du_rec + du_surf), f & F_NEW_INF, f & F_OLD_INF, f & F_NEW_NAN, f & F_OLD_NAN);
                 const double x = du * S.beta_scale;
                 if (isnan(x)) st = FAU_ERR_NAN; // metropolisCriterion throws: the launch ends before this move
-                else accept = metropolis(x, mv.u) ? 1 : 0;
-                if (!st) n_mv++;
+                else accept = metropolis(x, ms.u) ? 1 : 0;
+                if (!st) {
+                    n_mv++;
+                    n_pairs += 2ull * (unsigned long long)m * (unsigned long long)(S.n - m);
+                    n_k += (unsigned long long)K * (unsigned long long)m;
+                }
             }
             if (!st) {
                 if (A.acc_out) A.acc_out[poff + t] = (uint8_t)accept;
                 if (A.du_out) A.du_out[poff + t] = du;
             }
-            if (accept) { // State::sync trial -> accepted: positions, record, cell list
+            if (accept) { // State::sync trial -> accepted: positions, records, cell list, mass centre
                 n_acc++;
                 sum_du += du;
                 energy += du;
-                const int i = mv.i;
                 if (S.flags & SYS_SURFACE) {
 #pragma unroll
-                    for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], mv.dM[d]);
+                    for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
                 }
-                S.x[i] = mv.xn[0];
-                S.y[i] = mv.xn[1];
-                S.z[i] = mv.xn[2];
-                const uint4 rn = mv.rn;
-                S.rec[i] = rn;
-                if (S.flags & SYS_CELLS) {
-                    const int co = mv.cell_old, cn = mv.cell_new;
+                for (int a = 0; a < m; a++) {
+                    S.x[first + a] = ms.xn[a][0];
+                    S.y[first + a] = ms.xn[a][1];
+                    S.z[first + a] = ms.xn[a][2];
+                    S.rec[first + a] = ms.rec_new[a];
+                }
+                if (kind == FAU_MOVE_MOLECULAR) {
+                    const int g = ms.index;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) S.g_cm[3 * g + d] = ms.cm_new[d];
+                    S.g_cmrec[g] = ms.cmrec_new;
+                }
+                else if (S.flags & SYS_CELLS) {
+                    const int i = first;
+                    const uint4 rn = ms.rec_new[0];
+                    const int co = ms.cell_old, cn = ms.cell_new;
                     const int so = S.slot_of[i];
                     if (co == cn) {
                         S.cell_rec[(size_t)co * S.cap + so] = rn;
@@ -349,8 +351,8 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
     }
     __syncthreads();
     if (tid == 0) {
-        G.pair_evals += 2ull * (unsigned long long)(S.n > 0 ? S.n - 1 : 0) * n_mv;
-        G.k_updates += n_mv * (unsigned long long)K;
+        G.pair_evals += n_pairs;
+        G.k_updates += n_k;
         G.moves += n_mv;
         G.accepted += n_acc;
         G.sum_du += sum_du;
@@ -367,11 +369,11 @@ __global__ void __launch_bounds__(kF64Threads, 4) fp64_chain_kernel(ChainArgs A)
 }
 
 template <bool PH>
-cudaError_t launch_fp64_inst(const ChainArgs& a, int nblocks, int K, cudaStream_t st, bool prepare_only)
+cudaError_t launch_fp64_inst(const ChainArgs& a, int nblocks, int K, int n_groups, cudaStream_t st, bool prepare_only)
 {
     // the dynamic allowance is raised on demand, never inside a stream capture: callers prepare first
     static size_t granted = 0;
-    const size_t smem = fp64_smem_bytes(K);
+    const size_t smem = fp64_smem_bytes(K, n_groups);
     if (smem > granted || granted == 0) {
         const cudaError_t e =
             cudaFuncSetAttribute(fp64_chain_kernel<PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -385,17 +387,21 @@ cudaError_t launch_fp64_inst(const ChainArgs& a, int nblocks, int K, cudaStream_
 
 } // namespace
 
-size_t fp64_smem_bytes(int K) { return (size_t)(K > 0 ? K : 0) * sizeof(double2); }
-
-cudaError_t prepare_fp64(int K, bool philox)
+size_t fp64_smem_bytes(int K, int n_groups)
 {
-    return philox ? launch_fp64_inst<true>(ChainArgs{}, 0, K, nullptr, true)
-                  : launch_fp64_inst<false>(ChainArgs{}, 0, K, nullptr, true);
+    return (size_t)(K > 0 ? K : 0) * sizeof(double2) + (((size_t)(n_groups > 0 ? n_groups : 0) + 15) & ~size_t(15));
 }
 
-cudaError_t launch_fp64(const ChainArgs& a, int nblocks, int K, bool philox, cudaStream_t st)
+cudaError_t prepare_fp64(int K, int n_groups, bool philox)
 {
-    return philox ? launch_fp64_inst<true>(a, nblocks, K, st, false) : launch_fp64_inst<false>(a, nblocks, K, st, false);
+    return philox ? launch_fp64_inst<true>(ChainArgs{}, 0, K, n_groups, nullptr, true)
+                  : launch_fp64_inst<false>(ChainArgs{}, 0, K, n_groups, nullptr, true);
+}
+
+cudaError_t launch_fp64(const ChainArgs& a, int nblocks, int K, int n_groups, bool philox, cudaStream_t st)
+{
+    return philox ? launch_fp64_inst<true>(a, nblocks, K, n_groups, st, false)
+                  : launch_fp64_inst<false>(a, nblocks, K, n_groups, st, false);
 }
 
 } // namespace fau

@@ -109,10 +109,11 @@ cudaError_t launch_fold_q(DevSys* dsys, int K, cudaStream_t st); // pending Q(k)
 cudaError_t launch_plain_du(const DevSys* dsys, const PlainMove* pm, int n, int K, double2* dq, double* out,
                             int* flags, cudaStream_t st);
 cudaError_t launch_plain_commit(DevSys* dsys, const PlainMove* pm, int K, const double2* dq, cudaStream_t st);
-// FP64 replica chains (systems made with FAU_PREC_FP64; single-atom moves, 128-thread CTAs): the
-// plain FP64 form's arithmetic as a persistent chain, one CTA per system
-size_t fp64_smem_bytes(int K);
-cudaError_t prepare_fp64(int K, bool philox);
-cudaError_t launch_fp64(const ChainArgs& a, int nblocks, int K, bool philox, cudaStream_t st);
+// FP64 replica chains (systems made with FAU_PREC_FP64; single-atom and rigid-molecule moves,
+// 128-thread CTAs): the plain FP64 form's arithmetic as a persistent chain, one CTA per system;
+// K and n_groups the largest of the launch's systems
+size_t fp64_smem_bytes(int K, int n_groups);
+cudaError_t prepare_fp64(int K, int n_groups, bool philox);
+cudaError_t launch_fp64(const ChainArgs& a, int nblocks, int K, int n_groups, bool philox, cudaStream_t st);
 
 } // namespace fau

@@ -383,16 +383,16 @@ int fau_run_proposals(fau_sys* sys, const fau_proposal* proposals, int n,
  * in descending order of their block's cost (moves x particles), so that the
  * largest begin first, each on an SM of its own while SMs remain.
  * Systems made with FAU_PREC_FP64 run as FP64 replica chains (the plain FP64
- * form's pair sums, Ewald phases and Metropolis decision, all on the device;
- * single-atom moves; no finite maxenergy): a batch holds FP64 systems only or
- * none, else FAU_ERR_ARG. */
+ * form's pair sums, GroupCutoff, Ewald phases and Metropolis decision, all on
+ * the device; single-atom and rigid-molecule moves; no finite maxenergy): a
+ * batch holds FP64 systems only or none, else FAU_ERR_ARG. */
 int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* params,
                   fau_batch_stats* stats);
 
 /* Host-fed proposals for n systems in one launch (one CTA per system):
  * proposals[offsets[i] .. offsets[i+1]) belong to systems[i].  accepted_out
  * and du_out (optional) are indexed like proposals.  FP64 systems run as FP64
- * replica chains, as in fau_run_batch (single-atom or empty proposals only). */
+ * replica chains, as in fau_run_batch. */
 int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_proposal* proposals,
                             const int64_t* offsets, uint8_t* accepted_out, double* du_out,
                             fau_batch_stats* stats);

@@ -1,5 +1,6 @@
 """FP64 replica chains: systems made with FAU_PREC_FP64 run in fau_run_batch and
-fau_run_proposals_batch as persistent chains in plain FP64 arithmetic (fau_fp64.cu).
+fau_run_proposals_batch as persistent chains in plain FP64 arithmetic (fau_fp64.cu), for
+single-atom and rigid-molecule moves.
 
 The primitive model of the 200-ion electrolyte is specified in FP64 with 1e5 moves: its
 reference-stream chain is compared with the FP64 oracle move by move.  Both sides are FP64 and
@@ -139,13 +140,50 @@ def test_fp64_and_fp32c_systems_do_not_share_a_batch(ctx):
     b.close()
 
 
-def test_fp64_chain_rejects_molecular_proposals(ctx):
-    w = ctx.create(configs.spce_water(n_mol=256, L=18.6, precision=A.FAU_PREC_FP64))
-    props = _props(w.spec, 10)
-    assert (props["kind"] == A.FAU_MOVE_MOLECULAR).any()
-    with pytest.raises(F.FauError, match="single-atom"):
-        ctx.run_proposals_batch([w], props, np.array([0, 10], np.int64))
-    w.close()
+@pytest.mark.parametrize("make", [
+    lambda: configs.spce_water(n_mol=256, L=18.6, seed=3, precision=A.FAU_PREC_FP64),
+    lambda: configs.spce_water(n_mol=256, L=18.6, seed=5, epss=1.0, precision=A.FAU_PREC_FP64),
+    lambda: configs.spce_water(n_mol=512, L=24.8, seed=6, molecules=("M", "Q"), cutoff_g2g={"default": 7.0, "M Q": 10.0},
+                               precision=A.FAU_PREC_FP64),
+])
+def test_fp64_chain_rigid_molecules(ctx, make):
+    """Rigid SPC/E water (TranslateRotate moves of the reference stream, GroupCutoff per molecule
+    pair, Ewald and its surface term) through the FP64 chain kernel: the oracle's chain, and the
+    plain FP64 form's dU within 1e-13 of max(1, |dU|) kT (the two sum the group's pairs in
+    different orders); positions and mass centres bit-identical."""
+    spec = make()
+    g, o, st, acc, props, du = _fp64_vs_oracle(ctx, spec, 1000, 1e-10, atol=1e-11)
+    assert (props["kind"] == A.FAU_MOVE_MOLECULAR).all() and acc.sum() > 200
+    assert np.array_equal(g.mass_centers(), o.mass_centers())
+    p = ctx.create(spec)
+    acc_p, du_p, _ = p.run_proposals(props)
+    assert np.array_equal(acc_p, acc)
+    fin = np.isfinite(du)
+    assert (np.abs(du[fin] - du_p[fin]) <= 1e-13 * np.maximum(1.0, np.abs(du_p[fin]))).all()
+    assert np.array_equal(p.positions(), g.positions())
+    e_run, e_tot = g.running_energy(), g.energy_total()["total"]
+    assert abs(e_run - e_tot) <= 1e-9 * max(1.0, abs(e_tot))
+    p.close()
+
+
+def test_fp64_molecular_batch_equals_each_chain_alone(ctx):
+    """Device proposals (moltransrot): each FP64 water chain of a batch ends where it ends alone."""
+    spec = configs.spce_water(n_mol=256, L=18.6, seed=4, precision=A.FAU_PREC_FP64)
+    reps = [ctx.create(spec) for _ in range(3)]
+    streams = np.array([7, 8, 9], np.uint32)
+    st = ctx.run_batch(reps, 800, seed=2, dp=0.5, dprot=0.5, streams=streams)
+    assert st["moves"] == 3 * 800 and st["accepted"] > 300
+    for k, r in enumerate(reps):
+        alone = ctx.create(spec)
+        ctx.run_batch([alone], 800, seed=2, dp=0.5, dprot=0.5, streams=streams[k:k + 1])
+        assert np.array_equal(alone.positions(), r.positions())
+        assert np.array_equal(alone.mass_centers(), r.mass_centers())
+        assert alone.running_energy() == r.running_energy()
+        e_tot = r.energy_total()["total"]
+        assert abs(r.running_energy() - e_tot) <= 1e-9 * max(1.0, abs(e_tot))
+        alone.close()
+    for r in reps:
+        r.close()
 
 
 def _two_spheres(pos, sigma2=16.0, terms=A.FAU_PAIR_HS | A.FAU_PAIR_COULOMB):
