@@ -478,10 +478,17 @@ def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: in
         st = ctx.run_batch(systems, M, seed=1, counter_base=M, **kw)
         for s_ in systems:
             s_.close()
+        audit.clear()
+        if st["du_err_samples"]:
+            audit.update({"rel_scaled_max": st["du_err_scaled_max"], "rel_du_max": st["du_err_rel_max"],
+                          "probes": st["du_err_samples"]})
         return st["moves"] / (st["device_ms"] * 1e-3), st["pair_evals"] / (st["device_ms"] * 1e-3)
 
+    audit = {}  # the timed launch's audit probes (error of the FP32 changes against FP64)
+
     mps, pps = batch_rate(configs.primitive_model(n=200), replicas, 20000)
-    out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps}
+    out["primitive_model_200"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
+                                  "du_err_vs_fp64_audit": dict(audit)}
     # the primitive model as specified, in FP64: FP64 replica chains (fau_fp64.cu)
     mps, pps = batch_rate(configs.primitive_model(n=200, precision=A.FAU_PREC_FP64), replicas, 20000)
     out["primitive_model_200_fp64"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
@@ -494,7 +501,8 @@ def other_configs(ctx, configs, replicas: int, sweeps: int = 1000, pt_blocks: in
                                               "FP64 sin/cos of k.r for the K = 1152 k-vectors)"}
     mps, pps = batch_rate(configs.spce_water(n_mol=1000), replicas, 5000)
     out["spce_water_1000"] = {"replicas": replicas, "moves_per_s": mps, "pair_interactions_per_s": pps,
-                              "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)"}
+                              "kernel": "pipelined molecular kernel (1 preparing + 7 compute warps)",
+                              "du_err_vs_fp64_audit": dict(audit)}
     out["parallel_tempering_256"] = parallel_tempering(ctx, configs, sweeps, pt_blocks, pt_budget_s)
     return out
 

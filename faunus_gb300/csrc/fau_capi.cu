@@ -917,8 +917,8 @@ int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
     if ((rc = dev_alloc(s, &s->d_partials, kTotalPartials))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_flags, 4))) return bail(rc);
     if (lay.K > 0 && (rc = dev_alloc(s, &s->d_dq, lay.K))) return bail(rc);
-    // the pipelined kernel's audit probe record (systems of atomic groups run in it)
-    if (s->all_atomic && (rc = dev_alloc(s, &h.audit_rec, kAuditRecBytes))) return bail(rc);
+    // the audit probe record of the pipelined kernels (single-atom and molecular)
+    if ((rc = dev_alloc(s, &h.audit_rec, kAuditRecBytes))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d, 1))) return bail(rc);
     if ((rc = dev_alloc(s, &s->d_self, 1))) return bail(rc);
     if (cudaMemcpyAsync(s->d, &h, sizeof(DevSys), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||

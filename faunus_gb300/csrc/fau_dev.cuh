@@ -171,7 +171,16 @@ struct DevSys {
     double maxenergy;
     int maxe, pad6;
 };
-constexpr size_t kAuditRecBytes = 640; // a probe move of the pipelined kernel
+constexpr size_t kAuditRecBytes = 1024; // a probe move: the pipelined kernels' FastMove or MolProbe
+
+// the pipelined molecular kernel's probe move: the group it moves, its atoms' trial positions (the
+// old ones are the system's, unchanged by the probe), the new mass centre and the dipole change
+struct MolProbe {
+    int kind, index, m, first;
+    double cm_new[3], dM[3], du_surf, pad;
+    double xn[kMaxGroupAtoms][3];
+};
+static_assert(sizeof(MolProbe) <= kAuditRecBytes, "audit record size");
 
 // ---------------------------------------------------------------- fixed point
 __host__ __device__ inline uint32_t to_fixed(double x, double scale)

@@ -224,9 +224,13 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     const float dp_f = (float)(A.dp_sys ? A.dp_sys[blockIdx.x] : A.dp);
     const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
     const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
+    // the audit probe: one more move (the chain's next proposal; a host stream's last one again)
+    // evaluated after the last one on the final state, never decided or committed; its FP32
+    // energy change and the move go to the system's audit record for mol_audit_kernel
+    const long long nloop = nmoves + (A.audit && nmoves > 0 && G.audit_rec ? 1 : 0);
     // move idx's proposal: the host's (A.props, checked by prepare_move) or the device RNG's
     auto proposal = [&](long long idx) -> Proposal {
-        if constexpr (HOST) return load_proposal(A.props[poff + idx]);
+        if constexpr (HOST) return load_proposal(A.props[poff + (idx < nmoves ? idx : nmoves - 1)]);
         else return philox_proposal(S, ctr0 + (unsigned long long)idx, sys_id, A.seed, dp_f, dprot, true);
     };
     const int nt = S.nt;
@@ -300,24 +304,28 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     }
     __syncthreads();
 
-    for (long long mv = 0; mv < nmoves; mv++) {
+    for (long long mv = 0; mv < nloop; mv++) {
         const int cur = (int)(mv & 1);
         MoveShared& ms = msb[cur];
         MoveShared& mn = msb[cur ^ 1];
         const float2* tab = tabs + cur * tab_len;
         float2* tab_next = tabs + (cur ^ 1) * tab_len;
-        if (sh_stop || ms.stop || sh_time_up) { // a NaN energy change ended the chain, a proposal
-            consumed = sh_stop ? sh_consumed : mv; // was invalid, or the time budget is spent
-            err_code = sh_stop ? sh_stop : ms.stop;
+        const bool probe = mv == nmoves;
+        if (sh_stop || (ms.stop && !probe) || sh_time_up) { // a NaN energy change ended the chain, a
+            consumed = sh_stop ? sh_consumed : mv;          // proposal was invalid, or the time
+            err_code = sh_stop ? sh_stop : ms.stop;         // budget is spent
             break;
         }
+        if (probe && ms.stop) break; // no probe of an invalid proposal
+        // the probe's pair and k-vector evaluations are not counted
+        const unsigned long long n_pairs0 = n_pairs, n_k0 = n_k;
         const int kind = ms.kind;
         const int m = ms.m;
         FF accp{0.f, 0.f}, accr{0.f, 0.f};
         int flags = 0;
         if (warp == 0) {
             // ---- speculative preparation of move mv+1 (reads only the group it moves)
-            if (mv + 1 < nmoves) {
+            if (mv + 1 < nloop) {
                 const Proposal p = proposal(mv + 1);
                 tick(13);
                 prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc, timing ? &tacc[14] : nullptr);
@@ -616,6 +624,52 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         }
         __syncthreads(); // B1
         tick(tid == 0 ? 3 : 9);
+        if (probe) {
+            n_pairs = n_pairs0;
+            n_k = n_k0;
+            if (warp == 0) {
+                accp = (lane >= 1 && lane <= NWC) ? red_a[lane] : FF{0.f, 0.f};
+                flags = (lane >= 1 && lane <= NWC) ? red_f[lane] : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
+                    accp = ff_sum(accp, ta);
+                    flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+                }
+                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                if (lane < m) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) pr.xn[lane][d] = ms.xn[lane][d];
+                }
+                if (lane == 0) {
+                    double du_surf = 0.0;
+                    if (S.flags & SYS_SURFACE) {
+                        double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            const double mnv = __dadd_rn(M[d], ms.dM[d]);
+                            m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
+                            m2n = __dadd_rn(m2n, __dmul_rn(mnv, mnv));
+                        }
+                        du_surf = S.surf_pref * (m2n - m2o);
+                    }
+                    pr.kind = kind;
+                    pr.index = ms.index;
+                    pr.m = m;
+                    pr.first = ms.first;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        pr.cm_new[d] = ms.cm_new[d];
+                        pr.dM[d] = ms.dM[d];
+                    }
+                    pr.du_surf = du_surf;
+                    G.audit_du = ff_value(accp) + du_surf;
+                    G.audit_pending = kind == FAU_MOVE_MOLECULAR && flags == 0 ? 1 : 0; // finite in both states
+                    sh_prev_accept = 0; // the probe's pass folded the last accepted change
+                }
+            }
+            break;
+        }
 
         if (warp == 0) {
             accp = (lane >= 1 && lane <= NWC) ? red_a[lane] : FF{0.f, 0.f};
@@ -706,7 +760,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 __syncwarp();
                 __threadfence_block();
                 // the prepared next move read this group's old positions: prepare it again
-                if (mv + 1 < nmoves && mn.kind == FAU_MOVE_MOLECULAR && kind == FAU_MOVE_MOLECULAR &&
+                if (mv + 1 < nloop && mn.kind == FAU_MOVE_MOLECULAR && kind == FAU_MOVE_MOLECULAR &&
                     mn.index == ms.index) {
                     const Proposal p = proposal(mv + 1);
                     prepare_move(S, mn, p, lane, K ? tab_next : nullptr, nc);

@@ -135,3 +135,36 @@ def test_molecular_kernel_host_proposals(ctx):
         assert np.array_equal(acc_c.astype(np.uint8), acc[sl])
         assert np.array_equal(c.positions(), s.positions())
         assert np.allclose(du_c, du[sl], rtol=1e-9, atol=1e-9)
+
+
+def test_molecular_kernel_reports_its_error_against_fp64(ctx):
+    """Each launch's molecular chains end with a probe move (the next proposal, evaluated on the
+    final state and not decided) that mol_audit_kernel re-evaluates in FP64: the batch and each
+    system report its error, within the parity tolerance, and the probe leaves the chains as they
+    were (the same chain as one launch without probes)."""
+    specs = [configs.spce_water(n_mol=256, L=18.6, seed=40 + i) for i in range(3)]
+    specs.append(configs.spce_water(n_mol=256, L=18.6, seed=44, epss=1.0))
+    specs.append(configs.spce_water(n_mol=512, L=24.8, seed=45, molecules=("M", "Q"),
+                                    cutoff_g2g={"default": 7.0, "M Q": 10.0}))
+    systems = [ctx.create(s) for s in specs]
+    quiet = [ctx.create(s) for s in specs]
+    streams = np.arange(len(specs), dtype=np.uint32)
+    for b in range(3):
+        st = ctx.run_batch(systems, 400, seed=3, dp=0.5, dprot=0.5, streams=streams, counters=[400 * b] * len(specs),
+                           threads=160)
+        assert st["du_err_samples"] == len(specs)
+        assert 0.0 < st["du_err_scaled_max"] <= 1e-6
+    ctx.run_batch(quiet, 1200, seed=3, dp=0.5, dprot=0.5, streams=streams, threads=160, audit=False)
+    for s, q in zip(systems, quiet):
+        a = s.audit()
+        assert a["samples"] == 3 and 0.0 < a["rel_scaled_max"] <= 1e-6
+        assert q.audit()["samples"] == 0
+        assert np.array_equal(s.positions(), q.positions())
+        assert s.running_energy() == q.running_energy()
+        _consistent(s)
+    # host proposals (the reference stream) through the molecular kernel report theirs too
+    spec = specs[0]
+    g = ctx.create(spec)
+    props = F.MoveGenerator(spec, spec.extra["moves"], 5, 6, default_seeds=False).generate(300)
+    st = ctx.run_proposals_batch([g], props, np.array([0, 300], np.int64))
+    assert st["du_err_samples"] == 1 and st["du_err_scaled_max"] <= 1e-6
