@@ -10,7 +10,7 @@ molecular translate/rotate moves.  The server
   * keeps every admitted job's state resident on the device between launches;
   * advances all resident jobs together in one ``fau_run_batch`` launch per
     round (per-system dp and dprot; single-atom jobs in the pipelined kernel,
-    molecular ones beside them in the chain kernel) -- jobs join and leave
+    molecular ones beside them in the pipelined molecular kernel) -- jobs join and leave
     between rounds, so work that arrives while others run overlaps with them;
   * gives every job the same device time a round: with ``time_slice_s`` each
     chain runs until it has had that much time of its own (the kernels stop at
@@ -19,8 +19,10 @@ molecular translate/rotate moves.  The server
     ``block_moves`` calibration, after which its measured SM cycles per move
     set how many moves fit in ``round_cycles``;
   * retires a job when its moves are done and reports, per job, the queueing
-    and run time, and for the stream, p50/p99 latency (arrival -> result) and
-    the aggregate moves/s.
+    and run time and the error of its FP32 energy changes against FP64 (the
+    kernels' audit probes: a job's last round ends with one), and for the
+    stream, p50/p99 latency (arrival -> result), the aggregate moves/s and the
+    largest of those errors.
 
 Each job's moves come from the device counter RNG keyed by (server seed, job
 id, move counter), so a job's trajectory -- and its result -- is the same
@@ -61,6 +63,8 @@ class JobResult:
     accepted: int = 0
     energy: float = float("nan")  # running total energy at the end (kT)
     positions: Optional[np.ndarray] = None
+    # the audit probes' error against FP64 ({"rel_scaled_max", "rel_du_max", "samples"}), if any
+    du_err: Optional[dict] = None
     arrival_s: float = 0.0
     admitted_s: float = float("nan")
     finished_s: float = float("nan")
@@ -82,8 +86,9 @@ class _Active:
 
 class GpuBackend:
     """The device through the C ABI: one resident system per job.  `threads` is a fixed
-    kernel width (160: the pipelined kernel with 4 compute warps, molecular jobs in the chain
-    kernel), so that a job's chain is the same whatever other jobs share its launches."""
+    kernel width (160: the pipelined kernel with 4 compute warps, molecular jobs in 256-thread
+    CTAs of the pipelined molecular kernel), so that a job's chain is the same whatever other
+    jobs share its launches."""
 
     def __init__(self, ctx: Context, threads: int = 160):
         self.ctx = ctx
@@ -130,7 +135,7 @@ class GpuBackend:
     def result(self, handle, with_positions: bool) -> dict:
         c = handle.counters()
         return {"energy": handle.running_energy(), "accepted": c["accepted"], "moves": c["moves"],
-                "positions": handle.positions() if with_positions else None}
+                "positions": handle.positions() if with_positions else None, "du_err": handle.audit()}
 
     def close(self, handle) -> None:
         handle.close()
@@ -210,7 +215,7 @@ class Server:
             self.backend.close(a.handle)
             self.resident -= a.bytes
             self.results[jid] = JobResult(jid, "done", moves=r["moves"], accepted=r["accepted"], energy=r["energy"],
-                                          positions=r["positions"], arrival_s=a.job.arrival_s,
+                                          positions=r["positions"], du_err=r.get("du_err"), arrival_s=a.job.arrival_s,
                                           admitted_s=a.admitted_s, finished_s=now)
 
     def step(self) -> int:
@@ -272,6 +277,7 @@ class Server:
     def report(self) -> dict:
         done = [r for r in self.results.values() if r.status == "done"]
         lat = np.array([r.latency_s for r in done]) if done else np.zeros(0)
+        audited = [r.du_err for r in done if r.du_err and r.du_err.get("samples", 0) > 0]
         wall = self.now()
         return {
             "jobs_done": len(done),
@@ -282,6 +288,8 @@ class Server:
             "moves_per_s": self.moves_done / wall if wall > 0 else 0.0,
             "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "jobs_audited": len(audited),
+            "du_err_rel_scaled_max": max((d["rel_scaled_max"] for d in audited), default=None),
         }
 
 

@@ -5,7 +5,8 @@ acceptance counts and running energy, although the server sizes each job's share
 of a round from measured cycles (or from device time, in time-slice rounds) so
 launch boundaries differ between the runs (pending Q(k) changes and partial
 energy sums stay on the device across launches); p50/p99 latency and throughput
-are reported; an over-size job is rejected without disturbing the others."""
+are reported, with every job's error against FP64 from the kernels' audit probes; an over-size job
+is rejected without disturbing the others."""
 import numpy as np
 import pytest
 
@@ -61,6 +62,9 @@ def test_served_stream_reports_latency_and_rejects_oversize(ctx):
     assert rep["p50_latency_s"] is not None and rep["p99_latency_s"] >= rep["p50_latency_s"] > 0
     assert rep["moves"] == sum(j.moves for j in jobs if j.id != 999)
     assert srv.resident == 0
+    # every result carries the error of its FP32 energy changes against FP64 (audit probes)
+    assert rep["jobs_audited"] == 12 and 0.0 < rep["du_err_rel_scaled_max"] <= 1e-6
+    assert all(r.du_err["samples"] >= 1 for r in srv.results.values() if r.status == "done")
 
 
 
