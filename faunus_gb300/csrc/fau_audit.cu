@@ -1,7 +1,7 @@
 // fau_audit.cu -- the FP64 audit of the pipelined kernels' probe moves.
 //
-// After the last move of a launch each chain of fast_chain_kernel (and of mol_chain_kernel, for
-// molecular moves: mol_audit_kernel) evaluates one more move (its
+// After the last move of a launch each chain of fast_chain_kernel (and of mol_chain_kernel and
+// chain_kernel: probe_audit_kernel) evaluates one more move (its
 // next proposal) on its final state without deciding it, and leaves that move and its FP32
 // energy change in the system's audit record.  This kernel re-evaluates the same move in FP64
 // (fast_audit) and keeps the largest error of the FP32 change against it, so that every
@@ -51,25 +51,28 @@ cudaError_t launch_fast_audit(DevSys* const* sys, int n, cudaStream_t st)
     return cudaGetLastError();
 }
 
-// One CTA per system: the FP64 energy change of the molecular kernel's probe (a TranslateRotate
-// move left undecided on the final state) and the FP32 one's error against it.  FP64 as the plain
-// form evaluates it: GroupCutoff by FP64 mass-centre distances (src/energy.h:761-768), pair_u64 of
-// FP64 minimum-image distances against every particle of the other groups, the reciprocal change
-// from FP64 phases against Q(k) as the chain holds it; S is pair_mag64 of every pair of both states
-// plus (2 pi lB / V) A_k (|2 Re(Q* d)| + |d|^2) of every k-vector.
-__global__ void __launch_bounds__(128) mol_audit_kernel(DevSys* const* sys)
+// One CTA per system: the FP64 energy change of a probe of the molecular kernel or the chain
+// kernel (a TranslateRotate or AtomicTranslateRotate move left undecided on the final state) and
+// the FP32 one's error against it.  FP64 as the plain form evaluates it: for a molecular move
+// GroupCutoff by FP64 mass-centre distances (src/energy.h:761-768) and the particles of the other
+// groups, for a single atom every other particle; pair_u64 of FP64 minimum-image distances, the
+// reciprocal change from FP64 phases against Q(k) as the chain holds it; S is pair_mag64 of every
+// pair of both states plus (2 pi lB / V) A_k (|2 Re(Q* d)| + |d|^2) of every k-vector.
+__global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
 {
     DevSys& G = *sys[blockIdx.x];
     if (!G.audit_pending) return;
     const MolProbe& p = *reinterpret_cast<const MolProbe*>(G.audit_rec);
-    const int g = p.index, m = p.m, b = p.first;
-    const double cmo[3] = {G.g_cm[3 * g], G.g_cm[3 * g + 1], G.g_cm[3 * g + 2]};
+    const bool molecular = p.kind == FAU_MOVE_MOLECULAR;
+    const int g = molecular ? p.index : -1, m = p.m, b = p.first;
+    const double cmo[3] = {molecular ? G.g_cm[3 * g] : 0.0, molecular ? G.g_cm[3 * g + 1] : 0.0,
+                           molecular ? G.g_cm[3 * g + 2] : 0.0};
     double du = 0.0, sc = 0.0;
     for (int j = threadIdx.x; j < G.n; j += 128) {
         const int gj = G.group_of[j];
-        if (gj == g) continue;
+        if (molecular ? gj == g : j == b) continue;
         bool cut_o = false, cut_n = false;
-        const double c2 = G.cut_g2g2 >= 0.0 ? group_cut2(G, g, gj) : -1.0;
+        const double c2 = molecular && G.cut_g2g2 >= 0.0 ? group_cut2(G, g, gj) : -1.0;
         if (c2 >= 0.0 && !(G.g_flags[gj] & FAU_GROUP_ATOMIC)) {
             const double cmj[3] = {G.g_cm[3 * gj], G.g_cm[3 * gj + 1], G.g_cm[3 * gj + 2]};
             cut_o = sqdist_d(G, cmo, cmj) >= c2;
@@ -141,10 +144,10 @@ __global__ void __launch_bounds__(128) mol_audit_kernel(DevSys* const* sys)
     }
 }
 
-cudaError_t launch_mol_audit(DevSys* const* sys, int n, cudaStream_t st)
+cudaError_t launch_probe_audit(DevSys* const* sys, int n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    mol_audit_kernel<<<n, 128, 0, st>>>(sys);
+    probe_audit_kernel<<<n, 128, 0, st>>>(sys);
     return cudaGetLastError();
 }
 

@@ -573,7 +573,7 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
                                        : mol_dispatch_256(ae, nexact, Ke, nce, st2, false))
                              : launch_chain(ae, nexact, Ke, nce, threads, true, st2)) != cudaSuccess)
                 return e;
-            if (use_mol && a.audit && (e = launch_mol_audit(ae.sys, nexact, st2)) != cudaSuccess) return e;
+            if (a.audit && (e = launch_probe_audit(ae.sys, nexact, st2)) != cudaSuccess) return e;
             if ((e = cudaEventRecord(join_ev, st2)) != cudaSuccess) return e;
             if ((e = launch_fast(a, nfast, Kf, ncf, ntf, fwarps, true, occf, st)) != cudaSuccess) return e;
             if (a.audit && (e = launch_fast_audit(a.sys, nfast, st)) != cudaSuccess) return e;
@@ -584,13 +584,11 @@ extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const
             return a.audit ? launch_fast_audit(a.sys, nfast, st) : cudaSuccess;
         }
         if (f64) return launch_fp64(ae, nexact, Ke, g64, true, st);
-        if (use_mol) {
-            const cudaError_t e2 = mol512 ? mol_dispatch_512(ae, nexact, Ke, nce, st, false)
-                                          : mol_dispatch_256(ae, nexact, Ke, nce, st, false);
-            if (e2 != cudaSuccess || !a.audit) return e2;
-            return launch_mol_audit(ae.sys, nexact, st);
-        }
-        return launch_chain(ae, nexact, Ke, nce, threads, true, st);
+        const cudaError_t e2 = use_mol ? (mol512 ? mol_dispatch_512(ae, nexact, Ke, nce, st, false)
+                                                : mol_dispatch_256(ae, nexact, Ke, nce, st, false))
+                                       : launch_chain(ae, nexact, Ke, nce, threads, true, st);
+        if (e2 != cudaSuccess || !a.audit) return e2;
+        return launch_probe_audit(ae.sys, nexact, st);
     };
 
     // profiling: FAU_PHASE_TIMING=1 prints the chain kernel's per-phase cycles to stderr
@@ -886,7 +884,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
             ok = cudaEventRecord(fork_ev, st) == cudaSuccess && cudaStreamWaitEvent(st2, fork_ev, 0) == cudaSuccess &&
                  (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st2, false)
                           : launch_chain(ae, nexact, Ke, nce, 256, false, st2)) == cudaSuccess &&
-                 (!use_mol || launch_mol_audit(ae.sys, nexact, st2) == cudaSuccess) &&
+                 launch_probe_audit(ae.sys, nexact, st2) == cudaSuccess &&
                  cudaEventRecord(join_ev, st2) == cudaSuccess;
         }
         else if (f64) {
@@ -895,7 +893,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
         else {
             ok = (use_mol ? mol_dispatch_256(ae, nexact, Ke, nce, st, false)
                           : launch_chain(ae, nexact, Ke, nce, 256, false, st)) == cudaSuccess &&
-                 (!use_mol || launch_mol_audit(ae.sys, nexact, st) == cudaSuccess);
+                 launch_probe_audit(ae.sys, nexact, st) == cudaSuccess;
         }
     }
     if (ok && nfast) ok = launch_fast(a, nfast, Kf, ncf, ntf, 4, false, occf, st) == cudaSuccess;

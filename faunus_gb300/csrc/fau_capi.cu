@@ -1196,6 +1196,9 @@ static int pull_state(fau_sys* s)
     s->h.pair_evals = tmp.pair_evals;
     s->h.k_updates = tmp.k_updates;
     s->h.sum_du = tmp.sum_du;
+    s->h.audit_scaled_max = tmp.audit_scaled_max;
+    s->h.audit_rel_max = tmp.audit_rel_max;
+    s->h.audit_samples = tmp.audit_samples;
     return FAU_OK;
 }
 
@@ -1379,9 +1382,12 @@ static int run_chain(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, dou
         a.acc_out = acc ? s->d_acc + offset : nullptr;
         a.du_out = du ? s->d_du + offset : nullptr;
         a.detail = detail ? s->d_detail + offset : nullptr;
+        // a proposal stream's launch ends with the audit probe (single trials with detail do not)
+        a.audit = detail ? 0 : 1;
         CUDA_TRY(cudaEventRecord(s->ctx->ev0, st));
         CUDA_TRY(launch_chain(a, 1, s->K, s->h.knc, chain_threads(s), false, st));
         CUDA_TRY(cudaEventRecord(s->ctx->ev1, st));
+        if (a.audit) CUDA_TRY(launch_probe_audit(s->d_self, 1, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, s->ctx->ev0, s->ctx->ev1);
@@ -1411,7 +1417,7 @@ static int run_chain(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, dou
         stats->k_updates = (int64_t)(s->h.k_updates - before.k_updates);
         stats->energy_change = s->h.sum_du - before.sum_du;
         stats->energy = s->h.energy;
-        stats->max_rel_err = 0.0;
+        stats->max_rel_err = s->h.audit_scaled_max; // the audit probes' largest error since the system was made
         stats->device_ms = total_ms;
     }
     return rc;

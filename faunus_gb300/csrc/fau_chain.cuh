@@ -558,6 +558,11 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
     const double dprot = A.dprot_sys ? A.dprot_sys[blockIdx.x] : A.dprot;
     const bool detail = A.detail != nullptr;
     const int nt = S.nt;
+    // the audit probe (batched and stream launches; not the evaluate-only mode or a finite
+    // maxenergy): one more move, the chain's next proposal (a host stream's last one again),
+    // evaluated after the last one on the final state and never decided or committed; its FP32
+    // energy change and the move go to the system's audit record for probe_audit_kernel
+    const long long nloop = nmoves + (A.audit && nmoves > 0 && !A.pending && !S.maxe && G.audit_rec ? 1 : 0);
 
     unsigned long long n_acc = 0, n_pairs = 0, n_k = 0, n_mv = 0;
     int since_flush = S.q_since;
@@ -593,8 +598,10 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
     }
     __syncthreads();
 
-    for (long long mv = 0; mv < nmoves; mv++) {
+    for (long long mv = 0; mv < nloop; mv++) {
         if (ms.stop || sh_up_at >= 0) break;
+        const bool probe = mv == nmoves;
+        const unsigned long long n_pairs0 = n_pairs, n_k0 = n_k; // the probe's evaluations are not counted
         // ---- the previous move's Q(k) change (State::sync trial -> accepted, deferred)
         if (ms.prev_accept) {
             for (int k = tid; k < K; k += NT) {
@@ -891,6 +898,58 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
         }
         __syncthreads();
         tick(tid == 0 ? 3 : 9);
+        if (probe) {
+            n_pairs = n_pairs0;
+            n_k = n_k0;
+            if (warp == 0) {
+                accp = lane < NW ? red_a[lane] : FF{0.f, 0.f};
+                accr = lane < NW ? red_b[lane] : FF{0.f, 0.f};
+                flags = lane < NW ? red_f[lane] : 0;
+#pragma unroll
+                for (int o = NW / 2; o > 0; o >>= 1) {
+                    FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
+                    accp = ff_sum(accp, ta);
+                    if (sep) {
+                        FF tb{__shfl_xor_sync(0xffffffffu, accr.hi, o), __shfl_xor_sync(0xffffffffu, accr.lo, o)};
+                        accr = ff_sum(accr, tb);
+                    }
+                    flags |= __shfl_xor_sync(0xffffffffu, flags, o);
+                }
+                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                const int mm = kind == FAU_MOVE_NONE ? 0 : m;
+                if (lane < mm) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) pr.xn[lane][d] = ms.xn[lane][d];
+                }
+                if (lane == 0) {
+                    double du_surf = 0.0;
+                    if (kind != FAU_MOVE_NONE && (S.flags & SYS_SURFACE)) {
+                        double m2o = 0.0, m2n = 0.0;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            const double mn = __dadd_rn(M[d], ms.dM[d]);
+                            m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
+                            m2n = __dadd_rn(m2n, __dmul_rn(mn, mn));
+                        }
+                        du_surf = S.surf_pref * (m2n - m2o);
+                    }
+                    pr.kind = kind;
+                    pr.index = ms.index;
+                    pr.m = mm;
+                    pr.first = ms.first;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        pr.cm_new[d] = ms.cm_new[d];
+                        pr.dM[d] = ms.dM[d];
+                    }
+                    pr.du_surf = du_surf;
+                    G.audit_du = ff_value(accp) + ((sep ? ff_value(accr) : 0.0) + du_surf);
+                    G.audit_pending = kind != FAU_MOVE_NONE && flags == 0 ? 1 : 0; // finite in both states
+                    ms.prev_accept = 0; // the probe's pass folded the last accepted change
+                }
+            }
+            break;
+        }
 
         if (warp == 0) {
             accp = lane < NW ? red_a[lane] : FF{0.f, 0.f};
@@ -1076,16 +1135,22 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                         ms.consumed = mv + 1;
                     }
                 }
-                else if (mv + 1 < nmoves) {
-                    // ---- prepare the next move
+                else if (mv + 1 < nloop) {
+                    // ---- prepare the next move (after the last: the audit probe)
                     const Proposal p = PHILOX ? philox_proposal(S, ctr0 + (unsigned long long)(mv + 1), sys_id, A.seed,
                                                                 dp_f, dprot, molecular_sys)
-                                              : load_proposal(A.props[poff + mv + 1]);
+                                              : load_proposal(A.props[poff + (mv + 1 < nmoves ? mv + 1 : nmoves - 1)]);
                     prepare_move(S, ms, p, lane, K ? tab : nullptr, nc);
                     if (lane == 0) {
+                        if (mv + 1 == nmoves && ms.stop) { // no probe of an invalid proposal
+                            ms.stop = 0;
+                            ms.kind = FAU_MOVE_NONE;
+                            ms.m = 0;
+                        }
                         ms.prev_accept = accept;
                         ms.consumed = mv + 1;
                     }
+                    __syncwarp();
                 }
                 else if (lane == 0) {
                     ms.prev_accept = accept;

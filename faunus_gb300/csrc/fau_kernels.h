@@ -79,8 +79,8 @@ constexpr int kFastMaxNc = 40;
 size_t fast_smem_bytes_total(int K, int nc, int nt);
 // the FP64 audit of the pipelined kernel's probe moves (one CTA per system of `sys`)
 cudaError_t launch_fast_audit(DevSys* const* sys, int n, cudaStream_t st);
-// the FP64 audit of the molecular kernel's probe moves (one CTA per system of `sys`)
-cudaError_t launch_mol_audit(DevSys* const* sys, int n, cudaStream_t st);
+// the FP64 audit of the molecular and chain kernels' probe moves (one CTA per system of `sys`)
+cudaError_t launch_probe_audit(DevSys* const* sys, int n, cudaStream_t st);
 // occ: a system of the launch is flagged SYS_OCC.  Then 4 and 8 compute warps run the instance
 // holding every staging body, each CTA choosing by its system; otherwise the instance holding
 // only the whole-cell body (the same code for those systems, without the register pressure of

@@ -208,9 +208,11 @@ typedef struct fau_run_stats {
     int64_t k_updates;      /* Ewald k-vector x moved-atom phase updates          */
     double energy_change;   /* sum of accepted dU (sum_of_energy_changes)         */
     double energy;          /* running total energy after the run                 */
-    double max_rel_err;     /* 0 from this single-system entry point; the error against FP64
-                               is audited for systems that run in the pipelined kernel
-                               (fau_batch_stats.du_err_*, fau_get_audit)            */
+    double max_rel_err;     /* the largest error of the FP32 energy changes against FP64
+                               re-evaluations of audit probes (each launch ends with one
+                               move evaluated on the final state, not decided), relative
+                               to max(|dU|, S), since the system was made; 0 for the plain
+                               FP64 form (fau_get_audit gives the other measures)     */
     double device_ms;       /* device time of the run (CUDA events)               */
 } fau_run_stats;
 

@@ -402,3 +402,19 @@ def test_clone_is_an_independent_copy(ctx):
     ctx.run_batch([b], 500, seed=1, streams=[3], threads=256)
     assert np.array_equal(a.positions(), b.positions())
     assert np.array_equal(a.q(), b.q()) and np.array_equal(a.cells(), b.cells())
+
+
+def test_chain_kernel_reports_its_error_against_fp64(ctx):
+    """Proposal streams (fau_run_proposals) and chain-kernel batches (threads 256) end each launch
+    with an audit probe re-evaluated in FP64: fau_run_stats.max_rel_err and the batch's du_err_*
+    carry the error of the FP32 energy changes, within the parity tolerance; the chain is the
+    oracle's all the same."""
+    spec = configs.bulk_ewald(n_salt=1000, epss=1.0)
+    g = ctx.create(spec)
+    rep, _ = _compare_chain(g, spec, _props(spec, 1500), TOL_FP32C)
+    assert 0.0 < rep["stats"]["max_rel_err"] <= TOL_FP32C
+    assert g.audit()["samples"] == 1
+    w = configs.spce_water(n_mol=256, L=18.6, seed=3)
+    systems = [ctx.create(w), ctx.create(configs.primitive_model(n=200, seed=4))]
+    st = ctx.run_batch(systems, 600, seed=5, dp_per_system=[0.5, 2.0], dprot_per_system=[0.5, 0.0], threads=256)
+    assert st["du_err_samples"] == 2 and 0.0 < st["du_err_scaled_max"] <= TOL_FP32C
