@@ -419,7 +419,9 @@ def run_ours(args) -> None:
         "roofline": roof,
         "roofline_other": roof_other,
         "clocks": clk,
-        "gpu_launches": 3 * args.steps,
+        # per timed step (one fau_run_batch call): the chain kernel and its FP64 audit in the graph,
+        # and the two counter gathers around it
+        "gpu_launches": 4 * args.steps,
         "wall_s": wall,
     }
     if rank == 0 and not args.no_extras:
