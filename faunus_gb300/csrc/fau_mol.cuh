@@ -240,6 +240,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     double energy = sys_energy(S), sum_du = 0.0; // the pipelined kernel's unfolded part folded in
     double M[3] = {S.M[0], S.M[1], S.M[2]};
     long long consumed = nmoves;
+    bool counted = false; // the pair and k-vector counts were reduced before the audit probe
     int err_code = 0; // the status that ended the chain early (FAU_ERR_*), 0 if none
 
     // phase timers (profiling only): warp 0 (tid 0): 6 prepare ahead, 3 wait B1, 4 decision,
@@ -317,8 +318,19 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
             break;
         }
         if (probe && ms.stop) break; // no probe of an invalid proposal
-        // the probe's pair and k-vector evaluations are not counted
-        const unsigned long long n_pairs0 = n_pairs, n_k0 = n_k;
+        if (probe) { // the counts end before the probe's pair and k-vector evaluations
+            unsigned long long a = n_pairs, b = n_k;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                b += __shfl_xor_sync(0xffffffffu, b, o);
+            }
+            if (lane == 0) {
+                sm.red_u[warp][0] = a;
+                sm.red_u[warp][1] = b;
+            }
+            counted = true;
+        }
         const int kind = ms.kind;
         const int m = ms.m;
         FF accp{0.f, 0.f}, accr{0.f, 0.f};
@@ -624,53 +636,6 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         }
         __syncthreads(); // B1
         tick(tid == 0 ? 3 : 9);
-        if (probe) {
-            n_pairs = n_pairs0;
-            n_k = n_k0;
-            if (warp == 0) {
-                accp = (lane >= 1 && lane <= NWC) ? red_a[lane] : FF{0.f, 0.f};
-                flags = (lane >= 1 && lane <= NWC) ? red_f[lane] : 0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    FF ta{__shfl_xor_sync(0xffffffffu, accp.hi, o), __shfl_xor_sync(0xffffffffu, accp.lo, o)};
-                    accp = ff_sum(accp, ta);
-                    flags |= __shfl_xor_sync(0xffffffffu, flags, o);
-                }
-                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
-                if (lane < m) {
-#pragma unroll
-                    for (int d = 0; d < 3; d++) pr.xn[lane][d] = ms.xn[lane][d];
-                }
-                if (lane == 0) {
-                    double du_surf = 0.0;
-                    if (S.flags & SYS_SURFACE) {
-                        double m2o = 0.0, m2n = 0.0;
-#pragma unroll
-                        for (int d = 0; d < 3; d++) {
-                            const double mnv = __dadd_rn(M[d], ms.dM[d]);
-                            m2o = __dadd_rn(m2o, __dmul_rn(M[d], M[d]));
-                            m2n = __dadd_rn(m2n, __dmul_rn(mnv, mnv));
-                        }
-                        du_surf = S.surf_pref * (m2n - m2o);
-                    }
-                    pr.kind = kind;
-                    pr.index = ms.index;
-                    pr.m = m;
-                    pr.first = ms.first;
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        pr.cm_new[d] = ms.cm_new[d];
-                        pr.dM[d] = ms.dM[d];
-                    }
-                    pr.du_surf = du_surf;
-                    G.audit_du = ff_value(accp) + du_surf;
-                    G.audit_pending = kind == FAU_MOVE_MOLECULAR && flags == 0 ? 1 : 0; // finite in both states
-                    sh_prev_accept = 0; // the probe's pass folded the last accepted change
-                }
-            }
-            break;
-        }
-
         if (warp == 0) {
             accp = (lane >= 1 && lane <= NWC) ? red_a[lane] : FF{0.f, 0.f};
             flags = (lane >= 1 && lane <= NWC) ? red_f[lane] : 0;
@@ -695,23 +660,47 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                     du_surf = S.surf_pref * (m2n - m2o);
                 }
                 const double fin = ff_value(accp) + (0.0 + du_surf);
-                const double du =
-                    energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
-                const double x = du * S.beta_scale;
-                du_out = du;
-                if (isnan(x)) stop = FAU_ERR_NAN;
-                else accept = metropolis(x, ms.u) ? 1 : 0;
-                if (accept) {
-                    n_acc++;
-                    sum_du += du;
-                    energy += du;
+                if (probe) { // the audit probe: recorded for probe_audit_kernel, not decided
+                    MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                    pr.kind = kind;
+                    pr.index = ms.index;
+                    pr.m = m;
+                    pr.first = ms.first;
 #pragma unroll
-                    for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
+                    for (int d = 0; d < 3; d++) {
+                        pr.cm_new[d] = ms.cm_new[d];
+                        pr.dM[d] = ms.dM[d];
+                    }
+                    pr.du_surf = du_surf;
+                    G.audit_du = fin;
+                    G.audit_pending = flags == 0 ? 1 : 0; // finite in both states
                 }
-                if (!stop) n_mv++;
+                else {
+                    const double du =
+                        energy_change(fin, flags & F_NEW_INF, flags & F_OLD_INF, flags & F_NEW_NAN, flags & F_OLD_NAN);
+                    const double x = du * S.beta_scale;
+                    du_out = du;
+                    if (isnan(x)) stop = FAU_ERR_NAN;
+                    else accept = metropolis(x, ms.u) ? 1 : 0;
+                    if (accept) {
+                        n_acc++;
+                        sum_du += du;
+                        energy += du;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) M[d] = __dadd_rn(M[d], ms.dM[d]);
+                    }
+                    if (!stop) n_mv++;
+                }
             }
+            if (probe && kind != FAU_MOVE_NONE && lane < m) {
+                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+#pragma unroll
+                for (int d = 0; d < 3; d++) pr.xn[lane][d] = ms.xn[lane][d];
+            }
+            // the probe neither decides nor commits: accept stays 0, so the pass's fold of the last
+            // accepted change is the last (q_valid 0) and the loop ends after it
             if constexpr (HOST) {
-                if (lane == 0) { // per-move outputs of host-proposal batches
+                if (lane == 0 && !probe) { // per-move outputs of host-proposal batches
                     if (A.acc_out) A.acc_out[poff + mv] = (uint8_t)accept;
                     if (A.du_out) A.du_out[poff + mv] = du_out;
                 }
@@ -801,15 +790,17 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     }
     if (tid == 32) G.q_since = K ? since_flush : 0;
     auto& red_u = sm.red_u;
-    unsigned long long a = n_pairs, b = n_k;
+    if (!counted) {
+        unsigned long long a = n_pairs, b = n_k;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if (lane == 0) {
-        red_u[warp][0] = a;
-        red_u[warp][1] = b;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0) {
+            red_u[warp][0] = a;
+            red_u[warp][1] = b;
+        }
     }
     __syncthreads();
     if (tid == 0) {
