@@ -58,7 +58,9 @@ cudaError_t launch_fast_audit(DevSys* const* sys, int n, cudaStream_t st)
 // groups, for a single atom every other particle; pair_u64 of FP64 minimum-image distances, the
 // reciprocal change from FP64 phases against Q(k) as the chain holds it; S is pair_mag64 of every
 // pair of both states plus (2 pi lB / V) A_k (|2 Re(Q* d)| + |d|^2) of every k-vector.
-__global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
+constexpr int kProbeAuditThreads = 256; // FP64 chains of dependent instructions: many warps hide them
+
+__global__ void __launch_bounds__(kProbeAuditThreads) probe_audit_kernel(DevSys* const* sys)
 {
     DevSys& G = *sys[blockIdx.x];
     if (!G.audit_pending) return;
@@ -68,7 +70,7 @@ __global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
     const double cmo[3] = {molecular ? G.g_cm[3 * g] : 0.0, molecular ? G.g_cm[3 * g + 1] : 0.0,
                            molecular ? G.g_cm[3 * g + 2] : 0.0};
     double du = 0.0, sc = 0.0;
-    for (int j = threadIdx.x; j < G.n; j += 128) {
+    for (int j = threadIdx.x; j < G.n; j += kProbeAuditThreads) {
         const int gj = G.group_of[j];
         if (molecular ? gj == g : j == b) continue;
         bool cut_o = false, cut_n = false;
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
         }
     }
     const int K = (G.flags & SYS_EWALD) ? G.K : 0;
-    for (int k = threadIdx.x; k < K; k += 128) {
+    for (int k = threadIdx.x; k < K; k += kProbeAuditThreads) {
         int nx, ny, nz;
         kn_unpack(G.kn[k], nx, ny, nz);
         double dx = 0.0, dy = 0.0;
@@ -127,12 +129,12 @@ __global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
         du += __shfl_xor_sync(0xffffffffu, du, o);
         sc += __shfl_xor_sync(0xffffffffu, sc, o);
     }
-    __shared__ double2 red[4];
+    __shared__ double2 red[kProbeAuditThreads / 32];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(du, sc);
     __syncthreads();
     if (threadIdx.x == 0) {
         double d64 = p.du_surf, s64 = 0.0;
-        for (int w = 0; w < 4; w++) {
+        for (int w = 0; w < kProbeAuditThreads / 32; w++) {
             d64 += red[w].x;
             s64 += red[w].y;
         }
@@ -147,7 +149,7 @@ __global__ void __launch_bounds__(128) probe_audit_kernel(DevSys* const* sys)
 cudaError_t launch_probe_audit(DevSys* const* sys, int n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    probe_audit_kernel<<<n, 128, 0, st>>>(sys);
+    probe_audit_kernel<<<n, kProbeAuditThreads, 0, st>>>(sys);
     return cudaGetLastError();
 }
 
