@@ -599,8 +599,8 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
     __syncthreads();
 
     for (long long mv = 0; mv < nloop; mv++) {
-        if (ms.stop || sh_up_at >= 0) break;
-        const bool probe = mv == nmoves;
+        const bool probe = mv == nmoves; // after the last move the audit probe runs, time budget or not
+        if (ms.stop || (sh_up_at >= 0 && !probe)) break;
         const unsigned long long n_pairs0 = n_pairs, n_k0 = n_k; // the probe's evaluations are not counted
         // ---- the previous move's Q(k) change (State::sync trial -> accepted, deferred)
         if (ms.prev_accept) {

@@ -1173,8 +1173,8 @@ __device__ __forceinline__ void fast_chain_body(const ChainArgs& A, FastShared<N
             }
         }
         prev_accept = accept;
-        if (sh_up) { // the time budget is spent: the launch ends after move t
-            t++;
+        if (sh_up && t + 1 < nmoves) { // the time budget is spent: the launch ends after move t (after
+            t++;                        // the last move it still runs the audit probe)
             break;
         }
     }

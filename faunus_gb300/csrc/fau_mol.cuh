@@ -312,7 +312,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
         const float2* tab = tabs + cur * tab_len;
         float2* tab_next = tabs + (cur ^ 1) * tab_len;
         const bool probe = mv == nmoves;
-        if (sh_stop || (ms.stop && !probe) || sh_time_up) { // a NaN energy change ended the chain, a
+        if (sh_stop || (ms.stop && !probe) || (sh_time_up && !probe)) { // a NaN energy change ended the chain, a
             consumed = sh_stop ? sh_consumed : mv;          // proposal was invalid, or the time
             err_code = sh_stop ? sh_stop : ms.stop;         // budget is spent
             break;
