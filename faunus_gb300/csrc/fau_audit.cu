@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kProbeAuditThreads) probe_audit_kernel(DevSys*
 {
     DevSys& G = *sys[blockIdx.x];
     if (!G.audit_pending) return;
-    const MolProbe& p = *reinterpret_cast<const MolProbe*>(G.audit_rec);
+    const ProbeRecord& p = *reinterpret_cast<const ProbeRecord*>(G.audit_rec);
     const bool molecular = p.kind == FAU_MOVE_MOLECULAR;
     const int g = molecular ? p.index : -1, m = p.m, b = p.first;
     const double cmo[3] = {molecular ? G.g_cm[3 * g] : 0.0, molecular ? G.g_cm[3 * g + 1] : 0.0,

@@ -915,7 +915,7 @@ __global__ void __launch_bounds__(NT, 65536 / (NT * 128)) chain_kernel(ChainArgs
                     }
                     flags |= __shfl_xor_sync(0xffffffffu, flags, o);
                 }
-                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                ProbeRecord& pr = *reinterpret_cast<ProbeRecord*>(G.audit_rec);
                 const int mm = kind == FAU_MOVE_NONE ? 0 : m;
                 if (lane < mm) {
 #pragma unroll

@@ -171,16 +171,17 @@ struct DevSys {
     double maxenergy;
     int maxe, pad6;
 };
-constexpr size_t kAuditRecBytes = 1024; // a probe move: the pipelined kernels' FastMove or MolProbe
+constexpr size_t kAuditRecBytes = 1024; // a probe move: the pipelined kernel's FastMove or a ProbeRecord
 
-// the pipelined molecular kernel's probe move: the group it moves, its atoms' trial positions (the
-// old ones are the system's, unchanged by the probe), the new mass centre and the dipole change
-struct MolProbe {
+// the probe move of the molecular kernel or the chain kernel: its kind, the group (molecular) or
+// particle (single atom) it moves, the moved atoms' trial positions (the old ones are the
+// system's, unchanged by the probe), the new mass centre and the dipole change
+struct ProbeRecord {
     int kind, index, m, first;
     double cm_new[3], dM[3], du_surf, pad;
     double xn[kMaxGroupAtoms][3];
 };
-static_assert(sizeof(MolProbe) <= kAuditRecBytes, "audit record size");
+static_assert(sizeof(ProbeRecord) <= kAuditRecBytes, "audit record size");
 
 // ---------------------------------------------------------------- fixed point
 __host__ __device__ inline uint32_t to_fixed(double x, double scale)

@@ -661,7 +661,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 }
                 const double fin = ff_value(accp) + (0.0 + du_surf);
                 if (probe) { // the audit probe: recorded for probe_audit_kernel, not decided
-                    MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                    ProbeRecord& pr = *reinterpret_cast<ProbeRecord*>(G.audit_rec);
                     pr.kind = kind;
                     pr.index = ms.index;
                     pr.m = m;
@@ -693,7 +693,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
                 }
             }
             if (probe && kind != FAU_MOVE_NONE && lane < m) {
-                MolProbe& pr = *reinterpret_cast<MolProbe*>(G.audit_rec);
+                ProbeRecord& pr = *reinterpret_cast<ProbeRecord*>(G.audit_rec);
 #pragma unroll
                 for (int d = 0; d < 3; d++) pr.xn[lane][d] = ms.xn[lane][d];
             }
