@@ -249,6 +249,7 @@ static int run_volume_blocks(fau_ctx* ctx, fau_sys* const* systems, int n, const
 extern "C" int fau_run_batch(fau_ctx* ctx, fau_sys* const* systems, int n, const fau_batch_params* P,
                              fau_batch_stats* stats)
 {
+    const NvtxRange nvtx_range("fau_run_batch");
     if (!ctx || !systems || !P || n < 1) return fau_internal_fail(FAU_ERR_ARG, "invalid batch arguments");
     cudaStream_t st;
     int device;
@@ -732,6 +733,7 @@ extern "C" int fau_run_proposals_batch(fau_ctx* ctx, fau_sys* const* systems, in
                                        const int64_t* offsets, uint8_t* acc_out, double* du_out,
                                        fau_batch_stats* stats)
 {
+    const NvtxRange nvtx_range("fau_run_proposals_batch");
     if (!ctx || !systems || !props || !offsets || n < 1)
         return fau_internal_fail(FAU_ERR_ARG, "invalid batch arguments");
     cudaStream_t st;

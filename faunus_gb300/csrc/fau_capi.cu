@@ -505,6 +505,7 @@ static int refresh_energy(fau_sys* s);
 
 int fau_sys_create(fau_ctx* ctx, const fau_sys_desc* d, fau_sys** out)
 {
+    const fau::NvtxRange nvtx_range("fau_sys_create");
     if (!ctx || !out) return fail(FAU_ERR_ARG, "null argument");
     int rc = validate(d);
     if (rc) return rc;
@@ -1263,6 +1264,7 @@ static int refresh_energy(fau_sys* s)
 
 int fau_energy_total(fau_sys* s, fau_energy_terms* out)
 {
+    const fau::NvtxRange nvtx_range("fau_energy_total");
     if (!s || !out) return fail(FAU_ERR_ARG, "null argument");
     CUDA_TRY(cudaSetDevice(s->ctx->device));
     return compute_total(s, out);
@@ -1432,6 +1434,7 @@ static int run_segment(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, d
 // fau_volume_move performs each volume move in order.
 int fau_run_proposals(fau_sys* s, const fau_proposal* p, int n, uint8_t* acc, double* du, fau_run_stats* stats)
 {
+    const fau::NvtxRange nvtx_range("fau_run_proposals");
     if (!s || (!p && n > 0)) return fail(FAU_ERR_ARG, "null argument");
     CUDA_TRY(cudaSetDevice(s->ctx->device));
     int first_vol = -1;
@@ -1714,6 +1717,7 @@ inline void wrap1(double& a, double L, double half, double inv)
 
 int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_trial_result* out)
 {
+    const fau::NvtxRange nvtx_range("fau_volume_move");
     if (!s) return fail(FAU_ERR_ARG, "null system");
     if (!(new_volume > 0.0) || !std::isfinite(new_volume)) return fail(FAU_ERR_ARG, "new volume must be positive");
     if (method < FAU_VOLUME_ISOTROPIC || method > FAU_VOLUME_ISOCHORIC)
@@ -2169,6 +2173,7 @@ int fau_get_kvectors(fau_sys* s, int* n_out, double* k_out, double* ak_out)
 
 int fau_q_rebuild(fau_sys* s, double* drift)
 {
+    const fau::NvtxRange nvtx_range("fau_q_rebuild");
     if (!s) return fail(FAU_ERR_ARG, "null argument");
     if (s->K == 0) {
         if (drift) *drift = 0.0;

@@ -1,10 +1,20 @@
 // fau_kernels.h -- launch interface between the host runtime and the kernels.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/fau_gpu.h"
 
 namespace fau {
+
+// An NVTX range over a host phase (an entry point of the C ABI): named in a profiler's timeline
+// (nsys, ncu's range filter); without one attached, push and pop return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct DevSys;
 
