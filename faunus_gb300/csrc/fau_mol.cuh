@@ -226,7 +226,7 @@ __device__ __forceinline__ void mol_chain_body(const ChainArgs& A, MolShared<NT>
     const long long poff = A.prop_off ? A.prop_off[blockIdx.x] : 0;
     // the audit probe: one more move (the chain's next proposal; a host stream's last one again)
     // evaluated after the last one on the final state, never decided or committed; its FP32
-    // energy change and the move go to the system's audit record for mol_audit_kernel
+    // energy change and the move go to the system's audit record for probe_audit_kernel
     const long long nloop = nmoves + (A.audit && nmoves > 0 && G.audit_rec ? 1 : 0);
     // move idx's proposal: the host's (A.props, checked by prepare_move) or the device RNG's
     auto proposal = [&](long long idx) -> Proposal {

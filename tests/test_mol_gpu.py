@@ -139,7 +139,7 @@ def test_molecular_kernel_host_proposals(ctx):
 
 def test_molecular_kernel_reports_its_error_against_fp64(ctx):
     """Each launch's molecular chains end with a probe move (the next proposal, evaluated on the
-    final state and not decided) that mol_audit_kernel re-evaluates in FP64: the batch and each
+    final state and not decided) that probe_audit_kernel re-evaluates in FP64: the batch and each
     system report its error, within the parity tolerance, and the probe leaves the chains as they
     were (the same chain as one launch without probes)."""
     specs = [configs.spce_water(n_mol=256, L=18.6, seed=40 + i) for i in range(3)]
