@@ -20,7 +20,9 @@ molecular translate/rotate moves.  The server
     set how many moves fit in ``round_cycles``;
   * retires a job when its moves are done and reports, per job, the queueing
     and run time and the error of its FP32 energy changes against FP64 (the
-    kernels' audit probes: a job's last round ends with one), and for the
+    kernels' audit probes: a job's last round ends with one; a probe with an
+    infinite energy change, a hard-sphere overlap, has no finite error and is
+    not counted), and for the
     stream, p50/p99 latency (arrival -> result), the aggregate moves/s and the
     largest of those errors.
 
