@@ -210,3 +210,27 @@ def test_gpu_backend_keeps_progress_when_a_cell_list_fills():
     with pytest.raises(FauError):
         GpuBackend(Ctx(FAU_ERR_ARG)).run_timed([object()], [5], 0.01, seed=1, streams=[1], counters=[0],
                                                 dp=[1.0], dprot=[0.0])
+
+
+def test_report_carries_each_jobs_error_against_fp64():
+    """The backend's audit of a job (its probes' error against FP64) is kept in the job's result,
+    and the stream report gives how many jobs carry one and the largest error; a job whose
+    backend reports no probe (or none at all) counts as unaudited."""
+    srv, be, _ = _server(budget=100, slots=4)
+    audits = {0: {"rel_scaled_max": 2e-7, "rel_du_max": 1e-5, "samples": 3},
+              1: {"rel_scaled_max": 5e-7, "rel_du_max": 4e-5, "samples": 1},
+              2: {"rel_scaled_max": 0.0, "rel_du_max": 0.0, "samples": 0}}
+    plain = be.result
+
+    def result(h, with_positions):
+        r = plain(h, with_positions)
+        if h.spec["id"] in audits:
+            r["du_err"] = audits[h.spec["id"]]
+        return r
+
+    be.result = result
+    jobs = [Job(spec={"bytes": 10, "id": i}, moves=1000, id=i) for i in range(4)]
+    rep = srv.run(jobs)
+    assert rep["jobs_done"] == 4
+    assert rep["jobs_audited"] == 2 and rep["du_err_rel_scaled_max"] == 5e-7
+    assert srv.results[0].du_err["samples"] == 3 and srv.results[3].du_err is None
