@@ -32,13 +32,15 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build faunus_gb300")
 
 
-def _compile(src: Path, obj: Path, extra: list[str]) -> None:
+def _compile(src: Path, obj: Path, extra: list[str], host: list[str] | None = None) -> None:
+    """host: further host-compiler options, for the .cu and the .cpp sources alike."""
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(PKG.parent / "include")]
+    hostx = [a for h in (host or []) for a in ("-Xcompiler", h)]
     if src.suffix == ".cu":
-        cmd = [nvcc, *ARCH, "-lineinfo", *common, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, "-lineinfo", *common, *hostx, *extra, "-c", str(src), "-o", str(obj)]
     else:
-        cmd = [nvcc, "-x", "c++", *common, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, "-x", "c++", *common, *hostx, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -61,6 +63,35 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
+    if verbose:
+        print(f"built {out}")
+    return out
+
+
+def build_sanitized(verbose: bool = False) -> Path:
+    """The library with its host code under AddressSanitizer and UndefinedBehaviorSanitizer, as
+    ``_lib/libfau_gpu_san.so`` beside the product (never loaded by default): the CPU tests run
+    against it with ``FAU_GPU_LIB`` pointing at it and the sanitizer runtimes preloaded, e.g.
+
+        make -C oracle sanitize
+        FAU_GPU_LIB=faunus_gb300/_lib/libfau_gpu_san.so FAU_ORACLE_LIB=oracle/_build/liboracle_san.so \
+        LD_PRELOAD="$(gcc -print-file-name=libasan.so) $(gcc -print-file-name=libubsan.so)" \
+        ASAN_OPTIONS=detect_leaks=0 python -m pytest tests -m "not gpu"
+    """
+    san = ["-fsanitize=address", "-fsanitize=undefined", "-fno-omit-frame-pointer"]
+    objdir = PKG / "_build" / "san"
+    objdir.mkdir(parents=True, exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    srcs = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
+    objs = [objdir / (s.name + ".o") for s in srcs]
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        list(ex.map(lambda so: _compile(so[0], so[1], [], san), zip(srcs, objs)))
+    out = LIBDIR / "libfau_gpu_san.so"
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", str(out), *map(str, objs), *[a for h in san for a in ("-Xcompiler", h)],
+           "-lasan", "-lubsan"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(f"built {out}")
     return out

@@ -6,6 +6,7 @@ path never calls it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -14,7 +15,8 @@ import numpy as np
 from faunus_gb300 import _capi as A
 
 ROOT = Path(__file__).resolve().parent.parent
-LIB = ROOT / "oracle" / "_build" / "liboracle.so"
+# FAU_ORACLE_LIB: another build of the same oracle (e.g. oracle/Makefile's sanitize target)
+LIB = Path(os.environ.get("FAU_ORACLE_LIB", ROOT / "oracle" / "_build" / "liboracle.so"))
 _lib = None
 
 
