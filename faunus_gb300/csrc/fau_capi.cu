@@ -1745,7 +1745,7 @@ int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_t
     // Cuboid::setVolume (src/geometry.cpp:57-90)
     const double* L = s->h.L;
     const double v_old = L[0] * L[1] * L[2];
-    double sc[3], v_target = new_volume;
+    double sc[3];
     switch (method) {
     case FAU_VOLUME_ISOTROPIC: {
         const double a = std::cbrt(new_volume / v_old);
@@ -1762,15 +1762,13 @@ int fau_volume_move(fau_sys* s, double new_volume, int method, double u01, fau_t
         sc[0] = sc[1] = 1.0;
         sc[2] = new_volume / v_old;
         break;
-    default: {
+    default: { // isochoric: the shape changes, the volume stays
         const double a = std::cbrt(new_volume / v_old);
         sc[0] = sc[1] = a;
         sc[2] = 1 / (a * a);
-        v_target = v_old;
         break;
     }
     }
-    (void)v_target;
     double Ln[3], hn[3], in[3];
     for (int k = 0; k < 3; k++) {
         Ln[k] = L[k] * sc[k];
