@@ -18,6 +18,13 @@ advanced by M trial moves in one persistent chain-kernel launch.
           Nonbonded, O(K) Ewald per state, two-state sync) on all host
           threads, one chain per thread, bounded sample per step.
 
+Beside them the line carries each launch's error against FP64 (audit probes),
+the roofline forms, the plain single-system FP64 form, the served stream
+(p50/p99 latency, aggregate moves/s, the jobs' audited errors) and the other
+configurations: the primitive model in FP32C and as FP64 replica chains, the
+bulk system as FP64 replica chains, rigid SPC/E water, and the 256-walker
+parallel-tempering ladder beside its uniform-replica equivalent.
+
 Multi-GPU: replicas only (one process per GPU, each with its own R replicas,
 no collective on the data path); timing is max over ranks.
 """
